@@ -1,0 +1,144 @@
+"""Initial data for the workloads (seeded, synthetic; no dataset is involved).
+
+Every builder returns ``(problem, convar, primvar)`` with ``convar``/``primvar`` shaped
+``(nx, ny, 4)`` over the whole block including ghost cells, cell (i, j) at ``[i, j]`` --
+the reference's ``i * ny + j`` order (Fluid2d arrays, ``include/fluid_mesh.h:125-160``).
+Ghost cells are filled by clamping to the nearest interior cell; every step's boundary
+fill overwrites them before they are read.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .params import Problem2D
+
+
+def prim_to_con(prim: np.ndarray, gamma: float) -> np.ndarray:
+    """(rho, u, v, p) -> (rho, rho u, rho v, rho E), operand order of Primvar_to_convar_2D
+    (src/basic_function.cpp:851-857, Q_densityE :1123-1127)."""
+    rho, u, v, p = prim[..., 0], prim[..., 1], prim[..., 2], prim[..., 3]
+    out = np.empty_like(prim)
+    out[..., 0] = rho
+    out[..., 1] = rho * u
+    out[..., 2] = rho * v
+    out[..., 3] = rho * (p / rho / (gamma - 1) + 0.5 * (u * u + v * v))
+    return out
+
+
+def _fill_ghosts(a: np.ndarray, g: int) -> np.ndarray:
+    a[:g] = a[g]
+    a[-g:] = a[-g - 1]
+    a[:, :g] = a[:, g:g + 1]
+    a[:, -g:] = a[:, -g - 1:-g]
+    return a
+
+
+def riemann2d(n: int = 1024, order: int = 7, zones=None, discon=(0.7, 0.7),
+              characteristic: bool = True) -> tuple:
+    """Four-quadrant Riemann problem on [0,1]^2 with outflow boundaries.
+
+    Zone assignment follows IC_for_riemann_2d (src/2Dproblem.cpp:345-385): zone 1 lower-left,
+    zone 2 lower-right, zone 3 upper-right, zone 4 upper-left, tested with the reference's
+    ``i - ghost + 1 < discon / dx`` rule.  Default states are the quadrant states of the
+    reference's PlanarShock driver (src/2Dproblem.cpp:85-90).
+    """
+    if zones is None:
+        zones = ((0.138, 1.206, 1.206, 0.029), (0.5323, 0.0, 1.206, 0.3),
+                 (1.5, 0.0, 0.0, 1.5), (0.5323, 1.206, 0.0, 0.3))
+    pb = Problem2D(nodex=n, nodey=n, order=order, characteristic=characteristic,
+                   c1_euler=0.05, c2_euler=1.0, cfl=0.5, bc=("free",) * 4)
+    g = pb.ghost
+    prim = np.zeros((pb.nx, pb.ny, 4))
+    ii = (np.arange(pb.nx) - g + 1)[:, None].astype(np.float64)
+    jj = (np.arange(pb.ny) - g + 1)[None, :].astype(np.float64)
+    lx = ii < discon[0] / pb.dx
+    ly = jj < discon[1] / pb.dx
+    z = np.asarray(zones, dtype=np.float64)
+    for q, mask in enumerate((lx & ly, ~lx & ly, ~lx & ~ly, lx & ~ly)):
+        prim[mask] = z[q]
+    _fill_ghosts(prim, g)
+    return pb, prim_to_con(prim, pb.gamma), prim
+
+
+def random_riemann2d(n: int, seed: int, order: int = 7) -> tuple:
+    """Seeded random quadrant states: rho in [0.1, 2], p in [0.02, 2], u, v in [-1.5, 1.5]."""
+    rng = np.random.default_rng(seed)
+    zones = []
+    for _ in range(4):
+        zones.append((rng.uniform(0.1, 2.0), rng.uniform(-1.5, 1.5), rng.uniform(-1.5, 1.5),
+                      rng.uniform(0.02, 2.0)))
+    disc = (rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7))
+    return riemann2d(n, order=order, zones=zones, discon=disc)
+
+
+def isentropic_vortex(n: int = 200, order: int = 5, strength: float = 5.0,
+                      center=(5.0, 5.0), length: float = 10.0,
+                      characteristic: bool = True) -> tuple:
+    """Isentropic vortex on the periodic square [0, L]^2 over a unit freestream
+    (rho, u, v, p) = (1, 1, 1, 1); cell averages by 4x4 Gauss-Legendre quadrature.
+    The flow is smooth, so the numerical collision time is zero (c1 = c2 = 0) as in the
+    reference's smooth accuracy drivers (src/2Dproblem.cpp:1376-1377)."""
+    pb = Problem2D(nodex=n, nodey=n, order=order, characteristic=characteristic,
+                   c1_euler=0.0, c2_euler=0.0, cfl=0.5, left=0.0, right=length,
+                   down=0.0, up=length, bc=("periodic",) * 4)
+    gamma = pb.gamma
+    g = pb.ghost
+    xg, wg = np.polynomial.legendre.leggauss(4)
+    cons = np.zeros((pb.nx, pb.ny, 4))
+    xc = pb.left + (np.arange(pb.nx) - g + 0.5) * pb.dx
+    yc = pb.down + (np.arange(pb.ny) - g + 0.5) * pb.dy
+    for a, wa in zip(xg, wg):
+        for b, wb in zip(xg, wg):
+            x = xc[:, None] + 0.5 * pb.dx * a
+            y = yc[None, :] + 0.5 * pb.dy * b
+            dxv = x - center[0]
+            dyv = y - center[1]
+            r2 = dxv * dxv + dyv * dyv
+            e = np.exp(0.5 * (1.0 - r2))
+            du = -strength / (2 * math.pi) * e * dyv
+            dv = strength / (2 * math.pi) * e * dxv
+            t = 1.0 - (gamma - 1.0) * strength ** 2 / (8 * gamma * math.pi ** 2) * e * e
+            rho = t ** (1.0 / (gamma - 1.0))
+            prim = np.stack([rho, 1.0 + du, 1.0 + dv, rho * t], axis=-1)
+            cons += 0.25 * wa * wb * prim_to_con(prim, gamma)
+    from_c = con_to_prim(cons, gamma)
+    return pb, cons, from_c
+
+
+def sinwave2d(n: int = 20, order: int = 9, characteristic: bool = False) -> tuple:
+    """Density sine wave advected diagonally on the periodic square [0, 2]^2 (the reference's
+    2D accuracy test, ICfor_sinwave_2d, src/2Dproblem.cpp:1527-1564): exact cell averages of
+    rho = 1 + 0.2 sin(pi (x + y)), u = v = p = 1."""
+    pb = Problem2D(nodex=n, nodey=n, order=order, characteristic=characteristic,
+                   c1_euler=0.0, c2_euler=0.0, cfl=0.05, left=0.0, right=2.0, down=0.0,
+                   up=2.0, bc=("periodic",) * 4)
+    g = pb.ghost
+    pi = 3.14159265358979323846
+    prim = np.zeros((pb.nx, pb.ny, 4))
+    i = np.arange(pb.nx)[:, None]
+    j = np.arange(pb.ny)[None, :]
+    xl = (i - g) * pb.dx
+    xr = (i + 1 - g) * pb.dx
+    yl = (j - g) * pb.dy
+    yr = (j + 1 - g) * pb.dy
+    k1 = np.sin(pi * (xr + yr))
+    k2 = np.sin(pi * (xr + yl))
+    k3 = np.sin(pi * (xl + yr))
+    k4 = np.sin(pi * (xl + yl))
+    prim[..., 0] = 1.0 - 0.2 / pi / pi / pb.dx / pb.dy * ((k1 - k2) - (k3 - k4))
+    prim[..., 1:] = 1.0
+    return pb, prim_to_con(prim, pb.gamma), prim
+
+
+def con_to_prim(con: np.ndarray, gamma: float) -> np.ndarray:
+    """Convar_to_primvar_2D (src/basic_function.cpp:811-817, Pressure :1156-1159)."""
+    rho = con[..., 0]
+    out = np.empty_like(con)
+    out[..., 0] = rho
+    out[..., 1] = con[..., 1] / rho
+    out[..., 2] = con[..., 2] / rho
+    out[..., 3] = (gamma - 1.0) * (con[..., 3] - 0.5 * con[..., 1] * con[..., 1] / rho
+                                   - 0.5 * con[..., 2] * con[..., 2] / rho)
+    return out

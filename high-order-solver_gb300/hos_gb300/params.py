@@ -1,0 +1,90 @@
+"""Problem parameters shared by every implementation of the 2D step.
+
+``Params2D`` is the ctypes mirror of the C struct ``hos_params2d`` declared in
+``include/hos_gb300.h``.  Its fields are the knobs the reference sets as globals inside
+each problem driver (``src/2Dproblem.cpp:3-60`` in the reference project): mesh size and
+ghost layers (Block2d), reconstruction order and variables (cellreconstruction_2D_*,
+reconstruction_variable), Gauss points (gausspoint), gas constants (K, Gamma), the
+numerical collision-time coefficients (c1_euler, c2_euler), the CFL number and the four
+boundary functions.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+BC_FREE, BC_PERIODIC, BC_REFLECT, BC_INFLOW = 0, 1, 2, 3
+_BC_NAMES = {"free": BC_FREE, "outflow": BC_FREE, "periodic": BC_PERIODIC,
+             "reflect": BC_REFLECT, "reflective": BC_REFLECT, "inflow": BC_INFLOW}
+
+# Gauss points per face the reference pairs with each WENO-AO order
+# (weno_5th/7th/9th_ao_with_df_2gauss write 2, 3 and 4 points; src/reconstruction.cpp:2700,3093,3489)
+GAUSS_POINTS = {5: 2, 7: 3, 9: 4}
+
+
+class Params2D(ctypes.Structure):
+    _fields_ = [
+        ("nodex", ctypes.c_int), ("nodey", ctypes.c_int), ("ghost", ctypes.c_int),
+        ("order", ctypes.c_int), ("gausspoint", ctypes.c_int),
+        ("characteristic", ctypes.c_int), ("use_df", ctypes.c_int), ("K", ctypes.c_int),
+        ("gamma", ctypes.c_double), ("c1_euler", ctypes.c_double), ("c2_euler", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("left", ctypes.c_double), ("right", ctypes.c_double),
+        ("down", ctypes.c_double), ("up", ctypes.c_double),
+        ("bc", ctypes.c_int * 4), ("bc_prim", (ctypes.c_double * 4) * 4),
+    ]
+
+
+@dataclass
+class Problem2D:
+    """A 2D problem: mesh, scheme and boundary choices (one reference problem driver)."""
+
+    nodex: int
+    nodey: int
+    order: int = 5
+    characteristic: bool = True
+    ghost: int = 5
+    K: int = 3
+    gamma: float = 1.4
+    c1_euler: float = 0.05
+    c2_euler: float = 1.0
+    cfl: float = 0.5
+    left: float = 0.0
+    right: float = 1.0
+    down: float = 0.0
+    up: float = 1.0
+    bc: tuple = ("free", "free", "free", "free")
+    bc_prim: tuple = field(default_factory=lambda: ((0.0,) * 4,) * 4)
+
+    @property
+    def nx(self) -> int:
+        return self.nodex + 2 * self.ghost
+
+    @property
+    def ny(self) -> int:
+        return self.nodey + 2 * self.ghost
+
+    @property
+    def dx(self) -> float:
+        return (self.right - self.left) / self.nodex
+
+    @property
+    def dy(self) -> float:
+        return (self.up - self.down) / self.nodey
+
+    def to_c(self) -> Params2D:
+        p = Params2D()
+        p.nodex, p.nodey, p.ghost = self.nodex, self.nodey, self.ghost
+        p.order = self.order
+        p.gausspoint = GAUSS_POINTS[self.order]
+        p.characteristic = 1 if self.characteristic else 0
+        p.use_df = 1
+        p.K = self.K
+        p.gamma, p.c1_euler, p.c2_euler, p.cfl = self.gamma, self.c1_euler, self.c2_euler, self.cfl
+        p.left, p.right, p.down, p.up = self.left, self.right, self.down, self.up
+        for s in range(4):
+            b = self.bc[s]
+            p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
+            for v in range(4):
+                p.bc_prim[s][v] = float(self.bc_prim[s][v])
+        return p

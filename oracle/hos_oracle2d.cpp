@@ -1,0 +1,1145 @@
+// hos_oracle2d.cpp -- CPU FP64 restatement of the reference's 2D per-step hot path.
+//
+// TEST INFRASTRUCTURE ONLY: this is the checker for the CUDA path.  Only tests/, the smoke
+// check of __graft_entry__.py and the cpu_baseline leg of bench.py load it.  The product
+// (hos_gb300 package and its CUDA library) never includes, links or calls it.
+//
+// What it restates (file:line in the reference project XJTUZhangHong/high-order-solver):
+//   step driver ............ src/2Dproblem.cpp:128-157 (PlanarShock time loop)
+//   CopyFluid_new_to_old ... src/basic_function.cpp:1571-1584
+//   Get_CFL / Dtx .......... src/time_advance.cpp:264-305
+//   boundary conditions .... src/boundary_condition.cpp:66-186, 244-258, 367-442
+//   Convar_to_Primvar ...... src/basic_function.cpp:752-773 (blow-up -> status 1, no exit)
+//   normal recon (DF) ...... src/reconstruction.cpp:1701-1859 (WENO5), 1861-2028 (WENO7),
+//                            2030-2211 (WENO9); scalar kernels :480-657, :750-974, :1072-1364
+//   tangential recon (DF) .. src/reconstruction.cpp:2553-2838 (WENO5, 2 pts),
+//                            2840-3174 (WENO7, 3 pts), 3176-3609 (WENO9, 4 pts + Polynomial_9th)
+//   positivity fallback .... src/reconstruction.cpp:1439-1449
+//   g0 centre state ........ src/reconstruction.cpp:3652-3687 (computed once, inside the flux,
+//                            as GKS2D recomputes it anyway: src/flux_function.cpp:369-401)
+//   GKS2D flux ............. src/flux_function.cpp:317-343, 345-698
+//   Maxwellian moments ..... src/basic_function.cpp:110-187 (MMDF2d), 561-636 (Collision, A,
+//                            GL/GR/G_address), 638-719 (Get_Tau*, Alpha, Beta)
+//   characteristic vars .... src/basic_function.cpp:923-992
+//   S2O4 update ............ src/time_advance.cpp:221-230, 307-474
+//   DF factor .............. src/reconstruction.cpp:1451-1534
+//
+// Arithmetic follows the reference expression by expression (same operand order, x*x for
+// pow(x, 2), integer divisions 13/3 == 4 and 781/20 == 39 kept) so that, compiled with
+// -ffp-contract=off, it reproduces the reference bit for bit.  Deliberate differences:
+//   * Update_alpha's j loop bound uses nodex (src/reconstruction.cpp:1528); this restatement
+//     bounds j by min(nodex, nodey), identical on the square grids the workloads use.
+//   * No console output, no exit(): errors come back as status codes.
+#include "oracle_api.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <omp.h>
+
+namespace {
+
+// ----------------------------------------------------------------------------------------
+// configuration and state
+// ----------------------------------------------------------------------------------------
+struct Config {
+    hos2d_params p;
+    int nx = 0, ny = 0, g = 0, gp = 0;
+    double dx = 0, dy = 0;
+    double gloc[4] = {0, 0, 0, 0};
+    double gw[4] = {0, 0, 0, 0};
+    double K = 0, Gamma = 0;
+};
+Config C;
+
+struct Point { double convar[4], der1x[4], der1y[4]; };
+struct Recon { Point left, right, center; };
+
+std::vector<double> W, Wold, Prim, AX, AY;   // per cell: 4, 4, 4, 1, 1
+std::vector<Point> XL, YL;                    // line states: [face][side] (side 0 left, 1 right)
+std::vector<Recon> XG, YG;                    // Gauss states: [face][gp]
+std::vector<double> XF, YF;                   // flux: [face][stage][gp][8] (f[4], derf[4])
+std::vector<double> XX, YX;                   // stage flux combination x[4]: [face][gp][4]
+
+inline int cell(int i, int j) { return i * C.ny + j; }
+inline int face(int i, int j) { return i * (C.ny + 1) + j; }
+
+// S2O4 coefficients (src/time_advance.cpp:221-230): tc[stage][k][f or derf]
+const double TC[2][2][2] = {{{0.5, 1.0 / 8.0}, {0.0, 0.0}}, {{1.0, 1.0 / 6.0}, {0.0, 1.0 / 3.0}}};
+
+// ----------------------------------------------------------------------------------------
+// conversions (src/basic_function.cpp:811-842, 1102-1177)
+// ----------------------------------------------------------------------------------------
+inline void to_prim(double* pr, const double* w) {
+    pr[0] = w[0];
+    pr[1] = w[1] / w[0];
+    pr[2] = w[2] / w[0];
+    pr[3] = (C.Gamma - 1.0) * (w[3] - 0.5 * w[1] * w[1] / w[0] - 0.5 * w[2] * w[2] / w[0]);
+}
+inline double lambda_of(double rho, double u, double v, double rhoE) {
+    return (C.K + 2.0) * 0.25 * (rho / (rhoE - 0.5 * rho * (u * u + v * v)));
+}
+inline void to_ulambda(double* pr, const double* w) {
+    pr[0] = w[0];
+    pr[1] = w[1] / w[0];
+    pr[2] = w[2] / w[0];
+    pr[3] = lambda_of(w[0], pr[1], pr[2], w[3]);
+}
+inline void prim_to_con(double* w, const double* pr) {
+    w[0] = pr[0];
+    w[1] = pr[0] * pr[1];
+    w[2] = pr[0] * pr[2];
+    w[3] = pr[0] * (pr[3] / pr[0] / (C.Gamma - 1) + 0.5 * (pr[1] * pr[1] + pr[2] * pr[2]));
+}
+// (u, v) -> (v, -u): y-face quantities in the x-face frame (YchangetoX, :1192-1198)
+inline void rot_y_to_x(double* o, const double* w) { o[0] = w[0]; o[1] = w[2]; o[2] = -w[1]; o[3] = w[3]; }
+// inverse rotation (XchangetoY, :1200-1206)
+inline void rot_x_to_y(double* o, const double* w) { o[0] = w[0]; o[1] = -w[2]; o[2] = w[1]; o[3] = w[3]; }
+
+// characteristic projection with base primitive state (Convar_to_char, :960-992)
+inline void to_char(double* ch, const double* base, const double* w) {
+    double c = std::sqrt(C.Gamma * base[3] / base[0]);
+    double overc = 1.0 / c;
+    double alfa = (C.Gamma - 1.0) * 0.5 * overc * overc;
+    double u = base[1], v = base[2];
+    double s[4][4];
+    s[0][0] = 1.0 - alfa * (u * u + v * v); s[0][1] = 2.0 * alfa * u; s[0][2] = 2.0 * alfa * v; s[0][3] = -2.0 * alfa;
+    s[1][0] = -v; s[1][1] = 0.; s[1][2] = 1.; s[1][3] = 0.;
+    s[2][0] = 0.5 * (-u * overc + alfa * (u * u + v * v)); s[2][1] = 0.5 * overc - alfa * u; s[2][2] = -alfa * v; s[2][3] = alfa;
+    s[3][0] = 0.5 * (u * overc + alfa * (u * u + v * v)); s[3][1] = -0.5 * overc - alfa * u; s[3][2] = -alfa * v; s[3][3] = alfa;
+    for (int r = 0; r < 4; ++r) {
+        double acc = 0;
+        for (int k = 0; k < 4; ++k) acc = acc + s[r][k] * w[k];
+        ch[r] = acc;
+    }
+}
+// back-projection (Char_to_convar, :958-992 region, right eigenvectors)
+inline void from_char(double* w, const double* base, const double* ch) {
+    double c = std::sqrt(C.Gamma * base[3] / base[0]);
+    double u = base[1], v = base[2];
+    double s[4][4];
+    s[0][0] = 1.; s[0][1] = 0.0; s[0][2] = 1.0; s[0][3] = 1.0;
+    s[1][0] = u; s[1][1] = 0.; s[1][2] = u + c; s[1][3] = u - c;
+    s[2][0] = v; s[2][1] = 1.; s[2][2] = v; s[2][3] = v;
+    s[3][0] = 0.5 * (u * u + v * v); s[3][1] = v;
+    s[3][2] = 0.5 * (u * u + v * v) + c * u + c * c / (C.Gamma - 1.0);
+    s[3][3] = 0.5 * (u * u + v * v) - c * u + c * c / (C.Gamma - 1.0);
+    for (int r = 0; r < 4; ++r) {
+        double acc = 0;
+        for (int k = 0; k < 4; ++k) acc = acc + s[r][k] * ch[k];
+        w[r] = acc;
+    }
+}
+// positivity check of a reconstructed state (Check_Order_Reduce_by_Lambda_2D, :1439-1449)
+inline bool needs_order_reduction(const double* w) {
+    double lam = lambda_of(w[0], w[1] / w[0], w[2] / w[0], w[3]);
+    return lam <= 0.0 || !(lam == lam);
+}
+
+// ----------------------------------------------------------------------------------------
+// WENO-AO-DF weights.  The linear weights d, smoothness indicators and the Z-type
+// nonlinear weights are the published WENO-AO(5,3)/(7,5,3)/(9,7,5,3) construction as the
+// reference writes it (e.g. src/reconstruction.cpp:489-521, 763-830, 1087-1187).
+// s[] holds the stencil with s[r] the centre cell, r = 2, 3, 4.
+// ----------------------------------------------------------------------------------------
+inline double sq(double x) { return x * x; }
+
+inline void beta3(const double* s, int r, double* b) {
+    const double wn2 = s[r - 2], wn1 = s[r - 1], w0 = s[r], wp1 = s[r + 1], wp2 = s[r + 2];
+    b[0] = 13.0 / 12.0 * sq(wn2 - 2.0 * wn1 + w0) + 0.25 * sq(wn2 - 4.0 * wn1 + 3.0 * w0);
+    b[1] = 13.0 / 12.0 * sq(wn1 - 2.0 * w0 + wp1) + 0.25 * sq(wn1 - wp1);
+    b[2] = 13.0 / 12.0 * sq(w0 - 2.0 * wp1 + wp2) + 0.25 * sq(3.0 * w0 - 4.0 * wp1 + wp2);
+}
+// 7th-order indicator built from four cubic sub-stencils (:778-806); 13/3 and 781/20 are
+// integer divisions in the reference (4 and 39) and are kept as such.
+inline double beta7(const double* s, int r) {
+    const double wn3 = s[r - 3], wn2 = s[r - 2], wn1 = s[r - 1], w0 = s[r];
+    const double wp1 = s[r + 1], wp2 = s[r + 2], wp3 = s[r + 3];
+    double a1, a2, a3, b4[4];
+    a1 = (-19 * wn3 + 87 * wn2 - 177 * wn1 + 109 * w0) / 60.0;
+    a2 = (-wn3 + 4 * wn2 - 5 * wn1 + 2 * w0) / 2;
+    a3 = (-wn3 + 3 * wn2 - 3 * wn1 + w0) / 6.0;
+    b4[0] = (a1 + a3 / 10.0) * (a1 + a3 / 10.0) + 13 / 3 * a2 * a2 + 781 / 20 * a3 * a3;
+    a1 = (11 * wn2 - 63 * wn1 + 33 * w0 + 19 * wp1) / 60.0;
+    a2 = (wn1 - 2 * w0 + wp1) / 2;
+    a3 = (-wn2 + 3 * wn1 - 3 * w0 + wp1) / 6.0;
+    b4[1] = (a1 + a3 / 10.0) * (a1 + a3 / 10.0) + 13 / 3 * a2 * a2 + 781 / 20 * a3 * a3;
+    a1 = (-19 * wn1 - 33 * w0 + 63 * wp1 - 11 * wp2) / 60.0;
+    a2 = (wn1 - 2 * w0 + wp1) / 2;
+    a3 = (-wn1 + 3 * w0 - 3 * wp1 + wp2) / 6.0;
+    b4[2] = (a1 + a3 / 10.0) * (a1 + a3 / 10.0) + 13 / 3 * a2 * a2 + 781 / 20 * a3 * a3;
+    a1 = (-109 * w0 + 177 * wp1 - 87 * wp2 + 19 * wp3) / 60.0;
+    a2 = (2 * w0 - 5 * wp1 + 4 * wp2 - wp3) / 2;
+    a3 = (-w0 + 3 * wp1 - 3 * wp2 + wp3) / 6.0;
+    b4[3] = (a1 + a3 / 10.0) * (a1 + a3 / 10.0) + 13 / 3 * a2 * a2 + 781 / 20 * a3 * a3;
+    return 1.0 / 20.0 * (b4[0] + 9.0 * b4[1] + 9.0 * b4[2] + b4[3]) + std::abs(b4[0] - b4[1] - b4[2] + b4[3]);
+}
+// 9th-order indicator from five quartic sub-stencils (:1130-1169); returns beta5[2] (the
+// 5th-order indicator of this family) through b5mid.
+inline double beta9(const double* s, double* b5mid) {
+    const double wn4 = s[0], wn3 = s[1], wn2 = s[2], wn1 = s[3], w0 = s[4];
+    const double wp1 = s[5], wp2 = s[6], wp3 = s[7], wp4 = s[8];
+    double a1, a2, a3, a4, b5[5];
+    auto comb = [&]() {
+        return (a1 + a3 / 10.0) * (a1 + a3 / 10.0) + 13.0 / 3.0 * (a2 + 123.0 / 455.0 * a4) * (a2 + 123.0 / 455.0 * a4)
+               + 781.0 / 20.0 * a3 * a3 + 1421461.0 / 2275.0 * a4 * a4;
+    };
+    a1 = (-462 * wn1 + 336 * wn2 - 146 * wn3 + 27 * wn4 + 245 * w0) / 120.0;
+    a2 = (-240 * wn1 + 262 * wn2 - 128 * wn3 + 25 * wn4 + 81 * w0) / 56.0;
+    a3 = (-18 * wn1 + 24 * wn2 - 14 * wn3 + 3 * wn4 + 5 * w0) / 12.0;
+    a4 = (-4 * wn1 + 6 * wn2 - 4 * wn3 + wn4 + w0) / 24.0;
+    b5[0] = comb();
+    a1 = (-192 * wn1 + 66 * wn2 - 11 * wn3 + 110 * w0 + 27 * wp1) / 120;
+    a2 = (10 * wn1 + 12 * wn2 - 3 * wn3 - 44 * w0 + 25 * wp1) / 56;
+    a3 = (12 * wn1 - 6 * wn2 + wn3 - 10 * w0 + 3 * wp1) / 12;
+    a4 = (6 * wn1 - 4 * wn2 + wn3 - 4 * w0 + wp1) / 24;
+    b5[1] = comb();
+    a1 = (-82 * wn1 + 11 * wn2 + 82 * wp1 - 11 * wp2) / 120;
+    a2 = (40 * wn1 - 3 * wn2 - 74 * w0 + 40 * wp1 - 3 * wp2) / 56;
+    a3 = (2 * wn1 - wn2 - 2 * wp1 + wp2) / 12;
+    a4 = (-4 * wn1 + wn2 + 6 * w0 - 4 * wp1 + wp2) / 24;
+    b5[2] = comb();
+    a1 = (-27 * wn1 - 110 * w0 + 192 * wp1 - 66 * wp2 + 11 * wp3) / 120;
+    a2 = (25 * wn1 - 44 * w0 + 10 * wp1 + 12 * wp2 - 3 * wp3) / 56;
+    a3 = (-3 * wn1 + 10 * w0 - 12 * wp1 + 6 * wp2 - wp3) / 12;
+    a4 = (wn1 - 4 * w0 + 6 * wp1 - 4 * wp2 + wp3) / 24;
+    b5[3] = comb();
+    a1 = (-245 * w0 + 462 * wp1 - 336 * wp2 + 146 * wp3 - 27 * wp4) / 120;
+    a2 = (81 * w0 - 240 * wp1 + 262 * wp2 - 128 * wp3 + 25 * wp4) / 56;
+    a3 = (-5 * w0 + 18 * wp1 - 24 * wp2 + 14 * wp3 - 3 * wp4) / 12;
+    a4 = (w0 - 4 * wp1 + 6 * wp2 - 4 * wp3 + wp4) / 24;
+    b5[4] = comb();
+    *b5mid = b5[2];
+    return 1.0 / 70.0 * (b5[0] + 16.0 * b5[1] + 36.0 * b5[2] + 16.0 * b5[3] + b5[4]) + std::abs(b5[0] - b5[1] - b5[3] + b5[4]);
+}
+
+// Final AO weights fw[0..n-1] for order 5/7/9 (n = 4/5/6) on stencil s (DF variants,
+// epsilon 1e-6).  Returns n.
+int ao_weights(int order, const double* s, double* fw) {
+    const double dhi = 0.85, dlo = 0.85, davg = 0.85, davg1 = 0.85, davg2 = 0.85;
+    const double eps = 1e-6;
+    double beta[6], d[6];
+    int n;
+    if (order == 5) {
+        n = 4;
+        d[0] = (1.0 - dhi) * (1.0 - dlo) / 2.0;
+        d[1] = (1.0 - dhi) * dlo;
+        d[2] = (1.0 - dhi) * (1.0 - dlo) / 2.0;
+        d[3] = dhi;
+        beta3(s, 2, beta);
+        beta[3] = 1.0 / 6.0 * (beta[0] + 4.0 * beta[1] + beta[2]) + std::abs(beta[0] - beta[2]);
+    } else if (order == 7) {
+        n = 5;
+        d[0] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - davg) / 2.0;
+        d[1] = (1.0 - dhi) * (1.0 - davg) * dlo;
+        d[2] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - davg) / 2.0;
+        d[3] = (1.0 - dhi) * davg;
+        d[4] = dhi;
+        beta3(s, 3, beta);
+        beta[3] = 1.0 / 6.0 * (beta[0] + 4.0 * beta[1] + beta[2]) + std::abs(beta[0] - beta[2]);
+        beta[4] = beta7(s, 3);
+    } else {
+        n = 6;
+        d[0] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - davg1) * (1.0 - davg2) / 2.0;
+        d[1] = (1.0 - dhi) * (1.0 - davg1) * (1.0 - davg2) * dlo;
+        d[2] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - davg1) * (1.0 - davg2) / 2.0;
+        d[3] = (1.0 - dhi) * (1.0 - davg2) * davg1;
+        d[4] = (1.0 - dhi) * davg2;
+        d[5] = dhi;
+        beta3(s, 4, beta);
+        beta[4] = beta7(s, 4);
+        double b5mid;
+        beta[5] = beta9(s, &b5mid);
+        beta[3] = b5mid;
+    }
+    const int top = n - 1;
+    double tau;
+    if (n == 4)
+        tau = 1.0 / 3.0 * (std::abs(beta[3] - beta[0]) + std::abs(beta[3] - beta[1]) + std::abs(beta[3] - beta[2]));
+    else if (n == 5)
+        tau = 0.25 * (std::abs(beta[4] - beta[0]) + std::abs(beta[4] - beta[1]) + std::abs(beta[4] - beta[2]) + std::abs(beta[4] - beta[3]));
+    else
+        tau = 0.2 * (std::abs(beta[5] - beta[0]) + std::abs(beta[5] - beta[1]) + std::abs(beta[5] - beta[2]) + std::abs(beta[5] - beta[3]) + std::abs(beta[5] - beta[4]));
+    double alpha[6], ww[6], sum = 0.0;
+    for (int k = 0; k < n; ++k) {
+        double gd = tau / (beta[k] + eps);
+        alpha[k] = d[k] * (1.0 + gd * gd);
+        sum += alpha[k];
+    }
+    for (int k = 0; k < n; ++k) ww[k] = alpha[k] / sum;
+    fw[top] = ww[top] / d[top];
+    for (int k = 0; k < top; ++k) fw[k] = ww[k] - ww[top] / d[top] * d[k];
+    return n;
+}
+
+// DF factors from the alpha values along the stencil (e.g. :1731-1741, :1898-1909, :2074-2087)
+int df_factors(int order, const double* a, double* df) {
+    double s[6];
+    int n;
+    if (order == 5) {
+        n = 4;
+        s[0] = a[0] + a[2]; s[1] = a[1] + a[3]; s[2] = a[2] + a[4]; s[3] = a[0] + a[2] + a[4];
+    } else if (order == 7) {
+        n = 5;
+        s[0] = a[1] + a[3]; s[1] = a[2] + a[4]; s[2] = a[3] + a[5]; s[3] = a[1] + a[3] + a[5];
+        s[4] = a[0] + a[2] + a[4] + a[6];
+    } else {
+        n = 6;
+        s[0] = a[2] + a[4]; s[1] = a[3] + a[5]; s[2] = a[4] + a[6]; s[3] = a[2] + a[4] + a[6];
+        s[4] = a[1] + a[3] + a[5] + a[7]; s[5] = a[0] + a[2] + a[4] + a[6] + a[8];
+    }
+    for (int k = 0; k < n; ++k) df[k] = s[k] < 2.0 ? 1.0 : 2.0 / s[k];
+    return n;
+}
+
+// ----------------------------------------------------------------------------------------
+// normal (cell-face) candidate polynomials: value and first derivative at the left face
+// (x = -1/2 cell) or right face of the centre cell, scaled by the DF factor.
+// Left face: :526-536 / :835-847 / :1196-1210; right face: :612-622 / :936-948 / :1341-1355.
+// ----------------------------------------------------------------------------------------
+void normal_face(int order, int side, const double* s, const double* df, double h, double* p, double* px) {
+    const int r = order / 2;
+    const double w0 = s[r];
+    const double wn1 = s[r - 1], wn2 = s[r - 2], wp1 = s[r + 1], wp2 = s[r + 2];
+    const double wn3 = r >= 3 ? s[r - 3] : 0, wp3 = r >= 3 ? s[r + 3] : 0;
+    const double wn4 = r >= 4 ? s[r - 4] : 0, wp4 = r >= 4 ? s[r + 4] : 0;
+    if (side == 0) {
+        p[0] = w0 + df[0] * (-1.0 / 6.0 * wn2 + 5.0 / 6.0 * wn1 + 1.0 / 3.0 * w0 - w0);
+        p[1] = w0 + df[1] * (1.0 / 3.0 * wn1 + 5.0 / 6.0 * w0 - 1.0 / 6.0 * wp1 - w0);
+        p[2] = w0 + df[2] * (11.0 / 6.0 * w0 - 7.0 / 6.0 * wp1 + 1.0 / 3.0 * wp2 - w0);
+        p[3] = w0 + df[3] * ((1.0 / 60.0) * (47.0 * w0 + 27.0 * wn1 - 3.0 * wn2 - 13.0 * wp1 + 2.0 * wp2) - w0);
+        px[0] = df[0] * (w0 - wn1) / h;
+        px[1] = df[1] * (w0 - wn1) / h;
+        px[2] = -df[2] * ((2.0 * w0 - 3.0 * wp1 + wp2) / h);
+        px[3] = df[3] * (15.0 * w0 - 15.0 * wn1 + wn2 - wp1) / (12.0 * h);
+        if (order >= 7) {
+            p[4] = w0 + df[4] * ((order == 7 ? 1.0 / 420.0 : (1.0 / 420.0)) * (319.0 * w0 + 214.0 * wn1 - 38.0 * wn2 + 4.0 * wn3 - 101.0 * wp1 + 25.0 * wp2 - 3.0 * wp3) - w0);
+            px[4] = df[4] * (245.0 * w0 - 245.0 * wn1 + 25.0 * wn2 - 2.0 * wn3 - 25.0 * wp1 + 2.0 * wp2) / (180.0 * h);
+        }
+        if (order == 9) {
+            p[5] = w0 + df[5] * ((1.0 / 2520.0) * (1879.0 * w0 + 1375.0 * wn1 - 305.0 * wn2 + 55.0 * wn3 - 5.0 * wn4 - 641.0 * wp1 + 199.0 * wp2 - 41.0 * wp3 + 4.0 * wp4) - w0);
+            px[5] = df[5] * (7175.0 * w0 - 7175.0 * wn1 + 889.0 * wn2 - 119.0 * wn3 + 9.0 * wn4 - 889.0 * wp1 + 119.0 * wp2 - 9.0 * wp3) / (5040.0 * h);
+        }
+    } else {
+        p[0] = w0 + df[0] * (1.0 / 3.0 * wn2 - 7.0 / 6.0 * wn1 + 11.0 / 6.0 * w0 - w0);
+        p[1] = w0 + df[1] * (-1.0 / 6.0 * wn1 + 5.0 / 6.0 * w0 + 1.0 / 3.0 * wp1 - w0);
+        p[2] = w0 + df[2] * (1.0 / 3.0 * w0 + 5.0 / 6.0 * wp1 - 1.0 / 6.0 * wp2 - w0);
+        p[3] = w0 + df[3] * ((1.0 / 60.0) * (47.0 * w0 - 13.0 * wn1 + 2.0 * wn2 + 27.0 * wp1 - 3.0 * wp2) - w0);
+        px[0] = df[0] * (2.0 * w0 - 3.0 * wn1 + wn2) / h;
+        px[1] = df[1] * (-w0 + wp1) / h;
+        px[2] = df[2] * (-w0 + wp1) / h;
+        px[3] = df[3] * (-15.0 * w0 + wn1 + 15.0 * wp1 - wp2) / (12.0 * h);
+        if (order >= 7) {
+            p[4] = w0 + df[4] * (1.0 / 420.0 * (319.0 * w0 - 101.0 * wn1 + 25.0 * wn2 - 3.0 * wn3 + 214.0 * wp1 - 38.0 * wp2 + 4.0 * wp3) - w0);
+            px[4] = df[4] * (-245.0 * w0 + 25.0 * wn1 - 2.0 * wn2 + 245.0 * wp1 - 25.0 * wp2 + 2.0 * wp3) / (180.0 * h);
+        }
+        if (order == 9) {
+            p[5] = w0 + df[5] * ((1.0 / 2520) * (1879.0 * w0 - 641.0 * wn1 + 199.0 * wn2 - 41.0 * wn3 + 4.0 * wn4 + 1375.0 * wp1 - 305.0 * wp2 + 55.0 * wp3 - 5.0 * wp4) - w0);
+            px[5] = df[5] * (-7175.0 * w0 + 889.0 * wn1 - 119.0 * wn2 + 9.0 * wn3 + 7175.0 * wp1 - 889.0 * wp2 + 119.0 * wp3 - 9.0 * wp4) / (5040.0 * h);
+        }
+    }
+}
+
+// scalar normal reconstruction: value and slope at one face of the centre cell
+void weno_normal(int order, int side, const double* s, const double* df, double h, double& var, double& der) {
+    double fw[6], p[6], px[6];
+    int n = ao_weights(order, s, fw);
+    normal_face(order, side, s, df, h, p, px);
+    var = 0.0;
+    der = 0.0;
+    for (int k = 0; k < n; ++k) {
+        var += fw[k] * p[k];
+        der += fw[k] * px[k];
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// tangential candidate polynomials at the Gauss points of a face
+//   WENO5, 2 Gauss-Legendre points (:2793-2836), WENO7, 3 Gauss-Legendre points (:3093-3173),
+//   WENO9, 4 Gauss-Lobatto points via the 9th-order polynomial family (:3489-3609)
+// ----------------------------------------------------------------------------------------
+void tangent_points(int order, int ig, const double* s, const double* df, double h, double* p, double* px) {
+    if (order == 5) {
+        const double wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+        const double sqrt3 = 1.732050807568877294;
+        if (ig == 0) {
+            p[0] = w0 + df[0] * (w0 - (sqrt3 * w0) / 4 + (4 * wn1 - wn2) / (4 * sqrt3) - w0);
+            p[1] = w0 + df[1] * (w0 + (wn1 - wp1) / (4 * sqrt3) - w0);
+            p[2] = w0 + df[2] * ((1.0 / 12.0) * (3 * (4 + sqrt3) * w0 + sqrt3 * (-4 * wp1 + wp2)) - w0);
+            p[3] = w0 + df[3] * ((4314 * w0 + (4 + 500 * sqrt3) * wn1 - wn2 - 70 * sqrt3 * wn2 + 4 * wp1 - 500 * sqrt3 * wp1 - wp2 + 70 * sqrt3 * wp2) / 4320 - w0);
+            px[0] = -df[0] * ((-9 + sqrt3) * w0 - 2 * (-6 + sqrt3) * wn1 + (-3 + sqrt3) * wn2) / (6 * h);
+            px[1] = -df[1] * (-2 * sqrt3 * w0 + (3 + sqrt3) * wn1 + (-3 + sqrt3) * wp1) / (6 * h);
+            px[2] = -df[2] * ((9 + sqrt3) * w0 - 2 * (6 + sqrt3) * wp1 + (3 + sqrt3) * wp2) / (6 * h);
+            px[3] = df[3] * (48 * sqrt3 * w0 - 72 * wn1 - 26 * sqrt3 * wn1 + 9 * wn2 + 2 * sqrt3 * wn2 + 72 * wp1 - 26 * sqrt3 * wp1 - 9 * wp2 + 2 * sqrt3 * wp2) / (108 * h);
+        } else {
+            p[0] = w0 + df[0] * ((1.0 / 12.0) * (3 * (4 + sqrt3) * w0 + sqrt3 * (-4 * wn1 + wn2)) - w0);
+            p[1] = w0 + df[1] * (w0 + (-wn1 + wp1) / (4 * sqrt3) - w0);
+            p[2] = w0 + df[2] * (w0 - (sqrt3 * w0) / 4 + (4 * wp1 - wp2) / (4 * sqrt3) - w0);
+            p[3] = w0 + df[3] * ((4314 * w0 + (4 - 500 * sqrt3) * wn1 - wn2 + 70 * sqrt3 * wn2 + 4 * wp1 + 500 * sqrt3 * wp1 - wp2 - 70 * sqrt3 * wp2) / 4320 - w0);
+            px[0] = df[0] * ((9 + sqrt3) * w0 - 2 * (6 + sqrt3) * wn1 + (3 + sqrt3) * wn2) / (6 * h);
+            px[1] = df[1] * (-2 * sqrt3 * w0 + (-3 + sqrt3) * wn1 + (3 + sqrt3) * wp1) / (6 * h);
+            px[2] = df[2] * ((-9 + sqrt3) * w0 - 2 * (-6 + sqrt3) * wp1 + (-3 + sqrt3) * wp2) / (6 * h);
+            px[3] = -df[3] * ((48 * sqrt3 * w0 + 72 * wn1 - 26 * sqrt3 * wn1 - 9 * wn2 + 2 * sqrt3 * wn2 - 72 * wp1 - 26 * sqrt3 * wp1 + 9 * wp2 + 2 * sqrt3 * wp2) / (108 * h));
+        }
+        return;
+    }
+    if (order == 7) {
+        const double wn3 = s[0], wn2 = s[1], wn1 = s[2], w0 = s[3], wp1 = s[4], wp2 = s[5], wp3 = s[6];
+        const double sqrt15 = 3.872983346207417;
+        if (ig == 0) {
+            p[0] = w0 + df[0] * ((23.0 * w0 + 2.0 * wn1 - wn2) / 24.0 - w0);
+            p[1] = w0 + df[1] * ((26.0 * w0 - wn1 - wp1) / 24.0 - w0);
+            p[2] = w0 + df[2] * ((23.0 * w0 + 2.0 * wp1 - wp2) / 24.0 - w0);
+            p[3] = w0 + df[3] * ((2134.0 * w0 - 116.0 * wn1 + 9.0 * wn2 - 116.0 * wp1 + 9.0 * wp2) / 1920.0 - w0);
+            p[4] = w0 + df[4] * ((121004 * w0 - 7621 * wn1 + 954 * wn2 - 75 * wn3 - 7621 * wp1 + 954 * wp2 - 75 * wp3) / 107520.0 - w0);
+            px[0] = df[0] * (3.0 * w0 - 4.0 * wn1 + wn2) / (2.0 * h);
+            px[1] = df[1] * (-wn1 + wp1) / (2.0 * h);
+            px[2] = df[2] * (-3.0 * w0 + 4.0 * wp1 - wp2) / (2.0 * h);
+            px[3] = df[3] * (-34.0 * wn1 + 5.0 * wn2 + 34.0 * wp1 - 5.0 * wp2) / (48.0 * h);
+            px[4] = df[4] * (-9455 * wn1 + 2236 * wn2 - 259 * wn3 + 9455 * wp1 - 2236 * wp2 + 259 * wp3) / (11520.0 * h);
+        } else if (ig == 1) {
+            p[0] = w0 + df[0] * (((62 - 9 * sqrt15) * w0 + 4 * (-1 + 3 * sqrt15) * wn1 + (2 - 3 * sqrt15) * wn2) / 60.0 - w0);
+            p[1] = w0 + df[1] * ((56 * w0 + (2 + 3 * sqrt15) * wn1 + (2 - 3 * sqrt15) * wp1) / 60.0 - w0);
+            p[2] = w0 + df[2] * (((62 + 9 * sqrt15) * w0 - 4 * (1 + 3 * sqrt15) * wp1 + (2 + 3 * sqrt15) * wp2) / 60.0 - w0);
+            p[3] = w0 + df[3] * ((2186 * w0 + 4 * (29 + 41 * sqrt15) * wn1 - 9 * wn2 - 22 * sqrt15 * wn2 + 116 * wp1 - 164 * sqrt15 * wp1 - 9 * wp2 + 22 * sqrt15 * wp2) / 2400.0 - w0);
+            p[4] = w0 + df[4] * ((4534440 * w0 + 5 * (57144 + 78421 * sqrt15) * wn1 - 35748 * wn2 - 84364 * sqrt15 * wn2 + 2808 * wn3 + 9541 * sqrt15 * wn3 + 285720 * wp1 -
+                                  392105 * sqrt15 * wp1 - 35748 * wp2 + 84364 * sqrt15 * wp2 + 2808 * wp3 - 9541 * sqrt15 * wp3) / 5040000.0 - w0);
+            px[0] = df[0] * (-((-15 + sqrt15) * w0) + 2 * (-10 + sqrt15) * wn1 - (-5 + sqrt15) * wn2) / (10.0 * h);
+            px[1] = df[1] * (2 * sqrt15 * w0 - (5 + sqrt15) * wn1 - (-5 + sqrt15) * wp1) / (h * 10.0);
+            px[2] = df[2] * (-((15 + sqrt15) * w0) + 2 * (10 + sqrt15) * wp1 - (5 + sqrt15) * wp2) / (10.0 * h);
+            px[3] = df[3] * (78 * sqrt15 * w0 - 2 * (95 + 21 * sqrt15) * wn1 + 20 * wn2 + 3 * sqrt15 * wn2 + 190 * wp1 - 42 * sqrt15 * wp1 - 20 * wp2 + 3 * sqrt15 * wp2) / (300.0 * h);
+            px[4] = df[4] * (103860 * sqrt15 * w0 - 5 * (49925 + 11619 * sqrt15) * wn1 + 41300 * wn2 + 6678 * sqrt15 * wn2 - 4325 * wn3 - 513 * sqrt15 * wn3 + 249625 * wp1 -
+                             58095 * sqrt15 * wp1 - 41300 * wp2 + 6678 * sqrt15 * wp2 + 4325 * wp3 - 513 * sqrt15 * wp3) / (360000.0 * h);
+        } else {
+            p[0] = w0 + df[0] * (((62 + 9 * sqrt15) * w0 - 4 * (1 + 3 * sqrt15) * wn1 + (2 + 3 * sqrt15) * wn2) / 60.0 - w0);
+            p[1] = w0 + df[1] * ((56 * w0 + (2 - 3 * sqrt15) * wn1 + (2 + 3 * sqrt15) * wp1) / 60.0 - w0);
+            p[2] = w0 + df[2] * (((62 - 9 * sqrt15) * w0 + 4 * (-1 + 3 * sqrt15) * wp1 + (2 - 3 * sqrt15) * wp2) / 60.0 - w0);
+            p[3] = w0 + df[3] * ((2186 * w0 - 4 * (-29 + 41 * sqrt15) * wn1 - 9 * wn2 + 22 * sqrt15 * wn2 + 116 * wp1 + 164 * sqrt15 * wp1 - 9 * wp2 - 22 * sqrt15 * wp2) / 2400.0 - w0);
+            p[4] = w0 + df[4] * ((4534440 * w0 - 5 * (-57144 + 78421 * sqrt15) * wn1 - 35748 * wn2 + 84364 * sqrt15 * wn2 + 2808 * wn3 - 9541 * sqrt15 * wn3 + 285720 * wp1 +
+                                  392105 * sqrt15 * wp1 - 35748 * wp2 - 84364 * sqrt15 * wp2 + 2808 * wp3 + 9541 * sqrt15 * wp3) / 5040000.0 - w0);
+            px[0] = df[0] * ((15 + sqrt15) * w0 - 2 * (10 + sqrt15) * wn1 + (5 + sqrt15) * wn2) / (10.0 * h);
+            px[1] = df[1] * (-2 * sqrt15 * w0 - (5 - sqrt15) * wn1 + (5 + sqrt15) * wp1) / (h * 10.0);
+            px[2] = df[2] * ((-15 + sqrt15) * w0 - 2 * (-10 + sqrt15) * wp1 + (-5 + sqrt15) * wp2) / (10.0 * h);
+            px[3] = df[3] * (-78 * sqrt15 * w0 + 2 * (-95 + 21 * sqrt15) * wn1 + 20 * wn2 - 3 * sqrt15 * wn2 + 190 * wp1 + 42 * sqrt15 * wp1 - 20 * wp2 - 3 * sqrt15 * wp2) / (300.0 * h);
+            px[4] = df[4] * (-103860 * sqrt15 * w0 + 5 * (-49925 + 11619 * sqrt15) * wn1 + 41300 * wn2 - 6678 * sqrt15 * wn2 - 4325 * wn3 + 513 * sqrt15 * wn3 + 249625 * wp1 +
+                             58095 * sqrt15 * wp1 - 41300 * wp2 - 6678 * sqrt15 * wp2 + 4325 * wp3 + 513 * sqrt15 * wp3) / (360000.0 * h);
+        }
+        return;
+    }
+    // order 9: the polynomial family evaluated at the Lobatto abscissae
+    // x = -1, 0, -1/2 - sqrt5/10, -1/2 + sqrt5/10 of the face segment [-1, 0] (:3494-3543)
+    const double wn4 = s[0], wn3 = s[1], wn2 = s[2], wn1 = s[3], w0 = s[4];
+    const double wp1 = s[5], wp2 = s[6], wp3 = s[7], wp4 = s[8];
+    const double sqrt5 = 2.236067977499790;
+    double x = ig == 0 ? -1.0 : ig == 1 ? 0.0 : ig == 2 ? -0.5 - sqrt5 / 10.0 : -0.5 + sqrt5 / 10.0;
+    double a3, b3, c3;
+    a3 = (11 * w0 - 7 * wn1 + 2 * wn2) / 6.0; b3 = (2 * w0 - 3 * wn1 + wn2); c3 = (w0 - 2 * wn1 + wn2) / 2.0;
+    p[0] = w0 + df[0] * (a3 + b3 * x + c3 * x * x - w0); px[0] = df[0] * (b3 + 2.0 * c3 * x) / h;
+    a3 = (5 * w0 - wn1 + 2 * wp1) / 6.0; b3 = (-w0 + wp1); c3 = (-2 * w0 + wn1 + wp1) / 2.0;
+    p[1] = w0 + df[1] * (a3 + b3 * x + c3 * x * x - w0); px[1] = df[1] * (b3 + 2.0 * c3 * x) / h;
+    a3 = (2 * w0 + 5 * wp1 - wp2) / 6.0; b3 = (-w0 + wp1); c3 = (w0 - 2 * wp1 + wp2) / 2.0;
+    p[2] = w0 + df[2] * (a3 + b3 * x + c3 * x * x - w0); px[2] = df[2] * (b3 + 2.0 * c3 * x) / h;
+    double a5, b5, c5, d5, e5;
+    a5 = (47 * w0 - 13 * wn1 + 2 * wn2 + 27 * wp1 - 3 * wp2) / 60.0;
+    b5 = (-15 * w0 + wn1 + 15 * wp1 - wp2) / 12.0;
+    c5 = (-8 * w0 + 6 * wn1 - wn2 + 2 * wp1 + wp2) / 8.0;
+    d5 = (3 * w0 - wn1 - 3 * wp1 + wp2) / 6.0;
+    e5 = (6 * w0 - 4 * wn1 + wn2 - 4 * wp1 + wp2) / 24.0;
+    p[3] = w0 + df[3] * (a5 + b5 * x + c5 * x * x + d5 * x * x * x + e5 * x * x * x * x - w0);
+    px[3] = df[3] * (b5 + 2.0 * c5 * x + 3.0 * d5 * x * x + 4.0 * e5 * x * x * x) / h;
+    double a7, b7, c7, d7, e7, f7, g7;
+    a7 = (319 * w0 - 101 * wn1 + 25 * wn2 - 3 * wn3 + 214 * wp1 - 38 * wp2 + 4 * wp3) / 420.0;
+    b7 = (-245 * w0 + 25 * wn1 - 2 * wn2 + 245 * wp1 - 25 * wp2 + 2 * wp3) / 180.0;
+    c7 = (-230 * w0 + 210 * wn1 - 57 * wn2 + 7 * wn3 + 15 * wp1 + 63 * wp2 - 8 * wp3) / 240.0;
+    d7 = (28 * w0 - 11 * wn1 + wn2 - 28 * wp1 + 11 * wp2 - wp3) / 36.0;
+    e7 = (46 * w0 - 39 * wn1 + 15 * wn2 - 2 * wn3 - 24 * wp1 + 3 * wp2 + wp3) / 144.0;
+    f7 = (-10 * w0 + 5 * wn1 - wn2 + 10 * wp1 - 5 * wp2 + wp3) / 120.0;
+    g7 = (-20 * w0 + 15 * wn1 - 6 * wn2 + wn3 + 15 * wp1 - 6 * wp2 + wp3) / 720.0;
+    p[4] = w0 + df[4] * (a7 + b7 * x + c7 * x * x + d7 * x * x * x + e7 * x * x * x * x + f7 * x * x * x * x * x + g7 * x * x * x * x * x * x - w0);
+    px[4] = df[4] * (b7 + 2.0 * c7 * x + 3.0 * d7 * x * x + 4.0 * e7 * x * x * x + 5.0 * f7 * x * x * x * x + 6.0 * g7 * x * x * x * x * x) / h;
+    double a9, b9, c9, d9, e9, f9, g9, h9, i9;
+    a9 = (1879 * w0 - 641 * wn1 + 199 * wn2 - 41 * wn3 + 4 * wn4 + 1375 * wp1 - 305 * wp2 + 55 * wp3 - 5 * wp4) / 2520.0;
+    b9 = (-7175 * w0 + 889 * wn1 - 119 * wn2 + 9 * wn3 + 7175 * wp1 - 889 * wp2 + 119 * wp3 - 9 * wp4) / 5040.0;
+    c9 = (-27895 * w0 + 28679 * wn1 - 9835 * wn2 + 2081 * wn3 - 205 * wn4 - 2065 * wp1 + 11459 * wp2 - 2455 * wp3 + 236 * wp4) / 30240.0;
+    d9 = (1365 * w0 - 587 * wn1 + 89 * wn2 - 7 * wn3 - 1365 * wp1 + 587 * wp2 - 89 * wp3 + 7 * wp4) / 1440.0;
+    e9 = (1174 * w0 - 1160 * wn1 + 556 * wn2 - 128 * wn3 + 13 * wn4 - 464 * wp1 - 68 * wp2 + 88 * wp3 - 11 * wp4) / 3456.0;
+    f9 = (-75 * w0 + 41 * wn1 - 11 * wn2 + wn3 + 75 * wp1 - 41 * wp2 + 11 * wp3 - wp4) / 480.0;
+    g9 = (-380 * w0 + 334 * wn1 - 170 * wn2 + 46 * wn3 - 5 * wn4 + 250 * wp1 - 86 * wp2 + 10 * wp3 + wp4) / 8640.0;
+    h9 = (35 * w0 - 21 * wn1 + 7 * wn2 - wn3 - 35 * wp1 + 21 * wp2 - 7 * wp3 + wp4) / 5040.0;
+    i9 = (70 * w0 - 56 * wn1 + 28 * wn2 - 8 * wn3 + wn4 - 56 * wp1 + 28 * wp2 - 8 * wp3 + wp4) / 40320.0;
+    p[5] = w0 + df[5] * (a9 + b9 * x + c9 * x * x + d9 * x * x * x + e9 * x * x * x * x + f9 * x * x * x * x * x
+                         + g9 * x * x * x * x * x * x + h9 * x * x * x * x * x * x * x + i9 * x * x * x * x * x * x * x * x - w0);
+    px[5] = df[5] * (b9 + 2.0 * c9 * x + 3.0 * d9 * x * x + 4.0 * e9 * x * x * x + 5.0 * f9 * x * x * x * x
+                     + 6.0 * g9 * x * x * x * x * x + 7.0 * h9 * x * x * x * x * x * x + 8.0 * i9 * x * x * x * x * x * x * x) / h;
+}
+
+// scalar tangential reconstruction at all Gauss points of one face side
+void weno_tangent(int order, const double* s, const double* df, double h, double* g, double* gx) {
+    double fw[6], p[6], px[6];
+    int n = ao_weights(order, s, fw);
+    for (int ig = 0; ig < C.gp; ++ig) {
+        tangent_points(order, ig, s, df, h, p, px);
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < n; ++k) {
+            a += fw[k] * p[k];
+            b += fw[k] * px[k];
+        }
+        g[ig] = a;
+        gx[ig] = b;
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// normal reconstruction of one cell in one direction (WENO*_AO_with_df, :1731-1859 etc.)
+//   st[k][4]: stencil of cell states (already rotated for y), al[]: DF alpha along it.
+//   Lp: value/slope at the cell's left (lower) face, Rp: at its right (upper) face.
+// ----------------------------------------------------------------------------------------
+void normal_cell(int order, const double (*st)[4], const double* al, double h, Point& Lp, Point& Rp) {
+    const int r = order / 2, n = order;
+    double df[6];
+    df_factors(order, al, df);
+    double pn1[4], p0[4], pp1[4], bl[4], br[4];
+    to_prim(pn1, st[r - 1]);
+    to_prim(p0, st[r]);
+    to_prim(pp1, st[r + 1]);
+    for (int v = 0; v < 4; ++v) {
+        bl[v] = 0.5 * (pn1[v] + p0[v]);
+        br[v] = 0.5 * (pp1[v] + p0[v]);
+    }
+    double ch[9][4], s[9], var[4], der[4];
+    for (int side = 0; side < 2; ++side) {
+        const double* base = side == 0 ? bl : br;
+        for (int k = 0; k < n; ++k) {
+            if (C.p.characteristic) to_char(ch[k], base, st[k]);
+            else for (int v = 0; v < 4; ++v) ch[k][v] = st[k][v];
+        }
+        for (int v = 0; v < 4; ++v) {
+            for (int k = 0; k < n; ++k) s[k] = ch[k][v];
+            weno_normal(order, side, s, df, h, var[v], der[v]);
+        }
+        Point& P = side == 0 ? Lp : Rp;
+        if (C.p.characteristic) {
+            from_char(P.convar, base, var);
+            from_char(P.der1x, base, der);
+        } else {
+            for (int v = 0; v < 4; ++v) { P.convar[v] = var[v]; P.der1x[v] = der[v]; }
+        }
+    }
+    bool rr = needs_order_reduction(Rp.convar);
+    bool rl = needs_order_reduction(Lp.convar);
+    if (rl || rr) {
+        for (int v = 0; v < 4; ++v) {
+            Rp.convar[v] = st[r][v];
+            Lp.convar[v] = st[r][v];
+            Rp.der1x[v] = 0.0;
+            Lp.der1x[v] = 0.0;
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// tangential reconstruction of one face (weno_*th_ao_with_df_tangential, :2578-2791 etc.)
+//   ln[k][2]: line states (side 0 = left of face, 1 = right) along the face,
+//   a1/a2: DF alpha of the left / right cell column.  Writes gp Gauss states.
+//   For order 9 the right side reuses the left side's characteristic projection of the
+//   outermost stencil entries, as the reference does (:3318-3327: ren4/rep4 are not
+//   re-projected with the right base).
+// ----------------------------------------------------------------------------------------
+void tangent_face(int order, const Point (*ln)[2], const double* a1, const double* a2, double h, Recon* re) {
+    const int r = order / 2, n = order, gp = C.gp;
+    double df[2][6];
+    df_factors(order, a1, df[0]);
+    df_factors(order, a2, df[1]);
+    double ch[9][4], s[9];
+    for (int side = 0; side < 2; ++side) {
+        const Point& w0 = ln[r][side];
+        double base[4];
+        to_prim(base, w0.convar);
+        double var[4][4], der[4][4];
+        if (C.p.characteristic) {
+            for (int k = 0; k < n; ++k) {
+                if (order == 9 && side == 1 && (k == 0 || k == n - 1)) continue;  // reference quirk
+                to_char(ch[k], base, ln[k][side].convar);
+            }
+            for (int v = 0; v < 4; ++v) {
+                for (int k = 0; k < n; ++k) s[k] = ch[k][v];
+                double g[4], gx[4];
+                weno_tangent(order, s, df[side], h, g, gx);
+                for (int ig = 0; ig < gp; ++ig) { var[ig][v] = g[ig]; der[ig][v] = gx[ig]; }
+            }
+            for (int ig = 0; ig < gp; ++ig) {
+                Point& P = side == 0 ? re[ig].left : re[ig].right;
+                from_char(P.convar, base, var[ig]);
+                from_char(P.der1y, base, der[ig]);
+            }
+        } else {
+            for (int v = 0; v < 4; ++v) {
+                for (int k = 0; k < n; ++k) s[k] = ln[k][side].convar[v];
+                double g[4], gx[4];
+                weno_tangent(order, s, df[side], h, g, gx);
+                for (int ig = 0; ig < gp; ++ig) {
+                    Point& P = side == 0 ? re[ig].left : re[ig].right;
+                    P.convar[v] = g[ig];
+                    P.der1y[v] = gx[ig];
+                }
+            }
+        }
+        // normal slope reconstructed in conservative variables
+        for (int v = 0; v < 4; ++v) {
+            for (int k = 0; k < n; ++k) s[k] = ln[k][side].der1x[v];
+            double g[4], gx[4];
+            weno_tangent(order, s, df[side], h, g, gx);
+            for (int ig = 0; ig < gp; ++ig) {
+                Point& P = side == 0 ? re[ig].left : re[ig].right;
+                P.der1x[v] = g[ig];
+            }
+        }
+    }
+    for (int side = 0; side < 2; ++side)
+        for (int ig = 0; ig < gp; ++ig) {
+            Point& P = side == 0 ? re[ig].left : re[ig].right;
+            if (needs_order_reduction(P.convar)) {
+                const Point& w0 = ln[r][side];
+                for (int v = 0; v < 4; ++v) {
+                    P.convar[v] = w0.convar[v];
+                    P.der1x[v] = w0.der1x[v];
+                    P.der1y[v] = 0.0;
+                }
+            }
+        }
+}
+
+// ----------------------------------------------------------------------------------------
+// Maxwellian moments (MMDF2d, src/basic_function.cpp:110-187)
+// ----------------------------------------------------------------------------------------
+struct Moments {
+    double uwhole[7], uplus[7], uminus[7], vwhole[7];
+    double up[7][7][3], un[7][7][3], uv[7][7][3];
+    double xi2, xi4;
+};
+void moments(Moments& m, double u, double v, double lambda) {
+    const double pi = 3.14159265358979323846;
+    m.uwhole[0] = 1;
+    m.uwhole[1] = u;
+    m.uplus[0] = 0.5 * std::erfc(std::sqrt(lambda) * -u);
+    m.uminus[0] = 1.0 - m.uplus[0];
+    m.uplus[1] = u * m.uplus[0] + 0.5 * (std::exp(-lambda * u * u) / std::sqrt(pi * lambda));
+    m.uminus[1] = u - m.uplus[1];
+    double ol = 1.0 / lambda;
+    for (int i = 2; i <= 6; ++i) m.uwhole[i] = u * m.uwhole[i - 1] + 0.5 * (i - 1) * ol * m.uwhole[i - 2];
+    for (int i = 2; i <= 6; ++i) {
+        m.uplus[i] = u * m.uplus[i - 1] + 0.5 * (i - 1) * ol * m.uplus[i - 2];
+        m.uminus[i] = m.uwhole[i] - m.uplus[i];
+    }
+    m.vwhole[0] = 1;
+    m.vwhole[1] = v;
+    for (int i = 2; i <= 6; ++i) m.vwhole[i] = v * m.vwhole[i - 1] + 0.5 * (i - 1) * ol * m.vwhole[i - 2];
+    m.xi2 = 0.5 * C.K * ol;
+    m.xi4 = 0.25 * (C.K * C.K + 2 * C.K) * ol * ol;
+    for (int i = 0; i < 7; ++i)
+        for (int j = 0; j < 7; ++j)
+            for (int k = 0; k < 3; ++k)
+                if (i + j + 2 * k <= 6) {
+                    if (k == 0) {
+                        m.up[i][j][k] = m.uplus[i] * m.vwhole[j];
+                        m.un[i][j][k] = m.uminus[i] * m.vwhole[j];
+                    } else {
+                        double xi = k == 1 ? m.xi2 : m.xi4;
+                        m.up[i][j][k] = m.uplus[i] * m.vwhole[j] * xi;
+                        m.un[i][j][k] = m.uminus[i] * m.vwhole[j] * xi;
+                    }
+                    m.uv[i][j][k] = m.up[i][j][k] + m.un[i][j][k];
+                }
+}
+// moment contraction <a psi u^nu v^nv> over a table (GL/GR/G_address, :603-636)
+void contract(const double (*M)[7][3], int nu, int nv, const double* a, double* psi) {
+    const int u = nu, v = nv;
+    psi[0] = a[0] * M[u][v][0] + a[1] * M[u + 1][v][0] + a[2] * M[u][v + 1][0] + a[3] * 0.5 * (M[u + 2][v][0] + M[u][v + 2][0] + M[u][v][1]);
+    psi[1] = a[0] * M[u + 1][v][0] + a[1] * M[u + 2][v][0] + a[2] * M[u + 1][v + 1][0] + a[3] * 0.5 * (M[u + 3][v][0] + M[u + 1][v + 2][0] + M[u + 1][v][1]);
+    psi[2] = a[0] * M[u][v + 1][0] + a[1] * M[u + 1][v + 1][0] + a[2] * M[u][v + 2][0] + a[3] * 0.5 * (M[u + 2][v + 1][0] + M[u][v + 3][0] + M[u][v + 1][1]);
+    psi[3] = 0.5 * (a[0] * (M[u + 2][v][0] + M[u][v + 2][0] + M[u][v][1]) +
+                    a[1] * (M[u + 3][v][0] + M[u + 1][v + 2][0] + M[u + 1][v][1]) +
+                    a[2] * (M[u + 2][v + 1][0] + M[u][v + 3][0] + M[u][v + 1][1]) +
+                    a[3] * 0.5 * (M[u + 4][v][0] + M[u][v + 4][0] + M[u][v][2] + 2 * M[u + 2][v + 2][0] + 2 * M[u + 2][v][1] + 2 * M[u][v + 2][1]));
+}
+// micro-slope from a macroscopic slope (A, :571-583)
+void microslope(double* a, const double* der, const double* prim) {
+    double overden = 1.0 / prim[0];
+    double R4 = der[3] * overden - 0.5 * (prim[1] * prim[1] + prim[2] * prim[2] + 0.5 * (C.K + 2) / prim[3]) * der[0] * overden;
+    double R3 = (der[2] - prim[2] * der[0]) * overden;
+    double R2 = (der[1] - prim[1] * der[0]) * overden;
+    a[3] = (4.0 / (C.K + 2)) * prim[3] * prim[3] * (2 * R4 - 2 * prim[1] * R2 - 2 * prim[2] * R3);
+    a[2] = 2 * prim[3] * R3 - prim[2] * a[3];
+    a[1] = 2 * prim[3] * R2 - prim[1] * a[3];
+    a[0] = der[0] * overden - prim[1] * a[1] - prim[2] * a[2] - 0.5 * a[3] * (prim[1] * prim[1] + prim[2] * prim[2] + 0.5 * (C.K + 2) / prim[3]);
+}
+double tau_num(double dl, double dr, double ll, double lr, double dt) {
+    if (C.p.c1_euler <= 0 && C.p.c2_euler <= 0) return 0.0;
+    double Cc = C.p.c2_euler * std::abs(dl / ll - dr / lr) / std::abs(dl / ll + dr / lr);
+    return C.p.c1_euler * dt + dt * Cc;
+}
+
+// ----------------------------------------------------------------------------------------
+// GKS2D at one Gauss point (src/flux_function.cpp:345-698, gks2nd, Euler tau, S2O4 branch):
+// centre state by collision (also stored in re.center), the full second-order flux over
+// [0, dt] and [0, dt/2], combined into f = 4F(dt/2) - F(dt), derf = 4(F(dt) - 2F(dt/2)).
+// ----------------------------------------------------------------------------------------
+void gks2d(Recon& re, double dt, double* fo, double* dfo) {
+    double pl[4], pr[4], p0[4];
+    to_ulambda(pl, re.left.convar);
+    to_ulambda(pr, re.right.convar);
+    Moments ml, mr;
+    moments(ml, pl[1], pl[2], pl[3]);
+    moments(mr, pr[1], pr[2], pr[3]);
+    // collision (Collision, :561-569)
+    double* w0 = re.center.convar;
+    w0[0] = pl[0] * ml.uplus[0] + pr[0] * mr.uminus[0];
+    w0[1] = pl[0] * ml.uplus[1] + pr[0] * mr.uminus[1];
+    w0[2] = pl[0] * ml.vwhole[1] * ml.uplus[0] + pr[0] * mr.vwhole[1] * mr.uminus[0];
+    w0[3] = 0.5 * pl[0] * (ml.uplus[2] + ml.uplus[0] * ml.vwhole[2] + ml.uplus[0] * ml.xi2) +
+            0.5 * pr[0] * (mr.uminus[2] + mr.uminus[0] * mr.vwhole[2] + mr.uminus[0] * mr.xi2);
+    {
+        double alx[4], arx[4], al0x[4], ar0x[4], aly[4], ary[4], al0y[4], ar0y[4];
+        microslope(alx, re.left.der1x, pl);
+        microslope(arx, re.right.der1x, pr);
+        contract(ml.up, 0, 0, alx, al0x);
+        contract(mr.un, 0, 0, arx, ar0x);
+        microslope(aly, re.left.der1y, pl);
+        microslope(ary, re.right.der1y, pr);
+        contract(ml.up, 0, 0, aly, al0y);
+        contract(mr.un, 0, 0, ary, ar0y);
+        for (int v = 0; v < 4; ++v) {
+            re.center.der1x[v] = pl[0] * al0x[v] + pr[0] * ar0x[v];
+            re.center.der1y[v] = pl[0] * al0y[v] + pr[0] * ar0y[v];
+        }
+    }
+    to_ulambda(p0, re.center.convar);
+    const double tau = 0.0;  // Get_Tau_NS for Euler (:638-661)
+    double tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt);
+    double eta = std::exp(-dt / tn);
+    double t[6];
+    t[0] = tn * (1 - eta);
+    t[1] = tn * (eta * (dt + tn) - tn) + tau * tn * (eta - 1);
+    t[2] = tau * tn * (eta - 1);
+    t[3] = tn * eta + dt - tn;
+    t[4] = tn * (tn - eta * (dt + tn) - tau * (eta - 1)) - dt * tau;
+    t[5] = 0.5 * dt * dt - tau * tn * (eta - 1) - tau * dt;
+    const double unit[4] = {1, 0.0, 0.0, 0.0};
+    double F0[4], F1[4];
+    double glu[4], gru[4];
+    contract(ml.up, 1, 0, unit, glu);
+    contract(mr.un, 1, 0, unit, gru);
+    for (int i = 0; i < 4; ++i) F0[i] = pl[0] * t[0] * glu[i] + pr[0] * t[0] * gru[i];
+    Moments m0;
+    moments(m0, p0[1], p0[2], p0[3]);
+    double g0u[4];
+    contract(m0.uv, 1, 0, unit, g0u);
+    for (int i = 0; i < 4; ++i) F0[i] = F0[i] + p0[0] * t[3] * g0u[i];
+    double alx[4], alxuul[4], arx[4], arxuur[4], aly[4], alyuvl[4], ary[4], aryuvr[4];
+    microslope(alx, re.left.der1x, pl);
+    contract(ml.up, 2, 0, alx, alxuul);
+    microslope(arx, re.right.der1x, pr);
+    contract(mr.un, 2, 0, arx, arxuur);
+    microslope(aly, re.left.der1y, pl);
+    contract(ml.up, 1, 1, aly, alyuvl);
+    microslope(ary, re.right.der1y, pr);
+    contract(mr.un, 1, 1, ary, aryuvr);
+    for (int i = 0; i < 4; ++i) F0[i] = F0[i] + t[1] * (pl[0] * (alxuul[i] + alyuvl[i]) + pr[0] * (arxuur[i] + aryuvr[i]));
+    double alxu[4], alyv[4], arxu[4], aryv[4];
+    contract(ml.uv, 1, 0, alx, alxu);
+    contract(mr.uv, 1, 0, arx, arxu);
+    contract(ml.uv, 0, 1, aly, alyv);
+    contract(mr.uv, 0, 1, ary, aryv);
+    double Al[4], Ar[4], dAL[4], dAR[4];
+    for (int i = 0; i < 4; ++i) {
+        dAL[i] = -pl[0] * (alxu[i] + alyv[i]);
+        dAR[i] = -pr[0] * (arxu[i] + aryv[i]);
+    }
+    microslope(Al, dAL, pl);
+    microslope(Ar, dAR, pr);
+    double Alul[4], Arur[4];
+    contract(ml.up, 1, 0, Al, Alul);
+    contract(mr.un, 1, 0, Ar, Arur);
+    for (int i = 0; i < 4; ++i) F0[i] = F0[i] + t[2] * (pl[0] * Alul[i] + pr[0] * Arur[i]);
+    double a0x[4], a0xu[4], a0xuu[4], a0y[4], a0yv[4], a0yuv[4];
+    microslope(a0x, re.center.der1x, p0);
+    contract(m0.uv, 1, 0, a0x, a0xu);
+    contract(m0.uv, 2, 0, a0x, a0xuu);
+    microslope(a0y, re.center.der1y, p0);
+    contract(m0.uv, 0, 1, a0y, a0yv);
+    contract(m0.uv, 1, 1, a0y, a0yuv);
+    for (int i = 0; i < 4; ++i) F0[i] = F0[i] + p0[0] * t[4] * (a0xuu[i] + a0yuv[i]);
+    double dA0[4], A0[4], A0u[4];
+    for (int i = 0; i < 4; ++i) dA0[i] = -p0[0] * (a0xu[i] + a0yv[i]);
+    microslope(A0, dA0, p0);
+    contract(m0.uv, 1, 0, A0, A0u);
+    for (int i = 0; i < 4; ++i) F0[i] = F0[i] + p0[0] * t[5] * (A0u[i]);
+    // second time level dt/2 (:647-676)
+    double dt2 = 0.5 * dt;
+    tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt2);
+    eta = std::exp(-dt2 / tn);
+    t[0] = tn * (1 - eta);
+    t[1] = tn * (eta * (dt2 + tn) - tn) + tau * tn * (eta - 1);
+    t[2] = tau * tn * (eta - 1);
+    t[3] = tn * eta + dt2 - tn;
+    t[4] = tn * (tn - eta * (dt2 + tn) - tau * (eta - 1)) - dt2 * tau;
+    t[5] = 0.5 * dt2 * dt2 - tau * tn * (eta - 1) - tau * dt2;
+    for (int i = 0; i < 4; ++i) {
+        F1[i] = t[0] * (pl[0] * glu[i] + pr[0] * gru[i]);
+        F1[i] = F1[i] + t[1] * (pl[0] * (alxuul[i] + alyuvl[i]) + pr[0] * (arxuur[i] + aryuvr[i]));
+        F1[i] = F1[i] + t[2] * (pl[0] * Alul[i] + pr[0] * Arur[i]);
+        F1[i] = F1[i] + p0[0] * t[3] * g0u[i];
+        F1[i] = F1[i] + p0[0] * t[4] * (a0xuu[i] + a0yuv[i]);
+        F1[i] = F1[i] + p0[0] * t[5] * (A0u[i]);
+    }
+    for (int i = 0; i < 4; ++i) {
+        fo[i] = (4.0 * F1[i] - F0[i]);
+        dfo[i] = 4.0 * (F0[i] - 2.0 * F1[i]);
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// boundary conditions, applied left, right, down, up as the drivers do
+// ----------------------------------------------------------------------------------------
+void bc_side(int side) {
+    const int nx = C.nx, ny = C.ny, g = C.g;
+    const int kind = C.p.bc[side];
+    auto copy = [&](int dst, int src, int flipv) {
+        for (int v = 0; v < 4; ++v) W[4 * dst + v] = W[4 * src + v];
+        if (flipv) W[4 * dst + flipv] = -W[4 * src + flipv];
+    };
+    double inflow[4];
+    prim_to_con(inflow, C.p.bc_prim[side]);
+    if (side == 0 || side == 1) {
+        for (int k = 0; k < g; ++k) {
+            int i = side == 0 ? g - 1 - k : nx - g + k;  // same sweep order as the reference
+            for (int j = 0; j < ny; ++j) {
+                int dst = cell(i, j);
+                if (kind == HOS_BC_FREE) copy(dst, cell(side == 0 ? i + 1 : i - 1, j), 0);
+                else if (kind == HOS_BC_PERIODIC) copy(dst, cell(side == 0 ? i + C.p.nodex : i - C.p.nodex, j), 0);
+                else if (kind == HOS_BC_REFLECT) copy(dst, cell(side == 0 ? 2 * g - 1 - i : 2 * nx - 2 * g - 1 - i, j), 1);
+                else for (int v = 0; v < 4; ++v) W[4 * dst + v] = inflow[v];
+            }
+        }
+    } else {
+        for (int k = 0; k < g; ++k) {
+            int j = side == 2 ? g - 1 - k : ny - g + k;
+            for (int i = 0; i < nx; ++i) {
+                int dst = cell(i, j);
+                if (kind == HOS_BC_FREE) copy(dst, cell(i, side == 2 ? j + 1 : j - 1), 0);
+                else if (kind == HOS_BC_PERIODIC) copy(dst, cell(i, side == 2 ? j + C.p.nodey : j - C.p.nodey), 0);
+                else if (kind == HOS_BC_REFLECT) copy(dst, cell(i, side == 2 ? 2 * g - 1 - j : 2 * ny - 2 * g - 1 - j), 2);
+                else for (int v = 0; v < 4; ++v) W[4 * dst + v] = inflow[v];
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// DF indicator of a face from its Gauss states (Calculate_alpha_k / Calculate_alpha, :1463-1521)
+// ----------------------------------------------------------------------------------------
+double alpha_k(const double* pl, const double* pr) {
+    double Mln = pl[1] / std::sqrt(C.Gamma * pl[3] / pl[0]);
+    double Mlt = pl[2] / std::sqrt(C.Gamma * pl[3] / pl[0]);
+    double Mrn = pr[1] / std::sqrt(C.Gamma * pr[3] / pr[0]);
+    double Mrt = pr[2] / std::sqrt(C.Gamma * pr[3] / pr[0]);
+    double A = std::abs(pl[3] - pr[3]) / pl[3] + std::abs(pl[3] - pr[3]) / pr[3];
+    A = A + sq(Mln - Mrn) + sq(Mlt - Mrt);
+    return A;
+}
+double face_alpha(const Recon* re, bool yface) {
+    double a[4];
+    for (int ig = 0; ig < C.gp; ++ig) {
+        double pl[4], pr[4];
+        to_prim(pl, re[ig].left.convar);
+        to_prim(pr, re[ig].right.convar);
+        if (yface) {
+            double ql[4], qr[4];
+            rot_x_to_y(ql, pl);
+            rot_x_to_y(qr, pr);
+            a[ig] = alpha_k(ql, qr);
+        } else {
+            a[ig] = alpha_k(pl, pr);
+        }
+    }
+    double r = 0;
+    if (C.gp == 2) r = 0.5 * (a[0] + a[1]);
+    if (C.gp == 3) r = (a[0] + a[1] + a[2]) / 3.0;
+    if (C.gp == 4) r = 0.25 * (a[0] + a[1] + a[2] + a[3]);
+    return r < 2.0 ? 0.0 : r;
+}
+
+}  // namespace
+
+// ========================================================================================
+// C interface
+// ========================================================================================
+extern "C" {
+
+int oracle2d_init(const hos2d_params* p) {
+    C = Config();
+    C.p = *p;
+    if (!(p->order == 5 || p->order == 7 || p->order == 9)) return 2;
+    if (!p->use_df) return 2;  // only the discontinuity-feedback variants are restated
+    const int need_gp = p->order == 5 ? 2 : p->order == 7 ? 3 : 4;
+    if (p->gausspoint != need_gp) return 2;
+    if (p->ghost < p->order / 2 + 1) return 2;
+    C.g = p->ghost;
+    C.gp = p->gausspoint;
+    C.nx = p->nodex + 2 * p->ghost;
+    C.ny = p->nodey + 2 * p->ghost;
+    C.dx = (p->right - p->left) / p->nodex;
+    C.dy = (p->up - p->down) / p->nodey;
+    C.K = p->K;
+    C.Gamma = p->gamma;
+    if (C.gp == 2) { C.gw[0] = 0.5; C.gw[1] = 0.5; }
+    if (C.gp == 3) { C.gw[0] = 4.0 / 9.0; C.gw[1] = 0.5 - 0.5 * C.gw[0]; C.gw[2] = C.gw[1]; }
+    if (C.gp == 4) { C.gw[0] = 1.0 / 12.0; C.gw[1] = 1.0 / 12.0; C.gw[2] = 5.0 / 12.0; C.gw[3] = 5.0 / 12.0; }
+    const size_t nc = static_cast<size_t>(C.nx) * C.ny;
+    const size_t nf = static_cast<size_t>(C.nx + 1) * (C.ny + 1);
+    W.assign(4 * nc, 0.0);
+    Wold.assign(4 * nc, 0.0);
+    Prim.assign(4 * nc, 0.0);
+    AX.assign(nc, 0.0);
+    AY.assign(nc, 0.0);
+    Point z;
+    std::memset(&z, 0, sizeof z);
+    XL.assign(2 * nf, z);
+    YL.assign(2 * nf, z);
+    Recon zr;
+    std::memset(&zr, 0, sizeof zr);
+    XG.assign(nf * C.gp, zr);
+    YG.assign(nf * C.gp, zr);
+    XF.assign(nf * 2 * C.gp * 8, 0.0);
+    YF.assign(nf * 2 * C.gp * 8, 0.0);
+    XX.assign(nf * C.gp * 4, 0.0);
+    YX.assign(nf * C.gp * 4, 0.0);
+    return 0;
+}
+
+void oracle2d_free(void) {
+    std::vector<double>().swap(W);
+    std::vector<double>().swap(Wold);
+    std::vector<double>().swap(Prim);
+    std::vector<Point>().swap(XL);
+    std::vector<Point>().swap(YL);
+    std::vector<Recon>().swap(XG);
+    std::vector<Recon>().swap(YG);
+}
+
+void oracle2d_set_threads(int n) { omp_set_num_threads(n); }
+
+void oracle2d_set_state(const double* convar, const double* primvar) {
+    const size_t n = static_cast<size_t>(C.nx) * C.ny;
+    std::memcpy(W.data(), convar, 4 * n * sizeof(double));
+    if (primvar) std::memcpy(Prim.data(), primvar, 4 * n * sizeof(double));
+}
+
+void oracle2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y) {
+    const size_t n = static_cast<size_t>(C.nx) * C.ny;
+    if (convar) std::memcpy(convar, W.data(), 4 * n * sizeof(double));
+    if (primvar) std::memcpy(primvar, Prim.data(), 4 * n * sizeof(double));
+    if (alpha_x) std::memcpy(alpha_x, AX.data(), n * sizeof(double));
+    if (alpha_y) std::memcpy(alpha_y, AY.data(), n * sizeof(double));
+}
+
+// CopyFluid_new_to_old + Get_CFL with the primitive state of the previous stage
+// (src/time_advance.cpp:264-305)
+double oracle2d_begin_step(double tstop, double t) {
+    const int g = C.g;
+#pragma omp parallel for
+    for (int i = g; i < g + C.p.nodex; ++i)
+        for (int j = g; j < g + C.p.nodey; ++j)
+            for (int v = 0; v < 4; ++v) Wold[4 * cell(i, j) + v] = W[4 * cell(i, j) + v];
+    double dt = C.dx;
+    const double cfl = C.p.cfl;
+    auto dtx = [&](double d, double h, const double* pr) {
+        double tmp = std::sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + std::sqrt(C.Gamma * pr[3] / pr[0]);
+        if (tmp > cfl * h / d) d = cfl * h / tmp;
+        return d;
+    };
+    for (int i = g; i < C.nx - g; ++i)
+        for (int j = g; j < C.ny - g; ++j) {
+            const double* pr = &Prim[4 * cell(i, j)];
+            dt = dtx(dt, C.dx, pr);
+            dt = dtx(dt, C.dy, pr);
+        }
+    if (t + dt > tstop) dt = tstop - t + 1e-16;
+    return dt;
+}
+
+int oracle2d_stage(int stage, double dt) {
+    const int nx = C.nx, ny = C.ny, g = C.g, gp = C.gp, order = C.p.order, r = order / 2;
+    for (int s = 0; s < 4; ++s) bc_side(s);
+    // Convar_to_Primvar with the blow-up check
+    int bad = 0;
+#pragma omp parallel for reduction(| : bad)
+    for (int c = 0; c < nx * ny; ++c) {
+        double* pr = &Prim[4 * c];
+        to_prim(pr, &W[4 * c]);
+        if (pr[0] < 0 || pr[3] < 0 || std::isnan(pr[0]) || std::isnan(pr[3])) bad |= 1;
+    }
+    if (bad) return 1;
+    // normal reconstruction: x for cells with i in [g-1, nx-g], y for j in [g-1, ny-g]
+#pragma omp parallel for
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+            double st[9][4], al[9];
+            if (i > g - 2 && i < nx - g + 1) {
+                for (int k = 0; k < order; ++k) {
+                    const int c = cell(i + k - r, j);
+                    for (int v = 0; v < 4; ++v) st[k][v] = W[4 * c + v];
+                    al[k] = AX[c];
+                }
+                normal_cell(order, st, al, C.dx, XL[2 * face(i, j) + 1], XL[2 * face(i + 1, j) + 0]);
+            }
+            if (j > g - 2 && j < ny - g + 1) {
+                for (int k = 0; k < order; ++k) {
+                    const int c = cell(i, j + k - r);
+                    rot_y_to_x(st[k], &W[4 * c]);
+                    al[k] = AY[c];
+                }
+                normal_cell(order, st, al, C.dy, YL[2 * face(i, j) + 1], YL[2 * face(i, j + 1) + 0]);
+            }
+        }
+    // tangential reconstruction for cells in [g-1, n-g+1): x-face (i+1, j), y-face (i, j+1)
+#pragma omp parallel for
+    for (int i = g - 1; i < nx - g + 1; ++i)
+        for (int j = g - 1; j < ny - g + 1; ++j) {
+            Point ln[9][2];
+            double a1[9], a2[9];
+            // x-face (i+1, j): tangent along +y, left cell column i, right column i+1
+            for (int k = 0; k < order; ++k) {
+                const int f = face(i + 1, j + k - r);
+                ln[k][0] = XL[2 * f + 0];
+                ln[k][1] = XL[2 * f + 1];
+                a1[k] = AY[cell(i, j + k - r)];
+                a2[k] = AY[cell(i + 1, j + k - r)];
+            }
+            tangent_face(order, ln, a1, a2, C.dy, &XG[static_cast<size_t>(face(i + 1, j)) * gp]);
+            // y-face (i, j+1): tangent along -x, lower cell row j, upper row j+1
+            for (int k = 0; k < order; ++k) {
+                const int f = face(i - (k - r), j + 1);
+                ln[k][0] = YL[2 * f + 0];
+                ln[k][1] = YL[2 * f + 1];
+                a1[k] = AX[cell(i - (k - r), j)];
+                a2[k] = AX[cell(i - (k - r), j + 1)];
+            }
+            tangent_face(order, ln, a1, a2, C.dx, &YG[static_cast<size_t>(face(i, j + 1)) * gp]);
+        }
+    // fluxes (Calculate_flux, src/flux_function.cpp:317-343)
+#pragma omp parallel for
+    for (int i = g; i < g + C.p.nodex + 1; ++i)
+        for (int j = g; j < g + C.p.nodey; ++j)
+            for (int ig = 0; ig < gp; ++ig) {
+                const size_t f = face(i, j);
+                double* o = &XF[((f * 2 + stage) * gp + ig) * 8];
+                gks2d(XG[f * gp + ig], dt, o, o + 4);
+            }
+#pragma omp parallel for
+    for (int i = g; i < g + C.p.nodex; ++i)
+        for (int j = g; j < g + C.p.nodey + 1; ++j)
+            for (int ig = 0; ig < gp; ++ig) {
+                const size_t f = face(i, j);
+                double* o = &YF[((f * 2 + stage) * gp + ig) * 8];
+                gks2d(YG[f * gp + ig], dt, o, o + 4);
+            }
+    // stage combination per face and Gauss point (Update, src/time_advance.cpp:378-428)
+    auto combine = [&](std::vector<double>& F, std::vector<double>& X, int i0, int i1, int j0, int j1) {
+#pragma omp parallel for
+        for (int i = i0; i < i1; ++i)
+            for (int j = j0; j < j1; ++j)
+                for (int ig = 0; ig < gp; ++ig)
+                    for (int v = 0; v < 4; ++v) {
+                        const size_t f = face(i, j);
+                        double fl = 0.0;
+                        for (int k = 0; k < stage + 1; ++k) {
+                            const double* q = &F[((f * 2 + k) * gp + ig) * 8];
+                            fl = fl + C.gw[ig] * (TC[stage][k][0] * q[v] + TC[stage][k][1] * q[4 + v]);
+                        }
+                        X[(f * gp + ig) * 4 + v] = fl;
+                    }
+    };
+    combine(XF, XX, g, g + C.p.nodex + 1, g, g + C.p.nodey);
+    combine(YF, YX, g, g + C.p.nodex, g, g + C.p.nodey + 1);
+    // Update_with_gauss (src/time_advance.cpp:431-474): y-face fluxes rotate back to the
+    // global frame (local (n, t) -> global (-t, n)); x-face rotation is the identity.
+    const double area = C.dx * C.dy;
+#pragma omp parallel for
+    for (int i = g; i < g + C.p.nodex; ++i)
+        for (int j = g; j < g + C.p.nodey; ++j) {
+            const int c = cell(i, j);
+            const size_t f = face(i, j);
+            for (int v = 0; v < 4; ++v) {
+                W[4 * c + v] = Wold[4 * c + v];
+                double total = 0.0;
+                for (int ig = 0; ig < gp; ++ig) {
+                    auto yv = [&](size_t ff) {
+                        const double* x = &YX[(ff * gp + ig) * 4];
+                        return v == 1 ? x[1] * 0.0 - x[2] * 1.0 : v == 2 ? x[1] * 1.0 + x[2] * 0.0 : x[v];
+                    };
+                    auto xv = [&](size_t ff) {
+                        const double* x = &XX[(ff * gp + ig) * 4];
+                        return v == 1 ? x[1] * 1.0 - x[2] * 0.0 : v == 2 ? x[1] * 0.0 + x[2] * 1.0 : x[v];
+                    };
+                    total += C.dx * yv(f);
+                    total += -C.dx * yv(f + 1);
+                    total += C.dy * xv(f);
+                    total += -C.dy * xv(f + ny + 1);
+                }
+                W[4 * c + v] += total / area;
+            }
+        }
+    // DF factor update (Update_alpha, :1523-1534)
+    const int jend = g + std::min(C.p.nodex, C.p.nodey);
+#pragma omp parallel for
+    for (int i = g; i < g + C.p.nodex; ++i)
+        for (int j = g; j < jend; ++j) {
+            const int c = cell(i, j);
+            double al = face_alpha(&XG[static_cast<size_t>(face(i, j)) * gp], false);
+            double ar = face_alpha(&XG[static_cast<size_t>(face(i + 1, j)) * gp], false);
+            double ad = face_alpha(&YG[static_cast<size_t>(face(i, j)) * gp], true);
+            double au = face_alpha(&YG[static_cast<size_t>(face(i, j + 1)) * gp], true);
+            AX[c] = al + ar;
+            AY[c] = ad + au;
+        }
+    return 0;
+}
+
+int oracle2d_step(double tstop, double t, double* dt_out) {
+    double dt = oracle2d_begin_step(tstop, t);
+    if (dt_out) *dt_out = dt;
+    for (int s = 0; s < 2; ++s) {
+        int st = oracle2d_stage(s, dt);
+        if (st) return st;
+    }
+    return 0;
+}
+
+void oracle2d_get_gauss(int dir, double* out) {
+    std::vector<Recon>& G = dir == 0 ? XG : YG;
+    const size_t nf = static_cast<size_t>(C.nx + 1) * (C.ny + 1);
+    for (size_t f = 0; f < nf; ++f)
+        for (int ig = 0; ig < C.gp; ++ig) {
+            double* o = out + (f * C.gp + ig) * 36;
+            const Recon& re = G[f * C.gp + ig];
+            const Point* pts[3] = {&re.left, &re.right, &re.center};
+            for (int s = 0; s < 3; ++s)
+                for (int v = 0; v < 4; ++v) {
+                    o[s * 12 + v] = pts[s]->convar[v];
+                    o[s * 12 + 4 + v] = pts[s]->der1x[v];
+                    o[s * 12 + 8 + v] = pts[s]->der1y[v];
+                }
+        }
+}
+
+void oracle2d_get_flux(int dir, int stage, double* out) {
+    std::vector<double>& F = dir == 0 ? XF : YF;
+    const size_t nf = static_cast<size_t>(C.nx + 1) * (C.ny + 1);
+    for (size_t f = 0; f < nf; ++f)
+        for (int ig = 0; ig < C.gp; ++ig)
+            for (int k = 0; k < 8; ++k) out[(f * C.gp + ig) * 8 + k] = F[((f * 2 + stage) * C.gp + ig) * 8 + k];
+}
+
+}  // extern "C"

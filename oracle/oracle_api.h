@@ -1,0 +1,74 @@
+/*
+ * oracle_api.h -- C interface of the CPU oracle for the 2D GKS / WENO-AO / S2O4 step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The oracle is the checker for the CUDA path; nothing in the
+ * product (the hos_gb300 package and its CUDA library) includes, links or calls it.
+ * Two libraries implement this interface:
+ *   - liboracle.so    : the repository's own FP64 restatement (hos_oracle2d.cpp), which
+ *                       builds on any host and travels with the repository;
+ *   - _ref/libhosref.so : the unmodified reference sources compiled from where they lie plus
+ *                       a non-interactive driver (ref_driver.cpp); it only builds where the
+ *                       reference checkout exists and pins the restatement.
+ * Both export the same symbols with prefixes "oracle2d_" and "ref2d_".
+ *
+ * State layout is the reference's own: cell (i, j) at i*ny + j (y fastest) over the full
+ * block including ghost cells, 4 doubles per cell (rho, rho*u, rho*v, rho*E) -- the AoS
+ * order of Fluid2d::convar (include/fluid_mesh.h:125-160 in the reference).
+ */
+#ifndef HOS_ORACLE_API_H
+#define HOS_ORACLE_API_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Boundary kinds, one per side (left, right, down, up). */
+enum { HOS_BC_FREE = 0, HOS_BC_PERIODIC = 1, HOS_BC_REFLECT = 2, HOS_BC_INFLOW = 3 };
+
+typedef struct hos2d_params {
+    int nodex, nodey;     /* interior cells                                  */
+    int ghost;            /* ghost layers per side (reference drivers use 5) */
+    int order;            /* WENO-AO order: 5, 7 or 9                        */
+    int gausspoint;       /* Gauss points per face: 2 (5th), 3 (7th), 4 (9th)*/
+    int characteristic;   /* 1: characteristic variables, 0: conservative    */
+    int use_df;           /* 1: discontinuity-feedback variants (always 1 here) */
+    int K;                /* internal degrees of freedom (2D: K = 3 for gamma 1.4) */
+    double gamma;
+    double c1_euler, c2_euler;  /* numerical collision time coefficients     */
+    double cfl;
+    double left, right, down, up;
+    int bc[4];            /* left, right, down, up                           */
+    double bc_prim[4][4]; /* inflow primitive state per side (rho,u,v,p)     */
+} hos2d_params;
+
+/* ---- restatement (liboracle.so) ---- */
+int    oracle2d_init(const hos2d_params* p);
+void   oracle2d_free(void);
+void   oracle2d_set_threads(int n);
+void   oracle2d_set_state(const double* convar, const double* primvar);
+void   oracle2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);
+double oracle2d_begin_step(double tstop, double t);     /* CopyFluid_new_to_old + Get_CFL */
+int    oracle2d_stage(int stage, double dt);            /* one S2O4 stage; status 0 ok   */
+int    oracle2d_step(double tstop, double t, double* dt_out);
+/* Gauss-point states of the last stage: per face, per Gauss point, 36 doubles
+ * (left, right, centre) x (convar, der1x, der1y) x 4; faces (nx+1)*(ny+1), dir 0 = x. */
+void   oracle2d_get_gauss(int dir, double* out);
+/* Per-face, per-Gauss-point time-integrated flux f[4], derf[4] of stage s. */
+void   oracle2d_get_flux(int dir, int stage, double* out);
+
+/* ---- compiled reference (_ref/libhosref.so) ---- */
+int    ref2d_init(const hos2d_params* p);
+void   ref2d_free(void);
+void   ref2d_set_threads(int n);
+void   ref2d_set_state(const double* convar, const double* primvar);
+void   ref2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);
+double ref2d_begin_step(double tstop, double t);
+int    ref2d_stage(int stage, double dt);
+int    ref2d_step(double tstop, double t, double* dt_out);
+void   ref2d_get_gauss(int dir, double* out);
+void   ref2d_get_flux(int dir, int stage, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
