@@ -1,0 +1,41 @@
+// hos_face7.cu -- WENO7-AO-DF face kernels (x and y faces, FP64 and FP32 compute).
+#include "hos_launch.h"
+
+namespace hos {
+
+template <class T, int DIR>
+static cudaError_t launch_one(const FaceArgs& a, const Geometry& geo, cudaStream_t s) {
+    using S = FaceSmem<T, 7>;
+    const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;
+    const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;
+    dim3 grid((nodeT + TILE_T - 1) / TILE_T, (nodeN + 1 + TILE_N - 1) / TILE_N);
+    face_kernel<T, 7, DIR><<<grid, FACE_THREADS, S::bytes, s>>>(a, geo);
+    return cudaGetLastError();
+}
+
+// dynamic shared memory above 48 KB must be enabled per kernel on the current device
+cudaError_t configure_faces7(int precision) {
+    cudaError_t e;
+    if (precision == 0) {
+        if ((e = cudaFuncSetAttribute(face_kernel<double, 7, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)FaceSmem<double, 7>::bytes)) != cudaSuccess) return e;
+        return cudaFuncSetAttribute(face_kernel<double, 7, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)FaceSmem<double, 7>::bytes);
+    }
+    if ((e = cudaFuncSetAttribute(face_kernel<float, 7, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)FaceSmem<float, 7>::bytes)) != cudaSuccess) return e;
+    return cudaFuncSetAttribute(face_kernel<float, 7, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)FaceSmem<float, 7>::bytes);
+}
+
+cudaError_t launch_faces7(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s) {
+    cudaError_t e;
+    if (precision == 0) {
+        if ((e = launch_one<double, 0>(ax, geo, s)) != cudaSuccess) return e;
+        return launch_one<double, 1>(ay, geo, s);
+    }
+    if ((e = launch_one<float, 0>(ax, geo, s)) != cudaSuccess) return e;
+    return launch_one<float, 1>(ay, geo, s);
+}
+
+}  // namespace hos

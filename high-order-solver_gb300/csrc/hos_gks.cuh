@@ -1,0 +1,221 @@
+// hos_gks.cuh -- device math of the second-order gas-kinetic (GKS) flux at one Gauss point,
+// templated on the compute type T.
+//
+// Follows GKS2D (src/flux_function.cpp:345-698 in the reference project) for the branch the
+// hot path uses: gks2nd, Euler collision time (tau = 0, tau_num from c1/c2), S2O4 (two time
+// levels dt and dt/2).  The centre (g0) state is computed once here; the reference computes
+// the same collision twice (src/reconstruction.cpp:3652-3687 and again inside GKS2D).
+//
+// Maxwellian moments <u^i v^j xi^2k> (MMDF2d, src/basic_function.cpp:110-187) are formed on
+// the fly from the 1D half/full-space moment recurrences instead of materialising the three
+// 7x7x3 tables: the entry (i, j, k) is uplus[i] * vwhole[j] * xi_k exactly as the table
+// constructor computes it, so only the entries the contractions touch are ever evaluated.
+#pragma once
+#include "hos_weno.cuh"
+
+namespace hos {
+
+// half / full space moments of one Maxwellian
+template <class T> struct Mom {
+    T up[7], un[7], vw[7], xi2, xi4;
+    __device__ __forceinline__ void init(T u, T v, T lambda, T K) {
+        constexpr double pi = 3.14159265358979323846;
+        T uw[7];
+        uw[0] = T(1);
+        uw[1] = u;
+        up[0] = T(0.5) * erfc(sqrt(lambda) * -u);
+        un[0] = T(1.0) - up[0];
+        up[1] = u * up[0] + T(0.5) * (exp(-lambda * u * u) / sqrt(T(pi) * lambda));
+        un[1] = u - up[1];
+        const T ol = T(1.0) / lambda;
+#pragma unroll
+        for (int i = 2; i <= 6; ++i) uw[i] = u * uw[i - 1] + T(0.5 * (i - 1)) * ol * uw[i - 2];
+#pragma unroll
+        for (int i = 2; i <= 6; ++i) {
+            up[i] = u * up[i - 1] + T(0.5 * (i - 1)) * ol * up[i - 2];
+            un[i] = uw[i] - up[i];
+        }
+        vw[0] = T(1);
+        vw[1] = v;
+#pragma unroll
+        for (int i = 2; i <= 6; ++i) vw[i] = v * vw[i - 1] + T(0.5 * (i - 1)) * ol * vw[i - 2];
+        xi2 = T(0.5) * K * ol;
+        xi4 = T(0.25) * (K * K + T(2) * K) * ol * ol;
+    }
+};
+
+// table selectors: 0 = u > 0 half space, 1 = u < 0 half space, 2 = whole space
+template <class T, int TAB>
+__device__ __forceinline__ T M(const Mom<T>& m, int i, int j, int k) {
+    const T xk = k == 0 ? T(1) : k == 1 ? m.xi2 : m.xi4;
+    if (TAB == 0) return k == 0 ? m.up[i] * m.vw[j] : m.up[i] * m.vw[j] * xk;
+    if (TAB == 1) return k == 0 ? m.un[i] * m.vw[j] : m.un[i] * m.vw[j] * xk;
+    return k == 0 ? m.up[i] * m.vw[j] + m.un[i] * m.vw[j] : m.up[i] * m.vw[j] * xk + m.un[i] * m.vw[j] * xk;
+}
+
+// moment contraction <a psi u^NU v^NV> (GL_address / GR_address / G_address, :603-636)
+template <class T, int TAB, int NU, int NV>
+__device__ __forceinline__ void contract(const Mom<T>& m, const T* a, T* psi) {
+    constexpr int u = NU, v = NV;
+#define HM(i, j, k) M<T, TAB>(m, i, j, k)
+    psi[0] = a[0] * HM(u, v, 0) + a[1] * HM(u + 1, v, 0) + a[2] * HM(u, v + 1, 0) + a[3] * T(0.5) * (HM(u + 2, v, 0) + HM(u, v + 2, 0) + HM(u, v, 1));
+    psi[1] = a[0] * HM(u + 1, v, 0) + a[1] * HM(u + 2, v, 0) + a[2] * HM(u + 1, v + 1, 0) + a[3] * T(0.5) * (HM(u + 3, v, 0) + HM(u + 1, v + 2, 0) + HM(u + 1, v, 1));
+    psi[2] = a[0] * HM(u, v + 1, 0) + a[1] * HM(u + 1, v + 1, 0) + a[2] * HM(u, v + 2, 0) + a[3] * T(0.5) * (HM(u + 2, v + 1, 0) + HM(u, v + 3, 0) + HM(u, v + 1, 1));
+    psi[3] = T(0.5) * (a[0] * (HM(u + 2, v, 0) + HM(u, v + 2, 0) + HM(u, v, 1)) +
+                       a[1] * (HM(u + 3, v, 0) + HM(u + 1, v + 2, 0) + HM(u + 1, v, 1)) +
+                       a[2] * (HM(u + 2, v + 1, 0) + HM(u, v + 3, 0) + HM(u, v + 1, 1)) +
+                       a[3] * T(0.5) * (HM(u + 4, v, 0) + HM(u, v + 4, 0) + HM(u, v, 2) + T(2) * HM(u + 2, v + 2, 0) +
+                                        T(2) * HM(u + 2, v, 1) + T(2) * HM(u, v + 2, 1)));
+#undef HM
+}
+
+// micro-slope a from a macroscopic slope (A, src/basic_function.cpp:571-583)
+template <class T>
+__device__ __forceinline__ void microslope(T* a, const T* der, const T* prim, T K) {
+    const T overden = T(1.0) / prim[0];
+    const T q = prim[1] * prim[1] + prim[2] * prim[2] + T(0.5) * (K + T(2)) / prim[3];
+    const T R4 = der[3] * overden - T(0.5) * q * der[0] * overden;
+    const T R3 = (der[2] - prim[2] * der[0]) * overden;
+    const T R2 = (der[1] - prim[1] * der[0]) * overden;
+    a[3] = (T(4.0) / (K + T(2))) * prim[3] * prim[3] * (T(2) * R4 - T(2) * prim[1] * R2 - T(2) * prim[2] * R3);
+    a[2] = T(2) * prim[3] * R3 - prim[2] * a[3];
+    a[1] = T(2) * prim[3] * R2 - prim[1] * a[3];
+    a[0] = der[0] * overden - prim[1] * a[1] - prim[2] * a[2] - T(0.5) * a[3] * q;
+}
+
+template <class T>
+__device__ __forceinline__ void to_ulambda(T* pr, const T* w, T K) {
+    pr[0] = w[0];
+    pr[1] = w[1] / w[0];
+    pr[2] = w[2] / w[0];
+    pr[3] = lambda_of(w[0], pr[1], pr[2], w[3], K);
+}
+
+// Euler-type numerical collision time (Get_Tau, src/basic_function.cpp:663-708)
+template <class T>
+__device__ __forceinline__ T tau_num(T dl, T dr, T ll, T lr, T dt, T c1, T c2) {
+    if (c1 <= T(0) && c2 <= T(0)) return T(0.0);
+    const T Cc = c2 * fabsT(dl / ll - dr / lr) / fabsT(dl / ll + dr / lr);
+    return c1 * dt + dt * Cc;
+}
+
+// Gauss-point state: convar[4], der1x[4], der1y[4] of one side
+template <class T> struct GState { T w[4], dx[4], dy[4]; };
+
+// Time-integrated GKS flux at one Gauss point: fo = 4 F(dt/2) - F(dt),
+// dfo = 4 (F(dt) - 2 F(dt/2)) (src/flux_function.cpp:686-690).
+template <class T>
+__device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R, T dt, T K, T c1, T c2,
+                                          T* fo, T* dfo) {
+    T pl[4], pr[4], p0[4];
+    to_ulambda(pl, L.w, K);
+    to_ulambda(pr, R.w, K);
+    // partial results assembled into the two time levels at the end (same accumulation order
+    // as the reference): glu, gru and the <a u^2 + a u v> terms.  With tau = 0 the
+    // coefficient t[2] of the <A u> half-space terms is identically zero, so those terms
+    // (src/flux_function.cpp:528-567) are not formed.
+    T glu[4], gru[4], t1s[4], w0[4], c0x[4], c0y[4];
+    {
+        Mom<T> ml, mr;
+        ml.init(pl[1], pl[2], pl[3], K);
+        mr.init(pr[1], pr[2], pr[3], K);
+        // collision (Collision, src/basic_function.cpp:561-569)
+        w0[0] = pl[0] * ml.up[0] + pr[0] * mr.un[0];
+        w0[1] = pl[0] * ml.up[1] + pr[0] * mr.un[1];
+        w0[2] = pl[0] * ml.vw[1] * ml.up[0] + pr[0] * mr.vw[1] * mr.un[0];
+        w0[3] = T(0.5) * pl[0] * (ml.up[2] + ml.up[0] * ml.vw[2] + ml.up[0] * ml.xi2) +
+                T(0.5) * pr[0] * (mr.un[2] + mr.un[0] * mr.vw[2] + mr.un[0] * mr.xi2);
+        T alx[4], arx[4], aly[4], ary[4], q0[4], q1[4], q2[4], q3[4];
+        microslope(alx, L.dx, pl, K);
+        microslope(arx, R.dx, pr, K);
+        microslope(aly, L.dy, pl, K);
+        microslope(ary, R.dy, pr, K);
+        contract<T, 0, 0, 0>(ml, alx, q0);
+        contract<T, 1, 0, 0>(mr, arx, q1);
+        contract<T, 0, 0, 0>(ml, aly, q2);
+        contract<T, 1, 0, 0>(mr, ary, q3);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            c0x[v] = pl[0] * q0[v] + pr[0] * q1[v];
+            c0y[v] = pl[0] * q2[v] + pr[0] * q3[v];
+        }
+        const T unit[4] = {T(1), T(0.0), T(0.0), T(0.0)};
+        contract<T, 0, 1, 0>(ml, unit, glu);
+        contract<T, 1, 1, 0>(mr, unit, gru);
+        contract<T, 0, 2, 0>(ml, alx, q0);   // alxuul
+        contract<T, 1, 2, 0>(mr, arx, q1);   // arxuur
+        contract<T, 0, 1, 1>(ml, aly, q2);   // alyuvl
+        contract<T, 1, 1, 1>(mr, ary, q3);   // aryuvr
+#pragma unroll
+        for (int v = 0; v < 4; ++v) t1s[v] = pl[0] * (q0[v] + q2[v]) + pr[0] * (q1[v] + q3[v]);
+    }
+    to_ulambda(p0, w0, K);
+    T g0u[4], t4s[4], A0u[4];
+    {
+        Mom<T> m0;
+        m0.init(p0[1], p0[2], p0[3], K);
+        const T unit[4] = {T(1), T(0.0), T(0.0), T(0.0)};
+        contract<T, 2, 1, 0>(m0, unit, g0u);
+        T a0x[4], a0y[4], a0xu[4], a0xuu[4], a0yv[4], a0yuv[4];
+        microslope(a0x, c0x, p0, K);
+        contract<T, 2, 1, 0>(m0, a0x, a0xu);
+        contract<T, 2, 2, 0>(m0, a0x, a0xuu);
+        microslope(a0y, c0y, p0, K);
+        contract<T, 2, 0, 1>(m0, a0y, a0yv);
+        contract<T, 2, 1, 1>(m0, a0y, a0yuv);
+        T dA0[4], A0[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            t4s[v] = a0xuu[v] + a0yuv[v];
+            dA0[v] = -p0[0] * (a0xu[v] + a0yv[v]);
+        }
+        microslope(A0, dA0, p0, K);
+        contract<T, 2, 1, 0>(m0, A0, A0u);
+    }
+    // time-integration coefficients for tau = 0 (Euler) at dt and dt/2
+    T F0[4], F1[4];
+    {
+        const T tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt, c1, c2);
+        const T eta = exp(-dt / tn);
+        const T t0 = tn * (T(1) - eta);
+        const T t1 = tn * (eta * (dt + tn) - tn);
+        const T t3 = tn * eta + dt - tn;
+        const T t4 = tn * (tn - eta * (dt + tn));
+        const T t5 = T(0.5) * dt * dt;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            T f = pl[0] * t0 * glu[v] + pr[0] * t0 * gru[v];
+            f = f + p0[0] * t3 * g0u[v];
+            f = f + t1 * t1s[v];
+            f = f + p0[0] * t4 * t4s[v];
+            f = f + p0[0] * t5 * A0u[v];
+            F0[v] = f;
+        }
+    }
+    {
+        const T dt2 = T(0.5) * dt;
+        const T tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt2, c1, c2);
+        const T eta = exp(-dt2 / tn);
+        const T t0 = tn * (T(1) - eta);
+        const T t1 = tn * (eta * (dt2 + tn) - tn);
+        const T t3 = tn * eta + dt2 - tn;
+        const T t4 = tn * (tn - eta * (dt2 + tn));
+        const T t5 = T(0.5) * dt2 * dt2;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            T f = t0 * (pl[0] * glu[v] + pr[0] * gru[v]);
+            f = f + t1 * t1s[v];
+            f = f + p0[0] * t3 * g0u[v];
+            f = f + p0[0] * t4 * t4s[v];
+            f = f + p0[0] * t5 * A0u[v];
+            F1[v] = f;
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        fo[v] = (T(4.0) * F1[v] - F0[v]);
+        dfo[v] = T(4.0) * (F0[v] - T(2.0) * F1[v]);
+    }
+}
+
+}  // namespace hos

@@ -1,0 +1,434 @@
+// hos_kernels.cuh -- CUDA kernels of one S2O4 step on a uniform 2D block (sm_103a).
+//
+// Data layout in HBM (all FP64 regardless of the compute type T):
+//   W[4][nx*ny]        conserved variables, SoA planes, cell (i, j) at i*ny + j (the
+//                      reference's Fluid2d order, include/fluid_mesh.h:125-160), ghosts included
+//   Wold[4][nx*ny]     state at the start of the step (CopyFluid_new_to_old)
+//   AX, AY[nx*ny]      DF indicators alpha_x, alpha_y per cell (ghost entries stay 0)
+//   FX[4][nfx], FP[4][nfx], FAX[nfx]   x-face stage flux, stage-0 partial, face alpha
+//   FY[4][nfy], ...                     same for y-faces; faces indexed over the interior:
+//                      x-face (I, J), I in [0, nodex], J in [0, nodey): I*nodey + J
+//                      y-face (I, J), I in [0, nodex), J in [0, nodey]: I*(nodey+1) + J
+//   ctl                dt, t, CFL accumulator (bits of a positive double), status word
+//
+// One stage = bc_fill -> face_kernel<x> -> face_kernel<y> -> update_kernel.  The face
+// kernel fuses, for a tile of faces, the normal line reconstruction (staged in shared
+// memory), the tangential Gauss-point reconstruction (shared memory), the GKS flux per
+// Gauss point and the Gauss-weighted stage combination, so reconstructed interface states
+// never travel to HBM.
+#pragma once
+#include <cstdint>
+#include "hos_gks.cuh"
+
+namespace hos {
+
+struct StepCtl {
+    double dt;           // time step of the current step
+    double t;            // simulation time at the end of the current step
+    unsigned long long cfl_bits;  // running min of CFL candidates (positive doubles as bits)
+    unsigned int status; // bit 0: negative density/pressure or NaN (reference would exit)
+    unsigned int active; // 0 once t >= tstop: the step's kernels return without work
+};
+
+struct Geometry {
+    int nx, ny, g, nodex, nodey;
+    double dx, dy, cfl;
+    double gamma, K, c1, c2;
+    int characteristic;
+};
+
+// ------------------------------------------------------------------------------------------
+// ghost-cell fill: a single gather equal to the reference's sequential left, right, down, up
+// sweeps (src/boundary_condition.cpp:66-186, 244-258, 367-442): every ghost value comes from
+// an interior cell (or an inflow state) with the x-side rule applied first, then the y-side.
+// ------------------------------------------------------------------------------------------
+struct BcSpec {
+    int kind[4];          // left, right, down, up
+    double inflow[4][4];  // conserved inflow state per side
+};
+
+__device__ __forceinline__ int bc_map(int idx, int n_tot, int g, int node, int kind, bool low) {
+    if (kind == 0) return low ? g : n_tot - g - 1;                       // free: nearest interior
+    if (kind == 1) return low ? idx + node : idx - node;                 // periodic
+    return low ? 2 * g - 1 - idx : 2 * n_tot - 2 * g - 1 - idx;          // reflective
+}
+
+// ------------------------------------------------------------------------------------------
+// face kernel
+// ------------------------------------------------------------------------------------------
+struct FaceArgs {
+    const double* W;
+    const double* AN;   // DF alpha of the normal direction (alpha_x for x-faces)
+    const double* AT;   // DF alpha of the tangential direction
+    double* FX;         // stage flux combination [4][nf]
+    double* FP;         // stage-0 partial kept for stage 1 [4][nf]
+    double* FA;         // face DF indicator [nf]
+    const StepCtl* ctl;
+    int stage;
+};
+
+constexpr int TILE_N = 8;    // faces along the normal direction per tile
+constexpr int TILE_T = 16;   // faces along the tangential direction per tile
+constexpr int FACE_THREADS = 2 * TILE_N * TILE_T;
+
+template <int ORDER> struct GaussCount { static constexpr int GP = ORDER == 5 ? 2 : ORDER == 7 ? 3 : 4; };
+
+template <class T, int ORDER>
+struct FaceSmem {
+    static constexpr int r = ORDER / 2;
+    static constexpr int GP = GaussCount<ORDER>::GP;
+    static constexpr int TL = TILE_T + 2 * r;                      // line states along t
+    static constexpr int LINES = TILE_N * TL * 2 * 8;              // [fn][tl][side][8]
+    static constexpr int GSTATES = TILE_N * TILE_T * 2 * GP * 12;  // [face][side][gp][12]
+    static constexpr int FLUX = TILE_N * TILE_T * GP * 9;          // [face][gp][f4 d4 alpha]
+    static constexpr int UNION = LINES > FLUX ? LINES : FLUX;
+    static constexpr size_t bytes = sizeof(T) * (size_t)(UNION + GSTATES);
+};
+
+// Gauss weights of gausspoint 2 / 3 / 4 (SetGuassPoint, src/fluid_mesh.cpp:20-44)
+template <int GP>
+__device__ __forceinline__ double gauss_weight(int ig) {
+    if (GP == 2) return 0.5;
+    if (GP == 3) return ig == 0 ? 4.0 / 9.0 : 0.5 - 0.5 * (4.0 / 9.0);
+    return ig < 2 ? 1.0 / 12.0 : 5.0 / 12.0;
+}
+
+// DF indicator contribution of one Gauss point (Calculate_alpha_k, src/reconstruction.cpp:1463-1476);
+// y-face states are rotated back (XchangetoY) so the two Mach terms add in the reference order.
+template <class T, int DIR>
+__device__ __forceinline__ T alpha_k(const T* wl, const T* wr, T gamma) {
+    T pl[4], pr[4];
+    to_prim(pl, wl, gamma);
+    to_prim(pr, wr, gamma);
+    const T cl = sqrt(gamma * pl[3] / pl[0]);
+    const T cr = sqrt(gamma * pr[3] / pr[0]);
+    const T dn = pl[1] / cl - pr[1] / cr;
+    const T dtg = pl[2] / cl - pr[2] / cr;
+    T A = fabsT(pl[3] - pr[3]) / pl[3] + fabsT(pl[3] - pr[3]) / pr[3];
+    if (DIR == 0) A = A + dn * dn + dtg * dtg;
+    else A = A + dtg * dtg + dn * dn;
+    return A;
+}
+
+template <class T, int ORDER, int DIR>
+__global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry geo) {
+    using S = FaceSmem<T, ORDER>;
+    constexpr int r = S::r, N = ORDER, GP = S::GP, TL = S::TL;
+    constexpr int NW = AO<ORDER>::N;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* lines = reinterpret_cast<T*>(smem_raw);           // phase 1-2
+    T* flux = lines;                                     // phase 3-4 (aliases lines)
+    T* gst = lines + S::UNION;                           // phase 2-3
+
+    const int nx = geo.nx, ny = geo.ny, g = geo.g;
+    const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;  // faces along normal: nodeN + 1
+    const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;  // faces along tangent: nodeT
+    const T hN = T(DIR == 0 ? geo.dx : geo.dy);
+    const T hT = T(DIR == 0 ? geo.dy : geo.dx);
+    const T gamma = T(geo.gamma), K = T(geo.K);
+    const int N0 = blockIdx.y * TILE_N;   // first face index along the normal (0-based)
+    const int T0 = blockIdx.x * TILE_T;   // first face index along the tangent
+    const size_t plane = (size_t)nx * ny;
+    const int tid = threadIdx.x;
+    if (!a.ctl->active) return;
+    auto cidx = [&](int n, int t) -> size_t {
+        return DIR == 0 ? (size_t)n * ny + t : (size_t)t * ny + n;
+    };
+
+    // ---------------- phase 1: normal reconstruction of the tile's cells ----------------
+    // cells n in [g+N0-1, g+N0+TILE_N), t in [g+T0-r, g+T0+TILE_T+r)
+    for (int c = tid; c < (TILE_N + 1) * TL; c += FACE_THREADS) {
+        const int nl = c / TL, tl = c % TL;
+        const int n = g + N0 - 1 + nl;
+        const int t = g + T0 - r + tl;
+        const int tmax = DIR == 0 ? ny : nx;
+        if (n > g + nodeN || t >= tmax) continue;
+        T st[N][4], al[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const size_t ci = cidx(n + k - r, t);
+            T w[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) w[v] = T(a.W[v * plane + ci]);
+            if (DIR == 0) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) st[k][v] = w[v];
+            } else {  // YchangetoX: (u, v) -> (v, -u)
+                st[k][0] = w[0]; st[k][1] = w[2]; st[k][2] = -w[1]; st[k][3] = w[3];
+            }
+            al[k] = T(a.AN[ci]);
+        }
+        T df[NW];
+        df_factors<T, ORDER>(al, df);
+        T pn1[4], p0[4], pp1[4];
+        to_prim(pn1, st[r - 1], gamma);
+        to_prim(p0, st[r], gamma);
+        to_prim(pp1, st[r + 1], gamma);
+        T outv[2][8];
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            T base[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) base[v] = T(0.5) * ((side == 0 ? pn1[v] : pp1[v]) + p0[v]);
+            CharBase<T> cb;
+            T ch[N][4];
+            if (geo.characteristic) {
+                cb.init(base, gamma);
+#pragma unroll
+                for (int k = 0; k < N; ++k) cb.to_char(ch[k], st[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) ch[k][v] = st[k][v];
+            }
+            T var[4], der[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                T s[N], fw[NW], p[NW], px[NW];
+#pragma unroll
+                for (int k = 0; k < N; ++k) s[k] = ch[k][v];
+                ao_weights<T, ORDER>(s, fw);
+                if (side == 0) normal_face<T, ORDER, 0>(s, df, hN, p, px);
+                else normal_face<T, ORDER, 1>(s, df, hN, p, px);
+                T x = T(0.0), y = T(0.0);
+#pragma unroll
+                for (int k = 0; k < NW; ++k) { x += fw[k] * p[k]; y += fw[k] * px[k]; }
+                var[v] = x;
+                der[v] = y;
+            }
+            if (geo.characteristic) {
+                cb.from_char(outv[side], var);
+                cb.from_char(outv[side] + 4, der);
+            } else {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) { outv[side][v] = var[v]; outv[side][4 + v] = der[v]; }
+            }
+        }
+        // positivity fallback couples the two faces of the cell (src/reconstruction.cpp:1843-1858)
+        if (needs_order_reduction(outv[1], K) || needs_order_reduction(outv[0], K)) {
+#pragma unroll
+            for (int side = 0; side < 2; ++side)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) { outv[side][v] = st[r][v]; outv[side][4 + v] = T(0.0); }
+        }
+        // left-face value -> right side of face n; right-face value -> left side of face n+1
+        const int fl = n - (g + N0);
+        if (fl >= 0 && fl < TILE_N) {
+            T* d = lines + ((fl * TL + tl) * 2 + 1) * 8;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) d[q] = outv[0][q];
+        }
+        if (fl + 1 >= 0 && fl + 1 < TILE_N) {
+            T* d = lines + (((fl + 1) * TL + tl) * 2 + 0) * 8;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) d[q] = outv[1][q];
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase 2: tangential reconstruction, one (face, side) per thread ----------------
+    {
+        const int side = tid & 1;
+        const int fidx = tid >> 1;                 // face within the tile
+        const int fn = fidx / TILE_T, ft = fidx % TILE_T;
+        const int facen = N0 + fn, facet = T0 + ft;
+        if (facen <= nodeN && facet < nodeT) {
+            constexpr int sgn = DIR == 0 ? 1 : -1;  // y-face tangents run toward -x
+            const int tc = ft + r;                  // centre line index in the tile
+            const int ncell = g + facen - 1 + side; // cell column of this side
+            T al[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const int t = g + facet + sgn * (k - r);
+                al[k] = T(a.AT[cidx(ncell, t)]);
+            }
+            T df[NW];
+            df_factors<T, ORDER>(al, df);
+            auto line = [&](int k, int sd) -> const T* {
+                return lines + ((fn * TL + (tc + sgn * (k - r))) * 2 + sd) * 8;
+            };
+            const T* w0 = line(r, side);
+            T base[4], w0c[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) w0c[v] = w0[v];
+            to_prim(base, w0c, gamma);
+            T res[GP][12];
+            if (geo.characteristic) {
+                CharBase<T> cb;
+                cb.init(base, gamma);
+                T ch[N][4];
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    T w[4];
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) w[v] = line(k, side)[v];
+                    cb.to_char(ch[k], w);
+                }
+                if (ORDER == 9 && side == 1) {
+                    // the reference's right side keeps the left side's projection of the two
+                    // outermost entries (src/reconstruction.cpp:3318-3327)
+                    const T* l0 = line(r, 0);
+                    T b0[4], lw[4];
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) lw[v] = l0[v];
+                    to_prim(b0, lw, gamma);
+                    CharBase<T> cl;
+                    cl.init(b0, gamma);
+                    T w[4];
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) w[v] = line(0, 0)[v];
+                    cl.to_char(ch[0], w);
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) w[v] = line(N - 1, 0)[v];
+                    cl.to_char(ch[N - 1], w);
+                }
+                T gv[GP][4], gd[GP][4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    T s[N], fw[NW];
+#pragma unroll
+                    for (int k = 0; k < N; ++k) s[k] = ch[k][v];
+                    ao_weights<T, ORDER>(s, fw);
+#pragma unroll
+                    for (int ig = 0; ig < GP; ++ig) {
+                        T p[NW], px[NW];
+                        tangent_point<T, ORDER>(ig, s, df, hT, p, px);
+                        T x = T(0.0), y = T(0.0);
+#pragma unroll
+                        for (int k = 0; k < NW; ++k) { x += fw[k] * p[k]; y += fw[k] * px[k]; }
+                        gv[ig][v] = x;
+                        gd[ig][v] = y;
+                    }
+                }
+#pragma unroll
+                for (int ig = 0; ig < GP; ++ig) {
+                    cb.from_char(res[ig], gv[ig]);
+                    cb.from_char(res[ig] + 8, gd[ig]);
+                }
+            } else {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    T s[N], fw[NW];
+#pragma unroll
+                    for (int k = 0; k < N; ++k) s[k] = line(k, side)[v];
+                    ao_weights<T, ORDER>(s, fw);
+#pragma unroll
+                    for (int ig = 0; ig < GP; ++ig) {
+                        T p[NW], px[NW];
+                        tangent_point<T, ORDER>(ig, s, df, hT, p, px);
+                        T x = T(0.0), y = T(0.0);
+#pragma unroll
+                        for (int k = 0; k < NW; ++k) { x += fw[k] * p[k]; y += fw[k] * px[k]; }
+                        res[ig][v] = x;
+                        res[ig][8 + v] = y;
+                    }
+                }
+            }
+            // normal slope, reconstructed in conservative variables
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                T s[N], fw[NW];
+#pragma unroll
+                for (int k = 0; k < N; ++k) s[k] = line(k, side)[4 + v];
+                ao_weights<T, ORDER>(s, fw);
+#pragma unroll
+                for (int ig = 0; ig < GP; ++ig) {
+                    T p[NW], px[NW];
+                    tangent_point<T, ORDER>(ig, s, df, hT, p, px);
+                    T x = T(0.0);
+#pragma unroll
+                    for (int k = 0; k < NW; ++k) x += fw[k] * p[k];
+                    res[ig][4 + v] = x;
+                }
+            }
+            // positivity fallback per Gauss point (src/reconstruction.cpp:2764-2791)
+#pragma unroll
+            for (int ig = 0; ig < GP; ++ig) {
+                if (needs_order_reduction(res[ig], K)) {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        res[ig][v] = w0[v];
+                        res[ig][4 + v] = w0[4 + v];
+                        res[ig][8 + v] = T(0.0);
+                    }
+                }
+                T* d = gst + ((fidx * 2 + side) * GP + ig) * 12;
+#pragma unroll
+                for (int q = 0; q < 12; ++q) d[q] = res[ig][q];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase 3: GKS flux, one (face, Gauss point) per thread ----------------
+    const T dt = T(a.ctl->dt);
+    for (int item = tid; item < TILE_N * TILE_T * GP; item += FACE_THREADS) {
+        const int fidx = item / GP, ig = item % GP;
+        const int fn = fidx / TILE_T, ft = fidx % TILE_T;
+        if (N0 + fn > nodeN || T0 + ft >= nodeT) continue;
+        GState<T> L, R;
+        const T* sl = gst + ((fidx * 2 + 0) * GP + ig) * 12;
+        const T* sr = gst + ((fidx * 2 + 1) * GP + ig) * 12;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            L.w[v] = sl[v]; L.dx[v] = sl[4 + v]; L.dy[v] = sl[8 + v];
+            R.w[v] = sr[v]; R.dx[v] = sr[4 + v]; R.dy[v] = sr[8 + v];
+        }
+        T f[4], d[4];
+        gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
+        T* o = flux + (fidx * GP + ig) * 9;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { o[v] = f[v]; o[4 + v] = d[v]; }
+        o[8] = alpha_k<T, DIR>(L.w, R.w, gamma);
+    }
+    __syncthreads();
+
+    // ---------------- phase 4: Gauss-weighted S2O4 stage combination (FP64) ----------------
+    if (tid < TILE_N * TILE_T) {
+        const int fidx = tid, fn = fidx / TILE_T, ft = fidx % TILE_T;
+        const int facen = N0 + fn, facet = T0 + ft;
+        if (facen <= nodeN && facet < nodeT) {
+            const size_t nf = DIR == 0 ? (size_t)(geo.nodex + 1) * geo.nodey : (size_t)geo.nodex * (geo.nodey + 1);
+            const size_t fi = DIR == 0 ? (size_t)facen * geo.nodey + facet : (size_t)facet * (geo.nodey + 1) + facen;
+            double X[4], P[4];
+            double asum = 0.0;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) { X[v] = 0.0; P[v] = 0.0; }
+#pragma unroll
+            for (int ig = 0; ig < GP; ++ig) {
+                const T* o = flux + (fidx * GP + ig) * 9;
+                const double gw = gauss_weight<GP>(ig);
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const double fv = double(o[v]), dv = double(o[4 + v]);
+                    if (a.stage == 0) {
+                        X[v] += gw * (0.5 * fv + (1.0 / 8.0) * dv);
+                        P[v] += gw * (1.0 * fv + (1.0 / 6.0) * dv);
+                    } else {
+                        X[v] += gw * (0.0 * fv + (1.0 / 3.0) * dv);
+                    }
+                }
+                asum += double(o[8]);
+            }
+            // mean over Gauss points, zeroed below 2 (Calculate_alpha, :1497-1516)
+            double am = GP == 2 ? 0.5 * asum : GP == 3 ? asum / 3.0 : 0.25 * asum;
+            a.FA[fi] = am < 2.0 ? 0.0 : am;
+            if (a.stage == 1) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
+            }
+            // y-face local (normal, tangential) momentum -> global (Local_to_Global, :1226-1233)
+            double Xg[4] = {X[0], X[1], X[2], X[3]};
+            if (DIR == 1) { Xg[1] = -X[2]; Xg[2] = X[1]; }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) a.FX[v * nf + fi] = Xg[v];
+            if (a.stage == 0) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) a.FP[v * nf + fi] = P[v];
+            }
+        }
+    }
+}
+
+}  // namespace hos

@@ -1,0 +1,15 @@
+// hos_launch.h -- host-side launchers of the templated face kernels (one translation unit
+// per WENO-AO order so the three orders compile in parallel).
+#pragma once
+#include <cuda_runtime.h>
+#include "hos_kernels.cuh"
+
+namespace hos {
+// precision: 0 = FP64 compute, 1 = FP32 compute (state and accumulation stay FP64)
+cudaError_t configure_faces5(int precision);
+cudaError_t configure_faces7(int precision);
+cudaError_t configure_faces9(int precision);
+cudaError_t launch_faces5(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s);
+cudaError_t launch_faces7(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s);
+cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s);
+}  // namespace hos

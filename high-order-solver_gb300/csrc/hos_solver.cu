@@ -1,0 +1,593 @@
+// hos_solver.cu -- step kernels other than the face kernels, the C++ host solver and the
+// C ABI declared in include/hos_gb300.h.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/hos_gb300.h"
+#include "hos_launch.h"
+
+namespace hos {
+
+__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl) {
+    if (ctl && !ctl->active) return;
+    const int nx = geo.nx, ny = geo.ny, g = geo.g;
+    const long long nlr = 2LL * g * ny, ndu = 2LL * g * geo.nodex;
+    long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= nlr + ndu) return;
+    int i, j;
+    if (e < nlr) {
+        int il = (int)(e / ny);
+        j = (int)(e % ny);
+        i = il < g ? il : nx - 2 * g + il;
+    } else {
+        long long e2 = e - nlr;
+        int jl = (int)(e2 / geo.nodex);
+        i = g + (int)(e2 % geo.nodex);
+        j = jl < g ? jl : ny - 2 * g + jl;
+    }
+    const size_t plane = (size_t)nx * ny;
+    double out[4];
+    int si = i, sj = j;
+    bool flipu = false, flipv = false;
+    const bool yg = j < g || j >= ny - g;
+    const bool xg = i < g || i >= nx - g;
+    if (yg) {
+        const int side = j < g ? 2 : 3;
+        const int kind = bc.kind[side];
+        if (kind == 3) {
+            for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = bc.inflow[side][v];
+            return;
+        }
+        sj = bc_map(j, ny, g, geo.nodey, kind, side == 2);
+        flipv = kind == 2;
+    }
+    if (xg) {
+        const int side = i < g ? 0 : 1;
+        const int kind = bc.kind[side];
+        if (kind == 3) {
+            for (int v = 0; v < 4; ++v) out[v] = bc.inflow[side][v];
+            if (flipv) out[2] = -out[2];
+            for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = out[v];
+            return;
+        }
+        si = bc_map(i, nx, g, geo.nodex, kind, side == 0);
+        flipu = kind == 2;
+    }
+    const size_t src = (size_t)si * ny + sj;
+    for (int v = 0; v < 4; ++v) out[v] = W[v * plane + src];
+    if (flipu) out[1] = -out[1];
+    if (flipv) out[2] = -out[2];
+    for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = out[v];
+}
+
+
+// ------------------------------------------------------------------------------------------
+// update: W = Wold + (sum of face fluxes x length) / area over the interior cells
+// (Update_with_gauss, src/time_advance.cpp:431-474), the DF indicators of the cell
+// (Update_alpha, src/reconstruction.cpp:1523-1534) and, at stage 0, the CFL candidates of the
+// new state for the next step (Get_CFL / Dtx, src/time_advance.cpp:264-305: the reference
+// reads primitive variables refreshed at the start of the last stage).
+// ------------------------------------------------------------------------------------------
+struct UpdateArgs {
+    double* W;
+    double* Wold;
+    double* AX;
+    double* AY;
+    const double* FXx;  // x-face stage flux [4][nfx]
+    const double* FXy;  // y-face stage flux [4][nfy]
+    const double* FAx;
+    const double* FAy;
+    StepCtl* ctl;
+    int stage;
+};
+
+__device__ __forceinline__ void atomic_min_pos(unsigned long long* addr, double v) {
+    // positive doubles order like their bit patterns
+    atomicMin(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+__global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo) {
+    if (!a.ctl->active) return;
+    const int nodex = geo.nodex, nodey = geo.nodey, g = geo.g, ny = geo.ny;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    double cand = 1e300;
+    unsigned int bad = 0;
+    if (idx < nodex * nodey) {
+        const int I = idx / nodey, J = idx % nodey;
+        const size_t plane = (size_t)geo.nx * ny;
+        const size_t c = (size_t)(I + g) * ny + (J + g);
+        const size_t nfx = (size_t)(nodex + 1) * nodey, nfy = (size_t)nodex * (nodey + 1);
+        const size_t fl = (size_t)I * nodey + J, fr = fl + nodey;
+        const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
+        const double area = geo.dx * geo.dy;
+        double w[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            double old;
+            if (a.stage == 0) {
+                old = a.W[v * plane + c];
+                a.Wold[v * plane + c] = old;
+            } else {
+                old = a.Wold[v * plane + c];
+            }
+            double total = 0.0;
+            total += geo.dx * a.FXy[v * nfy + fd];
+            total += -geo.dx * a.FXy[v * nfy + fu];
+            total += geo.dy * a.FXx[v * nfx + fl];
+            total += -geo.dy * a.FXx[v * nfx + fr];
+            w[v] = old + total / area;
+            a.W[v * plane + c] = w[v];
+        }
+        const int jend = nodex < nodey ? nodex : nodey;
+        if (J < jend) {
+            a.AX[c] = a.FAx[fl] + a.FAx[fr];
+            a.AY[c] = a.FAy[fd] + a.FAy[fu];
+        }
+        double pr[4];
+        to_prim<double>(pr, w, geo.gamma);
+        if (pr[0] < 0 || pr[3] < 0 || isnan(pr[0]) || isnan(pr[3])) bad = 1;
+        if (a.stage == 0) {
+            const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] / pr[0]);
+            const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
+            if (qx > 0) cand = qx;
+            if (qy > 0 && qy < cand) cand = qy;
+        }
+    }
+    // block reduction of the CFL candidate and the status bit
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cand = fmin(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    __shared__ double sc[8];
+    __shared__ unsigned int sb[8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sc[wid] = cand; sb[wid] = bad; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = sc[0];
+        unsigned int b = sb[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmin(m, sc[k]); b |= sb[k]; }
+        if (a.stage == 0 && m < 1e300) atomic_min_pos(&a.ctl->cfl_bits, m);
+        if (b) atomicOr(&a.ctl->status, 1u);
+    }
+}
+
+// CFL candidates from a primitive state (the initial data's primvar at step 0)
+__global__ void __launch_bounds__(256) cfl_from_prim_kernel(const double* __restrict__ prim, Geometry geo, StepCtl* ctl) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    double cand = 1e300;
+    unsigned int bad = 0;
+    if (idx < geo.nodex * geo.nodey) {
+        const int I = idx / geo.nodey, J = idx % geo.nodey;
+        const size_t plane = (size_t)geo.nx * geo.ny;
+        const size_t c = (size_t)(I + geo.g) * geo.ny + (J + geo.g);
+        const double rho = prim[c], u = prim[plane + c], v = prim[2 * plane + c], p = prim[3 * plane + c];
+        const double tmp = sqrt(u * u + v * v) + sqrt(geo.gamma * p / rho);
+        const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
+        if (qx > 0) cand = qx;
+        if (qy > 0 && qy < cand) cand = qy;
+        if (rho < 0 || p < 0 || isnan(rho) || isnan(p)) bad = 1;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cand = fmin(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    __shared__ double sc[8];
+    __shared__ unsigned int sb[8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sc[wid] = cand; sb[wid] = bad; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = sc[0];
+        unsigned int b = sb[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmin(m, sc[k]); b |= sb[k]; }
+        if (m < 1e300) atomic_min_pos(&ctl->cfl_bits, m);
+        if (b) atomicOr(&ctl->status, 1u);
+    }
+}
+
+// step prologue: dt from the CFL accumulator (seeded with dx, as Get_CFL seeds with the
+// first cell's dx), clipped to the stop time (src/time_advance.cpp:285-289); the
+// accumulator is re-seeded for the candidates this step's stage 0 produces.
+__global__ void begin_step_kernel(StepCtl* ctl, double tstop, double seed) {
+    double dt = __longlong_as_double((long long)ctl->cfl_bits);
+    const double t = ctl->t;
+    // the driver loop runs while t < tstop; steps queued past it do nothing
+    ctl->active = t < tstop ? 1u : 0u;
+    if (!(t < tstop)) return;
+    if (t + dt > tstop) dt = tstop - t + 1e-16;
+    ctl->dt = dt;
+    ctl->t = t + dt;
+    ctl->cfl_bits = (unsigned long long)__double_as_longlong(seed);
+}
+
+
+// AoS [cells][4] <-> SoA [4][cells] transposes for the host-facing entry points
+__global__ void aos_to_soa_kernel(const double* __restrict__ aos, double* __restrict__ soa, size_t n) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    for (int v = 0; v < 4; ++v) soa[v * n + c] = aos[4 * c + v];
+}
+__global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __restrict__ aos, size_t n) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    for (int v = 0; v < 4; ++v) aos[4 * c + v] = soa[v * n + c];
+}
+// primitive variables of a conserved state (Convar_to_primvar_2D, src/basic_function.cpp:811-817)
+__global__ void prim_of_state_kernel(const double* __restrict__ W, double* __restrict__ P, size_t n, double gamma) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double w[4], p[4];
+    for (int v = 0; v < 4; ++v) w[v] = W[v * n + c];
+    to_prim<double>(p, w, gamma);
+    for (int v = 0; v < 4; ++v) P[v * n + c] = p[v];
+}
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+static int cuda_fail(cudaError_t e, const char* where) {
+    return fail(HOS_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace hos
+
+using namespace hos;
+
+struct hos_solver2d {
+    hos_params2d p;
+    int precision = 0;
+    Geometry geo;
+    BcSpec bc;
+    size_t ncell = 0, nfx = 0, nfy = 0;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    // device buffers
+    double* W = nullptr;
+    double* Wold = nullptr;
+    double* AX = nullptr;
+    double* AY = nullptr;
+    double* FXx = nullptr;
+    double* FPx = nullptr;
+    double* FAx = nullptr;
+    double* FXy = nullptr;
+    double* FPy = nullptr;
+    double* FAy = nullptr;
+    double* scratch = nullptr;  // 8 * ncell doubles: AoS staging + primitive planes
+    StepCtl* ctl = nullptr;
+    // captured step
+    cudaGraphExec_t graph = nullptr;
+    double graph_tstop = 0.0;
+};
+
+namespace {
+
+void free_all(hos_solver2d* s) {
+    double* bufs[] = {s->W, s->Wold, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->FXy, s->FPy, s->FAy, s->scratch};
+    for (double* b : bufs)
+        if (b) cudaFree(b);
+    if (s->ctl) cudaFree(s->ctl);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+int enqueue_stage(hos_solver2d* s, int stage) {
+    cudaError_t e;
+    const Geometry& geo = s->geo;
+    {
+        const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
+        bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "bc_fill");
+    }
+    FaceArgs ax{s->W, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->ctl, stage};
+    FaceArgs ay{s->W, s->AY, s->AX, s->FXy, s->FPy, s->FAy, s->ctl, stage};
+    switch (s->p.order) {
+        case 5: e = launch_faces5(s->precision, ax, ay, geo, s->stream); break;
+        case 7: e = launch_faces7(s->precision, ax, ay, geo, s->stream); break;
+        default: e = launch_faces9(s->precision, ax, ay, geo, s->stream); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
+    UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage};
+    const int n = geo.nodex * geo.nodey;
+    update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "update");
+    return HOS_OK;
+}
+
+int enqueue_begin(hos_solver2d* s, double tstop) {
+    begin_step_kernel<<<1, 1, 0, s->stream>>>(s->ctl, tstop, s->geo.dx);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "begin_step");
+}
+
+int enqueue_step(hos_solver2d* s, double tstop) {
+    int st = enqueue_begin(s, tstop);
+    if (st) return st;
+    for (int k = 0; k < 2; ++k)
+        if ((st = enqueue_stage(s, k)) != HOS_OK) return st;
+    return HOS_OK;
+}
+
+int reset_ctl_and_cfl(hos_solver2d* s, const double* dprim_soa) {
+    StepCtl c{};
+    c.dt = 0.0;
+    c.t = 0.0;
+    double seed = s->geo.dx;
+    std::memcpy(&c.cfl_bits, &seed, sizeof seed);
+    c.status = 0;
+    c.active = 1;
+    cudaError_t e = cudaMemcpyAsync(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "ctl upload");
+    const int n = s->geo.nodex * s->geo.nodey;
+    cfl_from_prim_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dprim_soa, s->geo, s->ctl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cfl_from_prim");
+    if ((e = cudaMemsetAsync(s->AX, 0, s->ncell * sizeof(double), s->stream)) != cudaSuccess) return cuda_fail(e, "memset");
+    if ((e = cudaMemsetAsync(s->AY, 0, s->ncell * sizeof(double), s->stream)) != cudaSuccess) return cuda_fail(e, "memset");
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "set_state");
+    StepCtl back;
+    if ((e = cudaMemcpy(&back, s->ctl, sizeof back, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "ctl read");
+    if (back.status & 1u) return fail(HOS_E_BLOWUP, "initial state has negative density/pressure or NaN");
+    return HOS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hos_last_error(void) { return g_last_error.c_str(); }
+
+int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) {
+    if (!params || !out) return fail(HOS_E_ARG, "null argument");
+    const hos_params2d& p = *params;
+    if (!(p.order == 5 || p.order == 7 || p.order == 9)) return fail(HOS_E_CONFIG, "order must be 5, 7 or 9");
+    const int need_gp = p.order == 5 ? 2 : p.order == 7 ? 3 : 4;
+    if (p.gausspoint != need_gp) return fail(HOS_E_CONFIG, "gausspoint must be 2/3/4 for order 5/7/9");
+    if (!p.use_df) return fail(HOS_E_CONFIG, "only the discontinuity-feedback variants are provided (use_df = 1)");
+    if (p.ghost < p.order / 2 + 1) return fail(HOS_E_CONFIG, "ghost must be >= order/2 + 1");
+    if (p.nodex < p.ghost || p.nodey < p.ghost) return fail(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
+    if (precision != HOS_FP64 && precision != HOS_FP32) return fail(HOS_E_CONFIG, "precision must be HOS_FP64 or HOS_FP32");
+    for (int k = 0; k < 4; ++k)
+        if (p.bc[k] < 0 || p.bc[k] > 3) return fail(HOS_E_CONFIG, "bad boundary kind");
+    if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC) ||
+        (p.bc[2] == HOS_BC_PERIODIC) != (p.bc[3] == HOS_BC_PERIODIC))
+        return fail(HOS_E_CONFIG, "periodic boundaries must be paired");
+    hos_solver2d* s = new (std::nothrow) hos_solver2d();
+    if (!s) return fail(HOS_E_NOMEM, "host allocation");
+    s->p = p;
+    s->precision = precision;
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e != cudaSuccess) { delete s; return cuda_fail(e, "cudaGetDevice"); }
+    Geometry& geo = s->geo;
+    geo.g = p.ghost;
+    geo.nodex = p.nodex;
+    geo.nodey = p.nodey;
+    geo.nx = p.nodex + 2 * p.ghost;
+    geo.ny = p.nodey + 2 * p.ghost;
+    geo.dx = (p.right - p.left) / p.nodex;
+    geo.dy = (p.up - p.down) / p.nodey;
+    geo.cfl = p.cfl;
+    geo.gamma = p.gamma;
+    geo.K = p.K;
+    geo.c1 = p.c1_euler;
+    geo.c2 = p.c2_euler;
+    geo.characteristic = p.characteristic ? 1 : 0;
+    for (int k = 0; k < 4; ++k) {
+        s->bc.kind[k] = p.bc[k];
+        const double* q = p.bc_prim[k];  // Primvar_to_convar_2D (src/basic_function.cpp:851-857)
+        s->bc.inflow[k][0] = q[0];
+        s->bc.inflow[k][1] = q[0] * q[1];
+        s->bc.inflow[k][2] = q[0] * q[2];
+        s->bc.inflow[k][3] = q[0] * (q[3] / q[0] / (p.gamma - 1) + 0.5 * (q[1] * q[1] + q[2] * q[2]));
+    }
+    s->ncell = (size_t)geo.nx * geo.ny;
+    s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;
+    s->nfy = (size_t)geo.nodex * (geo.nodey + 1);
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete s;
+        return cuda_fail(e, "stream");
+    }
+    struct { double** p; size_t n; } allocs[] = {
+        {&s->W, 4 * s->ncell}, {&s->Wold, 4 * s->ncell}, {&s->AX, s->ncell}, {&s->AY, s->ncell},
+        {&s->FXx, 4 * s->nfx}, {&s->FPx, 4 * s->nfx}, {&s->FAx, s->nfx},
+        {&s->FXy, 4 * s->nfy}, {&s->FPy, 4 * s->nfy}, {&s->FAy, s->nfy}, {&s->scratch, 8 * s->ncell}};
+    for (auto& a : allocs) {
+        if ((e = cudaMalloc(a.p, a.n * sizeof(double))) != cudaSuccess) {
+            free_all(s);
+            delete s;
+            return fail(HOS_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        cudaMemset(*a.p, 0, a.n * sizeof(double));
+    }
+    if ((e = cudaMalloc(&s->ctl, sizeof(StepCtl))) != cudaSuccess) {
+        free_all(s);
+        delete s;
+        return fail(HOS_E_NOMEM, "cudaMalloc ctl");
+    }
+    cudaMemset(s->ctl, 0, sizeof(StepCtl));
+    switch (p.order) {
+        case 5: e = configure_faces5(precision); break;
+        case 7: e = configure_faces7(precision); break;
+        default: e = configure_faces9(precision); break;
+    }
+    if (e != cudaSuccess) {
+        free_all(s);
+        delete s;
+        return cuda_fail(e, "configure face kernels");
+    }
+    *out = s;
+    return HOS_OK;
+}
+
+int hos2d_destroy(hos_solver2d* s) {
+    if (!s) return HOS_OK;
+    cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+    return HOS_OK;
+}
+
+int hos2d_dims(const hos_solver2d* s, int* nx, int* ny) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    if (nx) *nx = s->geo.nx;
+    if (ny) *ny = s->geo.ny;
+    return HOS_OK;
+}
+
+int hos2d_set_state(hos_solver2d* s, const double* convar, const double* primvar) {
+    if (!s || !convar) return fail(HOS_E_ARG, "null argument");
+    const size_t n = s->ncell;
+    double* stage = s->scratch;          // AoS staging [n][4]
+    double* prim = s->scratch + 4 * n;   // SoA primitive planes
+    cudaError_t e = cudaMemcpyAsync(stage, convar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "upload convar");
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    aos_to_soa_kernel<<<blocks, 256, 0, s->stream>>>(stage, s->W, n);
+    if (primvar) {
+        if ((e = cudaMemcpyAsync(stage, primvar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+            return cuda_fail(e, "upload primvar");
+        aos_to_soa_kernel<<<blocks, 256, 0, s->stream>>>(stage, prim, n);
+    } else {
+        prim_of_state_kernel<<<blocks, 256, 0, s->stream>>>(s->W, prim, n, s->geo.gamma);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "set_state");
+    return reset_ctl_and_cfl(s, prim);
+}
+
+int hos2d_set_state_device(hos_solver2d* s, const double* d_convar_soa, const double* d_primvar_soa) {
+    if (!s || !d_convar_soa) return fail(HOS_E_ARG, "null argument");
+    const size_t n = s->ncell;
+    double* prim = s->scratch + 4 * n;
+    cudaError_t e = cudaMemcpyAsync(s->W, d_convar_soa, 4 * n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "copy convar");
+    if (d_primvar_soa) {
+        e = cudaMemcpyAsync(prim, d_primvar_soa, 4 * n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream);
+    } else {
+        prim_of_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, prim, n, s->geo.gamma);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "copy primvar");
+    return reset_ctl_and_cfl(s, prim);
+}
+
+int hos2d_set_alpha(hos_solver2d* s, const double* alpha_x, const double* alpha_y) {
+    if (!s || !alpha_x || !alpha_y) return fail(HOS_E_ARG, "null argument");
+    cudaError_t e = cudaMemcpyAsync(s->AX, alpha_x, s->ncell * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->AY, alpha_y, s->ncell * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "set_alpha");
+}
+
+int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* alpha_x, double* alpha_y) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    const size_t n = s->ncell;
+    double* stage = s->scratch;
+    double* prim = s->scratch + 4 * n;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    cudaError_t e;
+    if (convar) {
+        soa_to_aos_kernel<<<blocks, 256, 0, s->stream>>>(s->W, stage, n);
+        if ((e = cudaMemcpyAsync(convar, stage, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+            return cuda_fail(e, "download convar");
+        if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "download convar");
+    }
+    if (primvar) {
+        prim_of_state_kernel<<<blocks, 256, 0, s->stream>>>(s->W, prim, n, s->geo.gamma);
+        soa_to_aos_kernel<<<blocks, 256, 0, s->stream>>>(prim, stage, n);
+        if ((e = cudaMemcpyAsync(primvar, stage, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+            return cuda_fail(e, "download primvar");
+        if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "download primvar");
+    }
+    if (alpha_x && (e = cudaMemcpyAsync(alpha_x, s->AX, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "download alpha_x");
+    if (alpha_y && (e = cudaMemcpyAsync(alpha_y, s->AY, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "download alpha_y");
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "get_state");
+    return HOS_OK;
+}
+
+int hos2d_begin_step(hos_solver2d* s, double tstop) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    return enqueue_begin(s, tstop);
+}
+
+int hos2d_boundary(hos_solver2d* s) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    const Geometry& geo = s->geo;
+    const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
+    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, nullptr);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "bc_fill");
+}
+
+int hos2d_stage(hos_solver2d* s, int stage) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    if (stage != 0 && stage != 1) return fail(HOS_E_ARG, "stage must be 0 or 1");
+    return enqueue_stage(s, stage);
+}
+
+int hos2d_step(hos_solver2d* s, double tstop) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    return enqueue_step(s, tstop);
+}
+
+int hos2d_advance(hos_solver2d* s, int nsteps, double tstop, int use_graph) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    if (nsteps < 0) return fail(HOS_E_ARG, "nsteps < 0");
+    cudaError_t e;
+    if (use_graph) {
+        if (!s->graph || s->graph_tstop != tstop) {
+            if (s->graph) {
+                cudaGraphExecDestroy(s->graph);
+                s->graph = nullptr;
+            }
+            cudaGraph_t g;
+            if ((e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                return cuda_fail(e, "begin capture");
+            int st = enqueue_step(s, tstop);
+            e = cudaStreamEndCapture(s->stream, &g);
+            if (st) return st;
+            if (e != cudaSuccess) return cuda_fail(e, "end capture");
+            e = cudaGraphInstantiate(&s->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+            s->graph_tstop = tstop;
+        }
+        for (int k = 0; k < nsteps; ++k)
+            if ((e = cudaGraphLaunch(s->graph, s->stream)) != cudaSuccess) return cuda_fail(e, "graph launch");
+        return HOS_OK;
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        int st = enqueue_step(s, tstop);
+        if (st) return st;
+    }
+    return HOS_OK;
+}
+
+int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "sync");
+    StepCtl c;
+    if ((e = cudaMemcpy(&c, s->ctl, sizeof c, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "ctl read");
+    if (t) *t = c.t;
+    if (dt) *dt = c.dt;
+    if (c.status & 1u) return fail(HOS_E_BLOWUP, "negative density/pressure or NaN in the state");
+    return HOS_OK;
+}
+
+int hos2d_launches_per_step(const hos_solver2d* s) {
+    (void)s;
+    return 1 + 2 * 4;  // begin_step + per stage (bc, x faces, y faces, update)
+}
+
+void* hos2d_stream(hos_solver2d* s) { return s ? (void*)s->stream : nullptr; }
+
+}  // extern "C"

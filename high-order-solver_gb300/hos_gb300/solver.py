@@ -1,0 +1,192 @@
+"""ctypes binding of the C ABI in include/hos_gb300.h.
+
+``Solver2D`` mirrors the reference's function-level stage API for this path
+(src/2Dproblem.cpp:128-157 in XJTUZhangHong/high-order-solver):
+
+    reference                                  this binding
+    CopyFluid_new_to_old + Get_CFL             Solver2D.get_cfl / begin_step
+    left/right/down/upboundary(...)            Solver2D.boundary
+    Convar_to_Primvar ... Update_alpha          Solver2D.stage(i)
+    loop body of the driver                    Solver2D.step
+    (blow-up exit(0) in Convar_to_Primvar)     HosBlowUp raised by sync()
+
+State arrays use the reference's cell order (i * ny + j, 4 doubles per cell).  There is no
+CPU fallback: without the CUDA library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .params import Params2D, Problem2D
+
+HOS_OK, HOS_E_BLOWUP, HOS_E_CONFIG, HOS_E_CUDA, HOS_E_ARG, HOS_E_NOMEM = range(6)
+FP64, FP32 = 0, 1
+
+_LIB = None
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+class HosError(RuntimeError):
+    pass
+
+
+class HosBlowUp(HosError):
+    """Negative density or pressure (or NaN) where the reference calls exit(0)
+    (Convar_to_Primvar, src/basic_function.cpp:752-773)."""
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "libhos_gb300.so"
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load the CUDA library; raises if it has not been built (no fallback path)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = Path(path) if path else library_path()
+    if not p.exists():
+        raise HosError(f"{p} is missing: build it with __graft_entry__.build() (nvcc, sm_103a)")
+    lib = ctypes.CDLL(str(p))
+    vp = ctypes.c_void_p
+    lib.hos2d_create.argtypes = [ctypes.POINTER(Params2D), ctypes.c_int, ctypes.POINTER(vp)]
+    lib.hos2d_destroy.argtypes = [vp]
+    lib.hos2d_dims.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    lib.hos2d_set_state.argtypes = [vp, _DP, _DP]
+    lib.hos2d_set_state_device.argtypes = [vp, vp, vp]
+    lib.hos2d_get_state.argtypes = [vp, _DP, _DP, _DP, _DP]
+    lib.hos2d_set_alpha.argtypes = [vp, _DP, _DP]
+    lib.hos2d_begin_step.argtypes = [vp, ctypes.c_double]
+    lib.hos2d_boundary.argtypes = [vp]
+    lib.hos2d_stage.argtypes = [vp, ctypes.c_int]
+    lib.hos2d_step.argtypes = [vp, ctypes.c_double]
+    lib.hos2d_advance.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    lib.hos2d_sync.argtypes = [vp, _DP, _DP]
+    lib.hos2d_launches_per_step.argtypes = [vp]
+    lib.hos2d_stream.argtypes = [vp]
+    lib.hos2d_stream.restype = vp
+    lib.hos_last_error.restype = ctypes.c_char_p
+    _LIB = lib
+    return lib
+
+
+def _check(code: int) -> None:
+    if code == HOS_OK:
+        return
+    msg = load().hos_last_error().decode(errors="replace")
+    if code == HOS_E_BLOWUP:
+        raise HosBlowUp(msg)
+    raise HosError(f"hos error {code}: {msg}")
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_DP)
+
+
+class Solver2D:
+    """One 2D problem resident on the current CUDA device."""
+
+    def __init__(self, problem: Problem2D, precision: int = FP64):
+        self.problem = problem
+        self.precision = precision
+        self._lib = load()
+        self._params = problem.to_c()
+        h = ctypes.c_void_p()
+        _check(self._lib.hos2d_create(ctypes.byref(self._params), precision, ctypes.byref(h)))
+        self._h = h
+        nx, ny = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.hos2d_dims(h, ctypes.byref(nx), ctypes.byref(ny)))
+        self.nx, self.ny = nx.value, ny.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hos2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ---------------------------------------------------------------------------
+    def set_state(self, convar: np.ndarray, primvar: np.ndarray | None = None) -> None:
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        if c.size != self.nx * self.ny * 4:
+            raise ValueError("convar must hold nx*ny*4 values")
+        p = None if primvar is None else np.ascontiguousarray(primvar, dtype=np.float64).reshape(-1)
+        _check(self._lib.hos2d_set_state(self._h, _ptr(c), _ptr(p)))
+
+    def set_state_device(self, convar_soa_ptr: int, primvar_soa_ptr: int | None = None) -> None:
+        _check(self._lib.hos2d_set_state_device(self._h, ctypes.c_void_p(convar_soa_ptr),
+                                                 ctypes.c_void_p(primvar_soa_ptr or 0) if primvar_soa_ptr else None))
+
+    def set_alpha(self, alpha_x: np.ndarray, alpha_y: np.ndarray) -> None:
+        ax = np.ascontiguousarray(alpha_x, dtype=np.float64).reshape(-1)
+        ay = np.ascontiguousarray(alpha_y, dtype=np.float64).reshape(-1)
+        if ax.size != self.nx * self.ny or ay.size != self.nx * self.ny:
+            raise ValueError("alpha arrays must hold nx*ny values")
+        _check(self._lib.hos2d_set_alpha(self._h, _ptr(ax), _ptr(ay)))
+
+    def get_state(self, primvar: bool = False):
+        n = self.nx * self.ny
+        c = np.empty(4 * n)
+        p = np.empty(4 * n) if primvar else None
+        ax = np.empty(n)
+        ay = np.empty(n)
+        _check(self._lib.hos2d_get_state(self._h, _ptr(c), _ptr(p), _ptr(ax), _ptr(ay)))
+        out = dict(convar=c.reshape(self.nx, self.ny, 4), alpha_x=ax.reshape(self.nx, self.ny),
+                   alpha_y=ay.reshape(self.nx, self.ny))
+        if primvar:
+            out["primvar"] = p.reshape(self.nx, self.ny, 4)
+        return out
+
+    # -- the reference's stage-level API --------------------------------------------------
+    def begin_step(self, tstop: float) -> None:
+        _check(self._lib.hos2d_begin_step(self._h, tstop))
+
+    def get_cfl(self, tstop: float) -> float:
+        """CopyFluid_new_to_old + Get_CFL; returns this step's dt (synchronises)."""
+        self.begin_step(tstop)
+        return self.sync()[1]
+
+    def boundary(self) -> None:
+        _check(self._lib.hos2d_boundary(self._h))
+
+    def stage(self, i: int) -> None:
+        _check(self._lib.hos2d_stage(self._h, i))
+
+    def step(self, tstop: float) -> None:
+        _check(self._lib.hos2d_step(self._h, tstop))
+
+    def advance(self, nsteps: int, tstop: float, graph: bool = True) -> None:
+        _check(self._lib.hos2d_advance(self._h, nsteps, tstop, 1 if graph else 0))
+
+    def sync(self) -> tuple[float, float]:
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        _check(self._lib.hos2d_sync(self._h, ctypes.byref(t), ctypes.byref(dt)))
+        return t.value, dt.value
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(self._lib.hos2d_launches_per_step(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.hos2d_stream(self._h) or 0)
+
+    def run(self, tstop: float, max_steps: int = 10**9, graph: bool = True, check_every: int = 50) -> int:
+        """Advance until t >= tstop (the driver's while loop); returns steps taken."""
+        steps = 0
+        t, _ = self.sync()
+        while t < tstop and steps < max_steps:
+            k = min(check_every, max_steps - steps)
+            self.advance(k, tstop, graph=graph)
+            steps += k
+            t, _ = self.sync()
+        return steps

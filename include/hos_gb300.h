@@ -1,0 +1,119 @@
+/*
+ * hos_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the high-order-solver 2D
+ * per-step hot path: WENO5/7/9-AO reconstruction with the discontinuity-feedback factor,
+ * the second-order gas-kinetic (GKS) flux, the two-stage fourth-order (S2O4) update, the
+ * ghost-cell fill and the CFL time-step reduction.
+ *
+ * Plain C types only (pointers, sizes, doubles); no CUDA or C++ types cross this boundary.
+ * Every function returns an int status: 0 ok, HOS_E_* otherwise.  Nothing calls exit().
+ *
+ * Reference interface replaced (XJTUZhangHong/high-order-solver, file:line):
+ *   problem setup globals + Block2d + allocators ... src/2Dproblem.cpp:7-81,
+ *        include/fluid_mesh.h:82-222, src/basic_function.cpp:1310-1491   -> hos2d_create
+ *   Fluid2d::convar / primvar of the initial data .... src/2Dproblem.cpp:345-385 -> hos2d_set_state
+ *   reading Fluid2d arrays back (output2d) ............ src/output.cpp:64-84     -> hos2d_get_state
+ *   CopyFluid_new_to_old + Get_CFL ..................... src/basic_function.cpp:1571-1584,
+ *                                                        src/time_advance.cpp:264-305 -> hos2d_begin_step
+ *   the four BoundaryCondition2d calls ................. src/boundary_condition.cpp:66-442 -> hos2d_boundary
+ *   one stage: BCs, Convar_to_Primvar, Reconstruction_within_cell, Reconstruction_forg0,
+ *     Calculate_flux, Update, Update_alpha ............. src/2Dproblem.cpp:137-157  -> hos2d_stage
+ *   one time step (the body of the driver's while loop) src/2Dproblem.cpp:128-159  -> hos2d_step
+ */
+#ifndef HOS_GB300_H
+#define HOS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define HOS_OK 0
+#define HOS_E_BLOWUP 1      /* negative density/pressure or NaN: where the reference exits */
+#define HOS_E_CONFIG 2      /* unsupported or inconsistent parameters                    */
+#define HOS_E_CUDA 3        /* CUDA runtime error (no device, launch failure, ...)       */
+#define HOS_E_ARG 4         /* null pointer or bad argument                              */
+#define HOS_E_NOMEM 5       /* device allocation failed                                  */
+
+/* boundary kinds, per side (left, right, down, up) */
+#define HOS_BC_FREE 0       /* free_boundary_*  (zero-gradient outflow)  */
+#define HOS_BC_PERIODIC 1   /* periodic_boundary_*                       */
+#define HOS_BC_REFLECT 2    /* reflection_boundary_*                     */
+#define HOS_BC_INFLOW 3     /* inflow_boundary_* with a fixed primitive state */
+
+/* compute precision of reconstruction and flux; state, stage combination and the CFL
+ * reduction are FP64 in both */
+#define HOS_FP64 0
+#define HOS_FP32 1
+
+/* Problem parameters: the globals and Block2d fields a reference 2D driver sets
+ * (src/2Dproblem.cpp:7-81).  Gausspoint must match the order: 5 -> 2, 7 -> 3, 9 -> 4. */
+typedef struct hos_params2d {
+    int nodex, nodey;       /* interior cells (Block2d::nodex / nodey)          */
+    int ghost;              /* ghost layers (Block2d::ghost), >= order/2 + 1    */
+    int order;              /* WENO-AO order: 5, 7 or 9                         */
+    int gausspoint;         /* Gauss points per face                           */
+    int characteristic;     /* reconstruction_variable: 1 characteristic, 0 conservative */
+    int use_df;             /* is_using_df_factor; must be 1                   */
+    int K;                  /* internal degrees of freedom                      */
+    double gamma;           /* Gamma                                            */
+    double c1_euler, c2_euler; /* numerical collision time tau_num = c1 dt + c2 dt |dp|/|p| */
+    double cfl;             /* Block2d::CFL                                     */
+    double left, right, down, up;  /* domain                                   */
+    int bc[4];              /* HOS_BC_* for left, right, down, up               */
+    double bc_prim[4][4];   /* inflow primitive state (rho, u, v, p) per side   */
+} hos_params2d;
+
+typedef struct hos_solver2d hos_solver2d;
+
+/* Allocate the device state for one problem on the current CUDA device. */
+int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out);
+int hos2d_destroy(hos_solver2d* s);
+
+/* Block sizes: nx = nodex + 2 ghost, ny = nodey + 2 ghost; state arrays hold nx*ny cells,
+ * cell (i, j) at i*ny + j, 4 doubles per cell (the reference's Fluid2d order). */
+int hos2d_dims(const hos_solver2d* s, int* nx, int* ny);
+
+/* Upload the conserved state (host, [nx*ny][4]) and optionally the primitive state the
+ * first step's CFL reads (host, [nx*ny][4], may be NULL: then derived from convar).
+ * Resets time to 0 and the DF indicators to 0.  Synchronous. */
+int hos2d_set_state(hos_solver2d* s, const double* convar, const double* primvar);
+/* Same from device memory already resident in HBM (SoA planes [4][nx*ny]). */
+int hos2d_set_state_device(hos_solver2d* s, const double* d_convar_soa, const double* d_primvar_soa);
+
+/* Restore the DF indicators alpha_x, alpha_y (host, [nx*ny]) of a state captured mid-run
+ * (Fluid2d::alpha_x / alpha_y, include/fluid_mesh.h:146-147).  Synchronous. */
+int hos2d_set_alpha(hos_solver2d* s, const double* alpha_x, const double* alpha_y);
+
+/* Download conserved state, primitive state of the last stage, alpha_x, alpha_y
+ * (host arrays; any pointer may be NULL).  Synchronous. */
+int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* alpha_x, double* alpha_y);
+
+/* CopyFluid_new_to_old + Get_CFL: fix this step's dt (clipped to tstop). Asynchronous. */
+int hos2d_begin_step(hos_solver2d* s, double tstop);
+/* Ghost-cell fill only. Asynchronous. */
+int hos2d_boundary(hos_solver2d* s);
+/* One S2O4 stage (0 or 1) with the dt fixed by hos2d_begin_step. Asynchronous. */
+int hos2d_stage(hos_solver2d* s, int stage);
+/* One full time step (begin_step + two stages). Asynchronous. */
+int hos2d_step(hos_solver2d* s, double tstop);
+/* nsteps full steps; replays a captured CUDA graph of one step when use_graph != 0. */
+int hos2d_advance(hos_solver2d* s, int nsteps, double tstop, int use_graph);
+
+/* Wait for queued work; report time, last dt and the blow-up status (HOS_E_BLOWUP). */
+int hos2d_sync(hos_solver2d* s, double* t, double* dt);
+
+/* Number of kernel launches one hos2d_step enqueues. */
+int hos2d_launches_per_step(const hos_solver2d* s);
+
+/* The CUDA stream the solver enqueues on (as an opaque pointer, for event timing). */
+void* hos2d_stream(hos_solver2d* s);
+
+/* Human-readable text of the last error on this thread. */
+const char* hos_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HOS_GB300_H */

@@ -1,0 +1,71 @@
+"""Generate the golden vectors under tests/golden/ by running the COMPILED REFERENCE
+(oracle/_ref/libhosref.so, built from the reference sources by oracle/Makefile) on small
+seeded cases.  Run from the repository root where the reference checkout exists:
+
+    python tests/golden/make_golden.py
+
+Each case stores the initial conserved/primitive state, the reference state (convar,
+alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps.  The 2D
+accuracy entries store the reference's own known-answer test (sinwave_2d,
+src/2Dproblem.cpp:1347-1603): L1/L2/Linf density errors at t = 2 on 10^2 and 20^2 meshes.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / "high-order-solver_gb300"))
+sys.path.insert(0, str(ROOT / "tests"))
+
+from hos_gb300 import cases  # noqa: E402
+from oracle_lib import CpuStep  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def step_cases():
+    yield "riemann_w5_char_24", cases.riemann2d(24, order=5)
+    yield "riemann_w7_char_24", cases.riemann2d(24, order=7)
+    yield "riemann_w9_char_24", cases.riemann2d(24, order=9)
+    yield "riemann_w7_cons_24", cases.riemann2d(24, order=7, characteristic=False)
+    yield "rriemann_w7_s11_20", cases.random_riemann2d(20, seed=11, order=7)
+    yield "vortex_w5_char_20", cases.isentropic_vortex(20, order=5)
+    yield "sinwave_w9_cons_16", cases.sinwave2d(16, order=9)
+
+
+def sinwave_errors(n, tstop=2.0):
+    pb, con, prim = cases.sinwave2d(n, order=9)
+    r = CpuStep("ref").init(pb)
+    r.set_state(con, prim)
+    while r.t < tstop:
+        r.step(tstop)
+    rho = r.state()["convar"][..., 0]
+    g = pb.ghost
+    exact = prim[..., 0]  # exact cell averages are periodic in t = 2 (one period)
+    e = np.abs(rho - exact)[g:-g, g:-g]
+    return np.array([e.mean(), np.sqrt((e * e).mean()), e.max()])
+
+
+def main():
+    for name, (pb, con, prim) in step_cases():
+        r = CpuStep("ref").init(pb)
+        r.set_state(con, prim)
+        dts = [r.step()]
+        s1 = r.state()
+        dts += [r.step(), r.step()]
+        s3 = r.state()
+        np.savez_compressed(OUT / f"{name}.npz", convar0=con, primvar0=prim,
+                            convar1=s1["convar"], alpha_x1=s1["alpha_x"], alpha_y1=s1["alpha_y"],
+                            convar3=s3["convar"], alpha_x3=s3["alpha_x"], alpha_y3=s3["alpha_y"],
+                            dts=np.array(dts))
+        print(name, dts)
+    errs = {f"n{n}": sinwave_errors(n) for n in (10, 20)}
+    np.savez_compressed(OUT / "sinwave_w9_accuracy.npz", **errs)
+    print(errs)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,101 @@
+"""Loaders for the two CPU implementations of the 2D step used as checkers:
+the repository's FP64 restatement (oracle/liboracle.so) and, where it could be built,
+the compiled reference (oracle/_ref/libhosref.so).  Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+ORACLE_DIR = ROOT / "oracle"
+REFERENCE = Path("/root/reference")
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+def _make(target=None):
+    cmd = ["make", "-s", "-C", str(ORACLE_DIR), f"-j{os.cpu_count() or 4}"]
+    if target:
+        cmd.append(target)
+    subprocess.run(cmd, check=True, capture_output=True)
+
+
+class CpuStep:
+    """One CPU implementation of the 2D step behind the oracle_api.h interface."""
+
+    def __init__(self, kind: str = "oracle"):
+        if kind == "oracle":
+            path, self.pre = ORACLE_DIR / "liboracle.so", "oracle2d_"
+            if not path.exists():
+                _make()
+        else:
+            path, self.pre = ORACLE_DIR / "_ref" / "libhosref.so", "ref2d_"
+            if not path.exists():
+                if not (REFERENCE / "src").is_dir():
+                    raise FileNotFoundError("reference checkout not present")
+                _make("ref")
+        self.lib = ctypes.CDLL(str(path))
+        self.fn("begin_step").restype = ctypes.c_double
+
+    def fn(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def init(self, pb, threads: int | None = None):
+        self.pb = pb
+        self.params = pb.to_c()
+        st = self.fn("init")(ctypes.byref(self.params))
+        if st != 0:
+            raise RuntimeError(f"init failed: {st}")
+        self.fn("set_threads")(threads or os.cpu_count() or 1)
+        self.t = 0.0
+        return self
+
+    def set_state(self, convar, primvar=None):
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        p = None if primvar is None else np.ascontiguousarray(primvar, dtype=np.float64).reshape(-1)
+        self._keep = (c, p)
+        self.fn("set_state")(c.ctypes.data_as(_DP), None if p is None else p.ctypes.data_as(_DP))
+        self.t = 0.0
+
+    def step(self, tstop: float = 1e30) -> float:
+        dt = ctypes.c_double()
+        st = self.fn("step")(ctypes.c_double(tstop), ctypes.c_double(self.t), ctypes.byref(dt))
+        if st != 0:
+            raise RuntimeError(f"blow-up (status {st})")
+        self.t += dt.value
+        return dt.value
+
+    def state(self):
+        nx, ny = self.pb.nx, self.pb.ny
+        c = np.empty(nx * ny * 4)
+        p = np.empty(nx * ny * 4)
+        ax = np.empty(nx * ny)
+        ay = np.empty(nx * ny)
+        self.fn("get_state")(c.ctypes.data_as(_DP), p.ctypes.data_as(_DP), ax.ctypes.data_as(_DP), ay.ctypes.data_as(_DP))
+        return dict(convar=c.reshape(nx, ny, 4), primvar=p.reshape(nx, ny, 4),
+                    alpha_x=ax.reshape(nx, ny), alpha_y=ay.reshape(nx, ny))
+
+    def gauss(self, direction: int):
+        nf = (self.pb.nx + 1) * (self.pb.ny + 1)
+        gp = self.params.gausspoint
+        out = np.empty(nf * gp * 36)
+        self.fn("get_gauss")(direction, out.ctypes.data_as(_DP))
+        return out.reshape(self.pb.nx + 1, self.pb.ny + 1, gp, 36)
+
+
+def ref_available() -> bool:
+    return (ORACLE_DIR / "_ref" / "libhosref.so").exists() or (REFERENCE / "src").is_dir()
+
+
+def interior(pb, a):
+    g = pb.ghost
+    return a[g:g + pb.nodex, g:g + pb.nodey]
+
+
+def rel_linf(a, b, pb):
+    a = interior(pb, a)
+    b = interior(pb, b)
+    return float(np.abs(a - b).max() / np.abs(b).max())

@@ -1,0 +1,232 @@
+"""GPU parity of the CUDA step against the oracle and the reference's golden vectors.
+
+Tolerances: the plain FP64 path must agree with the reference CPU solver to 1e-12 relative
+L-inf per step (max |W_gpu - W_ref| / max |W_ref| over interior cells, all 4 variables).
+The FP32-bulk path is bounded separately (relative L1 of density vs the FP64 run)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from hos_gb300 import cases
+from hos_gb300.solver import FP32, FP64, HosBlowUp, Solver2D
+from oracle_lib import CpuStep, interior, rel_linf
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+TOL_FP64 = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as ge
+    ge.build()
+
+
+def gpu_run(pb, con, prim, nsteps, precision=FP64, tstop=1e30, graph=False, alpha=None):
+    s = Solver2D(pb, precision)
+    s.set_state(con, prim)
+    if alpha is not None:
+        s.set_alpha(*alpha)
+    dts = []
+    for _ in range(nsteps):
+        if graph:
+            s.advance(1, tstop, graph=True)
+        else:
+            s.step(tstop)
+        dts.append(s.sync()[1])
+    st = s.get_state()
+    st["dts"] = dts
+    st["t"] = s.sync()[0]
+    s.close()
+    return st
+
+
+def oracle_run(pb, con, prim, nsteps, tstop=1e30):
+    o = CpuStep("oracle").init(pb)
+    o.set_state(con, prim)
+    dts = [o.step(tstop) for _ in range(nsteps)]
+    st = o.state()
+    st["dts"] = dts
+    return st
+
+
+GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem)
+
+
+def _golden_problem(name):
+    from test_oracle_cpu import _problem
+    return _problem(name)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_gpu_matches_reference_golden(name):
+    pb, _, _ = _golden_problem(name)
+    gold = np.load(GOLDEN / f"{name}.npz")
+    s1 = gpu_run(pb, gold["convar0"], gold["primvar0"], 1)
+    assert rel_linf(s1["convar"], gold["convar1"], pb) <= TOL_FP64
+    s3 = gpu_run(pb, gold["convar0"], gold["primvar0"], 3)
+    assert rel_linf(s3["convar"], gold["convar3"], pb) <= TOL_FP64
+    np.testing.assert_allclose(s3["dts"], gold["dts"], rtol=1e-14, atol=0)
+    for k in ("alpha_x3", "alpha_y3"):
+        a, b = s3[k[:-1]], gold[k]
+        assert np.abs(a - b).max() <= 1e-9 * max(1.0, np.abs(b).max())
+
+
+@pytest.mark.parametrize("order", [5, 7, 9])
+@pytest.mark.parametrize("charac", [True, False])
+@pytest.mark.parametrize("bc", ["free", "periodic", "reflect"])
+def test_gpu_step_parity_vs_oracle(order, charac, bc):
+    pb, con, prim = cases.random_riemann2d(40, seed=order + 3 * len(bc), order=order)
+    pb.characteristic = charac
+    pb.bc = (bc,) * 4
+    ref = oracle_run(pb, con, prim, 2)
+    got = gpu_run(pb, con, prim, 2)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+    np.testing.assert_allclose(got["dts"], ref["dts"], rtol=1e-14)
+
+
+def test_gpu_single_step_from_midrun_state():
+    """Per-step parity from the same mid-run state (DF indicators and lagged primitives set)."""
+    pb, con, prim = cases.riemann2d(48, order=7)
+    o = CpuStep("oracle").init(pb)
+    o.set_state(con, prim)
+    for _ in range(4):
+        o.step()
+    mid = o.state()
+    o.step()
+    nxt = o.state()
+    s = Solver2D(pb)
+    s.set_state(mid["convar"], mid["primvar"])
+    s.set_alpha(mid["alpha_x"], mid["alpha_y"])
+    s.step(1e30)
+    s.sync()
+    got = s.get_state()
+    s.close()
+    assert rel_linf(got["convar"], nxt["convar"], pb) <= TOL_FP64
+    assert np.abs(got["alpha_x"] - nxt["alpha_x"]).max() <= 1e-9 * max(1.0, np.abs(nxt["alpha_x"]).max())
+
+
+def test_gpu_inflow_reflect_boundaries():
+    pb, con, prim = cases.random_riemann2d(32, seed=5, order=5)
+    pb.bc = ("inflow", "free", "reflect", "free")
+    pb.bc_prim = ((1.2, 0.8, 0.1, 1.1), (0,) * 4, (0,) * 4, (0,) * 4)
+    ref = oracle_run(pb, con, prim, 3)
+    got = gpu_run(pb, con, prim, 3)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+
+
+def test_gpu_rectangular_domain():
+    pb, con, prim = cases.random_riemann2d(40, seed=9, order=7)
+    pb.nodey = 24
+    pb.up = 0.6
+    con = con[:, : pb.ny].copy()
+    prim = prim[:, : pb.ny].copy()
+    ref = oracle_run(pb, con, prim, 2)
+    got = gpu_run(pb, con, prim, 2)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+
+
+def test_boundary_fill_matches_oracle_ghosts():
+    pb, con, prim = cases.random_riemann2d(20, seed=2, order=9)
+    for bc in (("free",) * 4, ("periodic",) * 4, ("reflect", "free", "periodic", "periodic")):
+        pb.bc = bc
+        s = Solver2D(pb)
+        c = con.copy()
+        c[: pb.ghost] = 7.0  # garbage in the ghosts must be overwritten
+        s.set_state(c, prim)
+        s.boundary()
+        s.sync()
+        got = s.get_state()["convar"]
+        s.close()
+        exp = _ghost_fill(pb, c)
+        assert np.array_equal(got, exp), bc
+
+
+def _ghost_fill(pb, c):
+    """numpy restatement of the sequential left, right, down, up ghost sweeps"""
+    w = c.copy()
+    g, nx, ny = pb.ghost, pb.nx, pb.ny
+    for side in range(4):
+        kind = pb.bc[side]
+        for k in range(g):
+            if side < 2:
+                i = g - 1 - k if side == 0 else nx - g + k
+                src = {"free": i + 1 if side == 0 else i - 1, "periodic": i + pb.nodex if side == 0 else i - pb.nodex,
+                       "reflect": 2 * g - 1 - i if side == 0 else 2 * nx - 2 * g - 1 - i}[kind]
+                w[i] = w[src]
+                if kind == "reflect":
+                    w[i, :, 1] = -w[src, :, 1]
+            else:
+                j = g - 1 - k if side == 2 else ny - g + k
+                src = {"free": j + 1 if side == 2 else j - 1, "periodic": j + pb.nodey if side == 2 else j - pb.nodey,
+                       "reflect": 2 * g - 1 - j if side == 2 else 2 * ny - 2 * g - 1 - j}[kind]
+                w[:, j] = w[:, src]
+                if kind == "reflect":
+                    w[:, j, 2] = -w[:, src, 2]
+    return w
+
+
+def test_graph_replay_is_bitwise_identical():
+    pb, con, prim = cases.riemann2d(64, order=7)
+    a = gpu_run(pb, con, prim, 3, graph=False)
+    b = gpu_run(pb, con, prim, 3, graph=True)
+    assert np.array_equal(a["convar"], b["convar"])
+    assert a["dts"] == b["dts"]
+
+
+def test_run_to_stop_time_like_the_driver_loop():
+    pb, con, prim = cases.riemann2d(32, order=5)
+    tstop = 0.03
+    o = CpuStep("oracle").init(pb)
+    o.set_state(con, prim)
+    n = 0
+    while o.t < tstop:
+        o.step(tstop)
+        n += 1
+    s = Solver2D(pb)
+    s.set_state(con, prim)
+    steps = s.run(tstop, check_every=7)
+    t, _ = s.sync()
+    got = s.get_state()["convar"]
+    s.close()
+    assert abs(t - o.t) <= 1e-15
+    assert rel_linf(got, o.state()["convar"], pb) <= 1e-11
+    assert steps >= n  # extra queued steps are no-ops once t >= tstop
+
+
+def test_blowup_is_reported_not_exit():
+    pb, con, prim = cases.riemann2d(24, order=5)
+    bad = prim.copy()
+    bad[12, 12, 3] = -1.0
+    s = Solver2D(pb)
+    with pytest.raises(HosBlowUp):
+        s.set_state(con, bad)
+    s.close()
+
+
+def test_full_size_riemann_1024_one_step_parity():
+    """The benchmark workload itself (1024^2, WENO7-AO-DF, 3 Gauss points): one step
+    against the oracle at full size."""
+    pb, con, prim = cases.riemann2d(1024, order=7)
+    ref = oracle_run(pb, con, prim, 1)
+    got = gpu_run(pb, con, prim, 1)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+
+
+def test_periodic_conservation_large():
+    pb, con, prim = cases.isentropic_vortex(400, order=5)
+    got = gpu_run(pb, con, prim, 10)
+    t0 = interior(pb, con).sum(axis=(0, 1))
+    t1 = interior(pb, got["convar"]).sum(axis=(0, 1))
+    assert np.all(np.abs(t1 - t0) <= 1e-11 * np.abs(t0).max())
+
+
+@pytest.mark.parametrize("order", [5, 7, 9])
+def test_fp32_bulk_deviation_bounded(order):
+    pb, con, prim = cases.riemann2d(128, order=order)
+    a = gpu_run(pb, con, prim, 10, precision=FP64)
+    b = gpu_run(pb, con, prim, 10, precision=FP32)
+    ra, rb = interior(pb, a["convar"][..., 0]), interior(pb, b["convar"][..., 0])
+    l1 = np.abs(ra - rb).mean() / np.abs(ra).mean()
+    assert l1 <= 1e-4, l1
