@@ -28,14 +28,21 @@ cudaError_t configure_faces9(int precision) {
                                 (int)FaceSmem<float, 9>::bytes);
 }
 
-cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s) {
+// ev (optional): ev[0] recorded after the x-face launch, ev[1] after the y-face launch
+cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
+                           cudaEvent_t* ev) {
     cudaError_t e;
     if (precision == 0) {
         if ((e = launch_one<double, 0>(ax, geo, s)) != cudaSuccess) return e;
-        return launch_one<double, 1>(ay, geo, s);
+        if (ev) cudaEventRecord(ev[0], s);
+        if ((e = launch_one<double, 1>(ay, geo, s)) != cudaSuccess) return e;
+    } else {
+        if ((e = launch_one<float, 0>(ax, geo, s)) != cudaSuccess) return e;
+        if (ev) cudaEventRecord(ev[0], s);
+        if ((e = launch_one<float, 1>(ay, geo, s)) != cudaSuccess) return e;
     }
-    if ((e = launch_one<float, 0>(ax, geo, s)) != cudaSuccess) return e;
-    return launch_one<float, 1>(ay, geo, s);
+    if (ev) cudaEventRecord(ev[1], s);
+    return cudaSuccess;
 }
 
 }  // namespace hos

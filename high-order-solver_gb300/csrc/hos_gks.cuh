@@ -15,26 +15,16 @@
 
 namespace hos {
 
-// half / full space moments of one Maxwellian
+// half / full space moments of one Maxwellian.  init_half fills the u > 0 / u < 0 moments
+// (the left and right states' tables); init_whole only the full-space ones (the centre
+// state's table, which GKS2D contracts with G_address alone).
 template <class T> struct Mom {
-    T up[7], un[7], vw[7], xi2, xi4;
-    __device__ __forceinline__ void init(T u, T v, T lambda, T K) {
-        constexpr double pi = 3.14159265358979323846;
-        T uw[7];
+    T up[7], un[7], uw[7], vw[7], xi2, xi4;
+    __device__ __forceinline__ void whole(T u, T v, T ol, T K) {
         uw[0] = T(1);
         uw[1] = u;
-        up[0] = T(0.5) * erfc(sqrt(lambda) * -u);
-        un[0] = T(1.0) - up[0];
-        up[1] = u * up[0] + T(0.5) * (exp(-lambda * u * u) / sqrt(T(pi) * lambda));
-        un[1] = u - up[1];
-        const T ol = T(1.0) / lambda;
 #pragma unroll
         for (int i = 2; i <= 6; ++i) uw[i] = u * uw[i - 1] + T(0.5 * (i - 1)) * ol * uw[i - 2];
-#pragma unroll
-        for (int i = 2; i <= 6; ++i) {
-            up[i] = u * up[i - 1] + T(0.5 * (i - 1)) * ol * up[i - 2];
-            un[i] = uw[i] - up[i];
-        }
         vw[0] = T(1);
         vw[1] = v;
 #pragma unroll
@@ -42,15 +32,32 @@ template <class T> struct Mom {
         xi2 = T(0.5) * K * ol;
         xi4 = T(0.25) * (K * K + T(2) * K) * ol * ol;
     }
+    __device__ __forceinline__ void init_whole(T u, T v, T lambda, T K) { whole(u, v, T(1.0) / lambda, K); }
+    __device__ __forceinline__ void init_half(T u, T v, T lambda, T K) {
+        constexpr double pi = 3.14159265358979323846;
+        const T ol = T(1.0) / lambda;
+        whole(u, v, ol, K);
+        up[0] = T(0.5) * erfc(sqrt(lambda) * -u);
+        un[0] = T(1.0) - up[0];
+        up[1] = u * up[0] + T(0.5) * (exp(-lambda * u * u) / sqrt(T(pi) * lambda));
+        un[1] = u - up[1];
+#pragma unroll
+        for (int i = 2; i <= 6; ++i) {
+            up[i] = u * up[i - 1] + T(0.5 * (i - 1)) * ol * up[i - 2];
+            un[i] = uw[i] - up[i];
+        }
+    }
 };
 
-// table selectors: 0 = u > 0 half space, 1 = u < 0 half space, 2 = whole space
+// table selectors: 0 = u > 0 half space, 1 = u < 0 half space, 2 = whole space.  The
+// reference's whole-space table is uplus*v + uminus*v, equal to uwhole*v to within one
+// rounding; the whole-space recurrence is used directly.
 template <class T, int TAB>
 __device__ __forceinline__ T M(const Mom<T>& m, int i, int j, int k) {
     const T xk = k == 0 ? T(1) : k == 1 ? m.xi2 : m.xi4;
     if (TAB == 0) return k == 0 ? m.up[i] * m.vw[j] : m.up[i] * m.vw[j] * xk;
     if (TAB == 1) return k == 0 ? m.un[i] * m.vw[j] : m.un[i] * m.vw[j] * xk;
-    return k == 0 ? m.up[i] * m.vw[j] + m.un[i] * m.vw[j] : m.up[i] * m.vw[j] * xk + m.un[i] * m.vw[j] * xk;
+    return k == 0 ? m.uw[i] * m.vw[j] : m.uw[i] * m.vw[j] * xk;
 }
 
 // moment contraction <a psi u^NU v^NV> (GL_address / GR_address / G_address, :603-636)
@@ -69,15 +76,32 @@ __device__ __forceinline__ void contract(const Mom<T>& m, const T* a, T* psi) {
 #undef HM
 }
 
-// micro-slope a from a macroscopic slope (A, src/basic_function.cpp:571-583)
+// contraction with a = (1, 0, 0, 0): the moments <psi u^NU v^NV> themselves
+template <class T, int TAB, int NU, int NV>
+__device__ __forceinline__ void contract_unit(const Mom<T>& m, T* psi) {
+    constexpr int u = NU, v = NV;
+#define HM(i, j, k) M<T, TAB>(m, i, j, k)
+    psi[0] = HM(u, v, 0);
+    psi[1] = HM(u + 1, v, 0);
+    psi[2] = HM(u, v + 1, 0);
+    psi[3] = T(0.5) * (HM(u + 2, v, 0) + HM(u, v + 2, 0) + HM(u, v, 1));
+#undef HM
+}
+
+// micro-slope a from a macroscopic slope (A, src/basic_function.cpp:571-583);
+// K enters through hK = (K + 2) / 2 and c4K = 4 / (K + 2)
+template <class T> struct GasK {
+    T K, hK, c4K;
+    __device__ __forceinline__ explicit GasK(T k) : K(k), hK(T(0.5) * (k + T(2))), c4K(T(4.0) / (k + T(2))) {}
+};
 template <class T>
-__device__ __forceinline__ void microslope(T* a, const T* der, const T* prim, T K) {
+__device__ __forceinline__ void microslope(T* a, const T* der, const T* prim, const GasK<T>& gk) {
     const T overden = T(1.0) / prim[0];
-    const T q = prim[1] * prim[1] + prim[2] * prim[2] + T(0.5) * (K + T(2)) / prim[3];
+    const T q = prim[1] * prim[1] + prim[2] * prim[2] + gk.hK / prim[3];
     const T R4 = der[3] * overden - T(0.5) * q * der[0] * overden;
     const T R3 = (der[2] - prim[2] * der[0]) * overden;
     const T R2 = (der[1] - prim[1] * der[0]) * overden;
-    a[3] = (T(4.0) / (K + T(2))) * prim[3] * prim[3] * (T(2) * R4 - T(2) * prim[1] * R2 - T(2) * prim[2] * R3);
+    a[3] = gk.c4K * prim[3] * prim[3] * (T(2) * R4 - T(2) * prim[1] * R2 - T(2) * prim[2] * R3);
     a[2] = T(2) * prim[3] * R3 - prim[2] * a[3];
     a[1] = T(2) * prim[3] * R2 - prim[1] * a[3];
     a[0] = der[0] * overden - prim[1] * a[1] - prim[2] * a[2] - T(0.5) * a[3] * q;
@@ -85,17 +109,24 @@ __device__ __forceinline__ void microslope(T* a, const T* der, const T* prim, T 
 
 template <class T>
 __device__ __forceinline__ void to_ulambda(T* pr, const T* w, T K) {
+    const T ir = T(1.0) / w[0];
     pr[0] = w[0];
-    pr[1] = w[1] / w[0];
-    pr[2] = w[2] / w[0];
+    pr[1] = w[1] * ir;
+    pr[2] = w[2] * ir;
     pr[3] = lambda_of(w[0], pr[1], pr[2], w[3], K);
 }
 
-// Euler-type numerical collision time (Get_Tau, src/basic_function.cpp:663-708)
+// Euler-type numerical collision time tau_num = c1 dt + dt C (Get_Tau,
+// src/basic_function.cpp:663-708); C depends only on the left/right states, so it is formed
+// once for both time levels.
 template <class T>
-__device__ __forceinline__ T tau_num(T dl, T dr, T ll, T lr, T dt, T c1, T c2) {
+__device__ __forceinline__ T tau_ratio(T dl, T dr, T ll, T lr, T c2) {
+    const T a = dl / ll, b = dr / lr;
+    return c2 * fabsT(a - b) / fabsT(a + b);
+}
+template <class T>
+__device__ __forceinline__ T tau_num(T Cc, T dt, T c1, T c2) {
     if (c1 <= T(0) && c2 <= T(0)) return T(0.0);
-    const T Cc = c2 * fabsT(dl / ll - dr / lr) / fabsT(dl / ll + dr / lr);
     return c1 * dt + dt * Cc;
 }
 
@@ -107,6 +138,7 @@ template <class T> struct GState { T w[4], dx[4], dy[4]; };
 template <class T>
 __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R, T dt, T K, T c1, T c2,
                                           T* fo, T* dfo) {
+    const GasK<T> gk(K);
     T pl[4], pr[4], p0[4];
     to_ulambda(pl, L.w, K);
     to_ulambda(pr, R.w, K);
@@ -117,8 +149,8 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
     T glu[4], gru[4], t1s[4], w0[4], c0x[4], c0y[4];
     {
         Mom<T> ml, mr;
-        ml.init(pl[1], pl[2], pl[3], K);
-        mr.init(pr[1], pr[2], pr[3], K);
+        ml.init_half(pl[1], pl[2], pl[3], K);
+        mr.init_half(pr[1], pr[2], pr[3], K);
         // collision (Collision, src/basic_function.cpp:561-569)
         w0[0] = pl[0] * ml.up[0] + pr[0] * mr.un[0];
         w0[1] = pl[0] * ml.up[1] + pr[0] * mr.un[1];
@@ -126,10 +158,10 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
         w0[3] = T(0.5) * pl[0] * (ml.up[2] + ml.up[0] * ml.vw[2] + ml.up[0] * ml.xi2) +
                 T(0.5) * pr[0] * (mr.un[2] + mr.un[0] * mr.vw[2] + mr.un[0] * mr.xi2);
         T alx[4], arx[4], aly[4], ary[4], q0[4], q1[4], q2[4], q3[4];
-        microslope(alx, L.dx, pl, K);
-        microslope(arx, R.dx, pr, K);
-        microslope(aly, L.dy, pl, K);
-        microslope(ary, R.dy, pr, K);
+        microslope(alx, L.dx, pl, gk);
+        microslope(arx, R.dx, pr, gk);
+        microslope(aly, L.dy, pl, gk);
+        microslope(ary, R.dy, pr, gk);
         contract<T, 0, 0, 0>(ml, alx, q0);
         contract<T, 1, 0, 0>(mr, arx, q1);
         contract<T, 0, 0, 0>(ml, aly, q2);
@@ -139,9 +171,8 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
             c0x[v] = pl[0] * q0[v] + pr[0] * q1[v];
             c0y[v] = pl[0] * q2[v] + pr[0] * q3[v];
         }
-        const T unit[4] = {T(1), T(0.0), T(0.0), T(0.0)};
-        contract<T, 0, 1, 0>(ml, unit, glu);
-        contract<T, 1, 1, 0>(mr, unit, gru);
+        contract_unit<T, 0, 1, 0>(ml, glu);
+        contract_unit<T, 1, 1, 0>(mr, gru);
         contract<T, 0, 2, 0>(ml, alx, q0);   // alxuul
         contract<T, 1, 2, 0>(mr, arx, q1);   // arxuur
         contract<T, 0, 1, 1>(ml, aly, q2);   // alyuvl
@@ -153,14 +184,13 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
     T g0u[4], t4s[4], A0u[4];
     {
         Mom<T> m0;
-        m0.init(p0[1], p0[2], p0[3], K);
-        const T unit[4] = {T(1), T(0.0), T(0.0), T(0.0)};
-        contract<T, 2, 1, 0>(m0, unit, g0u);
+        m0.init_whole(p0[1], p0[2], p0[3], K);
+        contract_unit<T, 2, 1, 0>(m0, g0u);
         T a0x[4], a0y[4], a0xu[4], a0xuu[4], a0yv[4], a0yuv[4];
-        microslope(a0x, c0x, p0, K);
+        microslope(a0x, c0x, p0, gk);
         contract<T, 2, 1, 0>(m0, a0x, a0xu);
         contract<T, 2, 2, 0>(m0, a0x, a0xuu);
-        microslope(a0y, c0y, p0, K);
+        microslope(a0y, c0y, p0, gk);
         contract<T, 2, 0, 1>(m0, a0y, a0yv);
         contract<T, 2, 1, 1>(m0, a0y, a0yuv);
         T dA0[4], A0[4];
@@ -169,13 +199,14 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
             t4s[v] = a0xuu[v] + a0yuv[v];
             dA0[v] = -p0[0] * (a0xu[v] + a0yv[v]);
         }
-        microslope(A0, dA0, p0, K);
+        microslope(A0, dA0, p0, gk);
         contract<T, 2, 1, 0>(m0, A0, A0u);
     }
     // time-integration coefficients for tau = 0 (Euler) at dt and dt/2
     T F0[4], F1[4];
+    const T Cc = tau_ratio(pl[0], pr[0], pl[3], pr[3], c2);
     {
-        const T tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt, c1, c2);
+        const T tn = tau_num(Cc, dt, c1, c2);
         const T eta = exp(-dt / tn);
         const T t0 = tn * (T(1) - eta);
         const T t1 = tn * (eta * (dt + tn) - tn);
@@ -194,7 +225,7 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
     }
     {
         const T dt2 = T(0.5) * dt;
-        const T tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt2, c1, c2);
+        const T tn = tau_num(Cc, dt2, c1, c2);
         const T eta = exp(-dt2 / tn);
         const T t0 = tn * (T(1) - eta);
         const T t1 = tn * (eta * (dt2 + tn) - tn);

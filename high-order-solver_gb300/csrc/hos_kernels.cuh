@@ -123,8 +123,8 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
     const int nx = geo.nx, ny = geo.ny, g = geo.g;
     const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;  // faces along normal: nodeN + 1
     const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;  // faces along tangent: nodeT
-    const T hN = T(DIR == 0 ? geo.dx : geo.dy);
-    const T hT = T(DIR == 0 ? geo.dy : geo.dx);
+    const T hN = T(1.0 / (DIR == 0 ? geo.dx : geo.dy));   // inverse normal spacing
+    const T hT = T(1.0 / (DIR == 0 ? geo.dy : geo.dx));   // inverse face length
     const T gamma = T(geo.gamma), K = T(geo.K);
     const int N0 = blockIdx.y * TILE_N;   // first face index along the normal (0-based)
     const int T0 = blockIdx.x * TILE_T;   // first face index along the tangent

@@ -9,7 +9,10 @@ namespace hos {
 cudaError_t configure_faces5(int precision);
 cudaError_t configure_faces7(int precision);
 cudaError_t configure_faces9(int precision);
-cudaError_t launch_faces5(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s);
-cudaError_t launch_faces7(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s);
-cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s);
+cudaError_t launch_faces5(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
+                           cudaEvent_t* ev = nullptr);
+cudaError_t launch_faces7(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
+                           cudaEvent_t* ev = nullptr);
+cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
+                           cudaEvent_t* ev = nullptr);
 }  // namespace hos

@@ -279,26 +279,34 @@ void free_all(hos_solver2d* s) {
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
-int enqueue_stage(hos_solver2d* s, int stage) {
+// ev (optional): events recorded before the first and after every launch of the stage
+int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     cudaError_t e;
     const Geometry& geo = s->geo;
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], s->stream);
+    };
     {
         const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
         bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "bc_fill");
+        mark(0);
     }
     FaceArgs ax{s->W, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->ctl, stage};
     FaceArgs ay{s->W, s->AY, s->AX, s->FXy, s->FPy, s->FAy, s->ctl, stage};
+    // x faces then y faces, back to back on the stream (events after each when profiling)
+    const int prec = s->precision;
     switch (s->p.order) {
-        case 5: e = launch_faces5(s->precision, ax, ay, geo, s->stream); break;
-        case 7: e = launch_faces7(s->precision, ax, ay, geo, s->stream); break;
-        default: e = launch_faces9(s->precision, ax, ay, geo, s->stream); break;
+        case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
+        case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
+        default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
     UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage};
     const int n = geo.nodex * geo.nodey;
     update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "update");
+    mark(3);
     return HOS_OK;
 }
 
@@ -581,6 +589,30 @@ int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
     if (dt) *dt = c.dt;
     if (c.status & 1u) return fail(HOS_E_BLOWUP, "negative density/pressure or NaN in the state");
     return HOS_OK;
+}
+
+int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms) {
+    if (!s || !ms) return fail(HOS_E_ARG, "null argument");
+    cudaEvent_t ev[10];
+    for (auto& x : ev) cudaEventCreate(&x);
+    cudaEventRecord(ev[0], s->stream);
+    int st = enqueue_begin(s, tstop);
+    if (!st) {
+        cudaEventRecord(ev[1], s->stream);
+        st = enqueue_stage(s, 0, ev + 2);
+    }
+    if (!st) st = enqueue_stage(s, 1, ev + 6);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (!st && e == cudaSuccess) {
+        float f;
+        for (int k = 0; k < 9; ++k) {
+            cudaEventElapsedTime(&f, ev[k], ev[k + 1]);
+            ms[k] = f;
+        }
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (st) return st;
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "profile_step");
 }
 
 int hos2d_launches_per_step(const hos_solver2d* s) {

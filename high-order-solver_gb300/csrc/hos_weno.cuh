@@ -21,10 +21,11 @@ template <int ORDER> struct AO { static constexpr int N = ORDER == 5 ? 4 : ORDER
 // ---- conversions (src/basic_function.cpp:811-842, 1102-1177) ----
 template <class T>
 __device__ __forceinline__ void to_prim(T* pr, const T* w, T gamma) {
+    const T ir = T(1.0) / w[0];
     pr[0] = w[0];
-    pr[1] = w[1] / w[0];
-    pr[2] = w[2] / w[0];
-    pr[3] = (gamma - T(1.0)) * (w[3] - T(0.5) * w[1] * w[1] / w[0] - T(0.5) * w[2] * w[2] / w[0]);
+    pr[1] = w[1] * ir;
+    pr[2] = w[2] * ir;
+    pr[3] = (gamma - T(1.0)) * (w[3] - T(0.5) * (w[1] * pr[1] + w[2] * pr[2]));
 }
 template <class T>
 __device__ __forceinline__ T lambda_of(T rho, T u, T v, T rhoE, T K) {
@@ -32,7 +33,8 @@ __device__ __forceinline__ T lambda_of(T rho, T u, T v, T rhoE, T K) {
 }
 template <class T>
 __device__ __forceinline__ bool needs_order_reduction(const T* w, T K) {
-    T lam = lambda_of(w[0], w[1] / w[0], w[2] / w[0], w[3], K);
+    const T ir = T(1.0) / w[0];
+    T lam = lambda_of(w[0], w[1] * ir, w[2] * ir, w[3], K);
     return lam <= T(0) || !(lam == lam);
 }
 
@@ -83,22 +85,22 @@ template <class T>
 __device__ __forceinline__ T beta7(const T* s) {
     const T wn3 = s[0], wn2 = s[1], wn1 = s[2], w0 = s[3], wp1 = s[4], wp2 = s[5], wp3 = s[6];
     T a1, a2, a3, b0, b1, b2, b3;
-    a1 = (T(-19) * wn3 + T(87) * wn2 - T(177) * wn1 + T(109) * w0) / T(60.0);
-    a2 = (-wn3 + T(4) * wn2 - T(5) * wn1 + T(2) * w0) / T(2);
-    a3 = (-wn3 + T(3) * wn2 - T(3) * wn1 + w0) / T(6.0);
-    b0 = (a1 + a3 / T(10.0)) * (a1 + a3 / T(10.0)) + T(4) * a2 * a2 + T(39) * a3 * a3;
-    a1 = (T(11) * wn2 - T(63) * wn1 + T(33) * w0 + T(19) * wp1) / T(60.0);
-    a2 = (wn1 - T(2) * w0 + wp1) / T(2);
-    a3 = (-wn2 + T(3) * wn1 - T(3) * w0 + wp1) / T(6.0);
-    b1 = (a1 + a3 / T(10.0)) * (a1 + a3 / T(10.0)) + T(4) * a2 * a2 + T(39) * a3 * a3;
-    a1 = (T(-19) * wn1 - T(33) * w0 + T(63) * wp1 - T(11) * wp2) / T(60.0);
-    a2 = (wn1 - T(2) * w0 + wp1) / T(2);
-    a3 = (-wn1 + T(3) * w0 - T(3) * wp1 + wp2) / T(6.0);
-    b2 = (a1 + a3 / T(10.0)) * (a1 + a3 / T(10.0)) + T(4) * a2 * a2 + T(39) * a3 * a3;
-    a1 = (T(-109) * w0 + T(177) * wp1 - T(87) * wp2 + T(19) * wp3) / T(60.0);
-    a2 = (T(2) * w0 - T(5) * wp1 + T(4) * wp2 - wp3) / T(2);
-    a3 = (-w0 + T(3) * wp1 - T(3) * wp2 + wp3) / T(6.0);
-    b3 = (a1 + a3 / T(10.0)) * (a1 + a3 / T(10.0)) + T(4) * a2 * a2 + T(39) * a3 * a3;
+    a1 = (T(-19) * wn3 + T(87) * wn2 - T(177) * wn1 + T(109) * w0) * T(1.0 / (60.0));
+    a2 = (-wn3 + T(4) * wn2 - T(5) * wn1 + T(2) * w0) * T(1.0 / (2));
+    a3 = (-wn3 + T(3) * wn2 - T(3) * wn1 + w0) * T(1.0 / (6.0));
+    b0 = (a1 + a3 * T(1.0 / (10.0))) * (a1 + a3 * T(1.0 / (10.0))) + T(4) * a2 * a2 + T(39) * a3 * a3;
+    a1 = (T(11) * wn2 - T(63) * wn1 + T(33) * w0 + T(19) * wp1) * T(1.0 / (60.0));
+    a2 = (wn1 - T(2) * w0 + wp1) * T(1.0 / (2));
+    a3 = (-wn2 + T(3) * wn1 - T(3) * w0 + wp1) * T(1.0 / (6.0));
+    b1 = (a1 + a3 * T(1.0 / (10.0))) * (a1 + a3 * T(1.0 / (10.0))) + T(4) * a2 * a2 + T(39) * a3 * a3;
+    a1 = (T(-19) * wn1 - T(33) * w0 + T(63) * wp1 - T(11) * wp2) * T(1.0 / (60.0));
+    a2 = (wn1 - T(2) * w0 + wp1) * T(1.0 / (2));
+    a3 = (-wn1 + T(3) * w0 - T(3) * wp1 + wp2) * T(1.0 / (6.0));
+    b2 = (a1 + a3 * T(1.0 / (10.0))) * (a1 + a3 * T(1.0 / (10.0))) + T(4) * a2 * a2 + T(39) * a3 * a3;
+    a1 = (T(-109) * w0 + T(177) * wp1 - T(87) * wp2 + T(19) * wp3) * T(1.0 / (60.0));
+    a2 = (T(2) * w0 - T(5) * wp1 + T(4) * wp2 - wp3) * T(1.0 / (2));
+    a3 = (-w0 + T(3) * wp1 - T(3) * wp2 + wp3) * T(1.0 / (6.0));
+    b3 = (a1 + a3 * T(1.0 / (10.0))) * (a1 + a3 * T(1.0 / (10.0))) + T(4) * a2 * a2 + T(39) * a3 * a3;
     return T(1.0 / 20.0) * (b0 + T(9.0) * b1 + T(9.0) * b2 + b3) + fabsT(b0 - b1 - b2 + b3);
 }
 // s points at wn4 (9 entries); b5mid returns the middle quartic indicator
@@ -108,33 +110,33 @@ __device__ __forceinline__ T beta9(const T* s, T& b5mid) {
     const T wp1 = s[5], wp2 = s[6], wp3 = s[7], wp4 = s[8];
     T a1, a2, a3, a4, b[5];
 #define HOS_B9COMB                                                                          \
-    ((a1 + a3 / T(10.0)) * (a1 + a3 / T(10.0)) +                                            \
+    ((a1 + a3 * T(1.0 / (10.0))) * (a1 + a3 * T(1.0 / (10.0))) +                                            \
      T(13.0 / 3.0) * (a2 + T(123.0 / 455.0) * a4) * (a2 + T(123.0 / 455.0) * a4) +          \
      T(781.0 / 20.0) * a3 * a3 + T(1421461.0 / 2275.0) * a4 * a4)
-    a1 = (T(-462) * wn1 + T(336) * wn2 - T(146) * wn3 + T(27) * wn4 + T(245) * w0) / T(120.0);
-    a2 = (T(-240) * wn1 + T(262) * wn2 - T(128) * wn3 + T(25) * wn4 + T(81) * w0) / T(56.0);
-    a3 = (T(-18) * wn1 + T(24) * wn2 - T(14) * wn3 + T(3) * wn4 + T(5) * w0) / T(12.0);
-    a4 = (T(-4) * wn1 + T(6) * wn2 - T(4) * wn3 + wn4 + w0) / T(24.0);
+    a1 = (T(-462) * wn1 + T(336) * wn2 - T(146) * wn3 + T(27) * wn4 + T(245) * w0) * T(1.0 / (120.0));
+    a2 = (T(-240) * wn1 + T(262) * wn2 - T(128) * wn3 + T(25) * wn4 + T(81) * w0) * T(1.0 / (56.0));
+    a3 = (T(-18) * wn1 + T(24) * wn2 - T(14) * wn3 + T(3) * wn4 + T(5) * w0) * T(1.0 / (12.0));
+    a4 = (T(-4) * wn1 + T(6) * wn2 - T(4) * wn3 + wn4 + w0) * T(1.0 / (24.0));
     b[0] = HOS_B9COMB;
-    a1 = (T(-192) * wn1 + T(66) * wn2 - T(11) * wn3 + T(110) * w0 + T(27) * wp1) / T(120);
-    a2 = (T(10) * wn1 + T(12) * wn2 - T(3) * wn3 - T(44) * w0 + T(25) * wp1) / T(56);
-    a3 = (T(12) * wn1 - T(6) * wn2 + wn3 - T(10) * w0 + T(3) * wp1) / T(12);
-    a4 = (T(6) * wn1 - T(4) * wn2 + wn3 - T(4) * w0 + wp1) / T(24);
+    a1 = (T(-192) * wn1 + T(66) * wn2 - T(11) * wn3 + T(110) * w0 + T(27) * wp1) * T(1.0 / (120));
+    a2 = (T(10) * wn1 + T(12) * wn2 - T(3) * wn3 - T(44) * w0 + T(25) * wp1) * T(1.0 / (56));
+    a3 = (T(12) * wn1 - T(6) * wn2 + wn3 - T(10) * w0 + T(3) * wp1) * T(1.0 / (12));
+    a4 = (T(6) * wn1 - T(4) * wn2 + wn3 - T(4) * w0 + wp1) * T(1.0 / (24));
     b[1] = HOS_B9COMB;
-    a1 = (T(-82) * wn1 + T(11) * wn2 + T(82) * wp1 - T(11) * wp2) / T(120);
-    a2 = (T(40) * wn1 - T(3) * wn2 - T(74) * w0 + T(40) * wp1 - T(3) * wp2) / T(56);
-    a3 = (T(2) * wn1 - wn2 - T(2) * wp1 + wp2) / T(12);
-    a4 = (T(-4) * wn1 + wn2 + T(6) * w0 - T(4) * wp1 + wp2) / T(24);
+    a1 = (T(-82) * wn1 + T(11) * wn2 + T(82) * wp1 - T(11) * wp2) * T(1.0 / (120));
+    a2 = (T(40) * wn1 - T(3) * wn2 - T(74) * w0 + T(40) * wp1 - T(3) * wp2) * T(1.0 / (56));
+    a3 = (T(2) * wn1 - wn2 - T(2) * wp1 + wp2) * T(1.0 / (12));
+    a4 = (T(-4) * wn1 + wn2 + T(6) * w0 - T(4) * wp1 + wp2) * T(1.0 / (24));
     b[2] = HOS_B9COMB;
-    a1 = (T(-27) * wn1 - T(110) * w0 + T(192) * wp1 - T(66) * wp2 + T(11) * wp3) / T(120);
-    a2 = (T(25) * wn1 - T(44) * w0 + T(10) * wp1 + T(12) * wp2 - T(3) * wp3) / T(56);
-    a3 = (T(-3) * wn1 + T(10) * w0 - T(12) * wp1 + T(6) * wp2 - wp3) / T(12);
-    a4 = (wn1 - T(4) * w0 + T(6) * wp1 - T(4) * wp2 + wp3) / T(24);
+    a1 = (T(-27) * wn1 - T(110) * w0 + T(192) * wp1 - T(66) * wp2 + T(11) * wp3) * T(1.0 / (120));
+    a2 = (T(25) * wn1 - T(44) * w0 + T(10) * wp1 + T(12) * wp2 - T(3) * wp3) * T(1.0 / (56));
+    a3 = (T(-3) * wn1 + T(10) * w0 - T(12) * wp1 + T(6) * wp2 - wp3) * T(1.0 / (12));
+    a4 = (wn1 - T(4) * w0 + T(6) * wp1 - T(4) * wp2 + wp3) * T(1.0 / (24));
     b[3] = HOS_B9COMB;
-    a1 = (T(-245) * w0 + T(462) * wp1 - T(336) * wp2 + T(146) * wp3 - T(27) * wp4) / T(120);
-    a2 = (T(81) * w0 - T(240) * wp1 + T(262) * wp2 - T(128) * wp3 + T(25) * wp4) / T(56);
-    a3 = (T(-5) * w0 + T(18) * wp1 - T(24) * wp2 + T(14) * wp3 - T(3) * wp4) / T(12);
-    a4 = (w0 - T(4) * wp1 + T(6) * wp2 - T(4) * wp3 + wp4) / T(24);
+    a1 = (T(-245) * w0 + T(462) * wp1 - T(336) * wp2 + T(146) * wp3 - T(27) * wp4) * T(1.0 / (120));
+    a2 = (T(81) * w0 - T(240) * wp1 + T(262) * wp2 - T(128) * wp3 + T(25) * wp4) * T(1.0 / (56));
+    a3 = (T(-5) * w0 + T(18) * wp1 - T(24) * wp2 + T(14) * wp3 - T(3) * wp4) * T(1.0 / (12));
+    a4 = (w0 - T(4) * wp1 + T(6) * wp2 - T(4) * wp3 + wp4) * T(1.0 / (24));
     b[4] = HOS_B9COMB;
 #undef HOS_B9COMB
     b5mid = b[2];
@@ -189,9 +191,10 @@ __device__ __forceinline__ void ao_weights(const T* s, T* fw) {
     }
     T inv = T(1.0) / sum;
     T wtop = alpha[top] * inv;
-    fw[top] = wtop / T(dd[top]);
+    const T wt = wtop * T(1.0 / dd[top]);
+    fw[top] = wt;
 #pragma unroll
-    for (int k = 0; k < top; ++k) fw[k] = alpha[k] * inv - wtop / T(dd[top]) * T(dd[k]);
+    for (int k = 0; k < top; ++k) fw[k] = alpha[k] * inv - wt * T(dd[k]);
 }
 
 // DF factors from the alpha values along the stencil (e.g. :1731-1741, :1898-1909)
@@ -213,7 +216,7 @@ __device__ __forceinline__ void df_factors(const T* a, T* df) {
 
 // ---- candidate polynomials at the left (SIDE 0) or right (SIDE 1) face of the centre cell ----
 template <class T, int ORDER, int SIDE>
-__device__ __forceinline__ void normal_face(const T* s, const T* df, T h, T* p, T* px) {
+__device__ __forceinline__ void normal_face(const T* s, const T* df, T ih, T* p, T* px) {
     constexpr int r = ORDER / 2;
     const T w0 = s[r], wn1 = s[r - 1], wn2 = s[r - 2], wp1 = s[r + 1], wp2 = s[r + 2];
     const T wn3 = r >= 3 ? s[r >= 3 ? r - 3 : 0] : T(0), wp3 = r >= 3 ? s[r >= 3 ? r + 3 : 0] : T(0);
@@ -223,103 +226,103 @@ __device__ __forceinline__ void normal_face(const T* s, const T* df, T h, T* p, 
         p[1] = w0 + df[1] * (T(1.0 / 3.0) * wn1 + T(5.0 / 6.0) * w0 - T(1.0 / 6.0) * wp1 - w0);
         p[2] = w0 + df[2] * (T(11.0 / 6.0) * w0 - T(7.0 / 6.0) * wp1 + T(1.0 / 3.0) * wp2 - w0);
         p[3] = w0 + df[3] * (T(1.0 / 60.0) * (T(47.0) * w0 + T(27.0) * wn1 - T(3.0) * wn2 - T(13.0) * wp1 + T(2.0) * wp2) - w0);
-        px[0] = df[0] * (w0 - wn1) / h;
-        px[1] = df[1] * (w0 - wn1) / h;
-        px[2] = -df[2] * ((T(2.0) * w0 - T(3.0) * wp1 + wp2) / h);
-        px[3] = df[3] * (T(15.0) * w0 - T(15.0) * wn1 + wn2 - wp1) / (T(12.0) * h);
+        px[0] = df[0] * (w0 - wn1) * ih;
+        px[1] = df[1] * (w0 - wn1) * ih;
+        px[2] = -df[2] * ((T(2.0) * w0 - T(3.0) * wp1 + wp2) * ih);
+        px[3] = df[3] * (T(15.0) * w0 - T(15.0) * wn1 + wn2 - wp1) * (T(1.0 / 12.0) * ih);
         if (ORDER >= 7) {
             p[4] = w0 + df[4] * (T(1.0 / 420.0) * (T(319.0) * w0 + T(214.0) * wn1 - T(38.0) * wn2 + T(4.0) * wn3 - T(101.0) * wp1 + T(25.0) * wp2 - T(3.0) * wp3) - w0);
-            px[4] = df[4] * (T(245.0) * w0 - T(245.0) * wn1 + T(25.0) * wn2 - T(2.0) * wn3 - T(25.0) * wp1 + T(2.0) * wp2) / (T(180.0) * h);
+            px[4] = df[4] * (T(245.0) * w0 - T(245.0) * wn1 + T(25.0) * wn2 - T(2.0) * wn3 - T(25.0) * wp1 + T(2.0) * wp2) * (T(1.0 / 180.0) * ih);
         }
         if (ORDER == 9) {
             p[5] = w0 + df[5] * (T(1.0 / 2520.0) * (T(1879.0) * w0 + T(1375.0) * wn1 - T(305.0) * wn2 + T(55.0) * wn3 - T(5.0) * wn4 - T(641.0) * wp1 + T(199.0) * wp2 - T(41.0) * wp3 + T(4.0) * wp4) - w0);
-            px[5] = df[5] * (T(7175.0) * w0 - T(7175.0) * wn1 + T(889.0) * wn2 - T(119.0) * wn3 + T(9.0) * wn4 - T(889.0) * wp1 + T(119.0) * wp2 - T(9.0) * wp3) / (T(5040.0) * h);
+            px[5] = df[5] * (T(7175.0) * w0 - T(7175.0) * wn1 + T(889.0) * wn2 - T(119.0) * wn3 + T(9.0) * wn4 - T(889.0) * wp1 + T(119.0) * wp2 - T(9.0) * wp3) * (T(1.0 / 5040.0) * ih);
         }
     } else {
         p[0] = w0 + df[0] * (T(1.0 / 3.0) * wn2 - T(7.0 / 6.0) * wn1 + T(11.0 / 6.0) * w0 - w0);
         p[1] = w0 + df[1] * (T(-1.0 / 6.0) * wn1 + T(5.0 / 6.0) * w0 + T(1.0 / 3.0) * wp1 - w0);
         p[2] = w0 + df[2] * (T(1.0 / 3.0) * w0 + T(5.0 / 6.0) * wp1 - T(1.0 / 6.0) * wp2 - w0);
         p[3] = w0 + df[3] * (T(1.0 / 60.0) * (T(47.0) * w0 - T(13.0) * wn1 + T(2.0) * wn2 + T(27.0) * wp1 - T(3.0) * wp2) - w0);
-        px[0] = df[0] * (T(2.0) * w0 - T(3.0) * wn1 + wn2) / h;
-        px[1] = df[1] * (-w0 + wp1) / h;
-        px[2] = df[2] * (-w0 + wp1) / h;
-        px[3] = df[3] * (T(-15.0) * w0 + wn1 + T(15.0) * wp1 - wp2) / (T(12.0) * h);
+        px[0] = df[0] * (T(2.0) * w0 - T(3.0) * wn1 + wn2) * ih;
+        px[1] = df[1] * (-w0 + wp1) * ih;
+        px[2] = df[2] * (-w0 + wp1) * ih;
+        px[3] = df[3] * (T(-15.0) * w0 + wn1 + T(15.0) * wp1 - wp2) * (T(1.0 / 12.0) * ih);
         if (ORDER >= 7) {
             p[4] = w0 + df[4] * (T(1.0 / 420.0) * (T(319.0) * w0 - T(101.0) * wn1 + T(25.0) * wn2 - T(3.0) * wn3 + T(214.0) * wp1 - T(38.0) * wp2 + T(4.0) * wp3) - w0);
-            px[4] = df[4] * (T(-245.0) * w0 + T(25.0) * wn1 - T(2.0) * wn2 + T(245.0) * wp1 - T(25.0) * wp2 + T(2.0) * wp3) / (T(180.0) * h);
+            px[4] = df[4] * (T(-245.0) * w0 + T(25.0) * wn1 - T(2.0) * wn2 + T(245.0) * wp1 - T(25.0) * wp2 + T(2.0) * wp3) * (T(1.0 / 180.0) * ih);
         }
         if (ORDER == 9) {
             p[5] = w0 + df[5] * (T(1.0 / 2520.0) * (T(1879.0) * w0 - T(641.0) * wn1 + T(199.0) * wn2 - T(41.0) * wn3 + T(4.0) * wn4 + T(1375.0) * wp1 - T(305.0) * wp2 + T(55.0) * wp3 - T(5.0) * wp4) - w0);
-            px[5] = df[5] * (T(-7175.0) * w0 + T(889.0) * wn1 - T(119.0) * wn2 + T(9.0) * wn3 + T(7175.0) * wp1 - T(889.0) * wp2 + T(119.0) * wp3 - T(9.0) * wp4) / (T(5040.0) * h);
+            px[5] = df[5] * (T(-7175.0) * w0 + T(889.0) * wn1 - T(119.0) * wn2 + T(9.0) * wn3 + T(7175.0) * wp1 - T(889.0) * wp2 + T(119.0) * wp3 - T(9.0) * wp4) * (T(1.0 / 5040.0) * ih);
         }
     }
 }
 
 // ---- candidate polynomials at Gauss point IG of a face segment ----
 template <class T, int ORDER>
-__device__ __forceinline__ void tangent_point(int ig, const T* s, const T* df, T h, T* p, T* px) {
+__device__ __forceinline__ void tangent_point(int ig, const T* s, const T* df, T ih, T* p, T* px) {
     if (ORDER == 5) {
         const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
         constexpr double q = 1.732050807568877294;  // sqrt(3)
         if (ig == 0) {
-            p[0] = w0 + df[0] * (w0 - (T(q) * w0) / T(4) + (T(4) * wn1 - wn2) / T(4 * q) - w0);
-            p[1] = w0 + df[1] * (w0 + (wn1 - wp1) / T(4 * q) - w0);
+            p[0] = w0 + df[0] * (w0 - (T(q) * w0) * T(1.0 / (4)) + (T(4) * wn1 - wn2) * T(1.0 / (4 * q)) - w0);
+            p[1] = w0 + df[1] * (w0 + (wn1 - wp1) * T(1.0 / (4 * q)) - w0);
             p[2] = w0 + df[2] * (T(1.0 / 12.0) * (T(3 * (4 + q)) * w0 + T(q) * (T(-4) * wp1 + wp2)) - w0);
-            p[3] = w0 + df[3] * ((T(4314) * w0 + T(4 + 500 * q) * wn1 - wn2 - T(70 * q) * wn2 + T(4) * wp1 - T(500 * q) * wp1 - wp2 + T(70 * q) * wp2) / T(4320) - w0);
-            px[0] = -df[0] * (T(-9 + q) * w0 - T(2 * (-6 + q)) * wn1 + T(-3 + q) * wn2) / (T(6) * h);
-            px[1] = -df[1] * (T(-2 * q) * w0 + T(3 + q) * wn1 + T(-3 + q) * wp1) / (T(6) * h);
-            px[2] = -df[2] * (T(9 + q) * w0 - T(2 * (6 + q)) * wp1 + T(3 + q) * wp2) / (T(6) * h);
-            px[3] = df[3] * (T(48 * q) * w0 - T(72) * wn1 - T(26 * q) * wn1 + T(9) * wn2 + T(2 * q) * wn2 + T(72) * wp1 - T(26 * q) * wp1 - T(9) * wp2 + T(2 * q) * wp2) / (T(108) * h);
+            p[3] = w0 + df[3] * ((T(4314) * w0 + T(4 + 500 * q) * wn1 - wn2 - T(70 * q) * wn2 + T(4) * wp1 - T(500 * q) * wp1 - wp2 + T(70 * q) * wp2) * T(1.0 / (4320)) - w0);
+            px[0] = -df[0] * (T(-9 + q) * w0 - T(2 * (-6 + q)) * wn1 + T(-3 + q) * wn2) * (T(1.0 / 6) * ih);
+            px[1] = -df[1] * (T(-2 * q) * w0 + T(3 + q) * wn1 + T(-3 + q) * wp1) * (T(1.0 / 6) * ih);
+            px[2] = -df[2] * (T(9 + q) * w0 - T(2 * (6 + q)) * wp1 + T(3 + q) * wp2) * (T(1.0 / 6) * ih);
+            px[3] = df[3] * (T(48 * q) * w0 - T(72) * wn1 - T(26 * q) * wn1 + T(9) * wn2 + T(2 * q) * wn2 + T(72) * wp1 - T(26 * q) * wp1 - T(9) * wp2 + T(2 * q) * wp2) * (T(1.0 / 108) * ih);
         } else {
             p[0] = w0 + df[0] * (T(1.0 / 12.0) * (T(3 * (4 + q)) * w0 + T(q) * (T(-4) * wn1 + wn2)) - w0);
-            p[1] = w0 + df[1] * (w0 + (-wn1 + wp1) / T(4 * q) - w0);
-            p[2] = w0 + df[2] * (w0 - (T(q) * w0) / T(4) + (T(4) * wp1 - wp2) / T(4 * q) - w0);
-            p[3] = w0 + df[3] * ((T(4314) * w0 + T(4 - 500 * q) * wn1 - wn2 + T(70 * q) * wn2 + T(4) * wp1 + T(500 * q) * wp1 - wp2 - T(70 * q) * wp2) / T(4320) - w0);
-            px[0] = df[0] * (T(9 + q) * w0 - T(2 * (6 + q)) * wn1 + T(3 + q) * wn2) / (T(6) * h);
-            px[1] = df[1] * (T(-2 * q) * w0 + T(-3 + q) * wn1 + T(3 + q) * wp1) / (T(6) * h);
-            px[2] = df[2] * (T(-9 + q) * w0 - T(2 * (-6 + q)) * wp1 + T(-3 + q) * wp2) / (T(6) * h);
-            px[3] = -df[3] * ((T(48 * q) * w0 + T(72) * wn1 - T(26 * q) * wn1 - T(9) * wn2 + T(2 * q) * wn2 - T(72) * wp1 - T(26 * q) * wp1 + T(9) * wp2 + T(2 * q) * wp2) / (T(108) * h));
+            p[1] = w0 + df[1] * (w0 + (-wn1 + wp1) * T(1.0 / (4 * q)) - w0);
+            p[2] = w0 + df[2] * (w0 - (T(q) * w0) * T(1.0 / (4)) + (T(4) * wp1 - wp2) * T(1.0 / (4 * q)) - w0);
+            p[3] = w0 + df[3] * ((T(4314) * w0 + T(4 - 500 * q) * wn1 - wn2 + T(70 * q) * wn2 + T(4) * wp1 + T(500 * q) * wp1 - wp2 - T(70 * q) * wp2) * T(1.0 / (4320)) - w0);
+            px[0] = df[0] * (T(9 + q) * w0 - T(2 * (6 + q)) * wn1 + T(3 + q) * wn2) * (T(1.0 / 6) * ih);
+            px[1] = df[1] * (T(-2 * q) * w0 + T(-3 + q) * wn1 + T(3 + q) * wp1) * (T(1.0 / 6) * ih);
+            px[2] = df[2] * (T(-9 + q) * w0 - T(2 * (-6 + q)) * wp1 + T(-3 + q) * wp2) * (T(1.0 / 6) * ih);
+            px[3] = -df[3] * ((T(48 * q) * w0 + T(72) * wn1 - T(26 * q) * wn1 - T(9) * wn2 + T(2 * q) * wn2 - T(72) * wp1 - T(26 * q) * wp1 + T(9) * wp2 + T(2 * q) * wp2) * (T(1.0 / 108) * ih));
         }
     } else if (ORDER == 7) {
         const T wn3 = s[0], wn2 = s[1], wn1 = s[2], w0 = s[3], wp1 = s[4], wp2 = s[5], wp3 = s[6];
         constexpr double q = 3.872983346207417;  // sqrt(15)
         if (ig == 0) {
-            p[0] = w0 + df[0] * ((T(23.0) * w0 + T(2.0) * wn1 - wn2) / T(24.0) - w0);
-            p[1] = w0 + df[1] * ((T(26.0) * w0 - wn1 - wp1) / T(24.0) - w0);
-            p[2] = w0 + df[2] * ((T(23.0) * w0 + T(2.0) * wp1 - wp2) / T(24.0) - w0);
-            p[3] = w0 + df[3] * ((T(2134.0) * w0 - T(116.0) * wn1 + T(9.0) * wn2 - T(116.0) * wp1 + T(9.0) * wp2) / T(1920.0) - w0);
-            p[4] = w0 + df[4] * ((T(121004) * w0 - T(7621) * wn1 + T(954) * wn2 - T(75) * wn3 - T(7621) * wp1 + T(954) * wp2 - T(75) * wp3) / T(107520.0) - w0);
-            px[0] = df[0] * (T(3.0) * w0 - T(4.0) * wn1 + wn2) / (T(2.0) * h);
-            px[1] = df[1] * (-wn1 + wp1) / (T(2.0) * h);
-            px[2] = df[2] * (T(-3.0) * w0 + T(4.0) * wp1 - wp2) / (T(2.0) * h);
-            px[3] = df[3] * (T(-34.0) * wn1 + T(5.0) * wn2 + T(34.0) * wp1 - T(5.0) * wp2) / (T(48.0) * h);
-            px[4] = df[4] * (T(-9455) * wn1 + T(2236) * wn2 - T(259) * wn3 + T(9455) * wp1 - T(2236) * wp2 + T(259) * wp3) / (T(11520.0) * h);
+            p[0] = w0 + df[0] * ((T(23.0) * w0 + T(2.0) * wn1 - wn2) * T(1.0 / (24.0)) - w0);
+            p[1] = w0 + df[1] * ((T(26.0) * w0 - wn1 - wp1) * T(1.0 / (24.0)) - w0);
+            p[2] = w0 + df[2] * ((T(23.0) * w0 + T(2.0) * wp1 - wp2) * T(1.0 / (24.0)) - w0);
+            p[3] = w0 + df[3] * ((T(2134.0) * w0 - T(116.0) * wn1 + T(9.0) * wn2 - T(116.0) * wp1 + T(9.0) * wp2) * T(1.0 / (1920.0)) - w0);
+            p[4] = w0 + df[4] * ((T(121004) * w0 - T(7621) * wn1 + T(954) * wn2 - T(75) * wn3 - T(7621) * wp1 + T(954) * wp2 - T(75) * wp3) * T(1.0 / (107520.0)) - w0);
+            px[0] = df[0] * (T(3.0) * w0 - T(4.0) * wn1 + wn2) * (T(1.0 / 2.0) * ih);
+            px[1] = df[1] * (-wn1 + wp1) * (T(1.0 / 2.0) * ih);
+            px[2] = df[2] * (T(-3.0) * w0 + T(4.0) * wp1 - wp2) * (T(1.0 / 2.0) * ih);
+            px[3] = df[3] * (T(-34.0) * wn1 + T(5.0) * wn2 + T(34.0) * wp1 - T(5.0) * wp2) * (T(1.0 / 48.0) * ih);
+            px[4] = df[4] * (T(-9455) * wn1 + T(2236) * wn2 - T(259) * wn3 + T(9455) * wp1 - T(2236) * wp2 + T(259) * wp3) * (T(1.0 / 11520.0) * ih);
         } else if (ig == 1) {
-            p[0] = w0 + df[0] * ((T(62 - 9 * q) * w0 + T(4 * (-1 + 3 * q)) * wn1 + T(2 - 3 * q) * wn2) / T(60.0) - w0);
-            p[1] = w0 + df[1] * ((T(56) * w0 + T(2 + 3 * q) * wn1 + T(2 - 3 * q) * wp1) / T(60.0) - w0);
-            p[2] = w0 + df[2] * ((T(62 + 9 * q) * w0 - T(4 * (1 + 3 * q)) * wp1 + T(2 + 3 * q) * wp2) / T(60.0) - w0);
-            p[3] = w0 + df[3] * ((T(2186) * w0 + T(4 * (29 + 41 * q)) * wn1 - T(9) * wn2 - T(22 * q) * wn2 + T(116) * wp1 - T(164 * q) * wp1 - T(9) * wp2 + T(22 * q) * wp2) / T(2400.0) - w0);
+            p[0] = w0 + df[0] * ((T(62 - 9 * q) * w0 + T(4 * (-1 + 3 * q)) * wn1 + T(2 - 3 * q) * wn2) * T(1.0 / (60.0)) - w0);
+            p[1] = w0 + df[1] * ((T(56) * w0 + T(2 + 3 * q) * wn1 + T(2 - 3 * q) * wp1) * T(1.0 / (60.0)) - w0);
+            p[2] = w0 + df[2] * ((T(62 + 9 * q) * w0 - T(4 * (1 + 3 * q)) * wp1 + T(2 + 3 * q) * wp2) * T(1.0 / (60.0)) - w0);
+            p[3] = w0 + df[3] * ((T(2186) * w0 + T(4 * (29 + 41 * q)) * wn1 - T(9) * wn2 - T(22 * q) * wn2 + T(116) * wp1 - T(164 * q) * wp1 - T(9) * wp2 + T(22 * q) * wp2) * T(1.0 / (2400.0)) - w0);
             p[4] = w0 + df[4] * ((T(4534440) * w0 + T(5 * (57144 + 78421 * q)) * wn1 - T(35748) * wn2 - T(84364 * q) * wn2 + T(2808) * wn3 + T(9541 * q) * wn3 + T(285720) * wp1 -
-                                  T(392105 * q) * wp1 - T(35748) * wp2 + T(84364 * q) * wp2 + T(2808) * wp3 - T(9541 * q) * wp3) / T(5040000.0) - w0);
-            px[0] = df[0] * (-(T(-15 + q) * w0) + T(2 * (-10 + q)) * wn1 - T(-5 + q) * wn2) / (T(10.0) * h);
-            px[1] = df[1] * (T(2 * q) * w0 - T(5 + q) * wn1 - T(-5 + q) * wp1) / (h * T(10.0));
-            px[2] = df[2] * (-(T(15 + q) * w0) + T(2 * (10 + q)) * wp1 - T(5 + q) * wp2) / (T(10.0) * h);
-            px[3] = df[3] * (T(78 * q) * w0 - T(2 * (95 + 21 * q)) * wn1 + T(20) * wn2 + T(3 * q) * wn2 + T(190) * wp1 - T(42 * q) * wp1 - T(20) * wp2 + T(3 * q) * wp2) / (T(300.0) * h);
+                                  T(392105 * q) * wp1 - T(35748) * wp2 + T(84364 * q) * wp2 + T(2808) * wp3 - T(9541 * q) * wp3) * T(1.0 / (5040000.0)) - w0);
+            px[0] = df[0] * (-(T(-15 + q) * w0) + T(2 * (-10 + q)) * wn1 - T(-5 + q) * wn2) * (T(1.0 / 10.0) * ih);
+            px[1] = df[1] * (T(2 * q) * w0 - T(5 + q) * wn1 - T(-5 + q) * wp1) * (T(1.0 / 10.0) * ih);
+            px[2] = df[2] * (-(T(15 + q) * w0) + T(2 * (10 + q)) * wp1 - T(5 + q) * wp2) * (T(1.0 / 10.0) * ih);
+            px[3] = df[3] * (T(78 * q) * w0 - T(2 * (95 + 21 * q)) * wn1 + T(20) * wn2 + T(3 * q) * wn2 + T(190) * wp1 - T(42 * q) * wp1 - T(20) * wp2 + T(3 * q) * wp2) * (T(1.0 / 300.0) * ih);
             px[4] = df[4] * (T(103860 * q) * w0 - T(5 * (49925 + 11619 * q)) * wn1 + T(41300) * wn2 + T(6678 * q) * wn2 - T(4325) * wn3 - T(513 * q) * wn3 + T(249625) * wp1 -
-                             T(58095 * q) * wp1 - T(41300) * wp2 + T(6678 * q) * wp2 + T(4325) * wp3 - T(513 * q) * wp3) / (T(360000.0) * h);
+                             T(58095 * q) * wp1 - T(41300) * wp2 + T(6678 * q) * wp2 + T(4325) * wp3 - T(513 * q) * wp3) * (T(1.0 / 360000.0) * ih);
         } else {
-            p[0] = w0 + df[0] * ((T(62 + 9 * q) * w0 - T(4 * (1 + 3 * q)) * wn1 + T(2 + 3 * q) * wn2) / T(60.0) - w0);
-            p[1] = w0 + df[1] * ((T(56) * w0 + T(2 - 3 * q) * wn1 + T(2 + 3 * q) * wp1) / T(60.0) - w0);
-            p[2] = w0 + df[2] * ((T(62 - 9 * q) * w0 + T(4 * (-1 + 3 * q)) * wp1 + T(2 - 3 * q) * wp2) / T(60.0) - w0);
-            p[3] = w0 + df[3] * ((T(2186) * w0 - T(4 * (-29 + 41 * q)) * wn1 - T(9) * wn2 + T(22 * q) * wn2 + T(116) * wp1 + T(164 * q) * wp1 - T(9) * wp2 - T(22 * q) * wp2) / T(2400.0) - w0);
+            p[0] = w0 + df[0] * ((T(62 + 9 * q) * w0 - T(4 * (1 + 3 * q)) * wn1 + T(2 + 3 * q) * wn2) * T(1.0 / (60.0)) - w0);
+            p[1] = w0 + df[1] * ((T(56) * w0 + T(2 - 3 * q) * wn1 + T(2 + 3 * q) * wp1) * T(1.0 / (60.0)) - w0);
+            p[2] = w0 + df[2] * ((T(62 - 9 * q) * w0 + T(4 * (-1 + 3 * q)) * wp1 + T(2 - 3 * q) * wp2) * T(1.0 / (60.0)) - w0);
+            p[3] = w0 + df[3] * ((T(2186) * w0 - T(4 * (-29 + 41 * q)) * wn1 - T(9) * wn2 + T(22 * q) * wn2 + T(116) * wp1 + T(164 * q) * wp1 - T(9) * wp2 - T(22 * q) * wp2) * T(1.0 / (2400.0)) - w0);
             p[4] = w0 + df[4] * ((T(4534440) * w0 - T(5 * (-57144 + 78421 * q)) * wn1 - T(35748) * wn2 + T(84364 * q) * wn2 + T(2808) * wn3 - T(9541 * q) * wn3 + T(285720) * wp1 +
-                                  T(392105 * q) * wp1 - T(35748) * wp2 - T(84364 * q) * wp2 + T(2808) * wp3 + T(9541 * q) * wp3) / T(5040000.0) - w0);
-            px[0] = df[0] * (T(15 + q) * w0 - T(2 * (10 + q)) * wn1 + T(5 + q) * wn2) / (T(10.0) * h);
-            px[1] = df[1] * (T(-2 * q) * w0 - T(5 - q) * wn1 + T(5 + q) * wp1) / (h * T(10.0));
-            px[2] = df[2] * (T(-15 + q) * w0 - T(2 * (-10 + q)) * wp1 + T(-5 + q) * wp2) / (T(10.0) * h);
-            px[3] = df[3] * (T(-78 * q) * w0 + T(2 * (-95 + 21 * q)) * wn1 + T(20) * wn2 - T(3 * q) * wn2 + T(190) * wp1 + T(42 * q) * wp1 - T(20) * wp2 - T(3 * q) * wp2) / (T(300.0) * h);
+                                  T(392105 * q) * wp1 - T(35748) * wp2 - T(84364 * q) * wp2 + T(2808) * wp3 + T(9541 * q) * wp3) * T(1.0 / (5040000.0)) - w0);
+            px[0] = df[0] * (T(15 + q) * w0 - T(2 * (10 + q)) * wn1 + T(5 + q) * wn2) * (T(1.0 / 10.0) * ih);
+            px[1] = df[1] * (T(-2 * q) * w0 - T(5 - q) * wn1 + T(5 + q) * wp1) * (T(1.0 / 10.0) * ih);
+            px[2] = df[2] * (T(-15 + q) * w0 - T(2 * (-10 + q)) * wp1 + T(-5 + q) * wp2) * (T(1.0 / 10.0) * ih);
+            px[3] = df[3] * (T(-78 * q) * w0 + T(2 * (-95 + 21 * q)) * wn1 + T(20) * wn2 - T(3 * q) * wn2 + T(190) * wp1 + T(42 * q) * wp1 - T(20) * wp2 - T(3 * q) * wp2) * (T(1.0 / 300.0) * ih);
             px[4] = df[4] * (T(-103860 * q) * w0 + T(5 * (-49925 + 11619 * q)) * wn1 + T(41300) * wn2 - T(6678 * q) * wn2 - T(4325) * wn3 + T(513 * q) * wn3 + T(249625) * wp1 +
-                             T(58095 * q) * wp1 - T(41300) * wp2 - T(6678 * q) * wp2 + T(4325) * wp3 + T(513 * q) * wp3) / (T(360000.0) * h);
+                             T(58095 * q) * wp1 - T(41300) * wp2 - T(6678 * q) * wp2 + T(4325) * wp3 + T(513 * q) * wp3) * (T(1.0 / 360000.0) * ih);
         }
     } else {
         // 9th order: the polynomial family (Polynomial_9th, :3557-3609) at the Lobatto
@@ -330,44 +333,44 @@ __device__ __forceinline__ void tangent_point(int ig, const T* s, const T* df, T
         const T x = ig == 0 ? T(-1.0) : ig == 1 ? T(0.0) : ig == 2 ? T(-0.5 - r5 / 10.0) : T(-0.5 + r5 / 10.0);
         const T x2 = x * x, x3 = x * x * x, x4 = x * x * x * x;
         T a3, b3, c3;
-        a3 = (T(11) * w0 - T(7) * wn1 + T(2) * wn2) / T(6.0); b3 = (T(2) * w0 - T(3) * wn1 + wn2); c3 = (w0 - T(2) * wn1 + wn2) / T(2.0);
-        p[0] = w0 + df[0] * (a3 + b3 * x + c3 * x * x - w0); px[0] = df[0] * (b3 + T(2.0) * c3 * x) / h;
-        a3 = (T(5) * w0 - wn1 + T(2) * wp1) / T(6.0); b3 = (-w0 + wp1); c3 = (T(-2) * w0 + wn1 + wp1) / T(2.0);
-        p[1] = w0 + df[1] * (a3 + b3 * x + c3 * x * x - w0); px[1] = df[1] * (b3 + T(2.0) * c3 * x) / h;
-        a3 = (T(2) * w0 + T(5) * wp1 - wp2) / T(6.0); b3 = (-w0 + wp1); c3 = (w0 - T(2) * wp1 + wp2) / T(2.0);
-        p[2] = w0 + df[2] * (a3 + b3 * x + c3 * x * x - w0); px[2] = df[2] * (b3 + T(2.0) * c3 * x) / h;
+        a3 = (T(11) * w0 - T(7) * wn1 + T(2) * wn2) * T(1.0 / (6.0)); b3 = (T(2) * w0 - T(3) * wn1 + wn2); c3 = (w0 - T(2) * wn1 + wn2) * T(1.0 / (2.0));
+        p[0] = w0 + df[0] * (a3 + b3 * x + c3 * x * x - w0); px[0] = df[0] * (b3 + T(2.0) * c3 * x) * ih;
+        a3 = (T(5) * w0 - wn1 + T(2) * wp1) * T(1.0 / (6.0)); b3 = (-w0 + wp1); c3 = (T(-2) * w0 + wn1 + wp1) * T(1.0 / (2.0));
+        p[1] = w0 + df[1] * (a3 + b3 * x + c3 * x * x - w0); px[1] = df[1] * (b3 + T(2.0) * c3 * x) * ih;
+        a3 = (T(2) * w0 + T(5) * wp1 - wp2) * T(1.0 / (6.0)); b3 = (-w0 + wp1); c3 = (w0 - T(2) * wp1 + wp2) * T(1.0 / (2.0));
+        p[2] = w0 + df[2] * (a3 + b3 * x + c3 * x * x - w0); px[2] = df[2] * (b3 + T(2.0) * c3 * x) * ih;
         T a5, b5, c5, d5, e5;
-        a5 = (T(47) * w0 - T(13) * wn1 + T(2) * wn2 + T(27) * wp1 - T(3) * wp2) / T(60.0);
-        b5 = (T(-15) * w0 + wn1 + T(15) * wp1 - wp2) / T(12.0);
-        c5 = (T(-8) * w0 + T(6) * wn1 - wn2 + T(2) * wp1 + wp2) / T(8.0);
-        d5 = (T(3) * w0 - wn1 - T(3) * wp1 + wp2) / T(6.0);
-        e5 = (T(6) * w0 - T(4) * wn1 + wn2 - T(4) * wp1 + wp2) / T(24.0);
+        a5 = (T(47) * w0 - T(13) * wn1 + T(2) * wn2 + T(27) * wp1 - T(3) * wp2) * T(1.0 / (60.0));
+        b5 = (T(-15) * w0 + wn1 + T(15) * wp1 - wp2) * T(1.0 / (12.0));
+        c5 = (T(-8) * w0 + T(6) * wn1 - wn2 + T(2) * wp1 + wp2) * T(1.0 / (8.0));
+        d5 = (T(3) * w0 - wn1 - T(3) * wp1 + wp2) * T(1.0 / (6.0));
+        e5 = (T(6) * w0 - T(4) * wn1 + wn2 - T(4) * wp1 + wp2) * T(1.0 / (24.0));
         p[3] = w0 + df[3] * (a5 + b5 * x + c5 * x2 + d5 * x3 + e5 * x4 - w0);
-        px[3] = df[3] * (b5 + T(2.0) * c5 * x + T(3.0) * d5 * x2 + T(4.0) * e5 * x3) / h;
+        px[3] = df[3] * (b5 + T(2.0) * c5 * x + T(3.0) * d5 * x2 + T(4.0) * e5 * x3) * ih;
         T a7, b7, c7, d7, e7, f7, g7;
-        a7 = (T(319) * w0 - T(101) * wn1 + T(25) * wn2 - T(3) * wn3 + T(214) * wp1 - T(38) * wp2 + T(4) * wp3) / T(420.0);
-        b7 = (T(-245) * w0 + T(25) * wn1 - T(2) * wn2 + T(245) * wp1 - T(25) * wp2 + T(2) * wp3) / T(180.0);
-        c7 = (T(-230) * w0 + T(210) * wn1 - T(57) * wn2 + T(7) * wn3 + T(15) * wp1 + T(63) * wp2 - T(8) * wp3) / T(240.0);
-        d7 = (T(28) * w0 - T(11) * wn1 + wn2 - T(28) * wp1 + T(11) * wp2 - wp3) / T(36.0);
-        e7 = (T(46) * w0 - T(39) * wn1 + T(15) * wn2 - T(2) * wn3 - T(24) * wp1 + T(3) * wp2 + wp3) / T(144.0);
-        f7 = (T(-10) * w0 + T(5) * wn1 - wn2 + T(10) * wp1 - T(5) * wp2 + wp3) / T(120.0);
-        g7 = (T(-20) * w0 + T(15) * wn1 - T(6) * wn2 + wn3 + T(15) * wp1 - T(6) * wp2 + wp3) / T(720.0);
+        a7 = (T(319) * w0 - T(101) * wn1 + T(25) * wn2 - T(3) * wn3 + T(214) * wp1 - T(38) * wp2 + T(4) * wp3) * T(1.0 / (420.0));
+        b7 = (T(-245) * w0 + T(25) * wn1 - T(2) * wn2 + T(245) * wp1 - T(25) * wp2 + T(2) * wp3) * T(1.0 / (180.0));
+        c7 = (T(-230) * w0 + T(210) * wn1 - T(57) * wn2 + T(7) * wn3 + T(15) * wp1 + T(63) * wp2 - T(8) * wp3) * T(1.0 / (240.0));
+        d7 = (T(28) * w0 - T(11) * wn1 + wn2 - T(28) * wp1 + T(11) * wp2 - wp3) * T(1.0 / (36.0));
+        e7 = (T(46) * w0 - T(39) * wn1 + T(15) * wn2 - T(2) * wn3 - T(24) * wp1 + T(3) * wp2 + wp3) * T(1.0 / (144.0));
+        f7 = (T(-10) * w0 + T(5) * wn1 - wn2 + T(10) * wp1 - T(5) * wp2 + wp3) * T(1.0 / (120.0));
+        g7 = (T(-20) * w0 + T(15) * wn1 - T(6) * wn2 + wn3 + T(15) * wp1 - T(6) * wp2 + wp3) * T(1.0 / (720.0));
         const T x5 = x * x * x * x * x, x6 = x * x * x * x * x * x;
         p[4] = w0 + df[4] * (a7 + b7 * x + c7 * x2 + d7 * x3 + e7 * x4 + f7 * x5 + g7 * x6 - w0);
-        px[4] = df[4] * (b7 + T(2.0) * c7 * x + T(3.0) * d7 * x2 + T(4.0) * e7 * x3 + T(5.0) * f7 * x4 + T(6.0) * g7 * x5) / h;
+        px[4] = df[4] * (b7 + T(2.0) * c7 * x + T(3.0) * d7 * x2 + T(4.0) * e7 * x3 + T(5.0) * f7 * x4 + T(6.0) * g7 * x5) * ih;
         T a9, b9, c9, d9, e9, f9, g9, h9, i9;
-        a9 = (T(1879) * w0 - T(641) * wn1 + T(199) * wn2 - T(41) * wn3 + T(4) * wn4 + T(1375) * wp1 - T(305) * wp2 + T(55) * wp3 - T(5) * wp4) / T(2520.0);
-        b9 = (T(-7175) * w0 + T(889) * wn1 - T(119) * wn2 + T(9) * wn3 + T(7175) * wp1 - T(889) * wp2 + T(119) * wp3 - T(9) * wp4) / T(5040.0);
-        c9 = (T(-27895) * w0 + T(28679) * wn1 - T(9835) * wn2 + T(2081) * wn3 - T(205) * wn4 - T(2065) * wp1 + T(11459) * wp2 - T(2455) * wp3 + T(236) * wp4) / T(30240.0);
-        d9 = (T(1365) * w0 - T(587) * wn1 + T(89) * wn2 - T(7) * wn3 - T(1365) * wp1 + T(587) * wp2 - T(89) * wp3 + T(7) * wp4) / T(1440.0);
-        e9 = (T(1174) * w0 - T(1160) * wn1 + T(556) * wn2 - T(128) * wn3 + T(13) * wn4 - T(464) * wp1 - T(68) * wp2 + T(88) * wp3 - T(11) * wp4) / T(3456.0);
-        f9 = (T(-75) * w0 + T(41) * wn1 - T(11) * wn2 + wn3 + T(75) * wp1 - T(41) * wp2 + T(11) * wp3 - wp4) / T(480.0);
-        g9 = (T(-380) * w0 + T(334) * wn1 - T(170) * wn2 + T(46) * wn3 - T(5) * wn4 + T(250) * wp1 - T(86) * wp2 + T(10) * wp3 + wp4) / T(8640.0);
-        h9 = (T(35) * w0 - T(21) * wn1 + T(7) * wn2 - wn3 - T(35) * wp1 + T(21) * wp2 - T(7) * wp3 + wp4) / T(5040.0);
-        i9 = (T(70) * w0 - T(56) * wn1 + T(28) * wn2 - T(8) * wn3 + wn4 - T(56) * wp1 + T(28) * wp2 - T(8) * wp3 + wp4) / T(40320.0);
+        a9 = (T(1879) * w0 - T(641) * wn1 + T(199) * wn2 - T(41) * wn3 + T(4) * wn4 + T(1375) * wp1 - T(305) * wp2 + T(55) * wp3 - T(5) * wp4) * T(1.0 / (2520.0));
+        b9 = (T(-7175) * w0 + T(889) * wn1 - T(119) * wn2 + T(9) * wn3 + T(7175) * wp1 - T(889) * wp2 + T(119) * wp3 - T(9) * wp4) * T(1.0 / (5040.0));
+        c9 = (T(-27895) * w0 + T(28679) * wn1 - T(9835) * wn2 + T(2081) * wn3 - T(205) * wn4 - T(2065) * wp1 + T(11459) * wp2 - T(2455) * wp3 + T(236) * wp4) * T(1.0 / (30240.0));
+        d9 = (T(1365) * w0 - T(587) * wn1 + T(89) * wn2 - T(7) * wn3 - T(1365) * wp1 + T(587) * wp2 - T(89) * wp3 + T(7) * wp4) * T(1.0 / (1440.0));
+        e9 = (T(1174) * w0 - T(1160) * wn1 + T(556) * wn2 - T(128) * wn3 + T(13) * wn4 - T(464) * wp1 - T(68) * wp2 + T(88) * wp3 - T(11) * wp4) * T(1.0 / (3456.0));
+        f9 = (T(-75) * w0 + T(41) * wn1 - T(11) * wn2 + wn3 + T(75) * wp1 - T(41) * wp2 + T(11) * wp3 - wp4) * T(1.0 / (480.0));
+        g9 = (T(-380) * w0 + T(334) * wn1 - T(170) * wn2 + T(46) * wn3 - T(5) * wn4 + T(250) * wp1 - T(86) * wp2 + T(10) * wp3 + wp4) * T(1.0 / (8640.0));
+        h9 = (T(35) * w0 - T(21) * wn1 + T(7) * wn2 - wn3 - T(35) * wp1 + T(21) * wp2 - T(7) * wp3 + wp4) * T(1.0 / (5040.0));
+        i9 = (T(70) * w0 - T(56) * wn1 + T(28) * wn2 - T(8) * wn3 + wn4 - T(56) * wp1 + T(28) * wp2 - T(8) * wp3 + wp4) * T(1.0 / (40320.0));
         const T x7 = x6 * x, x8 = x7 * x;
         p[5] = w0 + df[5] * (a9 + b9 * x + c9 * x2 + d9 * x3 + e9 * x4 + f9 * x5 + g9 * x6 + h9 * x7 + i9 * x8 - w0);
-        px[5] = df[5] * (b9 + T(2.0) * c9 * x + T(3.0) * d9 * x2 + T(4.0) * e9 * x3 + T(5.0) * f9 * x4 + T(6.0) * g9 * x5 + T(7.0) * h9 * x6 + T(8.0) * i9 * x7) / h;
+        px[5] = df[5] * (b9 + T(2.0) * c9 * x + T(3.0) * d9 * x2 + T(4.0) * e9 * x3 + T(5.0) * f9 * x4 + T(6.0) * g9 * x5 + T(7.0) * h9 * x6 + T(8.0) * i9 * x7) * ih;
     }
 }
 

@@ -66,6 +66,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos2d_advance.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     lib.hos2d_sync.argtypes = [vp, _DP, _DP]
     lib.hos2d_launches_per_step.argtypes = [vp]
+    lib.hos2d_profile_step.argtypes = [vp, ctypes.c_double, _DP]
     lib.hos2d_stream.argtypes = [vp]
     lib.hos2d_stream.restype = vp
     lib.hos_last_error.restype = ctypes.c_char_p
@@ -171,6 +172,13 @@ class Solver2D:
         t, dt = ctypes.c_double(), ctypes.c_double()
         _check(self._lib.hos2d_sync(self._h, ctypes.byref(t), ctypes.byref(dt)))
         return t.value, dt.value
+
+    def profile_step(self, tstop: float = 1e30) -> dict:
+        """One step with events between launches: device milliseconds per kernel."""
+        ms = np.zeros(9)
+        _check(self._lib.hos2d_profile_step(self._h, tstop, _ptr(ms)))
+        names = ["begin_step"] + [f"{k}{st}" for st in (0, 1) for k in ("bc_fill", "face_x", "face_y", "update")]
+        return dict(zip(names, ms.tolist()))
 
     @property
     def launches_per_step(self) -> int:

@@ -49,7 +49,8 @@ class CpuStep:
         st = self.fn("init")(ctypes.byref(self.params))
         if st != 0:
             raise RuntimeError(f"init failed: {st}")
-        self.fn("set_threads")(threads or os.cpu_count() or 1)
+        ncpu = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        self.fn("set_threads")(threads or ncpu)
         self.t = 0.0
         return self
 
