@@ -53,6 +53,24 @@ __device__ __forceinline__ int bc_map(int idx, int n_tot, int g, int node, int k
     return low ? 2 * g - 1 - idx : 2 * n_tot - 2 * g - 1 - idx;          // reflective
 }
 
+// arguments of the cell update kernel (defined in hos_solver.cu)
+struct UpdateArgs {
+    double* W;
+    double* Wold;
+    double* AX;
+    double* AY;
+    const double* FXx;  // x-face stage flux [4][nfx]
+    const double* FXy;  // y-face stage flux [4][nfy]
+    const double* FAx;
+    const double* FAy;
+    StepCtl* ctl;
+    int stage;
+};
+
+// step kernels defined in hos_solver.cu
+__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl);
+__global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo);
+
 // ------------------------------------------------------------------------------------------
 // face kernel
 // ------------------------------------------------------------------------------------------

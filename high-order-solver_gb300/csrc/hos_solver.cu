@@ -71,18 +71,7 @@ __global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, 
 // new state for the next step (Get_CFL / Dtx, src/time_advance.cpp:264-305: the reference
 // reads primitive variables refreshed at the start of the last stage).
 // ------------------------------------------------------------------------------------------
-struct UpdateArgs {
-    double* W;
-    double* Wold;
-    double* AX;
-    double* AY;
-    const double* FXx;  // x-face stage flux [4][nfx]
-    const double* FXy;  // y-face stage flux [4][nfy]
-    const double* FAx;
-    const double* FAy;
-    StepCtl* ctl;
-    int stage;
-};
+
 
 __device__ __forceinline__ void atomic_min_pos(unsigned long long* addr, double v) {
     // positive doubles order like their bit patterns

@@ -120,6 +120,27 @@ void* hos2d_stream(hos_solver2d* s);
 /* Human-readable text of the last error on this thread. */
 const char* hos_last_error(void);
 
+/* ---- allocation-free step ------------------------------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device memory once
+ * running (a code that reserves its whole HBM budget in its own pool at start-up, or runs
+ * under a fixed memory quota on a shared GPU): one S2O4 step on caller-owned device
+ * buffers, with the step's scratch in a fixed static device array (about 11.7 MB, held by
+ * every GPU that loads the library until exit) and no cudaMalloc / cudaFree.
+ *   d_W        conserved state, SoA planes [4][nx*ny], ghosts included (in/out)
+ *   d_alpha_x, d_alpha_y   DF indicators [nx*ny] (in/out; zero before the first step)
+ *   dt         the step's time step (the caller's CFL choice)
+ *   stream     cudaStream_t as void* (NULL: default stream); the call synchronises it
+ * Problems with nodex or nodey above HOS_STATIC_MAX_NODE or ghost above
+ * HOS_STATIC_MAX_GHOST are rejected with HOS_E_CONFIG.  The first call on a device sets up
+ * that device (looks up the array's address); make it before any stream capture.  All
+ * calls share the one array, so calls that overlap on the GPU race.  Errors are described
+ * by hos_static_last_error(). */
+#define HOS_STATIC_MAX_NODE 256
+#define HOS_STATIC_MAX_GHOST 5
+int hos2d_step_static(const hos_params2d* params, int precision, double* d_W, double* d_alpha_x,
+                      double* d_alpha_y, double dt, void* stream);
+const char* hos_static_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
