@@ -100,7 +100,12 @@ struct FaceSmem {
     static constexpr int GSTATES = TILE_N * TILE_T * 2 * GP * 12;  // [face][side][gp][12]
     static constexpr int FLUX = TILE_N * TILE_T * GP * 9;          // [face][gp][f4 d4 alpha]
     static constexpr int UNION = LINES > FLUX ? LINES : FLUX;
-    static constexpr size_t bytes = sizeof(T) * (size_t)(UNION + GSTATES);
+    // phase-1 input tile: cells n in [g+N0-1-r, g+N0+TILE_N-1+r], t as the line states
+    static constexpr int TN = TILE_N + 1 + 2 * r;
+    static constexpr int WTILE = 5 * TN * TL;                      // W[4] + normal alpha, aliases GSTATES
+    static constexpr int ATILE = (TILE_N + 1) * TL;                // tangential alpha of the face cells
+    static_assert(WTILE <= GSTATES, "input tile must fit the Gauss-state region");
+    static constexpr size_t bytes = sizeof(T) * (size_t)(UNION + GSTATES + ATILE);
 };
 
 // Gauss weights of gausspoint 2 / 3 / 4 (SetGuassPoint, src/fluid_mesh.cpp:20-44)
@@ -137,6 +142,9 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
     T* lines = reinterpret_cast<T*>(smem_raw);           // phase 1-2
     T* flux = lines;                                     // phase 3-4 (aliases lines)
     T* gst = lines + S::UNION;                           // phase 2-3
+    T* wtile = gst;                                      // phase 0-1 (aliases gst)
+    T* antile = gst + 4 * S::TN * TL;                    // phase 0-1
+    T* attile = gst + S::GSTATES;                        // phase 0-2
 
     const int nx = geo.nx, ny = geo.ny, g = geo.g;
     const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;  // faces along normal: nodeN + 1
@@ -153,6 +161,28 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
         return DIR == 0 ? (size_t)n * ny + t : (size_t)t * ny + n;
     };
 
+    // ---------------- phase 0: stage the tile's cells once, converted to T ----------------
+    // cells n in [g+N0-1-r, g+N0+TILE_N-1+r] (the normal stencils), t in [g+T0-r, g+T0+TILE_T+r);
+    // y-face states are rotated into the x-face frame here (YchangetoX: (u, v) -> (v, -u)).
+    {
+        const int nmax = DIR == 0 ? nx : ny, tmax = DIR == 0 ? ny : nx;
+        for (int c = tid; c < S::TN * TL; c += FACE_THREADS) {
+            // x faces: t (= j) runs fastest; y faces: n (= j) runs fastest -- coalesced rows
+            const int nn = DIR == 0 ? c / TL : c % S::TN;
+            const int tl = DIR == 0 ? c % TL : c / S::TN;
+            const int n = g + N0 - 1 - r + nn, t = g + T0 - r + tl;
+            if (n >= nmax || t >= tmax) continue;
+            const size_t ci = cidx(n, t);
+            T w0 = T(a.W[ci]), w1 = T(a.W[plane + ci]), w2 = T(a.W[2 * plane + ci]), w3 = T(a.W[3 * plane + ci]);
+            T* d = wtile + (nn * TL + tl) * 4;
+            if (DIR == 0) { d[0] = w0; d[1] = w1; d[2] = w2; d[3] = w3; }
+            else { d[0] = w0; d[1] = w2; d[2] = -w1; d[3] = w3; }
+            antile[nn * TL + tl] = T(a.AN[ci]);
+            if (nn >= r && nn <= r + TILE_N) attile[(nn - r) * TL + tl] = T(a.AT[ci]);
+        }
+    }
+    __syncthreads();
+
     // ---------------- phase 1: normal reconstruction of the tile's cells ----------------
     // cells n in [g+N0-1, g+N0+TILE_N), t in [g+T0-r, g+T0+TILE_T+r)
     for (int c = tid; c < (TILE_N + 1) * TL; c += FACE_THREADS) {
@@ -164,17 +194,10 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
         T st[N][4], al[N];
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-            const size_t ci = cidx(n + k - r, t);
-            T w[4];
+            const T* q = wtile + ((nl + k) * TL + tl) * 4;
 #pragma unroll
-            for (int v = 0; v < 4; ++v) w[v] = T(a.W[v * plane + ci]);
-            if (DIR == 0) {
-#pragma unroll
-                for (int v = 0; v < 4; ++v) st[k][v] = w[v];
-            } else {  // YchangetoX: (u, v) -> (v, -u)
-                st[k][0] = w[0]; st[k][1] = w[2]; st[k][2] = -w[1]; st[k][3] = w[3];
-            }
-            al[k] = T(a.AN[ci]);
+            for (int v = 0; v < 4; ++v) st[k][v] = q[v];
+            al[k] = antile[(nl + k) * TL + tl];
         }
         T df[NW];
         df_factors<T, ORDER>(al, df);
@@ -254,13 +277,9 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
         if (facen <= nodeN && facet < nodeT) {
             constexpr int sgn = DIR == 0 ? 1 : -1;  // y-face tangents run toward -x
             const int tc = ft + r;                  // centre line index in the tile
-            const int ncell = g + facen - 1 + side; // cell column of this side
             T al[N];
 #pragma unroll
-            for (int k = 0; k < N; ++k) {
-                const int t = g + facet + sgn * (k - r);
-                al[k] = T(a.AT[cidx(ncell, t)]);
-            }
+            for (int k = 0; k < N; ++k) al[k] = attile[(fn + side) * TL + tc + sgn * (k - r)];
             T df[NW];
             df_factors<T, ORDER>(al, df);
             auto line = [&](int k, int sd) -> const T* {
@@ -402,35 +421,44 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
     }
     __syncthreads();
 
-    // ---------------- phase 4: Gauss-weighted S2O4 stage combination (FP64) ----------------
+    // ---------------- phase 4: Gauss quadrature, S2O4 stage combination, face DF indicator ----------------
     if (tid < TILE_N * TILE_T) {
         const int fidx = tid, fn = fidx / TILE_T, ft = fidx % TILE_T;
         const int facen = N0 + fn, facet = T0 + ft;
         if (facen <= nodeN && facet < nodeT) {
             const size_t nf = DIR == 0 ? (size_t)(geo.nodex + 1) * geo.nodey : (size_t)geo.nodex * (geo.nodey + 1);
             const size_t fi = DIR == 0 ? (size_t)facen * geo.nodey + facet : (size_t)facet * (geo.nodey + 1) + facen;
-            double X[4], P[4];
-            double asum = 0.0;
+            // Gauss quadrature of f and f_t over the face in the compute type; the S2O4
+            // stage combination of the two time-integral moments below is FP64
+            T Fq[4], Dq[4], asum = T(0.0);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) { X[v] = 0.0; P[v] = 0.0; }
+            for (int v = 0; v < 4; ++v) { Fq[v] = T(0.0); Dq[v] = T(0.0); }
 #pragma unroll
             for (int ig = 0; ig < GP; ++ig) {
                 const T* o = flux + (fidx * GP + ig) * 9;
-                const double gw = gauss_weight<GP>(ig);
+                const T gw = T(gauss_weight<GP>(ig));
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
-                    const double fv = double(o[v]), dv = double(o[4 + v]);
-                    if (a.stage == 0) {
-                        X[v] += gw * (0.5 * fv + (1.0 / 8.0) * dv);
-                        P[v] += gw * (1.0 * fv + (1.0 / 6.0) * dv);
-                    } else {
-                        X[v] += gw * (0.0 * fv + (1.0 / 3.0) * dv);
-                    }
+                    Fq[v] += gw * o[v];
+                    Dq[v] += gw * o[4 + v];
                 }
-                asum += double(o[8]);
+                asum += o[8];
+            }
+            double X[4], P[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const double F = double(Fq[v]), D = double(Dq[v]);
+                if (a.stage == 0) {
+                    X[v] = 0.5 * F + (1.0 / 8.0) * D;
+                    P[v] = 1.0 * F + (1.0 / 6.0) * D;
+                } else {
+                    X[v] = (1.0 / 3.0) * D;
+                    P[v] = 0.0;
+                }
             }
             // mean over Gauss points, zeroed below 2 (Calculate_alpha, :1497-1516)
-            double am = GP == 2 ? 0.5 * asum : GP == 3 ? asum / 3.0 : 0.25 * asum;
+            const double as = double(asum);
+            double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
             a.FA[fi] = am < 2.0 ? 0.0 : am;
             if (a.stage == 1) {
 #pragma unroll

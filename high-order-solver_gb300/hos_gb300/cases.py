@@ -12,7 +12,7 @@ import math
 
 import numpy as np
 
-from .params import Problem2D
+from .params import DF_ALWAYS, DF_AFTER_FIRST_STEP, Problem1D, Problem2D
 
 
 def prim_to_con(prim: np.ndarray, gamma: float) -> np.ndarray:
@@ -142,3 +142,44 @@ def con_to_prim(con: np.ndarray, gamma: float) -> np.ndarray:
     out[..., 3] = (gamma - 1.0) * (con[..., 3] - 0.5 * con[..., 1] * con[..., 1] / rho
                                    - 0.5 * con[..., 2] * con[..., 2] / rho)
     return out
+
+
+def prim_to_con_1d(prim: np.ndarray, gamma: float) -> np.ndarray:
+    """(rho, u, p) -> (rho, rho u, rho E) (Primvar_to_convar_1D, src/basic_function.cpp:844-849)."""
+    rho, u, p = prim[..., 0], prim[..., 1], prim[..., 2]
+    out = np.empty_like(prim)
+    out[..., 0] = rho
+    out[..., 1] = rho * u
+    out[..., 2] = rho * (p / rho / (gamma - 1) + 0.5 * (u * u))
+    return out
+
+
+def sod1d(n: int = 1000, order: int = 5, characteristic: bool = True) -> tuple:
+    """Sod shock tube on [0, 1]: (1, 0, 1) | (0.125, 0, 0.1) at x = 0.5, outflow ends,
+    WENO5-AO at step 0 then WENO5-AO-DF, GKS c1 = 0.05, c2 = 1, CFL 0.5 (SodTubeProblem,
+    src/1Dproblem.cpp:3-174).  Returns (problem, convar[nx, 3])."""
+    pb = Problem1D(nodex=n, order=order, characteristic=characteristic,
+                   df_mode=DF_AFTER_FIRST_STEP if order == 5 else DF_ALWAYS, update_alpha=True)
+    g = pb.ghost
+    prim = np.zeros((pb.nx, 3))
+    i = np.arange(pb.nx)
+    left = (i - g + 1).astype(np.float64) * pb.dx <= 0.5
+    prim[left] = (1.0, 0.0, 1.0)
+    prim[~left] = (0.125, 0.0, 0.1)
+    prim[:g] = prim[g]
+    return pb, prim_to_con_1d(prim, pb.gamma)
+
+
+def sinwave1d(n: int = 20) -> tuple:
+    """The reference's 1D accuracy test (accuracy_sinwave_1d, src/1Dproblem.cpp:540-706):
+    exact cell averages of rho = 1 + 0.2 sin(pi x) on the periodic [0, 2], u = p = 1,
+    WENO5-AO-DF in conservative variables with the DF indicators never updated, c1 = c2 = 0,
+    CFL 0.1.  Returns (problem, convar[nx, 3])."""
+    pb = Problem1D(nodex=n, order=5, characteristic=False, df_mode=DF_ALWAYS, update_alpha=False,
+                   c1_euler=0.0, c2_euler=0.0, cfl=0.1, left=0.0, right=2.0, bc=("periodic", "periodic"))
+    g = pb.ghost
+    pi = 3.14159265358979323846
+    i = np.arange(pb.nx)
+    prim = np.ones((pb.nx, 3))
+    prim[:, 0] = 1.0 - 0.2 / pi / pb.dx * (np.cos(pi * (i + 1 - g) * pb.dx) - np.cos(pi * (i - g) * pb.dx))
+    return pb, prim_to_con_1d(prim, pb.gamma)

@@ -88,3 +88,62 @@ class Problem2D:
             for v in range(4):
                 p.bc_prim[s][v] = float(self.bc_prim[s][v])
         return p
+
+
+class Params1D(ctypes.Structure):
+    """ctypes mirror of hos_params1d (include/hos_gb300.h): the knobs of the reference's 1D
+    drivers (SodTubeProblem, accuracy_sinwave_1d, src/1Dproblem.cpp:3-149, 540-640)."""
+
+    _fields_ = [
+        ("nodex", ctypes.c_int), ("ghost", ctypes.c_int), ("order", ctypes.c_int),
+        ("characteristic", ctypes.c_int), ("df_mode", ctypes.c_int), ("update_alpha", ctypes.c_int),
+        ("K", ctypes.c_int), ("gamma", ctypes.c_double), ("c1_euler", ctypes.c_double),
+        ("c2_euler", ctypes.c_double), ("cfl", ctypes.c_double), ("left", ctypes.c_double),
+        ("right", ctypes.c_double), ("bc", ctypes.c_int * 2),
+    ]
+
+
+# df_mode values: non-DF WENO5-AO always / DF variant always / non-DF at step 0 then DF
+DF_NEVER, DF_ALWAYS, DF_AFTER_FIRST_STEP = 0, 1, 2
+
+
+@dataclass
+class Problem1D:
+    """A 1D problem (one reference 1D driver)."""
+
+    nodex: int
+    order: int = 5
+    characteristic: bool = True
+    df_mode: int = DF_AFTER_FIRST_STEP
+    update_alpha: bool = True
+    ghost: int = 5
+    K: int = 4
+    gamma: float = 1.4
+    c1_euler: float = 0.05
+    c2_euler: float = 1.0
+    cfl: float = 0.5
+    left: float = 0.0
+    right: float = 1.0
+    bc: tuple = ("free", "free")
+
+    @property
+    def nx(self) -> int:
+        return self.nodex + 2 * self.ghost
+
+    @property
+    def dx(self) -> float:
+        return (self.right - self.left) / self.nodex
+
+    def to_c(self) -> Params1D:
+        p = Params1D()
+        p.nodex, p.ghost, p.order = self.nodex, self.ghost, self.order
+        p.characteristic = 1 if self.characteristic else 0
+        p.df_mode = int(self.df_mode)
+        p.update_alpha = 1 if self.update_alpha else 0
+        p.K = self.K
+        p.gamma, p.c1_euler, p.c2_euler, p.cfl = self.gamma, self.c1_euler, self.c2_euler, self.cfl
+        p.left, p.right = self.left, self.right
+        for s in range(2):
+            b = self.bc[s]
+            p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
+        return p

@@ -20,7 +20,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .params import Params2D, Problem2D
+from .params import Params1D, Params2D, Problem1D, Problem2D
 
 HOS_OK, HOS_E_BLOWUP, HOS_E_CONFIG, HOS_E_CUDA, HOS_E_ARG, HOS_E_NOMEM = range(6)
 FP64, FP32 = 0, 1
@@ -70,6 +70,14 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos2d_stream.argtypes = [vp]
     lib.hos2d_stream.restype = vp
     lib.hos_last_error.restype = ctypes.c_char_p
+    lib.hos1d_create.argtypes = [ctypes.POINTER(Params1D), ctypes.c_int, ctypes.POINTER(vp)]
+    lib.hos1d_destroy.argtypes = [vp]
+    lib.hos1d_set_state.argtypes = [vp, _DP]
+    lib.hos1d_get_state.argtypes = [vp, _DP, _DP]
+    lib.hos1d_step.argtypes = [vp, ctypes.c_double]
+    lib.hos1d_run.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.hos1d_sync.argtypes = [vp, _DP, _DP]
+    lib.hos1d_last_error.restype = ctypes.c_char_p
     _LIB = lib
     return lib
 
@@ -198,3 +206,61 @@ class Solver2D:
             steps += k
             t, _ = self.sync()
         return steps
+
+
+def _check1(code: int) -> None:
+    if code == HOS_OK:
+        return
+    msg = load().hos1d_last_error().decode(errors="replace")
+    if code == HOS_E_BLOWUP:
+        raise HosBlowUp(msg)
+    raise HosError(f"hos error {code}: {msg}")
+
+
+class Solver1D:
+    """One 1D problem resident on the current CUDA device (the reference's 1D drivers)."""
+
+    def __init__(self, problem: Problem1D, precision: int = FP64):
+        self.problem = problem
+        self._lib = load()
+        self._params = problem.to_c()
+        h = ctypes.c_void_p()
+        _check1(self._lib.hos1d_create(ctypes.byref(self._params), precision, ctypes.byref(h)))
+        self._h = h
+        self.nx = problem.nx
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hos1d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, convar: np.ndarray) -> None:
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        if c.size != 3 * self.nx:
+            raise ValueError("convar must hold nx*3 values")
+        _check1(self._lib.hos1d_set_state(self._h, _ptr(c)))
+
+    def get_state(self):
+        c = np.empty(3 * self.nx)
+        a = np.empty(self.nx)
+        _check1(self._lib.hos1d_get_state(self._h, _ptr(c), _ptr(a)))
+        return dict(convar=c.reshape(self.nx, 3), alpha=a)
+
+    def step(self, tstop: float) -> None:
+        _check1(self._lib.hos1d_step(self._h, tstop))
+
+    def run(self, tstop: float, max_steps: int = 10**9) -> int:
+        n = ctypes.c_int()
+        _check1(self._lib.hos1d_run(self._h, tstop, max_steps, ctypes.byref(n)))
+        return n.value
+
+    def sync(self) -> tuple[float, float]:
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        _check1(self._lib.hos1d_sync(self._h, ctypes.byref(t), ctypes.byref(dt)))
+        return t.value, dt.value

@@ -120,6 +120,47 @@ void* hos2d_stream(hos_solver2d* s);
 /* Human-readable text of the last error on this thread. */
 const char* hos_last_error(void);
 
+/* ---- 1D path --------------------------------------------------------------------------
+ * The reference's 1D drivers (SodTubeProblem, accuracy_sinwave_1d, src/1Dproblem.cpp:3-149,
+ * 519-735) over Fluid1d arrays: state of cell i at index i over the full line including
+ * ghosts, 3 doubles per cell (rho, rho*u, rho*E).  Replaces (file:line):
+ *   globals + Block1d + SetUniformMesh ..... src/1Dproblem.cpp:8-76            -> hos1d_create
+ *   ICforSodTube / ICfor_sinwave ........... src/1Dproblem.cpp:151-174, 692-706 -> hos1d_set_state
+ *   output1d ............................... src/output.cpp:3-15               -> hos1d_get_state
+ *   loop body: CopyFluid_new_to_old, Get_CFL, boundaries, Reconstruction_within_cell,
+ *     Reconstruction_forg0, Calculate_flux, Update, Update_alpha (src/1Dproblem.cpp:93-131)
+ *                                                                               -> hos1d_step
+ *   the while loop to tstop ................ src/1Dproblem.cpp:78-148          -> hos1d_run */
+typedef struct hos_params1d {
+    int nodex, ghost;
+    int order;            /* 5, 7, 9                                                        */
+    int characteristic;   /* reconstruction_variable                                        */
+    int df_mode;          /* 0: WENO5-AO (no DF) every step; 1: DF variant every step;
+                             2: WENO5-AO at step 0, then WENO5-AO-DF (the Sod driver)         */
+    int update_alpha;     /* 1: Update_alpha after every stage (Sod); 0: never (accuracy)  */
+    int K;
+    double gamma;
+    double c1_euler, c2_euler;
+    double cfl;
+    double left, right;
+    int bc[2];            /* HOS_BC_FREE, HOS_BC_PERIODIC or HOS_BC_REFLECT, left and right */
+} hos_params1d;
+
+typedef struct hos_solver1d hos_solver1d;
+
+int hos1d_create(const hos_params1d* params, int precision, hos_solver1d** out);
+int hos1d_destroy(hos_solver1d* s);
+/* host arrays [nx][3]; set_state resets time, step count and DF indicators (synchronous) */
+int hos1d_set_state(hos_solver1d* s, const double* convar);
+int hos1d_get_state(hos_solver1d* s, double* convar, double* alpha);
+/* one S2O4 step (asynchronous); steps queued once t >= tstop do nothing */
+int hos1d_step(hos_solver1d* s, double tstop);
+/* steps until t >= tstop or max_steps more steps; steps_done (may be NULL) receives the
+ * number of steps taken since hos1d_set_state */
+int hos1d_run(hos_solver1d* s, double tstop, int max_steps, int* steps_done);
+int hos1d_sync(hos_solver1d* s, double* t, double* dt);
+const char* hos1d_last_error(void);
+
 /* ---- allocation-free step ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory once
  * running (a code that reserves its whole HBM budget in its own pool at start-up, or runs

@@ -68,6 +68,33 @@ int    ref2d_step(double tstop, double t, double* dt_out);
 void   ref2d_get_gauss(int dir, double* out);
 void   ref2d_get_flux(int dir, int stage, double* out);
 
+/* ---- 1D (SodTubeProblem / accuracy_sinwave_1d, src/1Dproblem.cpp) ----
+ * State: cell i at index i over the full line including ghosts, 3 doubles per cell. */
+typedef struct hos1d_params {
+    int nodex, ghost;
+    int order;            /* 5, 7, 9 (DF variants); 5 also has the non-DF variant      */
+    int characteristic;   /* 1: characteristic variables, 0: conservative              */
+    int df_mode;          /* 0: non-DF WENO5-AO every step; 1: DF variant every step;
+                             2: non-DF at step 0, DF from step 1 (the Sod driver)        */
+    int update_alpha;     /* 1: Update_alpha after every stage (Sod); 0: never (accuracy) */
+    int K;
+    double gamma;
+    double c1_euler, c2_euler;
+    double cfl;
+    double left, right;
+    int bc[2];            /* left, right: HOS_BC_FREE / PERIODIC / REFLECT              */
+} hos1d_params;
+
+int    oracle1d_init(const hos1d_params* p);
+void   oracle1d_set_state(const double* convar);
+void   oracle1d_get_state(double* convar, double* alpha);
+int    oracle1d_step(double tstop, double t, int step, double* dt_out);
+
+int    ref1d_init(const hos1d_params* p);
+void   ref1d_set_state(const double* convar);
+void   ref1d_get_state(double* convar, double* alpha);
+int    ref1d_step(double tstop, double t, int step, double* dt_out);
+
 #ifdef __cplusplus
 }
 #endif

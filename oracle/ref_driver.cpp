@@ -214,3 +214,100 @@ void ref2d_get_flux(int dir, int stage, double* out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// 1D: the loop body of SodTubeProblem / accuracy_sinwave_1d (src/1Dproblem.cpp:93-131,
+// :606-640): CopyFluid_new_to_old, Get_CFL, the scheme switch after step 0, and per stage
+// the two boundary calls, Reconstruction_within_cell, Reconstruction_forg0, Calculate_flux,
+// Update and (when the driver uses it) Update_alpha.
+// ---------------------------------------------------------------------------------------
+namespace {
+Block1d g_b1;
+Fluid1d* g_f1 = nullptr;
+Interface1d* g_i1 = nullptr;
+Flux1d** g_fl1 = nullptr;
+hos1d_params g_p1;
+}  // namespace
+
+extern "C" {
+
+int ref1d_init(const hos1d_params* p) {
+    g_p1 = *p;
+    Block1d block;
+    block.nodex = p->nodex;
+    block.ghost = p->ghost;
+    block.CFL = p->cfl;
+    K = p->K;
+    Gamma = p->gamma;
+    gks1dsolver = gks2nd;
+    tau_type = Euler;
+    c1_euler = p->c1_euler;
+    c2_euler = p->c2_euler;
+    wenotype = wenoz;
+    reconstruction_variable = p->characteristic ? characteristic : conservative;
+    g0reconstruction = Center_collision;
+    flux_function = GKS;
+    timecoe_list = S2O4;
+    Initial_stages(block);
+    block.nx = block.nodex + 2 * block.ghost;
+    block.nodex_begin = block.ghost;
+    block.nodex_end = block.nodex + block.ghost - 1;
+    g_f1 = new Fluid1d[block.nx];
+    g_i1 = new Interface1d[block.nx + 1];
+    g_fl1 = Setflux_array(block);
+    block.left = p->left;
+    block.right = p->right;
+    block.dx = (block.right - block.left) / block.nodex;
+    SetUniformMesh(block, g_f1, g_i1, g_fl1);
+    block.t = 0;
+    block.step = 0;
+    g_b1 = block;
+    return 0;
+}
+
+void ref1d_set_state(const double* convar) {
+    for (int i = 0; i < g_b1.nx; ++i)
+        for (int v = 0; v < 3; ++v) g_f1[i].convar[v] = convar[3 * i + v];
+}
+
+void ref1d_get_state(double* convar, double* alpha) {
+    for (int i = 0; i < g_b1.nx; ++i) {
+        for (int v = 0; v < 3; ++v)
+            if (convar) convar[3 * i + v] = g_f1[i].convar[v];
+        if (alpha) alpha[i] = g_f1[i].alpha;
+    }
+}
+
+int ref1d_step(double tstop, double t, int step, double* dt_out) {
+    g_b1.t = t;
+    g_b1.step = step;
+    CopyFluid_new_to_old(g_f1, g_b1);
+    g_b1.dt = Get_CFL(g_b1, g_f1, tstop);
+    if (dt_out) *dt_out = g_b1.dt;
+    const bool df = g_p1.df_mode == 1 || (g_p1.df_mode == 2 && step > 0);
+    using Recon1 = Reconstruction_within_Cell;
+    if (g_p1.order == 5) cellreconstruction = df ? static_cast<Recon1>(WENO5_AO_with_DF) : static_cast<Recon1>(WENO5_AO);
+    else if (g_p1.order == 7) cellreconstruction = static_cast<Recon1>(WENO7_AO_with_DF);
+    else cellreconstruction = static_cast<Recon1>(WENO9_AO_with_DF);
+    Fluid1d bcv;
+    for (int i = 0; i < g_b1.stages; ++i) {
+        for (int side = 0; side < 2; ++side) {
+            const int kind = g_p1.bc[side];
+            if (kind == HOS_BC_FREE) {
+                if (side) free_boundary_right(g_f1, g_b1, bcv); else free_boundary_left(g_f1, g_b1, bcv);
+            } else if (kind == HOS_BC_PERIODIC) {
+                if (side) periodic_boundary_right(g_f1, g_b1, bcv); else periodic_boundary_left(g_f1, g_b1, bcv);
+            } else {
+                if (side) reflection_boundary_right(g_f1, g_b1, bcv); else reflection_boundary_left(g_f1, g_b1, bcv);
+            }
+        }
+        Reconstruction_within_cell(g_i1, g_f1, g_b1);
+        Reconstruction_forg0(g_i1, g_f1, g_b1);
+        Calculate_flux(g_fl1, g_i1, g_b1, i);
+        Update(g_f1, g_fl1, g_b1, i);
+        if (g_p1.update_alpha) Update_alpha(g_i1, g_f1, g_b1);
+    }
+    return 0;
+}
+
+}  // extern "C"

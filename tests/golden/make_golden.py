@@ -21,7 +21,7 @@ sys.path.insert(0, str(ROOT / "high-order-solver_gb300"))
 sys.path.insert(0, str(ROOT / "tests"))
 
 from hos_gb300 import cases  # noqa: E402
-from oracle_lib import CpuStep  # noqa: E402
+from oracle_lib import CpuStep, CpuStep1D  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
 
@@ -49,6 +49,39 @@ def sinwave_errors(n, tstop=2.0):
     return np.array([e.mean(), np.sqrt((e * e).mean()), e.max()])
 
 
+def sinwave1d_errors(n, tstop=2.0):
+    """1D accuracy driver (accuracy_sinwave_1d, src/1Dproblem.cpp:519-735): L1/L2/Linf of rho."""
+    pb, con = cases.sinwave1d(n)
+    r = CpuStep1D("ref").init(pb)
+    r.set_state(con)
+    r.run(tstop)
+    g = pb.ghost
+    e = np.abs(r.state()["convar"][g:-g, 0] - con[g:-g, 0])
+    return np.array([e.mean(), np.sqrt((e * e).mean()), e.max()])
+
+
+def one_d():
+    """Config 1 of the benchmark definition: 1D Sod, 1000 cells, run to t = 0.2 (plus small
+    variants), and the reference's 1D known-answer test at 10/20/40/80 cells."""
+    for name, (pb, con), tstop in (("sod1d_w5_char_1000", cases.sod1d(1000), 0.2),
+                                   ("sod1d_w7_char_200", cases.sod1d(200, order=7), 0.2),
+                                   ("sod1d_w9_char_200", cases.sod1d(200, order=9), 0.2),
+                                   ("sod1d_w5_cons_200", cases.sod1d(200, characteristic=False), 0.2)):
+        r = CpuStep1D("ref").init(pb)
+        r.set_state(con)
+        dts = [r.step(tstop) for _ in range(3)]
+        s3 = r.state()
+        n = 3 + r.run(tstop)
+        s = r.state()
+        np.savez_compressed(OUT / f"{name}.npz", convar0=con, convar3=s3["convar"], alpha3=s3["alpha"],
+                            dts=np.array(dts), convar_end=s["convar"], alpha_end=s["alpha"],
+                            t_end=np.array(r.t), steps=np.array(r.nstep))
+        print(name, r.nstep, r.t)
+    errs = {f"n{n}": sinwave1d_errors(n) for n in (10, 20, 40, 80)}
+    np.savez_compressed(OUT / "sinwave1d_w5_accuracy.npz", **errs)
+    print(errs)
+
+
 def main():
     for name, (pb, con, prim) in step_cases():
         r = CpuStep("ref").init(pb)
@@ -65,6 +98,7 @@ def main():
     errs = {f"n{n}": sinwave_errors(n) for n in (10, 20)}
     np.savez_compressed(OUT / "sinwave_w9_accuracy.npz", **errs)
     print(errs)
+    one_d()
 
 
 if __name__ == "__main__":

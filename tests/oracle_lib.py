@@ -100,3 +100,48 @@ def rel_linf(a, b, pb):
     a = interior(pb, a)
     b = interior(pb, b)
     return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+class CpuStep1D:
+    """1D counterpart of CpuStep (oracle1d_* / ref1d_*)."""
+
+    def __init__(self, kind: str = "oracle"):
+        base = CpuStep(kind)
+        self.lib = base.lib
+        self.pre = "oracle1d_" if kind == "oracle" else "ref1d_"
+
+    def fn(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def init(self, pb):
+        self.pb = pb
+        self.params = pb.to_c()
+        if self.fn("init")(ctypes.byref(self.params)) != 0:
+            raise RuntimeError("init failed")
+        self.t, self.nstep = 0.0, 0
+        return self
+
+    def set_state(self, convar):
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        self._keep = c
+        self.fn("set_state")(c.ctypes.data_as(_DP))
+        self.t, self.nstep = 0.0, 0
+
+    def step(self, tstop: float = 1e30) -> float:
+        dt = ctypes.c_double()
+        self.fn("step")(ctypes.c_double(tstop), ctypes.c_double(self.t), self.nstep, ctypes.byref(dt))
+        self.t += dt.value
+        self.nstep += 1
+        return dt.value
+
+    def run(self, tstop: float):
+        while self.t < tstop:
+            self.step(tstop)
+        return self.nstep
+
+    def state(self):
+        nx = self.pb.nx
+        c = np.empty(3 * nx)
+        a = np.empty(nx)
+        self.fn("get_state")(c.ctypes.data_as(_DP), a.ctypes.data_as(_DP))
+        return dict(convar=c.reshape(nx, 3), alpha=a)

@@ -51,7 +51,7 @@ def oracle_run(pb, con, prim, nsteps, tstop=1e30):
     return st
 
 
-GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem)
+GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem)
 
 
 def _golden_problem(name):
