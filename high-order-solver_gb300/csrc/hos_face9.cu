@@ -13,15 +13,24 @@ static cudaError_t launch_one(const FaceArgs& a, const Geometry& geo, cudaStream
     return cudaGetLastError();
 }
 
-// dynamic shared memory above 48 KB must be enabled per kernel on the current device
+// dynamic shared memory above 48 KB must be enabled per kernel on the current device; the
+// carveout asks for the largest shared-memory share of L1 so several tiles can be resident
+template <class T, int DIR>
+static cudaError_t carveout() {
+    return cudaFuncSetAttribute(face_kernel<T, 9, DIR>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
+}
+
 cudaError_t configure_faces9(int precision) {
     cudaError_t e;
     if (precision == 0) {
+        if ((e = carveout<double, 0>()) != cudaSuccess || (e = carveout<double, 1>()) != cudaSuccess) return e;
         if ((e = cudaFuncSetAttribute(face_kernel<double, 9, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)FaceSmem<double, 9>::bytes)) != cudaSuccess) return e;
         return cudaFuncSetAttribute(face_kernel<double, 9, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)FaceSmem<double, 9>::bytes);
     }
+    if ((e = carveout<float, 0>()) != cudaSuccess || (e = carveout<float, 1>()) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(face_kernel<float, 9, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)FaceSmem<float, 9>::bytes)) != cudaSuccess) return e;
     return cudaFuncSetAttribute(face_kernel<float, 9, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -28,6 +28,7 @@ struct StepCtl {
     unsigned long long cfl_bits;  // running min of CFL candidates (positive doubles as bits)
     unsigned int status; // bit 0: negative density/pressure or NaN (reference would exit)
     unsigned int active; // 0 once t >= tstop: the step's kernels return without work
+    double tbeg;         // simulation time at the start of the current step (Block2d::t)
 };
 
 struct Geometry {
@@ -45,6 +46,10 @@ struct Geometry {
 struct BcSpec {
     int kind[4];          // left, right, down, up
     double inflow[4][4];  // conserved inflow state per side
+    // wedge boundaries: x of the wall start, x of the top shock trace at t = 0 and its speed,
+    // cell-centre x of cell i = left + (i + 0.5 - ghost) dx, post/pre-shock conserved states
+    double wx0, wthr0, wspeed, left, dx;
+    double wpost[4], wpre[4];
 };
 
 __device__ __forceinline__ int bc_map(int idx, int n_tot, int g, int node, int kind, bool low) {
@@ -85,14 +90,22 @@ struct FaceArgs {
     int stage;
 };
 
-constexpr int TILE_N = 8;    // faces along the normal direction per tile
-constexpr int TILE_T = 16;   // faces along the tangential direction per tile
-constexpr int FACE_THREADS = 2 * TILE_N * TILE_T;
+// A tile is TN faces along the normal by TT along the tangent, handled by one CTA of
+// 2 * TN * TT = 256 threads (one thread per face side in the tangential phase).
+constexpr int FACE_THREADS = 256;
+template <int TN_, int TT_> struct TileShape {
+    static constexpr int N = TN_, T = TT_;
+    static_assert(2 * TN_ * TT_ == FACE_THREADS, "a tile has 128 faces");
+};
+using DefaultTile = TileShape<8, 16>;
+constexpr int TILE_N = DefaultTile::N;    // default tile: 8 faces along the normal
+constexpr int TILE_T = DefaultTile::T;    // by 16 along the tangent
 
 template <int ORDER> struct GaussCount { static constexpr int GP = ORDER == 5 ? 2 : ORDER == 7 ? 3 : 4; };
 
-template <class T, int ORDER>
+template <class T, int ORDER, class TS = DefaultTile>
 struct FaceSmem {
+    static constexpr int TILE_N = TS::N, TILE_T = TS::T;
     static constexpr int r = ORDER / 2;
     static constexpr int GP = GaussCount<ORDER>::GP;
     static constexpr int TL = TILE_T + 2 * r;                      // line states along t
@@ -133,12 +146,14 @@ __device__ __forceinline__ T alpha_k(const T* wl, const T* wr, T gamma) {
     return A;
 }
 
-template <class T, int ORDER, int DIR>
-__global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry geo) {
-    using S = FaceSmem<T, ORDER>;
+// One tile of faces: N0, T0 are the first face indices along the normal and the tangent.
+template <class T, int ORDER, int DIR, class TS>
+__device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo, const int N0, const int T0,
+                                          unsigned char* smem_raw) {
+    using S = FaceSmem<T, ORDER, TS>;
+    constexpr int TILE_N = TS::N, TILE_T = TS::T;
     constexpr int r = S::r, N = ORDER, GP = S::GP, TL = S::TL;
     constexpr int NW = AO<ORDER>::N;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* lines = reinterpret_cast<T*>(smem_raw);           // phase 1-2
     T* flux = lines;                                     // phase 3-4 (aliases lines)
     T* gst = lines + S::UNION;                           // phase 2-3
@@ -152,8 +167,6 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
     const T hN = T(1.0 / (DIR == 0 ? geo.dx : geo.dy));   // inverse normal spacing
     const T hT = T(1.0 / (DIR == 0 ? geo.dy : geo.dx));   // inverse face length
     const T gamma = T(geo.gamma), K = T(geo.K);
-    const int N0 = blockIdx.y * TILE_N;   // first face index along the normal (0-based)
-    const int T0 = blockIdx.x * TILE_T;   // first face index along the tangent
     const size_t plane = (size_t)nx * ny;
     const int tid = threadIdx.x;
     if (!a.ctl->active) return;
@@ -475,6 +488,12 @@ __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry
             }
         }
     }
+}
+
+template <class T, int ORDER, int DIR>
+__global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry geo) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    face_tile<T, ORDER, DIR, DefaultTile>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
 }
 
 }  // namespace hos

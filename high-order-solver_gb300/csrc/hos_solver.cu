@@ -41,8 +41,29 @@ __global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, 
             for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = bc.inflow[side][v];
             return;
         }
-        sj = bc_map(j, ny, g, geo.nodey, kind, side == 2);
-        flipv = kind == 2;
+        if (kind >= 4) {
+            // wedge boundaries act on i >= ghost only; the left ghost columns keep the
+            // left-side (inflow) value (src/2Dproblem.cpp:1045-1092)
+            if (i >= g) {
+                const double x = bc.left + (i + 0.5 - g) * bc.dx;
+                const double* st = nullptr;
+                if (kind == 5) {
+                    const double tb = ctl ? ctl->tbeg : 0.0;
+                    st = x < bc.wthr0 + bc.wspeed * tb ? bc.wpost : bc.wpre;
+                } else if (x < bc.wx0) {
+                    st = bc.wpost;
+                }
+                if (st) {
+                    for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = st[v];
+                    return;
+                }
+                sj = 2 * g - 1 - j;  // reflecting wall
+                flipv = true;
+            }
+        } else {
+            sj = bc_map(j, ny, g, geo.nodey, kind, side == 2);
+            flipv = kind == 2;
+        }
     }
     if (xg) {
         const int side = i < g ? 0 : 1;
@@ -188,6 +209,7 @@ __global__ void begin_step_kernel(StepCtl* ctl, double tstop, double seed) {
     const double t = ctl->t;
     // the driver loop runs while t < tstop; steps queued past it do nothing
     ctl->active = t < tstop ? 1u : 0u;
+    ctl->tbeg = t;
     if (!(t < tstop)) return;
     if (t + dt > tstop) dt = tstop - t + 1e-16;
     ctl->dt = dt;
@@ -218,6 +240,23 @@ __global__ void prim_of_state_kernel(const double* __restrict__ W, double* __res
 }
 
 static thread_local std::string g_last_error;
+
+// conserved wedge states and geometry (Primvar_to_convar_2D on the primitive states)
+void fill_wedge(BcSpec& bc, const hos_params2d& p, double dx) {
+    auto con = [&](const double* q, double* w) {
+        w[0] = q[0];
+        w[1] = q[0] * q[1];
+        w[2] = q[0] * q[2];
+        w[3] = q[0] * (q[3] / q[0] / (p.gamma - 1) + 0.5 * (q[1] * q[1] + q[2] * q[2]));
+    };
+    con(p.wedge_post, bc.wpost);
+    con(p.wedge_pre, bc.wpre);
+    bc.wx0 = p.wedge_x0;
+    bc.wthr0 = p.wedge_x0 + (p.up - p.down) / sqrt(3.0);
+    bc.wspeed = p.wedge_top_speed;
+    bc.left = p.left;
+    bc.dx = dx;
+}
 
 static int fail(int code, const std::string& msg) {
     g_last_error = msg;
@@ -352,7 +391,11 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     if (p.nodex < p.ghost || p.nodey < p.ghost) return fail(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail(HOS_E_CONFIG, "precision must be HOS_FP64 or HOS_FP32");
     for (int k = 0; k < 4; ++k)
-        if (p.bc[k] < 0 || p.bc[k] > 3) return fail(HOS_E_CONFIG, "bad boundary kind");
+        if (p.bc[k] < 0 || p.bc[k] > 5) return fail(HOS_E_CONFIG, "bad boundary kind");
+    if (p.bc[0] >= 4 || p.bc[1] >= 4 || (p.bc[2] == HOS_BC_WEDGE_TOP) || (p.bc[3] == HOS_BC_WEDGE_BOTTOM))
+        return fail(HOS_E_CONFIG, "wedge boundaries: HOS_BC_WEDGE_BOTTOM on the bottom, HOS_BC_WEDGE_TOP on the top");
+    if ((p.bc[2] >= 4 || p.bc[3] >= 4) && p.bc[0] != HOS_BC_INFLOW)
+        return fail(HOS_E_CONFIG, "wedge boundaries need an inflow left boundary");
     if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC) ||
         (p.bc[2] == HOS_BC_PERIODIC) != (p.bc[3] == HOS_BC_PERIODIC))
         return fail(HOS_E_CONFIG, "periodic boundaries must be paired");
@@ -384,6 +427,7 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
         s->bc.inflow[k][2] = q[0] * q[2];
         s->bc.inflow[k][3] = q[0] * (q[3] / q[0] / (p.gamma - 1) + 0.5 * (q[1] * q[1] + q[2] * q[2]));
     }
+    fill_wedge(s->bc, p, geo.dx);
     s->ncell = (size_t)geo.nx * geo.ny;
     s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;
     s->nfy = (size_t)geo.nodex * (geo.nodey + 1);

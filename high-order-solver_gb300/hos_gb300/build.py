@@ -18,7 +18,10 @@ LIB = PKG / "libhos_gb300.so"
 BUILD_DIR = PKG.parent / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]
+# -prec-div/-prec-sqrt/-ftz only change single-precision arithmetic: the FP32-bulk kernels
+# divide and take square roots with the fast hardware sequences; FP64 code is unaffected.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}",
+              "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 
 
 def nvcc() -> str:
@@ -36,7 +39,7 @@ def _needs_build() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h"))
+    deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps)
 
 

@@ -183,3 +183,83 @@ def sinwave1d(n: int = 20) -> tuple:
     prim = np.ones((pb.nx, 3))
     prim[:, 0] = 1.0 - 0.2 / pi / pb.dx * (np.cos(pi * (i + 1 - g) * pb.dx) - np.cos(pi * (i - g) * pb.dx))
     return pb, prim_to_con_1d(prim, pb.gamma)
+
+
+def oblique_shock_states(mach: float, gamma: float = 1.4):
+    """Pre- and post-shock primitive states of the double-Mach-reflection setup for a shock of
+    Mach number ``mach`` moving at 60 degrees into (1.4, 0, 0, 1) (Rankine-Hugoniot), and the
+    speed of its trace along a horizontal line.  Mach 10 returns the reference's literal
+    constants (src/2Dproblem.cpp:989-1013, 1031-1035)."""
+    if mach == 10.0:
+        post = (8.0, 4.125 * math.sqrt(3), -4.125, 116.5)
+        return post, (1.4, 0.0, 0.0, 1.0), 20 / math.sqrt(3.0)
+    rho1, p1 = 1.4, 1.0
+    c1 = math.sqrt(gamma * p1 / rho1)
+    m2 = mach * mach
+    rho2 = rho1 * (gamma + 1) * m2 / ((gamma - 1) * m2 + 2)
+    p2 = p1 * (2 * gamma * m2 - (gamma - 1)) / (gamma + 1)
+    un = mach * c1 * (1 - rho1 / rho2)
+    post = (rho2, un * math.sqrt(3) / 2, -un / 2, p2)
+    return post, (rho1, 0.0, 0.0, p1), 2 * mach * c1 / math.sqrt(3.0)
+
+
+def wedge2d(nodex: int = 240, nodey: int = 60, mach: float = 10.0, order: int = 5,
+            characteristic: bool = True, c1_euler: float = 0.2, c2_euler: float = 1.0) -> tuple:
+    """Oblique shock on a wedge: the reference's double Mach reflection (doubleMach,
+    ICforDoubleMach, boundaryforDoubleMach; src/2Dproblem.cpp:819-1093) on [0, 4] x [0, 1],
+    wall from x = 1/6, parameterised by the shock Mach number."""
+    post, pre, speed = oblique_shock_states(mach)
+    pb = Problem2D(nodex=nodex, nodey=nodey, order=order, characteristic=characteristic,
+                   c1_euler=c1_euler, c2_euler=c2_euler, cfl=0.5, left=0.0, right=4.0, down=0.0, up=1.0,
+                   bc=("inflow", "free", "wedge_bottom", "wedge_top"),
+                   bc_prim=(post, (0.0,) * 4, (0.0,) * 4, (0.0,) * 4),
+                   wedge_x0=1.0 / 6.0, wedge_top_speed=speed, wedge_post=post, wedge_pre=pre)
+    g = pb.ghost
+    x = pb.left + (np.arange(pb.nx) + 0.5 - g) * pb.dx
+    y = pb.down + (np.arange(pb.ny) + 0.5 - g) * pb.dy
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    behind = (X < 1.0 / 6.0) | (Y > math.sqrt(3) * (X - 1.0 / 6.0))
+    prim = np.empty((pb.nx, pb.ny, 4))
+    prim[behind] = post
+    prim[~behind] = pre
+    return pb, prim_to_con(prim, pb.gamma), prim
+
+
+def shock_vortex2d(n: int = 128, mach: float = 1.5, strength: float = 0.3, order: int = 5,
+                   characteristic: bool = True) -> tuple:
+    """Shock-vortex interaction on [0, 2] x [0, 1] (2n x n cells): a stationary normal shock at
+    x = 0.5 with upstream Mach ``mach``, upstream state (1, M sqrt(gamma), 0, 1), and an
+    isentropic vortex of strength ``strength`` (core radius 0.05, decay 0.204) centred at
+    (0.25, 0.5) in the upstream flow; inflow left, outflow right, reflective top and bottom."""
+    gamma = 1.4
+    u1 = mach * math.sqrt(gamma)
+    m2 = mach * mach
+    rho2 = (gamma + 1) * m2 / ((gamma - 1) * m2 + 2)
+    p2 = (2 * gamma * m2 - (gamma - 1)) / (gamma + 1)
+    up = (1.0, u1, 0.0, 1.0)
+    down = (rho2, u1 / rho2, 0.0, p2)
+    pb = Problem2D(nodex=2 * n, nodey=n, order=order, characteristic=characteristic,
+                   c1_euler=0.05, c2_euler=1.0, cfl=0.5, left=0.0, right=2.0, down=0.0, up=1.0,
+                   bc=("inflow", "free", "reflect", "reflect"),
+                   bc_prim=(up, (0.0,) * 4, (0.0,) * 4, (0.0,) * 4))
+    g = pb.ghost
+    x = pb.left + (np.arange(pb.nx) + 0.5 - g) * pb.dx
+    y = pb.down + (np.arange(pb.ny) + 0.5 - g) * pb.dy
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    prim = np.empty((pb.nx, pb.ny, 4))
+    prim[X < 0.5] = up
+    prim[X >= 0.5] = down
+    rc, alpha = 0.05, 0.204
+    dx_, dy_ = X - 0.25, Y - 0.5
+    tau = np.sqrt(dx_ * dx_ + dy_ * dy_) / rc
+    e = strength * np.exp(alpha * (1 - tau * tau))
+    r = np.maximum(np.sqrt(dx_ * dx_ + dy_ * dy_), 1e-300)
+    sin_t, cos_t = dy_ / r, dx_ / r
+    T = 1.0 - (gamma - 1) * strength ** 2 * np.exp(2 * alpha * (1 - tau * tau)) / (4 * alpha * gamma)
+    m = X < 0.5
+    rho = np.where(m, T ** (1 / (gamma - 1)), prim[..., 0])
+    prim[..., 1] = np.where(m, u1 + e * tau * sin_t, prim[..., 1])
+    prim[..., 2] = np.where(m, -e * tau * cos_t, prim[..., 2])
+    prim[..., 3] = np.where(m, rho * T, prim[..., 3])
+    prim[..., 0] = rho
+    return pb, prim_to_con(prim, pb.gamma), prim

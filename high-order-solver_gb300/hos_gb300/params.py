@@ -13,9 +13,10 @@ from __future__ import annotations
 import ctypes
 from dataclasses import dataclass, field
 
-BC_FREE, BC_PERIODIC, BC_REFLECT, BC_INFLOW = 0, 1, 2, 3
+BC_FREE, BC_PERIODIC, BC_REFLECT, BC_INFLOW, BC_WEDGE_BOTTOM, BC_WEDGE_TOP = 0, 1, 2, 3, 4, 5
 _BC_NAMES = {"free": BC_FREE, "outflow": BC_FREE, "periodic": BC_PERIODIC,
-             "reflect": BC_REFLECT, "reflective": BC_REFLECT, "inflow": BC_INFLOW}
+             "reflect": BC_REFLECT, "reflective": BC_REFLECT, "inflow": BC_INFLOW,
+             "wedge_bottom": BC_WEDGE_BOTTOM, "wedge_top": BC_WEDGE_TOP}
 
 # Gauss points per face the reference pairs with each WENO-AO order
 # (weno_5th/7th/9th_ao_with_df_2gauss write 2, 3 and 4 points; src/reconstruction.cpp:2700,3093,3489)
@@ -32,6 +33,8 @@ class Params2D(ctypes.Structure):
         ("left", ctypes.c_double), ("right", ctypes.c_double),
         ("down", ctypes.c_double), ("up", ctypes.c_double),
         ("bc", ctypes.c_int * 4), ("bc_prim", (ctypes.c_double * 4) * 4),
+        ("wedge_x0", ctypes.c_double), ("wedge_top_speed", ctypes.c_double),
+        ("wedge_post", ctypes.c_double * 4), ("wedge_pre", ctypes.c_double * 4),
     ]
 
 
@@ -55,6 +58,11 @@ class Problem2D:
     up: float = 1.0
     bc: tuple = ("free", "free", "free", "free")
     bc_prim: tuple = field(default_factory=lambda: ((0.0,) * 4,) * 4)
+    # oblique shock on a wedge (the reference's doubleMach boundary)
+    wedge_x0: float = 1.0 / 6.0
+    wedge_top_speed: float = 0.0
+    wedge_post: tuple = (0.0,) * 4
+    wedge_pre: tuple = (0.0,) * 4
 
     @property
     def nx(self) -> int:
@@ -87,6 +95,10 @@ class Problem2D:
             p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
             for v in range(4):
                 p.bc_prim[s][v] = float(self.bc_prim[s][v])
+        p.wedge_x0, p.wedge_top_speed = self.wedge_x0, self.wedge_top_speed
+        for v in range(4):
+            p.wedge_post[v] = float(self.wedge_post[v])
+            p.wedge_pre[v] = float(self.wedge_pre[v])
         return p
 
 

@@ -41,6 +41,11 @@ extern "C" {
 #define HOS_BC_PERIODIC 1   /* periodic_boundary_*                       */
 #define HOS_BC_REFLECT 2    /* reflection_boundary_*                     */
 #define HOS_BC_INFLOW 3     /* inflow_boundary_* with a fixed primitive state */
+/* the reference's double-Mach-reflection boundary (boundaryforDoubleMach,
+ * src/2Dproblem.cpp:1029-1093): an oblique shock hitting a wedge wall that starts at
+ * x = wedge_x0; the left side must be HOS_BC_INFLOW with the post-shock state */
+#define HOS_BC_WEDGE_BOTTOM 4 /* bottom: post-shock state for x < x0, reflecting wall after */
+#define HOS_BC_WEDGE_TOP 5    /* top: post-shock state left of the moving shock, pre-shock right */
 
 /* compute precision of reconstruction and flux; state, stage combination and the CFL
  * reduction are FP64 in both */
@@ -63,6 +68,12 @@ typedef struct hos_params2d {
     double left, right, down, up;  /* domain                                   */
     int bc[4];              /* HOS_BC_* for left, right, down, up               */
     double bc_prim[4][4];   /* inflow primitive state (rho, u, v, p) per side   */
+    /* wedge boundaries (HOS_BC_WEDGE_*): wall start, speed of the shock's trace along the
+     * top (20/sqrt(3) for the reference's Mach 10), post- and pre-shock primitive states */
+    double wedge_x0;
+    double wedge_top_speed;
+    double wedge_post[4];
+    double wedge_pre[4];
 } hos_params2d;
 
 typedef struct hos_solver2d hos_solver2d;

@@ -53,6 +53,7 @@ struct Config {
     double gloc[4] = {0, 0, 0, 0};
     double gw[4] = {0, 0, 0, 0};
     double K = 0, Gamma = 0;
+    double tbeg = 0;   // Block2d::t during the step (read by the wedge boundary)
 };
 Config C;
 
@@ -488,6 +489,27 @@ void bc_side(int side) {
                 else for (int v = 0; v < 4; ++v) W[4 * dst + v] = inflow[v];
             }
         }
+    } else if (kind == HOS_BC_WEDGE_TOP || kind == HOS_BC_WEDGE_BOTTOM) {
+        // boundaryforDoubleMach top / bottom parts (src/2Dproblem.cpp:1041-1092), i >= ghost
+        double post[4], pre[4];
+        prim_to_con(post, C.p.wedge_post);
+        prim_to_con(pre, C.p.wedge_pre);
+        const double height = C.p.up - C.p.down;
+        for (int k = 0; k < g; ++k) {
+            const int j = side == 2 ? g - 1 - k : ny - g + k;
+            for (int i = g; i < nx; ++i) {
+                const int dst = cell(i, j);
+                const double coordx = C.p.left + (i + 0.5 - g) * C.dx;
+                if (kind == HOS_BC_WEDGE_TOP) {
+                    const double* st = coordx < (C.p.wedge_x0 + height / std::sqrt(3.0) + C.p.wedge_top_speed * C.tbeg) ? post : pre;
+                    for (int v = 0; v < 4; ++v) W[4 * dst + v] = st[v];
+                } else if (coordx < C.p.wedge_x0) {
+                    for (int v = 0; v < 4; ++v) W[4 * dst + v] = post[v];
+                } else {
+                    copy(dst, cell(i, 2 * g - 1 - j), 2);
+                }
+            }
+        }
     } else {
         for (int k = 0; k < g; ++k) {
             int j = side == 2 ? g - 1 - k : ny - g + k;
@@ -614,6 +636,7 @@ void oracle2d_get_state(double* convar, double* primvar, double* alpha_x, double
 // (src/time_advance.cpp:264-305)
 double oracle2d_begin_step(double tstop, double t) {
     const int g = C.g;
+    C.tbeg = t;
 #pragma omp parallel for
     for (int i = g; i < g + C.p.nodex; ++i)
         for (int j = g; j < g + C.p.nodey; ++j)

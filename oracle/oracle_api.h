@@ -23,7 +23,8 @@ extern "C" {
 #endif
 
 /* Boundary kinds, one per side (left, right, down, up). */
-enum { HOS_BC_FREE = 0, HOS_BC_PERIODIC = 1, HOS_BC_REFLECT = 2, HOS_BC_INFLOW = 3 };
+enum { HOS_BC_FREE = 0, HOS_BC_PERIODIC = 1, HOS_BC_REFLECT = 2, HOS_BC_INFLOW = 3,
+       HOS_BC_WEDGE_BOTTOM = 4, HOS_BC_WEDGE_TOP = 5 };
 
 typedef struct hos2d_params {
     int nodex, nodey;     /* interior cells                                  */
@@ -39,6 +40,8 @@ typedef struct hos2d_params {
     double left, right, down, up;
     int bc[4];            /* left, right, down, up                           */
     double bc_prim[4][4]; /* inflow primitive state per side (rho,u,v,p)     */
+    /* wedge (double-Mach) boundaries, kinds 4 (bottom) and 5 (top) */
+    double wedge_x0, wedge_top_speed, wedge_post[4], wedge_pre[4];
 } hos2d_params;
 
 /* ---- restatement (liboracle.so) ---- */

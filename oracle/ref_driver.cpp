@@ -155,7 +155,12 @@ double ref2d_begin_step(double tstop, double t) {
 
 int ref2d_stage(int stage, double dt) {
     g_block.dt = dt;
-    for (int s = 0; s < 4; ++s) apply_bc(s);
+    if (g_bc[3] == HOS_BC_WEDGE_TOP) {
+        // the reference's own double-Mach boundary (Mach 10 states hard-wired in it)
+        boundaryforDoubleMach(g_fluids, g_block, g_bcvalue[0]);
+    } else {
+        for (int s = 0; s < 4; ++s) apply_bc(s);
+    }
     // Convar_to_Primvar exits the process on a blow-up (src/basic_function.cpp:768-772);
     // the harness checks first and reports a status instead.
     const int n = g_block.nx * g_block.ny;

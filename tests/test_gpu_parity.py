@@ -230,3 +230,19 @@ def test_fp32_bulk_deviation_bounded(order):
     ra, rb = interior(pb, a["convar"][..., 0]), interior(pb, b["convar"][..., 0])
     l1 = np.abs(ra - rb).mean() / np.abs(ra).mean()
     assert l1 <= 1e-4, l1
+
+
+@pytest.mark.parametrize("shape,mach", [((24, 24), 10.0), ((96, 24), 4.0)])
+def test_gpu_wedge_boundary_vs_oracle(shape, mach):
+    pb, con, prim = cases.wedge2d(shape[0], shape[1], mach=mach, order=5)
+    ref = oracle_run(pb, con, prim, 3, tstop=0.2)
+    got = gpu_run(pb, con, prim, 3, tstop=0.2)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+    np.testing.assert_allclose(got["dts"], ref["dts"], rtol=1e-14)
+
+
+def test_gpu_shock_vortex_vs_oracle():
+    pb, con, prim = cases.shock_vortex2d(48, mach=3.0, strength=0.4, order=5)
+    ref = oracle_run(pb, con, prim, 3)
+    got = gpu_run(pb, con, prim, 3)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64

@@ -111,3 +111,28 @@ def test_oracle_conserves_on_periodic_domain():
         o.step()
     tot = interior(pb, o.state()["convar"]).sum(axis=(0, 1))
     assert np.all(np.abs(tot - tot0) <= 1e-12 * np.abs(tot0).max())
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference checkout not present")
+def test_oracle_wedge_boundary_matches_reference_bitwise():
+    """Double-Mach-reflection boundary (boundaryforDoubleMach, src/2Dproblem.cpp:1029-1093,
+    Mach 10) on nodex = nodey (the reference's Update_alpha bound is only in range there)."""
+    pb, con, prim = cases.wedge2d(24, 24, mach=10.0, order=5)
+    a = CpuStep("ref").init(pb)
+    b = CpuStep("oracle").init(pb)
+    a.set_state(con, prim)
+    b.set_state(con, prim)
+    for _ in range(6):
+        assert a.step(0.2) == b.step(0.2)
+    assert np.array_equal(a.state()["convar"], b.state()["convar"])
+
+
+def test_oblique_shock_states_reduce_to_reference_constants():
+    post, pre, speed = cases.oblique_shock_states(10.0)
+    import math
+    assert post == (8.0, 4.125 * math.sqrt(3), -4.125, 116.5) and pre == (1.4, 0.0, 0.0, 1.0)
+    # the general Rankine-Hugoniot branch agrees with the literal Mach-10 constants
+    rho1, p1, g = 1.4, 1.0, 1.4
+    m2 = 100.0
+    assert abs(rho1 * (g + 1) * m2 / ((g - 1) * m2 + 2) - 8.0) < 1e-12
+    assert abs(p1 * (2 * g * m2 - (g - 1)) / (g + 1) - 116.5) < 1e-12
