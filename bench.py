@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CELLS, help=argparse.SUPPRESS)
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched sweep")
     return ap.parse_args()
 
 
@@ -189,6 +190,63 @@ def cpu_baseline_sample():
         el = time.perf_counter() - t0
     return {"value": n * n * steps / el, "unit": "cell-updates/s", "cores": cores, "kind": kind,
             "sample": f"{n}x{n} Riemann WENO7-AO-DF, {steps} S2O4 steps after 1 warm-up"}
+
+
+def batch_leg(dev, precision, count=64, seed=0, max_steps=4000):
+    """The batched sweep: ``count`` seeded shock-vortex / wedge problems (sides 128..768) in one
+    batch, face-tile shapes chosen by the autotuner, every step one CUDA-graph replay.  Runs
+    every problem to its end time; an event recorded after each step gives each problem's time
+    to solution (the end of the last step it was active in)."""
+    import torch
+
+    from hos_gb300 import cases
+    from hos_gb300.solver import Batch2D
+
+    sweep = cases.batch_sweep(count=count, seed=seed)
+    b = Batch2D([x[0] for x in sweep], [x[3] for x in sweep], precision)
+    for k, x in enumerate(sweep):
+        b.set_state(k, x[1], x[2])
+    t0 = time.perf_counter()
+    chosen, tune_ms = b.autotune(reps=3)
+    tune_s = time.perf_counter() - t0
+    ext = torch.cuda.ExternalStream(b.stream, device=dev)
+    b.advance(1, graph=True)          # instantiates the graph (batch step index 0)
+    for k, x in enumerate(sweep):     # back to the initial states
+        b.set_state(k, x[1], x[2])
+    base = 1
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    evs = []
+    while len(evs) < max_steps:
+        for _ in range(25):
+            b.advance(1, graph=True)
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(ext)
+            evs.append(ev)
+        if b.status(failed=True)[0] == 0:
+            break
+    torch.cuda.synchronize(dev)
+    act, t, last, failed = b.status(failed=True)
+    b.close()
+    cells = np.array([x[0].nodex * x[0].nodey for x in sweep], dtype=np.float64)
+    nsteps = last - base + 1          # steps each problem took (a failed one: up to its bad step)
+    tts = np.array([e0.elapsed_time(evs[int(n) - 1]) / 1e3 for n in nsteps])
+    done = ~failed
+    total = e0.elapsed_time(evs[int(nsteps.max()) - 1]) / 1e3
+    return {"problems": count, "seed": seed, "cells": int(cells.sum()),
+            "value": float((cells * nsteps).sum() / total), "unit": "cell-updates/s",
+            "wall_s": total, "batch_steps": int(nsteps.max()), "unfinished": int(act),
+            "blown_up": int(failed.sum()),
+            "blown_up_problems": [sweep[k][4] for k in np.flatnonzero(failed)],
+            "steps_per_problem": {"min": int(nsteps.min()), "max": int(nsteps.max())},
+            "time_to_solution_s": {"p50": float(np.percentile(tts[done], 50)),
+                                   "p99": float(np.percentile(tts[done], 99)), "max": float(tts[done].max()),
+                                   "over": "problems that reached their end time"},
+            "tiles": {"x": "x".join(map(str, Batch2D.SHAPES[chosen[0]])),
+                      "y": "x".join(map(str, Batch2D.SHAPES[chosen[1]]))},
+            "autotune_ms": tune_ms.round(3).tolist(), "autotune_s": tune_s, "graph": True,
+            "launches_per_step": 1 + 2 * 4, "gate": "off"}
 
 
 def main():
@@ -343,6 +401,8 @@ def main():
         line["roofline"]["frac"] = ach / dgemm_tflops
     if ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
+    if not args.no_batch:
+        line["variants"]["batch64_fp32"] = batch_leg(dev, FP32)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

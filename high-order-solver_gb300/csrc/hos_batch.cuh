@@ -1,0 +1,64 @@
+// hos_batch.cuh -- device side of the batched 2D step: problem descriptors, the tile table,
+// the persistent face kernel over the tiles of every problem, and the batched boundary,
+// update and step-prologue kernels (bodies shared with the single-problem step).
+#pragma once
+#include "../../include/hos_gb300.h"
+#include "hos_launch.h"
+#include "hos_step.cuh"
+
+namespace hos {
+namespace batch {
+
+struct Prob {
+    Geometry geo;
+    BcSpec bc;
+    double *W, *Wold, *AX, *AY, *FXx, *FPx, *FAx, *FXy, *FPy, *FAy;
+    StepCtl* ctl;
+    double tstop;
+    int* last_step;   // batch step index of this problem's last active step
+};
+
+struct TileRef { int p, n0, t0, pad; };
+
+// candidate tile shapes (faces along normal x tangent); 128 faces each
+using Shape0 = TileShape<8, 16>;
+using Shape1 = TileShape<4, 32>;
+using Shape2 = TileShape<16, 8>;
+constexpr int kShapes = 3;
+const int kShapeN[kShapes] = {8, 4, 16};
+const int kShapeT[kShapes] = {16, 32, 8};
+
+template <class T, int ORDER, int DIR, class TS>
+__global__ void __launch_bounds__(FACE_THREADS) face_batch_kernel(const Prob* __restrict__ probs,
+                                                                  const TileRef* __restrict__ tiles, int ntiles,
+                                                                  int stage) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        const TileRef tr = tiles[k];
+        const Prob* pr = probs + tr.p;
+        const Geometry geo = pr->geo;
+        FaceArgs a;
+        a.W = pr->W;
+        a.AN = DIR == 0 ? pr->AX : pr->AY;
+        a.AT = DIR == 0 ? pr->AY : pr->AX;
+        a.FX = DIR == 0 ? pr->FXx : pr->FXy;
+        a.FP = DIR == 0 ? pr->FPx : pr->FPy;
+        a.FA = DIR == 0 ? pr->FAx : pr->FAy;
+        a.ctl = pr->ctl;
+        a.stage = stage;
+        face_tile<T, ORDER, DIR, TS>(a, geo, tr.n0, tr.t0, smem_raw);
+        __syncthreads();  // the next tile reuses the shared memory
+    }
+}
+
+// launch / configure the face kernels of one order (defined per order in hos_batch{5,7,9}.cu);
+// orders 7 and 9 provide the default tile shape only
+cudaError_t launch_batch_faces5(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s);
+cudaError_t launch_batch_faces7(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s);
+cudaError_t launch_batch_faces9(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s);
+cudaError_t configure_batch5(int prec, int dir, int* bps);
+cudaError_t configure_batch7(int prec, int dir, int* bps);
+cudaError_t configure_batch9(int prec, int dir, int* bps);
+
+}  // namespace batch
+}  // namespace hos

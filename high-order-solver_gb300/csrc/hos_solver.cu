@@ -8,82 +8,14 @@
 
 #include "../../include/hos_gb300.h"
 #include "hos_launch.h"
+#include "hos_step.cuh"
 
 namespace hos {
 
 __global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl) {
     if (ctl && !ctl->active) return;
-    const int nx = geo.nx, ny = geo.ny, g = geo.g;
-    const long long nlr = 2LL * g * ny, ndu = 2LL * g * geo.nodex;
-    long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= nlr + ndu) return;
-    int i, j;
-    if (e < nlr) {
-        int il = (int)(e / ny);
-        j = (int)(e % ny);
-        i = il < g ? il : nx - 2 * g + il;
-    } else {
-        long long e2 = e - nlr;
-        int jl = (int)(e2 / geo.nodex);
-        i = g + (int)(e2 % geo.nodex);
-        j = jl < g ? jl : ny - 2 * g + jl;
-    }
-    const size_t plane = (size_t)nx * ny;
-    double out[4];
-    int si = i, sj = j;
-    bool flipu = false, flipv = false;
-    const bool yg = j < g || j >= ny - g;
-    const bool xg = i < g || i >= nx - g;
-    if (yg) {
-        const int side = j < g ? 2 : 3;
-        const int kind = bc.kind[side];
-        if (kind == 3) {
-            for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = bc.inflow[side][v];
-            return;
-        }
-        if (kind >= 4) {
-            // wedge boundaries act on i >= ghost only; the left ghost columns keep the
-            // left-side (inflow) value (src/2Dproblem.cpp:1045-1092)
-            if (i >= g) {
-                const double x = bc.left + (i + 0.5 - g) * bc.dx;
-                const double* st = nullptr;
-                if (kind == 5) {
-                    const double tb = ctl ? ctl->tbeg : 0.0;
-                    st = x < bc.wthr0 + bc.wspeed * tb ? bc.wpost : bc.wpre;
-                } else if (x < bc.wx0) {
-                    st = bc.wpost;
-                }
-                if (st) {
-                    for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = st[v];
-                    return;
-                }
-                sj = 2 * g - 1 - j;  // reflecting wall
-                flipv = true;
-            }
-        } else {
-            sj = bc_map(j, ny, g, geo.nodey, kind, side == 2);
-            flipv = kind == 2;
-        }
-    }
-    if (xg) {
-        const int side = i < g ? 0 : 1;
-        const int kind = bc.kind[side];
-        if (kind == 3) {
-            for (int v = 0; v < 4; ++v) out[v] = bc.inflow[side][v];
-            if (flipv) out[2] = -out[2];
-            for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = out[v];
-            return;
-        }
-        si = bc_map(i, nx, g, geo.nodex, kind, side == 0);
-        flipu = kind == 2;
-    }
-    const size_t src = (size_t)si * ny + sj;
-    for (int v = 0; v < 4; ++v) out[v] = W[v * plane + src];
-    if (flipu) out[1] = -out[1];
-    if (flipv) out[2] = -out[2];
-    for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = out[v];
+    bc_fill_one(W, geo, bc, ctl, blockIdx.x * (long long)blockDim.x + threadIdx.x);
 }
-
 
 // ------------------------------------------------------------------------------------------
 // update: W = Wold + (sum of face fluxes x length) / area over the interior cells
@@ -94,76 +26,12 @@ __global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, 
 // ------------------------------------------------------------------------------------------
 
 
-__device__ __forceinline__ void atomic_min_pos(unsigned long long* addr, double v) {
-    // positive doubles order like their bit patterns
-    atomicMin(addr, (unsigned long long)__double_as_longlong(v));
-}
-
 __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo) {
     if (!a.ctl->active) return;
-    const int nodex = geo.nodex, nodey = geo.nodey, g = geo.g, ny = geo.ny;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    double cand = 1e300;
-    unsigned int bad = 0;
-    if (idx < nodex * nodey) {
-        const int I = idx / nodey, J = idx % nodey;
-        const size_t plane = (size_t)geo.nx * ny;
-        const size_t c = (size_t)(I + g) * ny + (J + g);
-        const size_t nfx = (size_t)(nodex + 1) * nodey, nfy = (size_t)nodex * (nodey + 1);
-        const size_t fl = (size_t)I * nodey + J, fr = fl + nodey;
-        const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
-        const double area = geo.dx * geo.dy;
-        double w[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            double old;
-            if (a.stage == 0) {
-                old = a.W[v * plane + c];
-                a.Wold[v * plane + c] = old;
-            } else {
-                old = a.Wold[v * plane + c];
-            }
-            double total = 0.0;
-            total += geo.dx * a.FXy[v * nfy + fd];
-            total += -geo.dx * a.FXy[v * nfy + fu];
-            total += geo.dy * a.FXx[v * nfx + fl];
-            total += -geo.dy * a.FXx[v * nfx + fr];
-            w[v] = old + total / area;
-            a.W[v * plane + c] = w[v];
-        }
-        const int jend = nodex < nodey ? nodex : nodey;
-        if (J < jend) {
-            a.AX[c] = a.FAx[fl] + a.FAx[fr];
-            a.AY[c] = a.FAy[fd] + a.FAy[fu];
-        }
-        double pr[4];
-        to_prim<double>(pr, w, geo.gamma);
-        if (pr[0] < 0 || pr[3] < 0 || isnan(pr[0]) || isnan(pr[3])) bad = 1;
-        if (a.stage == 0) {
-            const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] / pr[0]);
-            const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
-            if (qx > 0) cand = qx;
-            if (qy > 0 && qy < cand) cand = qy;
-        }
-    }
-    // block reduction of the CFL candidate and the status bit
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        cand = fmin(cand, __shfl_xor_sync(0xffffffffu, cand, o));
-        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
-    }
-    __shared__ double sc[8];
-    __shared__ unsigned int sb[8];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { sc[wid] = cand; sb[wid] = bad; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = sc[0];
-        unsigned int b = sb[0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmin(m, sc[k]); b |= sb[k]; }
-        if (a.stage == 0 && m < 1e300) atomic_min_pos(&a.ctl->cfl_bits, m);
-        if (b) atomicOr(&a.ctl->status, 1u);
-    }
+    double cand;
+    unsigned int bad;
+    update_one(a, geo, blockIdx.x * blockDim.x + threadIdx.x, cand, bad);
+    reduce_block(cand, bad, a.ctl, a.stage == 0);
 }
 
 // CFL candidates from a primitive state (the initial data's primvar at step 0)
@@ -201,22 +69,7 @@ __global__ void __launch_bounds__(256) cfl_from_prim_kernel(const double* __rest
     }
 }
 
-// step prologue: dt from the CFL accumulator (seeded with dx, as Get_CFL seeds with the
-// first cell's dx), clipped to the stop time (src/time_advance.cpp:285-289); the
-// accumulator is re-seeded for the candidates this step's stage 0 produces.
-__global__ void begin_step_kernel(StepCtl* ctl, double tstop, double seed) {
-    double dt = __longlong_as_double((long long)ctl->cfl_bits);
-    const double t = ctl->t;
-    // the driver loop runs while t < tstop; steps queued past it do nothing
-    ctl->active = t < tstop ? 1u : 0u;
-    ctl->tbeg = t;
-    if (!(t < tstop)) return;
-    if (t + dt > tstop) dt = tstop - t + 1e-16;
-    ctl->dt = dt;
-    ctl->t = t + dt;
-    ctl->cfl_bits = (unsigned long long)__double_as_longlong(seed);
-}
-
+__global__ void begin_step_kernel(StepCtl* ctl, double tstop, double seed) { begin_step_one(ctl, tstop, seed); }
 
 // AoS [cells][4] <-> SoA [4][cells] transposes for the host-facing entry points
 __global__ void aos_to_soa_kernel(const double* __restrict__ aos, double* __restrict__ soa, size_t n) {

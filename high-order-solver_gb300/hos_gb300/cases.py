@@ -263,3 +263,34 @@ def shock_vortex2d(n: int = 128, mach: float = 1.5, strength: float = 0.3, order
     prim[..., 3] = np.where(m, rho * T, prim[..., 3])
     prim[..., 0] = rho
     return pb, prim_to_con(prim, pb.gamma), prim
+
+
+def batch_sweep(count: int = 64, seed: int = 0, side_min: int = 128, side_max: int = 768,
+                mach_min: float = 1.5, mach_max: float = 10.0, strength_max: float = 0.5,
+                order: int = 5) -> list:
+    """A seeded sweep of independent shock-vortex and oblique-shock-on-wedge problems of uneven
+    sizes: even entries are shock-vortex problems, odd entries wedges.  The grid side ``s`` (the
+    number of cells along x) is drawn uniformly from [side_min, side_max] and rounded to a
+    multiple of 4; shock-vortex grids are s x s/2 on [0,2]x[0,1], wedge grids s x s/4 on
+    [0,4]x[0,1] (square cells in both).  Shock Mach numbers are uniform in [mach_min, mach_max]
+    and vortex strengths uniform in [0, strength_max].  End times are set so that the vortex
+    crosses 0.3 of the domain height through the shock (0.3 / u_upstream) and the wedge shock
+    trace moves the same distance whatever its Mach number (0.5 / M).
+
+    Returns a list of (problem, convar, primvar, tstop, label)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        s = int(rng.integers(side_min, side_max + 1)) // 4 * 4
+        mach = float(rng.uniform(mach_min, mach_max))
+        if k % 2 == 0:
+            strength = float(rng.uniform(0.0, strength_max))
+            pb, con, prim = shock_vortex2d(s // 2, mach=mach, strength=strength, order=order)
+            tstop = 0.3 / (mach * math.sqrt(pb.gamma))
+            label = f"shock_vortex {pb.nodex}x{pb.nodey} M={mach:.2f} eps={strength:.2f}"
+        else:
+            pb, con, prim = wedge2d(s, s // 4, mach=mach, order=order)
+            tstop = 0.5 / mach
+            label = f"wedge {pb.nodex}x{pb.nodey} M={mach:.2f}"
+        out.append((pb, con, prim, tstop, label))
+    return out

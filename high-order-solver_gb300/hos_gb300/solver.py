@@ -78,6 +78,19 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos1d_run.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.hos1d_sync.argtypes = [vp, _DP, _DP]
     lib.hos1d_last_error.restype = ctypes.c_char_p
+    lib.hos_batch2d_create.argtypes = [ctypes.POINTER(Params2D), _DP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+    lib.hos_batch2d_destroy.argtypes = [vp]
+    lib.hos_batch2d_set_state.argtypes = [vp, ctypes.c_int, _DP, _DP]
+    lib.hos_batch2d_get_state.argtypes = [vp, ctypes.c_int, _DP, _DP, _DP]
+    lib.hos_batch2d_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _DP]
+    lib.hos_batch2d_advance.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.hos_batch2d_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int), _DP, ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_int)]
+    lib.hos_batch2d_cells.argtypes = [vp]
+    lib.hos_batch2d_cells.restype = ctypes.c_longlong
+    lib.hos_batch2d_stream.argtypes = [vp]
+    lib.hos_batch2d_stream.restype = vp
+    lib.hos_batch2d_last_error.restype = ctypes.c_char_p
     _LIB = lib
     return lib
 
@@ -264,3 +277,83 @@ class Solver1D:
         t, dt = ctypes.c_double(), ctypes.c_double()
         _check1(self._lib.hos1d_sync(self._h, ctypes.byref(t), ctypes.byref(dt)))
         return t.value, dt.value
+
+
+def _checkb(code: int) -> None:
+    if code == HOS_OK:
+        return
+    msg = load().hos_batch2d_last_error().decode(errors="replace")
+    if code == HOS_E_BLOWUP:
+        raise HosBlowUp(msg)
+    raise HosError(f"hos error {code}: {msg}")
+
+
+class Batch2D:
+    """Independent 2D problems advanced together (one launch per phase for the batch)."""
+
+    SHAPES = ((8, 16), (4, 32), (16, 8))   # face-tile shapes (normal x tangential)
+
+    def __init__(self, problems, tstops, precision: int = FP64):
+        self._lib = load()
+        self.problems = list(problems)
+        arr = (Params2D * len(self.problems))(*[p.to_c() for p in self.problems])
+        ts = np.ascontiguousarray(tstops, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _checkb(self._lib.hos_batch2d_create(arr, _ptr(ts), len(self.problems), precision, ctypes.byref(h)))
+        self._h = h
+        self.count = len(self.problems)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hos_batch2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, k: int, convar: np.ndarray, primvar: np.ndarray | None = None) -> None:
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        p = None if primvar is None else np.ascontiguousarray(primvar, dtype=np.float64).reshape(-1)
+        _checkb(self._lib.hos_batch2d_set_state(self._h, k, _ptr(c), _ptr(p)))
+
+    def get_state(self, k: int):
+        pb = self.problems[k]
+        c = np.empty(pb.nx * pb.ny * 4)
+        ax = np.empty(pb.nx * pb.ny)
+        ay = np.empty(pb.nx * pb.ny)
+        _checkb(self._lib.hos_batch2d_get_state(self._h, k, _ptr(c), _ptr(ax), _ptr(ay)))
+        return dict(convar=c.reshape(pb.nx, pb.ny, 4), alpha_x=ax.reshape(pb.nx, pb.ny),
+                    alpha_y=ay.reshape(pb.nx, pb.ny))
+
+    def autotune(self, reps: int = 3):
+        ch = (ctypes.c_int * 2)()
+        ms = np.zeros(6)
+        _checkb(self._lib.hos_batch2d_autotune(self._h, reps, ch, _ptr(ms)))
+        return tuple(ch), ms.reshape(2, 3)
+
+    def advance(self, nsteps: int, graph: bool = True) -> None:
+        _checkb(self._lib.hos_batch2d_advance(self._h, nsteps, 1 if graph else 0))
+
+    def status(self, failed: bool = False):
+        """(problems still running, t per problem, batch step index of each problem's last
+        step[, per-problem failure flags]).  Without ``failed`` a blown-up problem raises
+        HosBlowUp; with it, the flags say which problems stopped on a bad state."""
+        act = ctypes.c_int()
+        t = np.empty(self.count)
+        last = (ctypes.c_int * self.count)()
+        bad = (ctypes.c_int * self.count)() if failed else None
+        _checkb(self._lib.hos_batch2d_status(self._h, ctypes.byref(act), _ptr(t), last, bad))
+        if failed:
+            return act.value, t, np.array(last[:]), np.array(bad[:], dtype=bool)
+        return act.value, t, np.array(last[:])
+
+    @property
+    def cells(self) -> int:
+        return int(self._lib.hos_batch2d_cells(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.hos_batch2d_stream(self._h) or 0)

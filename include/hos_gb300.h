@@ -172,6 +172,33 @@ int hos1d_run(hos_solver1d* s, double tstop, int max_steps, int* steps_done);
 int hos1d_sync(hos_solver1d* s, double* t, double* dt);
 const char* hos1d_last_error(void);
 
+/* ---- batches of independent 2D problems ------------------------------------------------
+ * No counterpart in the reference (each of its drivers advances one Block2d).  count
+ * problems of uneven sizes, one stop time each, advanced together: one launch per phase for
+ * the whole batch (face kernels persist over a table of every problem's tiles), each problem
+ * keeping its own dt, boundaries and stop time; problems that reach their stop time idle.
+ * All problems share the WENO-AO order and the precision.  Per problem the operations are
+ * those of hos2d_step, so results equal the single-problem solver's. */
+typedef struct hos_batch2d hos_batch2d;
+int hos_batch2d_create(const hos_params2d* params, const double* tstop, int count, int precision,
+                       hos_batch2d** out);
+int hos_batch2d_destroy(hos_batch2d* b);
+int hos_batch2d_set_state(hos_batch2d* b, int k, const double* convar, const double* primvar);
+int hos_batch2d_get_state(hos_batch2d* b, int k, double* convar, double* alpha_x, double* alpha_y);
+/* time each face-tile shape (reps launches) on the current state and keep the fastest per
+ * direction; chosen[2] receives the shape indices, ms[6] the times (either may be NULL) */
+int hos_batch2d_autotune(hos_batch2d* b, int reps, int* chosen, double* ms);
+/* nsteps batch steps; with use_graph the step is captured once and replayed */
+int hos_batch2d_advance(hos_batch2d* b, int nsteps, int use_graph);
+/* problems still running, per-problem time, the batch step index of each problem's last step
+ * and per-problem failure flags (arrays of count, may be NULL).  A problem whose state turns
+ * bad (negative density/pressure or NaN: the reference's exit) stops stepping; the others go
+ * on.  With failed == NULL such a failure is reported as HOS_E_BLOWUP. */
+int hos_batch2d_status(hos_batch2d* b, int* active, double* t, int* last_step, int* failed);
+long long hos_batch2d_cells(const hos_batch2d* b);
+void* hos_batch2d_stream(hos_batch2d* b);
+const char* hos_batch2d_last_error(void);
+
 /* ---- allocation-free step ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory once
  * running (a code that reserves its whole HBM budget in its own pool at start-up, or runs

@@ -2,6 +2,8 @@
 function include/hos_gb300.h declares, the ctypes struct matches the C struct layout, and
 calls fail with a status code (no crash, no CPU fallback) when no GPU is present."""
 import ctypes
+
+import numpy as np
 import re
 import subprocess
 import textwrap
@@ -101,3 +103,16 @@ def test_bad_config_rejected_before_touching_cuda(lib):
     p.gausspoint = 2
     p.use_df = 0
     assert lib.hos2d_create(ctypes.byref(p), 0, ctypes.byref(h)) == hs.HOS_E_CONFIG
+
+
+def test_batch_sweep_is_seeded_and_in_range():
+    from hos_gb300 import cases
+
+    a = cases.batch_sweep(count=8, seed=5)
+    b = cases.batch_sweep(count=8, seed=5)
+    assert [x[4] for x in a] == [x[4] for x in b]
+    for k, (pb, con, prim, tstop, label) in enumerate(a):
+        assert 128 <= pb.nodex <= 768 and pb.nodex % 4 == 0
+        assert pb.nodey == pb.nodex // (2 if k % 2 == 0 else 4)
+        assert abs(pb.dx - pb.dy) < 1e-15 and tstop > 0
+        assert con.shape == (pb.nx, pb.ny, 4) and np.isfinite(con).all() and (con[..., 0] > 0).all()
