@@ -540,26 +540,42 @@ void free1(hos_solver1d* s) {
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
-int enqueue_step1(hos_solver1d* s, double tstop) {
-    const Geo& geo = s->geo;
-    begin1d_kernel<<<1, 1, 0, s->stream>>>(s->ctl, tstop, geo.dx, s->first ? 1 : 0);
+int enqueue_begin1(hos_solver1d* s, double tstop) {
+    begin1d_kernel<<<1, 1, 0, s->stream>>>(s->ctl, tstop, s->geo.dx, s->first ? 1 : 0);
     s->first = false;
-    for (int stage = 0; stage < 2; ++stage) {
-        bc1d_kernel<<<1, 32, 0, s->stream>>>(s->W, geo, s->ctl);
-        FaceArgs1 fa{s->W, s->AL, s->FX, s->FP, s->FA, s->ctl, stage};
-        cudaError_t e;
-        if (s->precision == 0)
-            e = geo.order == 5 ? launch_face<double, 5>(fa, geo, s->stream)
-              : geo.order == 7 ? launch_face<double, 7>(fa, geo, s->stream)
-                               : launch_face<double, 9>(fa, geo, s->stream);
-        else
-            e = geo.order == 5 ? launch_face<float, 5>(fa, geo, s->stream)
-              : geo.order == 7 ? launch_face<float, 7>(fa, geo, s->stream)
-                               : launch_face<float, 9>(fa, geo, s->stream);
-        if (e != cudaSuccess) return fail1(HOS_E_CUDA, std::string("face1d: ") + cudaGetErrorString(e));
-        update1d_kernel<<<(geo.nodex + 255) / 256, 256, 0, s->stream>>>(s->W, s->Wold, s->AL, s->FX, s->FA, s->ctl, geo, stage);
-        if ((e = cudaGetLastError()) != cudaSuccess) return fail1(HOS_E_CUDA, std::string("update1d: ") + cudaGetErrorString(e));
-    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? HOS_OK : fail1(HOS_E_CUDA, std::string("begin1d: ") + cudaGetErrorString(e));
+}
+
+int enqueue_stage1(hos_solver1d* s, int stage) {
+    const Geo& geo = s->geo;
+    bc1d_kernel<<<1, 32, 0, s->stream>>>(s->W, geo, s->ctl);
+    FaceArgs1 fa{s->W, s->AL, s->FX, s->FP, s->FA, s->ctl, stage};
+    cudaError_t e;
+    if (s->precision == 0)
+        e = geo.order == 5 ? launch_face<double, 5>(fa, geo, s->stream)
+          : geo.order == 7 ? launch_face<double, 7>(fa, geo, s->stream)
+                           : launch_face<double, 9>(fa, geo, s->stream);
+    else
+        e = geo.order == 5 ? launch_face<float, 5>(fa, geo, s->stream)
+          : geo.order == 7 ? launch_face<float, 7>(fa, geo, s->stream)
+                           : launch_face<float, 9>(fa, geo, s->stream);
+    if (e != cudaSuccess) return fail1(HOS_E_CUDA, std::string("face1d: ") + cudaGetErrorString(e));
+    update1d_kernel<<<(geo.nodex + 255) / 256, 256, 0, s->stream>>>(s->W, s->Wold, s->AL, s->FX, s->FA, s->ctl, geo, stage);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail1(HOS_E_CUDA, std::string("update1d: ") + cudaGetErrorString(e));
+    return HOS_OK;
+}
+
+int enqueue_step1(hos_solver1d* s, double tstop) {
+    int st = enqueue_begin1(s, tstop);
+    for (int stage = 0; stage < 2 && !st; ++stage) st = enqueue_stage1(s, stage);
+    return st;
+}
+
+int check_bc1(const int* bc) {
+    for (int k = 0; k < 2; ++k)
+        if (bc[k] < 0 || bc[k] > 2) return fail1(HOS_E_CONFIG, "1D boundaries: free, periodic or reflective");
+    if ((bc[0] == HOS_BC_PERIODIC) != (bc[1] == HOS_BC_PERIODIC)) return fail1(HOS_E_CONFIG, "periodic boundaries must be paired");
     return HOS_OK;
 }
 
@@ -577,9 +593,7 @@ int hos1d_create(const hos_params1d* params, int precision, hos_solver1d** out) 
     if (p.df_mode < 0 || p.df_mode > 2) return fail1(HOS_E_CONFIG, "bad df_mode");
     if (p.ghost < p.order / 2 + 1 || p.nodex < p.ghost) return fail1(HOS_E_CONFIG, "ghost/nodex too small");
     if (p.ghost > 16) return fail1(HOS_E_CONFIG, "ghost must be <= 16");  // one warp fills both ends
-    for (int k = 0; k < 2; ++k)
-        if (p.bc[k] < 0 || p.bc[k] > 2) return fail1(HOS_E_CONFIG, "1D boundaries: free, periodic or reflective");
-    if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC)) return fail1(HOS_E_CONFIG, "periodic boundaries must be paired");
+    if (int st = check_bc1(p.bc)) return st;
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail1(HOS_E_CONFIG, "bad precision");
     hos_solver1d* s = new (std::nothrow) hos_solver1d();
     if (!s) return fail1(HOS_E_NOMEM, "host allocation");
@@ -683,6 +697,44 @@ int hos1d_get_state(hos_solver1d* s, double* convar, double* alpha) {
 int hos1d_step(hos_solver1d* s, double tstop) {
     if (!s) return fail1(HOS_E_ARG, "null solver");
     return enqueue_step1(s, tstop);
+}
+
+int hos1d_begin_step(hos_solver1d* s, double tstop) {
+    if (!s) return fail1(HOS_E_ARG, "null solver");
+    return enqueue_begin1(s, tstop);
+}
+
+int hos1d_stage(hos_solver1d* s, int stage) {
+    if (!s) return fail1(HOS_E_ARG, "null solver");
+    if (stage != 0 && stage != 1) return fail1(HOS_E_ARG, "stage must be 0 or 1");
+    return enqueue_stage1(s, stage);
+}
+
+int hos1d_set_boundary(hos_solver1d* s, const int* bc) {
+    if (!s || !bc) return fail1(HOS_E_ARG, "null argument");
+    if (int st = check_bc1(bc)) return st;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fail1(HOS_E_CUDA, std::string("set_boundary: ") + cudaGetErrorString(e));
+    s->p.bc[0] = s->geo.bc[0] = bc[0];
+    s->p.bc[1] = s->geo.bc[1] = bc[1];
+    return HOS_OK;
+}
+
+int hos1d_set_alpha(hos_solver1d* s, const double* alpha) {
+    if (!s || !alpha) return fail1(HOS_E_ARG, "null argument");
+    cudaError_t e = cudaMemcpyAsync(s->AL, alpha, s->geo.nx * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? HOS_OK : fail1(HOS_E_CUDA, std::string("set_alpha: ") + cudaGetErrorString(e));
+}
+
+int hos1d_set_time(hos_solver1d* s, double t) {
+    if (!s) return fail1(HOS_E_ARG, "null solver");
+    Ctl c;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&c, s->ctl, sizeof c, cudaMemcpyDeviceToHost);
+    c.t = t;
+    if (e == cudaSuccess) e = cudaMemcpy(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? HOS_OK : fail1(HOS_E_CUDA, std::string("set_time: ") + cudaGetErrorString(e));
 }
 
 int hos1d_run(hos_solver1d* s, double tstop, int max_steps, int* steps_done) {

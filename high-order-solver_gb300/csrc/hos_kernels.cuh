@@ -73,7 +73,7 @@ struct UpdateArgs {
 };
 
 // step kernels defined in hos_solver.cu
-__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl);
+__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl, int skip_inactive);
 __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo);
 
 // ------------------------------------------------------------------------------------------

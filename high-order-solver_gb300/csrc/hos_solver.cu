@@ -12,8 +12,10 @@
 
 namespace hos {
 
-__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl) {
-    if (ctl && !ctl->active) return;
+// ghost fill; inside a step (skip_inactive) a finished problem does nothing.  ctl supplies the
+// step's start time for the time-dependent wedge boundary.
+__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl, int skip_inactive) {
+    if (skip_inactive && !ctl->active) return;
     bc_fill_one(W, geo, bc, ctl, blockIdx.x * (long long)blockDim.x + threadIdx.x);
 }
 
@@ -151,6 +153,31 @@ struct hos_solver2d {
 
 namespace {
 
+int check_boundaries(const hos_params2d& p) {
+    for (int k = 0; k < 4; ++k)
+        if (p.bc[k] < 0 || p.bc[k] > 5) return fail(HOS_E_CONFIG, "bad boundary kind");
+    if (p.bc[0] >= 4 || p.bc[1] >= 4 || (p.bc[2] == HOS_BC_WEDGE_TOP) || (p.bc[3] == HOS_BC_WEDGE_BOTTOM))
+        return fail(HOS_E_CONFIG, "wedge boundaries: HOS_BC_WEDGE_BOTTOM on the bottom, HOS_BC_WEDGE_TOP on the top");
+    if ((p.bc[2] >= 4 || p.bc[3] >= 4) && p.bc[0] != HOS_BC_INFLOW)
+        return fail(HOS_E_CONFIG, "wedge boundaries need an inflow left boundary");
+    if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC) ||
+        (p.bc[2] == HOS_BC_PERIODIC) != (p.bc[3] == HOS_BC_PERIODIC))
+        return fail(HOS_E_CONFIG, "periodic boundaries must be paired");
+    return HOS_OK;
+}
+
+void fill_boundaries(BcSpec& bc, const hos_params2d& p, double dx) {
+    for (int k = 0; k < 4; ++k) {
+        bc.kind[k] = p.bc[k];
+        const double* q = p.bc_prim[k];  // Primvar_to_convar_2D (src/basic_function.cpp:851-857)
+        bc.inflow[k][0] = q[0];
+        bc.inflow[k][1] = q[0] * q[1];
+        bc.inflow[k][2] = q[0] * q[2];
+        bc.inflow[k][3] = q[0] * (q[3] / q[0] / (p.gamma - 1) + 0.5 * (q[1] * q[1] + q[2] * q[2]));
+    }
+    fill_wedge(bc, p, dx);
+}
+
 void free_all(hos_solver2d* s) {
     double* bufs[] = {s->W, s->Wold, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->FXy, s->FPy, s->FAy, s->scratch};
     for (double* b : bufs)
@@ -169,7 +196,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     };
     {
         const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
-        bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl);
+        bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 1);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "bc_fill");
         mark(0);
     }
@@ -243,15 +270,7 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     if (p.ghost < p.order / 2 + 1) return fail(HOS_E_CONFIG, "ghost must be >= order/2 + 1");
     if (p.nodex < p.ghost || p.nodey < p.ghost) return fail(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail(HOS_E_CONFIG, "precision must be HOS_FP64 or HOS_FP32");
-    for (int k = 0; k < 4; ++k)
-        if (p.bc[k] < 0 || p.bc[k] > 5) return fail(HOS_E_CONFIG, "bad boundary kind");
-    if (p.bc[0] >= 4 || p.bc[1] >= 4 || (p.bc[2] == HOS_BC_WEDGE_TOP) || (p.bc[3] == HOS_BC_WEDGE_BOTTOM))
-        return fail(HOS_E_CONFIG, "wedge boundaries: HOS_BC_WEDGE_BOTTOM on the bottom, HOS_BC_WEDGE_TOP on the top");
-    if ((p.bc[2] >= 4 || p.bc[3] >= 4) && p.bc[0] != HOS_BC_INFLOW)
-        return fail(HOS_E_CONFIG, "wedge boundaries need an inflow left boundary");
-    if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC) ||
-        (p.bc[2] == HOS_BC_PERIODIC) != (p.bc[3] == HOS_BC_PERIODIC))
-        return fail(HOS_E_CONFIG, "periodic boundaries must be paired");
+    if (int st = check_boundaries(p)) return st;
     hos_solver2d* s = new (std::nothrow) hos_solver2d();
     if (!s) return fail(HOS_E_NOMEM, "host allocation");
     s->p = p;
@@ -272,15 +291,7 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     geo.c1 = p.c1_euler;
     geo.c2 = p.c2_euler;
     geo.characteristic = p.characteristic ? 1 : 0;
-    for (int k = 0; k < 4; ++k) {
-        s->bc.kind[k] = p.bc[k];
-        const double* q = p.bc_prim[k];  // Primvar_to_convar_2D (src/basic_function.cpp:851-857)
-        s->bc.inflow[k][0] = q[0];
-        s->bc.inflow[k][1] = q[0] * q[1];
-        s->bc.inflow[k][2] = q[0] * q[2];
-        s->bc.inflow[k][3] = q[0] * (q[3] / q[0] / (p.gamma - 1) + 0.5 * (q[1] * q[1] + q[2] * q[2]));
-    }
-    fill_wedge(s->bc, p, geo.dx);
+    fill_boundaries(s->bc, p, geo.dx);
     s->ncell = (size_t)geo.nx * geo.ny;
     s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;
     s->nfy = (size_t)geo.nodex * (geo.nodey + 1);
@@ -407,6 +418,36 @@ int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* al
     return HOS_OK;
 }
 
+int hos2d_set_boundary(hos_solver2d* s, const int* bc, const double* bc_prim) {
+    if (!s || !bc) return fail(HOS_E_ARG, "null argument");
+    hos_params2d p = s->p;
+    for (int k = 0; k < 4; ++k) {
+        p.bc[k] = bc[k];
+        if (bc_prim)
+            for (int v = 0; v < 4; ++v) p.bc_prim[k][v] = bc_prim[4 * k + v];
+    }
+    if (int st = check_boundaries(p)) return st;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "set_boundary");
+    s->p = p;
+    fill_boundaries(s->bc, p, s->geo.dx);
+    if (s->graph) {  // the captured step holds the old boundary description
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    return HOS_OK;
+}
+
+int hos2d_set_time(hos_solver2d* s, double t) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    StepCtl c;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&c, s->ctl, sizeof c, cudaMemcpyDeviceToHost);
+    c.t = t;
+    if (e == cudaSuccess) e = cudaMemcpy(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "set_time");
+}
+
 int hos2d_begin_step(hos_solver2d* s, double tstop) {
     if (!s) return fail(HOS_E_ARG, "null solver");
     return enqueue_begin(s, tstop);
@@ -416,7 +457,7 @@ int hos2d_boundary(hos_solver2d* s) {
     if (!s) return fail(HOS_E_ARG, "null solver");
     const Geometry& geo = s->geo;
     const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
-    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, nullptr);
+    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 0);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? HOS_OK : cuda_fail(e, "bc_fill");
 }

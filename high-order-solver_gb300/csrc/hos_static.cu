@@ -142,7 +142,7 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_static(HOS_E_CUDA, std::string("ctl: ") + cudaGetErrorString(e));
     for (int stage = 0; stage < 2; ++stage) {
         const long long nb = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
-        bc_fill_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(d_W, geo, bc, ctl);
+        bc_fill_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(d_W, geo, bc, ctl, 1);
         FaceArgs ax{d_W, d_alpha_x, d_alpha_y, FXx, FPx, FAx, ctl, stage};
         FaceArgs ay{d_W, d_alpha_y, d_alpha_x, FXy, FPy, FAy, ctl, stage};
         e = p.order == 5 ? launch_faces5(precision, ax, ay, geo, s)

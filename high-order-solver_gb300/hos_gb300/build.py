@@ -1,7 +1,9 @@
-"""Build the CUDA library (sm_103a) in-tree: hos_gb300/libhos_gb300.so.
+"""Build the libraries in-tree: hos_gb300/libhos_gb300.so (CUDA, sm_103a) and
+hos_gb300/libhos_ref.so (the reference's C++ function-level API over it).
 
 Each .cu translation unit is compiled by nvcc in parallel and linked into one shared
-library with the static CUDA runtime.  No cmake, no torch extension machinery.
+library with the static CUDA runtime; the C++ API layer (refapi/*.cpp) is compiled by the
+host C++ compiler and linked against libhos_gb300.so.  No cmake, no torch extension machinery.
 """
 from __future__ import annotations
 
@@ -15,6 +17,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG.parent / "csrc"
 INCLUDE = PKG.parent.parent / "include"
 LIB = PKG / "libhos_gb300.so"
+REF_LIB = PKG / "libhos_ref.so"
+REFAPI = PKG.parent / "refapi"
 BUILD_DIR = PKG.parent / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -36,11 +40,26 @@ def sources() -> list[Path]:
 
 
 def _needs_build() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not REF_LIB.exists():
         return True
-    t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
+    t = min(LIB.stat().st_mtime, REF_LIB.stat().st_mtime)
+    deps = list(CSRC.glob("*")) + list(REFAPI.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps)
+
+
+def build_refapi() -> Path:
+    """Compile the reference-API layer and link it against libhos_ref.so's CUDA library."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("a C++ compiler (g++) is required to build libhos_ref.so")
+    tmp = REF_LIB.with_suffix(".so.tmp")
+    cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", f"-I{INCLUDE}", *map(str, sorted(REFAPI.glob("*.cpp"))),
+           "-o", str(tmp), f"-L{PKG}", "-lhos_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"libhos_ref.so build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, REF_LIB)
+    return REF_LIB
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
@@ -69,6 +88,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_refapi()
     return LIB
 
 

@@ -97,13 +97,21 @@ int hos2d_set_state_device(hos_solver2d* s, const double* d_convar_soa, const do
  * (Fluid2d::alpha_x / alpha_y, include/fluid_mesh.h:146-147).  Synchronous. */
 int hos2d_set_alpha(hos_solver2d* s, const double* alpha_x, const double* alpha_y);
 
-/* Download conserved state, primitive state of the last stage, alpha_x, alpha_y
- * (host arrays; any pointer may be NULL).  Synchronous. */
+/* Download the conserved state, its primitive variables, alpha_x, alpha_y (host arrays;
+ * any pointer may be NULL).  Synchronous. */
 int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* alpha_x, double* alpha_y);
+
+/* Replace the four boundary kinds (HOS_BC_*, left, right, down, up) and, when bc_prim is not
+ * NULL, the inflow primitive states ([4][4], same order): the driver reassigning its
+ * BoundaryCondition2d slots (src/2Dproblem.cpp:20-28).  Waits for queued work. */
+int hos2d_set_boundary(hos_solver2d* s, const int* bc, const double* bc_prim);
+/* Set the simulation time (Block2d::t) the next step starts from.  Synchronous. */
+int hos2d_set_time(hos_solver2d* s, double t);
 
 /* CopyFluid_new_to_old + Get_CFL: fix this step's dt (clipped to tstop). Asynchronous. */
 int hos2d_begin_step(hos_solver2d* s, double tstop);
-/* Ghost-cell fill only. Asynchronous. */
+/* Ghost-cell fill of the current state (the wedge boundary at the current step's start
+ * time). Asynchronous. */
 int hos2d_boundary(hos_solver2d* s);
 /* One S2O4 stage (0 or 1) with the dt fixed by hos2d_begin_step. Asynchronous. */
 int hos2d_stage(hos_solver2d* s, int stage);
@@ -170,6 +178,17 @@ int hos1d_step(hos_solver1d* s, double tstop);
  * number of steps taken since hos1d_set_state */
 int hos1d_run(hos_solver1d* s, double tstop, int max_steps, int* steps_done);
 int hos1d_sync(hos_solver1d* s, double* t, double* dt);
+/* The step in pieces, for callers that keep the reference's loop (src/1Dproblem.cpp:96-131):
+ * begin_step = CopyFluid_new_to_old + Get_CFL (dt then readable through hos1d_sync), stage =
+ * boundaries + reconstruction + flux + Update + Update_alpha of S2O4 stage 0 or 1.  Both are
+ * asynchronous. */
+int hos1d_begin_step(hos_solver1d* s, double tstop);
+int hos1d_stage(hos_solver1d* s, int stage);
+/* Replace the two boundary kinds (the driver reassigning its BoundaryCondition slots). */
+int hos1d_set_boundary(hos_solver1d* s, const int* bc);
+/* Restore the DF indicators (Fluid1d::alpha, host [nx]) and the simulation time. */
+int hos1d_set_alpha(hos_solver1d* s, const double* alpha);
+int hos1d_set_time(hos_solver1d* s, double t);
 const char* hos1d_last_error(void);
 
 /* ---- batches of independent 2D problems ------------------------------------------------

@@ -5,7 +5,12 @@ seeded cases.  Run from the repository root where the reference checkout exists:
     python tests/golden/make_golden.py
 
 Each case stores the initial conserved/primitive state, the reference state (convar,
-alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps.  The 2D
+alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps.
+
+tests/golden/refapi/ holds runs of the reference-API drivers (tests/refapi/driver2d.cpp,
+driver1d.cpp) linked against the reference's own objects (oracle/Makefile, refdrivers): the
+input state, the Fluid arrays after the run and every dt; the 1D entry is the complete Sod
+run of the benchmark definition (1000 cells to t = 0.2).  The 2D
 accuracy entries store the reference's own known-answer test (sinwave_2d,
 src/2Dproblem.cpp:1347-1603): L1/L2/Linf density errors at t = 2 on 10^2 and 20^2 meshes.
 """
@@ -82,6 +87,27 @@ def one_d():
     print(errs)
 
 
+def refapi():
+    import subprocess
+
+    from refapi_lib import config1d, config2d, refapi_cases_2d, run1d, run2d
+
+    subprocess.run(["make", "-C", str(ROOT / "oracle"), "refdrivers"], check=True, capture_output=True)
+    d2 = ROOT / "oracle" / "_ref" / "driver2d"
+    d1 = ROOT / "oracle" / "_ref" / "driver1d"
+    out = OUT / "refapi"
+    out.mkdir(exist_ok=True)
+    for name, (pb, con, prim), steps in refapi_cases_2d():
+        r = run2d(d2, pb, con, prim, config2d(pb, steps))
+        np.savez_compressed(out / f"{name}.npz", convar0=con, primvar0=prim, steps_asked=steps,
+                            **{k: np.asarray(v) for k, v in r.items()})
+        print(name, r["steps"], r["dts"])
+    pb, con = cases.sod1d(1000)
+    r = run1d(d1, pb, con, config1d(pb, 100000, "switch", tstop=0.2))
+    np.savez_compressed(out / "refapi_sod1d_1000.npz", convar0=con, **{k: np.asarray(v) for k, v in r.items()})
+    print("refapi_sod1d_1000", r["steps"], r["t"])
+
+
 def main():
     for name, (pb, con, prim) in step_cases():
         r = CpuStep("ref").init(pb)
@@ -99,6 +125,7 @@ def main():
     np.savez_compressed(OUT / "sinwave_w9_accuracy.npz", **errs)
     print(errs)
     one_d()
+    refapi()
 
 
 if __name__ == "__main__":
