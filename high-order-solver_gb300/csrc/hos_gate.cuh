@@ -1,0 +1,373 @@
+// hos_gate.cuh -- the learned smoothness gate of the FP32-bulk path.
+//
+// A 16 -> 32 -> 32 -> 1 MLP (ReLU, BF16 weights and activations, FP32 accumulation on the
+// tensor cores through mma.sync m16n8k16) reads, for one cell and one direction, the
+// normalised WENO-AO smoothness indicators of the cell's normal stencil in density and
+// pressure (7 per variable: the candidate-stencil betas padded to 6, and tau) and the cell's
+// discontinuity-feedback indicator, and predicts whether the nonlinear WENO-AO weights of all
+// four characteristic variables on both faces of the cell stay within GATE_EPS of the linear
+// weights.  Where it says so, the face kernel reconstructs with the full-stencil polynomial
+// alone (no characteristic projection, no weights); everything else, and every linear result
+// that fails the positivity / oscillation check, takes the full WENO-AO path.
+//
+// The reference has no such gate; its full WENO-AO reconstruction (src/reconstruction.cpp)
+// stays the judge: labels, audits and the deviation tests compare against it.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "hos_kernels.cuh"
+
+namespace hos {
+namespace gate {
+
+constexpr int NF = 16;   // inputs
+constexpr int NH = 32;   // hidden width
+// parameter vector (floats): W1[NH][NF], b1[NH], W2[NH][NH], b2[NH], w3[NH], b3 -- weights
+// stored output-major (W[out][in]) so that an mma B fragment pair is one 32-bit load
+constexpr int OFF_W1 = 0;
+constexpr int OFF_B1 = OFF_W1 + NH * NF;
+constexpr int OFF_W2 = OFF_B1 + NH;
+constexpr int OFF_B2 = OFF_W2 + NH * NH;
+constexpr int OFF_W3 = OFF_B2 + NH;
+constexpr int OFF_B3 = OFF_W3 + NH;
+constexpr int NPARAM = OFF_B3 + 1;
+constexpr float GATE_EPS = 0.02f;   // label: max_k |omega_k - d_k| <= GATE_EPS
+constexpr int NS = NF + 4;          // sample record: features, label, distance, cell, direction
+
+// inference copy of the network: BF16 weights (w3 padded to 8 output rows) and FP32 biases
+struct Net {
+    const __nv_bfloat16* w1;   // [NH][NF]
+    const __nv_bfloat16* w2;   // [NH][NH]
+    const __nv_bfloat16* w3;   // [8][NH], rows 1..7 zero
+    const float* b1;
+    const float* b2;
+    const float* b3;
+};
+constexpr size_t NET_BF16 = NH * NF + NH * NH + 8 * NH;   // bf16 elements of the inference copy
+constexpr size_t NET_F32 = NH + NH + 1;                  // fp32 elements (biases)
+
+struct Stats {
+    unsigned long long cells[2];      // cells gated per direction
+    unsigned long long smooth[2];     // predicted smooth per direction
+    unsigned long long audited;       // predicted-smooth cells re-checked with full weights
+    unsigned long long false_neg;     // of those, weights farther than GATE_EPS from linear
+    unsigned long long samples;       // training samples written
+    unsigned long long fallback;      // linear results rejected by the a-posteriori check
+};
+
+// ---------------- features ----------------
+
+// Normalised indicators of one stencil: betas / (sum beta + tau + 1e-10 c^2), padded to 6, then
+// tau.  The floor keeps variations below 1e-5 of the value (FP32 rounding of the primitives
+// included) from looking like structure.
+template <int ORDER>
+__device__ __forceinline__ void indicator_features(const float* s, float* f) {
+    constexpr int NW = AO<ORDER>::N;
+    float beta[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const float tau = ao_betas<float, ORDER>(s, beta);
+    float sum = tau;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) sum += beta[k];
+    const float c = s[ORDER / 2];
+    const float inv = 1.0f / (sum + 1e-10f * c * c + 1e-30f);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[k] = k < NW ? beta[k] * inv : 0.0f;
+    f[6] = tau * inv;
+}
+
+// Features of cell c along direction DIR (0: x, i stride ny; 1: y, unit stride) from the FP64
+// state planes; alpha is the cell's DF indicator in that direction.
+template <int ORDER, int DIR>
+__device__ __forceinline__ void cell_features(const double* __restrict__ W, size_t plane, size_t c, long long stride,
+                                              float gamma, float alpha, float* f) {
+    constexpr int N = ORDER, r = ORDER / 2;
+    float rho[N], p[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const size_t q = (size_t)((long long)c + (k - r) * stride);
+        float w[4] = {float(W[q]), float(W[plane + q]), float(W[2 * plane + q]), float(W[3 * plane + q])};
+        float pr[4];
+        to_prim(pr, w, gamma);
+        rho[k] = pr[0];
+        p[k] = pr[3];
+    }
+    indicator_features<ORDER>(rho, f);
+    indicator_features<ORDER>(p, f + 7);
+    f[14] = alpha / (1.0f + alpha);
+    f[15] = 0.0f;
+}
+
+// True label quantity of cell c along DIR: the largest distance of the nonlinear weights from
+// the linear ones over both faces and the four (characteristic) variables, computed as the
+// face kernel's normal reconstruction would (src/reconstruction.cpp:1861-2028 for WENO7).
+template <int ORDER, int DIR>
+__device__ __forceinline__ float weight_distance(const double* __restrict__ W, size_t plane, size_t c,
+                                                 long long stride, float gamma, int characteristic) {
+    constexpr int N = ORDER, r = ORDER / 2;
+    float st[N][4];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const size_t q = (size_t)((long long)c + (k - r) * stride);
+        const float w0 = float(W[q]), w1 = float(W[plane + q]), w2 = float(W[2 * plane + q]), w3 = float(W[3 * plane + q]);
+        st[k][0] = w0;
+        st[k][1] = DIR == 0 ? w1 : w2;   // y stencils in the rotated frame (YchangetoX)
+        st[k][2] = DIR == 0 ? w2 : -w1;
+        st[k][3] = w3;
+    }
+    float pn1[4], p0[4], pp1[4];
+    to_prim(pn1, st[r - 1], gamma);
+    to_prim(p0, st[r], gamma);
+    to_prim(pp1, st[r + 1], gamma);
+    float dmax = 0.0f;
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        float ch[N][4];
+        if (characteristic) {
+            float base[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) base[v] = 0.5f * ((side == 0 ? pn1[v] : pp1[v]) + p0[v]);
+            CharBase<float> cb;
+            cb.init(base, gamma);
+#pragma unroll
+            for (int k = 0; k < N; ++k) cb.to_char(ch[k], st[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) ch[k][v] = st[k][v];
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            float s[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k) s[k] = ch[k][v];
+            dmax = fmaxf(dmax, ao_weight_distance<float, ORDER>(s));
+        }
+    }
+    return dmax;
+}
+
+// ---------------- the MLP on the tensor cores ----------------
+
+__device__ __forceinline__ void mma_bf16_16816(float* c, const unsigned* a, unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<unsigned*>(&v);
+}
+
+__device__ __forceinline__ unsigned ld_pair(const __nv_bfloat16* p) { return *reinterpret_cast<const unsigned*>(p); }
+
+// One warp evaluates 16 rows: x points at the rows' BF16 features ([16][NF], row stride NF);
+// hidden activations (after ReLU, rounded to BF16 as the next layer reads them) go to h1/h2
+// ([16][NH] FP32, may be null) and the output logits to z[16].
+__device__ __forceinline__ void mlp16(const Net& net, const __nv_bfloat16* x, float* h1, float* h2, float* z) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    unsigned a[4];
+    a[0] = ld_pair(x + g * NF + 2 * t);
+    a[1] = ld_pair(x + (g + 8) * NF + 2 * t);
+    a[2] = ld_pair(x + g * NF + 2 * t + 8);
+    a[3] = ld_pair(x + (g + 8) * NF + 2 * t + 8);
+    float c1[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        const int n = nt * 8 + 2 * t;
+        c1[nt][0] = net.b1[n];
+        c1[nt][1] = net.b1[n + 1];
+        c1[nt][2] = net.b1[n];
+        c1[nt][3] = net.b1[n + 1];
+        const __nv_bfloat16* wr = net.w1 + (nt * 8 + g) * NF;
+        mma_bf16_16816(c1[nt], a, ld_pair(wr + 2 * t), ld_pair(wr + 2 * t + 8));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) c1[nt][q] = __bfloat162float(__float2bfloat16_rn(fmaxf(c1[nt][q], 0.0f)));
+        if (h1) {
+            h1[g * NH + n] = c1[nt][0];
+            h1[g * NH + n + 1] = c1[nt][1];
+            h1[(g + 8) * NH + n] = c1[nt][2];
+            h1[(g + 8) * NH + n + 1] = c1[nt][3];
+        }
+    }
+    float c2[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        const int n = nt * 8 + 2 * t;
+        c2[nt][0] = net.b2[n];
+        c2[nt][1] = net.b2[n + 1];
+        c2[nt][2] = net.b2[n];
+        c2[nt][3] = net.b2[n + 1];
+    }
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        // accumulator fragments of layer 1 are the A fragments of layer 2
+        unsigned a2[4] = {pack_bf16(c1[2 * ks][0], c1[2 * ks][1]), pack_bf16(c1[2 * ks][2], c1[2 * ks][3]),
+                          pack_bf16(c1[2 * ks + 1][0], c1[2 * ks + 1][1]),
+                          pack_bf16(c1[2 * ks + 1][2], c1[2 * ks + 1][3])};
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            const __nv_bfloat16* wr = net.w2 + (nt * 8 + g) * NH + ks * 16;
+            mma_bf16_16816(c2[nt], a2, ld_pair(wr + 2 * t), ld_pair(wr + 2 * t + 8));
+        }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        const int n = nt * 8 + 2 * t;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) c2[nt][q] = __bfloat162float(__float2bfloat16_rn(fmaxf(c2[nt][q], 0.0f)));
+        if (h2) {
+            h2[g * NH + n] = c2[nt][0];
+            h2[g * NH + n + 1] = c2[nt][1];
+            h2[(g + 8) * NH + n] = c2[nt][2];
+            h2[(g + 8) * NH + n + 1] = c2[nt][3];
+        }
+    }
+    float c3[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        unsigned a3[4] = {pack_bf16(c2[2 * ks][0], c2[2 * ks][1]), pack_bf16(c2[2 * ks][2], c2[2 * ks][3]),
+                          pack_bf16(c2[2 * ks + 1][0], c2[2 * ks + 1][1]),
+                          pack_bf16(c2[2 * ks + 1][2], c2[2 * ks + 1][3])};
+        const __nv_bfloat16* wr = net.w3 + g * NH + ks * 16;
+        mma_bf16_16816(c3, a3, ld_pair(wr + 2 * t), ld_pair(wr + 2 * t + 8));
+    }
+    if (t == 0) {   // output column 0
+        z[g] = c3[0] + net.b3[0];
+        z[g + 8] = c3[2] + net.b3[0];
+    }
+}
+
+__device__ __forceinline__ unsigned mix_hash(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+struct GateArgs {
+    const double* W;
+    const double* AX;
+    const double* AY;
+    unsigned char* flags;      // [nx*ny]: bit 0 x-smooth, bit 1 y-smooth (null in collect mode)
+    Stats* stats;
+    float threshold;           // logit above which a cell is predicted smooth
+    unsigned audit_mask;       // audit predicted-smooth cells whose hash & mask == 0
+    unsigned seed;
+    float* samples;            // collect mode: [capacity][NS] features, label, distance, cell, dir
+    unsigned long long capacity;
+    unsigned sample_mask;      // collect cells whose hash & mask == 0
+    const StepCtl* ctl;        // inactive problems skip (may be null)
+};
+
+constexpr int GATE_THREADS = 256;
+
+// One thread per cell, both directions.  Stencils that leave the array get no flag (the face
+// kernel then reconstructs that cell with full WENO-AO).
+template <int ORDER>
+__global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net, Geometry geo) {
+    __shared__ __align__(16) __nv_bfloat16 xs[GATE_THREADS / 32][32 * NF];
+    __shared__ float zs[GATE_THREADS / 32][32];
+    if (a.ctl && !a.ctl->active) return;   // uniform over the grid
+    constexpr int r = ORDER / 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t plane = (size_t)geo.nx * geo.ny;
+    const size_t c = (size_t)blockIdx.x * GATE_THREADS + threadIdx.x;
+    const bool in = c < plane;
+    const int i = in ? (int)(c / geo.ny) : 0, j = in ? (int)(c % geo.ny) : 0;
+    const float gamma = float(geo.gamma);
+    unsigned char flag = 0;
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const int pos = dir == 0 ? i : j, n = dir == 0 ? geo.nx : geo.ny;
+        const bool fits = in && pos >= r && pos < n - r;
+        const long long stride = dir == 0 ? geo.ny : 1;
+        float f[NF];
+        if (fits) {
+            const float al = float(dir == 0 ? a.AX[c] : a.AY[c]);
+            if (dir == 0) cell_features<ORDER, 0>(a.W, plane, c, stride, gamma, al, f);
+            else cell_features<ORDER, 1>(a.W, plane, c, stride, gamma, al, f);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NF; ++k) f[k] = 0.0f;
+        }
+        __nv_bfloat16* row = xs[warp] + lane * NF;
+#pragma unroll
+        for (int k = 0; k < NF; k += 2)
+            *reinterpret_cast<__nv_bfloat162*>(row + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
+        __syncwarp();
+        mlp16(net, xs[warp], nullptr, nullptr, zs[warp]);
+        mlp16(net, xs[warp] + 16 * NF, nullptr, nullptr, zs[warp] + 16);
+        __syncwarp();
+        const float z = zs[warp][lane];
+        const bool smooth = fits && z > a.threshold;
+        const unsigned h = mix_hash((unsigned)c * 2u + (unsigned)dir + a.seed * 0x9e3779b9u);
+        if (a.samples && fits && (h & a.sample_mask) == 0) {
+            const float d = dir == 0 ? weight_distance<ORDER, 0>(a.W, plane, c, stride, gamma, geo.characteristic)
+                                     : weight_distance<ORDER, 1>(a.W, plane, c, stride, gamma, geo.characteristic);
+            const unsigned long long slot = atomicAdd(&a.stats->samples, 1ull);
+            if (slot < a.capacity) {
+                float* o = a.samples + slot * NS;
+#pragma unroll
+                for (int k = 0; k < NF; ++k) o[k] = f[k];
+                o[NF] = d <= GATE_EPS ? 1.0f : 0.0f;
+                o[NF + 1] = d;
+                o[NF + 2] = float(c);
+                o[NF + 3] = float(dir);
+            }
+        }
+        if (a.flags) {
+            if (smooth && (h & a.audit_mask) == 0) {
+                const float d = dir == 0 ? weight_distance<ORDER, 0>(a.W, plane, c, stride, gamma, geo.characteristic)
+                                         : weight_distance<ORDER, 1>(a.W, plane, c, stride, gamma, geo.characteristic);
+                atomicAdd(&a.stats->audited, 1ull);
+                if (d > GATE_EPS) atomicAdd(&a.stats->false_neg, 1ull);
+            }
+            const unsigned fits_mask = __ballot_sync(0xffffffffu, fits);
+            const unsigned smooth_mask = __ballot_sync(0xffffffffu, smooth);
+            if (lane == 0) {
+                atomicAdd(&a.stats->cells[dir], (unsigned long long)__popc(fits_mask));
+                atomicAdd(&a.stats->smooth[dir], (unsigned long long)__popc(smooth_mask));
+            }
+        }
+        flag |= smooth ? (unsigned char)(1u << dir) : (unsigned char)0;
+        __syncwarp();
+    }
+    if (a.flags && in) a.flags[c] = flag;
+}
+
+}  // namespace gate
+}  // namespace hos
+
+// ---------------- host side (hos_gate.cu) ----------------
+namespace hos {
+namespace gate {
+cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s);
+}  // namespace gate
+}  // namespace hos
+
+// the network object behind the C ABI's hos_gate handle
+struct hos_gate {
+    float* params = nullptr;          // [NPARAM] FP32 master parameters
+    float* m = nullptr;               // Adam moments
+    float* v = nullptr;
+    float* grad = nullptr;
+    __nv_bfloat16* wbf = nullptr;     // inference copy: w1 | w2 | w3 (NET_BF16)
+    float* bias = nullptr;            // b1 | b2 | b3 (NET_F32)
+    float* samples = nullptr;         // [capacity][NS]
+    unsigned long long capacity = 0;
+    hos::gate::Stats* stats = nullptr;
+    double* loss = nullptr;
+    int step = 0;
+    unsigned collect_seed = 1;
+    cudaStream_t stream = nullptr;
+    hos::gate::Net net() const {
+        using namespace hos::gate;
+        return Net{wbf, wbf + NH * NF, wbf + NH * NF + NH * NH, bias, bias + NH, bias + 2 * NH};
+    }
+};

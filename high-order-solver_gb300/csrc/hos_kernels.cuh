@@ -88,6 +88,10 @@ struct FaceArgs {
     double* FA;         // face DF indicator [nf]
     const StepCtl* ctl;
     int stage;
+    // learned gate (FP32 path only): per-cell flags, bit 0 x-smooth, bit 1 y-smooth; counter
+    // of linear results the a-posteriori check rejected
+    const unsigned char* gate;
+    unsigned long long* fallback;
 };
 
 // A tile is TN faces along the normal by TT along the tangent, handled by one CTA of
@@ -118,7 +122,9 @@ struct FaceSmem {
     static constexpr int WTILE = 5 * TN * TL;                      // W[4] + normal alpha, aliases GSTATES
     static constexpr int ATILE = (TILE_N + 1) * TL;                // tangential alpha of the face cells
     static_assert(WTILE <= GSTATES, "input tile must fit the Gauss-state region");
+    static constexpr int GFLAGS = ((TILE_N + 1) * TL + (int)sizeof(T) - 1) / (int)sizeof(T);  // gate flag bytes
     static constexpr size_t bytes = sizeof(T) * (size_t)(UNION + GSTATES + ATILE);
+    static constexpr size_t gated_bytes = bytes + sizeof(T) * (size_t)GFLAGS;
 };
 
 // Gauss weights of gausspoint 2 / 3 / 4 (SetGuassPoint, src/fluid_mesh.cpp:20-44)
@@ -146,8 +152,25 @@ __device__ __forceinline__ T alpha_k(const T* wl, const T* wr, T gamma) {
     return A;
 }
 
+// A-posteriori check of a linear (gated) reconstruction: density and total energy of each
+// reconstructed state stay within the range of the three central stencil entries widened by a
+// tenth of that range, and the state keeps a positive temperature.
+template <class T>
+__device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, const T* wp, T K) {
+    if (needs_order_reduction(q, K)) return false;
+#pragma unroll
+    for (int v = 0; v < 4; v += 3) {
+        const T lo = fminT(fminT(wm[v], w0[v]), wp[v]), hi = fmaxT(fmaxT(wm[v], w0[v]), wp[v]);
+        const T m = T(0.1) * (hi - lo) + T(1e-6) * fabsT(w0[v]);
+        if (!(q[v] >= lo - m && q[v] <= hi + m)) return false;
+    }
+    return true;
+}
+
 // One tile of faces: N0, T0 are the first face indices along the normal and the tangent.
-template <class T, int ORDER, int DIR, class TS>
+// GATED (FP32 only): cells the learned gate marks smooth reconstruct with the full-stencil
+// polynomial alone; see hos_gate.cuh.
+template <class T, int ORDER, int DIR, class TS, bool GATED = false>
 __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo, const int N0, const int T0,
                                           unsigned char* smem_raw) {
     using S = FaceSmem<T, ORDER, TS>;
@@ -160,6 +183,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     T* wtile = gst;                                      // phase 0-1 (aliases gst)
     T* antile = gst + 4 * S::TN * TL;                    // phase 0-1
     T* attile = gst + S::GSTATES;                        // phase 0-2
+    unsigned char* gfl = reinterpret_cast<unsigned char*>(attile + S::ATILE);  // phase 0-2 (GATED)
 
     const int nx = geo.nx, ny = geo.ny, g = geo.g;
     const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;  // faces along normal: nodeN + 1
@@ -191,7 +215,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             if (DIR == 0) { d[0] = w0; d[1] = w1; d[2] = w2; d[3] = w3; }
             else { d[0] = w0; d[1] = w2; d[2] = -w1; d[3] = w3; }
             antile[nn * TL + tl] = T(a.AN[ci]);
-            if (nn >= r && nn <= r + TILE_N) attile[(nn - r) * TL + tl] = T(a.AT[ci]);
+            if (nn >= r && nn <= r + TILE_N) {
+                attile[(nn - r) * TL + tl] = T(a.AT[ci]);
+                if constexpr (GATED) gfl[(nn - r) * TL + tl] = a.gate[ci];
+            }
         }
     }
     __syncthreads();
@@ -219,8 +246,28 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         to_prim(p0, st[r], gamma);
         to_prim(pp1, st[r + 1], gamma);
         T outv[2][8];
+        bool lin = false;
+        if constexpr (GATED) if ((gfl[nl * TL + tl] >> DIR) & 1) {
+            // predicted smooth: the linear weights select the full-stencil polynomial, and a
+            // linear reconstruction commutes with the characteristic projection
 #pragma unroll
-        for (int side = 0; side < 2; ++side) {
+            for (int side = 0; side < 2; ++side)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    T s[N], p[NW], px[NW];
+#pragma unroll
+                    for (int k = 0; k < N; ++k) s[k] = st[k][v];
+                    if (side == 0) normal_face<T, ORDER, 0>(s, df, hN, p, px);
+                    else normal_face<T, ORDER, 1>(s, df, hN, p, px);
+                    outv[side][v] = p[NW - 1];
+                    outv[side][4 + v] = px[NW - 1];
+                }
+            lin = linear_ok<T>(outv[0], st[r - 1], st[r], st[r + 1], K) &&
+                  linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K);
+            if (!lin) atomicAdd(a.fallback, 1ull);
+        }
+#pragma unroll
+        for (int side = 0; side < 2 && !lin; ++side) {
             T base[4];
 #pragma unroll
             for (int v = 0; v < 4; ++v) base[v] = T(0.5) * ((side == 0 ? pn1[v] : pp1[v]) + p0[v]);
@@ -299,12 +346,35 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 return lines + ((fn * TL + (tc + sgn * (k - r))) * 2 + sd) * 8;
             };
             const T* w0 = line(r, side);
+            T res[GP][12];
+            bool lin = false;
+            if constexpr (GATED) if ((gfl[(fn + side) * TL + tc] >> (1 - DIR)) & 1) {
+                // the side cell is smooth along the tangent: full-stencil polynomial at the
+                // Gauss points, in conservative variables
+#pragma unroll
+                for (int v = 0; v < 8; ++v) {
+                    T s[N];
+#pragma unroll
+                    for (int k = 0; k < N; ++k) s[k] = line(k, side)[v];
+#pragma unroll
+                    for (int ig = 0; ig < GP; ++ig) {
+                        T p[NW], px[NW];
+                        tangent_point<T, ORDER>(ig, s, df, hT, p, px);
+                        res[ig][v] = p[NW - 1];
+                        if (v < 4) res[ig][8 + v] = px[NW - 1];
+                    }
+                }
+                lin = true;
+#pragma unroll
+                for (int ig = 0; ig < GP; ++ig) lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K);
+                if (!lin) atomicAdd(a.fallback, 1ull);
+            }
             T base[4], w0c[4];
 #pragma unroll
             for (int v = 0; v < 4; ++v) w0c[v] = w0[v];
             to_prim(base, w0c, gamma);
-            T res[GP][12];
-            if (geo.characteristic) {
+            if (lin) {
+            } else if (geo.characteristic) {
                 CharBase<T> cb;
                 cb.init(base, gamma);
                 T ch[N][4];
@@ -377,7 +447,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             }
             // normal slope, reconstructed in conservative variables
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
+            for (int v = 0; v < 4 && !lin; ++v) {
                 T s[N], fw[NW];
 #pragma unroll
                 for (int k = 0; k < N; ++k) s[k] = line(k, side)[4 + v];
@@ -490,10 +560,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     }
 }
 
-template <class T, int ORDER, int DIR>
+template <class T, int ORDER, int DIR, bool GATED = false>
 __global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry geo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    face_tile<T, ORDER, DIR, DefaultTile>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
+    face_tile<T, ORDER, DIR, DefaultTile, GATED>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
 }
 
 }  // namespace hos

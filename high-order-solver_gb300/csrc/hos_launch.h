@@ -5,7 +5,8 @@
 #include "hos_kernels.cuh"
 
 namespace hos {
-// precision: 0 = FP64 compute, 1 = FP32 compute (state and accumulation stay FP64)
+// precision: 0 = FP64 compute, 1 = FP32 compute (state and accumulation stay FP64),
+// 2 = FP32 compute with the learned gate (FaceArgs::gate set)
 cudaError_t configure_faces5(int precision);
 cudaError_t configure_faces7(int precision);
 cudaError_t configure_faces9(int precision);

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/hos_gb300.h"
+#include "hos_gate.cuh"
 #include "hos_launch.h"
 #include "hos_step.cuh"
 
@@ -149,6 +150,19 @@ struct hos_solver2d {
     // captured step
     cudaGraphExec_t graph = nullptr;
     double graph_tstop = 0.0;
+    // learned gate (FP32 path): per-cell flags, counters, the network's inference copy
+    int gated = 0;
+    unsigned char* gflags = nullptr;
+    gate::Stats* gstats = nullptr;
+    __nv_bfloat16* gw = nullptr;
+    float* gb = nullptr;
+    float gthreshold = 0.0f;
+    unsigned gaudit_mask = 0;
+    unsigned gseed = 0;
+    gate::Net gnet() const {
+        using namespace gate;
+        return Net{gw, gw + NH * NF, gw + NH * NF + NH * NH, gb, gb + NH, gb + 2 * NH};
+    }
 };
 
 namespace {
@@ -183,6 +197,9 @@ void free_all(hos_solver2d* s) {
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->ctl) cudaFree(s->ctl);
+    void* gbufs[] = {s->gflags, s->gstats, s->gw, s->gb};
+    for (void* b : gbufs)
+        if (b) cudaFree(b);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
@@ -202,8 +219,16 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     }
     FaceArgs ax{s->W, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->ctl, stage};
     FaceArgs ay{s->W, s->AY, s->AX, s->FXy, s->FPy, s->FAy, s->ctl, stage};
+    if (s->gated) {
+        // per-cell smoothness flags of this stage's state (ghosts filled) for both directions
+        gate::GateArgs ga{s->W, s->AX, s->AY, s->gflags, s->gstats, s->gthreshold, s->gaudit_mask, s->gseed++,
+                          nullptr, 0, 0xffffffffu, s->ctl};
+        if ((e = gate::launch_gate(s->p.order, ga, s->gnet(), geo, s->stream)) != cudaSuccess) return cuda_fail(e, "gate");
+        ax.gate = ay.gate = s->gflags;
+        ax.fallback = ay.fallback = &s->gstats->fallback;
+    }
     // x faces then y faces, back to back on the stream (events after each when profiling)
-    const int prec = s->precision;
+    const int prec = s->gated ? 2 : s->precision;
     switch (s->p.order) {
         case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
         case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
@@ -448,6 +473,77 @@ int hos2d_set_time(hos_solver2d* s, double t) {
     return e == cudaSuccess ? HOS_OK : cuda_fail(e, "set_time");
 }
 
+int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audit_log2) {
+    using namespace gate;
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "set_gate");
+    if (s->graph) {  // the captured step has the old launch sequence
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    if (!g) {
+        s->gated = 0;
+        return HOS_OK;
+    }
+    if (s->precision != HOS_FP32) return fail(HOS_E_CONFIG, "the learned gate runs on the FP32-bulk path");
+    if (audit_log2 < 0 || audit_log2 > 31) return fail(HOS_E_ARG, "audit_log2 must be 0..31");
+    if (!s->gflags) {
+        if ((e = cudaMalloc(&s->gflags, s->ncell)) == cudaSuccess && (e = cudaMalloc(&s->gstats, sizeof(Stats))) == cudaSuccess &&
+            (e = cudaMalloc(&s->gw, NET_BF16 * sizeof(__nv_bfloat16))) == cudaSuccess)
+            e = cudaMalloc(&s->gb, NET_F32 * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(s->gstats, 0, sizeof(Stats));
+        if (e != cudaSuccess) return fail(HOS_E_NOMEM, std::string("gate buffers: ") + cudaGetErrorString(e));
+    }
+    // the solver keeps its own copy, so the network can go on training
+    if ((e = cudaStreamSynchronize(g->stream)) == cudaSuccess &&
+        (e = cudaMemcpy(s->gw, g->wbf, NET_BF16 * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice)) == cudaSuccess)
+        e = cudaMemcpy(s->gb, g->bias, NET_F32 * sizeof(float), cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "set_gate copy");
+    switch (s->p.order) {
+        case 5: e = configure_faces5(2); break;
+        case 7: e = configure_faces7(2); break;
+        default: e = configure_faces9(2); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "configure gated face kernels");
+    s->gthreshold = threshold;
+    s->gaudit_mask = audit_log2 == 31 ? 0xffffffffu : (1u << audit_log2) - 1u;
+    s->gated = 1;
+    return HOS_OK;
+}
+
+int hos2d_gate_stats(hos_solver2d* s, unsigned long long* stats, int reset) {
+    if (!s || !stats) return fail(HOS_E_ARG, "null argument");
+    if (!s->gstats) {
+        std::memset(stats, 0, 8 * sizeof(unsigned long long));
+        return HOS_OK;
+    }
+    gate::Stats st;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, s->gstats, sizeof st, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(s->gstats, 0, sizeof st);
+    if (e != cudaSuccess) return cuda_fail(e, "gate_stats");
+    const unsigned long long v[8] = {st.cells[0], st.cells[1], st.smooth[0], st.smooth[1], st.audited, st.false_neg,
+                                     st.fallback, st.samples};
+    std::memcpy(stats, v, sizeof v);
+    return HOS_OK;
+}
+
+int hos_gate_collect(hos_gate* g, hos_solver2d* s, int sample_log2) {
+    using namespace gate;
+    if (!g || !s || sample_log2 < 0 || sample_log2 > 31) return fail(HOS_E_ARG, "bad argument");
+    if (!g->samples) return fail(HOS_E_CONFIG, "the gate was created without sample capacity");
+    const Geometry& geo = s->geo;
+    const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
+    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 0);
+    GateArgs ga{s->W, s->AX, s->AY, nullptr, g->stats, 0.0f, 0xffffffffu, g->collect_seed++, g->samples, g->capacity,
+                sample_log2 == 31 ? 0xffffffffu : (1u << sample_log2) - 1u, nullptr};
+    cudaError_t e = cudaStreamSynchronize(g->stream);   // the network's copy is current
+    if (e == cudaSuccess) e = launch_gate(s->p.order, ga, g->net(), geo, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "gate collect");
+}
+
 int hos2d_begin_step(hos_solver2d* s, double tstop) {
     if (!s) return fail(HOS_E_ARG, "null solver");
     return enqueue_begin(s, tstop);
@@ -543,8 +639,8 @@ int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms) {
 }
 
 int hos2d_launches_per_step(const hos_solver2d* s) {
-    (void)s;
-    return 1 + 2 * 4;  // begin_step + per stage (bc, x faces, y faces, update)
+    // begin_step + per stage (bc, [gate,] x faces, y faces, update)
+    return 1 + 2 * (4 + (s && s->gated ? 1 : 0));
 }
 
 void* hos2d_stream(hos_solver2d* s) { return s ? (void*)s->stream : nullptr; }

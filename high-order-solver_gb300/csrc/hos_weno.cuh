@@ -14,6 +14,8 @@ namespace hos {
 
 template <class T> __device__ __forceinline__ T sq(T x) { return x * x; }
 template <class T> __device__ __forceinline__ T fabsT(T x) { return x < T(0) ? -x : x; }
+template <class T> __device__ __forceinline__ T fmaxT(T a, T b) { return a > b ? a : b; }
+template <class T> __device__ __forceinline__ T fminT(T a, T b) { return a < b ? a : b; }
 
 // number of candidate polynomials per order
 template <int ORDER> struct AO { static constexpr int N = ORDER == 5 ? 4 : ORDER == 7 ? 5 : 6; };
@@ -144,44 +146,61 @@ __device__ __forceinline__ T beta9(const T* s, T& b5mid) {
            fabsT(b[0] - b[1] - b[3] + b[4]);
 }
 
-// Final adaptive-order weights of the DF variants (epsilon 1e-6, Z-type weights).
-template <class T, int ORDER>
-__device__ __forceinline__ void ao_weights(const T* s, T* fw) {
-    constexpr int N = AO<ORDER>::N;
+// Linear weights d_k of the candidate polynomials (0.85 for every level, as the reference sets).
+template <int ORDER>
+__device__ __forceinline__ void ao_linear(double* dd) {
     constexpr double dhi = 0.85, dlo = 0.85, dav = 0.85;
-    double dd[6];
-    T beta[6];
     if (ORDER == 5) {
         dd[0] = (1.0 - dhi) * (1.0 - dlo) / 2.0; dd[1] = (1.0 - dhi) * dlo;
         dd[2] = (1.0 - dhi) * (1.0 - dlo) / 2.0; dd[3] = dhi;
-        beta3<T>(s, beta);
-        beta[3] = T(1.0 / 6.0) * (beta[0] + T(4.0) * beta[1] + beta[2]) + fabsT(beta[0] - beta[2]);
     } else if (ORDER == 7) {
         dd[0] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - dav) / 2.0; dd[1] = (1.0 - dhi) * (1.0 - dav) * dlo;
         dd[2] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - dav) / 2.0; dd[3] = (1.0 - dhi) * dav; dd[4] = dhi;
-        beta3<T>(s + 1, beta);
-        beta[3] = T(1.0 / 6.0) * (beta[0] + T(4.0) * beta[1] + beta[2]) + fabsT(beta[0] - beta[2]);
-        beta[4] = beta7<T>(s);
     } else {
         dd[0] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - dav) * (1.0 - dav) / 2.0;
         dd[1] = (1.0 - dhi) * (1.0 - dav) * (1.0 - dav) * dlo;
         dd[2] = (1.0 - dhi) * (1.0 - dlo) * (1.0 - dav) * (1.0 - dav) / 2.0;
         dd[3] = (1.0 - dhi) * (1.0 - dav) * dav; dd[4] = (1.0 - dhi) * dav; dd[5] = dhi;
+    }
+}
+
+// Smoothness indicators beta_k of the candidate stencils (the last one the full stencil) and
+// the global indicator tau (mean |beta_top - beta_k|); s holds the ORDER stencil entries.
+template <class T, int ORDER>
+__device__ __forceinline__ T ao_betas(const T* s, T* beta) {
+    constexpr int N = AO<ORDER>::N;
+    if (ORDER == 5) {
+        beta3<T>(s, beta);
+        beta[3] = T(1.0 / 6.0) * (beta[0] + T(4.0) * beta[1] + beta[2]) + fabsT(beta[0] - beta[2]);
+    } else if (ORDER == 7) {
+        beta3<T>(s + 1, beta);
+        beta[3] = T(1.0 / 6.0) * (beta[0] + T(4.0) * beta[1] + beta[2]) + fabsT(beta[0] - beta[2]);
+        beta[4] = beta7<T>(s);
+    } else {
         beta3<T>(s + 2, beta);
         beta[4] = beta7<T>(s + 1);
         T mid;
         beta[5] = beta9<T>(s, mid);
         beta[3] = mid;
     }
-    constexpr int top = N - 1;
-    T tau;
     if (N == 4)
-        tau = T(1.0 / 3.0) * (fabsT(beta[3] - beta[0]) + fabsT(beta[3] - beta[1]) + fabsT(beta[3] - beta[2]));
-    else if (N == 5)
-        tau = T(0.25) * (fabsT(beta[4] - beta[0]) + fabsT(beta[4] - beta[1]) + fabsT(beta[4] - beta[2]) + fabsT(beta[4] - beta[3]));
-    else
-        tau = T(0.2) * (fabsT(beta[5] - beta[0]) + fabsT(beta[5] - beta[1]) + fabsT(beta[5] - beta[2]) +
-                        fabsT(beta[5] - beta[3]) + fabsT(beta[5] - beta[4]));
+        return T(1.0 / 3.0) * (fabsT(beta[3] - beta[0]) + fabsT(beta[3] - beta[1]) + fabsT(beta[3] - beta[2]));
+    if (N == 5)
+        return T(0.25) * (fabsT(beta[4] - beta[0]) + fabsT(beta[4] - beta[1]) + fabsT(beta[4] - beta[2]) +
+                          fabsT(beta[4] - beta[3]));
+    return T(0.2) * (fabsT(beta[5] - beta[0]) + fabsT(beta[5] - beta[1]) + fabsT(beta[5] - beta[2]) +
+                     fabsT(beta[5] - beta[3]) + fabsT(beta[5] - beta[4]));
+}
+
+// Final adaptive-order weights of the DF variants (epsilon 1e-6, Z-type weights).
+template <class T, int ORDER>
+__device__ __forceinline__ void ao_weights(const T* s, T* fw) {
+    constexpr int N = AO<ORDER>::N;
+    double dd[6];
+    ao_linear<ORDER>(dd);
+    T beta[6];
+    const T tau = ao_betas<T, ORDER>(s, beta);
+    constexpr int top = N - 1;
     T alpha[6], sum = T(0.0);
 #pragma unroll
     for (int k = 0; k < N; ++k) {
@@ -195,6 +214,29 @@ __device__ __forceinline__ void ao_weights(const T* s, T* fw) {
     fw[top] = wt;
 #pragma unroll
     for (int k = 0; k < top; ++k) fw[k] = alpha[k] * inv - wt * T(dd[k]);
+}
+
+// Largest distance max_k |omega_k - d_k| of the normalised nonlinear weights from the linear
+// weights: 0 where the reconstruction is the linear (full-stencil) one.
+template <class T, int ORDER>
+__device__ __forceinline__ T ao_weight_distance(const T* s) {
+    constexpr int N = AO<ORDER>::N;
+    double dd[6];
+    ao_linear<ORDER>(dd);
+    T beta[6];
+    const T tau = ao_betas<T, ORDER>(s, beta);
+    T alpha[6], sum = T(0.0);
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        T gd = tau / (beta[k] + T(1e-6));
+        alpha[k] = T(dd[k]) * (T(1.0) + gd * gd);
+        sum += alpha[k];
+    }
+    const T inv = T(1.0) / sum;
+    T dmax = T(0.0);
+#pragma unroll
+    for (int k = 0; k < N; ++k) dmax = fmaxT(dmax, fabsT(alpha[k] * inv - T(dd[k])));
+    return dmax;
 }
 
 // DF factors from the alpha values along the stencil (e.g. :1731-1741, :1898-1909)

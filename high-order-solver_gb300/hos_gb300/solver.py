@@ -91,6 +91,24 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos_batch2d_stream.argtypes = [vp]
     lib.hos_batch2d_stream.restype = vp
     lib.hos_batch2d_last_error.restype = ctypes.c_char_p
+    _FP = ctypes.POINTER(ctypes.c_float)
+    _ULL = ctypes.POINTER(ctypes.c_ulonglong)
+    lib.hos_gate_create.argtypes = [ctypes.c_ulonglong, ctypes.c_uint, ctypes.POINTER(vp)]
+    lib.hos_gate_destroy.argtypes = [vp]
+    lib.hos_gate_get_params.argtypes = [vp, _FP]
+    lib.hos_gate_set_params.argtypes = [vp, _FP]
+    lib.hos_gate_collect.argtypes = [vp, vp, ctypes.c_int]
+    lib.hos_gate_sample_count.argtypes = [vp, _ULL]
+    lib.hos_gate_get_samples.argtypes = [vp, _FP, ctypes.c_ulonglong]
+    lib.hos_gate_set_samples.argtypes = [vp, _FP, ctypes.c_ulonglong]
+    lib.hos_gate_clear_samples.argtypes = [vp]
+    lib.hos_gate_gradient.argtypes = [vp, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_float, ctypes.c_float, _FP, _DP]
+    lib.hos_gate_forward.argtypes = [vp, ctypes.c_ulonglong, ctypes.c_int, _FP]
+    lib.hos_gate_train.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_uint, _DP]
+    lib.hos_gate_last_error.restype = ctypes.c_char_p
+    lib.hos2d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
+    lib.hos2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     _LIB = lib
     return lib
 
@@ -208,6 +226,16 @@ class Solver2D:
     @property
     def stream(self) -> int:
         return int(self._lib.hos2d_stream(self._h) or 0)
+
+    def set_gate(self, gate: "Gate | None", threshold: float = 0.0, audit_log2: int = 6) -> None:
+        """Attach a copy of a learned gate (FP32 solvers); None detaches it."""
+        _check(self._lib.hos2d_set_gate(self._h, gate._h if gate is not None else None, threshold, audit_log2))
+
+    def gate_stats(self, reset: bool = False) -> dict:
+        v = (ctypes.c_ulonglong * 8)()
+        _check(self._lib.hos2d_gate_stats(self._h, v, 1 if reset else 0))
+        keys = ("cells_x", "cells_y", "smooth_x", "smooth_y", "audited", "false_neg", "fallback", "unused")
+        return dict(zip(keys, (int(x) for x in v)))
 
     def run(self, tstop: float, max_steps: int = 10**9, graph: bool = True, check_every: int = 50) -> int:
         """Advance until t >= tstop (the driver's while loop); returns steps taken."""
@@ -357,3 +385,89 @@ class Batch2D:
     @property
     def stream(self) -> int:
         return int(self._lib.hos_batch2d_stream(self._h) or 0)
+
+
+def _checkg(code: int) -> None:
+    if code == HOS_OK:
+        return
+    msg = load().hos_gate_last_error().decode(errors="replace") or load().hos_last_error().decode(errors="replace")
+    raise HosError(msg)
+
+
+class Gate:
+    """The learned smoothness gate: a 16-32-32-1 MLP trained on the GPU on labels the solver
+    writes from its own states (``collect``)."""
+
+    FEATURES = 16
+    SAMPLE = 20
+    PARAMS = 1633
+
+    def __init__(self, capacity: int = 1 << 22, seed: int = 1):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        _checkg(self._lib.hos_gate_create(capacity, seed, ctypes.byref(h)))
+        self._h = h
+        self.capacity = capacity
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hos_gate_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.empty(self.PARAMS, np.float32)
+        _checkg(self._lib.hos_gate_get_params(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    @params.setter
+    def params(self, value) -> None:
+        v = np.ascontiguousarray(value, np.float32)
+        assert v.size == self.PARAMS
+        _checkg(self._lib.hos_gate_set_params(self._h, v.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def collect(self, solver: "Solver2D", sample_log2: int = 4) -> None:
+        _check(self._lib.hos_gate_collect(self._h, solver._h, sample_log2))
+
+    @property
+    def count(self) -> int:
+        n = ctypes.c_ulonglong()
+        _checkg(self._lib.hos_gate_sample_count(self._h, ctypes.byref(n)))
+        return int(n.value)
+
+    def samples(self) -> np.ndarray:
+        n = self.count
+        out = np.empty((n, self.SAMPLE), np.float32)
+        _checkg(self._lib.hos_gate_get_samples(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n))
+        return out
+
+    def set_samples(self, s: np.ndarray) -> None:
+        s = np.ascontiguousarray(s, np.float32).reshape(-1, self.SAMPLE)
+        _checkg(self._lib.hos_gate_set_samples(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(s)))
+
+    def clear(self) -> None:
+        _checkg(self._lib.hos_gate_clear_samples(self._h))
+
+    def gradient(self, first: int, n: int, w_pos: float = 1.0, w_neg: float = 4.0):
+        g = np.empty(self.PARAMS, np.float32)
+        loss = ctypes.c_double()
+        _checkg(self._lib.hos_gate_gradient(self._h, first, n, w_pos, w_neg,
+                                            g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss)))
+        return g, loss.value
+
+    def forward(self, first: int, n: int) -> np.ndarray:
+        z = np.empty(n, np.float32)
+        _checkg(self._lib.hos_gate_forward(self._h, first, n, z.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return z
+
+    def train(self, steps: int, batch: int = 4096, lr: float = 3e-3, w_pos: float = 1.0, w_neg: float = 4.0,
+              seed: int = 0) -> float:
+        loss = ctypes.c_double()
+        _checkg(self._lib.hos_gate_train(self._h, steps, batch, lr, w_pos, w_neg, seed, ctypes.byref(loss)))
+        return loss.value

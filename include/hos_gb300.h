@@ -139,6 +139,46 @@ void* hos2d_stream(hos_solver2d* s);
 /* Human-readable text of the last error on this thread. */
 const char* hos_last_error(void);
 
+/* ---- learned gate (FP32-bulk path; no counterpart in the reference) ---------------------
+ * A 16 -> 32 -> 32 -> 1 MLP (BF16 weights, FP32 accumulation on the tensor cores) predicts,
+ * per cell and direction, from the normalised WENO-AO smoothness indicators of density and
+ * pressure and the DF indicator, whether the nonlinear weights of all characteristic variables
+ * stay within 0.02 of the linear weights; predicted-smooth cells reconstruct with the
+ * full-stencil polynomial, everything else (and every linear result failing the positivity /
+ * oscillation check) with full WENO-AO.  Labels come from the solver's own states
+ * (hos_gate_collect); training runs on the GPU (hos_gate_train). */
+#define HOS_GATE_FEATURES 16
+#define HOS_GATE_SAMPLE 20     /* floats per sample: 16 features, label (1 smooth), distance, cell, direction */
+#define HOS_GATE_PARAMS 1633   /* W1[32][16] b1[32] W2[32][32] b2[32] w3[32] b3 */
+typedef struct hos_gate hos_gate;
+int hos_gate_create(unsigned long long sample_capacity, unsigned seed, hos_gate** out);
+int hos_gate_destroy(hos_gate* g);
+int hos_gate_get_params(hos_gate* g, float* params);
+int hos_gate_set_params(hos_gate* g, const float* params);
+/* append labelled samples of a solver's current state: cells whose hash has sample_log2 low
+ * zero bits, both directions */
+int hos_gate_collect(hos_gate* g, hos_solver2d* s, int sample_log2);
+int hos_gate_sample_count(hos_gate* g, unsigned long long* n);
+int hos_gate_get_samples(hos_gate* g, float* out, unsigned long long n);
+int hos_gate_set_samples(hos_gate* g, const float* in, unsigned long long n);
+int hos_gate_clear_samples(hos_gate* g);
+/* gradient (HOS_GATE_PARAMS floats) and loss of the class-weighted mean cross-entropy over
+ * samples [first, first + n); no parameter update */
+int hos_gate_gradient(hos_gate* g, unsigned long long first, int n, float w_pos, float w_neg, float* grad,
+                      double* loss);
+int hos_gate_forward(hos_gate* g, unsigned long long first, int n, float* logits);
+/* steps Adam updates on mini-batches of batch samples */
+int hos_gate_train(hos_gate* g, int steps, int batch, float lr, float w_pos, float w_neg, unsigned seed,
+                   double* mean_loss);
+const char* hos_gate_last_error(void);
+/* attach a copy of the network to an FP32 solver (NULL detaches): cells with logit above
+ * threshold take the linear path; predicted-smooth cells whose hash has audit_log2 low zero
+ * bits are re-checked with full weights */
+int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audit_log2);
+/* counters since the last reset: cells gated x, y; predicted smooth x, y; audited; audited but
+ * not smooth (false negatives of the gate); linear results rejected; (unused) */
+int hos2d_gate_stats(hos_solver2d* s, unsigned long long* stats, int reset);
+
 /* ---- 1D path --------------------------------------------------------------------------
  * The reference's 1D drivers (SodTubeProblem, accuracy_sinwave_1d, src/1Dproblem.cpp:3-149,
  * 519-735) over Fluid1d arrays: state of cell i at index i over the full line including

@@ -558,6 +558,76 @@ double face_alpha(const Recon* re, bool yface) {
     return r < 2.0 ? 0.0 : r;
 }
 
+// ----------------------------------------------------------------------------------------
+// learned-gate features and labels (the gate has no counterpart in the reference; this is
+// its CPU statement, in FP64, for the tests)
+// ----------------------------------------------------------------------------------------
+double gate_betas(int order, const double* s, double* beta) {
+    int n;
+    if (order == 5) {
+        n = 4;
+        beta3(s, 2, beta);
+        beta[3] = 1.0 / 6.0 * (beta[0] + 4.0 * beta[1] + beta[2]) + std::abs(beta[0] - beta[2]);
+    } else if (order == 7) {
+        n = 5;
+        beta3(s, 3, beta);
+        beta[3] = 1.0 / 6.0 * (beta[0] + 4.0 * beta[1] + beta[2]) + std::abs(beta[0] - beta[2]);
+        beta[4] = beta7(s, 3);
+    } else {
+        n = 6;
+        beta3(s, 4, beta);
+        beta[4] = beta7(s, 4);
+        double mid;
+        beta[5] = beta9(s, &mid);
+        beta[3] = mid;
+    }
+    double tau = 0;
+    for (int k = 0; k < n - 1; ++k) tau += std::abs(beta[n - 1] - beta[k]);
+    return tau / (n - 1);
+}
+
+void gate_linear(int order, double* d) {
+    const double h = 0.85;
+    if (order == 5) {
+        d[0] = (1 - h) * (1 - h) / 2; d[1] = (1 - h) * h; d[2] = d[0]; d[3] = h;
+    } else if (order == 7) {
+        d[0] = (1 - h) * (1 - h) * (1 - h) / 2; d[1] = (1 - h) * (1 - h) * h; d[2] = d[0];
+        d[3] = (1 - h) * h; d[4] = h;
+    } else {
+        d[0] = (1 - h) * (1 - h) * (1 - h) * (1 - h) / 2; d[1] = (1 - h) * (1 - h) * (1 - h) * h; d[2] = d[0];
+        d[3] = (1 - h) * (1 - h) * h; d[4] = (1 - h) * h; d[5] = h;
+    }
+}
+
+// 7 normalised indicators of one stencil: betas / (sum + tau + 1e-10 c^2), padded to 6, then tau
+void gate_indicators(int order, const double* s, double* f) {
+    const int n = order == 5 ? 4 : order == 7 ? 5 : 6;
+    double beta[6] = {0, 0, 0, 0, 0, 0};
+    const double tau = gate_betas(order, s, beta);
+    double sum = tau;
+    for (int k = 0; k < n; ++k) sum += beta[k];
+    const double c = s[order / 2];
+    const double inv = 1.0 / (sum + 1e-10 * c * c + 1e-30);
+    for (int k = 0; k < 6; ++k) f[k] = k < n ? beta[k] * inv : 0.0;
+    f[6] = tau * inv;
+}
+
+// largest |omega_k - d_k| of the Z-type AO weights (epsilon 1e-6)
+double gate_distance(int order, const double* s) {
+    const int n = order == 5 ? 4 : order == 7 ? 5 : 6;
+    double beta[6], d[6], a[6], sum = 0;
+    const double tau = gate_betas(order, s, beta);
+    gate_linear(order, d);
+    for (int k = 0; k < n; ++k) {
+        const double q = tau / (beta[k] + 1e-6);
+        a[k] = d[k] * (1.0 + q * q);
+        sum += a[k];
+    }
+    double dm = 0;
+    for (int k = 0; k < n; ++k) dm = std::max(dm, std::abs(a[k] / sum - d[k]));
+    return dm;
+}
+
 }  // namespace
 
 // ========================================================================================
@@ -829,6 +899,60 @@ void oracle2d_get_flux(int dir, int stage, double* out) {
     for (size_t f = 0; f < nf; ++f)
         for (int ig = 0; ig < C.gp; ++ig)
             for (int k = 0; k < 8; ++k) out[(f * C.gp + ig) * 8 + k] = F[((f * 2 + stage) * C.gp + ig) * 8 + k];
+}
+
+// Gate features ([ncell][2][16]) and label distances ([ncell][2]; -1 where the stencil leaves
+// the array) of a state (AoS convar, DF indicators), in the configuration of oracle2d_init.
+void oracle2d_gate_cells(const double* convar, const double* alpha_x, const double* alpha_y, double* feat,
+                         double* dist) {
+    const int order = C.p.order, N = order, r = order / 2;
+    for (int i = 0; i < C.nx; ++i)
+        for (int j = 0; j < C.ny; ++j) {
+            const int c = cell(i, j);
+            for (int dir = 0; dir < 2; ++dir) {
+                double* f = feat + (static_cast<size_t>(c) * 2 + dir) * 16;
+                double& dd = dist[static_cast<size_t>(c) * 2 + dir];
+                for (int k = 0; k < 16; ++k) f[k] = 0.0;
+                const int pos = dir == 0 ? i : j, lim = dir == 0 ? C.nx : C.ny;
+                if (pos < r || pos >= lim - r) {
+                    dd = -1.0;
+                    continue;
+                }
+                double st[9][4], rho[9], pr[9];
+                for (int k = 0; k < N; ++k) {
+                    const int q = dir == 0 ? cell(i + k - r, j) : cell(i, j + k - r);
+                    if (dir == 0) for (int v = 0; v < 4; ++v) st[k][v] = convar[4 * q + v];
+                    else rot_y_to_x(st[k], convar + 4 * q);
+                    double pv[4];
+                    to_prim(pv, st[k]);
+                    rho[k] = pv[0];
+                    pr[k] = pv[3];
+                }
+                gate_indicators(order, rho, f);
+                gate_indicators(order, pr, f + 7);
+                const double al = dir == 0 ? alpha_x[c] : alpha_y[c];
+                f[14] = al / (1.0 + al);
+                double pn1[4], p0[4], pp1[4];
+                to_prim(pn1, st[r - 1]);
+                to_prim(p0, st[r]);
+                to_prim(pp1, st[r + 1]);
+                double dm = 0;
+                for (int side = 0; side < 2; ++side) {
+                    double base[4], ch[9][4];
+                    for (int v = 0; v < 4; ++v) base[v] = 0.5 * ((side == 0 ? pn1[v] : pp1[v]) + p0[v]);
+                    for (int k = 0; k < N; ++k) {
+                        if (C.p.characteristic) to_char(ch[k], base, st[k]);
+                        else for (int v = 0; v < 4; ++v) ch[k][v] = st[k][v];
+                    }
+                    for (int v = 0; v < 4; ++v) {
+                        double sv[9];
+                        for (int k = 0; k < N; ++k) sv[k] = ch[k][v];
+                        dm = std::max(dm, gate_distance(order, sv));
+                    }
+                }
+                dd = dm;
+            }
+        }
 }
 
 }  // extern "C"

@@ -47,6 +47,8 @@ typedef struct hos2d_params {
 /* ---- restatement (liboracle.so) ---- */
 int    oracle2d_init(const hos2d_params* p);
 void   oracle2d_free(void);
+/* learned-gate features [ncell][2][16] and label distances [ncell][2] of a state (test oracle) */
+void   oracle2d_gate_cells(const double* convar, const double* alpha_x, const double* alpha_y, double* feat, double* dist);
 void   oracle2d_set_threads(int n);
 void   oracle2d_set_state(const double* convar, const double* primvar);
 void   oracle2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);

@@ -145,3 +145,19 @@ class CpuStep1D:
         a = np.empty(nx)
         self.fn("get_state")(c.ctypes.data_as(_DP), a.ctypes.data_as(_DP))
         return dict(convar=c.reshape(nx, 3), alpha=a)
+
+
+def gate_cells(pb, convar, alpha_x=None, alpha_y=None):
+    """Oracle gate features [nx, ny, 2, 16] and weight distances [nx, ny, 2] (-1 where the
+    stencil leaves the array) of a state, in FP64."""
+    cpu = CpuStep("oracle").init(pb)
+    n = pb.nx * pb.ny
+    c = np.ascontiguousarray(convar, np.float64).reshape(-1)
+    ax = np.zeros(n) if alpha_x is None else np.ascontiguousarray(alpha_x, np.float64).reshape(-1)
+    ay = np.zeros(n) if alpha_y is None else np.ascontiguousarray(alpha_y, np.float64).reshape(-1)
+    feat = np.empty(n * 2 * 16)
+    dist = np.empty(n * 2)
+    fn = cpu.fn("gate_cells")
+    fn(c.ctypes.data_as(_DP), ax.ctypes.data_as(_DP), ay.ctypes.data_as(_DP), feat.ctypes.data_as(_DP),
+       dist.ctypes.data_as(_DP))
+    return feat.reshape(pb.nx, pb.ny, 2, 16), dist.reshape(pb.nx, pb.ny, 2)
