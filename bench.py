@@ -8,12 +8,14 @@ Seeded synthetic initial data; no dataset is involved.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line.  ``value`` is cell-updates/s of the plain FP64 path with the state
-resident in HBM (CUDA events on the solver's stream, L2 flushed between steps, summed
-over K steps, max over ranks); ``e2e`` is the same metric through the C ABI with host
-buffers (upload, step, download every step).  ``variants`` reports the FP32-bulk path and
-its density deviation from the FP64 run.  ``--impl reference`` times the CPU
-implementation of the same step on the host cores.
+Prints one JSON line.  ``value`` is cell-updates/s of the gated FP32 form (reconstruction,
+flux and the learned gate in FP32/BF16; state, stage combination and CFL in FP64) with the
+state resident in HBM (CUDA events on the solver's stream, L2 flushed between steps, summed
+over K steps, max over ranks); ``plain_fp64`` is the plain FP64 path on the same data and
+``accuracy`` the density deviation between them after the same steps.  The gate is trained
+first on the solver's own 256^2 / 512^2 random-quadrant runs.  ``e2e`` is the headline metric
+through the C ABI with host buffers (upload, step, download every step).  ``--impl reference``
+times the CPU implementation of the same step on the host cores.
 """
 from __future__ import annotations
 
@@ -36,7 +38,7 @@ sys.path.insert(0, str(ROOT / "high-order-solver_gb300"))
 N_CELLS = 1024
 ORDER = 7
 WORKLOAD = "riemann2d_1024x1024_weno7ao_df_char_gp3_gks_s2o4"
-METRIC = "cell-updates/s per S2O4 step"
+METRIC = "cell-updates/s per S2O4 step: gated FP32 vs plain FP64 on GB300 at stated L1 error"
 # FP64 operations one face-kernel launch executes per face (2 x DFMA + DADD + DMUL, counted
 # by ncu on the 256^2 case), and the algorithmic HBM bytes of one face-kernel launch per
 # face: W (32 B) + two DF indicators (16 B) read, stage flux (32 B) + face alpha (8 B)
@@ -45,6 +47,12 @@ FLOP_PER_FACE = 24028.0
 BYTES_PER_FACE = 120.0
 # dram__bytes_read + write per face of one face-kernel launch (ncu, 256^2 case: 4.02 MB / 65,792)
 TRAFFIC_PER_FACE = 61.0
+# FP32 operations (2 x FFMA + FADD + FMUL) one gated FP32 face-kernel launch executes per face,
+# and its DRAM traffic per face (ncu, 256^2 Riemann WENO7 after 20 steps; the plain FP32
+# kernel executes 16,751 per face)
+FP32_FLOP_PER_FACE_GATED = 7050.0
+TRAFFIC_PER_FACE_FP32 = 80.5
+AUDIT_LOG2 = 10   # audit one warp in 1024 of predicted-smooth cells with full weights
 
 
 def parse():
@@ -55,6 +63,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CELLS, help=argparse.SUPPRESS)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched sweep")
+    ap.add_argument("--case", choices=["gated256"], default=None,
+                    help="small profiling case: gate trained as in the bench, then 21 plain FP32 and 21 "
+                         "gated FP32 steps of the 256^2 WENO7 Riemann problem (no timing output)")
     return ap.parse_args()
 
 
@@ -249,15 +260,73 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000):
             "launches_per_step": 1 + 2 * 4, "gate": "off"}
 
 
+def sgemm_tflops(torch, dev):
+    """FP32 (no TF32) cuBLAS GEMM throughput: the FP32-pipe peak the gated kernels are held to."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    m = torch.randn(8192, 8192, dtype=torch.float32, device=dev)
+    torch.matmul(m, m)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        torch.matmul(m, m)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    return 5 * 2 * 8192 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+
+
+def dgemm_tflops(torch, dev):
+    m = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(m, m)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        torch.matmul(m, m)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    return 3 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+
+
+def profile_case():
+    """The launches the ncu summaries under profiles/ capture (see --case): the steps run inside
+    NVTX ranges "plain" and "gated" so that ncu --nvtx-include selects them."""
+    import torch
+
+    from hos_gb300 import cases, gate_train
+    from hos_gb300.solver import FP32, Solver2D
+
+    gate, rep = gate_train.train(order=ORDER, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
+                                 train_steps=3000, batch=4096)
+    pb, con, prim = cases.riemann2d(256, order=ORDER)
+    for gated in (False, True):
+        s = Solver2D(pb, FP32)
+        s.set_state(con, prim)
+        if gated:
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+        torch.cuda.nvtx.range_push("gated" if gated else "plain")
+        s.advance(21, 1e30, graph=False)
+        s.sync()
+        torch.cuda.nvtx.range_pop()
+        print("gated" if gated else "plain", s.gate_stats() if gated else "", flush=True)
+        s.close()
+    gate.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.case == "gated256":
+        profile_case()
+        return
     import torch
     import torch.distributed as dist
 
-    from hos_gb300 import cases
+    from hos_gb300 import cases, gate_train
     from hos_gb300.solver import FP32, FP64, Solver2D
 
     ws, rank, local = dist_env()
@@ -268,6 +337,7 @@ def main():
     n = args.n
     pb, con, prim = cases.riemann2d(n, order=ORDER)
     cells = pb.nodex * pb.nodey
+    g = pb.ghost
 
     # 256 MB buffer written between timed steps to flush the 129 MB L2
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
@@ -277,7 +347,6 @@ def main():
         for _ in range(w):
             solver.advance(1, 1e30, graph=True)
         solver.sync()
-        total = 0.0
         evs = []
         for _ in range(k):
             flush.zero_()
@@ -289,120 +358,147 @@ def main():
             b.record(ext)
             evs.append((a, b))
         solver.sync()
-        for a, b in evs:
-            total += a.elapsed_time(b) / 1e3
-        return total
+        return sum(a.elapsed_time(b) / 1e3 for a, b in evs)
 
-    # ---- plain FP64 path, state resident in HBM ----
-    s64 = Solver2D(pb, FP64)
-    s64.set_state(con, prim)
-    with ClockSampler(local) as clk:
+    def kernel_ms(solver, reps=3):
+        prof = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            prof.append(solver.profile_step(1e30))
+        return {k: float(np.mean([q[k] for q in prof])) for k in prof[0]}
+
+    # ---- the learned gate, trained on the solver's own 256^2 / 512^2 random-quadrant runs ----
+    t0 = time.perf_counter()
+    gate, rep = gate_train.train(order=ORDER, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
+                                 train_steps=3000, batch=4096)
+    train_s = time.perf_counter() - t0
+
+    def run(precision, gated, clk=None):
+        s = Solver2D(pb, precision)
+        s.set_state(con, prim)
+        if gated:
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
         if ws > 1:
             dist.barrier()
         torch.cuda.synchronize(dev)
-        t64 = timed_steps(s64, args.steps, args.warmup)
+        t = timed_steps(s, args.steps, args.warmup)
         torch.cuda.synchronize(dev)
-    if ws > 1:
-        tt = torch.tensor([t64], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t64 = float(tt.item())
-    value = ws * cells * args.steps / t64
-    rho64 = s64.get_state()["convar"][..., 0]
-    # per-kernel device times of a few steps (L2 flushed before each)
-    prof = []
-    for _ in range(3):
-        flush.zero_()
-        torch.cuda.synchronize(dev)
-        prof.append(s64.profile_step(1e30))
-    kern_ms = {k: float(np.mean([p[k] for p in prof])) for k in prof[0]}
-    face_ms = float(np.mean([kern_ms[k] for k in ("face_x0", "face_y0", "face_x1", "face_y1")]))
+        if ws > 1:
+            tt = torch.tensor([t], device=dev, dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = float(tt.item())
+        return s, t
 
-    # ---- FP32-bulk path (FP64 state / accumulation), same steps, deviation vs FP64 ----
-    s32 = Solver2D(pb, FP32)
-    s32.set_state(con, prim)
-    t32 = timed_steps(s32, args.steps, args.warmup)
-    rho32 = s32.get_state()["convar"][..., 0]
-    g = pb.ghost
-    a, b = rho64[g:-g, g:-g], rho32[g:-g, g:-g]
-    l1_dev = float(np.abs(a - b).mean() / np.abs(a).mean())
-    linf_dev = float(np.abs(a - b).max() / np.abs(a).max())
+    # ---- gated FP32 (the headline), plain FP64 and plain FP32 on the same initial data ----
+    with ClockSampler(local) as clk:
+        sg, tg = run(FP32, True)
+    gstats = sg.gate_stats()
+    kern_g = kernel_ms(sg)
+    rho_g = sg.get_state()["convar"][g:-g, g:-g, 0]
+    s64, t64 = run(FP64, False)
+    kern_64 = kernel_ms(s64)
+    rho_64 = s64.get_state()["convar"][g:-g, g:-g, 0]
+    s32, t32 = run(FP32, False)
+    kern_32 = kernel_ms(s32)
+    rho_32 = s32.get_state()["convar"][g:-g, g:-g, 0]
+    s64.close()
     s32.close()
 
-    # ---- end to end through the C ABI with pinned host buffers ----
+    def dev_l1(a, b):
+        return float(np.abs(a - b).mean() / np.abs(b).mean())
+
+    def dev_linf(a, b):
+        return float(np.abs(a - b).max() / np.abs(b).max())
+
+    # ---- end to end through the C ABI with pinned host buffers (gated FP32 solver) ----
     host_in = torch.from_numpy(np.ascontiguousarray(con.reshape(-1))).pin_memory()
     host_prim = torch.from_numpy(np.ascontiguousarray(prim.reshape(-1))).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
-    lib = s64._lib
+    lib = sg._lib
     dp = ctypes.POINTER(ctypes.c_double)
     pin = ctypes.cast(host_in.data_ptr(), dp)
     ppr = ctypes.cast(host_prim.data_ptr(), dp)
     pout = ctypes.cast(host_out.data_ptr(), dp)
-    ke = max(3, args.steps // 2)
-    for _ in range(1):
-        lib.hos2d_set_state(s64._h, pin, ppr)
-        s64.step(1e30)
-        lib.hos2d_get_state(s64._h, pout, None, None, None)
+    ke = max(3, args.steps)
+    lib.hos2d_set_state(sg._h, pin, ppr)
+    sg.step(1e30)
+    lib.hos2d_get_state(sg._h, pout, None, None, None)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(ke):
-        assert lib.hos2d_set_state(s64._h, pin, ppr) == 0
-        s64.step(1e30)
-        assert lib.hos2d_get_state(s64._h, pout, None, None, None) == 0
+        assert lib.hos2d_set_state(sg._h, pin, ppr) == 0
+        sg.step(1e30)
+        assert lib.hos2d_get_state(sg._h, pout, None, None, None) == 0
     te = time.perf_counter() - t0
     e2e_value = ws * cells * ke / te
-    s64.close()
+    launches = args.steps * sg.launches_per_step
+    sg.close()
 
     hbm_peak, hbm_src = peaks()
     if rank != 0:
+        gate.close()
         if ws > 1:
             dist.destroy_process_group()
         return
 
-    # FP64 peak measured here by cuBLAS DGEMM (the denominator of the compute roofline)
-    m = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
-    torch.matmul(m, m)
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(3):
-        torch.matmul(m, m)
-    e1.record()
-    torch.cuda.synchronize(dev)
-    dgemm_tflops = 3 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
-
-    ms = 1e3 * t64 / args.steps
-    faces_per_launch = (pb.nodex + 1) * pb.nodey
-    achieved_gbs = BYTES_PER_FACE * faces_per_launch / (face_ms / 1e3) / 1e9
+    fp32_peak = sgemm_tflops(torch, dev)
+    fp64_peak = dgemm_tflops(torch, dev)
+    faces = (pb.nodex + 1) * pb.nodey
+    face_g = float(np.mean([kern_g[k] for k in ("face_x0", "face_y0", "face_x1", "face_y1")]))
+    face_64 = float(np.mean([kern_64[k] for k in ("face_x0", "face_y0", "face_x1", "face_y1")]))
+    fl_g = FP32_FLOP_PER_FACE_GATED * faces / (face_g / 1e3) / 1e12
+    fl_64 = FLOP_PER_FACE * faces / (face_64 / 1e3) / 1e12
+    bytes_gbs = BYTES_PER_FACE * faces / (face_g / 1e3) / 1e9
+    smooth = (gstats["smooth_x"] + gstats["smooth_y"]) / max(1, gstats["cells_x"] + gstats["cells_y"])
     line = {
-        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": METRIC, "value": ws * cells * args.steps / tg, "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tg / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 reconstruction/flux/gate (bf16 MLP on tensor cores); f64 state, stage combination, CFL",
+        "data": "synthetic",
         "config": {"workload": WORKLOAD, "cells": cells, "order": ORDER, "gauss_points": 3,
-                   "characteristic": True, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed between timed steps (256 MB write)"},
+                   "characteristic": True, "form": "gated FP32 (learned gate) vs plain FP64",
+                   "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "gate_training": "seeded random-quadrant runs at 256^2 and 512^2 (4 seeds each, 120 steps)"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(2 * host_in.numel() * 8),
                 "d2h_bytes_per_step": int(host_out.numel() * 8)},
-        "gpu_launches": args.steps * 9,
-        "roofline": {"kernel": "face_kernel<double,7,x|y>", "bound": "fp64", "unit": "TFLOP/s",
-                     "achieved": None, "peak": dgemm_tflops,
-                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run", "frac": None,
-                     "traffic": TRAFFIC_PER_FACE * faces_per_launch, "launch_ms": face_ms,
-                     "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": achieved_gbs / hbm_peak, "peak_source": hbm_src}},
+        "gpu_launches": launches,
+        "roofline": {"kernel": "face_kernel<float,7,x|y,gated>", "bound": "fp32", "unit": "TFLOP/s",
+                     "achieved": fl_g, "peak": fp32_peak, "frac": fl_g / fp32_peak,
+                     "peak_source": "cuBLAS SGEMM 8192^3 (no TF32) measured in this run",
+                     "flop_per_face": FP32_FLOP_PER_FACE_GATED, "launch_ms": face_g,
+                     "traffic": TRAFFIC_PER_FACE_FP32 * faces,
+                     "hbm": {"achieved": bytes_gbs, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": bytes_gbs / hbm_peak, "peak_source": hbm_src}},
+        "plain_fp64": {"value": ws * cells * args.steps / t64, "unit": "cell-updates/s",
+                       "ms_per_step": 1e3 * t64 / args.steps, "gated_fp32_speedup": t64 / tg,
+                       "roofline": {"kernel": "face_kernel<double,7,x|y>", "bound": "fp64", "unit": "TFLOP/s",
+                                    "achieved": fl_64, "peak": fp64_peak, "frac": fl_64 / fp64_peak,
+                                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                                    "flop_per_face": FLOP_PER_FACE, "launch_ms": face_64,
+                                    "traffic": TRAFFIC_PER_FACE * faces}},
+        "accuracy": {"steps_compared": args.steps + args.warmup,
+                     "rho_rel_l1_gated_vs_fp64": dev_l1(rho_g, rho_64),
+                     "rho_rel_linf_gated_vs_fp64": dev_linf(rho_g, rho_64),
+                     "rho_rel_l1_fp32_vs_fp64": dev_l1(rho_32, rho_64),
+                     "rho_rel_l1_gated_vs_fp32": dev_l1(rho_g, rho_32)},
+        "gate": {"train_s": train_s, "samples": rep.samples, "smooth_label_fraction": rep.smooth_fraction,
+                 "threshold": rep.threshold, "heldout": rep.heldout,
+                 "linear_path_fraction": smooth, "audited": gstats["audited"],
+                 "audit_false_negative_rate": gstats["false_neg"] / max(1, gstats["audited"]),
+                 "aposteriori_rejections": gstats["fallback"], "audit_rate": 2.0 ** -AUDIT_LOG2},
         "variants": {"fp32_bulk": {"value": cells * args.steps / t32, "unit": "cell-updates/s",
-                                   "speedup_vs_fp64": t64 / t32, "rho_rel_l1_vs_fp64": l1_dev,
-                                   "rho_rel_linf_vs_fp64": linf_dev}},
-        "kernels_ms": kern_ms,
+                                   "ms_per_step": 1e3 * t32 / args.steps, "gated_speedup": t32 / tg}},
+        "kernels_ms": {"gated_fp32": kern_g, "fp32": kern_32, "fp64": kern_64},
         "clocks": clk.summary(),
     }
-    if FLOP_PER_FACE:
-        ach = FLOP_PER_FACE * faces_per_launch / (face_ms / 1e3) / 1e12
-        line["roofline"]["achieved"] = ach
-        line["roofline"]["frac"] = ach / dgemm_tflops
     if ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
     if not args.no_batch:
         line["variants"]["batch64_fp32"] = batch_leg(dev, FP32)
+    gate.close()
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

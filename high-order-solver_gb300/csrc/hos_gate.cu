@@ -146,8 +146,7 @@ __global__ void adam_kernel(float* params, float* m, float* v, float* grad, int 
 
 
 cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s) {
-    const size_t n = (size_t)geo.nx * geo.ny;
-    const unsigned blocks = (unsigned)((n + GATE_THREADS - 1) / GATE_THREADS);
+    const dim3 blocks((geo.ny + GATE_TILE - 1) / GATE_TILE, (geo.nx + GATE_TILE - 1) / GATE_TILE);
     if (order == 5) gate_kernel<5><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
     else if (order == 7) gate_kernel<7><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
     else gate_kernel<9><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);

@@ -75,28 +75,6 @@ __device__ __forceinline__ void indicator_features(const float* s, float* f) {
     f[6] = tau * inv;
 }
 
-// Features of cell c along direction DIR (0: x, i stride ny; 1: y, unit stride) from the FP64
-// state planes; alpha is the cell's DF indicator in that direction.
-template <int ORDER, int DIR>
-__device__ __forceinline__ void cell_features(const double* __restrict__ W, size_t plane, size_t c, long long stride,
-                                              float gamma, float alpha, float* f) {
-    constexpr int N = ORDER, r = ORDER / 2;
-    float rho[N], p[N];
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const size_t q = (size_t)((long long)c + (k - r) * stride);
-        float w[4] = {float(W[q]), float(W[plane + q]), float(W[2 * plane + q]), float(W[3 * plane + q])};
-        float pr[4];
-        to_prim(pr, w, gamma);
-        rho[k] = pr[0];
-        p[k] = pr[3];
-    }
-    indicator_features<ORDER>(rho, f);
-    indicator_features<ORDER>(p, f + 7);
-    f[14] = alpha / (1.0f + alpha);
-    f[15] = 0.0f;
-}
-
 // True label quantity of cell c along DIR: the largest distance of the nonlinear weights from
 // the linear ones over both faces and the four (characteristic) variables, computed as the
 // face kernel's normal reconstruction would (src/reconstruction.cpp:1861-2028 for WENO7).
@@ -266,21 +244,45 @@ struct GateArgs {
 };
 
 constexpr int GATE_THREADS = 256;
+constexpr int GATE_TILE = 16;   // 16 x 16 cells per block, one thread per cell
 
-// One thread per cell, both directions.  Stencils that leave the array get no flag (the face
-// kernel then reconstructs that cell with full WENO-AO).
+// One block per 16 x 16 tile of cells, one thread per cell, both directions.  The tile and
+// its stencil halo are converted once to FP32 density and pressure in shared memory; the
+// features are read from there.  Stencils that leave the array get no flag (the face kernel
+// then reconstructs that cell with full WENO-AO).
 template <int ORDER>
 __global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net, Geometry geo) {
+    constexpr int r = ORDER / 2, H = GATE_TILE + 2 * r;
     __shared__ __align__(16) __nv_bfloat16 xs[GATE_THREADS / 32][32 * NF];
     __shared__ float zs[GATE_THREADS / 32][32];
+    __shared__ float srho[H][H + 1], sp[H][H + 1];
+    __shared__ unsigned counts[4];           // cells x, cells y, smooth x, smooth y of the block
     if (a.ctl && !a.ctl->active) return;   // uniform over the grid
-    constexpr int r = ORDER / 2;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid < 4) counts[tid] = 0;
+    const int i0 = blockIdx.y * GATE_TILE, j0 = blockIdx.x * GATE_TILE;
     const size_t plane = (size_t)geo.nx * geo.ny;
-    const size_t c = (size_t)blockIdx.x * GATE_THREADS + threadIdx.x;
-    const bool in = c < plane;
-    const int i = in ? (int)(c / geo.ny) : 0, j = in ? (int)(c % geo.ny) : 0;
     const float gamma = float(geo.gamma);
+    for (int e = tid; e < H * H; e += GATE_THREADS) {
+        const int hi = e / H, hj = e % H;               // j fastest: coalesced rows
+        const int gi = i0 - r + hi, gj = j0 - r + hj;
+        float rho = 0.0f, pr = 0.0f;
+        if (gi >= 0 && gi < geo.nx && gj >= 0 && gj < geo.ny) {
+            const size_t q = (size_t)gi * geo.ny + gj;
+            float w[4] = {float(a.W[q]), float(a.W[plane + q]), float(a.W[2 * plane + q]), float(a.W[3 * plane + q])};
+            float pv[4];
+            to_prim(pv, w, gamma);
+            rho = pv[0];
+            pr = pv[3];
+        }
+        srho[hi][hj] = rho;
+        sp[hi][hj] = pr;
+    }
+    __syncthreads();
+    const int ti = tid / GATE_TILE, tj = tid % GATE_TILE;
+    const int i = i0 + ti, j = j0 + tj;
+    const bool in = i < geo.nx && j < geo.ny;
+    const size_t c = in ? (size_t)i * geo.ny + j : 0;
     unsigned char flag = 0;
 #pragma unroll
     for (int dir = 0; dir < 2; ++dir) {
@@ -289,9 +291,18 @@ __global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net,
         const long long stride = dir == 0 ? geo.ny : 1;
         float f[NF];
         if (fits) {
+            float rs[ORDER], ps[ORDER];
+#pragma unroll
+            for (int k = 0; k < ORDER; ++k) {
+                const int hi = dir == 0 ? ti + k : ti + r, hj = dir == 0 ? tj + r : tj + k;
+                rs[k] = srho[hi][hj];
+                ps[k] = sp[hi][hj];
+            }
+            indicator_features<ORDER>(rs, f);
+            indicator_features<ORDER>(ps, f + 7);
             const float al = float(dir == 0 ? a.AX[c] : a.AY[c]);
-            if (dir == 0) cell_features<ORDER, 0>(a.W, plane, c, stride, gamma, al, f);
-            else cell_features<ORDER, 1>(a.W, plane, c, stride, gamma, al, f);
+            f[14] = al / (1.0f + al);
+            f[15] = 0.0f;
         } else {
 #pragma unroll
             for (int k = 0; k < NF; ++k) f[k] = 0.0f;
@@ -322,7 +333,11 @@ __global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net,
             }
         }
         if (a.flags) {
-            if (smooth && (h & a.audit_mask) == 0) {
+            // audits are drawn per warp, so an audited warp re-checks all its predicted-smooth
+            // cells together instead of stalling 31 lanes behind one
+            const unsigned wid = (blockIdx.y * gridDim.x + blockIdx.x) * (GATE_THREADS / 32) + warp;
+            const unsigned hw = mix_hash(wid * 2u + (unsigned)dir + a.seed * 0x85ebca6bu);
+            if (smooth && (hw & a.audit_mask) == 0) {
                 const float d = dir == 0 ? weight_distance<ORDER, 0>(a.W, plane, c, stride, gamma, geo.characteristic)
                                          : weight_distance<ORDER, 1>(a.W, plane, c, stride, gamma, geo.characteristic);
                 atomicAdd(&a.stats->audited, 1ull);
@@ -331,14 +346,20 @@ __global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net,
             const unsigned fits_mask = __ballot_sync(0xffffffffu, fits);
             const unsigned smooth_mask = __ballot_sync(0xffffffffu, smooth);
             if (lane == 0) {
-                atomicAdd(&a.stats->cells[dir], (unsigned long long)__popc(fits_mask));
-                atomicAdd(&a.stats->smooth[dir], (unsigned long long)__popc(smooth_mask));
+                atomicAdd(&counts[dir], (unsigned)__popc(fits_mask));
+                atomicAdd(&counts[2 + dir], (unsigned)__popc(smooth_mask));
             }
         }
         flag |= smooth ? (unsigned char)(1u << dir) : (unsigned char)0;
         __syncwarp();
     }
     if (a.flags && in) a.flags[c] = flag;
+    if (a.flags) {
+        // one global update per block and counter
+        __syncthreads();
+        if (tid < 2) atomicAdd(&a.stats->cells[tid], (unsigned long long)counts[tid]);
+        else if (tid < 4) atomicAdd(&a.stats->smooth[tid - 2], (unsigned long long)counts[tid]);
+    }
 }
 
 }  // namespace gate

@@ -194,6 +194,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     const size_t plane = (size_t)nx * ny;
     const int tid = threadIdx.x;
     if (!a.ctl->active) return;
+    __shared__ unsigned rejected;   // GATED: linear results the check rejected in this tile
+    if constexpr (GATED) if (tid == 0) rejected = 0;
     auto cidx = [&](int n, int t) -> size_t {
         return DIR == 0 ? (size_t)n * ny + t : (size_t)t * ny + n;
     };
@@ -264,7 +266,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 }
             lin = linear_ok<T>(outv[0], st[r - 1], st[r], st[r + 1], K) &&
                   linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K);
-            if (!lin) atomicAdd(a.fallback, 1ull);
+            if (!lin) atomicAdd(&rejected, 1u);
         }
 #pragma unroll
         for (int side = 0; side < 2 && !lin; ++side) {
@@ -367,7 +369,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 lin = true;
 #pragma unroll
                 for (int ig = 0; ig < GP; ++ig) lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K);
-                if (!lin) atomicAdd(a.fallback, 1ull);
+                if (!lin) atomicAdd(&rejected, 1u);
             }
             T base[4], w0c[4];
 #pragma unroll
@@ -480,6 +482,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         }
     }
     __syncthreads();
+
+    if constexpr (GATED) if (tid == 0 && rejected) atomicAdd(a.fallback, (unsigned long long)rejected);
 
     // ---------------- phase 3: GKS flux, one (face, Gauss point) per thread ----------------
     const T dt = T(a.ctl->dt);

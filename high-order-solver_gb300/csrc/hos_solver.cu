@@ -204,7 +204,8 @@ void free_all(hos_solver2d* s) {
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
-// ev (optional): events recorded before the first and after every launch of the stage
+// ev (optional): 5 events, after the boundary fill, the gate (recorded with no launch when the
+// solver has no gate), the x faces, the y faces and the update
 int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     cudaError_t e;
     const Geometry& geo = s->geo;
@@ -227,19 +228,20 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
         ax.gate = ay.gate = s->gflags;
         ax.fallback = ay.fallback = &s->gstats->fallback;
     }
+    mark(1);
     // x faces then y faces, back to back on the stream (events after each when profiling)
     const int prec = s->gated ? 2 : s->precision;
     switch (s->p.order) {
-        case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
-        case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
-        default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 1 : nullptr); break;
+        case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
+        case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
+        default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
     UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage};
     const int n = geo.nodex * geo.nodey;
     update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "update");
-    mark(3);
+    mark(4);
     return HOS_OK;
 }
 
@@ -616,7 +618,7 @@ int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
 
 int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms) {
     if (!s || !ms) return fail(HOS_E_ARG, "null argument");
-    cudaEvent_t ev[10];
+    cudaEvent_t ev[12];
     for (auto& x : ev) cudaEventCreate(&x);
     cudaEventRecord(ev[0], s->stream);
     int st = enqueue_begin(s, tstop);
@@ -624,11 +626,11 @@ int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms) {
         cudaEventRecord(ev[1], s->stream);
         st = enqueue_stage(s, 0, ev + 2);
     }
-    if (!st) st = enqueue_stage(s, 1, ev + 6);
+    if (!st) st = enqueue_stage(s, 1, ev + 7);
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (!st && e == cudaSuccess) {
         float f;
-        for (int k = 0; k < 9; ++k) {
+        for (int k = 0; k < 11; ++k) {
             cudaEventElapsedTime(&f, ev[k], ev[k + 1]);
             ms[k] = f;
         }

@@ -98,7 +98,8 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         const size_t nfx = (size_t)(nodex + 1) * nodey, nfy = (size_t)nodex * (nodey + 1);
         const size_t fl = (size_t)I * nodey + J, fr = fl + nodey;
         const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
-        const double area = geo.dx * geo.dy;
+        // one reciprocal instead of four divisions: the FP64 pipe is the update's bound
+        const double iarea = 1.0 / (geo.dx * geo.dy);
         double w[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
@@ -114,7 +115,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             total += -geo.dx * a.FXy[v * nfy + fu];
             total += geo.dy * a.FXx[v * nfx + fl];
             total += -geo.dy * a.FXx[v * nfx + fr];
-            w[v] = old + total / area;
+            w[v] = old + total * iarea;
             a.W[v * plane + c] = w[v];
         }
         const int jend = nodex < nodey ? nodex : nodey;
@@ -122,12 +123,18 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             a.AX[c] = a.FAx[fl] + a.FAx[fr];
             a.AY[c] = a.FAy[fd] + a.FAy[fu];
         }
+        const double ir = 1.0 / w[0];
         double pr[4];
-        to_prim<double>(pr, w, geo.gamma);
+        pr[0] = w[0];
+        pr[1] = w[1] * ir;
+        pr[2] = w[2] * ir;
+        pr[3] = (geo.gamma - 1.0) * (w[3] - 0.5 * (w[1] * pr[1] + w[2] * pr[2]));
         if (pr[0] < 0 || pr[3] < 0 || isnan(pr[0]) || isnan(pr[3])) bad = 1;
         if (a.stage == 0) {
-            const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] / pr[0]);
-            const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
+            // Dtx (src/time_advance.cpp:264-305) with one reciprocal for both directions
+            const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] * ir);
+            const double it = geo.cfl / tmp;
+            const double qx = geo.dx * it, qy = geo.dy * it;
             if (qx > 0) cand = qx;
             if (qy > 0 && qy < cand) cand = qy;
         }

@@ -214,9 +214,9 @@ class Solver2D:
 
     def profile_step(self, tstop: float = 1e30) -> dict:
         """One step with events between launches: device milliseconds per kernel."""
-        ms = np.zeros(9)
+        ms = np.zeros(11)
         _check(self._lib.hos2d_profile_step(self._h, tstop, _ptr(ms)))
-        names = ["begin_step"] + [f"{k}{st}" for st in (0, 1) for k in ("bc_fill", "face_x", "face_y", "update")]
+        names = ["begin_step"] + [f"{k}{st}" for st in (0, 1) for k in ("bc_fill", "gate", "face_x", "face_y", "update")]
         return dict(zip(names, ms.tolist()))
 
     @property

@@ -125,7 +125,7 @@ int hos2d_sync(hos_solver2d* s, double* t, double* dt);
 
 /* One full time step with CUDA events between its launches; synchronises and writes the
  * device time in milliseconds of each launch, in order: begin_step, then per stage
- * bc_fill, x-face kernel, y-face kernel, update (9 values).  The reference has no
+ * bc_fill, gate (0 without a gate), x-face kernel, y-face kernel, update (11 values).  The reference has no
  * counterpart; it replaces its clock()-based Runtime timer (include/output.h:15-25) with
  * per-kernel device timing. */
 int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms);
