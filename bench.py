@@ -49,10 +49,11 @@ BYTES_PER_FACE = 120.0
 TRAFFIC_PER_FACE = 61.0
 # FP32 operations (2 x FFMA + FADD + FMUL) one gated FP32 face-kernel launch executes per face,
 # and its DRAM traffic per face (ncu, 256^2 Riemann WENO7 after 20 steps; the plain FP32
-# kernel executes 16,751 per face)
-FP32_FLOP_PER_FACE_GATED = 7050.0
-TRAFFIC_PER_FACE_FP32 = 80.5
+# kernel executes 17,998 per face)
+FP32_FLOP_PER_FACE_GATED = 7586.0
+TRAFFIC_PER_FACE_FP32 = 86.4
 AUDIT_LOG2 = 10   # audit one warp in 1024 of predicted-smooth cells with full weights
+ACC_STEPS = 200   # steps of the 512^2 runs whose density deviation the line states
 
 
 def parse():
@@ -203,7 +204,7 @@ def cpu_baseline_sample():
             "sample": f"{n}x{n} Riemann WENO7-AO-DF, {steps} S2O4 steps after 1 warm-up"}
 
 
-def batch_leg(dev, precision, count=64, seed=0, max_steps=4000):
+def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, threshold=0.0):
     """The batched sweep: ``count`` seeded shock-vortex / wedge problems (sides 128..768) in one
     batch, face-tile shapes chosen by the autotuner, every step one CUDA-graph replay.  Runs
     every problem to its end time; an event recorded after each step gives each problem's time
@@ -220,6 +221,8 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000):
     t0 = time.perf_counter()
     chosen, tune_ms = b.autotune(reps=3)
     tune_s = time.perf_counter() - t0
+    if gate is not None:
+        b.set_gate(gate, threshold, audit_log2=AUDIT_LOG2)
     ext = torch.cuda.ExternalStream(b.stream, device=dev)
     b.advance(1, graph=True)          # instantiates the graph (batch step index 0)
     for k, x in enumerate(sweep):     # back to the initial states
@@ -239,6 +242,7 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000):
             break
     torch.cuda.synchronize(dev)
     act, t, last, failed = b.status(failed=True)
+    gst = b.gate_stats() if gate is not None else None
     b.close()
     cells = np.array([x[0].nodex * x[0].nodey for x in sweep], dtype=np.float64)
     nsteps = last - base + 1          # steps each problem took (a failed one: up to its bad step)
@@ -257,7 +261,11 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000):
             "tiles": {"x": "x".join(map(str, Batch2D.SHAPES[chosen[0]])),
                       "y": "x".join(map(str, Batch2D.SHAPES[chosen[1]]))},
             "autotune_ms": tune_ms.round(3).tolist(), "autotune_s": tune_s, "graph": True,
-            "launches_per_step": 1 + 2 * 4, "gate": "off"}
+            "launches_per_step": 1 + 2 * (4 + (gate is not None)),
+            "gate": "off" if gst is None else {
+                "linear_path_fraction": (gst["smooth_x"] + gst["smooth_y"]) / max(1, gst["cells_x"] + gst["cells_y"]),
+                "audited": gst["audited"], "audit_false_negative_rate": gst["false_neg"] / max(1, gst["audited"]),
+                "aposteriori_rejections": gst["fallback"]}}
 
 
 def sgemm_tflops(torch, dev):
@@ -393,17 +401,29 @@ def main():
     # ---- gated FP32 (the headline), plain FP64 and plain FP32 on the same initial data ----
     with ClockSampler(local) as clk:
         sg, tg = run(FP32, True)
-    gstats = sg.gate_stats()
-    kern_g = kernel_ms(sg)
-    rho_g = sg.get_state()["convar"][g:-g, g:-g, 0]
-    s64, t64 = run(FP64, False)
-    kern_64 = kernel_ms(s64)
-    rho_64 = s64.get_state()["convar"][g:-g, g:-g, 0]
-    s32, t32 = run(FP32, False)
-    kern_32 = kernel_ms(s32)
-    rho_32 = s32.get_state()["convar"][g:-g, g:-g, 0]
+        gstats = sg.gate_stats()
+        kern_g = kernel_ms(sg)
+        rho_g = sg.get_state()["convar"][g:-g, g:-g, 0]
+        s64, t64 = run(FP64, False)
+        kern_64 = kernel_ms(s64)
+        rho_64 = s64.get_state()["convar"][g:-g, g:-g, 0]
+        s32, t32 = run(FP32, False)
+        kern_32 = kernel_ms(s32)
+        rho_32 = s32.get_state()["convar"][g:-g, g:-g, 0]
     s64.close()
     s32.close()
+
+    # deviation once the solution has structure: 512^2, 200 steps of each form from the same data
+    pa, ca, pra = cases.riemann2d(512, order=ORDER)
+    long_rho = {}
+    for name, prec, gated in (("fp64", FP64, False), ("fp32", FP32, False), ("gated", FP32, True)):
+        s = Solver2D(pa, prec)
+        s.set_state(ca, pra)
+        if gated:
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+        s.advance(ACC_STEPS, 1e30, graph=True)
+        long_rho[name] = s.get_state()["convar"][g:-g, g:-g, 0]
+        s.close()
 
     def dev_l1(a, b):
         return float(np.abs(a - b).mean() / np.abs(b).mean())
@@ -483,7 +503,11 @@ def main():
                      "rho_rel_l1_gated_vs_fp64": dev_l1(rho_g, rho_64),
                      "rho_rel_linf_gated_vs_fp64": dev_linf(rho_g, rho_64),
                      "rho_rel_l1_fp32_vs_fp64": dev_l1(rho_32, rho_64),
-                     "rho_rel_l1_gated_vs_fp32": dev_l1(rho_g, rho_32)},
+                     "rho_rel_l1_gated_vs_fp32": dev_l1(rho_g, rho_32),
+                     "developed": {"grid": "512x512", "steps": ACC_STEPS,
+                                   "rho_rel_l1_gated_vs_fp64": dev_l1(long_rho["gated"], long_rho["fp64"]),
+                                   "rho_rel_linf_gated_vs_fp64": dev_linf(long_rho["gated"], long_rho["fp64"]),
+                                   "rho_rel_l1_fp32_vs_fp64": dev_l1(long_rho["fp32"], long_rho["fp64"])}},
         "gate": {"train_s": train_s, "samples": rep.samples, "smooth_label_fraction": rep.smooth_fraction,
                  "threshold": rep.threshold, "heldout": rep.heldout,
                  "linear_path_fraction": smooth, "audited": gstats["audited"],
@@ -497,7 +521,12 @@ def main():
     if ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
     if not args.no_batch:
-        line["variants"]["batch64_fp32"] = batch_leg(dev, FP32)
+        # the sweep runs WENO5: its gate is trained the same way on WENO5 runs
+        gate5, rep5 = gate_train.train(order=5, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
+                                       train_steps=3000, batch=4096)
+        line["variants"]["batch64_fp32_gated"] = batch_leg(dev, FP32, gate=gate5, threshold=rep5.threshold)
+        line["variants"]["batch64_fp32_gated"]["gate_heldout"] = rep5.heldout
+        gate5.close()
     gate.close()
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "hos_batch.cuh"
+#include "hos_gate.cuh"
 
 namespace hos {
 
@@ -68,6 +69,23 @@ __global__ void begin_batch_kernel(const Prob* __restrict__ probs, int count, in
 }
 
 
+// learned gate over all problems: one block per 16 x 16 tile of a problem's cells
+struct GateTile { int p, i0, j0, pad; };
+
+template <int ORDER>
+__global__ void __launch_bounds__(gate::GATE_THREADS) gate_batch_kernel(const Prob* __restrict__ probs,
+                                                                        const GateTile* __restrict__ tiles, int ntiles,
+                                                                        gate::Net net, gate::Stats* stats, float threshold,
+                                                                        unsigned audit_mask, unsigned seed) {
+    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        const GateTile t = tiles[k];
+        const Prob* pr = probs + t.p;
+        gate::GateArgs a{pr->W, pr->AX, pr->AY, pr->gflags, stats, threshold, audit_mask, seed,
+                         nullptr, 0, 0xffffffffu, pr->ctl};
+        gate::gate_tile<ORDER>(a, net, pr->geo, t.i0, t.j0, (unsigned)k);
+    }
+}
+
 thread_local std::string g_errb;
 int failb(int code, const std::string& m) {
     g_errb = m;
@@ -100,6 +118,17 @@ struct hos_batch2d {
     long long cells = 0;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
+    // learned gate (FP32 batches)
+    int gated = 0;
+    unsigned char* gflags = nullptr;
+    gate::Stats* gstats = nullptr;
+    __nv_bfloat16* gw = nullptr;
+    float* gb = nullptr;
+    GateTile* gtiles = nullptr;
+    int ngtiles = 0;
+    float gthreshold = 0.0f;
+    unsigned gaudit_mask = 0;
+    unsigned gseed = 0;
 };
 
 namespace {
@@ -109,7 +138,8 @@ void freeb(hos_batch2d* b) {
     for (int d = 0; d < 2; ++d)
         for (int k = 0; k < kShapes; ++k)
             if (b->tiles_by_shape[d][k]) cudaFree(b->tiles_by_shape[d][k]);
-    void* ptrs[] = {b->probs, b->arena, b->ctls, b->last_step, b->counter, b->staging};
+    void* ptrs[] = {b->probs, b->arena, b->ctls, b->last_step, b->counter, b->staging,
+                    b->gflags, b->gstats, b->gw, b->gb, b->gtiles};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -120,9 +150,11 @@ cudaError_t launch_faces(hos_batch2d* b, int dir, int stage) {
     const int nt = b->ntiles[dir][sh];
     const int grid = std::max(1, std::min(nt, b->sms * std::max(1, b->bps[dir][sh])));
     const TileRef* t = b->tiles_by_shape[dir][sh];
-    if (b->order == 5) return launch_batch_faces5(b->precision, sh, dir, b->probs, t, nt, stage, grid, b->stream);
-    if (b->order == 7) return launch_batch_faces7(b->precision, sh, dir, b->probs, t, nt, stage, grid, b->stream);
-    return launch_batch_faces9(b->precision, sh, dir, b->probs, t, nt, stage, grid, b->stream);
+    const int prec = b->gated ? 2 : b->precision;
+    unsigned long long* fb = b->gated ? &b->gstats->fallback : nullptr;
+    if (b->order == 5) return launch_batch_faces5(prec, sh, dir, b->probs, t, nt, stage, grid, b->stream, fb);
+    if (b->order == 7) return launch_batch_faces7(prec, sh, dir, b->probs, t, nt, stage, grid, b->stream, fb);
+    return launch_batch_faces9(prec, sh, dir, b->probs, t, nt, stage, grid, b->stream, fb);
 }
 
 int enqueue_batch_step(hos_batch2d* b) {
@@ -135,6 +167,21 @@ int enqueue_batch_step(hos_batch2d* b) {
     }
     for (int stage = 0; stage < 2; ++stage) {
         bc_batch_kernel<<<dim3(std::min(maxg, 64), b->count), 256, 0, b->stream>>>(b->probs);
+        if (b->gated) {
+            const int grid = std::min(b->ngtiles, b->sms * 8);
+            const gate::Net net{b->gw, b->gw + gate::NH * gate::NF, b->gw + gate::NH * gate::NF + gate::NH * gate::NH,
+                                b->gb, b->gb + gate::NH, b->gb + 2 * gate::NH};
+            const unsigned seed = b->gseed++;
+            if (b->order == 5)
+                gate_batch_kernel<5><<<grid, gate::GATE_THREADS, 0, b->stream>>>(b->probs, b->gtiles, b->ngtiles, net, b->gstats,
+                                                                                 b->gthreshold, b->gaudit_mask, seed);
+            else if (b->order == 7)
+                gate_batch_kernel<7><<<grid, gate::GATE_THREADS, 0, b->stream>>>(b->probs, b->gtiles, b->ngtiles, net, b->gstats,
+                                                                                 b->gthreshold, b->gaudit_mask, seed);
+            else
+                gate_batch_kernel<9><<<grid, gate::GATE_THREADS, 0, b->stream>>>(b->probs, b->gtiles, b->ngtiles, net, b->gstats,
+                                                                                 b->gthreshold, b->gaudit_mask, seed);
+        }
         if ((e = launch_faces(b, 0, stage)) != cudaSuccess) return failb(HOS_E_CUDA, std::string("face x: ") + cudaGetErrorString(e));
         if ((e = launch_faces(b, 1, stage)) != cudaSuccess) return failb(HOS_E_CUDA, std::string("face y: ") + cudaGetErrorString(e));
         update_batch_kernel<<<dim3(std::min(maxc, 256), b->count), 256, 0, b->stream>>>(b->probs, stage);
@@ -450,6 +497,79 @@ int hos_batch2d_status(hos_batch2d* b, int* active, double* t, int* last_step, i
     if (!bad) return HOS_OK;
     // with per-problem flags the caller sees which problems failed; the others are intact
     return failed ? HOS_OK : failb(HOS_E_BLOWUP, std::to_string(bad) + " problem(s) of the batch blew up");
+}
+
+int hos_batch2d_set_gate(hos_batch2d* b, const hos_gate* g, float threshold, int audit_log2) {
+    using namespace gate;
+    if (!b) return failb(HOS_E_ARG, "null batch");
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return failb(HOS_E_CUDA, "set_gate");
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    if (!g) {
+        b->gated = 0;
+        return HOS_OK;
+    }
+    if (b->precision != HOS_FP32) return failb(HOS_E_CONFIG, "the learned gate runs on the FP32-bulk path");
+    if (audit_log2 < 0 || audit_log2 > 31) return failb(HOS_E_ARG, "audit_log2 must be 0..31");
+    if (!b->gflags) {
+        size_t total = 0;
+        std::vector<GateTile> gt;
+        for (int k = 0; k < b->count; ++k) {
+            const Geometry& geo = b->host_probs[k].geo;
+            total += (size_t)geo.nx * geo.ny;
+            for (int i0 = 0; i0 < geo.nx; i0 += GATE_TILE)
+                for (int j0 = 0; j0 < geo.ny; j0 += GATE_TILE) gt.push_back(GateTile{k, i0, j0, 0});
+        }
+        if ((e = cudaMalloc(&b->gflags, total)) == cudaSuccess && (e = cudaMemset(b->gflags, 0, total)) == cudaSuccess &&
+            (e = cudaMalloc(&b->gstats, sizeof(Stats))) == cudaSuccess && (e = cudaMemset(b->gstats, 0, sizeof(Stats))) == cudaSuccess &&
+            (e = cudaMalloc(&b->gw, NET_BF16 * sizeof(__nv_bfloat16))) == cudaSuccess &&
+            (e = cudaMalloc(&b->gb, NET_F32 * sizeof(float))) == cudaSuccess &&
+            (e = cudaMalloc(&b->gtiles, gt.size() * sizeof(GateTile))) == cudaSuccess)
+            e = cudaMemcpy(b->gtiles, gt.data(), gt.size() * sizeof(GateTile), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return failb(HOS_E_NOMEM, std::string("gate buffers: ") + cudaGetErrorString(e));
+        b->ngtiles = (int)gt.size();
+        size_t off = 0;
+        for (int k = 0; k < b->count; ++k) {
+            const Geometry& geo = b->host_probs[k].geo;
+            b->host_probs[k].gflags = b->gflags + off;
+            off += (size_t)geo.nx * geo.ny;
+        }
+        e = cudaMemcpy(b->probs, b->host_probs.data(), b->count * sizeof(Prob), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return failb(HOS_E_CUDA, "problem table");
+    }
+    if ((e = cudaStreamSynchronize(g->stream)) == cudaSuccess &&
+        (e = cudaMemcpy(b->gw, g->wbf, NET_BF16 * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice)) == cudaSuccess)
+        e = cudaMemcpy(b->gb, g->bias, NET_F32 * sizeof(float), cudaMemcpyDeviceToDevice);
+    for (int dir = 0; dir < 2 && e == cudaSuccess; ++dir) {
+        int bps[kShapes] = {0, 0, 0};
+        e = b->order == 5 ? configure_batch5(2, dir, bps) : b->order == 7 ? configure_batch7(2, dir, bps)
+                                                                          : configure_batch9(2, dir, bps);
+    }
+    if (e != cudaSuccess) return failb(HOS_E_CUDA, std::string("set_gate: ") + cudaGetErrorString(e));
+    b->gthreshold = threshold;
+    b->gaudit_mask = audit_log2 == 31 ? 0xffffffffu : (1u << audit_log2) - 1u;
+    b->gated = 1;
+    return HOS_OK;
+}
+
+int hos_batch2d_gate_stats(hos_batch2d* b, unsigned long long* stats, int reset) {
+    if (!b || !stats) return failb(HOS_E_ARG, "null argument");
+    if (!b->gstats) {
+        std::memset(stats, 0, 8 * sizeof(unsigned long long));
+        return HOS_OK;
+    }
+    gate::Stats st;
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, b->gstats, sizeof st, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(b->gstats, 0, sizeof st);
+    if (e != cudaSuccess) return failb(HOS_E_CUDA, "gate_stats");
+    const unsigned long long v[8] = {st.cells[0], st.cells[1], st.smooth[0], st.smooth[1], st.audited, st.false_neg,
+                                     st.fallback, st.samples};
+    std::memcpy(stats, v, sizeof v);
+    return HOS_OK;
 }
 
 long long hos_batch2d_cells(const hos_batch2d* b) { return b ? b->cells : 0; }

@@ -16,6 +16,7 @@ struct Prob {
     StepCtl* ctl;
     double tstop;
     int* last_step;   // batch step index of this problem's last active step
+    unsigned char* gflags;   // learned-gate flags of this problem's cells (gated batches)
 };
 
 struct TileRef { int p, n0, t0, pad; };
@@ -28,10 +29,11 @@ constexpr int kShapes = 3;
 const int kShapeN[kShapes] = {8, 4, 16};
 const int kShapeT[kShapes] = {16, 32, 8};
 
-template <class T, int ORDER, int DIR, class TS>
-__global__ void __launch_bounds__(FACE_THREADS) face_batch_kernel(const Prob* __restrict__ probs,
+// FP32 tiles fit two CTAs per SM in 128 registers; FP64 tiles need more registers than that
+template <class T, int ORDER, int DIR, class TS, bool GATED = false>
+__global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_batch_kernel(const Prob* __restrict__ probs,
                                                                   const TileRef* __restrict__ tiles, int ntiles,
-                                                                  int stage) {
+                                                                  int stage, unsigned long long* fallback) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
         const TileRef tr = tiles[k];
@@ -46,16 +48,18 @@ __global__ void __launch_bounds__(FACE_THREADS) face_batch_kernel(const Prob* __
         a.FA = DIR == 0 ? pr->FAx : pr->FAy;
         a.ctl = pr->ctl;
         a.stage = stage;
-        face_tile<T, ORDER, DIR, TS>(a, geo, tr.n0, tr.t0, smem_raw);
+        a.gate = pr->gflags;
+        a.fallback = fallback;
+        face_tile<T, ORDER, DIR, TS, GATED>(a, geo, tr.n0, tr.t0, smem_raw);
         __syncthreads();  // the next tile reuses the shared memory
     }
 }
 
 // launch / configure the face kernels of one order (defined per order in hos_batch{5,7,9}.cu);
-// orders 7 and 9 provide the default tile shape only
-cudaError_t launch_batch_faces5(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s);
-cudaError_t launch_batch_faces7(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s);
-cudaError_t launch_batch_faces9(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s);
+// orders 7 and 9 provide the default tile shape only; prec 0 FP64, 1 FP32, 2 gated FP32
+cudaError_t launch_batch_faces5(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s, unsigned long long* fallback);
+cudaError_t launch_batch_faces7(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s, unsigned long long* fallback);
+cudaError_t launch_batch_faces9(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid, cudaStream_t s, unsigned long long* fallback);
 cudaError_t configure_batch5(int prec, int dir, int* bps);
 cudaError_t configure_batch7(int prec, int dir, int* bps);
 cudaError_t configure_batch9(int prec, int dir, int* bps);

@@ -1,26 +1,30 @@
-// hos_batch7.cu -- batched WENO7-AO-DF face kernels (1 tile shape, FP64 and FP32 compute).
+// hos_batch7.cu -- batched WENO7-AO-DF face kernels (the default tile shape; FP64, FP32 and gated FP32).
 #include "hos_batch.cuh"
 
 namespace hos {
 namespace batch {
 
-template <class T, int DIR>
+template <class T, int DIR, bool GATED>
 static cudaError_t launch_t(int shape, const Prob* probs, const TileRef* tiles, int ntiles, int stage, int grid,
-                            cudaStream_t s) {
+                            cudaStream_t s, unsigned long long* fallback) {
     switch (shape) {
-        case 0:
-            face_batch_kernel<T, 7, DIR, Shape0><<<grid, FACE_THREADS, FaceSmem<T, 7, Shape0>::bytes, s>>>(probs, tiles, ntiles, stage);
+        case 0: {
+            using S = FaceSmem<T, 7, Shape0>;
+            face_batch_kernel<T, 7, DIR, Shape0, GATED><<<grid, FACE_THREADS, GATED ? S::gated_bytes : S::bytes, s>>>(
+                probs, tiles, ntiles, stage, fallback);
             break;
+        }
         default:
             return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
-template <class T, int DIR, class TS>
+template <class T, int DIR, class TS, bool GATED>
 static cudaError_t configure_one(int* blocks_per_sm) {
-    auto k = face_batch_kernel<T, 7, DIR, TS>;
-    const int bytes = (int)FaceSmem<T, 7, TS>::bytes;
+    auto k = face_batch_kernel<T, 7, DIR, TS, GATED>;
+    using S = FaceSmem<T, 7, TS>;
+    const int bytes = (int)(GATED ? S::gated_bytes : S::bytes);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
@@ -28,26 +32,28 @@ static cudaError_t configure_one(int* blocks_per_sm) {
     return e;
 }
 
-template <class T, int DIR>
+template <class T, int DIR, bool GATED>
 static cudaError_t configure_t(int* bps) {
     cudaError_t e;
-    if ((e = configure_one<T, DIR, Shape0>(&bps[0])) != cudaSuccess) return e;
-    bps[1] = 0;  // shape not provided for this order
-    bps[2] = 0;  // shape not provided for this order
+    if ((e = configure_one<T, DIR, Shape0, GATED>(&bps[0])) != cudaSuccess) return e;
+    bps[1] = bps[2] = 0;   // shapes 1 and 2 are not instantiated for this order
     return cudaSuccess;
 }
 
 cudaError_t launch_batch_faces7(int prec, int shape, int dir, const Prob* probs, const TileRef* tiles, int ntiles, int stage,
-                                 int grid, cudaStream_t s) {
-    if (prec == 0) return dir == 0 ? launch_t<double, 0>(shape, probs, tiles, ntiles, stage, grid, s)
-                                   : launch_t<double, 1>(shape, probs, tiles, ntiles, stage, grid, s);
-    return dir == 0 ? launch_t<float, 0>(shape, probs, tiles, ntiles, stage, grid, s)
-                    : launch_t<float, 1>(shape, probs, tiles, ntiles, stage, grid, s);
+                                 int grid, cudaStream_t s, unsigned long long* fallback) {
+    if (prec == 0) return dir == 0 ? launch_t<double, 0, false>(shape, probs, tiles, ntiles, stage, grid, s, fallback)
+                                   : launch_t<double, 1, false>(shape, probs, tiles, ntiles, stage, grid, s, fallback);
+    if (prec == 1) return dir == 0 ? launch_t<float, 0, false>(shape, probs, tiles, ntiles, stage, grid, s, fallback)
+                                   : launch_t<float, 1, false>(shape, probs, tiles, ntiles, stage, grid, s, fallback);
+    return dir == 0 ? launch_t<float, 0, true>(shape, probs, tiles, ntiles, stage, grid, s, fallback)
+                    : launch_t<float, 1, true>(shape, probs, tiles, ntiles, stage, grid, s, fallback);
 }
 
 cudaError_t configure_batch7(int prec, int dir, int* bps) {
-    if (prec == 0) return dir == 0 ? configure_t<double, 0>(bps) : configure_t<double, 1>(bps);
-    return dir == 0 ? configure_t<float, 0>(bps) : configure_t<float, 1>(bps);
+    if (prec == 0) return dir == 0 ? configure_t<double, 0, false>(bps) : configure_t<double, 1, false>(bps);
+    if (prec == 1) return dir == 0 ? configure_t<float, 0, false>(bps) : configure_t<float, 1, false>(bps);
+    return dir == 0 ? configure_t<float, 0, true>(bps) : configure_t<float, 1, true>(bps);
 }
 
 }  // namespace batch

@@ -250,17 +250,18 @@ constexpr int GATE_TILE = 16;   // 16 x 16 cells per block, one thread per cell
 // its stencil halo are converted once to FP32 density and pressure in shared memory; the
 // features are read from there.  Stencils that leave the array get no flag (the face kernel
 // then reconstructs that cell with full WENO-AO).
+// One 16 x 16 tile with first cell (i0, j0); tile_id numbers the tile for the audit draw.
 template <int ORDER>
-__global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net, Geometry geo) {
+__device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, const Geometry& geo, int i0, int j0,
+                                          unsigned tile_id) {
     constexpr int r = ORDER / 2, H = GATE_TILE + 2 * r;
     __shared__ __align__(16) __nv_bfloat16 xs[GATE_THREADS / 32][32 * NF];
     __shared__ float zs[GATE_THREADS / 32][32];
     __shared__ float srho[H][H + 1], sp[H][H + 1];
     __shared__ unsigned counts[4];           // cells x, cells y, smooth x, smooth y of the block
-    if (a.ctl && !a.ctl->active) return;   // uniform over the grid
+    if (a.ctl && !a.ctl->active) return;   // uniform over the block
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid < 4) counts[tid] = 0;
-    const int i0 = blockIdx.y * GATE_TILE, j0 = blockIdx.x * GATE_TILE;
     const size_t plane = (size_t)geo.nx * geo.ny;
     const float gamma = float(geo.gamma);
     for (int e = tid; e < H * H; e += GATE_THREADS) {
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net,
         if (a.flags) {
             // audits are drawn per warp, so an audited warp re-checks all its predicted-smooth
             // cells together instead of stalling 31 lanes behind one
-            const unsigned wid = (blockIdx.y * gridDim.x + blockIdx.x) * (GATE_THREADS / 32) + warp;
+            const unsigned wid = tile_id * (GATE_THREADS / 32) + warp;
             const unsigned hw = mix_hash(wid * 2u + (unsigned)dir + a.seed * 0x85ebca6bu);
             if (smooth && (hw & a.audit_mask) == 0) {
                 const float d = dir == 0 ? weight_distance<ORDER, 0>(a.W, plane, c, stride, gamma, geo.characteristic)
@@ -360,6 +361,12 @@ __global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net,
         if (tid < 2) atomicAdd(&a.stats->cells[tid], (unsigned long long)counts[tid]);
         else if (tid < 4) atomicAdd(&a.stats->smooth[tid - 2], (unsigned long long)counts[tid]);
     }
+    __syncthreads();   // the shared arrays are reused by the block's next tile
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net, Geometry geo) {
+    gate_tile<ORDER>(a, net, geo, blockIdx.y * GATE_TILE, blockIdx.x * GATE_TILE, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 }  // namespace gate

@@ -565,7 +565,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
 }
 
 template <class T, int ORDER, int DIR, bool GATED = false>
-__global__ void __launch_bounds__(FACE_THREADS) face_kernel(FaceArgs a, Geometry geo) {
+__global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_kernel(FaceArgs a, Geometry geo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     face_tile<T, ORDER, DIR, DefaultTile, GATED>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
 }

@@ -108,6 +108,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                    ctypes.c_uint, _DP]
     lib.hos_gate_last_error.restype = ctypes.c_char_p
     lib.hos2d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
+    lib.hos_batch2d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
+    lib.hos_batch2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     lib.hos2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     _LIB = lib
     return lib
@@ -377,6 +379,16 @@ class Batch2D:
         if failed:
             return act.value, t, np.array(last[:]), np.array(bad[:], dtype=bool)
         return act.value, t, np.array(last[:])
+
+    def set_gate(self, gate, threshold: float = 0.0, audit_log2: int = 10) -> None:
+        """Attach a copy of a learned gate (FP32 batches); None detaches it."""
+        _checkb(self._lib.hos_batch2d_set_gate(self._h, gate._h if gate is not None else None, threshold, audit_log2))
+
+    def gate_stats(self, reset: bool = False) -> dict:
+        v = (ctypes.c_ulonglong * 8)()
+        _checkb(self._lib.hos_batch2d_gate_stats(self._h, v, 1 if reset else 0))
+        keys = ("cells_x", "cells_y", "smooth_x", "smooth_y", "audited", "false_neg", "fallback", "unused")
+        return dict(zip(keys, (int(x) for x in v)))
 
     @property
     def cells(self) -> int:

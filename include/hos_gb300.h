@@ -254,6 +254,9 @@ int hos_batch2d_advance(hos_batch2d* b, int nsteps, int use_graph);
  * bad (negative density/pressure or NaN: the reference's exit) stops stepping; the others go
  * on.  With failed == NULL such a failure is reported as HOS_E_BLOWUP. */
 int hos_batch2d_status(hos_batch2d* b, int* active, double* t, int* last_step, int* failed);
+/* attach a copy of a learned gate to an FP32 batch (NULL detaches); counters as hos2d_gate_stats */
+int hos_batch2d_set_gate(hos_batch2d* b, const hos_gate* g, float threshold, int audit_log2);
+int hos_batch2d_gate_stats(hos_batch2d* b, unsigned long long* stats, int reset);
 long long hos_batch2d_cells(const hos_batch2d* b);
 void* hos_batch2d_stream(hos_batch2d* b);
 const char* hos_batch2d_last_error(void);
