@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const Prob* __restric
         cmin = fmin(cmin, c);
         bad |= b;
     }
-    reduce_block(cmin, bad, pr->ctl, stage == 0);
+    reduce_block(cmin, bad, pr->ctl, stage == cfl_stage(geo));
 }
 
 // step prologue for every problem (one block); *counter is the batch step index
@@ -207,6 +207,8 @@ int hos_batch2d_create(const hos_params2d* params, const double* tstop, int coun
             return failb(HOS_E_CONFIG, "problem " + std::to_string(k) + ": bad order/gausspoint/ghost/size");
         for (int s = 0; s < 4; ++s)
             if (p.bc[s] < 0 || p.bc[s] > 5) return failb(HOS_E_CONFIG, "bad boundary kind");
+        if (p.integrator != HOS_INT_S2O4 || p.flux != HOS_FLUX_GKS)
+            return failb(HOS_E_CONFIG, "batches run S2O4 with the GKS flux");
         if (p.bc[0] >= 4 || p.bc[1] >= 4 || p.bc[2] == HOS_BC_WEDGE_TOP || p.bc[3] == HOS_BC_WEDGE_BOTTOM ||
             ((p.bc[2] >= 4 || p.bc[3] >= 4) && p.bc[0] != HOS_BC_INFLOW))
             return failb(HOS_E_CONFIG, "bad wedge boundary placement");

@@ -249,4 +249,31 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
     }
 }
 
+// Lax-Friedrichs flux times dt of one Gauss point in the face frame (LF2D,
+// src/flux_function.cpp:700-735): the larger of |u| + c on the two sides as dissipation.
+template <class T>
+__device__ __forceinline__ void lf_point(const T* wl, const T* wr, T dt, T gamma, T* f) {
+    T pl[4], pr[4];
+    to_prim(pl, wl, gamma);
+    to_prim(pr, wr, gamma);
+    const T kl = fabsT(pl[1]) + sqrt(gamma * pl[3] / pl[0]);
+    const T kr = fabsT(pr[1]) + sqrt(gamma * pr[3] / pr[0]);
+    const T beta = kr > kl ? kr : kl;
+    const T ig = T(1.0) / (gamma - T(1.0));
+    T fl[4], fr[4];
+    const T* q[2] = {pl, pr};
+    T* o[2] = {fl, fr};
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+        const T* p = q[sd];
+        o[sd][0] = p[0] * p[1];
+        o[sd][1] = p[0] * p[1] * p[1] + p[3];
+        o[sd][2] = p[0] * p[1] * p[2];
+        const T e = T(0.5) * (p[1] * p[1] + p[2] * p[2]) * p[0] + p[3] * ig;
+        o[sd][3] = p[1] * (e + p[3]);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) f[m] = dt * (T(0.5) * ((fl[m] + fr[m]) - beta * (wr[m] - wl[m])));
+}
+
 }  // namespace hos

@@ -36,7 +36,38 @@ struct Geometry {
     double dx, dy, cfl;
     double gamma, K, c1, c2;
     int characteristic;
+    int integrator = 0;   // HOS_INT_*: S2O4, S1O1, S1O2, RK2, RK3, RK4
+    int flux = 0;         // HOS_FLUX_*: GKS2D, LF2D
+    int stages = 2;
 };
+
+// Stages per step and Block2d::timecoefficient[s][k][f or derf] of each time-marching method
+// (S1O1_2D ... RK4_2D, src/time_advance.cpp:197-247).  RK3 combines states instead
+// (Update_with_gauss_RK3, :476-532): its flux weights per stage are 1, 1/4, 2/3.
+__host__ __device__ constexpr int integrator_stages(int integrator) {
+    return integrator == 1 || integrator == 2 ? 1 : integrator == 4 ? 3 : integrator == 5 ? 4 : 2;
+}
+__device__ __forceinline__ double time_coefficient(int integrator, int s, int k, int j) {
+    switch (integrator) {
+        case 0:   // S2O4
+            if (s == 0) return k == 0 ? (j == 0 ? 0.5 : 1.0 / 8.0) : 0.0;
+            return k == 0 ? (j == 0 ? 1.0 : 1.0 / 6.0) : (j == 0 ? 0.0 : 1.0 / 3.0);
+        case 1:   // S1O1
+            return s == 0 && k == 0 && j == 0 ? 1.0 : 0.0;
+        case 2:   // S1O2
+            return s == 0 && k == 0 ? (j == 0 ? 1.0 : 0.5) : 0.0;
+        case 3:   // RK2
+            if (j) return 0.0;
+            return s == 0 ? (k == 0 ? 1.0 : 0.0) : 0.5;
+        case 4:   // RK3: flux weight of the stage itself
+            if (j || k != s) return 0.0;
+            return s == 0 ? 1.0 : s == 1 ? 0.25 : 2.0 / 3.0;
+        default:  // RK4
+            if (j) return 0.0;
+            if (s < 3) return k == s ? (s == 2 ? 1.0 : 0.5) : 0.0;
+            return k == 0 || k == 3 ? 1.0 / 6.0 : 1.0 / 3.0;
+    }
+}
 
 // ------------------------------------------------------------------------------------------
 // ghost-cell fill: a single gather equal to the reference's sequential left, right, down, up
@@ -92,6 +123,10 @@ struct FaceArgs {
     // of linear results the a-posteriori check rejected
     const unsigned char* gate;
     unsigned long long* fallback;
+    // time-marching methods other than S2O4: Gauss-integrated flux and its time derivative of
+    // every earlier stage [stage][4][nf]
+    double* FS;
+    double* DS;
 };
 
 // A tile is TN faces along the normal by TT along the tangent, handled by one CTA of
@@ -500,7 +535,20 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             R.w[v] = sr[v]; R.dx[v] = sr[4 + v]; R.dy[v] = sr[8 + v];
         }
         T f[4], d[4];
-        gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
+        if (geo.flux == 1) {
+            lf_point<T>(L.w, R.w, dt, gamma, f);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) d[v] = T(0.0);
+        } else {
+            gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
+            if (geo.integrator == 1) {   // S1O1 takes the dt integral F0 = f + d / 2 alone
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    f[v] = f[v] + T(0.5) * d[v];
+                    d[v] = T(0.0);
+                }
+            }
+        }
         T* o = flux + (fidx * GP + ig) * 9;
 #pragma unroll
         for (int v = 0; v < 4; ++v) { o[v] = f[v]; o[4 + v] = d[v]; }
@@ -532,14 +580,31 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 asum += o[8];
             }
             double X[4], P[4];
+            const bool s2o4 = geo.integrator == 0;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
                 const double F = double(Fq[v]), D = double(Dq[v]);
-                if (a.stage == 0) {
-                    X[v] = 0.5 * F + (1.0 / 8.0) * D;
-                    P[v] = 1.0 * F + (1.0 / 6.0) * D;
+                if (s2o4) {
+                    if (a.stage == 0) {
+                        X[v] = 0.5 * F + (1.0 / 8.0) * D;
+                        P[v] = 1.0 * F + (1.0 / 6.0) * D;
+                    } else {
+                        X[v] = (1.0 / 3.0) * D;
+                        P[v] = 0.0;
+                    }
                 } else {
-                    X[v] = (1.0 / 3.0) * D;
+                    // X_s = sum over stages k <= s of c[s][k] (F_k, D_k) (Update, :378-428)
+                    const int sg = a.stage;
+                    double x = time_coefficient(geo.integrator, sg, sg, 0) * F +
+                               time_coefficient(geo.integrator, sg, sg, 1) * D;
+                    for (int k = 0; k < sg; ++k)
+                        x += time_coefficient(geo.integrator, sg, k, 0) * a.FS[((size_t)k * 4 + v) * nf + fi] +
+                             time_coefficient(geo.integrator, sg, k, 1) * a.DS[((size_t)k * 4 + v) * nf + fi];
+                    X[v] = x;
+                    if (sg + 1 < geo.stages) {
+                        a.FS[((size_t)sg * 4 + v) * nf + fi] = F;
+                        a.DS[((size_t)sg * 4 + v) * nf + fi] = D;
+                    }
                     P[v] = 0.0;
                 }
             }
@@ -547,7 +612,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             const double as = double(asum);
             double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
             a.FA[fi] = am < 2.0 ? 0.0 : am;
-            if (a.stage == 1) {
+            if (s2o4 && a.stage == 1) {
 #pragma unroll
                 for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
             }
@@ -556,7 +621,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             if (DIR == 1) { Xg[1] = -X[2]; Xg[2] = X[1]; }
 #pragma unroll
             for (int v = 0; v < 4; ++v) a.FX[v * nf + fi] = Xg[v];
-            if (a.stage == 0) {
+            if (s2o4 && a.stage == 0) {
 #pragma unroll
                 for (int v = 0; v < 4; ++v) a.FP[v * nf + fi] = P[v];
             }

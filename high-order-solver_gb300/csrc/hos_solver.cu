@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo)
     double cand;
     unsigned int bad;
     update_one(a, geo, blockIdx.x * blockDim.x + threadIdx.x, cand, bad);
-    reduce_block(cand, bad, a.ctl, a.stage == 0);
+    reduce_block(cand, bad, a.ctl, a.stage == cfl_stage(geo));
 }
 
 // CFL candidates from a primitive state (the initial data's primvar at step 0)
@@ -146,6 +146,8 @@ struct hos_solver2d {
     double* FPy = nullptr;
     double* FAy = nullptr;
     double* scratch = nullptr;  // 8 * ncell doubles: AoS staging + primitive planes
+    double* stagex = nullptr;   // methods other than S2O4: per-stage F and D of x faces [2][4][4][nfx]
+    double* stagey = nullptr;   // ... and of y faces
     StepCtl* ctl = nullptr;
     // captured step
     cudaGraphExec_t graph = nullptr;
@@ -193,7 +195,8 @@ void fill_boundaries(BcSpec& bc, const hos_params2d& p, double dx) {
 }
 
 void free_all(hos_solver2d* s) {
-    double* bufs[] = {s->W, s->Wold, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->FXy, s->FPy, s->FAy, s->scratch};
+    double* bufs[] = {s->W, s->Wold, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->FXy, s->FPy, s->FAy, s->scratch,
+                      s->stagex, s->stagey};
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->ctl) cudaFree(s->ctl);
@@ -220,6 +223,12 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     }
     FaceArgs ax{s->W, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->ctl, stage};
     FaceArgs ay{s->W, s->AY, s->AX, s->FXy, s->FPy, s->FAy, s->ctl, stage};
+    if (s->stagex) {
+        ax.FS = s->stagex;
+        ax.DS = s->stagex + 16 * s->nfx;
+        ay.FS = s->stagey;
+        ay.DS = s->stagey + 16 * s->nfy;
+    }
     if (s->gated) {
         // per-cell smoothness flags of this stage's state (ghosts filled) for both directions
         gate::GateArgs ga{s->W, s->AX, s->AY, s->gflags, s->gstats, s->gthreshold, s->gaudit_mask, s->gseed++,
@@ -254,7 +263,7 @@ int enqueue_begin(hos_solver2d* s, double tstop) {
 int enqueue_step(hos_solver2d* s, double tstop) {
     int st = enqueue_begin(s, tstop);
     if (st) return st;
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < s->geo.stages; ++k)
         if ((st = enqueue_stage(s, k)) != HOS_OK) return st;
     return HOS_OK;
 }
@@ -298,6 +307,8 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     if (p.nodex < p.ghost || p.nodey < p.ghost) return fail(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail(HOS_E_CONFIG, "precision must be HOS_FP64 or HOS_FP32");
     if (int st = check_boundaries(p)) return st;
+    if (p.integrator < HOS_INT_S2O4 || p.integrator > HOS_INT_RK4) return fail(HOS_E_CONFIG, "bad time-marching method");
+    if (p.flux != HOS_FLUX_GKS && p.flux != HOS_FLUX_LF) return fail(HOS_E_CONFIG, "bad flux");
     hos_solver2d* s = new (std::nothrow) hos_solver2d();
     if (!s) return fail(HOS_E_NOMEM, "host allocation");
     s->p = p;
@@ -318,6 +329,9 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     geo.c1 = p.c1_euler;
     geo.c2 = p.c2_euler;
     geo.characteristic = p.characteristic ? 1 : 0;
+    geo.integrator = p.integrator;
+    geo.flux = p.flux;
+    geo.stages = integrator_stages(p.integrator);
     fill_boundaries(s->bc, p, geo.dx);
     s->ncell = (size_t)geo.nx * geo.ny;
     s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;
@@ -329,8 +343,10 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     struct { double** p; size_t n; } allocs[] = {
         {&s->W, 4 * s->ncell}, {&s->Wold, 4 * s->ncell}, {&s->AX, s->ncell}, {&s->AY, s->ncell},
         {&s->FXx, 4 * s->nfx}, {&s->FPx, 4 * s->nfx}, {&s->FAx, s->nfx},
-        {&s->FXy, 4 * s->nfy}, {&s->FPy, 4 * s->nfy}, {&s->FAy, s->nfy}, {&s->scratch, 8 * s->ncell}};
+        {&s->FXy, 4 * s->nfy}, {&s->FPy, 4 * s->nfy}, {&s->FAy, s->nfy}, {&s->scratch, 8 * s->ncell},
+        {&s->stagex, p.integrator ? 32 * s->nfx : 0}, {&s->stagey, p.integrator ? 32 * s->nfy : 0}};
     for (auto& a : allocs) {
+        if (a.n == 0) continue;
         if ((e = cudaMalloc(a.p, a.n * sizeof(double))) != cudaSuccess) {
             free_all(s);
             delete s;
@@ -562,7 +578,7 @@ int hos2d_boundary(hos_solver2d* s) {
 
 int hos2d_stage(hos_solver2d* s, int stage) {
     if (!s) return fail(HOS_E_ARG, "null solver");
-    if (stage != 0 && stage != 1) return fail(HOS_E_ARG, "stage must be 0 or 1");
+    if (stage < 0 || stage >= s->geo.stages) return fail(HOS_E_ARG, "stage out of range for the time-marching method");
     return enqueue_stage(s, stage);
 }
 
@@ -618,6 +634,7 @@ int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
 
 int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms) {
     if (!s || !ms) return fail(HOS_E_ARG, "null argument");
+    if (s->geo.stages != 2) return fail(HOS_E_CONFIG, "per-kernel profiling covers two-stage methods");
     cudaEvent_t ev[12];
     for (auto& x : ev) cudaEventCreate(&x);
     cudaEventRecord(ev[0], s->stream);
@@ -642,7 +659,7 @@ int hos2d_profile_step(hos_solver2d* s, double tstop, double* ms) {
 
 int hos2d_launches_per_step(const hos_solver2d* s) {
     // begin_step + per stage (bc, [gate,] x faces, y faces, update)
-    return 1 + 2 * (4 + (s && s->gated ? 1 : 0));
+    return 1 + (s ? s->geo.stages : 2) * (4 + (s && s->gated ? 1 : 0));
 }
 
 void* hos2d_stream(hos_solver2d* s) { return s ? (void*)s->stream : nullptr; }

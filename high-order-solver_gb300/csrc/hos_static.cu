@@ -69,6 +69,8 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
     if (p.gausspoint != (p.order == 5 ? 2 : p.order == 7 ? 3 : 4))
         return fail_static(HOS_E_CONFIG, "gausspoint must be 2/3/4 for order 5/7/9");
     if (!p.use_df) return fail_static(HOS_E_CONFIG, "use_df must be 1");
+    if (p.integrator != HOS_INT_S2O4 || p.flux != HOS_FLUX_GKS)
+        return fail_static(HOS_E_CONFIG, "the allocation-free step runs S2O4 with the GKS flux");
     if (p.ghost < p.order / 2 + 1) return fail_static(HOS_E_CONFIG, "ghost must be >= order/2 + 1");
     if (p.nodex < p.ghost || p.nodey < p.ghost) return fail_static(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
     if (p.nodex > kMaxNode || p.nodey > kMaxNode || p.ghost > kMaxGhost)

@@ -85,7 +85,10 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* addr, double 
     atomicMin(addr, (unsigned long long)__double_as_longlong(v));
 }
 
-// update of interior cell idx; returns its CFL candidate (stage 0) and blow-up bit
+// the stage whose update produces the next step's CFL candidates
+__device__ __forceinline__ int cfl_stage(const Geometry& geo) { return geo.stages >= 2 ? geo.stages - 2 : 0; }
+
+// update of interior cell idx; returns its CFL candidate (at cfl_stage) and blow-up bit
 __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& geo, int idx, double& cand,
                                            unsigned int& bad) {
     const int nodex = geo.nodex, nodey = geo.nodey, g = geo.g, ny = geo.ny;
@@ -100,22 +103,29 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
         // one reciprocal instead of four divisions: the FP64 pipe is the update's bound
         const double iarea = 1.0 / (geo.dx * geo.dy);
-        double w[4];
+        double w[4], w0[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             double old;
+            const double cur = a.W[v * plane + c];   // the state the stage started from
             if (a.stage == 0) {
-                old = a.W[v * plane + c];
+                old = cur;
                 a.Wold[v * plane + c] = old;
             } else {
                 old = a.Wold[v * plane + c];
             }
+            w0[v] = cur;
             double total = 0.0;
             total += geo.dx * a.FXy[v * nfy + fd];
             total += -geo.dx * a.FXy[v * nfy + fu];
             total += geo.dy * a.FXx[v * nfx + fl];
             total += -geo.dy * a.FXx[v * nfx + fr];
-            w[v] = old + total * iarea;
+            if (geo.integrator == 4 && a.stage == 1)        // RK3 (Update_with_gauss_RK3, :511-526)
+                w[v] = 0.75 * old + 0.25 * cur + total * iarea;
+            else if (geo.integrator == 4 && a.stage == 2)
+                w[v] = 1.0 / 3.0 * old + 2.0 / 3.0 * cur + total * iarea;
+            else
+                w[v] = old + total * iarea;
             a.W[v * plane + c] = w[v];
         }
         const int jend = nodex < nodey ? nodex : nodey;
@@ -130,9 +140,20 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         pr[2] = w[2] * ir;
         pr[3] = (geo.gamma - 1.0) * (w[3] - 0.5 * (w[1] * pr[1] + w[2] * pr[2]));
         if (pr[0] < 0 || pr[3] < 0 || isnan(pr[0]) || isnan(pr[3])) bad = 1;
-        if (a.stage == 0) {
+        if (a.stage == cfl_stage(geo)) {
+            // the reference's Get_CFL reads the primitives converted at the start of the last
+            // stage: the new state of stage stages - 2, or the step's starting state for
+            // one-stage methods
+            double ir2 = ir;
+            if (geo.stages == 1) {
+                ir2 = 1.0 / w0[0];
+                pr[0] = w0[0];
+                pr[1] = w0[1] * ir2;
+                pr[2] = w0[2] * ir2;
+                pr[3] = (geo.gamma - 1.0) * (w0[3] - 0.5 * (w0[1] * pr[1] + w0[2] * pr[2]));
+            }
             // Dtx (src/time_advance.cpp:264-305) with one reciprocal for both directions
-            const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] * ir);
+            const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] * ir2);
             const double it = geo.cfl / tmp;
             const double qx = geo.dx * it, qy = geo.dy * it;
             if (qx > 0) cand = qx;

@@ -35,7 +35,14 @@ class Params2D(ctypes.Structure):
         ("bc", ctypes.c_int * 4), ("bc_prim", (ctypes.c_double * 4) * 4),
         ("wedge_x0", ctypes.c_double), ("wedge_top_speed", ctypes.c_double),
         ("wedge_post", ctypes.c_double * 4), ("wedge_pre", ctypes.c_double * 4),
+        ("integrator", ctypes.c_int), ("flux", ctypes.c_int),
     ]
+
+
+# time-marching methods and fluxes (HOS_INT_*, HOS_FLUX_* in include/hos_gb300.h)
+INTEGRATORS = {"S2O4": 0, "S1O1": 1, "S1O2": 2, "RK2": 3, "RK3": 4, "RK4": 5}
+STAGES = {0: 2, 1: 1, 2: 1, 3: 2, 4: 3, 5: 4}
+FLUXES = {"GKS": 0, "LF": 1}
 
 
 @dataclass
@@ -63,6 +70,9 @@ class Problem2D:
     wedge_top_speed: float = 0.0
     wedge_post: tuple = (0.0,) * 4
     wedge_pre: tuple = (0.0,) * 4
+    # time marching and flux (the reference's timecoe_list_2d / flux_function_2d)
+    integrator: str = "S2O4"
+    flux: str = "GKS"
 
     @property
     def nx(self) -> int:
@@ -99,6 +109,8 @@ class Problem2D:
         for v in range(4):
             p.wedge_post[v] = float(self.wedge_post[v])
             p.wedge_pre[v] = float(self.wedge_pre[v])
+        p.integrator = INTEGRATORS[self.integrator]
+        p.flux = FLUXES[self.flux]
         return p
 
 

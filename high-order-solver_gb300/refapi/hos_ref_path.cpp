@@ -128,11 +128,23 @@ hos_params2d params2(const Block2d& b, int* order_out) {
         stop(HOS_E_CONFIG, "the GPU path provides the discontinuity-feedback WENO-AO variants: set is_using_df_factor = true");
     if (g0reconstruction_2D_normal != Center_do_nothing_normal || g0reconstruction_2D_tangent != Center_all_collision_multi)
         stop(HOS_E_CONFIG, "the GPU path builds the GKS centre state by Center_all_collision_multi");
-    if (flux_function_2d != GKS2D) stop(HOS_E_CONFIG, "the GPU path provides the GKS2D flux");
+    if (flux_function_2d != GKS2D && flux_function_2d != LF2D)
+        stop(HOS_E_CONFIG, "the GPU path provides the GKS2D and LF2D fluxes");
     if (tau_type != Euler) stop(HOS_E_CONFIG, "the GPU path provides the Euler collision time (tau_type = Euler)");
-    if (timecoe_list_2d != S2O4_2D) stop(HOS_E_CONFIG, "the GPU path provides S2O4_2D time marching");
-    if (b.stages != 2) stop(HOS_E_CONFIG, "S2O4 has two stages: call Initial_stages(block) after setting timecoe_list_2d");
+    int integrator = -1, stages = 0;
+    const TimeMarchingCoefficient_2d methods[6] = {S2O4_2D, S1O1_2D, S1O2_2D, RK2_2D, RK3_2D, RK4_2D};
+    const int method_stages[6] = {2, 1, 1, 2, 3, 4};
+    for (int k = 0; k < 6; ++k)
+        if (timecoe_list_2d == methods[k]) {
+            integrator = k;
+            stages = method_stages[k];
+        }
+    if (integrator < 0) stop(HOS_E_CONFIG, "the GPU path provides S2O4_2D, S1O1_2D, S1O2_2D and RK2/3/4_2D time marching");
+    if (b.stages != stages)
+        stop(HOS_E_CONFIG, "Block2d::stages does not match timecoe_list_2d: call Initial_stages(block) after setting it");
     hos_params2d p{};
+    p.integrator = integrator;
+    p.flux = flux_function_2d == LF2D ? HOS_FLUX_LF : HOS_FLUX_GKS;
     p.nodex = b.nodex;
     p.nodey = b.nodey;
     p.ghost = b.ghost;
@@ -471,11 +483,35 @@ void Update(Fluid2d* fluids, Flux2d_gauss**, Flux2d_gauss**, Block2d block, int 
 // fused: the device updates the DF indicators at the end of each stage
 void Update_alpha(Interface2d*, Interface2d*, Fluid2d* fluids, Block2d) { known2(fluids, "Update_alpha"); }
 
-void S1O1_2D(Block2d& block) { block.stages = 1; }
-void S1O2_2D(Block2d& block) { block.stages = 1; }
-void RK2_2D(Block2d& block) { block.stages = 2; }
+// the other methods' coefficient tables (src/time_advance.cpp:198-247); RK3 combines
+// states in its update and sets none
+void S1O1_2D(Block2d& block) {
+    block.stages = 1;
+    block.timecoefficient[0][0][0] = 1.0;
+    block.timecoefficient[0][0][1] = 0.0;
+}
+void S1O2_2D(Block2d& block) {
+    block.stages = 1;
+    block.timecoefficient[0][0][0] = 1.0;
+    block.timecoefficient[0][0][1] = 0.5;
+}
+void RK2_2D(Block2d& block) {
+    block.stages = 2;
+    block.timecoefficient[0][0][0] = 1.0;
+    block.timecoefficient[1][0][0] = 0.5;
+    block.timecoefficient[1][1][0] = 0.5;
+}
 void RK3_2D(Block2d& block) { block.stages = 3; }
-void RK4_2D(Block2d& block) { block.stages = 4; }
+void RK4_2D(Block2d& block) {
+    block.stages = 4;
+    block.timecoefficient[0][0][0] = 0.5;
+    block.timecoefficient[1][1][0] = 0.5;
+    block.timecoefficient[2][2][0] = 1.0;
+    block.timecoefficient[3][0][0] = 1.0 / 6.0;
+    block.timecoefficient[3][1][0] = 1.0 / 3.0;
+    block.timecoefficient[3][2][0] = 1.0 / 3.0;
+    block.timecoefficient[3][3][0] = 1.0 / 6.0;
+}
 
 // the two-stage fourth-order method: stage 1 at dt/2 with coefficients (1/2 of F, 1/8 of the
 // flux time-derivative), stage 2 combining both stages (1/6, 1/3) (src/time_advance.cpp:221-230)

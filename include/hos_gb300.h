@@ -47,6 +47,17 @@ extern "C" {
 #define HOS_BC_WEDGE_BOTTOM 4 /* bottom: post-shock state for x < x0, reflecting wall after */
 #define HOS_BC_WEDGE_TOP 5    /* top: post-shock state left of the moving shock, pre-shock right */
 
+/* time-marching methods (the reference's TimeMarchingCoefficient_2d slot values) */
+#define HOS_INT_S2O4 0      /* two-stage fourth order (default)           */
+#define HOS_INT_S1O1 1      /* one stage, first order                     */
+#define HOS_INT_S1O2 2      /* one stage, second order (flux time derivative) */
+#define HOS_INT_RK2 3       /* two-stage Runge-Kutta                      */
+#define HOS_INT_RK3 4       /* three-stage strong-stability-preserving RK */
+#define HOS_INT_RK4 5       /* classical four-stage Runge-Kutta           */
+/* interface fluxes (the reference's Flux_function_2d slot values) */
+#define HOS_FLUX_GKS 0      /* GKS2D, second order                        */
+#define HOS_FLUX_LF 1       /* LF2D, Lax-Friedrichs (Euler)               */
+
 /* compute precision of reconstruction and flux; state, stage combination and the CFL
  * reduction are FP64 in both */
 #define HOS_FP64 0
@@ -74,6 +85,10 @@ typedef struct hos_params2d {
     double wedge_top_speed;
     double wedge_post[4];
     double wedge_pre[4];
+    /* time marching (timecoe_list_2d, src/time_advance.cpp:197-247) and flux
+     * (flux_function_2d, src/flux_function.cpp:314-754); 0 / 0 = S2O4 with GKS2D */
+    int integrator;         /* HOS_INT_*  */
+    int flux;               /* HOS_FLUX_* */
 } hos_params2d;
 
 typedef struct hos_solver2d hos_solver2d;

@@ -30,9 +30,10 @@
  * the same conditions throw hos_ref_error instead.
  *
  * Provided: WENO5/7/9-AO with the discontinuity-feedback factor (WENO5-AO without it in 1D),
- * GKS2D / GKS with Euler collision time, S2O4, free / periodic / reflective / inflow boundaries.
+ * GKS2D / GKS with Euler collision time and LF2D; S2O4 (1D, 2D) and S1O1, S1O2, RK2, RK3, RK4
+ * (2D); free / periodic / reflective / inflow boundaries; the output writers.
  * Not provided (rejected at the first step): first-order and Van Leer reconstruction, GKS2D_smooth,
- * LF, LF2D, RK and S1O* integrators, no-slip walls, NS collision time, the 3D path.
+ * the 1D LF flux and 1D RK integrators, no-slip walls, NS collision time, the 3D path.
  */
 #ifndef HOS_REF_API_H
 #define HOS_REF_API_H
@@ -158,6 +159,11 @@ void Calculate_flux(Flux2d_gauss** xfluxes, Flux2d_gauss** yfluxes, Interface2d*
 void GKS2D_smooth(Flux2d& flux, Recon2d& interface, double dt);
 void GKS2D(Flux2d& flux, Recon2d& interface, double dt);
 void LF2D(Flux2d& flux, Recon2d& interface, double dt);
+
+/* ---- output writers (src/output.cpp:3-84): same file names, order and formatting ---- */
+void output1d(Fluid1d* fluids, Block1d block);
+void output2d(Fluid2d* fluids, Block2d block);
+void output_error_form(double CFL, double dt_ratio, int mesh_set, int* mesh_number, double** error);
 
 /* ---- boundary conditions (src/boundary_condition.cpp) ---- */
 void free_boundary_left(Fluid1d* fluids, Block1d block, Fluid1d bcvalue);

@@ -54,6 +54,8 @@ struct Config {
     double gw[4] = {0, 0, 0, 0};
     double K = 0, Gamma = 0;
     double tbeg = 0;   // Block2d::t during the step (read by the wedge boundary)
+    int stages = 2;
+    double tc[5][5][2] = {};   // Block2d::timecoefficient of the time-marching method
 };
 Config C;
 
@@ -63,14 +65,44 @@ struct Recon { Point left, right, center; };
 std::vector<double> W, Wold, Prim, AX, AY;   // per cell: 4, 4, 4, 1, 1
 std::vector<Point> XL, YL;                    // line states: [face][side] (side 0 left, 1 right)
 std::vector<Recon> XG, YG;                    // Gauss states: [face][gp]
-std::vector<double> XF, YF;                   // flux: [face][stage][gp][8] (f[4], derf[4])
+std::vector<double> XF, YF;                   // flux: [face][stage (4)][gp][8] (f[4], derf[4])
 std::vector<double> XX, YX;                   // stage flux combination x[4]: [face][gp][4]
 
 inline int cell(int i, int j) { return i * C.ny + j; }
 inline int face(int i, int j) { return i * (C.ny + 1) + j; }
 
-// S2O4 coefficients (src/time_advance.cpp:221-230): tc[stage][k][f or derf]
-const double TC[2][2][2] = {{{0.5, 1.0 / 8.0}, {0.0, 0.0}}, {{1.0, 1.0 / 6.0}, {0.0, 1.0 / 3.0}}};
+// time-marching coefficients tc[stage][k][f or derf] (S1O1_2D ... RK4_2D,
+// src/time_advance.cpp:197-247); RK3 has its own state combination (:476-532)
+void set_integrator(int integrator) {
+    for (auto& a : C.tc)
+        for (auto& b : a) b[0] = b[1] = 0.0;
+    switch (integrator) {
+        case 0:  // S2O4
+            C.stages = 2;
+            C.tc[0][0][0] = 0.5; C.tc[0][0][1] = 1.0 / 8.0;
+            C.tc[1][0][0] = 1.0; C.tc[1][1][0] = 0.0; C.tc[1][0][1] = 1.0 / 6.0; C.tc[1][1][1] = 1.0 / 3.0;
+            break;
+        case 1:  // S1O1
+            C.stages = 1;
+            C.tc[0][0][0] = 1.0; C.tc[0][0][1] = 0.0;
+            break;
+        case 2:  // S1O2
+            C.stages = 1;
+            C.tc[0][0][0] = 1.0; C.tc[0][0][1] = 0.5;
+            break;
+        case 3:  // RK2
+            C.stages = 2;
+            C.tc[0][0][0] = 1.0; C.tc[1][0][0] = 0.5; C.tc[1][1][0] = 0.5;
+            break;
+        case 4:  // RK3
+            C.stages = 3;
+            break;
+        default:  // RK4
+            C.stages = 4;
+            C.tc[0][0][0] = 0.5; C.tc[1][1][0] = 0.5; C.tc[2][2][0] = 1.0;
+            C.tc[3][0][0] = 1.0 / 6.0; C.tc[3][1][0] = 1.0 / 3.0; C.tc[3][2][0] = 1.0 / 3.0; C.tc[3][3][0] = 1.0 / 6.0;
+    }
+}
 
 // ----------------------------------------------------------------------------------------
 // conversions (src/basic_function.cpp:811-842, 1102-1177)
@@ -352,7 +384,7 @@ double tau_num(double dl, double dr, double ll, double lr, double dt) {
 // centre state by collision (also stored in re.center), the full second-order flux over
 // [0, dt] and [0, dt/2], combined into f = 4F(dt/2) - F(dt), derf = 4(F(dt) - 2F(dt/2)).
 // ----------------------------------------------------------------------------------------
-void gks2d(Recon& re, double dt, double* fo, double* dfo) {
+void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
     double pl[4], pr[4], p0[4];
     to_ulambda(pl, re.left.convar);
     to_ulambda(pr, re.right.convar);
@@ -442,6 +474,13 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo) {
     microslope(A0, dA0, p0);
     contract(m0.uv, 1, 0, A0, A0u);
     for (int i = 0; i < 4; ++i) F0[i] = F0[i] + p0[0] * t[5] * (A0u[i]);
+    if (one_level) {   // S1O1 takes the dt integral alone (:637-645)
+        for (int i = 0; i < 4; ++i) {
+            fo[i] = F0[i];
+            dfo[i] = 0.0;
+        }
+        return;
+    }
     // second time level dt/2 (:647-676)
     double dt2 = 0.5 * dt;
     tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt2);
@@ -463,6 +502,31 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo) {
     for (int i = 0; i < 4; ++i) {
         fo[i] = (4.0 * F1[i] - F0[i]);
         dfo[i] = 4.0 * (F0[i] - 2.0 * F1[i]);
+    }
+}
+
+// Lax-Friedrichs flux times dt at a Gauss point (LF2D, src/flux_function.cpp:700-735)
+void lf2d(const Recon& re, double dt, double* fo, double* dfo) {
+    double pl[4], pr[4];
+    to_prim(pl, re.left.convar);
+    to_prim(pr, re.right.convar);
+    const double kl = std::abs(pl[1]) + std::sqrt(C.Gamma * pl[3] / pl[0]);
+    const double kr = std::abs(pr[1]) + std::sqrt(C.Gamma * pr[3] / pr[0]);
+    const double beta = kr > kl ? kr : kl;
+    auto flux = [](const double* q, double* f) {
+        f[0] = q[0] * q[1];
+        f[1] = q[0] * q[1] * q[1] + q[3];
+        f[2] = q[0] * q[1] * q[2];
+        const double e = 0.5 * (q[1] * q[1] + q[2] * q[2]) * q[0] + q[3] / (C.Gamma - 1.0);
+        f[3] = q[1] * (e + q[3]);
+    };
+    double fl[4], fr[4];
+    flux(pl, fl);
+    flux(pr, fr);
+    for (int m = 0; m < 4; ++m) {
+        fo[m] = 0.5 * ((fl[m] + fr[m]) - beta * (re.right.convar[m] - re.left.convar[m]));
+        fo[m] *= dt;
+        dfo[m] = 0.0;
     }
 }
 
@@ -669,8 +733,10 @@ int oracle2d_init(const hos2d_params* p) {
     std::memset(&zr, 0, sizeof zr);
     XG.assign(nf * C.gp, zr);
     YG.assign(nf * C.gp, zr);
-    XF.assign(nf * 2 * C.gp * 8, 0.0);
-    YF.assign(nf * 2 * C.gp * 8, 0.0);
+    XF.assign(nf * 4 * C.gp * 8, 0.0);
+    YF.assign(nf * 4 * C.gp * 8, 0.0);
+    if (p->integrator < 0 || p->integrator > 5 || p->flux < 0 || p->flux > 1) return 2;
+    set_integrator(p->integrator);
     XX.assign(nf * C.gp * 4, 0.0);
     YX.assign(nf * C.gp * 4, 0.0);
     return 0;
@@ -793,16 +859,18 @@ int oracle2d_stage(int stage, double dt) {
         for (int j = g; j < g + C.p.nodey; ++j)
             for (int ig = 0; ig < gp; ++ig) {
                 const size_t f = face(i, j);
-                double* o = &XF[((f * 2 + stage) * gp + ig) * 8];
-                gks2d(XG[f * gp + ig], dt, o, o + 4);
+                double* o = &XF[((f * 4 + stage) * gp + ig) * 8];
+                if (C.p.flux == 1) lf2d(XG[f * gp + ig], dt, o, o + 4);
+                else gks2d(XG[f * gp + ig], dt, o, o + 4, C.p.integrator == 1);
             }
 #pragma omp parallel for
     for (int i = g; i < g + C.p.nodex; ++i)
         for (int j = g; j < g + C.p.nodey + 1; ++j)
             for (int ig = 0; ig < gp; ++ig) {
                 const size_t f = face(i, j);
-                double* o = &YF[((f * 2 + stage) * gp + ig) * 8];
-                gks2d(YG[f * gp + ig], dt, o, o + 4);
+                double* o = &YF[((f * 4 + stage) * gp + ig) * 8];
+                if (C.p.flux == 1) lf2d(YG[f * gp + ig], dt, o, o + 4);
+                else gks2d(YG[f * gp + ig], dt, o, o + 4, C.p.integrator == 1);
             }
     // stage combination per face and Gauss point (Update, src/time_advance.cpp:378-428)
     auto combine = [&](std::vector<double>& F, std::vector<double>& X, int i0, int i1, int j0, int j1) {
@@ -813,9 +881,14 @@ int oracle2d_stage(int stage, double dt) {
                     for (int v = 0; v < 4; ++v) {
                         const size_t f = face(i, j);
                         double fl = 0.0;
-                        for (int k = 0; k < stage + 1; ++k) {
-                            const double* q = &F[((f * 2 + k) * gp + ig) * 8];
-                            fl = fl + C.gw[ig] * (TC[stage][k][0] * q[v] + TC[stage][k][1] * q[4 + v]);
+                        if (C.p.integrator == 4) {   // RK3 (:317-372)
+                            const double q = F[((f * 4 + stage) * gp + ig) * 8 + v];
+                            fl = stage == 0 ? C.gw[ig] * q : stage == 1 ? 0.25 * C.gw[ig] * q : 2.0 / 3.0 * C.gw[ig] * q;
+                        } else {
+                            for (int k = 0; k < stage + 1; ++k) {
+                                const double* q = &F[((f * 4 + k) * gp + ig) * 8];
+                                fl = fl + C.gw[ig] * (C.tc[stage][k][0] * q[v] + C.tc[stage][k][1] * q[4 + v]);
+                            }
                         }
                         X[(f * gp + ig) * 4 + v] = fl;
                     }
@@ -831,6 +904,7 @@ int oracle2d_stage(int stage, double dt) {
             const int c = cell(i, j);
             const size_t f = face(i, j);
             for (int v = 0; v < 4; ++v) {
+                const double cur = W[4 * c + v];   // the RK3 stage state (convar_stage1 / _stage2)
                 W[4 * c + v] = Wold[4 * c + v];
                 double total = 0.0;
                 for (int ig = 0; ig < gp; ++ig) {
@@ -847,7 +921,12 @@ int oracle2d_stage(int stage, double dt) {
                     total += C.dy * xv(f);
                     total += -C.dy * xv(f + ny + 1);
                 }
-                W[4 * c + v] += total / area;
+                if (C.p.integrator == 4 && stage == 1)
+                    W[4 * c + v] = 0.75 * Wold[4 * c + v] + 0.25 * cur + total / area;
+                else if (C.p.integrator == 4 && stage == 2)
+                    W[4 * c + v] = 1.0 / 3.0 * Wold[4 * c + v] + 2.0 / 3.0 * cur + total / area;
+                else
+                    W[4 * c + v] += total / area;
             }
         }
     // DF factor update (Update_alpha, :1523-1534)
@@ -869,7 +948,7 @@ int oracle2d_stage(int stage, double dt) {
 int oracle2d_step(double tstop, double t, double* dt_out) {
     double dt = oracle2d_begin_step(tstop, t);
     if (dt_out) *dt_out = dt;
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < C.stages; ++s) {
         int st = oracle2d_stage(s, dt);
         if (st) return st;
     }
@@ -898,7 +977,7 @@ void oracle2d_get_flux(int dir, int stage, double* out) {
     const size_t nf = static_cast<size_t>(C.nx + 1) * (C.ny + 1);
     for (size_t f = 0; f < nf; ++f)
         for (int ig = 0; ig < C.gp; ++ig)
-            for (int k = 0; k < 8; ++k) out[(f * C.gp + ig) * 8 + k] = F[((f * 2 + stage) * C.gp + ig) * 8 + k];
+            for (int k = 0; k < 8; ++k) out[(f * C.gp + ig) * 8 + k] = F[((f * 4 + stage) * C.gp + ig) * 8 + k];
 }
 
 // Gate features ([ncell][2][16]) and label distances ([ncell][2]; -1 where the stencil leaves

@@ -42,6 +42,8 @@ typedef struct hos2d_params {
     double bc_prim[4][4]; /* inflow primitive state per side (rho,u,v,p)     */
     /* wedge (double-Mach) boundaries, kinds 4 (bottom) and 5 (top) */
     double wedge_x0, wedge_top_speed, wedge_post[4], wedge_pre[4];
+    /* time marching: 0 S2O4, 1 S1O1, 2 S1O2, 3 RK2, 4 RK3, 5 RK4; flux: 0 GKS2D, 1 LF2D */
+    int integrator, flux;
 } hos2d_params;
 
 /* ---- restatement (liboracle.so) ---- */

@@ -93,8 +93,16 @@ int ref2d_init(const hos2d_params* p) {
     c1_euler = p->c1_euler;
     c2_euler = p->c2_euler;
     is_Prandtl_fix = false;
-    flux_function_2d = GKS2D;
-    timecoe_list_2d = S2O4_2D;
+    flux_function_2d = p->flux == 1 ? LF2D : GKS2D;
+    switch (p->integrator) {
+        case 0: timecoe_list_2d = S2O4_2D; break;
+        case 1: timecoe_list_2d = S1O1_2D; break;
+        case 2: timecoe_list_2d = S1O2_2D; break;
+        case 3: timecoe_list_2d = RK2_2D; break;
+        case 4: timecoe_list_2d = RK3_2D; break;
+        case 5: timecoe_list_2d = RK4_2D; break;
+        default: return 2;
+    }
     Initial_stages(block);
     block.nx = block.nodex + 2 * block.ghost;
     block.ny = block.nodey + 2 * block.ghost;

@@ -39,6 +39,10 @@ def step_cases():
     yield "rriemann_w7_s11_20", cases.random_riemann2d(20, seed=11, order=7)
     yield "vortex_w5_char_20", cases.isentropic_vortex(20, order=5)
     yield "sinwave_w9_cons_16", cases.sinwave2d(16, order=9)
+    from test_oracle_cpu import _problem
+    for name in ("tmarch_s1o1_gks_w5_24", "tmarch_s1o2_gks_w5_24", "tmarch_rk2_gks_w7_24",
+                 "tmarch_rk3_lf_w5_24", "tmarch_rk4_gks_w9_24", "tmarch_s2o4_lf_w7_24"):
+        yield name, _problem(name)
 
 
 def sinwave_errors(n, tstop=2.0):
@@ -108,8 +112,10 @@ def refapi():
     print("refapi_sod1d_1000", r["steps"], r["t"])
 
 
-def main():
+def main(only=None):
     for name, (pb, con, prim) in step_cases():
+        if only and not name.startswith(only):
+            continue
         r = CpuStep("ref").init(pb)
         r.set_state(con, prim)
         dts = [r.step()]
@@ -121,6 +127,8 @@ def main():
                             convar3=s3["convar"], alpha_x3=s3["alpha_x"], alpha_y3=s3["alpha_y"],
                             dts=np.array(dts))
         print(name, dts)
+    if only:
+        return
     errs = {f"n{n}": sinwave_errors(n) for n in (10, 20)}
     np.savez_compressed(OUT / "sinwave_w9_accuracy.npz", **errs)
     print(errs)
@@ -129,4 +137,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

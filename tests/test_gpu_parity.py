@@ -246,3 +246,15 @@ def test_gpu_shock_vortex_vs_oracle():
     ref = oracle_run(pb, con, prim, 3)
     got = gpu_run(pb, con, prim, 3)
     assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+
+
+@pytest.mark.parametrize("integrator", ["S1O1", "S1O2", "RK2", "RK3", "RK4"])
+@pytest.mark.parametrize("flux", ["GKS", "LF"])
+def test_gpu_time_marching_and_flux_vs_oracle(integrator, flux):
+    """The reference's other TimeMarchingCoefficient_2d and Flux_function_2d slot values."""
+    pb, con, prim = cases.random_riemann2d(40, seed=5, order=7)
+    pb.integrator, pb.flux = integrator, flux
+    got = gpu_run(pb, con, prim, 4)
+    ref = oracle_run(pb, con, prim, 4)
+    assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
+    np.testing.assert_allclose(got["dts"], ref["dts"], rtol=1e-14, atol=0)

@@ -24,6 +24,13 @@ def _problem(name):
         return cases.isentropic_vortex(n, order=5)
     if name.startswith("sinwave"):
         return cases.sinwave2d(n, order=9)
+    if name.startswith("tmarch"):
+        # tmarch_<integrator>_<flux>_w<order>_<n>: the quadrant problem with another time
+        # marching / flux choice
+        _, integ, flux, w, _ = name.split("_")
+        pb, con, prim = cases.riemann2d(n, order=int(w[1]))
+        pb.integrator, pb.flux = integ.upper(), flux.upper()
+        return pb, con, prim
     raise KeyError(name)
 
 

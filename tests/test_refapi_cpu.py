@@ -116,3 +116,21 @@ def test_refapi_sod_fixture_equals_the_oracle():
     o.run(0.2)
     st = o.state()
     assert np.array_equal(st["convar"], gold["convar"])
+
+
+@pytest.mark.skipif(not REF_INCLUDE.exists(), reason="reference checkout absent")
+def test_output_writers_are_byte_identical_to_the_reference(tmp_path):
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "refdrivers"], check=True, capture_output=True)
+    _lib_built()
+    ours = tmp_path / "outputs_ours"
+    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{ROOT / 'include'}", str(ROOT / "tests" / "refapi" / "outputs.cpp"),
+                    "-o", str(ours), f"-L{PKG}", "-lhos_ref", "-lhos_gb300", f"-Wl,-rpath,{PKG}"], check=True)
+    outs = {}
+    for name, exe in (("ref", ROOT / "oracle" / "_ref" / "outputs"), ("ours", ours)):
+        run = tmp_path / name / "run"
+        (tmp_path / name / "data").mkdir(parents=True)
+        run.mkdir()
+        subprocess.run([str(exe)], cwd=run, check=True, capture_output=True)
+        outs[name] = {p.name: p.read_bytes() for p in (tmp_path / name / "data").iterdir()}
+    assert set(outs["ref"]) == {"R.txt", "R-42.txt", "error.txt"}
+    assert outs["ours"] == outs["ref"]
