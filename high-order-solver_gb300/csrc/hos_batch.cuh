@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_bat
         const TileRef tr = tiles[k];
         const Prob* pr = probs + tr.p;
         const Geometry geo = pr->geo;
-        FaceArgs a;
+        FaceArgs a{};   // members not set below (FP32 mirrors, per-stage buffers) stay null
         a.W = pr->W;
         a.AN = DIR == 0 ? pr->AX : pr->AY;
         a.AT = DIR == 0 ? pr->AY : pr->AX;

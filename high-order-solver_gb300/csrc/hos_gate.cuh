@@ -241,6 +241,7 @@ struct GateArgs {
     unsigned long long capacity;
     unsigned sample_mask;      // collect cells whose hash & mask == 0
     const StepCtl* ctl;        // inactive problems skip (may be null)
+    const float* W32 = nullptr;   // FP32 mirror of W (FP32 solvers; null: convert W)
 };
 
 constexpr int GATE_THREADS = 256;
@@ -270,7 +271,12 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, con
         float rho = 0.0f, pr = 0.0f;
         if (gi >= 0 && gi < geo.nx && gj >= 0 && gj < geo.ny) {
             const size_t q = (size_t)gi * geo.ny + gj;
-            float w[4] = {float(a.W[q]), float(a.W[plane + q]), float(a.W[2 * plane + q]), float(a.W[3 * plane + q])};
+            float w[4];
+            if (a.W32) {
+                w[0] = a.W32[q]; w[1] = a.W32[plane + q]; w[2] = a.W32[2 * plane + q]; w[3] = a.W32[3 * plane + q];
+            } else {
+                w[0] = float(a.W[q]); w[1] = float(a.W[plane + q]); w[2] = float(a.W[2 * plane + q]); w[3] = float(a.W[3 * plane + q]);
+            }
             float pv[4];
             to_prim(pv, w, gamma);
             rho = pv[0];

@@ -101,10 +101,13 @@ struct UpdateArgs {
     const double* FAy;
     StepCtl* ctl;
     int stage;
+    float* W32;   // FP32 solvers: mirror of W and of alpha_x | alpha_y (may be null)
+    float* A32;
 };
 
 // step kernels defined in hos_solver.cu
-__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl, int skip_inactive);
+__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl, int skip_inactive,
+                               float* W32 = nullptr);
 __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo);
 
 // ------------------------------------------------------------------------------------------
@@ -127,6 +130,11 @@ struct FaceArgs {
     // every earlier stage [stage][4][nf]
     double* FS;
     double* DS;
+    // FP32 solvers: FP32 mirrors of the state and of the DF indicators, read by the FP32 tiles
+    // instead of converting the FP64 arrays (null: convert)
+    const float* W32;
+    const float* AN32;
+    const float* AT32;
 };
 
 // A tile is TN faces along the normal by TT along the tangent, handled by one CTA of
@@ -247,13 +255,27 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             const int n = g + N0 - 1 - r + nn, t = g + T0 - r + tl;
             if (n >= nmax || t >= tmax) continue;
             const size_t ci = cidx(n, t);
-            T w0 = T(a.W[ci]), w1 = T(a.W[plane + ci]), w2 = T(a.W[2 * plane + ci]), w3 = T(a.W[3 * plane + ci]);
+            T w0, w1, w2, w3, an, at;
+            bool mirrored = false;
+            if constexpr (sizeof(T) == 4) {
+                if (a.W32) {
+                    w0 = a.W32[ci]; w1 = a.W32[plane + ci]; w2 = a.W32[2 * plane + ci]; w3 = a.W32[3 * plane + ci];
+                    an = a.AN32[ci];
+                    at = a.AT32[ci];
+                    mirrored = true;
+                }
+            }
+            if (!mirrored) {
+                w0 = T(a.W[ci]); w1 = T(a.W[plane + ci]); w2 = T(a.W[2 * plane + ci]); w3 = T(a.W[3 * plane + ci]);
+                an = T(a.AN[ci]);
+                at = T(a.AT[ci]);
+            }
             T* d = wtile + (nn * TL + tl) * 4;
             if (DIR == 0) { d[0] = w0; d[1] = w1; d[2] = w2; d[3] = w3; }
             else { d[0] = w0; d[1] = w2; d[2] = -w1; d[3] = w3; }
-            antile[nn * TL + tl] = T(a.AN[ci]);
+            antile[nn * TL + tl] = an;
             if (nn >= r && nn <= r + TILE_N) {
-                attile[(nn - r) * TL + tl] = T(a.AT[ci]);
+                attile[(nn - r) * TL + tl] = at;
                 if constexpr (GATED) gfl[(nn - r) * TL + tl] = a.gate[ci];
             }
         }

@@ -15,9 +15,22 @@ namespace hos {
 
 // ghost fill; inside a step (skip_inactive) a finished problem does nothing.  ctl supplies the
 // step's start time for the time-dependent wedge boundary.
-__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl, int skip_inactive) {
+__global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, const StepCtl* ctl, int skip_inactive,
+                               float* W32) {
     if (skip_inactive && !ctl->active) return;
-    bc_fill_one(W, geo, bc, ctl, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+    bc_fill_one(W, geo, bc, ctl, blockIdx.x * (long long)blockDim.x + threadIdx.x, W32);
+}
+
+// FP32 mirrors of the whole state and of the DF indicators (after an upload)
+__global__ void mirror_state_kernel(const double* __restrict__ W, const double* __restrict__ AX,
+                                    const double* __restrict__ AY, float* __restrict__ W32, float* __restrict__ A32,
+                                    size_t n) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) W32[v * n + c] = (float)W[v * n + c];
+        A32[c] = (float)AX[c];
+        A32[n + c] = (float)AY[c];
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -146,6 +159,8 @@ struct hos_solver2d {
     double* FPy = nullptr;
     double* FAy = nullptr;
     double* scratch = nullptr;  // 8 * ncell doubles: AoS staging + primitive planes
+    float* W32 = nullptr;       // FP32 solvers: mirror of W [4][nx*ny] ...
+    float* A32 = nullptr;       // ... and of alpha_x | alpha_y [2][nx*ny]
     double* stagex = nullptr;   // methods other than S2O4: per-stage F and D of x faces [2][4][4][nfx]
     double* stagey = nullptr;   // ... and of y faces
     StepCtl* ctl = nullptr;
@@ -200,7 +215,7 @@ void free_all(hos_solver2d* s) {
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->ctl) cudaFree(s->ctl);
-    void* gbufs[] = {s->gflags, s->gstats, s->gw, s->gb};
+    void* gbufs[] = {s->gflags, s->gstats, s->gw, s->gb, s->W32, s->A32};
     for (void* b : gbufs)
         if (b) cudaFree(b);
     if (s->graph) cudaGraphExecDestroy(s->graph);
@@ -217,12 +232,17 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     };
     {
         const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
-        bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 1);
+        bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 1, s->W32);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "bc_fill");
         mark(0);
     }
     FaceArgs ax{s->W, s->AX, s->AY, s->FXx, s->FPx, s->FAx, s->ctl, stage};
     FaceArgs ay{s->W, s->AY, s->AX, s->FXy, s->FPy, s->FAy, s->ctl, stage};
+    if (s->W32) {
+        ax.W32 = ay.W32 = s->W32;
+        ax.AN32 = ay.AT32 = s->A32;
+        ax.AT32 = ay.AN32 = s->A32 + s->ncell;
+    }
     if (s->stagex) {
         ax.FS = s->stagex;
         ax.DS = s->stagex + 16 * s->nfx;
@@ -232,7 +252,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     if (s->gated) {
         // per-cell smoothness flags of this stage's state (ghosts filled) for both directions
         gate::GateArgs ga{s->W, s->AX, s->AY, s->gflags, s->gstats, s->gthreshold, s->gaudit_mask, s->gseed++,
-                          nullptr, 0, 0xffffffffu, s->ctl};
+                          nullptr, 0, 0xffffffffu, s->ctl, s->W32};
         if ((e = gate::launch_gate(s->p.order, ga, s->gnet(), geo, s->stream)) != cudaSuccess) return cuda_fail(e, "gate");
         ax.gate = ay.gate = s->gflags;
         ax.fallback = ay.fallback = &s->gstats->fallback;
@@ -246,7 +266,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
         default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
-    UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage};
+    UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage, s->W32, s->A32};
     const int n = geo.nodex * geo.nodey;
     update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "update");
@@ -268,6 +288,13 @@ int enqueue_step(hos_solver2d* s, double tstop) {
     return HOS_OK;
 }
 
+cudaError_t refresh_mirror(hos_solver2d* s) {
+    if (!s->W32) return cudaSuccess;
+    mirror_state_kernel<<<(unsigned)std::min<size_t>((s->ncell + 255) / 256, 4096), 256, 0, s->stream>>>(
+        s->W, s->AX, s->AY, s->W32, s->A32, s->ncell);
+    return cudaGetLastError();
+}
+
 int reset_ctl_and_cfl(hos_solver2d* s, const double* dprim_soa) {
     StepCtl c{};
     c.dt = 0.0;
@@ -283,6 +310,7 @@ int reset_ctl_and_cfl(hos_solver2d* s, const double* dprim_soa) {
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cfl_from_prim");
     if ((e = cudaMemsetAsync(s->AX, 0, s->ncell * sizeof(double), s->stream)) != cudaSuccess) return cuda_fail(e, "memset");
     if ((e = cudaMemsetAsync(s->AY, 0, s->ncell * sizeof(double), s->stream)) != cudaSuccess) return cuda_fail(e, "memset");
+    if ((e = refresh_mirror(s)) != cudaSuccess) return cuda_fail(e, "mirror");
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "set_state");
     StepCtl back;
     if ((e = cudaMemcpy(&back, s->ctl, sizeof back, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "ctl read");
@@ -359,6 +387,16 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
         delete s;
         return fail(HOS_E_NOMEM, "cudaMalloc ctl");
     }
+    if (precision == HOS_FP32) {
+        if ((e = cudaMalloc(&s->W32, 4 * s->ncell * sizeof(float))) != cudaSuccess ||
+            (e = cudaMalloc(&s->A32, 2 * s->ncell * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemset(s->W32, 0, 4 * s->ncell * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemset(s->A32, 0, 2 * s->ncell * sizeof(float))) != cudaSuccess) {
+            free_all(s);
+            delete s;
+            return fail(HOS_E_NOMEM, "cudaMalloc FP32 mirror");
+        }
+    }
     cudaMemset(s->ctl, 0, sizeof(StepCtl));
     switch (p.order) {
         case 5: e = configure_faces5(precision); break;
@@ -429,6 +467,7 @@ int hos2d_set_alpha(hos_solver2d* s, const double* alpha_x, const double* alpha_
     if (!s || !alpha_x || !alpha_y) return fail(HOS_E_ARG, "null argument");
     cudaError_t e = cudaMemcpyAsync(s->AX, alpha_x, s->ncell * sizeof(double), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->AY, alpha_y, s->ncell * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = refresh_mirror(s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     return e == cudaSuccess ? HOS_OK : cuda_fail(e, "set_alpha");
 }
@@ -553,7 +592,7 @@ int hos_gate_collect(hos_gate* g, hos_solver2d* s, int sample_log2) {
     if (!g->samples) return fail(HOS_E_CONFIG, "the gate was created without sample capacity");
     const Geometry& geo = s->geo;
     const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
-    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 0);
+    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 0, s->W32);
     GateArgs ga{s->W, s->AX, s->AY, nullptr, g->stats, 0.0f, 0xffffffffu, g->collect_seed++, g->samples, g->capacity,
                 sample_log2 == 31 ? 0xffffffffu : (1u << sample_log2) - 1u, nullptr};
     cudaError_t e = cudaStreamSynchronize(g->stream);   // the network's copy is current
@@ -571,7 +610,7 @@ int hos2d_boundary(hos_solver2d* s) {
     if (!s) return fail(HOS_E_ARG, "null solver");
     const Geometry& geo = s->geo;
     const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
-    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 0);
+    bc_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->W, geo, s->bc, s->ctl, 0, s->W32);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? HOS_OK : cuda_fail(e, "bc_fill");
 }

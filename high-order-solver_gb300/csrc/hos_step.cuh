@@ -8,7 +8,7 @@ namespace hos {
 
 // ghost cell number e of the block (left/right strips first, then bottom/top strips)
 __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geometry& geo, const BcSpec& bc,
-                                            const StepCtl* ctl, long long e) {
+                                            const StepCtl* ctl, long long e, float* __restrict__ W32 = nullptr) {
     const int nx = geo.nx, ny = geo.ny, g = geo.g;
     const long long nlr = 2LL * g * ny, ndu = 2LL * g * geo.nodex;
     if (e >= nlr + ndu) return;
@@ -24,6 +24,11 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
         j = jl < g ? jl : ny - 2 * g + jl;
     }
     const size_t plane = (size_t)nx * ny;
+    // the FP32 mirror of the state (FP32 solvers) takes the same ghost values, rounded
+    auto put = [&](int v, double x) {
+        W[v * plane + (size_t)i * ny + j] = x;
+        if (W32) W32[v * plane + (size_t)i * ny + j] = (float)x;
+    };
     double out[4];
     int si = i, sj = j;
     bool flipu = false, flipv = false;
@@ -33,7 +38,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
         const int side = j < g ? 2 : 3;
         const int kind = bc.kind[side];
         if (kind == 3) {
-            for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = bc.inflow[side][v];
+            for (int v = 0; v < 4; ++v) put(v, bc.inflow[side][v]);
             return;
         }
         if (kind >= 4) {
@@ -49,7 +54,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
                     st = bc.wpost;
                 }
                 if (st) {
-                    for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = st[v];
+                    for (int v = 0; v < 4; ++v) put(v, st[v]);
                     return;
                 }
                 sj = 2 * g - 1 - j;  // reflecting wall
@@ -66,7 +71,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
         if (kind == 3) {
             for (int v = 0; v < 4; ++v) out[v] = bc.inflow[side][v];
             if (flipv) out[2] = -out[2];
-            for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = out[v];
+            for (int v = 0; v < 4; ++v) put(v, out[v]);
             return;
         }
         si = bc_map(i, nx, g, geo.nodex, kind, side == 0);
@@ -76,7 +81,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
     for (int v = 0; v < 4; ++v) out[v] = W[v * plane + src];
     if (flipu) out[1] = -out[1];
     if (flipv) out[2] = -out[2];
-    for (int v = 0; v < 4; ++v) W[v * plane + (size_t)i * ny + j] = out[v];
+    for (int v = 0; v < 4; ++v) put(v, out[v]);
 }
 
 
@@ -106,8 +111,11 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         double w[4], w0[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
+            // the state the stage started from: needed at stage 0 (snapshot, and the CFL of
+            // one-stage methods) and by RK3's state combination
+            const bool need_cur = a.stage == 0 || geo.integrator == 4;
+            const double cur = need_cur ? a.W[v * plane + c] : 0.0;
             double old;
-            const double cur = a.W[v * plane + c];   // the state the stage started from
             if (a.stage == 0) {
                 old = cur;
                 a.Wold[v * plane + c] = old;
@@ -127,11 +135,17 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             else
                 w[v] = old + total * iarea;
             a.W[v * plane + c] = w[v];
+            if (a.W32) a.W32[v * plane + c] = (float)w[v];
         }
         const int jend = nodex < nodey ? nodex : nodey;
         if (J < jend) {
-            a.AX[c] = a.FAx[fl] + a.FAx[fr];
-            a.AY[c] = a.FAy[fd] + a.FAy[fu];
+            const double ax = a.FAx[fl] + a.FAx[fr], ay = a.FAy[fd] + a.FAy[fu];
+            a.AX[c] = ax;
+            a.AY[c] = ay;
+            if (a.A32) {
+                a.A32[c] = (float)ax;
+                a.A32[plane + c] = (float)ay;
+            }
         }
         const double ir = 1.0 / w[0];
         double pr[4];
