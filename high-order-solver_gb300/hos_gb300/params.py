@@ -171,3 +171,78 @@ class Problem1D:
             b = self.bc[s]
             p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
         return p
+
+
+class Params3D(ctypes.Structure):
+    """ctypes mirror of hos_params3d (include/hos_gb300.h): the knobs of the reference's 3D
+    driver (CubicTube, src/3Dproblem.cpp:3-66) plus the viscosity of the Navier-Stokes
+    collision time (Get_Tau_NS, src/basic_function.cpp:638-661) and periodic sides."""
+
+    _fields_ = [
+        ("nodex", ctypes.c_int), ("nodey", ctypes.c_int), ("nodez", ctypes.c_int), ("ghost", ctypes.c_int),
+        ("characteristic", ctypes.c_int), ("K", ctypes.c_int),
+        ("gamma", ctypes.c_double), ("c1_euler", ctypes.c_double), ("c2_euler", ctypes.c_double),
+        ("cfl", ctypes.c_double), ("tau_type", ctypes.c_int), ("mu", ctypes.c_double),
+        ("left", ctypes.c_double), ("right", ctypes.c_double), ("down", ctypes.c_double),
+        ("up", ctypes.c_double), ("back", ctypes.c_double), ("front", ctypes.c_double),
+        ("bc", ctypes.c_int * 6),
+    ]
+
+
+TAU_EULER, TAU_NS = 0, 1
+
+
+@dataclass
+class Problem3D:
+    """A 3D problem: WENO5-AO (non-DF) on 2x2 Gauss points per face, GKS3D, S2O4."""
+
+    nodex: int
+    nodey: int
+    nodez: int
+    characteristic: bool = True
+    ghost: int = 3
+    K: int = 2
+    gamma: float = 1.4
+    c1_euler: float = 0.05
+    c2_euler: float = 1.0
+    cfl: float = 0.5
+    tau_type: int = TAU_EULER
+    mu: float = 0.0
+    left: float = 0.0
+    right: float = 1.0
+    down: float = 0.0
+    up: float = 1.0
+    back: float = 0.0
+    front: float = 1.0
+    bc: tuple = ("free",) * 6
+
+    @property
+    def shape(self) -> tuple:
+        g = 2 * self.ghost
+        return (self.nodex + g, self.nodey + g, self.nodez + g)
+
+    @property
+    def dx(self) -> float:
+        return (self.right - self.left) / self.nodex
+
+    @property
+    def dy(self) -> float:
+        return (self.up - self.down) / self.nodey
+
+    @property
+    def dz(self) -> float:
+        return (self.front - self.back) / self.nodez
+
+    def to_c(self) -> Params3D:
+        p = Params3D()
+        p.nodex, p.nodey, p.nodez, p.ghost = self.nodex, self.nodey, self.nodez, self.ghost
+        p.characteristic = 1 if self.characteristic else 0
+        p.K = self.K
+        p.gamma, p.c1_euler, p.c2_euler, p.cfl = self.gamma, self.c1_euler, self.c2_euler, self.cfl
+        p.tau_type, p.mu = int(self.tau_type), float(self.mu)
+        p.left, p.right, p.down, p.up, p.back, p.front = (self.left, self.right, self.down, self.up,
+                                                          self.back, self.front)
+        for s in range(6):
+            b = self.bc[s]
+            p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
+        return p

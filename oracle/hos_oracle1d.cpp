@@ -86,55 +86,6 @@ inline bool needs_reduce(const double* w) {
     return lam <= 0.0 || !(lam == lam);
 }
 
-// non-DF WENO5-AO (wenoz, epsilon 1e-10, full 5th-order indicator), :161-360
-void weno5_plain(int side, const double* s, double h, double& var, double& der) {
-    const double dhi = 0.85, dlo = 0.85, eps = 1e-10;
-    const double wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
-    double d[4] = {(1.0 - dhi) * (1.0 - dlo) / 2.0, (1.0 - dhi) * dlo, (1.0 - dhi) * (1.0 - dlo) / 2.0, dhi};
-    double beta[4];
-    beta3(s, 2, beta);
-    beta[3] = (1.0 / 5040.0) * (231153.0 * w0 * w0 + 104963.0 * wn1 * wn1 + 6908.0 * wn2 * wn2 -
-                                38947.0 * wn2 * wp1 + 104963.0 * wp1 * wp1 +
-                                wn1 * (-51001.0 * wn2 + 179098.0 * wp1 - 38947.0 * wp2) -
-                                3.0 * w0 * (99692.0 * wn1 - 22641.0 * wn2 + 99692.0 * wp1 - 22641.0 * wp2) +
-                                8209.0 * wn2 * wp2 - 51001.0 * wp1 * wp2 + 6908.0 * wp2 * wp2);
-    double tau = 1.0 / 3.0 * (std::abs(beta[3] - beta[0]) + std::abs(beta[3] - beta[1]) + std::abs(beta[3] - beta[2]));
-    double alpha[4], sum = 0.0, ww[4], fw[4], p[4], px[4];
-    for (int k = 0; k < 4; ++k) {
-        double gd = tau / (beta[k] + eps);
-        alpha[k] = d[k] * (1 + gd * gd);
-        sum += alpha[k];
-    }
-    for (int k = 0; k < 4; ++k) ww[k] = alpha[k] / sum;
-    if (side == 0) {
-        p[0] = -1.0 / 6.0 * wn2 + 5.0 / 6.0 * wn1 + 1.0 / 3.0 * w0;
-        p[1] = 1.0 / 3.0 * wn1 + 5.0 / 6.0 * w0 - 1.0 / 6.0 * wp1;
-        p[2] = 11.0 / 6.0 * w0 - 7.0 / 6.0 * wp1 + 1.0 / 3.0 * wp2;
-        p[3] = (1.0 / 60.0) * (47.0 * w0 + 27.0 * wn1 - 3.0 * wn2 - 13.0 * wp1 + 2.0 * wp2);
-        px[0] = (w0 - wn1) / h;
-        px[1] = (w0 - wn1) / h;
-        px[2] = -((2.0 * w0 - 3.0 * wp1 + wp2) / h);
-        px[3] = (15.0 * w0 - 15.0 * wn1 + wn2 - wp1) / (12.0 * h);
-    } else {
-        p[0] = 1.0 / 3.0 * wn2 - 7.0 / 6.0 * wn1 + 11.0 / 6.0 * w0;
-        p[1] = -1.0 / 6.0 * wn1 + 5.0 / 6.0 * w0 + 1.0 / 3.0 * wp1;
-        p[2] = 1.0 / 3.0 * w0 + 5.0 / 6.0 * wp1 - 1.0 / 6.0 * wp2;
-        p[3] = (1.0 / 60.0) * (47.0 * w0 - 13.0 * wn1 + 2.0 * wn2 + 27.0 * wp1 - 3.0 * wp2);
-        px[0] = (2.0 * w0 - 3.0 * wn1 + wn2) / h;
-        px[1] = (-w0 + wp1) / h;
-        px[2] = (-w0 + wp1) / h;
-        px[3] = (-15.0 * w0 + wn1 + 15.0 * wp1 - wp2) / (12.0 * h);
-    }
-    fw[3] = ww[3] / d[3];
-    for (int k = 0; k < 3; ++k) fw[k] = ww[k] - ww[3] / d[3] * d[k];
-    var = 0.0;
-    der = 0.0;
-    for (int k = 0; k < 4; ++k) {
-        var += fw[k] * p[k];
-        der += fw[k] * px[k];
-    }
-}
-
 // one cell: values and slopes at its left face (L) and right face (R)
 void recon_cell(int i, bool df_variant, Pt& L, Pt& R) {
     const int order = P.order, r = order / 2, n = order;

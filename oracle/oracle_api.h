@@ -102,6 +102,37 @@ void   ref1d_set_state(const double* convar);
 void   ref1d_get_state(double* convar, double* alpha);
 int    ref1d_step(double tstop, double t, int step, double* dt_out);
 
+/* ---- 3D (CubicTube's loop, src/3Dproblem.cpp:125-157; non-DF WENO5-AO, 2x2 Gauss
+ * points per face, GKS3D, S2O4).  State: cell (i, j, k) at (i*ny + j)*nz + k over the full
+ * block including ghosts, 5 doubles per cell (rho, rho u, rho v, rho w, rho E). */
+typedef struct hos3d_params {
+    int nodex, nodey, nodez, ghost;   /* ghost >= 3                                       */
+    int characteristic;               /* 1: characteristic variables, 0: conservative     */
+    int K;                            /* internal degrees of freedom (K = 2 for gamma 1.4) */
+    double gamma;
+    double c1_euler, c2_euler;        /* numerical collision time coefficients           */
+    double cfl;
+    int tau_type;                     /* 0: Euler, 1: Navier-Stokes with viscosity mu     */
+    double mu;
+    double left, right, down, up, back, front;
+    int bc[6];                        /* left, right, down, up, back, front: FREE / PERIODIC / REFLECT */
+} hos3d_params;
+
+int    oracle3d_init(const hos3d_params* p);
+void   oracle3d_free(void);
+void   oracle3d_set_state(const double* convar, const double* primvar);  /* primvar may be NULL */
+void   oracle3d_get_state(double* convar, double* primvar);
+double oracle3d_begin_step(double tstop, double t);
+int    oracle3d_stage(int stage, double dt);
+int    oracle3d_step(double tstop, double t, double* dt_out);
+/* 1: keep the collision time of dt at the dt/2 level (the 1D GKS convention), for comparing
+ * one-dimensional 3D data with the 1D restatement; 0 (default): recompute it (GKS3D) */
+void   oracle3d_set_half_tau_of_dt(int on);
+/* per interior face of direction dir, stage fluxes summed over the 4 Gauss points with
+ * weight 1/4, in the face frame: [face][stage][f 5, derf 5]; faces ordered (normal, t1, t2)
+ * with x faces (i, j, k), y faces (j, nx-1-i, k), z faces (k, j, nx-1-i) over interior cells */
+void   oracle3d_get_flux(int dir, double* out);
+
 #ifdef __cplusplus
 }
 #endif

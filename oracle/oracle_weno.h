@@ -344,5 +344,116 @@ inline void tangent_points(int order, int ig, const double* s, const double* df,
                      + 6.0 * g9 * x * x * x * x * x + 7.0 * h9 * x * x * x * x * x * x + 8.0 * i9 * x * x * x * x * x * x * x) / h;
 }
 
+// ----------------------------------------------------------------------------------------
+// Non-DF WENO5-AO (the 1D step-0 scheme and the 3D scheme).
+// ----------------------------------------------------------------------------------------
+// full 5th-order indicator of the big stencil (src/reconstruction.cpp:184-188, :2423-2427)
+inline double beta5_big(double wn2, double wn1, double w0, double wp1, double wp2) {
+    return (1.0 / 5040.0) * (231153.0 * w0 * w0 + 104963.0 * wn1 * wn1 + 6908.0 * wn2 * wn2 -
+                             38947.0 * wn2 * wp1 + 104963.0 * wp1 * wp1 +
+                             wn1 * (-51001.0 * wn2 + 179098.0 * wp1 - 38947.0 * wp2) -
+                             3.0 * w0 * (99692.0 * wn1 - 22641.0 * wn2 + 99692.0 * wp1 - 22641.0 * wp2) +
+                             8209.0 * wn2 * wp2 - 51001.0 * wp1 * wp2 + 6908.0 * wp2 * wp2);
+}
+
+// non-DF WENO5-AO (wenoz, epsilon 1e-10, full 5th-order indicator), :161-360
+inline void weno5_plain(int side, const double* s, double h, double& var, double& der) {
+    const double dhi = 0.85, dlo = 0.85, eps = 1e-10;
+    const double wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+    double d[4] = {(1.0 - dhi) * (1.0 - dlo) / 2.0, (1.0 - dhi) * dlo, (1.0 - dhi) * (1.0 - dlo) / 2.0, dhi};
+    double beta[4];
+    beta3(s, 2, beta);
+    beta[3] = beta5_big(wn2, wn1, w0, wp1, wp2);
+    double tau = 1.0 / 3.0 * (std::abs(beta[3] - beta[0]) + std::abs(beta[3] - beta[1]) + std::abs(beta[3] - beta[2]));
+    double alpha[4], sum = 0.0, ww[4], fw[4], p[4], px[4];
+    for (int k = 0; k < 4; ++k) {
+        double gd = tau / (beta[k] + eps);
+        alpha[k] = d[k] * (1 + gd * gd);
+        sum += alpha[k];
+    }
+    for (int k = 0; k < 4; ++k) ww[k] = alpha[k] / sum;
+    if (side == 0) {
+        p[0] = -1.0 / 6.0 * wn2 + 5.0 / 6.0 * wn1 + 1.0 / 3.0 * w0;
+        p[1] = 1.0 / 3.0 * wn1 + 5.0 / 6.0 * w0 - 1.0 / 6.0 * wp1;
+        p[2] = 11.0 / 6.0 * w0 - 7.0 / 6.0 * wp1 + 1.0 / 3.0 * wp2;
+        p[3] = (1.0 / 60.0) * (47.0 * w0 + 27.0 * wn1 - 3.0 * wn2 - 13.0 * wp1 + 2.0 * wp2);
+        px[0] = (w0 - wn1) / h;
+        px[1] = (w0 - wn1) / h;
+        px[2] = -((2.0 * w0 - 3.0 * wp1 + wp2) / h);
+        px[3] = (15.0 * w0 - 15.0 * wn1 + wn2 - wp1) / (12.0 * h);
+    } else {
+        p[0] = 1.0 / 3.0 * wn2 - 7.0 / 6.0 * wn1 + 11.0 / 6.0 * w0;
+        p[1] = -1.0 / 6.0 * wn1 + 5.0 / 6.0 * w0 + 1.0 / 3.0 * wp1;
+        p[2] = 1.0 / 3.0 * w0 + 5.0 / 6.0 * wp1 - 1.0 / 6.0 * wp2;
+        p[3] = (1.0 / 60.0) * (47.0 * w0 - 13.0 * wn1 + 2.0 * wn2 + 27.0 * wp1 - 3.0 * wp2);
+        px[0] = (2.0 * w0 - 3.0 * wn1 + wn2) / h;
+        px[1] = (-w0 + wp1) / h;
+        px[2] = (-w0 + wp1) / h;
+        px[3] = (-15.0 * w0 + wn1 + 15.0 * wp1 - wp2) / (12.0 * h);
+    }
+    fw[3] = ww[3] / d[3];
+    for (int k = 0; k < 3; ++k) fw[k] = ww[k] - ww[3] / d[3] * d[k];
+    var = 0.0;
+    der = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        var += fw[k] * p[k];
+        der += fw[k] * px[k];
+    }
+}
+
+// Non-DF WENO5-AO at the two Gauss-Legendre points -h/(2 sqrt 3) (g[0]) and +h/(2 sqrt 3)
+// (g[1]) of the centre cell, with first derivatives when want_der (weno_5th_ao_2gauss,
+// src/reconstruction.cpp:2393-2551: epsilon 1e-6, wenoz weights).
+inline void weno5_2gauss(const double* s, double h, bool want_der, double* g, double* gx) {
+    const double dhi = 0.85, dlo = 0.85, eps = 1e-6;
+    const double wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+    double d[4] = {(1 - dhi) * (1 - dlo) * 0.5, (1 - dhi) * dlo, (1 - dhi) * (1 - dlo) * 0.5, dhi};
+    double beta[4];
+    beta3(s, 2, beta);
+    beta[3] = beta5_big(wn2, wn1, w0, wp1, wp2);
+    double tau = 1.0 / 3.0 * (std::abs(beta[3] - beta[0]) + std::abs(beta[3] - beta[1]) + std::abs(beta[3] - beta[2]));
+    double alpha[4], sum = 0.0, ww[4], fw[4], p[4], px[4];
+    for (int k = 0; k < 4; ++k) {
+        double gd = tau / (beta[k] + eps);
+        alpha[k] = d[k] * (1 + gd * gd);
+        sum += alpha[k];
+    }
+    for (int k = 0; k < 4; ++k) ww[k] = alpha[k] / sum;
+    fw[3] = ww[3] / d[3];
+    for (int k = 0; k < 3; ++k) fw[k] = ww[k] - ww[3] / d[3] * d[k];
+    const double sqrt3 = 1.732050807568877294;
+    p[0] = w0 - (sqrt3 * w0) / 4 + (4 * wn1 - wn2) / (4 * sqrt3);
+    p[1] = w0 + (wn1 - wp1) / (4 * sqrt3);
+    p[2] = (1.0 / 12.0) * (3 * (4 + sqrt3) * w0 + sqrt3 * (-4 * wp1 + wp2));
+    p[3] = (4314 * w0 + (4 + 500 * sqrt3) * wn1 - wn2 - 70 * sqrt3 * wn2 +
+            4 * wp1 - 500 * sqrt3 * wp1 - wp2 + 70 * sqrt3 * wp2) / 4320;
+    g[0] = 0;
+    for (int k = 0; k < 4; ++k) g[0] += fw[k] * p[k];
+    if (want_der) {
+        px[0] = -((-9 + sqrt3) * w0 - 2 * (-6 + sqrt3) * wn1 + (-3 + sqrt3) * wn2) / (6 * h);
+        px[1] = -(-2 * sqrt3 * w0 + (3 + sqrt3) * wn1 + (-3 + sqrt3) * wp1) / (6 * h);
+        px[2] = -((9 + sqrt3) * w0 - 2 * (6 + sqrt3) * wp1 + (3 + sqrt3) * wp2) / (6 * h);
+        px[3] = (48 * sqrt3 * w0 - 72 * wn1 - 26 * sqrt3 * wn1 + 9 * wn2 +
+                 2 * sqrt3 * wn2 + 72 * wp1 - 26 * sqrt3 * wp1 - 9 * wp2 + 2 * sqrt3 * wp2) / (108 * h);
+        gx[0] = 0;
+        for (int k = 0; k < 4; ++k) gx[0] += fw[k] * px[k];
+    }
+    p[0] = (1.0 / 12.0) * (3 * (4 + sqrt3) * w0 + sqrt3 * (-4 * wn1 + wn2));
+    p[1] = w0 + (-wn1 + wp1) / (4 * sqrt3);
+    p[2] = w0 - (sqrt3 * w0) / 4 + (4 * wp1 - wp2) / (4 * sqrt3);
+    p[3] = (4314 * w0 + (4 - 500 * sqrt3) * wn1 - wn2 + 70 * sqrt3 * wn2 +
+            4 * wp1 + 500 * sqrt3 * wp1 - wp2 - 70 * sqrt3 * wp2) / 4320;
+    g[1] = 0;
+    for (int k = 0; k < 4; ++k) g[1] += fw[k] * p[k];
+    if (want_der) {
+        px[0] = ((9 + sqrt3) * w0 - 2 * (6 + sqrt3) * wn1 + (3 + sqrt3) * wn2) / (6 * h);
+        px[1] = (-2 * sqrt3 * w0 + (-3 + sqrt3) * wn1 + (3 + sqrt3) * wp1) / (6 * h);
+        px[2] = ((-9 + sqrt3) * w0 - 2 * (-6 + sqrt3) * wp1 + (-3 + sqrt3) * wp2) / (6 * h);
+        px[3] = -((48 * sqrt3 * w0 + 72 * wn1 - 26 * sqrt3 * wn1 - 9 * wn2 +
+                   2 * sqrt3 * wn2 - 72 * wp1 - 26 * sqrt3 * wp1 + 9 * wp2 + 2 * sqrt3 * wp2) / (108 * h));
+        gx[1] = 0;
+        for (int k = 0; k < 4; ++k) gx[1] += fw[k] * px[k];
+    }
+}
 
 }  // namespace oracle_weno

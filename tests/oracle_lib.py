@@ -161,3 +161,46 @@ def gate_cells(pb, convar, alpha_x=None, alpha_y=None):
     fn(c.ctypes.data_as(_DP), ax.ctypes.data_as(_DP), ay.ctypes.data_as(_DP), feat.ctypes.data_as(_DP),
        dist.ctypes.data_as(_DP))
     return feat.reshape(pb.nx, pb.ny, 2, 16), dist.reshape(pb.nx, pb.ny, 2)
+
+
+class CpuStep3D:
+    """The 3D restatement (oracle3d_*)."""
+
+    def __init__(self):
+        self.lib = CpuStep("oracle").lib
+        self.lib.oracle3d_begin_step.restype = ctypes.c_double
+
+    def fn(self, name):
+        return getattr(self.lib, "oracle3d_" + name)
+
+    def init(self, pb):
+        self.pb = pb
+        self.params = pb.to_c()
+        if self.fn("init")(ctypes.byref(self.params)) != 0:
+            raise RuntimeError("init failed")
+        self.t, self.nstep = 0.0, 0
+        return self
+
+    def set_state(self, convar, primvar=None):
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        p = None if primvar is None else np.ascontiguousarray(primvar, dtype=np.float64).reshape(-1)
+        self._keep = (c, p)
+        self.fn("set_state")(c.ctypes.data_as(_DP), None if p is None else p.ctypes.data_as(_DP))
+        self.t, self.nstep = 0.0, 0
+
+    def step(self, tstop: float = 1e30) -> float:
+        dt = ctypes.c_double()
+        st = self.fn("step")(ctypes.c_double(tstop), ctypes.c_double(self.t), ctypes.byref(dt))
+        if st != 0:
+            raise RuntimeError(f"3D oracle blew up at t={self.t}")
+        self.t += dt.value
+        self.nstep += 1
+        return dt.value
+
+    def state(self):
+        shp = self.pb.shape
+        n = shp[0] * shp[1] * shp[2]
+        c = np.empty(5 * n)
+        p = np.empty(5 * n)
+        self.fn("get_state")(c.ctypes.data_as(_DP), p.ctypes.data_as(_DP))
+        return dict(convar=c.reshape(*shp, 5), primvar=p.reshape(*shp, 5))
