@@ -20,7 +20,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .params import Params1D, Params2D, Problem1D, Problem2D
+from .params import Params1D, Params2D, Params3D, Problem1D, Problem2D, Problem3D
 
 HOS_OK, HOS_E_BLOWUP, HOS_E_CONFIG, HOS_E_CUDA, HOS_E_ARG, HOS_E_NOMEM = range(6)
 FP64, FP32 = 0, 1
@@ -111,6 +111,19 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos_batch2d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
     lib.hos_batch2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     lib.hos2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
+    lib.hos3d_create.argtypes = [ctypes.POINTER(Params3D), ctypes.c_int, ctypes.POINTER(vp)]
+    lib.hos3d_destroy.argtypes = [vp]
+    lib.hos3d_set_state.argtypes = [vp, _DP, _DP]
+    lib.hos3d_get_state.argtypes = [vp, _DP, _DP]
+    lib.hos3d_step.argtypes = [vp, ctypes.c_double]
+    lib.hos3d_advance.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    lib.hos3d_sync.argtypes = [vp, _DP, _DP]
+    lib.hos3d_begin_step.argtypes = [vp, ctypes.c_double]
+    lib.hos3d_stage.argtypes = [vp, ctypes.c_int]
+    lib.hos3d_set_time.argtypes = [vp, ctypes.c_double]
+    lib.hos3d_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.hos3d_profile_step.argtypes = [vp, ctypes.c_double, _FP, ctypes.c_int]
+    lib.hos3d_last_error.restype = ctypes.c_char_p
     _LIB = lib
     return lib
 
@@ -307,6 +320,105 @@ class Solver1D:
         t, dt = ctypes.c_double(), ctypes.c_double()
         _check1(self._lib.hos1d_sync(self._h, ctypes.byref(t), ctypes.byref(dt)))
         return t.value, dt.value
+
+
+def _check3(code: int) -> None:
+    if code == HOS_OK:
+        return
+    msg = load().hos3d_last_error().decode(errors="replace")
+    if code == HOS_E_BLOWUP:
+        raise HosBlowUp(msg)
+    raise HosError(f"hos error {code}: {msg}")
+
+
+class Solver3D:
+    """One 3D problem resident on the current CUDA device (the reference's CubicTube loop,
+    src/3Dproblem.cpp:125-157): WENO5-AO on 2 x 2 Gauss points per face, GKS3D, S2O4.
+    State arrays use the reference's cell order ((i * ny + j) * nz + k, 5 doubles per cell)."""
+
+    PROFILE_KEYS = ["begin_step"] + [f"{k}{s}" for s in (0, 1) for k in
+                                     ("bc", "face_x", "line_x", "point_x", "face_y", "line_y", "point_y",
+                                      "face_z", "line_z", "point_z", "update")]
+
+    def __init__(self, problem: Problem3D, precision: int = FP64):
+        self.problem = problem
+        self._lib = load()
+        self._params = problem.to_c()
+        h = ctypes.c_void_p()
+        _check3(self._lib.hos3d_create(ctypes.byref(self._params), precision, ctypes.byref(h)))
+        self._h = h
+        self.shape = problem.shape
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hos3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _n(self) -> int:
+        return self.shape[0] * self.shape[1] * self.shape[2]
+
+    def set_state(self, convar: np.ndarray, primvar: np.ndarray | None = None) -> None:
+        c = np.ascontiguousarray(convar, dtype=np.float64).reshape(-1)
+        if c.size != 5 * self._n():
+            raise ValueError("convar must hold nx*ny*nz*5 values")
+        p = None if primvar is None else np.ascontiguousarray(primvar, dtype=np.float64).reshape(-1)
+        _check3(self._lib.hos3d_set_state(self._h, _ptr(c), _ptr(p)))
+
+    def get_state(self, primvar: bool = False):
+        c = np.empty(5 * self._n())
+        p = np.empty(5 * self._n()) if primvar else None
+        _check3(self._lib.hos3d_get_state(self._h, _ptr(c), _ptr(p)))
+        out = dict(convar=c.reshape(*self.shape, 5))
+        if primvar:
+            out["primvar"] = p.reshape(*self.shape, 5)
+        return out
+
+    def step(self, tstop: float = 1e30) -> None:
+        _check3(self._lib.hos3d_step(self._h, tstop))
+
+    def advance(self, nsteps: int, tstop: float = 1e30) -> None:
+        _check3(self._lib.hos3d_advance(self._h, nsteps, tstop))
+
+    def begin_step(self, tstop: float = 1e30) -> None:
+        _check3(self._lib.hos3d_begin_step(self._h, tstop))
+
+    def stage(self, i: int) -> None:
+        _check3(self._lib.hos3d_stage(self._h, i))
+
+    def sync(self) -> tuple[float, float]:
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        _check3(self._lib.hos3d_sync(self._h, ctypes.byref(t), ctypes.byref(dt)))
+        return t.value, dt.value
+
+    def set_time(self, t: float) -> None:
+        _check3(self._lib.hos3d_set_time(self._h, t))
+
+    @property
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        _check3(self._lib.hos3d_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
+
+    def profile_step(self, tstop: float = 1e30) -> dict:
+        ms = (ctypes.c_float * 23)()
+        _check3(self._lib.hos3d_profile_step(self._h, tstop, ms, 23))
+        return dict(zip(self.PROFILE_KEYS, [float(x) for x in ms]))
+
+    def run(self, tstop: float, max_steps: int = 10**9, check_every: int = 20) -> int:
+        steps = 0
+        t, _ = self.sync()
+        while t < tstop and steps < max_steps:
+            k = min(check_every, max_steps - steps)
+            self.advance(k, tstop)
+            steps += k
+            t, _ = self.sync()
+        return steps
 
 
 def _checkb(code: int) -> None:

@@ -246,6 +246,63 @@ int hos1d_set_alpha(hos_solver1d* s, const double* alpha);
 int hos1d_set_time(hos_solver1d* s, double t);
 const char* hos1d_last_error(void);
 
+/* ---- 3D path --------------------------------------------------------------------------
+ * The reference's 3D driver (CubicTube, src/3Dproblem.cpp:3-172): non-DF WENO5-AO face values,
+ * tangential sweeps to 2 x 2 Gauss points per face (gausspoint = 4, weights 1/4), GKS3D, S2O4,
+ * over Fluid3d arrays: state of cell (i, j, k) at (i*ny + j)*nz + k over the full block
+ * including ghosts, 5 doubles per cell (rho, rho u, rho v, rho w, rho E).  Replaces (file:line):
+ *   globals + Block3d + SetUniformMesh ..... src/3Dproblem.cpp:8-97           -> hos3d_create
+ *   ICfor_cubic_sod (any initial state) .... src/3Dproblem.cpp:174-219         -> hos3d_set_state
+ *   output3d ............................... src/output.cpp                    -> hos3d_get_state
+ *   loop body: CopyFluid_new_to_old, Get_CFL, six boundaries, Convar_to_primvar,
+ *     Reconstruction_within_cell, Reconstruction_forg0, Calculate_flux, Update_gauss
+ *     (src/3Dproblem.cpp:125-157) ........................................... -> hos3d_step
+ * GKS3D there converts the face states with Convar_to_primvar_3D and uses the pressure where the
+ * Maxwellian's lambda belongs (src/flux_function.cpp:831-836); this library uses lambda, as the
+ * reference's 1D and 2D fluxes do.  Sides may be free (the reference's only 3D boundary),
+ * periodic or reflecting; tau_type 1 adds the Navier-Stokes collision time 2 mu lambda / rho
+ * (Get_Tau_NS / Get_Tau, src/basic_function.cpp:638-708) and the viscous time-step cap of Dtx_3d
+ * (src/time_advance.cpp:826-848). */
+typedef struct hos_params3d {
+    int nodex, nodey, nodez, ghost;   /* ghost >= 3                                      */
+    int characteristic;               /* reconstruction_variable                         */
+    int K;                            /* internal degrees of freedom (2 for gamma 1.4)   */
+    double gamma;
+    double c1_euler, c2_euler;
+    double cfl;
+    int tau_type;                     /* 0 Euler, 1 Navier-Stokes                        */
+    double mu;                        /* dynamic viscosity (tau_type 1)                   */
+    double left, right, down, up, back, front;
+    int bc[6];                        /* left, right, down, up, back, front: HOS_BC_FREE,
+                                         HOS_BC_PERIODIC or HOS_BC_REFLECT                */
+} hos_params3d;
+
+typedef struct hos_solver3d hos_solver3d;
+
+/* precision HOS_FP64, or HOS_FP32 for the reconstruction and flux (state, stage combination
+ * and CFL stay FP64) */
+int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out);
+int hos3d_destroy(hos_solver3d* s);
+/* host arrays [ncell][5]; primvar (may be NULL) gives the primitives the first Get_CFL reads
+ * (rho, u, v, w, p); otherwise they are converted from convar.  Synchronous. */
+int hos3d_set_state(hos_solver3d* s, const double* convar, const double* primvar);
+/* convar and/or primvar (either may be NULL), [ncell][5]; synchronous */
+int hos3d_get_state(hos_solver3d* s, double* convar, double* primvar);
+/* one S2O4 step (asynchronous); steps queued once t >= tstop do nothing */
+int hos3d_step(hos_solver3d* s, double tstop);
+int hos3d_advance(hos_solver3d* s, int nsteps, double tstop);
+int hos3d_sync(hos_solver3d* s, double* t, double* dt);
+/* the step in pieces, as the reference's loop calls it */
+int hos3d_begin_step(hos_solver3d* s, double tstop);
+int hos3d_stage(hos_solver3d* s, int stage);
+int hos3d_set_time(hos_solver3d* s, double t);
+/* the solver's CUDA stream (cudaStream_t) */
+int hos3d_stream(hos_solver3d* s, void** stream);
+/* one step with an event after every launch: ms[0] begin, then per stage (11 each):
+ * boundaries, face/line/point+flux of x, of y, of z, update; n >= 23 */
+int hos3d_profile_step(hos_solver3d* s, double tstop, float* ms, int n);
+const char* hos3d_last_error(void);
+
 /* ---- batches of independent 2D problems ------------------------------------------------
  * No counterpart in the reference (each of its drivers advances one Block2d).  count
  * problems of uneven sizes, one stop time each, advanced together: one launch per phase for
