@@ -53,6 +53,7 @@ TRAFFIC_PER_FACE = 61.0
 FP32_FLOP_PER_FACE_GATED = 7586.0
 TRAFFIC_PER_FACE_FP32 = 86.4
 AUDIT_LOG2 = 10   # audit one warp in 1024 of predicted-smooth cells with full weights
+N_3D = 256        # cells per side of the 3D Taylor-Green leg
 ACC_STEPS = 200   # steps of the 512^2 runs whose density deviation the line states
 
 
@@ -64,9 +65,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CELLS, help=argparse.SUPPRESS)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched sweep")
-    ap.add_argument("--case", choices=["gated256"], default=None,
-                    help="small profiling case: gate trained as in the bench, then 21 plain FP32 and 21 "
-                         "gated FP32 steps of the 256^2 WENO7 Riemann problem (no timing output)")
+    ap.add_argument("--no-3d", action="store_true", help="skip the 3D Taylor-Green leg")
+    ap.add_argument("--case", choices=["gated256", "tgv3d64"], default=None,
+                    help="small profiling case: gated256 = gate trained as in the bench, then 21 plain FP32 "
+                         "and 21 gated FP32 steps of the 256^2 WENO7 Riemann problem; tgv3d64 = 2 FP32 and "
+                         "1 FP64 steps of the 64^3 Taylor-Green vortex in NVTX ranges fp32 / fp64")
     return ap.parse_args()
 
 
@@ -268,6 +271,86 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
                 "aposteriori_rejections": gst["fallback"]}}
 
 
+def tgv3d_leg(torch, dev, flush, steps, warmup, n=N_3D):
+    """3D Taylor-Green vortex, n^3 cells (WENO5-AO on 2 x 2 Gauss points per face, GKS3D with
+    the Navier-Stokes collision time, S2O4): FP32 bulk and FP64, state resident in HBM, CUDA
+    events on the solver's stream, L2 flushed between timed steps; FP32-vs-FP64 density
+    deviation after 20 steps at 128^3; the 3D restatement timed on the host cores."""
+    from hos_gb300 import cases
+    from hos_gb300.solver import FP32, FP64, Solver3D
+
+    pb, con = cases.tgv3d(n)
+    cells = n ** 3
+    out = {"workload": f"tgv3d_{n}^3_re1600_ma0.1_weno5ao_char_4gp_gks3d_ns_s2o4", "cells": cells}
+
+    def timed(prec, k, w):
+        s = Solver3D(pb, prec)
+        s.set_state(con)
+        ext = torch.cuda.ExternalStream(s.stream, device=dev)
+        s.advance(w)
+        s.sync()
+        evs = []
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+            s.advance(1)
+            b.record(ext)
+            evs.append((a, b))
+        s.sync()
+        t = sum(a.elapsed_time(b) / 1e3 for a, b in evs)
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        prof = s.profile_step()
+        s.close()
+        return t, prof
+
+    t32, prof32 = timed(FP32, steps, warmup)
+    k64 = min(steps, 2)
+    t64, prof64 = timed(FP64, k64, 1)
+    out["fp32_bulk"] = {"value": cells * steps / t32, "unit": "cell-updates/s", "ms_per_step": 1e3 * t32 / steps,
+                        "steps": steps, "warmup": warmup, "kernels_ms": prof32}
+    out["fp64"] = {"value": cells * k64 / t64, "unit": "cell-updates/s", "ms_per_step": 1e3 * t64 / k64,
+                   "steps": k64, "warmup": 1, "kernels_ms": prof64}
+    out["fp32_speedup"] = (t64 / k64) / (t32 / steps)
+    # FP32 bulk against FP64 after 20 steps at 128^3
+    pa, ca = cases.tgv3d(128)
+    rho = {}
+    for name, prec in (("fp64", FP64), ("fp32", FP32)):
+        s = Solver3D(pa, prec)
+        s.set_state(ca)
+        s.advance(20)
+        st = s.get_state()["convar"][3:-3, 3:-3, 3:-3]
+        rho[name] = st[..., 0]
+        if name == "fp64":
+            ke0 = 0.5 * float((ca[3:-3, 3:-3, 3:-3, 1] ** 2 + ca[3:-3, 3:-3, 3:-3, 2] ** 2).mean())
+            ke1 = 0.5 * float(((st[..., 1] ** 2 + st[..., 2] ** 2 + st[..., 3] ** 2) / st[..., 0]).mean())
+            t_end = s.sync()[0]
+        s.close()
+    out["accuracy"] = {"grid": "128^3", "steps": 20, "t": t_end,
+                       "rho_rel_l1_fp32_vs_fp64": float(np.abs(rho["fp32"] - rho["fp64"]).mean()
+                                                        / np.abs(rho["fp64"]).mean()),
+                       "kinetic_energy_ratio_fp64": ke1 / ke0}
+    # the 3D restatement on the host cores, bounded sample
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import CpuStep3D
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    pc, cc = cases.tgv3d(32)
+    cpu = CpuStep3D().init(pc)
+    cpu.set_state(cc)
+    cpu.step()
+    nst, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 8.0 and nst < 50:
+        cpu.step()
+        nst += 1
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": 32 ** 3 * nst / el, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                           "sample": f"32^3 Taylor-Green, {nst} S2O4 steps after 1 warm-up (OpenMP)"}
+    return out
+
+
 def sgemm_tflops(torch, dev):
     """FP32 (no TF32) cuBLAS GEMM throughput: the FP32-pipe peak the gated kernels are held to."""
     prev = torch.backends.cuda.matmul.allow_tf32
@@ -323,6 +406,26 @@ def profile_case():
     gate.close()
 
 
+def profile_case_3d():
+    """The launches of the 3D ncu summaries: 64^3 Taylor-Green, 2 FP32 steps in NVTX range
+    "fp32", then 1 FP64 step in "fp64"."""
+    import torch
+
+    from hos_gb300 import cases
+    from hos_gb300.solver import FP32, FP64, Solver3D
+
+    pb, con = cases.tgv3d(64)
+    for name, prec, k in (("fp32", FP32, 2), ("fp64", FP64, 1)):
+        s = Solver3D(pb, prec)
+        s.set_state(con)
+        torch.cuda.nvtx.range_push(name)
+        s.advance(k)
+        s.sync()
+        torch.cuda.nvtx.range_pop()
+        print(name, s.sync(), flush=True)
+        s.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -330,6 +433,9 @@ def main():
         return
     if args.case == "gated256":
         profile_case()
+        return
+    if args.case == "tgv3d64":
+        profile_case_3d()
         return
     import torch
     import torch.distributed as dist
@@ -520,6 +626,8 @@ def main():
     }
     if ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
+    if not args.no_3d:
+        line["variants"]["tgv3d"] = tgv3d_leg(torch, dev, flush, args.steps, args.warmup)
     if not args.no_batch:
         # the sweep runs WENO5: its gate is trained the same way on WENO5 runs
         gate5, rep5 = gate_train.train(order=5, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,

@@ -96,17 +96,10 @@ __device__ __forceinline__ void reduce3(double cand, unsigned bad, Ctl3* ctl, bo
     }
 }
 
-// S2O4 stage-combined flux of one face from its per-stage (f, derf) (Update_gauss,
-// src/time_advance.cpp:862-940, coefficients S2O4_3D :732-741)
-__device__ __forceinline__ void combine3(const double* FS, size_t nf, size_t f, int stage, double* out) {
-    const double c[2][2][2] = {{{0.5, 1.0 / 8.0}, {0.0, 0.0}}, {{1.0, 1.0 / 6.0}, {0.0, 1.0 / 3.0}}};
+// the stage-combined flux of one face (written by the point kernel)
+__device__ __forceinline__ void load_flux3(const double* FS, size_t nf, size_t f, double* out) {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-        double s = 0.0;
-        for (int k = 0; k <= stage; ++k)
-            s = s + (c[stage][k][0] * FS[((size_t)k * 10 + v) * nf + f] + c[stage][k][1] * FS[((size_t)k * 10 + 5 + v) * nf + f]);
-        out[v] = s;
-    }
+    for (int v = 0; v < 5; ++v) out[v] = FS[v * nf + f];
 }
 
 // W = W_old + sum over the six faces; y and z face fluxes turned back to the global frame
@@ -127,12 +120,12 @@ __global__ void __launch_bounds__(256) update3_kernel(double* __restrict__ W, do
         const size_t c = ((size_t)(I + g.g) * g.ny + (J + g.g)) * g.nz + (K + g.g);
         double xl[5], xr[5], yl[5], yr[5], zl[5], zr[5];
         const int Ib = g.nodex - 1 - I;
-        combine3(FX, lx.n(), lx.idx(I, J, K), stage, xl);
-        combine3(FX, lx.n(), lx.idx(I + 1, J, K), stage, xr);
-        combine3(FY, ly.n(), ly.idx(J, Ib, K), stage, yl);
-        combine3(FY, ly.n(), ly.idx(J + 1, Ib, K), stage, yr);
-        combine3(FZ, lz.n(), lz.idx(K, J, Ib), stage, zl);
-        combine3(FZ, lz.n(), lz.idx(K + 1, J, Ib), stage, zr);
+        load_flux3(FX, lx.n(), lx.idx(I, J, K), xl);
+        load_flux3(FX, lx.n(), lx.idx(I + 1, J, K), xr);
+        load_flux3(FY, ly.n(), ly.idx(J, Ib, K), yl);
+        load_flux3(FY, ly.n(), ly.idx(J + 1, Ib, K), yr);
+        load_flux3(FZ, lz.n(), lz.idx(K, J, Ib), zl);
+        load_flux3(FZ, lz.n(), lz.idx(K + 1, J, Ib), zr);
         const double idx_ = 1.0 / g.dx, idy = 1.0 / g.dy, idz = 1.0 / g.dz;
         // global-frame flux differences: y faces (u, v) = (-v', u'), z faces (u, w) = (-w', u')
         double tot[5];
@@ -380,9 +373,9 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
         {(void**)&s->W, 5 * s->ncell * sizeof(double)},
         {(void**)&s->Wold, 5 * s->ncell * sizeof(double)},
         {(void**)&s->stage_buf, 5 * s->ncell * sizeof(double)},
-        {(void**)&s->FS[0], 20 * s->dirs[0].fs.n() * sizeof(double)},
-        {(void**)&s->FS[1], 20 * s->dirs[1].fs.n() * sizeof(double)},
-        {(void**)&s->FS[2], 20 * s->dirs[2].fs.n() * sizeof(double)},
+        {(void**)&s->FS[0], 10 * s->dirs[0].fs.n() * sizeof(double)},
+        {(void**)&s->FS[1], 10 * s->dirs[1].fs.n() * sizeof(double)},
+        {(void**)&s->FS[2], 10 * s->dirs[2].fs.n() * sizeof(double)},
         {&s->FV, 20 * nfv * tsz},
         {&s->LV, 60 * nlv * tsz},
         {(void**)&s->ctl, sizeof(Ctl3)}};

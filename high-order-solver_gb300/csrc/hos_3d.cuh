@@ -689,10 +689,14 @@ __global__ void __launch_bounds__(LINE3_THREADS) line3_kernel(const T* __restric
 
 // Points and fluxes: one thread per Gauss line of an interior face (the two lines of a face
 // in a lane pair).  The sweep along c of the line values of both sides to the line's two
-// Gauss points (order reduction per line), GKS3D at both points, and the face's flux summed
-// over its four points with weight 1/4 into FS[stage][f 5 | derf 5][face] (face frame).
+// Gauss points (order reduction per line), GKS3D at both points, the face's (f, derf) summed
+// over its four points with weight 1/4, and the S2O4 stage combination in FP64 (Update_gauss,
+// src/time_advance.cpp:862-940; S2O4_3D :732-741): FS[0][v][face] receives the stage's
+// combined flux, 1/2 f0 + 1/8 derf0 at stage 0 and (f0 + 1/6 derf0) + (0 f1 + 1/3 derf1) at
+// stage 1, whose first part stage 0 leaves in FS[1][v][face].  Face frame.  T = float runs
+// three 128-thread CTAs per SM (168 registers).
 template <class T>
-__global__ void __launch_bounds__(POINT3_THREADS) point3_kernel(const T* __restrict__ LV, double* __restrict__ FS,
+__global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3_kernel(const T* __restrict__ LV, double* __restrict__ FS,
                                                                 Geo3 g, Dir3 d, const Ctl3* ctl, int stage) {
     if (!ctl->active) return;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -757,7 +761,15 @@ __global__ void __launch_bounds__(POINT3_THREADS) point3_kernel(const T* __restr
     if (valid && ig == 0) {
         const size_t f = d.fs.idx(a, b, c);
 #pragma unroll
-        for (int q = 0; q < 10; ++q) FS[((size_t)stage * 10 + q) * nfs + f] = (double)acc[q];
+        for (int v = 0; v < 5; ++v) {
+            const double fv = (double)acc[v], dv = (double)acc[5 + v];
+            if (stage == 0) {
+                FS[v * nfs + f] = 0.0 + (0.5 * fv + (1.0 / 8.0) * dv);
+                FS[(5 + v) * nfs + f] = 0.0 + (1.0 * fv + (1.0 / 6.0) * dv);
+            } else {
+                FS[v * nfs + f] = FS[(5 + v) * nfs + f] + (0.0 * fv + (1.0 / 3.0) * dv);
+            }
+        }
     }
 }
 
