@@ -54,6 +54,12 @@ FP32_FLOP_PER_FACE_GATED = 7586.0
 TRAFFIC_PER_FACE_FP32 = 86.4
 AUDIT_LOG2 = 10   # audit one warp in 1024 of predicted-smooth cells with full weights
 N_3D = 256        # cells per side of the 3D Taylor-Green leg
+# 3D point kernel (tangential point sweep + GKS3D at 4 Gauss points + FP64 stage combination):
+# flop per face (2 x FMA + ADD + MUL; ncu, 64^3 TGV) of the FP32 and FP64 builds, and the FP32
+# build's DRAM bytes per face
+FP32_FLOP_PER_FACE_POINT3 = 28400.0
+FP64_FLOP_PER_FACE_POINT3 = 37100.0
+TRAFFIC_PER_FACE_POINT3 = 289.0
 ACC_STEPS = 200   # steps of the 512^2 runs whose density deviation the line states
 
 
@@ -271,11 +277,12 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
                 "aposteriori_rejections": gst["fallback"]}}
 
 
-def tgv3d_leg(torch, dev, flush, steps, warmup, n=N_3D):
+def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n512=True):
     """3D Taylor-Green vortex, n^3 cells (WENO5-AO on 2 x 2 Gauss points per face, GKS3D with
     the Navier-Stokes collision time, S2O4): FP32 bulk and FP64, state resident in HBM, CUDA
     events on the solver's stream, L2 flushed between timed steps; FP32-vs-FP64 density
-    deviation after 20 steps at 128^3; the 3D restatement timed on the host cores."""
+    deviation, kinetic-energy and dissipation-rate deviation over 20 steps at 128^3; 512^3 FP32
+    and FP64 throughput; the 3D restatement timed on the host cores."""
     from hos_gb300 import cases
     from hos_gb300.solver import FP32, FP64, Solver3D
 
@@ -315,24 +322,66 @@ def tgv3d_leg(torch, dev, flush, steps, warmup, n=N_3D):
     out["fp64"] = {"value": cells * k64 / t64, "unit": "cell-updates/s", "ms_per_step": 1e3 * t64 / k64,
                    "steps": k64, "warmup": 1, "kernels_ms": prof64}
     out["fp32_speedup"] = (t64 / k64) / (t32 / steps)
-    # FP32 bulk against FP64 after 20 steps at 128^3
+    faces = (n + 1) * n * n
+    for name, prof, flop, peak, unit_peak in (("fp32_bulk", prof32, FP32_FLOP_PER_FACE_POINT3, fp32_peak, "SGEMM"),
+                                              ("fp64", prof64, FP64_FLOP_PER_FACE_POINT3, fp64_peak, "DGEMM")):
+        ms = float(np.mean([v for k, v in prof.items() if k.startswith("point")]))
+        ach = flop * faces / (ms / 1e3) / 1e12
+        out[name]["roofline"] = {"kernel": f"point3_kernel<{'float' if name == 'fp32_bulk' else 'double'}>",
+                                 "bound": "fp32" if name == "fp32_bulk" else "fp64", "unit": "TFLOP/s",
+                                 "achieved": ach, "peak": peak, "frac": ach / peak,
+                                 "peak_source": f"cuBLAS {unit_peak} measured in this run",
+                                 "flop_per_face": flop, "launch_ms": ms,
+                                 "traffic": TRAFFIC_PER_FACE_POINT3 * faces if name == "fp32_bulk" else None}
+    # FP32 bulk against FP64 from the same initial data, 128^3, 20 steps: density deviation,
+    # kinetic energy <rho |u|^2 / 2> and its dissipation rate -dKE/dt per step
     pa, ca = cases.tgv3d(128)
-    rho = {}
+    rho, ke, ts = {}, {}, {}
     for name, prec in (("fp64", FP64), ("fp32", FP32)):
         s = Solver3D(pa, prec)
         s.set_state(ca)
-        s.advance(20)
-        st = s.get_state()["convar"][3:-3, 3:-3, 3:-3]
+        kk, tt = [], []
+        for i in range(21):
+            st = s.get_state()["convar"][3:-3, 3:-3, 3:-3]
+            kk.append(0.5 * float(((st[..., 1] ** 2 + st[..., 2] ** 2 + st[..., 3] ** 2) / st[..., 0]).mean()))
+            tt.append(s.sync()[0])
+            if i < 20:
+                s.advance(1)
         rho[name] = st[..., 0]
-        if name == "fp64":
-            ke0 = 0.5 * float((ca[3:-3, 3:-3, 3:-3, 1] ** 2 + ca[3:-3, 3:-3, 3:-3, 2] ** 2).mean())
-            ke1 = 0.5 * float(((st[..., 1] ** 2 + st[..., 2] ** 2 + st[..., 3] ** 2) / st[..., 0]).mean())
-            t_end = s.sync()[0]
+        ke[name], ts[name] = np.array(kk), np.array(tt)
         s.close()
-    out["accuracy"] = {"grid": "128^3", "steps": 20, "t": t_end,
+    eps = {k: -np.diff(ke[k]) / np.diff(ts[k]) for k in ke}
+    out["accuracy"] = {"grid": "128^3", "steps": 20, "t": float(ts["fp64"][-1]),
                        "rho_rel_l1_fp32_vs_fp64": float(np.abs(rho["fp32"] - rho["fp64"]).mean()
                                                         / np.abs(rho["fp64"]).mean()),
-                       "kinetic_energy_ratio_fp64": ke1 / ke0}
+                       "kinetic_energy_rel_dev_max": float(np.abs(ke["fp32"] - ke["fp64"]).max() / ke["fp64"][0]),
+                       "dissipation_rate_rel_dev_max": float(np.abs(eps["fp32"] - eps["fp64"]).max()
+                                                             / np.abs(eps["fp64"]).max()),
+                       "kinetic_energy_ratio_fp64": float(ke["fp64"][-1] / ke["fp64"][0])}
+    # 512^3: FP32 bulk (1 warm-up, 2 timed steps) and FP64 (1 timed step, ~45 s)
+    if n512:
+        pb5, con5 = cases.tgv3d(512)
+        big = {}
+        for name, prec, k, w in (("fp32_bulk", FP32, 2, 1), ("fp64", FP64, 1, 0)):
+            s = Solver3D(pb5, prec)
+            s.set_state(con5)
+            ext = torch.cuda.ExternalStream(s.stream, device=dev)
+            s.advance(w)
+            s.sync()
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+            s.advance(k)
+            b.record(ext)
+            s.sync()
+            t = a.elapsed_time(b) / 1e3
+            big[name] = {"value": 512 ** 3 * k / t, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / k,
+                         "steps": k, "warmup": w}
+            s.close()
+        del con5
+        big["fp32_speedup"] = big["fp32_bulk"]["value"] / big["fp64"]["value"]
+        out["n512"] = big
     # the 3D restatement on the host cores, bounded sample
     sys.path.insert(0, str(ROOT / "tests"))
     from oracle_lib import CpuStep3D
@@ -627,7 +676,7 @@ def main():
     if ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
     if not args.no_3d:
-        line["variants"]["tgv3d"] = tgv3d_leg(torch, dev, flush, args.steps, args.warmup)
+        line["variants"]["tgv3d"] = tgv3d_leg(torch, dev, flush, args.steps, args.warmup, fp32_peak, fp64_peak)
     if not args.no_batch:
         # the sweep runs WENO5: its gate is trained the same way on WENO5 runs
         gate5, rep5 = gate_train.train(order=5, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
