@@ -38,6 +38,7 @@ struct Geometry {
     int characteristic;
     int integrator = 0;   // HOS_INT_*: S2O4, S1O1, S1O2, RK2, RK3, RK4
     int flux = 0;         // HOS_FLUX_*: GKS2D, LF2D
+    int first_order = 0;  // 1: first-order reconstruction (First_order_normal / _tangent)
     int stages = 2;
 };
 
@@ -306,7 +307,16 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         to_prim(pp1, st[r + 1], gamma);
         T outv[2][8];
         bool lin = false;
-        if constexpr (GATED) if ((gfl[nl * TL + tl] >> DIR) & 1) {
+        if (geo.first_order) {
+            // First_order_normal (src/reconstruction.cpp:1537-1560): the cell average in the
+            // face frame, zero slope, on both faces
+#pragma unroll
+            for (int side = 0; side < 2; ++side)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) { outv[side][v] = st[r][v]; outv[side][4 + v] = T(0.0); }
+            lin = true;
+        }
+        if constexpr (GATED) if (!lin && ((gfl[nl * TL + tl] >> DIR) & 1)) {
             // predicted smooth: the linear weights select the full-stencil polynomial, and a
             // linear reconstruction commutes with the characteristic projection
 #pragma unroll
@@ -407,7 +417,20 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             const T* w0 = line(r, side);
             T res[GP][12];
             bool lin = false;
-            if constexpr (GATED) if ((gfl[(fn + side) * TL + tc] >> (1 - DIR)) & 1) {
+            if (geo.first_order) {
+                // First_order_tangent (:2214-2231): every Gauss point takes the line value and
+                // its normal slope, zero tangential slope
+#pragma unroll
+                for (int ig = 0; ig < GP; ++ig)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        res[ig][v] = w0[v];
+                        res[ig][4 + v] = w0[4 + v];
+                        res[ig][8 + v] = T(0.0);
+                    }
+                lin = true;
+            }
+            if constexpr (GATED) if (!lin && ((gfl[(fn + side) * TL + tc] >> (1 - DIR)) & 1)) {
                 // the side cell is smooth along the tangent: full-stencil polynomial at the
                 // Gauss points, in conservative variables
 #pragma unroll

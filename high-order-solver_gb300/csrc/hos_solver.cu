@@ -520,6 +520,20 @@ int hos2d_set_boundary(hos_solver2d* s, const int* bc, const double* bc_prim) {
     return HOS_OK;
 }
 
+int hos2d_set_reconstruction(hos_solver2d* s, int mode) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    if (mode != HOS_RECON_WENO && mode != HOS_RECON_FIRST_ORDER) return fail(HOS_E_ARG, "bad reconstruction mode");
+    if (s->geo.first_order == mode) return HOS_OK;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "set_reconstruction");
+    s->geo.first_order = mode;
+    if (s->graph) {  // the captured step holds the old geometry
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    return HOS_OK;
+}
+
 int hos2d_set_time(hos_solver2d* s, double t) {
     if (!s) return fail(HOS_E_ARG, "null solver");
     StepCtl c;

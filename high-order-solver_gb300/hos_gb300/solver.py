@@ -67,6 +67,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos2d_sync.argtypes = [vp, _DP, _DP]
     lib.hos2d_launches_per_step.argtypes = [vp]
     lib.hos2d_profile_step.argtypes = [vp, ctypes.c_double, _DP]
+    lib.hos2d_set_reconstruction.argtypes = [vp, ctypes.c_int]
     lib.hos2d_stream.argtypes = [vp]
     lib.hos2d_stream.restype = vp
     lib.hos_last_error.restype = ctypes.c_char_p
@@ -180,6 +181,11 @@ class Solver2D:
     def set_state_device(self, convar_soa_ptr: int, primvar_soa_ptr: int | None = None) -> None:
         _check(self._lib.hos2d_set_state_device(self._h, ctypes.c_void_p(convar_soa_ptr),
                                                  ctypes.c_void_p(primvar_soa_ptr or 0) if primvar_soa_ptr else None))
+
+    def set_reconstruction(self, first_order: bool) -> None:
+        """First_order_normal / _tangent (True) or the WENO-AO scheme (False) for the following
+        stages: the reference drivers' step-0 switch (src/2Dproblem.cpp:733-745)."""
+        _check(self._lib.hos2d_set_reconstruction(self._h, 1 if first_order else 0))
 
     def set_alpha(self, alpha_x: np.ndarray, alpha_y: np.ndarray) -> None:
         ax = np.ascontiguousarray(alpha_x, dtype=np.float64).reshape(-1)

@@ -118,12 +118,25 @@ int tangent_order_of(Reconstruction_within_Cell_2D_tangent f) {
     return 0;
 }
 
-// the problem parameters the globals and the Block2d describe (src/2Dproblem.cpp:7-81)
-hos_params2d params2(const Block2d& b, int* order_out) {
-    const int order = order_of(cellreconstruction_2D_normal);
-    if (!order) stop(HOS_E_CONFIG, "the GPU path provides WENO5/7/9-AO reconstruction (cellreconstruction_2D_normal)");
-    if (tangent_order_of(cellreconstruction_2D_tangent) != order)
-        stop(HOS_E_CONFIG, "cellreconstruction_2D_tangent must be the WENO-AO variant of the normal reconstruction's order");
+// the problem parameters the globals and the Block2d describe (src/2Dproblem.cpp:7-81).
+// First_order_normal / _tangent (the drivers' step 0 when is_using_df_factor is set,
+// src/2Dproblem.cpp:733-745) run on the solver of the order whose Gauss points gausspoint
+// names, which the drivers then pair with their WENO-AO-DF scheme.
+hos_params2d params2(const Block2d& b, int* order_out, int* first_order_out = nullptr) {
+    const bool fo = cellreconstruction_2D_normal == First_order_normal;
+    int order;
+    if (fo) {
+        if (cellreconstruction_2D_tangent != First_order_tangent)
+            stop(HOS_E_CONFIG, "First_order_normal goes with First_order_tangent");
+        order = gausspoint == 2 ? 5 : gausspoint == 3 ? 7 : gausspoint == 4 ? 9 : 0;
+        if (!order) stop(HOS_E_CONFIG, "first-order reconstruction runs with gausspoint 2, 3 or 4");
+    } else {
+        order = order_of(cellreconstruction_2D_normal);
+        if (!order) stop(HOS_E_CONFIG, "the GPU path provides WENO5/7/9-AO and first-order reconstruction (cellreconstruction_2D_normal)");
+        if (tangent_order_of(cellreconstruction_2D_tangent) != order)
+            stop(HOS_E_CONFIG, "cellreconstruction_2D_tangent must be the WENO-AO variant of the normal reconstruction's order");
+    }
+    if (first_order_out) *first_order_out = fo ? 1 : 0;
     if (!is_using_df_factor)
         stop(HOS_E_CONFIG, "the GPU path provides the discontinuity-feedback WENO-AO variants: set is_using_df_factor = true");
     if (g0reconstruction_2D_normal != Center_do_nothing_normal || g0reconstruction_2D_tangent != Center_all_collision_multi)
@@ -456,6 +469,13 @@ void Update(Fluid2d* fluids, Flux2d_gauss**, Flux2d_gauss**, Block2d block, int 
             check2(hos2d_begin_step(c.h, c.tstop), "rebuild");  // the same dt: it depends on the state
             c.next = 0;
         }
+    }
+    {
+        // the slots may switch between first order and WENO-AO from one step to the next
+        int order = 0, fo = 0;
+        params2(block, &order, &fo);
+        if (order != c.order) stop(HOS_E_CONFIG, "the reconstruction order changed under a running solver");
+        check2(hos2d_set_reconstruction(c.h, fo ? HOS_RECON_FIRST_ORDER : HOS_RECON_WENO), "Update");
     }
     apply_boundaries2(c);
     check2(hos2d_stage(c.h, stage), "Update");

@@ -122,6 +122,14 @@ int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* al
 int hos2d_set_boundary(hos_solver2d* s, const int* bc, const double* bc_prim);
 /* Set the simulation time (Block2d::t) the next step starts from.  Synchronous. */
 int hos2d_set_time(hos_solver2d* s, double t);
+/* Reconstruction of the following stages: HOS_RECON_WENO (the WENO-AO-DF scheme of the
+ * solver's order, the default) or HOS_RECON_FIRST_ORDER (First_order_normal /
+ * First_order_tangent, src/reconstruction.cpp:1537-1560, 2214-2231: cell averages, zero
+ * slopes -- the step-0 scheme of the reference's drivers when is_using_df_factor is set,
+ * e.g. src/2Dproblem.cpp:733-745).  The Gauss points stay those of the solver's order. */
+#define HOS_RECON_WENO 0
+#define HOS_RECON_FIRST_ORDER 1
+int hos2d_set_reconstruction(hos_solver2d* s, int mode);
 
 /* CopyFluid_new_to_old + Get_CFL: fix this step's dt (clipped to tstop). Asynchronous. */
 int hos2d_begin_step(hos_solver2d* s, double tstop);

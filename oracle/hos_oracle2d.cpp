@@ -56,6 +56,7 @@ struct Config {
     double tbeg = 0;   // Block2d::t during the step (read by the wedge boundary)
     int stages = 2;
     double tc[5][5][2] = {};   // Block2d::timecoefficient of the time-marching method
+    int first_order = 0;       // First_order_normal / _tangent in the reconstruction slots
 };
 Config C;
 
@@ -196,6 +197,15 @@ void weno_tangent(int order, const double* s, const double* df, double h, double
 // ----------------------------------------------------------------------------------------
 void normal_cell(int order, const double (*st)[4], const double* al, double h, Point& Lp, Point& Rp) {
     const int r = order / 2, n = order;
+    if (C.first_order) {  // First_order_normal (src/reconstruction.cpp:1537-1560)
+        for (int v = 0; v < 4; ++v) {
+            Lp.convar[v] = st[r][v];
+            Rp.convar[v] = st[r][v];
+            Lp.der1x[v] = 0.0;
+            Rp.der1x[v] = 0.0;
+        }
+        return;
+    }
     double df[6];
     df_factors(order, al, df);
     double pn1[4], p0[4], pp1[4], bl[4], br[4];
@@ -247,6 +257,18 @@ void normal_cell(int order, const double (*st)[4], const double* al, double h, P
 // ----------------------------------------------------------------------------------------
 void tangent_face(int order, const Point (*ln)[2], const double* a1, const double* a2, double h, Recon* re) {
     const int r = order / 2, n = order, gp = C.gp;
+    if (C.first_order) {  // First_order_tangent (src/reconstruction.cpp:2214-2231)
+        for (int side = 0; side < 2; ++side)
+            for (int ig = 0; ig < gp; ++ig) {
+                Point& P = side == 0 ? re[ig].left : re[ig].right;
+                for (int v = 0; v < 4; ++v) {
+                    P.convar[v] = ln[r][side].convar[v];
+                    P.der1x[v] = ln[r][side].der1x[v];
+                    P.der1y[v] = 0.0;
+                }
+            }
+        return;
+    }
     double df[2][6];
     df_factors(order, a1, df[0]);
     df_factors(order, a2, df[1]);
@@ -753,6 +775,8 @@ void oracle2d_free(void) {
 }
 
 void oracle2d_set_threads(int n) { omp_set_num_threads(n); }
+
+void oracle2d_set_first_order(int on) { C.first_order = on ? 1 : 0; }
 
 void oracle2d_set_state(const double* convar, const double* primvar) {
     const size_t n = static_cast<size_t>(C.nx) * C.ny;

@@ -52,6 +52,9 @@ void   oracle2d_free(void);
 /* learned-gate features [ncell][2][16] and label distances [ncell][2] of a state (test oracle) */
 void   oracle2d_gate_cells(const double* convar, const double* alpha_x, const double* alpha_y, double* feat, double* dist);
 void   oracle2d_set_threads(int n);
+/* 1: First_order_normal / First_order_tangent in the reconstruction slots (the drivers' step 0
+ * when is_using_df_factor is set); 0: the WENO-AO scheme of the configured order */
+void   oracle2d_set_first_order(int on);
 void   oracle2d_set_state(const double* convar, const double* primvar);
 void   oracle2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);
 double oracle2d_begin_step(double tstop, double t);     /* CopyFluid_new_to_old + Get_CFL */
@@ -67,6 +70,7 @@ void   oracle2d_get_flux(int dir, int stage, double* out);
 int    ref2d_init(const hos2d_params* p);
 void   ref2d_free(void);
 void   ref2d_set_threads(int n);
+void   ref2d_set_first_order(int on);
 void   ref2d_set_state(const double* convar, const double* primvar);
 void   ref2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);
 double ref2d_begin_step(double tstop, double t);

@@ -55,6 +55,16 @@ void apply_bc(int side) {
 
 extern "C" {
 
+// the WENO slots ref2d_init chose, restored by ref2d_set_first_order(0)
+Reconstruction_within_Cell_2D_normal g_weno_normal = nullptr;
+Reconstruction_within_Cell_2D_tangent g_weno_tangent = nullptr;
+
+// the drivers' step-0 switch (e.g. src/2Dproblem.cpp:733-745)
+void ref2d_set_first_order(int on) {
+    cellreconstruction_2D_normal = on ? First_order_normal : g_weno_normal;
+    cellreconstruction_2D_tangent = on ? First_order_tangent : g_weno_tangent;
+}
+
 int ref2d_init(const hos2d_params* p) {
     Block2d block;
     block.uniform = true;
@@ -85,6 +95,8 @@ int ref2d_init(const hos2d_params* p) {
     } else {
         return 2;
     }
+    g_weno_normal = cellreconstruction_2D_normal;
+    g_weno_tangent = cellreconstruction_2D_tangent;
     g0reconstruction_2D_normal = Center_do_nothing_normal;
     g0reconstruction_2D_tangent = Center_all_collision_multi;
     is_reduce_order_warning = false;

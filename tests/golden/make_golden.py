@@ -5,7 +5,9 @@ seeded cases.  Run from the repository root where the reference checkout exists:
     python tests/golden/make_golden.py
 
 Each case stores the initial conserved/primitive state, the reference state (convar,
-alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps.
+alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps ("fo_" cases run
+step 0 with First_order_normal / First_order_tangent, as the drivers do when
+is_using_df_factor is set).
 
 tests/golden/refapi/ holds runs of the reference-API drivers (tests/refapi/driver2d.cpp,
 driver1d.cpp) linked against the reference's own objects (oracle/Makefile, refdrivers): the
@@ -42,6 +44,8 @@ def step_cases():
     from test_oracle_cpu import _problem
     for name in ("tmarch_s1o1_gks_w5_24", "tmarch_s1o2_gks_w5_24", "tmarch_rk2_gks_w7_24",
                  "tmarch_rk3_lf_w5_24", "tmarch_rk4_gks_w9_24", "tmarch_s2o4_lf_w7_24"):
+        yield name, _problem(name)
+    for name in ("fo_w5_free_24", "fo_w7_periodic_24", "fo_w9_reflect_24"):
         yield name, _problem(name)
 
 
@@ -113,14 +117,22 @@ def refapi():
 
 
 def main(only=None):
+    if only == "refapi":
+        refapi()
+        return
     for name, (pb, con, prim) in step_cases():
         if only and not name.startswith(only):
             continue
+        from test_oracle_cpu import first_order_steps
         r = CpuStep("ref").init(pb)
         r.set_state(con, prim)
-        dts = [r.step()]
-        s1 = r.state()
-        dts += [r.step(), r.step()]
+        fo = first_order_steps(name)
+        dts = []
+        for k in range(3):
+            r.fn("set_first_order")(1 if k < fo else 0)
+            dts.append(r.step())
+            if k == 0:
+                s1 = r.state()
         s3 = r.state()
         np.savez_compressed(OUT / f"{name}.npz", convar0=con, primvar0=prim,
                             convar1=s1["convar"], alpha_x1=s1["alpha_x"], alpha_y1=s1["alpha_y"],

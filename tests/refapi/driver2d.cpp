@@ -7,7 +7,9 @@
 //   driver2d <config.txt> <state_in.bin> <state_out.bin>
 //
 // config.txt: "key value..." lines (nodex nodey ghost order characteristic K gamma c1 c2 cfl
-// left right down up bc (4 names) bcprim (side r u v p) steps tstop precision mirror).
+// left right down up bc (4 names) bcprim (side r u v p) steps tstop precision mirror, and
+// optionally first_order_steps: steps that start with First_order_normal / _tangent, as the
+// reference's drivers do at step 0 when is_using_df_factor is set, src/2Dproblem.cpp:733-745).
 // state_in.bin: convar then primvar, [nx*ny][4] doubles each.  state_out.bin: convar, primvar,
 // alpha_x, alpha_y, then t, the step count and every step's dt.
 #include <cstdio>
@@ -138,6 +140,7 @@ int main(int argc, char** argv) {
 
     const double tstop = num("tstop");
     const int steps = (int)num("steps");
+    const int fo_steps = cfg.count("first_order_steps") ? (int)num("first_order_steps") : 0;
     std::vector<double> dts;
     block.t = 0;
     block.step = 0;
@@ -149,8 +152,13 @@ int main(int argc, char** argv) {
             block.dt = Get_CFL(block, fluids, tstop);
             dts.push_back(block.dt);
             if (is_using_df_factor) {
-                cellreconstruction_2D_normal = normal_df;
-                cellreconstruction_2D_tangent = tangent_df;
+                if (block.step < fo_steps) {
+                    cellreconstruction_2D_normal = First_order_normal;
+                    cellreconstruction_2D_tangent = First_order_tangent;
+                } else {
+                    cellreconstruction_2D_normal = normal_df;
+                    cellreconstruction_2D_tangent = tangent_df;
+                }
             }
             for (int i = 0; i < block.stages; i++) {
                 leftboundary(fluids, block, bcvalue[0]);

@@ -39,6 +39,8 @@ def config2d(pb, steps: int, tstop: float = 1e30, precision: int = 0, mirror: in
              f"c1 {pb.c1_euler!r}", f"c2 {pb.c2_euler!r}", f"cfl {pb.cfl!r}", f"left {pb.left!r}",
              f"right {pb.right!r}", f"down {pb.down!r}", f"up {pb.up!r}", "bc " + " ".join(bc),
              f"steps {steps}", f"tstop {tstop!r}", f"precision {precision}", f"mirror {mirror}"]
+    if getattr(pb, "first_order_steps", 0):
+        lines.append(f"first_order_steps {pb.first_order_steps}")
     bp = []
     for s in range(4):
         if bc[s] == "inflow":
@@ -103,6 +105,10 @@ def refapi_cases_2d():
     inflow = cases.riemann2d(20, order=5)
     inflow[0].bc = ("inflow", "free", "reflect", "reflect")
     inflow[0].bc_prim = ((1.2, 0.8, 0.1, 1.0), (0.0,) * 4, (0.0,) * 4, (0.0,) * 4)
+    fo = cases.random_riemann2d(20, seed=9, order=9)
+    fo[0].bc = ("reflect",) * 4
+    fo[0].first_order_steps = 1     # the drivers' first-order step 0 (e.g. doubleMach)
     return [("refapi_riemann_w7_24", cases.riemann2d(24, order=7), 5),
+            ("refapi_fo_w9_reflect_20", fo, 4),
             ("refapi_inflow_reflect_w5_20", inflow, 5),
             ("refapi_vortex_w9_20", cases.isentropic_vortex(20, order=9), 3)]

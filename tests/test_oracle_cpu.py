@@ -12,6 +12,11 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem)
 
 
+def first_order_steps(name):
+    """steps run with first-order reconstruction at the start of a golden case"""
+    return 1 if name.startswith("fo_") else 0
+
+
 def _problem(name):
     n = int(name.rsplit("_", 1)[1])
     if name.startswith("riemann"):
@@ -24,6 +29,13 @@ def _problem(name):
         return cases.isentropic_vortex(n, order=5)
     if name.startswith("sinwave"):
         return cases.sinwave2d(n, order=9)
+    if name.startswith("fo_"):
+        # fo_w<order>_<bc>_<n>: seeded random quadrants, first-order reconstruction at step 0
+        # then WENO-AO-DF (the drivers' is_using_df_factor switch, src/2Dproblem.cpp:733-745)
+        _, w, bc, _ = name.split("_")
+        pb, con, prim = cases.random_riemann2d(n, seed=int(w[1]), order=int(w[1]))
+        pb.bc = (bc,) * 4
+        return pb, con, prim
     if name.startswith("tmarch"):
         # tmarch_<integrator>_<flux>_w<order>_<n>: the quadrant problem with another time
         # marching / flux choice
@@ -47,9 +59,13 @@ def test_oracle_matches_golden_bitwise(name):
     gold = np.load(GOLDEN / f"{name}.npz")
     o = CpuStep("oracle").init(pb, threads=4)
     o.set_state(gold["convar0"], gold["primvar0"])
-    dts = [o.step()]
-    s1 = o.state()
-    dts += [o.step(), o.step()]
+    fo = first_order_steps(name)
+    dts = []
+    for k in range(3):
+        o.fn("set_first_order")(1 if k < fo else 0)
+        dts.append(o.step())
+        if k == 0:
+            s1 = o.state()
     s3 = o.state()
     assert np.array_equal(np.array(dts), gold["dts"])
     for k, s in (("1", s1), ("3", s3)):
