@@ -249,6 +249,155 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
     }
 }
 
+// Navier-Stokes collision times (tau_type NS): Get_Tau_NS and Get_Tau
+// (src/basic_function.cpp:638-708) with viscosity Mu (or Nu when Mu <= 0)
+template <class T>
+struct NsParam {
+    T c2, mu, nu, prc;   // prc: Prandtl fix factor 1/Pr - 1, 0 when the fix is off
+};
+template <class T>
+__device__ __forceinline__ T tau_phys(const NsParam<T>& q, T d0, T l0) {
+    if (q.mu > T(0)) return T(2.0) * q.mu * l0 / d0;
+    if (q.nu > T(0)) return T(2) * q.nu * l0;
+    return T(0);
+}
+template <class T>
+__device__ __forceinline__ T tau_num_ns(const NsParam<T>& q, T ratio, T dt, T d0, T l0) {
+    T tn = ratio * dt;   // c2 |rho_l/lambda_l - rho_r/lambda_r| / |... + ...| dt
+    if (tn != tn) tn = T(0);
+    if ((q.mu > T(0) && q.nu > T(0)) || (q.mu < T(0) && q.nu < T(0))) return T(0);
+    if (q.mu > T(0)) return tn + T(2.0) * q.mu * l0 / d0;
+    if (q.nu > T(0)) return tn + T(2) * q.nu * l0;
+    return T(0);
+}
+
+// GKS2D with the Navier-Stokes collision time at one Gauss point: the full set of
+// time-integration coefficients with tau != 0 (src/flux_function.cpp:410-690), including the
+// <A u> half-space terms of both sides and the Prandtl fix of the energy flux.  Kept out of
+// line: the Euler path above stays the hot path's code.
+template <class T>
+__device__ __noinline__ void gks_point_ns(const GState<T>& L, const GState<T>& R, T dt, T K, const NsParam<T> q,
+                                          T* fo, T* dfo) {
+    const GasK<T> gk(K);
+    T pl[4], pr[4], p0[4];
+    to_ulambda(pl, L.w, K);
+    to_ulambda(pr, R.w, K);
+    T glu[4], gru[4], t1s[4], t2s[4], w0[4], c0x[4], c0y[4];
+    {
+        Mom<T> ml, mr;
+        ml.init_half(pl[1], pl[2], pl[3], K);
+        mr.init_half(pr[1], pr[2], pr[3], K);
+        w0[0] = pl[0] * ml.up[0] + pr[0] * mr.un[0];
+        w0[1] = pl[0] * ml.up[1] + pr[0] * mr.un[1];
+        w0[2] = pl[0] * ml.vw[1] * ml.up[0] + pr[0] * mr.vw[1] * mr.un[0];
+        w0[3] = T(0.5) * pl[0] * (ml.up[2] + ml.up[0] * ml.vw[2] + ml.up[0] * ml.xi2) +
+                T(0.5) * pr[0] * (mr.un[2] + mr.un[0] * mr.vw[2] + mr.un[0] * mr.xi2);
+        T alx[4], arx[4], aly[4], ary[4], q0[4], q1[4], q2[4], q3[4];
+        microslope(alx, L.dx, pl, gk);
+        microslope(arx, R.dx, pr, gk);
+        microslope(aly, L.dy, pl, gk);
+        microslope(ary, R.dy, pr, gk);
+        contract<T, 0, 0, 0>(ml, alx, q0);
+        contract<T, 1, 0, 0>(mr, arx, q1);
+        contract<T, 0, 0, 0>(ml, aly, q2);
+        contract<T, 1, 0, 0>(mr, ary, q3);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            c0x[v] = pl[0] * q0[v] + pr[0] * q1[v];
+            c0y[v] = pl[0] * q2[v] + pr[0] * q3[v];
+        }
+        contract_unit<T, 0, 1, 0>(ml, glu);
+        contract_unit<T, 1, 1, 0>(mr, gru);
+        contract<T, 0, 2, 0>(ml, alx, q0);
+        contract<T, 1, 2, 0>(mr, arx, q1);
+        contract<T, 0, 1, 1>(ml, aly, q2);
+        contract<T, 1, 1, 1>(mr, ary, q3);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) t1s[v] = pl[0] * (q0[v] + q2[v]) + pr[0] * (q1[v] + q3[v]);
+        // time derivatives of the sides' distributions from the compatibility condition,
+        // with the whole-space moments of each side's Maxwellian (:528-567)
+        T dl[4], dr[4], Al[4], Ar[4];
+        contract<T, 2, 1, 0>(ml, alx, q0);
+        contract<T, 2, 0, 1>(ml, aly, q2);
+        contract<T, 2, 1, 0>(mr, arx, q1);
+        contract<T, 2, 0, 1>(mr, ary, q3);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            dl[v] = -pl[0] * (q0[v] + q2[v]);
+            dr[v] = -pr[0] * (q1[v] + q3[v]);
+        }
+        microslope(Al, dl, pl, gk);
+        microslope(Ar, dr, pr, gk);
+        contract<T, 0, 1, 0>(ml, Al, q0);
+        contract<T, 1, 1, 0>(mr, Ar, q1);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) t2s[v] = pl[0] * q0[v] + pr[0] * q1[v];
+    }
+    to_ulambda(p0, w0, K);
+    T g0u[4], a0xuu[4], t4s[4], A0u[4];
+    {
+        Mom<T> m0;
+        m0.init_whole(p0[1], p0[2], p0[3], K);
+        contract_unit<T, 2, 1, 0>(m0, g0u);
+        T a0x[4], a0y[4], a0xu[4], a0yv[4], a0yuv[4];
+        microslope(a0x, c0x, p0, gk);
+        contract<T, 2, 1, 0>(m0, a0x, a0xu);
+        contract<T, 2, 2, 0>(m0, a0x, a0xuu);
+        microslope(a0y, c0y, p0, gk);
+        contract<T, 2, 0, 1>(m0, a0y, a0yv);
+        contract<T, 2, 1, 1>(m0, a0y, a0yuv);
+        T dA0[4], A0[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            t4s[v] = a0xuu[v] + a0yuv[v];
+            dA0[v] = -p0[0] * (a0xu[v] + a0yv[v]);
+        }
+        microslope(A0, dA0, p0, gk);
+        contract<T, 2, 1, 0>(m0, A0, A0u);
+    }
+    const T tau = tau_phys(q, p0[0], p0[3]);
+    const T ratio = tau_ratio(pl[0], pr[0], pl[3], pr[3], q.c2);
+    // heat-flux correction of the Prandtl fix (:630-636, :678-684)
+    const T qs0 = a0xuu[3] + A0u[3] - p0[1] * (a0xuu[1] + A0u[1]) - p0[2] * (a0xuu[2] + A0u[2]);
+    T F[2][4];
+#pragma unroll
+    for (int lev = 0; lev < 2; ++lev) {
+        const T h = lev == 0 ? dt : T(0.5) * dt;
+        const T tn = tau_num_ns(q, ratio, h, p0[0], p0[3]);
+        const T eta = exp(-h / tn);
+        const T t0 = tn * (T(1) - eta);
+        const T t1 = tn * (eta * (h + tn) - tn) + tau * tn * (eta - T(1));
+        const T t2 = tau * tn * (eta - T(1));
+        const T t3 = tn * eta + h - tn;
+        const T t4 = tn * (tn - eta * (h + tn) - tau * (eta - T(1))) - h * tau;
+        const T t5 = T(0.5) * h * h - tau * tn * (eta - T(1)) - tau * h;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            T f;
+            if (lev == 0) {
+                f = pl[0] * t0 * glu[v] + pr[0] * t0 * gru[v];
+                f = f + p0[0] * t3 * g0u[v];
+                f = f + t1 * t1s[v];
+                f = f + t2 * t2s[v];
+            } else {
+                f = t0 * (pl[0] * glu[v] + pr[0] * gru[v]);
+                f = f + t1 * t1s[v];
+                f = f + t2 * t2s[v];
+                f = f + p0[0] * t3 * g0u[v];
+            }
+            f = f + p0[0] * t4 * t4s[v];
+            f = f + p0[0] * t5 * A0u[v];
+            F[lev][v] = f;
+        }
+        if (q.prc != T(0)) F[lev][3] += q.prc * (qs0 * (-p0[0] * tau * h));
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        fo[v] = (T(4.0) * F[1][v] - F[0][v]);
+        dfo[v] = T(4.0) * (F[0][v] - T(2.0) * F[1][v]);
+    }
+}
+
 // Lax-Friedrichs flux times dt of one Gauss point in the face frame (LF2D,
 // src/flux_function.cpp:700-735): the larger of |u| + c on the two sides as dissipation.
 template <class T>

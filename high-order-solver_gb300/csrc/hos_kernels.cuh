@@ -39,6 +39,9 @@ struct Geometry {
     int integrator = 0;   // HOS_INT_*: S2O4, S1O1, S1O2, RK2, RK3, RK4
     int flux = 0;         // HOS_FLUX_*: GKS2D, LF2D
     int first_order = 0;  // 1: first-order reconstruction (First_order_normal / _tangent)
+    // Navier-Stokes collision time (tau_type 1): Mu, Nu; Prandtl fix factor 1/Pr - 1 (0: off)
+    int tau_type = 0;
+    double mu = -1.0, nu = -1.0, prandtl_coef = 0.0;
     int stages = 2;
 };
 
@@ -82,12 +85,13 @@ struct BcSpec {
     // cell-centre x of cell i = left + (i + 0.5 - ghost) dx, post/pre-shock conserved states
     double wx0, wthr0, wspeed, left, dx;
     double wpost[4], wpre[4];
+    double wall[4][2];    // no-slip walls (HOS_BC_NOSLIP): wall velocity per side
 };
 
 __device__ __forceinline__ int bc_map(int idx, int n_tot, int g, int node, int kind, bool low) {
     if (kind == 0) return low ? g : n_tot - g - 1;                       // free: nearest interior
     if (kind == 1) return low ? idx + node : idx - node;                 // periodic
-    return low ? 2 * g - 1 - idx : 2 * n_tot - 2 * g - 1 - idx;          // reflective
+    return low ? 2 * g - 1 - idx : 2 * n_tot - 2 * g - 1 - idx;          // reflective / no-slip
 }
 
 // arguments of the cell update kernel (defined in hos_solver.cu)
@@ -585,7 +589,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
 #pragma unroll
             for (int v = 0; v < 4; ++v) d[v] = T(0.0);
         } else {
-            gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
+            if (geo.tau_type == 1)
+                gks_point_ns<T>(L, R, dt, K, NsParam<T>{T(geo.c2), T(geo.mu), T(geo.nu), T(geo.prandtl_coef)}, f, d);
+            else
+                gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
             if (geo.integrator == 1) {   // S1O1 takes the dt integral F0 = f + d / 2 alone
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {

@@ -64,6 +64,12 @@ __global__ void __launch_bounds__(256) cfl_from_prim_kernel(const double* __rest
         const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
         if (qx > 0) cand = qx;
         if (qy > 0 && qy < cand) cand = qy;
+        if (geo.tau_type == 1 && geo.mu > 0) {   // viscous cap of Dtx
+            const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
+            const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
+            if (cx < cand) cand = cx;
+            if (cy < cand) cand = cy;
+        }
         if (rho < 0 || p < 0 || isnan(rho) || isnan(p)) bad = 1;
     }
 #pragma unroll
@@ -185,11 +191,12 @@ struct hos_solver2d {
 namespace {
 
 int check_boundaries(const hos_params2d& p) {
+    auto wedge = [](int k) { return k == HOS_BC_WEDGE_BOTTOM || k == HOS_BC_WEDGE_TOP; };
     for (int k = 0; k < 4; ++k)
-        if (p.bc[k] < 0 || p.bc[k] > 5) return fail(HOS_E_CONFIG, "bad boundary kind");
-    if (p.bc[0] >= 4 || p.bc[1] >= 4 || (p.bc[2] == HOS_BC_WEDGE_TOP) || (p.bc[3] == HOS_BC_WEDGE_BOTTOM))
+        if (p.bc[k] < 0 || p.bc[k] > HOS_BC_NOSLIP) return fail(HOS_E_CONFIG, "bad boundary kind");
+    if (wedge(p.bc[0]) || wedge(p.bc[1]) || (p.bc[2] == HOS_BC_WEDGE_TOP) || (p.bc[3] == HOS_BC_WEDGE_BOTTOM))
         return fail(HOS_E_CONFIG, "wedge boundaries: HOS_BC_WEDGE_BOTTOM on the bottom, HOS_BC_WEDGE_TOP on the top");
-    if ((p.bc[2] >= 4 || p.bc[3] >= 4) && p.bc[0] != HOS_BC_INFLOW)
+    if ((wedge(p.bc[2]) || wedge(p.bc[3])) && p.bc[0] != HOS_BC_INFLOW)
         return fail(HOS_E_CONFIG, "wedge boundaries need an inflow left boundary");
     if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC) ||
         (p.bc[2] == HOS_BC_PERIODIC) != (p.bc[3] == HOS_BC_PERIODIC))
@@ -205,6 +212,8 @@ void fill_boundaries(BcSpec& bc, const hos_params2d& p, double dx) {
         bc.inflow[k][1] = q[0] * q[1];
         bc.inflow[k][2] = q[0] * q[2];
         bc.inflow[k][3] = q[0] * (q[3] / q[0] / (p.gamma - 1) + 0.5 * (q[1] * q[1] + q[2] * q[2]));
+        bc.wall[k][0] = q[1];   // no-slip wall velocity (bcvalue.primvar[1..2])
+        bc.wall[k][1] = q[2];
     }
     fill_wedge(bc, p, dx);
 }
@@ -337,6 +346,10 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     if (int st = check_boundaries(p)) return st;
     if (p.integrator < HOS_INT_S2O4 || p.integrator > HOS_INT_RK4) return fail(HOS_E_CONFIG, "bad time-marching method");
     if (p.flux != HOS_FLUX_GKS && p.flux != HOS_FLUX_LF) return fail(HOS_E_CONFIG, "bad flux");
+    if (p.tau_type != HOS_TAU_EULER && p.tau_type != HOS_TAU_NS) return fail(HOS_E_CONFIG, "bad tau_type");
+    if (p.tau_type == HOS_TAU_NS && p.flux != HOS_FLUX_GKS)
+        return fail(HOS_E_CONFIG, "the Navier-Stokes collision time goes with the GKS2D flux");
+    if (p.prandtl_fix && !(p.prandtl > 0)) return fail(HOS_E_CONFIG, "the Prandtl fix needs prandtl > 0");
     hos_solver2d* s = new (std::nothrow) hos_solver2d();
     if (!s) return fail(HOS_E_NOMEM, "host allocation");
     s->p = p;
@@ -360,6 +373,10 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     geo.integrator = p.integrator;
     geo.flux = p.flux;
     geo.stages = integrator_stages(p.integrator);
+    geo.tau_type = p.tau_type;
+    geo.mu = p.mu;
+    geo.nu = p.nu;
+    geo.prandtl_coef = p.tau_type == HOS_TAU_NS && p.prandtl_fix ? 1.0 / p.prandtl - 1.0 : 0.0;
     fill_boundaries(s->bc, p, geo.dx);
     s->ncell = (size_t)geo.nx * geo.ny;
     s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;

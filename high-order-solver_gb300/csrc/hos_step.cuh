@@ -2,6 +2,7 @@
 // kernel: ghost-cell gather, cell update with the CFL / blow-up reduction, step prologue.
 // Shared by the single-problem kernels (hos_solver.cu) and the batched kernels (hos_batch.cu).
 #pragma once
+#include "../../include/hos_gb300.h"
 #include "hos_kernels.cuh"
 
 namespace hos {
@@ -32,6 +33,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
     double out[4];
     int si = i, sj = j;
     bool flipu = false, flipv = false;
+    int wallx = -1, wally = -1;   // no-slip side applied on the x / y axis
     const bool yg = j < g || j >= ny - g;
     const bool xg = i < g || i >= nx - g;
     if (yg) {
@@ -41,7 +43,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
             for (int v = 0; v < 4; ++v) put(v, bc.inflow[side][v]);
             return;
         }
-        if (kind >= 4) {
+        if (kind == 4 || kind == 5) {
             // wedge boundaries act on i >= ghost only; the left ghost columns keep the
             // left-side (inflow) value (src/2Dproblem.cpp:1045-1092)
             if (i >= g) {
@@ -63,6 +65,7 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
         } else {
             sj = bc_map(j, ny, g, geo.nodey, kind, side == 2);
             flipv = kind == 2;
+            if (kind == HOS_BC_NOSLIP) wally = side;
         }
     }
     if (xg) {
@@ -76,11 +79,23 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
         }
         si = bc_map(i, nx, g, geo.nodex, kind, side == 0);
         flipu = kind == 2;
+        if (kind == HOS_BC_NOSLIP) wallx = side;
     }
     const size_t src = (size_t)si * ny + sj;
     for (int v = 0; v < 4; ++v) out[v] = W[v * plane + src];
+    // the x sides' rule first, then the y sides' (the drivers fill left, right, down, up);
+    // no-slip: 2 rho u_wall - rho u for both components (noslip_adiabatic_boundary_*,
+    // src/boundary_condition.cpp:290-365)
     if (flipu) out[1] = -out[1];
+    if (wallx >= 0) {
+        out[1] = 2 * out[0] * bc.wall[wallx][0] - out[1];
+        out[2] = 2 * out[0] * bc.wall[wallx][1] - out[2];
+    }
     if (flipv) out[2] = -out[2];
+    if (wally >= 0) {
+        out[1] = 2 * out[0] * bc.wall[wally][0] - out[1];
+        out[2] = 2 * out[0] * bc.wall[wally][1] - out[2];
+    }
     for (int v = 0; v < 4; ++v) put(v, out[v]);
 }
 
@@ -172,6 +187,13 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             const double qx = geo.dx * it, qy = geo.dy * it;
             if (qx > 0) cand = qx;
             if (qy > 0 && qy < cand) cand = qy;
+            if (geo.tau_type == 1 && geo.mu > 0) {
+                // viscous cap of Dtx (src/time_advance.cpp:300-303), the same for every cell
+                const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
+                const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
+                if (cx < cand) cand = cx;
+                if (cy < cand) cand = cy;
+            }
         }
     }
 }

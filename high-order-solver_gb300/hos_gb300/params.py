@@ -13,10 +13,10 @@ from __future__ import annotations
 import ctypes
 from dataclasses import dataclass, field
 
-BC_FREE, BC_PERIODIC, BC_REFLECT, BC_INFLOW, BC_WEDGE_BOTTOM, BC_WEDGE_TOP = 0, 1, 2, 3, 4, 5
+BC_FREE, BC_PERIODIC, BC_REFLECT, BC_INFLOW, BC_WEDGE_BOTTOM, BC_WEDGE_TOP, BC_NOSLIP = 0, 1, 2, 3, 4, 5, 6
 _BC_NAMES = {"free": BC_FREE, "outflow": BC_FREE, "periodic": BC_PERIODIC,
              "reflect": BC_REFLECT, "reflective": BC_REFLECT, "inflow": BC_INFLOW,
-             "wedge_bottom": BC_WEDGE_BOTTOM, "wedge_top": BC_WEDGE_TOP}
+             "wedge_bottom": BC_WEDGE_BOTTOM, "wedge_top": BC_WEDGE_TOP, "noslip": BC_NOSLIP}
 
 # Gauss points per face the reference pairs with each WENO-AO order
 # (weno_5th/7th/9th_ao_with_df_2gauss write 2, 3 and 4 points; src/reconstruction.cpp:2700,3093,3489)
@@ -36,6 +36,8 @@ class Params2D(ctypes.Structure):
         ("wedge_x0", ctypes.c_double), ("wedge_top_speed", ctypes.c_double),
         ("wedge_post", ctypes.c_double * 4), ("wedge_pre", ctypes.c_double * 4),
         ("integrator", ctypes.c_int), ("flux", ctypes.c_int),
+        ("tau_type", ctypes.c_int), ("mu", ctypes.c_double), ("nu", ctypes.c_double),
+        ("prandtl_fix", ctypes.c_int), ("prandtl", ctypes.c_double),
     ]
 
 
@@ -73,6 +75,13 @@ class Problem2D:
     # time marching and flux (the reference's timecoe_list_2d / flux_function_2d)
     integrator: str = "S2O4"
     flux: str = "GKS"
+    # collision time (tau_type, Mu, Nu) and the Prandtl fix (is_Prandtl_fix, Pr); the
+    # reference's defaults Mu = Nu = -1, Pr = 1
+    tau_type: int = 0
+    mu: float = -1.0
+    nu: float = -1.0
+    prandtl_fix: bool = False
+    prandtl: float = 1.0
 
     @property
     def nx(self) -> int:
@@ -111,6 +120,8 @@ class Problem2D:
             p.wedge_pre[v] = float(self.wedge_pre[v])
         p.integrator = INTEGRATORS[self.integrator]
         p.flux = FLUXES[self.flux]
+        p.tau_type, p.mu, p.nu = int(self.tau_type), float(self.mu), float(self.nu)
+        p.prandtl_fix, p.prandtl = 1 if self.prandtl_fix else 0, float(self.prandtl)
         return p
 
 

@@ -81,7 +81,7 @@ struct Side {
 
 bool same(const Side& a, const Side& b) {
     if (a.kind != b.kind) return false;
-    if (a.kind != HOS_BC_INFLOW) return true;
+    if (a.kind != HOS_BC_INFLOW && a.kind != HOS_BC_NOSLIP) return true;
     for (int v = 0; v < 4; ++v)
         if (a.prim[v] != b.prim[v]) return false;
     return true;
@@ -143,7 +143,9 @@ hos_params2d params2(const Block2d& b, int* order_out, int* first_order_out = nu
         stop(HOS_E_CONFIG, "the GPU path builds the GKS centre state by Center_all_collision_multi");
     if (flux_function_2d != GKS2D && flux_function_2d != LF2D)
         stop(HOS_E_CONFIG, "the GPU path provides the GKS2D and LF2D fluxes");
-    if (tau_type != Euler) stop(HOS_E_CONFIG, "the GPU path provides the Euler collision time (tau_type = Euler)");
+    if (tau_type != Euler && tau_type != NS) stop(HOS_E_CONFIG, "the GPU path provides the Euler and NS collision times");
+    if (tau_type == NS && flux_function_2d != GKS2D)
+        stop(HOS_E_CONFIG, "the GPU path provides the NS collision time with GKS2D (LF2D's viscous term is not provided)");
     int integrator = -1, stages = 0;
     const TimeMarchingCoefficient_2d methods[6] = {S2O4_2D, S1O1_2D, S1O2_2D, RK2_2D, RK3_2D, RK4_2D};
     const int method_stages[6] = {2, 1, 1, 2, 3, 4};
@@ -170,6 +172,11 @@ hos_params2d params2(const Block2d& b, int* order_out, int* first_order_out = nu
     p.c1_euler = c1_euler;
     p.c2_euler = c2_euler;
     p.cfl = b.CFL;
+    p.tau_type = tau_type == NS ? HOS_TAU_NS : HOS_TAU_EULER;
+    p.mu = Mu;
+    p.nu = Nu;
+    p.prandtl_fix = is_Prandtl_fix ? 1 : 0;
+    p.prandtl = Pr;
     p.left = b.left;
     p.right = b.right;
     p.down = b.down;
@@ -272,7 +279,7 @@ Ctx2& live2(const Fluid2d* f, const char* who) {
 void record2(const Fluid2d* f, int side, int kind, const Fluid2d* bcvalue) {
     Ctx2& c = ctx2(f);
     c.pend[side].kind = kind;
-    if (kind == HOS_BC_INFLOW && bcvalue)
+    if ((kind == HOS_BC_INFLOW || kind == HOS_BC_NOSLIP) && bcvalue)
         for (int v = 0; v < 4; ++v) c.pend[side].prim[v] = bcvalue->primvar[v];
     c.pend_mask |= 1u << side;
 }
@@ -289,7 +296,8 @@ void apply_boundaries2(Ctx2& c) {
         want[3].kind = HOS_BC_WEDGE_TOP;
     }
     for (int s = 0; s < 4; ++s)
-        if (want[s].kind == -2) stop(HOS_E_CONFIG, "the GPU path provides free, periodic, reflective and inflow boundaries");
+        if (want[s].kind == -2)
+            stop(HOS_E_CONFIG, "the GPU path provides free, periodic, reflective, inflow and no-slip adiabatic boundaries");
     bool changed = false;
     for (int s = 0; s < 4; ++s) changed |= !same(want[s], c.cur[s]);
     if (changed) {
@@ -357,7 +365,7 @@ void create1(Ctx1& c, const Block1d& b, const Fluid1d* f) {
     if (!order) stop(HOS_E_CONFIG, "the GPU path provides WENO5-AO and WENO5/7/9-AO-DF reconstruction (cellreconstruction)");
     if (g0reconstruction != Center_collision) stop(HOS_E_CONFIG, "the GPU path builds the GKS centre state by Center_collision");
     if (flux_function != GKS) stop(HOS_E_CONFIG, "the GPU path provides the GKS flux");
-    if (tau_type != Euler) stop(HOS_E_CONFIG, "the GPU path provides the Euler collision time (tau_type = Euler)");
+    if (tau_type != Euler) stop(HOS_E_CONFIG, "the 1D GPU path provides the Euler collision time (tau_type = Euler)");
     if (timecoe_list != S2O4) stop(HOS_E_CONFIG, "the GPU path provides S2O4 time marching");
     if (b.stages != 2) stop(HOS_E_CONFIG, "S2O4 has two stages: call Initial_stages(block) after setting timecoe_list");
     hos_params1d p{};
@@ -568,10 +576,10 @@ void reflection_boundary_up(Fluid2d* f, Block2d, Fluid2d) { record2(f, 3, HOS_BC
 void inflow_boundary_left(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 0, HOS_BC_INFLOW, &v); }
 void inflow_boundary_right(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 1, HOS_BC_INFLOW, &v); }
 void inflow_boundary_up(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 3, HOS_BC_INFLOW, &v); }
-void noslip_adiabatic_boundary_left(Fluid2d* f, Block2d, Fluid2d) { record2(f, 0, -2, nullptr); }
-void noslip_adiabatic_boundary_right(Fluid2d* f, Block2d, Fluid2d) { record2(f, 1, -2, nullptr); }
-void noslip_adiabatic_boundary_down(Fluid2d* f, Block2d, Fluid2d) { record2(f, 2, -2, nullptr); }
-void noslip_adiabatic_boundary_up(Fluid2d* f, Block2d, Fluid2d) { record2(f, 3, -2, nullptr); }
+void noslip_adiabatic_boundary_left(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 0, HOS_BC_NOSLIP, &v); }
+void noslip_adiabatic_boundary_right(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 1, HOS_BC_NOSLIP, &v); }
+void noslip_adiabatic_boundary_down(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 2, HOS_BC_NOSLIP, &v); }
+void noslip_adiabatic_boundary_up(Fluid2d* f, Block2d, Fluid2d v) { record2(f, 3, HOS_BC_NOSLIP, &v); }
 
 // reconstruction / flux slot values: identify the scheme; the work is fused in the stage
 void First_order_normal(Interface2d&, Interface2d&, Interface2d&, Interface2d&, Fluid2d*, Block2d) { not_fused("First_order_normal"); }

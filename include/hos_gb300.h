@@ -46,6 +46,9 @@ extern "C" {
  * x = wedge_x0; the left side must be HOS_BC_INFLOW with the post-shock state */
 #define HOS_BC_WEDGE_BOTTOM 4 /* bottom: post-shock state for x < x0, reflecting wall after */
 #define HOS_BC_WEDGE_TOP 5    /* top: post-shock state left of the moving shock, pre-shock right */
+#define HOS_BC_NOSLIP 6       /* noslip_adiabatic_boundary_*: mirrored density and energy, momentum
+                                 2 rho u_wall - rho u (both components); wall velocity
+                                 (bc_prim[side][1], bc_prim[side][2]) */
 
 /* time-marching methods (the reference's TimeMarchingCoefficient_2d slot values) */
 #define HOS_INT_S2O4 0      /* two-stage fourth order (default)           */
@@ -89,7 +92,18 @@ typedef struct hos_params2d {
      * (flux_function_2d, src/flux_function.cpp:314-754); 0 / 0 = S2O4 with GKS2D */
     int integrator;         /* HOS_INT_*  */
     int flux;               /* HOS_FLUX_* */
+    /* collision time (tau_type, src/basic_function.cpp:638-708): HOS_TAU_EULER, or
+     * HOS_TAU_NS with the physical tau = 2 Mu lambda / rho (or 2 Nu lambda) added to the
+     * numerical one, and the viscous time-step cap of Dtx (src/time_advance.cpp:292-305);
+     * prandtl_fix = is_Prandtl_fix, with Prandtl number prandtl (= Pr) */
+    int tau_type;
+    double mu, nu;
+    int prandtl_fix;
+    double prandtl;
 } hos_params2d;
+
+#define HOS_TAU_EULER 0
+#define HOS_TAU_NS 1
 
 typedef struct hos_solver2d hos_solver2d;
 

@@ -30,11 +30,13 @@
  * the same conditions throw hos_ref_error instead.
  *
  * Provided: WENO5/7/9-AO with the discontinuity-feedback factor (WENO5-AO without it in 1D),
- * first-order reconstruction (First_order_normal / _tangent, the drivers' step 0), GKS2D / GKS
- * with Euler collision time and LF2D; S2O4 (1D, 2D) and S1O1, S1O2, RK2, RK3, RK4 (2D); free /
- * periodic / reflective / inflow boundaries; the output writers.
- * Not provided (rejected at the first step): Van Leer reconstruction, GKS2D_smooth,
- * the 1D LF flux and 1D RK integrators, no-slip walls, NS collision time, the 3D path.
+ * first-order reconstruction (First_order_normal / _tangent, the drivers' step 0), GKS2D with
+ * the Euler or NS collision time (Mu / Nu, is_Prandtl_fix / Pr), GKS (1D) and LF2D; S2O4 (1D,
+ * 2D) and S1O1, S1O2, RK2, RK3, RK4 (2D); free / periodic / reflective / inflow / no-slip
+ * adiabatic boundaries; the output writers.
+ * Not provided (rejected at the first step): Van Leer reconstruction, GKS2D_smooth, LF2D's
+ * viscous term, the 1D LF flux and 1D RK integrators, the 3D C++ API (the 3D path is the C ABI
+ * hos3d_*).
  */
 #ifndef HOS_REF_API_H
 #define HOS_REF_API_H

@@ -395,10 +395,27 @@ void microslope(double* a, const double* der, const double* prim) {
     a[1] = 2 * prim[3] * R2 - prim[1] * a[3];
     a[0] = der[0] * overden - prim[1] * a[1] - prim[2] * a[2] - 0.5 * a[3] * (prim[1] * prim[1] + prim[2] * prim[2] + 0.5 * (C.K + 2) / prim[3]);
 }
-double tau_num(double dl, double dr, double ll, double lr, double dt) {
+// Get_Tau (src/basic_function.cpp:663-708): Euler numerical collision time, or the
+// Navier-Stokes one (numerical part c2 |.| dt plus the physical 2 Mu lambda0 / rho0)
+double tau_num(double dl, double dr, double ll, double lr, double dt, double d0 = 0.0, double l0 = 0.0) {
+    if (C.p.tau_type == 1) {
+        double tn = C.p.c2_euler * std::abs(dl / ll - dr / lr) / std::abs(dl / ll + dr / lr) * dt;
+        if (tn != tn) tn = 0.0;
+        if ((C.p.mu > 0.0 && C.p.nu > 0.0) || (C.p.mu < 0.0 && C.p.nu < 0.0)) return 0.0;
+        if (C.p.mu > 0.0) return tn + 2.0 * C.p.mu * l0 / d0;
+        if (C.p.nu > 0.0) return tn + 2 * C.p.nu * l0;
+        return 0.0;
+    }
     if (C.p.c1_euler <= 0 && C.p.c2_euler <= 0) return 0.0;
     double Cc = C.p.c2_euler * std::abs(dl / ll - dr / lr) / std::abs(dl / ll + dr / lr);
     return C.p.c1_euler * dt + dt * Cc;
+}
+// Get_Tau_NS (:638-661)
+double tau_ns(double d0, double l0) {
+    if (C.p.tau_type != 1) return 0.0;
+    if (C.p.mu > 0.0) return 2.0 * C.p.mu * l0 / d0;
+    if (C.p.nu > 0.0) return 2 * C.p.nu * l0;
+    return 0.0;
 }
 
 // ----------------------------------------------------------------------------------------
@@ -436,8 +453,8 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
         }
     }
     to_ulambda(p0, re.center.convar);
-    const double tau = 0.0;  // Get_Tau_NS for Euler (:638-661)
-    double tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt);
+    const double tau = tau_ns(p0[0], p0[3]);
+    double tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt, p0[0], p0[3]);
     double eta = std::exp(-dt / tn);
     double t[6];
     t[0] = tn * (1 - eta);
@@ -496,6 +513,11 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
     microslope(A0, dA0, p0);
     contract(m0.uv, 1, 0, A0, A0u);
     for (int i = 0; i < 4; ++i) F0[i] = F0[i] + p0[0] * t[5] * (A0u[i]);
+    if (C.p.prandtl_fix) {   // heat-flux correction (:630-636)
+        double qs = a0xuu[3] + A0u[3] - p0[1] * (a0xuu[1] + A0u[1]) - p0[2] * (a0xuu[2] + A0u[2]);
+        qs *= -p0[0] * tau * dt;
+        F0[3] += (1.0 / C.p.prandtl - 1.0) * qs;
+    }
     if (one_level) {   // S1O1 takes the dt integral alone (:637-645)
         for (int i = 0; i < 4; ++i) {
             fo[i] = F0[i];
@@ -505,7 +527,7 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
     }
     // second time level dt/2 (:647-676)
     double dt2 = 0.5 * dt;
-    tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt2);
+    tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt2, p0[0], p0[3]);
     eta = std::exp(-dt2 / tn);
     t[0] = tn * (1 - eta);
     t[1] = tn * (eta * (dt2 + tn) - tn) + tau * tn * (eta - 1);
@@ -520,6 +542,11 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
         F1[i] = F1[i] + p0[0] * t[3] * g0u[i];
         F1[i] = F1[i] + p0[0] * t[4] * (a0xuu[i] + a0yuv[i]);
         F1[i] = F1[i] + p0[0] * t[5] * (A0u[i]);
+    }
+    if (C.p.prandtl_fix) {   // (:678-684)
+        double qs = a0xuu[3] + A0u[3] - p0[1] * (a0xuu[1] + A0u[1]) - p0[2] * (a0xuu[2] + A0u[2]);
+        qs *= -p0[0] * tau * 0.5 * dt;
+        F1[3] += (1.0 / C.p.prandtl - 1.0) * qs;
     }
     for (int i = 0; i < 4; ++i) {
         fo[i] = (4.0 * F1[i] - F0[i]);
@@ -564,6 +591,14 @@ void bc_side(int side) {
     };
     double inflow[4];
     prim_to_con(inflow, C.p.bc_prim[side]);
+    // noslip_adiabatic_boundary_* (src/boundary_condition.cpp:290-365): mirrored cell, density
+    // and energy copied, both momentum components 2 rho u_wall - rho u
+    auto noslip = [&](int dst, int src) {
+        W[4 * dst + 0] = W[4 * src + 0];
+        W[4 * dst + 1] = 2 * W[4 * dst + 0] * C.p.bc_prim[side][1] - W[4 * src + 1];
+        W[4 * dst + 2] = 2 * W[4 * dst + 0] * C.p.bc_prim[side][2] - W[4 * src + 2];
+        W[4 * dst + 3] = W[4 * src + 3];
+    };
     if (side == 0 || side == 1) {
         for (int k = 0; k < g; ++k) {
             int i = side == 0 ? g - 1 - k : nx - g + k;  // same sweep order as the reference
@@ -572,6 +607,7 @@ void bc_side(int side) {
                 if (kind == HOS_BC_FREE) copy(dst, cell(side == 0 ? i + 1 : i - 1, j), 0);
                 else if (kind == HOS_BC_PERIODIC) copy(dst, cell(side == 0 ? i + C.p.nodex : i - C.p.nodex, j), 0);
                 else if (kind == HOS_BC_REFLECT) copy(dst, cell(side == 0 ? 2 * g - 1 - i : 2 * nx - 2 * g - 1 - i, j), 1);
+                else if (kind == HOS_BC_NOSLIP) noslip(dst, cell(side == 0 ? 2 * g - 1 - i : 2 * nx - 2 * g - 1 - i, j));
                 else for (int v = 0; v < 4; ++v) W[4 * dst + v] = inflow[v];
             }
         }
@@ -604,6 +640,7 @@ void bc_side(int side) {
                 if (kind == HOS_BC_FREE) copy(dst, cell(i, side == 2 ? j + 1 : j - 1), 0);
                 else if (kind == HOS_BC_PERIODIC) copy(dst, cell(i, side == 2 ? j + C.p.nodey : j - C.p.nodey), 0);
                 else if (kind == HOS_BC_REFLECT) copy(dst, cell(i, side == 2 ? 2 * g - 1 - j : 2 * ny - 2 * g - 1 - j), 2);
+                else if (kind == HOS_BC_NOSLIP) noslip(dst, cell(i, side == 2 ? 2 * g - 1 - j : 2 * ny - 2 * g - 1 - j));
                 else for (int v = 0; v < 4; ++v) W[4 * dst + v] = inflow[v];
             }
         }
@@ -806,6 +843,8 @@ double oracle2d_begin_step(double tstop, double t) {
     auto dtx = [&](double d, double h, const double* pr) {
         double tmp = std::sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + std::sqrt(C.Gamma * pr[3] / pr[0]);
         if (tmp > cfl * h / d) d = cfl * h / tmp;
+        // viscous cap (Dtx, src/time_advance.cpp:300-303)
+        if (d > 0.25 * cfl * h * h / C.p.mu && C.p.tau_type == 1 && C.p.mu > 0) d = 0.25 * cfl * h * h / C.p.mu;
         return d;
     };
     for (int i = g; i < C.nx - g; ++i)

@@ -24,7 +24,7 @@ extern "C" {
 
 /* Boundary kinds, one per side (left, right, down, up). */
 enum { HOS_BC_FREE = 0, HOS_BC_PERIODIC = 1, HOS_BC_REFLECT = 2, HOS_BC_INFLOW = 3,
-       HOS_BC_WEDGE_BOTTOM = 4, HOS_BC_WEDGE_TOP = 5 };
+       HOS_BC_WEDGE_BOTTOM = 4, HOS_BC_WEDGE_TOP = 5, HOS_BC_NOSLIP = 6 };
 
 typedef struct hos2d_params {
     int nodex, nodey;     /* interior cells                                  */
@@ -44,6 +44,13 @@ typedef struct hos2d_params {
     double wedge_x0, wedge_top_speed, wedge_post[4], wedge_pre[4];
     /* time marching: 0 S2O4, 1 S1O1, 2 S1O2, 3 RK2, 4 RK3, 5 RK4; flux: 0 GKS2D, 1 LF2D */
     int integrator, flux;
+    /* collision time: 0 Euler, 1 Navier-Stokes with Mu / Nu (Get_Tau_NS, Get_Tau); Prandtl
+     * fix of the heat flux (is_Prandtl_fix, Pr).  No-slip walls (HOS_BC_NOSLIP) take their
+     * wall velocity from bc_prim[side][1..2]. */
+    int tau_type;
+    double mu, nu;
+    int prandtl_fix;
+    double prandtl;
 } hos2d_params;
 
 /* ---- restatement (liboracle.so) ---- */

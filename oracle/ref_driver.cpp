@@ -49,6 +49,12 @@ void apply_bc(int side) {
         if (side == 1) inflow_boundary_right(f, b, v);
         if (side == 3) inflow_boundary_up(f, b, v);
         break;
+    case HOS_BC_NOSLIP:
+        if (side == 0) noslip_adiabatic_boundary_left(f, b, v);
+        if (side == 1) noslip_adiabatic_boundary_right(f, b, v);
+        if (side == 2) noslip_adiabatic_boundary_down(f, b, v);
+        if (side == 3) noslip_adiabatic_boundary_up(f, b, v);
+        break;
     }
 }
 }  // namespace
@@ -101,10 +107,13 @@ int ref2d_init(const hos2d_params* p) {
     g0reconstruction_2D_tangent = Center_all_collision_multi;
     is_reduce_order_warning = false;
     gks2dsolver = gks2nd_2d;
-    tau_type = Euler;
+    tau_type = p->tau_type == 1 ? NS : Euler;
+    Mu = p->mu;
+    Nu = p->nu;
     c1_euler = p->c1_euler;
     c2_euler = p->c2_euler;
-    is_Prandtl_fix = false;
+    is_Prandtl_fix = p->prandtl_fix != 0;
+    Pr = p->prandtl;
     flux_function_2d = p->flux == 1 ? LF2D : GKS2D;
     switch (p->integrator) {
         case 0: timecoe_list_2d = S2O4_2D; break;

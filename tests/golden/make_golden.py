@@ -7,7 +7,8 @@ seeded cases.  Run from the repository root where the reference checkout exists:
 Each case stores the initial conserved/primitive state, the reference state (convar,
 alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps ("fo_" cases run
 step 0 with First_order_normal / First_order_tangent, as the drivers do when
-is_using_df_factor is set).
+is_using_df_factor is set; "ns_" cases use the Navier-Stokes collision time, no-slip walls
+and the Prandtl fix, also with a first-order step 0).
 
 tests/golden/refapi/ holds runs of the reference-API drivers (tests/refapi/driver2d.cpp,
 driver1d.cpp) linked against the reference's own objects (oracle/Makefile, refdrivers): the
@@ -45,7 +46,8 @@ def step_cases():
     for name in ("tmarch_s1o1_gks_w5_24", "tmarch_s1o2_gks_w5_24", "tmarch_rk2_gks_w7_24",
                  "tmarch_rk3_lf_w5_24", "tmarch_rk4_gks_w9_24", "tmarch_s2o4_lf_w7_24"):
         yield name, _problem(name)
-    for name in ("fo_w5_free_24", "fo_w7_periodic_24", "fo_w9_reflect_24"):
+    for name in ("fo_w5_free_24", "fo_w7_periodic_24", "fo_w9_reflect_24",
+                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w9_nu_24"):
         yield name, _problem(name)
 
 

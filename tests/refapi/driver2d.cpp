@@ -9,7 +9,9 @@
 // config.txt: "key value..." lines (nodex nodey ghost order characteristic K gamma c1 c2 cfl
 // left right down up bc (4 names) bcprim (side r u v p) steps tstop precision mirror, and
 // optionally first_order_steps: steps that start with First_order_normal / _tangent, as the
-// reference's drivers do at step 0 when is_using_df_factor is set, src/2Dproblem.cpp:733-745).
+// reference's drivers do at step 0 when is_using_df_factor is set, src/2Dproblem.cpp:733-745;
+// tau_type (1: NS), mu, nu, prandtl_fix, pr: the collision-time globals; bc names may be
+// noslip, whose wall velocity comes from the side's bcprim entry).
 // state_in.bin: convar then primvar, [nx*ny][4] doubles each.  state_out.bin: convar, primvar,
 // alpha_x, alpha_y, then t, the step count and every step's dt.
 #include <cstdio>
@@ -58,15 +60,16 @@ int main(int argc, char** argv) {
 
     std::map<std::string, BoundaryCondition2d> low = {
         {"free", free_boundary_left}, {"periodic", periodic_boundary_left}, {"reflect", reflection_boundary_left},
-        {"inflow", inflow_boundary_left}};
+        {"inflow", inflow_boundary_left}, {"noslip", noslip_adiabatic_boundary_left}};
     std::map<std::string, BoundaryCondition2d> high = {
         {"free", free_boundary_right}, {"periodic", periodic_boundary_right}, {"reflect", reflection_boundary_right},
-        {"inflow", inflow_boundary_right}};
+        {"inflow", inflow_boundary_right}, {"noslip", noslip_adiabatic_boundary_right}};
     std::map<std::string, BoundaryCondition2d> down = {
-        {"free", free_boundary_down}, {"periodic", periodic_boundary_down}, {"reflect", reflection_boundary_down}};
+        {"free", free_boundary_down}, {"periodic", periodic_boundary_down}, {"reflect", reflection_boundary_down},
+        {"noslip", noslip_adiabatic_boundary_down}};
     std::map<std::string, BoundaryCondition2d> up = {
         {"free", free_boundary_up}, {"periodic", periodic_boundary_up}, {"reflect", reflection_boundary_up},
-        {"inflow", inflow_boundary_up}};
+        {"inflow", inflow_boundary_up}, {"noslip", noslip_adiabatic_boundary_up}};
     BoundaryCondition2d leftboundary = low.at(cfg.at("bc")[0]);
     BoundaryCondition2d rightboundary = high.at(cfg.at("bc")[1]);
     BoundaryCondition2d downboundary = down.at(cfg.at("bc")[2]);
@@ -93,7 +96,11 @@ int main(int argc, char** argv) {
     is_reduce_order_warning = false;
     is_using_df_factor = true;
     gks2dsolver = gks2nd_2d;
-    tau_type = Euler;
+    tau_type = cfg.count("tau_type") && num("tau_type") == 1 ? NS : Euler;
+    if (cfg.count("mu")) Mu = num("mu");
+    if (cfg.count("nu")) Nu = num("nu");
+    if (cfg.count("prandtl_fix")) is_Prandtl_fix = num("prandtl_fix") != 0;
+    if (cfg.count("pr")) Pr = num("pr");
     c1_euler = num("c1");
     c2_euler = num("c2");
     flux_function_2d = GKS2D;

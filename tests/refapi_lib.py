@@ -17,7 +17,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[1]
 PKG = ROOT / "high-order-solver_gb300" / "hos_gb300"
 DRIVER_DIR = Path(__file__).resolve().parent / "refapi"
-BC_NAMES = {0: "free", 1: "periodic", 2: "reflect", 3: "inflow"}
+BC_NAMES = {0: "free", 1: "periodic", 2: "reflect", 3: "inflow", 6: "noslip"}
 
 
 def build_driver(name: str, out_dir: Path) -> Path:
@@ -41,9 +41,12 @@ def config2d(pb, steps: int, tstop: float = 1e30, precision: int = 0, mirror: in
              f"steps {steps}", f"tstop {tstop!r}", f"precision {precision}", f"mirror {mirror}"]
     if getattr(pb, "first_order_steps", 0):
         lines.append(f"first_order_steps {pb.first_order_steps}")
+    if getattr(pb, "tau_type", 0):
+        lines += [f"tau_type {pb.tau_type}", f"mu {pb.mu!r}", f"nu {pb.nu!r}",
+                  f"prandtl_fix {int(pb.prandtl_fix)}", f"pr {pb.prandtl!r}"]
     bp = []
     for s in range(4):
-        if bc[s] == "inflow":
+        if bc[s] in ("inflow", "noslip"):
             bp += [str(s)] + [repr(float(v)) for v in pb.bc_prim[s]]
     if bp:
         lines.append("bcprim " + " ".join(bp))
@@ -108,7 +111,14 @@ def refapi_cases_2d():
     fo = cases.random_riemann2d(20, seed=9, order=9)
     fo[0].bc = ("reflect",) * 4
     fo[0].first_order_steps = 1     # the drivers' first-order step 0 (e.g. doubleMach)
+    # the viscous_sod_shock_problem loop (src/2Dproblem.cpp:1095-1283): NS collision time,
+    # no-slip adiabatic left / right / bottom, reflecting top, first-order step 0, WENO5-AO-DF
+    ns = cases.random_riemann2d(20, seed=5, order=5)
+    ns[0].bc = ("noslip", "noslip", "noslip", "reflect")
+    ns[0].tau_type, ns[0].mu, ns[0].c2_euler = 1, 1e-3, 9.0
+    ns[0].first_order_steps = 1
     return [("refapi_riemann_w7_24", cases.riemann2d(24, order=7), 5),
             ("refapi_fo_w9_reflect_20", fo, 4),
+            ("refapi_ns_noslip_w5_20", ns, 4),
             ("refapi_inflow_reflect_w5_20", inflow, 5),
             ("refapi_vortex_w9_20", cases.isentropic_vortex(20, order=9), 3)]

@@ -14,7 +14,7 @@ STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.
 
 def first_order_steps(name):
     """steps run with first-order reconstruction at the start of a golden case"""
-    return 1 if name.startswith("fo_") else 0
+    return 1 if name.startswith(("fo_", "ns_")) else 0
 
 
 def _problem(name):
@@ -35,6 +35,24 @@ def _problem(name):
         _, w, bc, _ = name.split("_")
         pb, con, prim = cases.random_riemann2d(n, seed=int(w[1]), order=int(w[1]))
         pb.bc = (bc,) * 4
+        return pb, con, prim
+    if name.startswith("ns_"):
+        # ns_w<order>_<variant>_<n>: Navier-Stokes collision time, first-order step 0
+        #   noslip : the viscous_sod_shock_problem set-up (src/2Dproblem.cpp:1095-1160): no-slip
+        #            adiabatic left/right/bottom, reflecting top, Mu = 1e-3, c2 = 9
+        #   wall   : moving no-slip walls, Prandtl fix (Pr = 0.72), Mu = 0.05 (viscous dt cap)
+        #   nu     : kinematic viscosity Nu = 2e-3 (Mu unset), periodic
+        _, w, variant, _ = name.split("_")
+        order = int(w[1])
+        pb, con, prim = cases.random_riemann2d(n, seed=order, order=order)
+        pb.tau_type, pb.c2_euler = 1, 9.0
+        if variant == "noslip":
+            pb.bc, pb.mu = ("noslip", "noslip", "noslip", "reflect"), 1e-3
+        elif variant == "wall":
+            pb.bc, pb.mu, pb.prandtl_fix, pb.prandtl = ("noslip",) * 4, 0.05, True, 0.72
+            pb.bc_prim = ((0.0, 0.0, 0.2, 0.0), (0.0, 0.0, -0.1, 0.0), (0.0, 0.3, 0.0, 0.0), (0.0, -0.25, 0.0, 0.0))
+        else:
+            pb.bc, pb.mu, pb.nu = ("periodic",) * 4, -1.0, 2e-3
         return pb, con, prim
     if name.startswith("tmarch"):
         # tmarch_<integrator>_<flux>_w<order>_<n>: the quadrant problem with another time
