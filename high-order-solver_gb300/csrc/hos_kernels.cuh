@@ -39,6 +39,7 @@ struct Geometry {
     int integrator = 0;   // HOS_INT_*: S2O4, S1O1, S1O2, RK2, RK3, RK4
     int flux = 0;         // HOS_FLUX_*: GKS2D, LF2D
     int first_order = 0;  // 1: first-order reconstruction (First_order_normal / _tangent)
+    int source = 0;       // 1: Update_with_source (gravity along +y; S2O4 stage 0 alone updates)
     // Navier-Stokes collision time (tau_type 1): Mu, Nu; Prandtl fix factor 1/Pr - 1 (0: off)
     int tau_type = 0;
     double mu = -1.0, nu = -1.0, prandtl_coef = 0.0;
@@ -637,7 +638,11 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             for (int v = 0; v < 4; ++v) {
                 const double F = double(Fq[v]), D = double(Dq[v]);
                 if (s2o4) {
-                    if (a.stage == 0) {
+                    if (geo.source) {
+                        // Update_with_source: the Gauss-weighted f of the stage itself
+                        X[v] = F;
+                        P[v] = 0.0;
+                    } else if (a.stage == 0) {
                         X[v] = 0.5 * F + (1.0 / 8.0) * D;
                         P[v] = 1.0 * F + (1.0 / 6.0) * D;
                     } else {
@@ -664,7 +669,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             const double as = double(asum);
             double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
             a.FA[fi] = am < 2.0 ? 0.0 : am;
-            if (s2o4 && a.stage == 1) {
+            if (s2o4 && a.stage == 1 && !geo.source) {
 #pragma unroll
                 for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
             }

@@ -551,6 +551,21 @@ int hos2d_set_reconstruction(hos_solver2d* s, int mode) {
     return HOS_OK;
 }
 
+int hos2d_set_source(hos_solver2d* s, int on) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    if (on && s->geo.integrator != HOS_INT_S2O4) return fail(HOS_E_CONFIG, "the source update is provided with S2O4");
+    const int mode = on ? 1 : 0;
+    if (s->geo.source == mode) return HOS_OK;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "set_source");
+    s->geo.source = mode;
+    if (s->graph) {  // the captured step holds the old geometry
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    return HOS_OK;
+}
+
 int hos2d_set_time(hos_solver2d* s, double t) {
     if (!s) return fail(HOS_E_ARG, "null solver");
     StepCtl c;

@@ -128,7 +128,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         for (int v = 0; v < 4; ++v) {
             // the state the stage started from: needed at stage 0 (snapshot, and the CFL of
             // one-stage methods) and by RK3's state combination
-            const bool need_cur = a.stage == 0 || geo.integrator == 4;
+            const bool need_cur = a.stage == 0 || geo.integrator == 4 || geo.source;
             const double cur = need_cur ? a.W[v * plane + c] : 0.0;
             double old;
             if (a.stage == 0) {
@@ -143,7 +143,17 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             total += -geo.dx * a.FXy[v * nfy + fu];
             total += geo.dy * a.FXx[v * nfx + fl];
             total += -geo.dy * a.FXx[v * nfx + fr];
-            if (geo.integrator == 4 && a.stage == 1)        // RK3 (Update_with_gauss_RK3, :511-526)
+            if (geo.source) {
+                // Update_with_source under S2O4 (src/time_advance.cpp:534-704): stage 0 takes
+                // W_old + dt (L + S), S = (0, 0, rho, rho v) of the stage's state; stage 1
+                // leaves the state
+                if (a.stage == 0) {
+                    const double S = v == 2 ? a.W[c] : v == 3 ? a.W[2 * plane + c] : 0.0;
+                    w[v] = old + (total * iarea + a.ctl->dt * S);
+                } else {
+                    w[v] = cur;
+                }
+            } else if (geo.integrator == 4 && a.stage == 1)        // RK3 (Update_with_gauss_RK3, :511-526)
                 w[v] = 0.75 * old + 0.25 * cur + total * iarea;
             else if (geo.integrator == 4 && a.stage == 2)
                 w[v] = 1.0 / 3.0 * old + 2.0 / 3.0 * cur + total * iarea;

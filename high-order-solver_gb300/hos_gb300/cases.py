@@ -322,3 +322,34 @@ def tgv3d(n: int = 256, re: float = 1600.0, mach: float = 0.1, gamma: float = 1.
     con[..., 3] = 0.0
     con[..., 4] = p / (gamma - 1) + 0.5 * (u * u + v * v)
     return pb, con
+
+
+def rt2d(nodex: int = 100, order: int = 5) -> tuple:
+    """Rayleigh-Taylor set-up of the reference's RT_instability driver (src/2Dproblem.cpp:611-818):
+    [0, 0.25] x [0, 1] with nodex x 4 nodex cells, density 2 below y = 0.5 and 1 above,
+    hydrostatic pressure p = 2y + 1 / y + 1.5, vertical velocity perturbation
+    v = -0.025 c cos(8 pi x); reflecting left/right walls and the fixed bottom (2, 0, 0, 1) and
+    top (1, 0, 0, 2.5) states of RT_boundary (src/boundary_condition.cpp:188-242).  The gravity
+    source of Update_with_source acts along +y.  Returns (problem, convar, primvar)."""
+    gamma = 1.4
+    pb = Problem2D(nodex=nodex, nodey=4 * nodex, order=order, ghost=5, K=3, gamma=gamma, c1_euler=0.05,
+                   c2_euler=1.0, cfl=0.5, left=0.0, right=0.25, down=0.0, up=1.0,
+                   bc=("reflect", "reflect", "inflow", "inflow"),
+                   bc_prim=((0.0,) * 4, (0.0,) * 4, (2.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 2.5)))
+    g = pb.ghost
+    dx, dy = pb.dx, pb.dy
+    prim = np.zeros((pb.nx, pb.ny, 4))
+    for i in range(g, pb.nx - g):
+        x = (i - g + 0.5) * dx
+        for j in range(g, pb.ny - g):
+            if j - g + 1 < 0.5 / dy:
+                p = 2.0 * (j - g + 0.5) * dy + 1.0
+                c = math.sqrt(gamma * p / 2.0)
+                prim[i, j] = (2.0, 0.0, -0.025 * c * math.cos(8.0 * math.pi * x), p)
+            else:
+                p = (j - g + 0.5) * dy + 1.5
+                c = math.sqrt(gamma * p / 1.0)
+                prim[i, j] = (1.0, 0.0, -0.025 * c * math.cos(8.0 * math.pi * x), p)
+    prim = _fill_ghosts(prim, g)   # ghosts: filled by the boundaries before first use
+    con = prim_to_con(prim, gamma)
+    return pb, con, prim

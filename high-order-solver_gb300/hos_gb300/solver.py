@@ -68,6 +68,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos2d_launches_per_step.argtypes = [vp]
     lib.hos2d_profile_step.argtypes = [vp, ctypes.c_double, _DP]
     lib.hos2d_set_reconstruction.argtypes = [vp, ctypes.c_int]
+    lib.hos2d_set_source.argtypes = [vp, ctypes.c_int]
     lib.hos2d_stream.argtypes = [vp]
     lib.hos2d_stream.restype = vp
     lib.hos_last_error.restype = ctypes.c_char_p
@@ -186,6 +187,10 @@ class Solver2D:
         """First_order_normal / _tangent (True) or the WENO-AO scheme (False) for the following
         stages: the reference drivers' step-0 switch (src/2Dproblem.cpp:733-745)."""
         _check(self._lib.hos2d_set_reconstruction(self._h, 1 if first_order else 0))
+
+    def set_source(self, on: bool) -> None:
+        """Update_with_source (gravity along +y, the RT_instability driver) as the stage update."""
+        _check(self._lib.hos2d_set_source(self._h, 1 if on else 0))
 
     def set_alpha(self, alpha_x: np.ndarray, alpha_y: np.ndarray) -> None:
         ax = np.ascontiguousarray(alpha_x, dtype=np.float64).reshape(-1)

@@ -144,6 +144,11 @@ int hos2d_set_time(hos_solver2d* s, double t);
 #define HOS_RECON_WENO 0
 #define HOS_RECON_FIRST_ORDER 1
 int hos2d_set_reconstruction(hos_solver2d* s, int mode);
+/* 1: the stage update is Update_with_source (src/time_advance.cpp:534-704, the RT_instability
+ * driver): gravity source S = (0, 0, rho, rho v); under S2O4 stage 0 sets
+ * W = W_old + dt (L(W) + S(W)) from the stage's Gauss-weighted fluxes f and stage 1 leaves the
+ * state (fluxes and DF indicators are still computed), as the reference does.  S2O4 only. */
+int hos2d_set_source(hos_solver2d* s, int on);
 
 /* CopyFluid_new_to_old + Get_CFL: fix this step's dt (clipped to tstop). Asynchronous. */
 int hos2d_begin_step(hos_solver2d* s, double tstop);

@@ -57,6 +57,7 @@ struct Config {
     int stages = 2;
     double tc[5][5][2] = {};   // Block2d::timecoefficient of the time-marching method
     int first_order = 0;       // First_order_normal / _tangent in the reconstruction slots
+    int source = 0;            // Update_with_source instead of Update (gravity source)
 };
 Config C;
 
@@ -815,6 +816,8 @@ void oracle2d_set_threads(int n) { omp_set_num_threads(n); }
 
 void oracle2d_set_first_order(int on) { C.first_order = on ? 1 : 0; }
 
+void oracle2d_set_source(int on) { C.source = on ? 1 : 0; }
+
 void oracle2d_set_state(const double* convar, const double* primvar) {
     const size_t n = static_cast<size_t>(C.nx) * C.ny;
     std::memcpy(W.data(), convar, 4 * n * sizeof(double));
@@ -956,6 +959,38 @@ int oracle2d_stage(int stage, double dt) {
                         X[(f * gp + ig) * 4 + v] = fl;
                     }
     };
+    if (C.source) {
+        // Update_with_source (src/time_advance.cpp:534-704) under S2O4: stage 0 takes
+        // W = W_old + dt (L + S) with L the Gauss-weighted face fluxes f of the stage (global
+        // frame) over dx dt and S = (0, 0, rho, rho v) of the current state; stage 1 leaves W
+        if (stage == 0) {
+            const double dx = C.dx, dy = C.dy;
+#pragma omp parallel for
+            for (int i = g; i < g + C.p.nodex; ++i)
+                for (int j = g; j < g + C.p.nodey; ++j) {
+                    const int c = cell(i, j);
+                    const size_t f = face(i, j);
+                    double Lw[4] = {0, 0, 0, 0};
+                    for (int v = 0; v < 4; ++v)
+                        for (int ig = 0; ig < gp; ++ig) {
+                            auto xf = [&](size_t ff) {
+                                const double* x = &XF[((ff * 4 + stage) * gp + ig) * 8];
+                                return v == 1 ? x[1] * 1.0 - x[2] * 0.0 : v == 2 ? x[1] * 0.0 + x[2] * 1.0 : x[v];
+                            };
+                            auto yf = [&](size_t ff) {
+                                const double* x = &YF[((ff * 4 + stage) * gp + ig) * 8];
+                                return v == 1 ? x[1] * 0.0 - x[2] * 1.0 : v == 2 ? x[1] * 1.0 + x[2] * 0.0 : x[v];
+                            };
+                            Lw[v] += C.gw[ig] * ((xf(f) - xf(f + ny + 1)) / dx / dt + (yf(f) - yf(f + 1)) / dy / dt);
+                        }
+                    const double S[4] = {0.0, 0.0, W[4 * c + 0], W[4 * c + 2]};
+                    for (int v = 0; v < 4; ++v) {
+                        const double L1 = Lw[v] + S[v];
+                        W[4 * c + v] = Wold[4 * c + v] + dt * L1;
+                    }
+                }
+        }
+    } else {
     combine(XF, XX, g, g + C.p.nodex + 1, g, g + C.p.nodey);
     combine(YF, YX, g, g + C.p.nodex, g, g + C.p.nodey + 1);
     // Update_with_gauss (src/time_advance.cpp:431-474): y-face fluxes rotate back to the
@@ -992,6 +1027,7 @@ int oracle2d_stage(int stage, double dt) {
                     W[4 * c + v] += total / area;
             }
         }
+    }
     // DF factor update (Update_alpha, :1523-1534)
     const int jend = g + std::min(C.p.nodex, C.p.nodey);
 #pragma omp parallel for

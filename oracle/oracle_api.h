@@ -62,6 +62,8 @@ void   oracle2d_set_threads(int n);
 /* 1: First_order_normal / First_order_tangent in the reconstruction slots (the drivers' step 0
  * when is_using_df_factor is set); 0: the WENO-AO scheme of the configured order */
 void   oracle2d_set_first_order(int on);
+/* 1: the stage update is Update_with_source (gravity source, the RT_instability driver) */
+void   oracle2d_set_source(int on);
 void   oracle2d_set_state(const double* convar, const double* primvar);
 void   oracle2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);
 double oracle2d_begin_step(double tstop, double t);     /* CopyFluid_new_to_old + Get_CFL */
@@ -78,6 +80,7 @@ int    ref2d_init(const hos2d_params* p);
 void   ref2d_free(void);
 void   ref2d_set_threads(int n);
 void   ref2d_set_first_order(int on);
+void   ref2d_set_source(int on);
 void   ref2d_set_state(const double* convar, const double* primvar);
 void   ref2d_get_state(double* convar, double* primvar, double* alpha_x, double* alpha_y);
 double ref2d_begin_step(double tstop, double t);

@@ -65,6 +65,10 @@ extern "C" {
 Reconstruction_within_Cell_2D_normal g_weno_normal = nullptr;
 Reconstruction_within_Cell_2D_tangent g_weno_tangent = nullptr;
 
+// Update_with_source in place of Update (the RT_instability loop, src/2Dproblem.cpp:752-758)
+int g_source = 0;
+void ref2d_set_source(int on) { g_source = on; }
+
 // the drivers' step-0 switch (e.g. src/2Dproblem.cpp:733-745)
 void ref2d_set_first_order(int on) {
     cellreconstruction_2D_normal = on ? First_order_normal : g_weno_normal;
@@ -187,6 +191,10 @@ int ref2d_stage(int stage, double dt) {
     if (g_bc[3] == HOS_BC_WEDGE_TOP) {
         // the reference's own double-Mach boundary (Mach 10 states hard-wired in it)
         boundaryforDoubleMach(g_fluids, g_block, g_bcvalue[0]);
+    } else if (g_source) {
+        // the RT_instability loop's own boundary (src/boundary_condition.cpp:188-242): reflecting
+        // sides, fixed bottom and top states
+        RT_boundary(g_fluids, g_block);
     } else {
         for (int s = 0; s < 4; ++s) apply_bc(s);
     }
@@ -202,7 +210,8 @@ int ref2d_stage(int stage, double dt) {
     Reconstruction_within_cell(g_xif, g_yif, g_fluids, g_block);
     Reconstruction_forg0(g_xif, g_yif, g_fluids, g_block);
     Calculate_flux(g_xfl, g_yfl, g_xif, g_yif, g_block, stage);
-    Update(g_fluids, g_xfl, g_yfl, g_block, stage);
+    if (g_source) Update_with_source(g_fluids, g_xfl, g_yfl, g_block, stage);
+    else Update(g_fluids, g_xfl, g_yfl, g_block, stage);
     if (is_using_df_factor) Update_alpha(g_xif, g_yif, g_fluids, g_block);
     return 0;
 }

@@ -8,7 +8,8 @@ Each case stores the initial conserved/primitive state, the reference state (con
 alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps ("fo_" cases run
 step 0 with First_order_normal / First_order_tangent, as the drivers do when
 is_using_df_factor is set; "ns_" cases use the Navier-Stokes collision time, no-slip walls
-and the Prandtl fix, also with a first-order step 0).
+and the Prandtl fix, also with a first-order step 0; "rt_" is the RT_instability loop with
+Update_with_source).
 
 tests/golden/refapi/ holds runs of the reference-API drivers (tests/refapi/driver2d.cpp,
 driver1d.cpp) linked against the reference's own objects (oracle/Makefile, refdrivers): the
@@ -47,7 +48,7 @@ def step_cases():
                  "tmarch_rk3_lf_w5_24", "tmarch_rk4_gks_w9_24", "tmarch_s2o4_lf_w7_24"):
         yield name, _problem(name)
     for name in ("fo_w5_free_24", "fo_w7_periodic_24", "fo_w9_reflect_24",
-                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w9_nu_24"):
+                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w9_nu_24", "rt_w5_12"):
         yield name, _problem(name)
 
 
@@ -125,9 +126,10 @@ def main(only=None):
     for name, (pb, con, prim) in step_cases():
         if only and not name.startswith(only):
             continue
-        from test_oracle_cpu import first_order_steps
+        from test_oracle_cpu import first_order_steps, with_source
         r = CpuStep("ref").init(pb)
         r.set_state(con, prim)
+        r.fn("set_source")(1 if with_source(name) else 0)
         fo = first_order_steps(name)
         dts = []
         for k in range(3):

@@ -59,9 +59,10 @@ def test_batch_equals_single_problem_solver(precision, graph):
 def _close(got, ref, precision, what=None):
     """The batched face kernels are separate instantiations of the single-problem kernel's
     tile code; nvcc contracts multiply-adds differently in them, so the two agree to rounding:
-    relative to each variable's scale 1e-13 in FP64, 1e-6 in FP32."""
+    relative to each variable's scale 1e-13 in FP64, 1e-5 in FP32 (a few steps of FP32 rounding
+    carried through shocks)."""
     scale = np.maximum(np.abs(ref).max(axis=(0, 1)), 1e-300)
-    tol = 1e-13 if precision == FP64 else 1e-6
+    tol = 1e-13 if precision == FP64 else 1e-5
     assert (np.abs(got - ref) / scale).max() <= tol, what
 
 

@@ -23,9 +23,12 @@ def built():
     ge.build()
 
 
-def gpu_run(pb, con, prim, nsteps, precision=FP64, tstop=1e30, graph=False, alpha=None, first_order_steps=0):
+def gpu_run(pb, con, prim, nsteps, precision=FP64, tstop=1e30, graph=False, alpha=None, first_order_steps=0,
+            source=False):
     s = Solver2D(pb, precision)
     s.set_state(con, prim)
+    if source:
+        s.set_source(True)
     if alpha is not None:
         s.set_alpha(*alpha)
     dts = []
@@ -62,13 +65,13 @@ def _golden_problem(name):
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_gpu_matches_reference_golden(name):
-    from test_oracle_cpu import first_order_steps
+    from test_oracle_cpu import first_order_steps, with_source
     pb, _, _ = _golden_problem(name)
     gold = np.load(GOLDEN / f"{name}.npz")
-    fo = first_order_steps(name)
-    s1 = gpu_run(pb, gold["convar0"], gold["primvar0"], 1, first_order_steps=fo)
+    fo, src = first_order_steps(name), with_source(name)
+    s1 = gpu_run(pb, gold["convar0"], gold["primvar0"], 1, first_order_steps=fo, source=src)
     assert rel_linf(s1["convar"], gold["convar1"], pb) <= TOL_FP64
-    s3 = gpu_run(pb, gold["convar0"], gold["primvar0"], 3, first_order_steps=fo)
+    s3 = gpu_run(pb, gold["convar0"], gold["primvar0"], 3, first_order_steps=fo, source=src)
     assert rel_linf(s3["convar"], gold["convar3"], pb) <= TOL_FP64
     np.testing.assert_allclose(s3["dts"], gold["dts"], rtol=1e-14, atol=0)
     for k in ("alpha_x3", "alpha_y3"):

@@ -14,7 +14,12 @@ STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.
 
 def first_order_steps(name):
     """steps run with first-order reconstruction at the start of a golden case"""
-    return 1 if name.startswith(("fo_", "ns_")) else 0
+    return 1 if name.startswith(("fo_", "ns_", "rt_")) else 0
+
+
+def with_source(name):
+    """cases whose stage update is Update_with_source (the RT_instability driver)"""
+    return name.startswith("rt_")
 
 
 def _problem(name):
@@ -36,6 +41,9 @@ def _problem(name):
         pb, con, prim = cases.random_riemann2d(n, seed=int(w[1]), order=int(w[1]))
         pb.bc = (bc,) * 4
         return pb, con, prim
+    if name.startswith("rt_"):
+        # rt_w5_<nodex>: the RT_instability set-up, first-order step 0, gravity source
+        return cases.rt2d(n, order=5)
     if name.startswith("ns_"):
         # ns_w<order>_<variant>_<n>: Navier-Stokes collision time, first-order step 0
         #   noslip : the viscous_sod_shock_problem set-up (src/2Dproblem.cpp:1095-1160): no-slip
@@ -77,6 +85,7 @@ def test_oracle_matches_golden_bitwise(name):
     gold = np.load(GOLDEN / f"{name}.npz")
     o = CpuStep("oracle").init(pb, threads=4)
     o.set_state(gold["convar0"], gold["primvar0"])
+    o.fn("set_source")(1 if with_source(name) else 0)
     fo = first_order_steps(name)
     dts = []
     for k in range(3):
