@@ -148,7 +148,9 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 // W_old + dt (L + S), S = (0, 0, rho, rho v) of the stage's state; stage 1
                 // leaves the state
                 if (a.stage == 0) {
-                    const double S = v == 2 ? a.W[c] : v == 3 ? a.W[2 * plane + c] : 0.0;
+                    // the stage's state: w0[0] and w0[2] hold rho and rho v read before this
+                    // loop wrote the new values
+                    const double S = v == 2 ? w0[0] : v == 3 ? w0[2] : 0.0;
                     w[v] = old + (total * iarea + a.ctl->dt * S);
                 } else {
                     w[v] = cur;

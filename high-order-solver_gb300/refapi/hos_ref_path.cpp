@@ -459,7 +459,36 @@ void Calculate_flux(Flux2d_gauss**, Flux2d_gauss**, Interface2d*, Interface2d*, 
         stop(HOS_E_CONFIG, "wrong middle stage,pls check the time marching setting");
 }
 
+namespace {
+void update2(Fluid2d* fluids, Block2d block, int stage, bool source);
+}
+
 void Update(Fluid2d* fluids, Flux2d_gauss**, Flux2d_gauss**, Block2d block, int stage) {
+    update2(fluids, block, stage, false);
+}
+
+// the RT_instability loop's update (src/time_advance.cpp:534-704): gravity source, S2O4 stage 0
+void Update_with_source(Fluid2d* fluids, Flux2d_gauss**, Flux2d_gauss**, Block2d block, int stage) {
+    update2(fluids, block, stage, true);
+}
+
+// RT_boundary (src/boundary_condition.cpp:188-242): reflecting left / right, the fixed bottom
+// (rho, u, v, p) = (2, 0, 0, 1) and top (1, 0, 0, 2.5) states
+void RT_boundary(Fluid2d* fluids, Block2d) {
+    Fluid2d bottom, top;
+    const double b[4] = {2.0, 0.0, 0.0, 1.0}, t[4] = {1.0, 0.0, 0.0, 2.5};
+    for (int v = 0; v < 4; ++v) {
+        bottom.primvar[v] = b[v];
+        top.primvar[v] = t[v];
+    }
+    record2(fluids, 0, HOS_BC_REFLECT, nullptr);
+    record2(fluids, 1, HOS_BC_REFLECT, nullptr);
+    record2(fluids, 2, HOS_BC_INFLOW, &bottom);
+    record2(fluids, 3, HOS_BC_INFLOW, &top);
+}
+
+namespace {
+void update2(Fluid2d* fluids, Block2d block, int stage, bool source) {
     Ctx2& c = live2(fluids, "Update");
     if (stage != c.next) stop(HOS_E_CONFIG, "wrong middle stage,pls check the time marching setting");
     if (stage == 0) {
@@ -484,6 +513,7 @@ void Update(Fluid2d* fluids, Flux2d_gauss**, Flux2d_gauss**, Block2d block, int 
         params2(block, &order, &fo);
         if (order != c.order) stop(HOS_E_CONFIG, "the reconstruction order changed under a running solver");
         check2(hos2d_set_reconstruction(c.h, fo ? HOS_RECON_FIRST_ORDER : HOS_RECON_WENO), "Update");
+        check2(hos2d_set_source(c.h, source ? 1 : 0), "Update_with_source");
     }
     apply_boundaries2(c);
     check2(hos2d_stage(c.h, stage), "Update");
@@ -507,6 +537,7 @@ void Update(Fluid2d* fluids, Flux2d_gauss**, Flux2d_gauss**, Block2d block, int 
         if (g_mirror) download2(c, fluids);
     }
 }
+}  // namespace
 
 // fused: the device updates the DF indicators at the end of each stage
 void Update_alpha(Interface2d*, Interface2d*, Fluid2d* fluids, Block2d) { known2(fluids, "Update_alpha"); }

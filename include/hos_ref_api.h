@@ -33,7 +33,8 @@
  * first-order reconstruction (First_order_normal / _tangent, the drivers' step 0), GKS2D with
  * the Euler or NS collision time (Mu / Nu, is_Prandtl_fix / Pr), GKS (1D) and LF2D; S2O4 (1D,
  * 2D) and S1O1, S1O2, RK2, RK3, RK4 (2D); free / periodic / reflective / inflow / no-slip
- * adiabatic boundaries; the output writers.
+ * adiabatic boundaries, RT_boundary, Update_with_source (gravity source, S2O4); the output
+ * writers.
  * Not provided (rejected at the first step): Van Leer reconstruction, GKS2D_smooth, LF2D's
  * viscous term, the 1D LF flux and 1D RK integrators, the 3D C++ API (the 3D path is the C ABI
  * hos3d_*).
@@ -115,6 +116,7 @@ void RK3_2D(Block2d& block);
 void Initial_stages(Block2d& block);
 double Get_CFL(Block2d& block, Fluid2d* fluids, double tstop);
 void Update(Fluid2d* fluids, Flux2d_gauss** xfluxes, Flux2d_gauss** yfluxes, Block2d block, int stage);
+void Update_with_source(Fluid2d* fluids, Flux2d_gauss** xfluxes, Flux2d_gauss** yfluxes, Block2d block, int stage);
 
 /* ---- reconstruction (src/reconstruction.cpp) ---- */
 void Reconstruction_within_cell(Interface1d* interfaces, Fluid1d* fluids, Block1d block);
@@ -194,6 +196,7 @@ void noslip_adiabatic_boundary_left(Fluid2d* fluids, Block2d block, Fluid2d bcva
 void noslip_adiabatic_boundary_right(Fluid2d* fluids, Block2d block, Fluid2d bcvalue);
 void noslip_adiabatic_boundary_down(Fluid2d* fluids, Block2d block, Fluid2d bcvalue);
 void noslip_adiabatic_boundary_up(Fluid2d* fluids, Block2d block, Fluid2d bcvalue);
+void RT_boundary(Fluid2d* fluids, Block2d block);
 
 /* ---- controls of this library (no counterpart in the reference) ---- */
 #define HOS_REF_EXIT 0    /* print and exit(0) where the reference does (default) */

@@ -48,7 +48,7 @@ def step_cases():
                  "tmarch_rk3_lf_w5_24", "tmarch_rk4_gks_w9_24", "tmarch_s2o4_lf_w7_24"):
         yield name, _problem(name)
     for name in ("fo_w5_free_24", "fo_w7_periodic_24", "fo_w9_reflect_24",
-                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w9_nu_24", "rt_w5_12"):
+                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w7_cap_24", "ns_w9_nu_24", "rt_w5_12"):
         yield name, _problem(name)
 
 

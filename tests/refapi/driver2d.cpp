@@ -11,7 +11,8 @@
 // optionally first_order_steps: steps that start with First_order_normal / _tangent, as the
 // reference's drivers do at step 0 when is_using_df_factor is set, src/2Dproblem.cpp:733-745;
 // tau_type (1: NS), mu, nu, prandtl_fix, pr: the collision-time globals; bc names may be
-// noslip, whose wall velocity comes from the side's bcprim entry).
+// noslip, whose wall velocity comes from the side's bcprim entry; source 1: the RT_instability
+// loop, RT_boundary and Update_with_source, src/2Dproblem.cpp:746-763).
 // state_in.bin: convar then primvar, [nx*ny][4] doubles each.  state_out.bin: convar, primvar,
 // alpha_x, alpha_y, then t, the step count and every step's dt.
 #include <cstdio>
@@ -70,10 +71,12 @@ int main(int argc, char** argv) {
     std::map<std::string, BoundaryCondition2d> up = {
         {"free", free_boundary_up}, {"periodic", periodic_boundary_up}, {"reflect", reflection_boundary_up},
         {"inflow", inflow_boundary_up}, {"noslip", noslip_adiabatic_boundary_up}};
-    BoundaryCondition2d leftboundary = low.at(cfg.at("bc")[0]);
-    BoundaryCondition2d rightboundary = high.at(cfg.at("bc")[1]);
-    BoundaryCondition2d downboundary = down.at(cfg.at("bc")[2]);
-    BoundaryCondition2d upboundary = up.at(cfg.at("bc")[3]);
+    const bool source = cfg.count("source") && num("source") != 0;   // the RT_instability loop
+    // (its own RT_boundary fills every side, whose bottom inflow has no side function)
+    BoundaryCondition2d leftboundary = source ? nullptr : low.at(cfg.at("bc")[0]);
+    BoundaryCondition2d rightboundary = source ? nullptr : high.at(cfg.at("bc")[1]);
+    BoundaryCondition2d downboundary = source ? nullptr : down.at(cfg.at("bc")[2]);
+    BoundaryCondition2d upboundary = source ? nullptr : up.at(cfg.at("bc")[3]);
     if (cfg.count("bcprim"))
         for (size_t k = 0; k + 5 <= cfg["bcprim"].size(); k += 5) {
             const int side = (int)num("bcprim", (int)k);
@@ -168,15 +171,20 @@ int main(int argc, char** argv) {
                 }
             }
             for (int i = 0; i < block.stages; i++) {
-                leftboundary(fluids, block, bcvalue[0]);
-                rightboundary(fluids, block, bcvalue[1]);
-                downboundary(fluids, block, bcvalue[2]);
-                upboundary(fluids, block, bcvalue[3]);
+                if (source) {
+                    RT_boundary(fluids, block);
+                } else {
+                    leftboundary(fluids, block, bcvalue[0]);
+                    rightboundary(fluids, block, bcvalue[1]);
+                    downboundary(fluids, block, bcvalue[2]);
+                    upboundary(fluids, block, bcvalue[3]);
+                }
                 Convar_to_Primvar(fluids, block);
                 Reconstruction_within_cell(xinterfaces, yinterfaces, fluids, block);
                 Reconstruction_forg0(xinterfaces, yinterfaces, fluids, block);
                 Calculate_flux(xfluxes, yfluxes, xinterfaces, yinterfaces, block, i);
-                Update(fluids, xfluxes, yfluxes, block, i);
+                if (source) Update_with_source(fluids, xfluxes, yfluxes, block, i);
+                else Update(fluids, xfluxes, yfluxes, block, i);
                 if (is_using_df_factor) Update_alpha(xinterfaces, yinterfaces, fluids, block);
             }
             block.step++;

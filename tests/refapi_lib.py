@@ -41,6 +41,8 @@ def config2d(pb, steps: int, tstop: float = 1e30, precision: int = 0, mirror: in
              f"steps {steps}", f"tstop {tstop!r}", f"precision {precision}", f"mirror {mirror}"]
     if getattr(pb, "first_order_steps", 0):
         lines.append(f"first_order_steps {pb.first_order_steps}")
+    if getattr(pb, "source", False):
+        lines.append("source 1")
     if getattr(pb, "tau_type", 0):
         lines += [f"tau_type {pb.tau_type}", f"mu {pb.mu!r}", f"nu {pb.nu!r}",
                   f"prandtl_fix {int(pb.prandtl_fix)}", f"pr {pb.prandtl!r}"]
@@ -117,7 +119,11 @@ def refapi_cases_2d():
     ns[0].bc = ("noslip", "noslip", "noslip", "reflect")
     ns[0].tau_type, ns[0].mu, ns[0].c2_euler = 1, 1e-3, 9.0
     ns[0].first_order_steps = 1
+    # the RT_instability loop (src/2Dproblem.cpp:699-763): RT_boundary, Update_with_source
+    rt = cases.rt2d(12)
+    rt[0].source, rt[0].first_order_steps = True, 1
     return [("refapi_riemann_w7_24", cases.riemann2d(24, order=7), 5),
+            ("refapi_rt_w5_12", rt, 4),
             ("refapi_fo_w9_reflect_20", fo, 4),
             ("refapi_ns_noslip_w5_20", ns, 4),
             ("refapi_inflow_reflect_w5_20", inflow, 5),

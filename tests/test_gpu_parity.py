@@ -55,6 +55,12 @@ def oracle_run(pb, con, prim, nsteps, tstop=1e30):
     return st
 
 
+# The viscous-cap case: the reference algorithm itself carries a 1e-15 relative perturbation
+# of the initial state to ~4e-12 after three steps there (tau_num >> dt in the GKS time
+# coefficients; test_oracle_cpu.test_viscous_cap_case_amplifies_rounding), so after three steps
+# it is held to the rounding it amplifies; after one step to 1e-12 like every case.
+TOL_AFTER_3 = {"ns_w7_cap_24": 1e-10}
+
 GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem)
 
 
@@ -72,7 +78,7 @@ def test_gpu_matches_reference_golden(name):
     s1 = gpu_run(pb, gold["convar0"], gold["primvar0"], 1, first_order_steps=fo, source=src)
     assert rel_linf(s1["convar"], gold["convar1"], pb) <= TOL_FP64
     s3 = gpu_run(pb, gold["convar0"], gold["primvar0"], 3, first_order_steps=fo, source=src)
-    assert rel_linf(s3["convar"], gold["convar3"], pb) <= TOL_FP64
+    assert rel_linf(s3["convar"], gold["convar3"], pb) <= TOL_AFTER_3.get(name, TOL_FP64)
     np.testing.assert_allclose(s3["dts"], gold["dts"], rtol=1e-14, atol=0)
     for k in ("alpha_x3", "alpha_y3"):
         a, b = s3[k[:-1]], gold[k]

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from hos_gb300 import cases
-from oracle_lib import CpuStep, ref_available, interior
+from oracle_lib import CpuStep, interior, ref_available, rel_linf
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem)
@@ -48,7 +48,8 @@ def _problem(name):
         # ns_w<order>_<variant>_<n>: Navier-Stokes collision time, first-order step 0
         #   noslip : the viscous_sod_shock_problem set-up (src/2Dproblem.cpp:1095-1160): no-slip
         #            adiabatic left/right/bottom, reflecting top, Mu = 1e-3, c2 = 9
-        #   wall   : moving no-slip walls, Prandtl fix (Pr = 0.72), Mu = 0.05 (viscous dt cap)
+        #   wall   : moving no-slip walls, Prandtl fix (Pr = 0.72), Mu = 0.01, c2 = 1
+        #   cap    : as wall with Mu = 0.05, c2 = 9: the viscous dt cap decides every step
         #   nu     : kinematic viscosity Nu = 2e-3 (Mu unset), periodic
         _, w, variant, _ = name.split("_")
         order = int(w[1])
@@ -56,8 +57,9 @@ def _problem(name):
         pb.tau_type, pb.c2_euler = 1, 9.0
         if variant == "noslip":
             pb.bc, pb.mu = ("noslip", "noslip", "noslip", "reflect"), 1e-3
-        elif variant == "wall":
-            pb.bc, pb.mu, pb.prandtl_fix, pb.prandtl = ("noslip",) * 4, 0.05, True, 0.72
+        elif variant in ("wall", "cap"):
+            pb.bc, pb.prandtl_fix, pb.prandtl = ("noslip",) * 4, True, 0.72
+            pb.mu, pb.c2_euler = (0.01, 1.0) if variant == "wall" else (0.05, 9.0)
             pb.bc_prim = ((0.0, 0.0, 0.2, 0.0), (0.0, 0.0, -0.1, 0.0), (0.0, 0.3, 0.0, 0.0), (0.0, -0.25, 0.0, 0.0))
         else:
             pb.bc, pb.mu, pb.nu = ("periodic",) * 4, -1.0, 2e-3
@@ -186,3 +188,19 @@ def test_oblique_shock_states_reduce_to_reference_constants():
     m2 = 100.0
     assert abs(rho1 * (g + 1) * m2 / ((g - 1) * m2 + 2) - 8.0) < 1e-12
     assert abs(p1 * (2 * g * m2 - (g - 1)) / (g + 1) - 116.5) < 1e-12
+
+
+def test_viscous_cap_case_amplifies_rounding():
+    """In the viscous-cap case the algorithm amplifies rounding: a 1e-15 relative perturbation
+    of the initial state grows past 1e-13 within three steps (the GKS time coefficients
+    with tau_num >> dt cancel), which bounds how closely any other arithmetic can follow it."""
+    pb, con, prim = _problem("ns_w7_cap_24")
+    runs = []
+    for eps in (0.0, 1e-15):
+        o = CpuStep("oracle").init(pb, threads=4)
+        o.set_state(con * (1 + eps * np.sin(np.arange(con.size).reshape(con.shape))), prim)
+        for k in range(3):
+            o.fn("set_first_order")(1 if k == 0 else 0)
+            o.step()
+        runs.append(o.state()["convar"])
+    assert rel_linf(runs[1], runs[0], pb) > 1e-13

@@ -88,8 +88,8 @@ def test_driver_reports_a_missing_gpu_as_the_reference_api_error(tmp_path):
         run2d(exe, pb, con, prim, config2d(pb, 1))
 
 
-@pytest.mark.parametrize("name", ["refapi_riemann_w7_24", "refapi_fo_w9_reflect_20", "refapi_ns_noslip_w5_20",
-                                  "refapi_inflow_reflect_w5_20", "refapi_vortex_w9_20"])
+@pytest.mark.parametrize("name", ["refapi_riemann_w7_24", "refapi_rt_w5_12", "refapi_fo_w9_reflect_20",
+                                  "refapi_ns_noslip_w5_20", "refapi_inflow_reflect_w5_20", "refapi_vortex_w9_20"])
 def test_refapi_fixture_equals_the_oracle(name):
     """The reference run of the same driver loop equals the oracle bit for bit."""
     from oracle_lib import CpuStep
@@ -99,6 +99,7 @@ def test_refapi_fixture_equals_the_oracle(name):
     gold = np.load(GOLDEN / f"{name}.npz")
     o = CpuStep("oracle").init(pb)
     o.set_state(gold["convar0"], gold["primvar0"])
+    o.fn("set_source")(1 if getattr(pb, "source", False) else 0)
     fo = getattr(pb, "first_order_steps", 0)
     dts = []
     for k in range(steps):
