@@ -273,10 +273,10 @@ __device__ __forceinline__ T tau_num_ns(const NsParam<T>& q, T ratio, T dt, T d0
 
 // GKS2D with the Navier-Stokes collision time at one Gauss point: the full set of
 // time-integration coefficients with tau != 0 (src/flux_function.cpp:410-690), including the
-// <A u> half-space terms of both sides and the Prandtl fix of the energy flux.  Kept out of
-// line: the Euler path above stays the hot path's code.
+// <A u> half-space terms of both sides and the Prandtl fix of the energy flux.  The face
+// kernel branches between this and the Euler form once per launch (tau_type is uniform).
 template <class T>
-__device__ __noinline__ void gks_point_ns(const GState<T>& L, const GState<T>& R, T dt, T K, const NsParam<T> q,
+__device__ __forceinline__ void gks_point_ns(const GState<T>& L, const GState<T>& R, T dt, T K, const NsParam<T> q,
                                           T* fo, T* dfo) {
     const GasK<T> gk(K);
     T pl[4], pr[4], p0[4];
