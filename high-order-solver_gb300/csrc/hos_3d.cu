@@ -14,6 +14,7 @@
 #include <string>
 
 #include "../../include/hos_gb300.h"
+#include "hos_3d_gate.cuh"
 #include "hos_3d_launch.h"
 
 namespace hos {
@@ -33,7 +34,7 @@ __device__ __forceinline__ int bc_src3(int x, int n, int g, int kind, bool low, 
 }
 
 __global__ void __launch_bounds__(256) bc3_kernel(double* __restrict__ W, Geo3 g, const Ctl3* ctl) {
-    if (!ctl->active) return;
+    if (ctl && !ctl->active) return;
     const size_t plane = (size_t)g.nx * g.ny * g.nz;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= plane) return;
@@ -230,6 +231,15 @@ struct hos_solver3d {
     Ctl3* ctl = nullptr;
     bool first = true;
     size_t ncell = 0;
+    // learned gate (FP32): flags per cell, counters, the network's inference copy
+    bool gated = false;
+    unsigned char* gflags = nullptr;
+    float2* grp = nullptr;
+    Stats3* gstats = nullptr;
+    __nv_bfloat16* gw = nullptr;
+    float* gb = nullptr;
+    float gthreshold = 0.0f;
+    unsigned gaudit_mask = 0, gseed = 1;
 };
 
 namespace {
@@ -240,6 +250,9 @@ void free3(hos_solver3d* s) {
         if (x) cudaFree(x);
     if (s->FV) cudaFree(s->FV);
     if (s->LV) cudaFree(s->LV);
+    void* gbufs[] = {s->gflags, s->grp, s->gstats, s->gw, s->gb};
+    for (void* x : gbufs)
+        if (x) cudaFree(x);
     if (s->ctl) cudaFree(s->ctl);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
@@ -260,9 +273,22 @@ Dir3 make_dir(const Geo3& g, int dir) {
 
 cudaError_t flux_dir(hos_solver3d* s, int dir, int stage, cudaEvent_t* ev) {
     const Dir3& d = s->dirs[dir];
+    const Gate3 gt{s->gated ? s->gflags : nullptr, s->gated ? &s->gstats->fallback : nullptr};
     if (s->precision == HOS_FP32)
-        return launch_flux3<float>(s->W, (float*)s->FV, (float*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream, ev);
-    return launch_flux3<double>(s->W, (double*)s->FV, (double*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream, ev);
+        return launch_flux3<float>(s->W, (float*)s->FV, (float*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream, ev,
+                                   gt);
+    return launch_flux3<double>(s->W, (double*)s->FV, (double*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream, ev,
+                                gt);
+}
+
+GateRun3 gate_run(hos_solver3d* s, const gate::Net& net) {
+    GateRun3 r{};
+    r.W = s->W;
+    r.rp = s->grp;
+    r.g = s->geo;
+    r.net = net;
+    r.ctl = s->ctl;
+    return r;
 }
 
 unsigned blocks(size_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
@@ -275,21 +301,33 @@ int enqueue_begin3(hos_solver3d* s, double tstop, cudaEvent_t ev) {
     return e == cudaSuccess ? HOS_OK : fail3(HOS_E_CUDA, std::string("begin3: ") + cudaGetErrorString(e));
 }
 
-// ev (may be null): 11 events, after the boundaries, after face/line/point of x, then of y,
-// then of z, and after the update
+// ev (may be null): 12 events, after the boundaries, after the gate (recorded without a launch
+// when the solver has no gate), after face/line/point of x, then of y, then of z, and after the
+// update
 int enqueue_stage3(hos_solver3d* s, int stage, cudaEvent_t* ev) {
     const Geo3& g = s->geo;
     bc3_kernel<<<blocks((size_t)g.nx * g.ny * g.nz, 256), 256, 0, s->stream>>>(s->W, g, s->ctl);
     if (ev) cudaEventRecord(ev[0], s->stream);
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && s->gated) {
+        GateRun3 r = gate_run(s, gate::Net{s->gw, s->gw + gate::NH * gate::NF, s->gw + gate::NH * gate::NF + gate::NH * gate::NH,
+                                           s->gb, s->gb + gate::NH, s->gb + 2 * gate::NH});
+        r.flags = s->gflags;
+        r.stats = s->gstats;
+        r.threshold = s->gthreshold;
+        r.audit_mask = s->gaudit_mask;
+        r.seed = s->gseed++;
+        e = launch_gate3(r, s->stream);
+    }
+    if (ev) cudaEventRecord(ev[1], s->stream);
     for (int dir = 0; dir < 3 && e == cudaSuccess; ++dir) {
-        e = flux_dir(s, dir, stage, ev ? ev + 1 + 3 * dir : nullptr);
+        e = flux_dir(s, dir, stage, ev ? ev + 2 + 3 * dir : nullptr);
     }
     if (e != cudaSuccess) return fail3(HOS_E_CUDA, std::string("flux3: ") + cudaGetErrorString(e));
     const size_t nc = (size_t)g.nodex * g.nodey * g.nodez;
     update3_kernel<<<blocks(nc, 256), 256, 0, s->stream>>>(s->W, s->Wold, s->FS[0], s->FS[1], s->FS[2], s->ctl, g,
                                                            s->dirs[0].fs, s->dirs[1].fs, s->dirs[2].fs, stage);
-    if (ev) cudaEventRecord(ev[10], s->stream);
+    if (ev) cudaEventRecord(ev[11], s->stream);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail3(HOS_E_CUDA, std::string("update3: ") + cudaGetErrorString(e));
     return HOS_OK;
 }
@@ -503,18 +541,88 @@ int hos3d_stream(hos_solver3d* s, void** stream) {
 }
 
 int hos3d_profile_step(hos_solver3d* s, double tstop, float* ms, int n) {
-    if (!s || !ms || n < 23) return fail3(HOS_E_ARG, "need 23 timings");
-    cudaEvent_t ev[24];
+    if (!s || !ms || n < 25) return fail3(HOS_E_ARG, "need 25 timings");
+    cudaEvent_t ev[26];
     for (auto& x : ev) cudaEventCreate(&x);
     cudaEventRecord(ev[0], s->stream);
     int st = enqueue_begin3(s, tstop, ev[1]);
-    for (int stage = 0; stage < 2 && !st; ++stage) st = enqueue_stage3(s, stage, ev + 2 + 11 * stage);
+    for (int stage = 0; stage < 2 && !st; ++stage) st = enqueue_stage3(s, stage, ev + 2 + 12 * stage);
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (!st && e == cudaSuccess)
-        for (int k = 0; k < 23; ++k) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+        for (int k = 0; k < 25; ++k) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
     for (auto& x : ev) cudaEventDestroy(x);
     if (st) return st;
     return e == cudaSuccess ? HOS_OK : fail3(HOS_E_CUDA, std::string("profile: ") + cudaGetErrorString(e));
+}
+
+int hos3d_set_gate(hos_solver3d* s, const hos_gate* g, float threshold, int audit_log2) {
+    using namespace gate;
+    if (!s) return fail3(HOS_E_ARG, "null solver");
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fail3(HOS_E_CUDA, std::string("set_gate: ") + cudaGetErrorString(e));
+    if (!g) {
+        s->gated = false;
+        return HOS_OK;
+    }
+    if (s->precision != HOS_FP32) return fail3(HOS_E_CONFIG, "the learned gate runs on the FP32-bulk path");
+    if (audit_log2 < 0 || audit_log2 > 31) return fail3(HOS_E_ARG, "audit_log2 must be 0..31");
+    if (!s->grp && (e = cudaMalloc(&s->grp, s->ncell * sizeof(float2))) != cudaSuccess)
+        return fail3(HOS_E_NOMEM, std::string("gate buffers: ") + cudaGetErrorString(e));
+    if (!s->gflags) {
+        if ((e = cudaMalloc(&s->gflags, s->ncell)) == cudaSuccess && (e = cudaMalloc(&s->gstats, sizeof(Stats3))) == cudaSuccess &&
+            (e = cudaMalloc(&s->gw, NET_BF16 * sizeof(__nv_bfloat16))) == cudaSuccess)
+            e = cudaMalloc(&s->gb, NET_F32 * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(s->gstats, 0, sizeof(Stats3));
+        if (e != cudaSuccess) return fail3(HOS_E_NOMEM, std::string("gate buffers: ") + cudaGetErrorString(e));
+    }
+    // the solver keeps its own copy of the network, which can go on training
+    if ((e = cudaStreamSynchronize(g->stream)) == cudaSuccess &&
+        (e = cudaMemcpy(s->gw, g->wbf, NET_BF16 * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice)) == cudaSuccess)
+        e = cudaMemcpy(s->gb, g->bias, NET_F32 * sizeof(float), cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) return fail3(HOS_E_CUDA, std::string("set_gate copy: ") + cudaGetErrorString(e));
+    s->gthreshold = threshold;
+    s->gaudit_mask = audit_log2 == 31 ? 0xffffffffu : (1u << audit_log2) - 1u;
+    s->gated = true;
+    return HOS_OK;
+}
+
+int hos3d_gate_stats(hos_solver3d* s, unsigned long long* stats, int reset) {
+    if (!s || !stats) return fail3(HOS_E_ARG, "null argument");
+    if (!s->gstats) {
+        std::memset(stats, 0, 10 * sizeof(unsigned long long));
+        return HOS_OK;
+    }
+    Stats3 st;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, s->gstats, sizeof st, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(s->gstats, 0, sizeof st);
+    if (e != cudaSuccess) return fail3(HOS_E_CUDA, std::string("gate_stats: ") + cudaGetErrorString(e));
+    const unsigned long long v[10] = {st.cells[0], st.cells[1], st.cells[2], st.smooth[0], st.smooth[1], st.smooth[2],
+                                      st.audited, st.false_neg, st.fallback, 0};
+    std::memcpy(stats, v, sizeof v);
+    return HOS_OK;
+}
+
+int hos_gate_collect3d(hos_gate* g, hos_solver3d* s, int sample_log2) {
+    using namespace gate;
+    if (!g || !s || sample_log2 < 0 || sample_log2 > 31) return fail3(HOS_E_ARG, "bad argument");
+    if (!g->samples) return fail3(HOS_E_CONFIG, "the gate was created without sample capacity");
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && !s->grp) e = cudaMalloc(&s->grp, s->ncell * sizeof(float2));
+    if (e != cudaSuccess) return fail3(HOS_E_NOMEM, std::string("gate collect: ") + cudaGetErrorString(e));
+    const Geo3& geo = s->geo;
+    bc3_kernel<<<blocks((size_t)geo.nx * geo.ny * geo.nz, 256), 256, 0, s->stream>>>(s->W, geo, nullptr);
+    GateRun3 r = gate_run(s, g->net());
+    r.ctl = nullptr;
+    r.seed = g->collect_seed++;
+    r.samples = g->samples;
+    r.capacity = g->capacity;
+    r.sample_count = &g->stats->samples;
+    r.sample_mask = sample_log2 == 31 ? 0xffffffffu : (1u << sample_log2) - 1u;
+    e = cudaStreamSynchronize(g->stream);   // the network's copy is current
+    if (e == cudaSuccess) e = launch_gate3(r, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? HOS_OK : fail3(HOS_E_CUDA, std::string("gate collect: ") + cudaGetErrorString(e));
 }
 
 }  // extern "C"

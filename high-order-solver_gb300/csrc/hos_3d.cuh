@@ -166,7 +166,13 @@ __device__ __forceinline__ void weights5(const T* s, T eps, T* fw) {
     const T d0 = T(0.5) * T(0.15) * T(0.15), d1 = T(0.15) * T(0.85), d3 = T(0.85);
     T b[4];
     beta3<T>(s, b);
-    b[3] = beta5_big(s[0], s[1], s[2], s[3], s[4]);
+    if constexpr (sizeof(T) == 4) {
+        // the big-stencil indicator expands into terms ~1e5 w^2 that cancel; it depends on
+        // differences only, so FP32 evaluates it about the centre value
+        b[3] = beta5_big(s[0] - s[2], s[1] - s[2], T(0), s[3] - s[2], s[4] - s[2]);
+    } else {
+        b[3] = beta5_big(s[0], s[1], s[2], s[3], s[4]);
+    }
     const T tau = T(1.0 / 3.0) * (fabsT(b[3] - b[0]) + fabsT(b[3] - b[1]) + fabsT(b[3] - b[2]));
     T al[4];
     const T dd[4] = {d0, d1, d0, d3};
@@ -488,6 +494,63 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
     }
 }
 
+// ---- learned gate (FP32 path): linear reconstructions and their check --------------------
+// Per cell one flag byte, bit a set when the gate predicts the WENO5-AO weights of the cell's
+// stencil along global axis a (0 x, 1 y, 2 z) to stay near the linear weights.  Flagged
+// reconstructions take the big-stencil polynomial alone in conservative variables (the linear
+// weights select it, and a linear reconstruction commutes with the characteristic projection);
+// a result that fails the check below takes the full WENO5-AO path.
+struct Gate3 {
+    const unsigned char* flags;    // null: no gate
+    unsigned long long* fallback;  // linear results the check rejected
+};
+// global axis of a direction's normal (k 0), first (1) and second (2) tangential sweep
+__host__ __device__ constexpr int axis3(int dir, int k) {
+    return k == 0 ? dir : k == 1 ? (dir == 1 ? 0 : 1) : (dir == 2 ? 0 : 2);
+}
+// value and slope of the big-stencil polynomial at the left (side 0) or right face
+template <class T>
+__device__ __forceinline__ void lin5_face(int side, const T* s, T ih, T& var, T& der) {
+    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+    if (side == 0) {
+        var = T(1.0 / 60.0) * (T(47) * w0 + T(27) * wn1 - T(3) * wn2 - T(13) * wp1 + T(2) * wp2);
+        der = (T(15) * w0 - T(15) * wn1 + wn2 - wp1) * (T(1.0 / 12.0) * ih);
+    } else {
+        var = T(1.0 / 60.0) * (T(47) * w0 - T(13) * wn1 + T(2) * wn2 + T(27) * wp1 - T(3) * wp2);
+        der = (T(-15) * w0 + wn1 + T(15) * wp1 - wp2) * (T(1.0 / 12.0) * ih);
+    }
+}
+// the big-stencil polynomial at the two Gauss points (and its slope when DER)
+template <class T, bool DER>
+__device__ __forceinline__ void lin5_2g(const T* s, T ih, T* g, T* gx) {
+    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+    const T r3 = T(1.732050807568877294);
+    g[0] = (T(4314) * w0 + (T(4) + T(500) * r3) * wn1 - wn2 - T(70) * r3 * wn2 + T(4) * wp1 - T(500) * r3 * wp1 - wp2
+            + T(70) * r3 * wp2) * T(1.0 / 4320.0);
+    g[1] = (T(4314) * w0 + (T(4) - T(500) * r3) * wn1 - wn2 + T(70) * r3 * wn2 + T(4) * wp1 + T(500) * r3 * wp1 - wp2
+            - T(70) * r3 * wp2) * T(1.0 / 4320.0);
+    if (DER) {
+        const T i108h = ih * T(1.0 / 108.0);
+        gx[0] = (T(48) * r3 * w0 - T(72) * wn1 - T(26) * r3 * wn1 + T(9) * wn2 + T(2) * r3 * wn2 + T(72) * wp1
+                 - T(26) * r3 * wp1 - T(9) * wp2 + T(2) * r3 * wp2) * i108h;
+        gx[1] = -(T(48) * r3 * w0 + T(72) * wn1 - T(26) * r3 * wn1 - T(9) * wn2 + T(2) * r3 * wn2 - T(72) * wp1
+                  - T(26) * r3 * wp1 + T(9) * wp2 + T(2) * r3 * wp2) * i108h;
+    }
+}
+// a linear result is kept when it has a positive temperature and its density and total energy
+// lie within the three central stencil states' range widened by a tenth of that range
+template <class T>
+__device__ __forceinline__ bool lin5_ok(const T* q, const T* wm, const T* w0, const T* wp, T K) {
+    if (reduce5<T>(q, K)) return false;
+#pragma unroll
+    for (int v = 0; v < 5; v += 4) {
+        const T lo = fminT(fminT(wm[v], w0[v]), wp[v]), hi = fmaxT(fmaxT(wm[v], w0[v]), wp[v]);
+        const T m = T(0.1) * (hi - lo) + T(1e-6) * fabsT(w0[v]);
+        if (!(q[v] >= lo - m && q[v] <= hi + m)) return false;
+    }
+    return true;
+}
+
 // ---- kernels ---------------------------------------------------------------------------
 constexpr int FACE3_THREADS = 128;
 constexpr int LINE3_THREADS = 128;
@@ -498,9 +561,9 @@ constexpr int POINT3_THREADS = 128;
 // left-hand state of face a+1), WENO5_AO (src/reconstruction.cpp:3803-3925).  The two values
 // fall back to the cell average with zero slope when either has a non-positive lambda.
 // FV planes: q 0..4 left-hand value, 5..9 its normal slope, 10..14 right-hand value, 15..19.
-template <class T>
+template <class T, bool GATED = false>
 __global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const double* __restrict__ W, T* __restrict__ FV,
-                                                              Geo3 g, Dir3 d, const Ctl3* ctl) {
+                                                              Geo3 g, Dir3 d, const Ctl3* ctl, Gate3 gt) {
     if (!ctl->active) return;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.cel.n()) return;
@@ -522,8 +585,23 @@ __global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const double* __re
 #pragma unroll
     for (int m = 0; m < 3; ++m) prim5<T>(pr[m], st[1 + m], gamma);
     T oc[2][5], od[2][5];
+    bool lin = false;
+    if constexpr (GATED) {
+        const size_t cc = cell_of(g, d.dir, ac + G, b0 - 2 + G, c0 - 2 + G);
+        if ((gt.flags[cc] >> axis3(d.dir, 0)) & 1) {
 #pragma unroll
-    for (int side = 0; side < 2; ++side) {
+            for (int side = 0; side < 2; ++side)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const T s5[5] = {st[0][v], st[1][v], st[2][v], st[3][v], st[4][v]};
+                    lin5_face<T>(side, s5, ih, oc[side][v], od[side][v]);
+                }
+            lin = lin5_ok<T>(oc[0], st[1], st[2], st[3], K) && lin5_ok<T>(oc[1], st[1], st[2], st[3], K);
+            if (!lin) atomicAdd(gt.fallback, 1ull);
+        }
+    }
+#pragma unroll
+    for (int side = 0; side < 2 && !lin; ++side) {
         T s5[5][5];
         Char5<T> ch;
         if (g.characteristic) {
@@ -641,9 +719,9 @@ __device__ __forceinline__ void sweep_side(const T (*st)[NQ][5], T ih, const Geo
 // along b of the face values of both sides to the two Gauss lines, with the order reduction
 // of the position (any non-positive lambda: both lines take the face values, zero slope).
 // LV planes [ig][side][value 5 | normal slope 5 | t1 slope 5].
-template <class T>
+template <class T, bool GATED = false>
 __global__ void __launch_bounds__(LINE3_THREADS) line3_kernel(const T* __restrict__ FV, T* __restrict__ LV, Geo3 g,
-                                                              Dir3 d, const Ctl3* ctl) {
+                                                              Dir3 d, const Ctl3* ctl, Gate3 gt) {
     if (!ctl->active) return;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.lv.n()) return;
@@ -665,7 +743,31 @@ __global__ void __launch_bounds__(LINE3_THREADS) line3_kernel(const T* __restric
             }
         }
         T out[2][3][5];
-        sweep_side<T, 2>(st, ih, g, out);
+        bool lin = false;
+        if constexpr (GATED) {
+            // the side's cell, smooth along this sweep's axis: the big-stencil polynomial
+            const size_t cc = cell_of(g, d.dir, a - 1 + side + g.g, b + g.g, c - 2 + g.g);
+            if ((gt.flags[cc] >> axis3(d.dir, 1)) & 1) {
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const T s0[5] = {st[0][0][v], st[1][0][v], st[2][0][v], st[3][0][v], st[4][0][v]};
+                    const T s1[5] = {st[0][1][v], st[1][1][v], st[2][1][v], st[3][1][v], st[4][1][v]};
+                    T gv[2], gx[2], gd[2];
+                    lin5_2g<T, true>(s0, ih, gv, gx);
+                    lin5_2g<T, false>(s1, ih, gd, gd);
+#pragma unroll
+                    for (int ig = 0; ig < 2; ++ig) {
+                        out[ig][0][v] = gv[ig];
+                        out[ig][2][v] = gx[ig];
+                        out[ig][1][v] = gd[ig];
+                    }
+                }
+                lin = lin5_ok<T>(out[0][0], st[1][0], st[2][0], st[3][0], K) &&
+                      lin5_ok<T>(out[1][0], st[1][0], st[2][0], st[3][0], K);
+                if (!lin) atomicAdd(gt.fallback, 1ull);
+            }
+        }
+        if (!lin) sweep_side<T, 2>(st, ih, g, out);
 #pragma unroll
         for (int ig = 0; ig < 2; ++ig) {
             reduce = reduce || reduce5<T>(out[ig][0], K);
@@ -695,9 +797,9 @@ __global__ void __launch_bounds__(LINE3_THREADS) line3_kernel(const T* __restric
 // combined flux, 1/2 f0 + 1/8 derf0 at stage 0 and (f0 + 1/6 derf0) + (0 f1 + 1/3 derf1) at
 // stage 1, whose first part stage 0 leaves in FS[1][v][face].  Face frame.  T = float runs
 // three 128-thread CTAs per SM (168 registers).
-template <class T>
+template <class T, bool GATED = false>
 __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3_kernel(const T* __restrict__ LV, double* __restrict__ FS,
-                                                                Geo3 g, Dir3 d, const Ctl3* ctl, int stage) {
+                                                                Geo3 g, Dir3 d, const Ctl3* ctl, int stage, Gate3 gt) {
     if (!ctl->active) return;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t nfs = d.fs.n(), nlv = d.lv.n();
@@ -726,7 +828,33 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
                     for (int v = 0; v < 5; ++v) st[m][q][v] = LV[(((ig * 2 + side) * 3 + q) * 5 + v) * nlv + l];
             }
             T out[2][4][5];
-            sweep_side<T, 3>(st, ih, g, out);
+            bool lin = false;
+            if constexpr (GATED) {
+                const size_t cc = cell_of(g, d.dir, a - 1 + side + g.g, b + g.g, c + g.g);
+                if ((gt.flags[cc] >> axis3(d.dir, 2)) & 1) {
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        T sv[5], gv[2], gx[2];
+#pragma unroll
+                        for (int m = 0; m < 5; ++m) sv[m] = st[m][0][v];
+                        lin5_2g<T, true>(sv, ih, gv, gx);
+#pragma unroll
+                        for (int ig = 0; ig < 2; ++ig) { out[ig][0][v] = gv[ig]; out[ig][3][v] = gx[ig]; }
+#pragma unroll
+                        for (int q = 1; q < 3; ++q) {
+#pragma unroll
+                            for (int m = 0; m < 5; ++m) sv[m] = st[m][q][v];
+                            lin5_2g<T, false>(sv, ih, gv, gx);
+                            out[0][q][v] = gv[0];
+                            out[1][q][v] = gv[1];
+                        }
+                    }
+                    lin = lin5_ok<T>(out[0][0], st[1][0], st[2][0], st[3][0], K) &&
+                          lin5_ok<T>(out[1][0], st[1][0], st[2][0], st[3][0], K);
+                    if (!lin) atomicAdd(gt.fallback, 1ull);
+                }
+            }
+            if (!lin) sweep_side<T, 3>(st, ih, g, out);
 #pragma unroll
             for (int ip = 0; ip < 2; ++ip) {
                 reduce = reduce || reduce5<T>(out[ip][0], K);

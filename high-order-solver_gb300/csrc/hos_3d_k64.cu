@@ -6,14 +6,15 @@ namespace d3 {
 
 template <>
 cudaError_t launch_flux3<double>(const double* W, double* FV, double* LV, double* FS, const Geo3& g, const Dir3& d,
-                              const Ctl3* ctl, int stage, cudaStream_t s, cudaEvent_t* ev) {
+                              const Ctl3* ctl, int stage, cudaStream_t s, cudaEvent_t* ev, Gate3 gt) {
+    if (gt.flags) return cudaErrorInvalidValue;   // the gate runs on the FP32-bulk path only
     const size_t nc = d.cel.n(), nl = d.lv.n(), np = 2 * d.fs.n();
-    face3_kernel<double><<<(unsigned)((nc + FACE3_THREADS - 1) / FACE3_THREADS), FACE3_THREADS, 0, s>>>(W, FV, g, d, ctl);
+    face3_kernel<double><<<(unsigned)((nc + FACE3_THREADS - 1) / FACE3_THREADS), FACE3_THREADS, 0, s>>>(W, FV, g, d, ctl, gt);
     if (ev) cudaEventRecord(ev[0], s);
-    line3_kernel<double><<<(unsigned)((nl + LINE3_THREADS - 1) / LINE3_THREADS), LINE3_THREADS, 0, s>>>(FV, LV, g, d, ctl);
+    line3_kernel<double><<<(unsigned)((nl + LINE3_THREADS - 1) / LINE3_THREADS), LINE3_THREADS, 0, s>>>(FV, LV, g, d, ctl, gt);
     if (ev) cudaEventRecord(ev[1], s);
     point3_kernel<double><<<(unsigned)((np + POINT3_THREADS - 1) / POINT3_THREADS), POINT3_THREADS, 0, s>>>(LV, FS, g, d, ctl,
-                                                                                                     stage);
+                                                                                                       stage, gt);
     if (ev) cudaEventRecord(ev[2], s);
     return cudaGetLastError();
 }

@@ -207,8 +207,8 @@ int hos_batch2d_create(const hos_params2d* params, const double* tstop, int coun
             return failb(HOS_E_CONFIG, "problem " + std::to_string(k) + ": bad order/gausspoint/ghost/size");
         for (int s = 0; s < 4; ++s)
             if (p.bc[s] < 0 || p.bc[s] > 5) return failb(HOS_E_CONFIG, "bad boundary kind");
-        if (p.integrator != HOS_INT_S2O4 || p.flux != HOS_FLUX_GKS)
-            return failb(HOS_E_CONFIG, "batches run S2O4 with the GKS flux");
+        if (p.integrator != HOS_INT_S2O4 || p.flux != HOS_FLUX_GKS || p.tau_type != HOS_TAU_EULER)
+            return failb(HOS_E_CONFIG, "batches run S2O4 with the Euler GKS flux");
         if (p.bc[0] >= 4 || p.bc[1] >= 4 || p.bc[2] == HOS_BC_WEDGE_TOP || p.bc[3] == HOS_BC_WEDGE_BOTTOM ||
             ((p.bc[2] >= 4 || p.bc[3] >= 4) && p.bc[0] != HOS_BC_INFLOW))
             return failb(HOS_E_CONFIG, "bad wedge boundary placement");

@@ -219,7 +219,7 @@ __device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, 
 // One tile of faces: N0, T0 are the first face indices along the normal and the tangent.
 // GATED (FP32 only): cells the learned gate marks smooth reconstruct with the full-stencil
 // polynomial alone; see hos_gate.cuh.
-template <class T, int ORDER, int DIR, class TS, bool GATED = false>
+template <class T, int ORDER, int DIR, class TS, bool GATED = false, bool NS = false>
 __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo, const int N0, const int T0,
                                           unsigned char* smem_raw) {
     using S = FaceSmem<T, ORDER, TS>;
@@ -590,7 +590,9 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
 #pragma unroll
             for (int v = 0; v < 4; ++v) d[v] = T(0.0);
         } else {
-            if (geo.tau_type == 1)
+            // the Navier-Stokes form is a separate instantiation: the Euler kernels carry none
+            // of its code
+            if constexpr (NS)
                 gks_point_ns<T>(L, R, dt, K, NsParam<T>{T(geo.c2), T(geo.mu), T(geo.nu), T(geo.prandtl_coef)}, f, d);
             else
                 gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
@@ -686,10 +688,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     }
 }
 
-template <class T, int ORDER, int DIR, bool GATED = false>
+template <class T, int ORDER, int DIR, bool GATED = false, bool NS = false>
 __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_kernel(FaceArgs a, Geometry geo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    face_tile<T, ORDER, DIR, DefaultTile, GATED>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
+    face_tile<T, ORDER, DIR, DefaultTile, GATED, NS>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
 }
 
 }  // namespace hos

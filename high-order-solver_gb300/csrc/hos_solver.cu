@@ -268,7 +268,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     }
     mark(1);
     // x faces then y faces, back to back on the stream (events after each when profiling)
-    const int prec = s->gated ? 2 : s->precision;
+    const int prec = geo.tau_type == HOS_TAU_NS ? (s->precision == HOS_FP64 ? 3 : 4) : s->gated ? 2 : s->precision;
     switch (s->p.order) {
         case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
         case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
@@ -415,10 +415,11 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
         }
     }
     cudaMemset(s->ctl, 0, sizeof(StepCtl));
+    const int variant = p.tau_type == HOS_TAU_NS ? (precision == HOS_FP64 ? 3 : 4) : precision;
     switch (p.order) {
-        case 5: e = configure_faces5(precision); break;
-        case 7: e = configure_faces7(precision); break;
-        default: e = configure_faces9(precision); break;
+        case 5: e = configure_faces5(variant); break;
+        case 7: e = configure_faces7(variant); break;
+        default: e = configure_faces9(variant); break;
     }
     if (e != cudaSuccess) {
         free_all(s);
@@ -590,6 +591,7 @@ int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audi
         return HOS_OK;
     }
     if (s->precision != HOS_FP32) return fail(HOS_E_CONFIG, "the learned gate runs on the FP32-bulk path");
+    if (s->geo.tau_type == HOS_TAU_NS) return fail(HOS_E_CONFIG, "the learned gate runs with the Euler collision time");
     if (audit_log2 < 0 || audit_log2 > 31) return fail(HOS_E_ARG, "audit_log2 must be 0..31");
     if (!s->gflags) {
         if ((e = cudaMalloc(&s->gflags, s->ncell)) == cudaSuccess && (e = cudaMalloc(&s->gstats, sizeof(Stats))) == cudaSuccess &&

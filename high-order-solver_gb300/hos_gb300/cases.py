@@ -353,3 +353,21 @@ def rt2d(nodex: int = 100, order: int = 5) -> tuple:
     prim = _fill_ghosts(prim, g)   # ghosts: filled by the boundaries before first use
     con = prim_to_con(prim, gamma)
     return pb, con, prim
+
+
+def random_octants3d(n: int, seed: int, characteristic: bool = True) -> tuple:
+    """A 3D Riemann problem on [0, 1]^3 for gate training: eight octants around a seeded centre
+    with seeded states (rho in [0.3, 2], p in [0.2, 2], u, v, w in [-1, 1]), free sides."""
+    rng = np.random.default_rng(seed)
+    pb = Problem3D(nodex=n, nodey=n, nodez=n, ghost=3, characteristic=characteristic)
+    ctr = rng.uniform(0.35, 0.65, size=3)
+    states = np.stack([rng.uniform(0.3, 2.0, 8), rng.uniform(-1, 1, 8), rng.uniform(-1, 1, 8),
+                       rng.uniform(-1, 1, 8), rng.uniform(0.2, 2.0, 8)], -1)
+    xc = (np.arange(pb.shape[0]) - 3 + 0.5) / n
+    X, Y, Z = np.meshgrid(xc, xc, xc, indexing="ij", sparse=True)
+    octant = (X > ctr[0]).astype(int) * 4 + (Y > ctr[1]).astype(int) * 2 + (Z > ctr[2]).astype(int)
+    prim = states[np.broadcast_to(octant, pb.shape)]
+    rho, u, v, w, p = (prim[..., q] for q in range(5))
+    gamma = pb.gamma
+    con = np.stack([rho, rho * u, rho * v, rho * w, p / (gamma - 1) + 0.5 * rho * (u * u + v * v + w * w)], -1)
+    return pb, con

@@ -11,7 +11,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import cases
-from .solver import FP32, Gate, Solver2D
+from .solver import FP32, Gate, Solver2D, Solver3D
 
 
 @dataclass
@@ -58,12 +58,40 @@ def evaluate(z: np.ndarray, y: np.ndarray, threshold: float) -> dict:
     return {"coverage": cov, "false_negative_rate": fn, "accuracy": acc, "n": int(len(z))}
 
 
+def collect3d(gate: Gate, sizes=(48, 64), seeds=range(3), steps: int = 40, every: int = 5,
+              sample_log2: int = 4) -> None:
+    """Append samples of FP32 3D runs: random-octant Riemann problems (sharp fronts) and the
+    Taylor-Green vortex (smooth), every ``every``-th step."""
+    runs = [cases.random_octants3d(n, seed=100 * n + sd) for n in sizes for sd in seeds]
+    runs += [cases.tgv3d(n) for n in sizes]
+    for pb, con in runs:
+        s = Solver3D(pb, FP32)
+        s.set_state(con)
+        for _ in range(0, steps, every):
+            s.advance(every)
+            gate.collect3d(s, sample_log2)
+        s.close()
+
+
+def train3d(sizes=(48, 64), seeds=range(3), steps: int = 40, sample_log2: int = 4, train_steps: int = 3000,
+            batch: int = 4096, lr: float = 3e-3, w_neg: float = 4.0, fn_target: float = 0.01,
+            capacity: int = 1 << 22, seed: int = 1):
+    """The 3D gate: samples of 3D runs, the same training and calibration; (gate, report)."""
+    g = Gate(capacity=capacity, seed=seed)
+    collect3d(g, sizes, seeds, steps, sample_log2=sample_log2)
+    return g, _fit(g, train_steps, batch, lr, w_neg, fn_target, seed)
+
+
 def train(order: int = 7, sizes=(256, 512), seeds=range(4), steps: int = 120, sample_log2: int = 5,
           train_steps: int = 3000, batch: int = 4096, lr: float = 3e-3, w_neg: float = 4.0,
           fn_target: float = 0.01, capacity: int = 1 << 22, seed: int = 1):
     """Collect, train and calibrate a gate; returns (gate, report)."""
     g = Gate(capacity=capacity, seed=seed)
     collect(g, order, sizes, seeds, steps, sample_log2=sample_log2)
+    return g, _fit(g, train_steps, batch, lr, w_neg, fn_target, seed)
+
+
+def _fit(g: Gate, train_steps: int, batch: int, lr: float, w_neg: float, fn_target: float, seed: int) -> GateReport:
     n = g.count
     rep = GateReport(samples=n)
     s = g.samples()
@@ -80,4 +108,4 @@ def train(order: int = 7, sizes=(256, 512), seeds=range(4), steps: int = 120, sa
     rep.threshold = choose_threshold(z, y, fn_target)
     rep.heldout = evaluate(z, y, rep.threshold)
     g.set_samples(s)   # keep everything for further training / inspection
-    return g, rep
+    return rep

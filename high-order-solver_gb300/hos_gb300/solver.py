@@ -125,6 +125,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos3d_set_time.argtypes = [vp, ctypes.c_double]
     lib.hos3d_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.hos3d_profile_step.argtypes = [vp, ctypes.c_double, _FP, ctypes.c_int]
+    lib.hos3d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
+    lib.hos3d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
+    lib.hos_gate_collect3d.argtypes = [vp, vp, ctypes.c_int]
     lib.hos3d_last_error.restype = ctypes.c_char_p
     _LIB = lib
     return lib
@@ -348,7 +351,7 @@ class Solver3D:
     State arrays use the reference's cell order ((i * ny + j) * nz + k, 5 doubles per cell)."""
 
     PROFILE_KEYS = ["begin_step"] + [f"{k}{s}" for s in (0, 1) for k in
-                                     ("bc", "face_x", "line_x", "point_x", "face_y", "line_y", "point_y",
+                                     ("bc", "gate", "face_x", "line_x", "point_x", "face_y", "line_y", "point_y",
                                       "face_z", "line_z", "point_z", "update")]
 
     def __init__(self, problem: Problem3D, precision: int = FP64):
@@ -417,9 +420,20 @@ class Solver3D:
         return v.value or 0
 
     def profile_step(self, tstop: float = 1e30) -> dict:
-        ms = (ctypes.c_float * 23)()
-        _check3(self._lib.hos3d_profile_step(self._h, tstop, ms, 23))
+        ms = (ctypes.c_float * 25)()
+        _check3(self._lib.hos3d_profile_step(self._h, tstop, ms, 25))
         return dict(zip(self.PROFILE_KEYS, [float(x) for x in ms]))
+
+    def set_gate(self, gate: "Gate | None", threshold: float = 0.0, audit_log2: int = 10) -> None:
+        _check3(self._lib.hos3d_set_gate(self._h, gate._h if gate is not None else None, threshold, audit_log2))
+
+    GATE_KEYS = ["cells_x", "cells_y", "cells_z", "smooth_x", "smooth_y", "smooth_z", "audited", "false_neg",
+                 "fallback", "unused"]
+
+    def gate_stats(self, reset: bool = False) -> dict:
+        v = (ctypes.c_ulonglong * 10)()
+        _check3(self._lib.hos3d_gate_stats(self._h, v, 1 if reset else 0))
+        return dict(zip(self.GATE_KEYS, [int(x) for x in v]))
 
     def run(self, tstop: float, max_steps: int = 10**9, check_every: int = 20) -> int:
         steps = 0
@@ -569,6 +583,10 @@ class Gate:
 
     def collect(self, solver: "Solver2D", sample_log2: int = 4) -> None:
         _check(self._lib.hos_gate_collect(self._h, solver._h, sample_log2))
+
+    def collect3d(self, solver: "Solver3D", sample_log2: int = 4) -> None:
+        """Samples of a 3D solver's state: features along x, y and z of sampled cells."""
+        _check3(self._lib.hos_gate_collect3d(self._h, solver._h, sample_log2))
 
     @property
     def count(self) -> int:

@@ -325,9 +325,19 @@ int hos3d_stage(hos_solver3d* s, int stage);
 int hos3d_set_time(hos_solver3d* s, double t);
 /* the solver's CUDA stream (cudaStream_t) */
 int hos3d_stream(hos_solver3d* s, void** stream);
-/* one step with an event after every launch: ms[0] begin, then per stage (11 each):
- * boundaries, face/line/point+flux of x, of y, of z, update; n >= 23 */
+/* one step with an event after every launch: ms[0] begin, then per stage (12 each):
+ * boundaries, gate (0 without one), face/line/point+flux of x, of y, of z, update; n >= 25 */
 int hos3d_profile_step(hos_solver3d* s, double tstop, float* ms, int n);
+/* The learned gate on the 3D FP32-bulk path (the 2D gate's network and training; inputs are
+ * the WENO5-AO indicators of each cell's stencil along x, y and z): predicted-smooth
+ * reconstructions along an axis take the big-stencil polynomial in conservative variables,
+ * checked a posteriori.  g == NULL detaches.  The solver copies the network. */
+int hos3d_set_gate(hos_solver3d* s, const hos_gate* g, float threshold, int audit_log2);
+/* counters since the last reset: cells gated along x, y, z; predicted smooth along x, y, z;
+ * audited; audited but not smooth; linear results rejected; (unused) */
+int hos3d_gate_stats(hos_solver3d* s, unsigned long long* stats, int reset);
+/* training samples from a 3D solver's current state (boundaries filled first) */
+int hos_gate_collect3d(hos_gate* g, hos_solver3d* s, int sample_log2);
 const char* hos3d_last_error(void);
 
 /* ---- batches of independent 2D problems ------------------------------------------------
