@@ -60,6 +60,10 @@ N_3D = 256        # cells per side of the 3D Taylor-Green leg
 FP32_FLOP_PER_FACE_POINT3 = 28400.0
 FP64_FLOP_PER_FACE_POINT3 = 37100.0
 TRAFFIC_PER_FACE_POINT3 = 289.0
+# the gated FP32 point kernel on the Taylor-Green vortex (every face flagged smooth; ncu, 64^3):
+# flop per face and DRAM bytes per face
+GATED_FLOP_PER_FACE_POINT3 = 17440.0
+GATED_TRAFFIC_PER_FACE_POINT3 = 290.0
 ACC_STEPS = 200   # steps of the 512^2 runs whose density deviation the line states
 
 
@@ -279,20 +283,27 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
 
 def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n512=True):
     """3D Taylor-Green vortex, n^3 cells (WENO5-AO on 2 x 2 Gauss points per face, GKS3D with
-    the Navier-Stokes collision time, S2O4): FP32 bulk and FP64, state resident in HBM, CUDA
-    events on the solver's stream, L2 flushed between timed steps; FP32-vs-FP64 density
-    deviation, kinetic-energy and dissipation-rate deviation over 20 steps at 128^3; 512^3 FP32
-    and FP64 throughput; the 3D restatement timed on the host cores."""
-    from hos_gb300 import cases
+    the Navier-Stokes collision time, S2O4): gated FP32 bulk (the learned gate trained on the
+    solver's own 3D runs first, outside the timed region), plain FP32 bulk and FP64, state
+    resident in HBM, CUDA events on the solver's stream, L2 flushed between timed steps;
+    density, kinetic-energy and dissipation-rate deviation from FP64 over 20 steps at 128^3;
+    512^3 throughput; the 3D restatement timed on the host cores."""
+    from hos_gb300 import cases, gate_train
     from hos_gb300.solver import FP32, FP64, Solver3D
+
+    t0 = time.perf_counter()
+    gate, rep = gate_train.train3d()
+    train_s = time.perf_counter() - t0
 
     pb, con = cases.tgv3d(n)
     cells = n ** 3
     out = {"workload": f"tgv3d_{n}^3_re1600_ma0.1_weno5ao_char_4gp_gks3d_ns_s2o4", "cells": cells}
 
-    def timed(prec, k, w):
+    def timed(prec, k, w, gated=False):
         s = Solver3D(pb, prec)
         s.set_state(con)
+        if gated:
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
         ext = torch.cuda.ExternalStream(s.stream, device=dev)
         s.advance(w)
         s.sync()
@@ -311,35 +322,52 @@ def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n5
         flush.zero_()
         torch.cuda.synchronize(dev)
         prof = s.profile_step()
+        st = s.gate_stats() if gated else None
         s.close()
-        return t, prof
+        return t, prof, st
 
-    t32, prof32 = timed(FP32, steps, warmup)
+    tg, profg, statsg = timed(FP32, steps, warmup, gated=True)
+    t32, prof32, _ = timed(FP32, steps, warmup)
     k64 = min(steps, 2)
-    t64, prof64 = timed(FP64, k64, 1)
+    t64, prof64, _ = timed(FP64, k64, 1)
+    cells_g = statsg["cells_x"] + statsg["cells_y"] + statsg["cells_z"]
+    out["gated_fp32"] = {"value": cells * steps / tg, "unit": "cell-updates/s", "ms_per_step": 1e3 * tg / steps,
+                         "steps": steps, "warmup": warmup, "kernels_ms": profg,
+                         "gate": {"train_s": train_s, "samples": rep.samples, "threshold": rep.threshold,
+                                  "heldout": rep.heldout, "audit_log2": AUDIT_LOG2,
+                                  "smooth_fraction": (statsg["smooth_x"] + statsg["smooth_y"] + statsg["smooth_z"])
+                                  / max(cells_g, 1),
+                                  "audited": statsg["audited"], "false_neg": statsg["false_neg"],
+                                  "fallback_faces": statsg["fallback"]}}
+    out["gated_speedup_vs_fp64"] = (t64 / k64) / (tg / steps)
+    out["gated_speedup_vs_fp32"] = t32 / tg
     out["fp32_bulk"] = {"value": cells * steps / t32, "unit": "cell-updates/s", "ms_per_step": 1e3 * t32 / steps,
                         "steps": steps, "warmup": warmup, "kernels_ms": prof32}
     out["fp64"] = {"value": cells * k64 / t64, "unit": "cell-updates/s", "ms_per_step": 1e3 * t64 / k64,
                    "steps": k64, "warmup": 1, "kernels_ms": prof64}
     out["fp32_speedup"] = (t64 / k64) / (t32 / steps)
     faces = (n + 1) * n * n
-    for name, prof, flop, peak, unit_peak in (("fp32_bulk", prof32, FP32_FLOP_PER_FACE_POINT3, fp32_peak, "SGEMM"),
+    for name, prof, flop, peak, unit_peak in (("gated_fp32", profg, GATED_FLOP_PER_FACE_POINT3, fp32_peak, "SGEMM"),
+                                              ("fp32_bulk", prof32, FP32_FLOP_PER_FACE_POINT3, fp32_peak, "SGEMM"),
                                               ("fp64", prof64, FP64_FLOP_PER_FACE_POINT3, fp64_peak, "DGEMM")):
         ms = float(np.mean([v for k, v in prof.items() if k.startswith("point")]))
         ach = flop * faces / (ms / 1e3) / 1e12
-        out[name]["roofline"] = {"kernel": f"point3_kernel<{'float' if name == 'fp32_bulk' else 'double'}>",
-                                 "bound": "fp32" if name == "fp32_bulk" else "fp64", "unit": "TFLOP/s",
+        kern = {"gated_fp32": "point3_kernel<float, gated>", "fp32_bulk": "point3_kernel<float>"}.get(name, "point3_kernel<double>")
+        out[name]["roofline"] = {"kernel": kern, "bound": "fp64" if name == "fp64" else "fp32", "unit": "TFLOP/s",
                                  "achieved": ach, "peak": peak, "frac": ach / peak,
                                  "peak_source": f"cuBLAS {unit_peak} measured in this run",
                                  "flop_per_face": flop, "launch_ms": ms,
-                                 "traffic": TRAFFIC_PER_FACE_POINT3 * faces if name == "fp32_bulk" else None}
-    # FP32 bulk against FP64 from the same initial data, 128^3, 20 steps: density deviation,
-    # kinetic energy <rho |u|^2 / 2> and its dissipation rate -dKE/dt per step
+                                 "traffic": {"fp32_bulk": TRAFFIC_PER_FACE_POINT3 * faces,
+                                             "gated_fp32": GATED_TRAFFIC_PER_FACE_POINT3 * faces}.get(name)}
+    # FP32 bulk (plain and gated) against FP64 from the same initial data, 128^3, 20 steps:
+    # density deviation, kinetic energy <rho |u|^2 / 2> and its dissipation rate -dKE/dt
     pa, ca = cases.tgv3d(128)
     rho, ke, ts = {}, {}, {}
-    for name, prec in (("fp64", FP64), ("fp32", FP32)):
+    for name, prec in (("fp64", FP64), ("fp32", FP32), ("gated", FP32)):
         s = Solver3D(pa, prec)
         s.set_state(ca)
+        if name == "gated":
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
         kk, tt = [], []
         for i in range(21):
             st = s.get_state()["convar"][3:-3, 3:-3, 3:-3]
@@ -357,14 +385,22 @@ def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n5
                        "kinetic_energy_rel_dev_max": float(np.abs(ke["fp32"] - ke["fp64"]).max() / ke["fp64"][0]),
                        "dissipation_rate_rel_dev_max": float(np.abs(eps["fp32"] - eps["fp64"]).max()
                                                              / np.abs(eps["fp64"]).max()),
-                       "kinetic_energy_ratio_fp64": float(ke["fp64"][-1] / ke["fp64"][0])}
+                       "kinetic_energy_ratio_fp64": float(ke["fp64"][-1] / ke["fp64"][0]),
+                       "rho_rel_l1_gated_vs_fp64": float(np.abs(rho["gated"] - rho["fp64"]).mean()
+                                                         / np.abs(rho["fp64"]).mean()),
+                       "kinetic_energy_rel_dev_max_gated": float(np.abs(ke["gated"] - ke["fp64"]).max()
+                                                                 / ke["fp64"][0]),
+                       "dissipation_rate_rel_dev_max_gated": float(np.abs(eps["gated"] - eps["fp64"]).max()
+                                                                   / np.abs(eps["fp64"]).max())}
     # 512^3: FP32 bulk (1 warm-up, 2 timed steps) and FP64 (1 timed step, ~45 s)
     if n512:
         pb5, con5 = cases.tgv3d(512)
         big = {}
-        for name, prec, k, w in (("fp32_bulk", FP32, 2, 1), ("fp64", FP64, 1, 0)):
+        for name, prec, k, w in (("gated_fp32", FP32, 2, 1), ("fp32_bulk", FP32, 2, 1), ("fp64", FP64, 1, 0)):
             s = Solver3D(pb5, prec)
             s.set_state(con5)
+            if name == "gated_fp32":
+                s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
             ext = torch.cuda.ExternalStream(s.stream, device=dev)
             s.advance(w)
             s.sync()
@@ -381,6 +417,7 @@ def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n5
             s.close()
         del con5
         big["fp32_speedup"] = big["fp32_bulk"]["value"] / big["fp64"]["value"]
+        big["gated_speedup_vs_fp64"] = big["gated_fp32"]["value"] / big["fp64"]["value"]
         out["n512"] = big
     # the 3D restatement on the host cores, bounded sample
     sys.path.insert(0, str(ROOT / "tests"))
@@ -397,6 +434,7 @@ def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n5
     el = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": 32 ** 3 * nst / el, "unit": "cell-updates/s", "cores": cores, "kind": "port",
                            "sample": f"32^3 Taylor-Green, {nst} S2O4 steps after 1 warm-up (OpenMP)"}
+    gate.close()
     return out
 
 
@@ -457,22 +495,27 @@ def profile_case():
 
 def profile_case_3d():
     """The launches of the 3D ncu summaries: 64^3 Taylor-Green, 2 FP32 steps in NVTX range
-    "fp32", then 1 FP64 step in "fp64"."""
+    "fp32", 2 gated FP32 steps in "gated" (a gate trained on 32^3 runs first), then 1 FP64 step
+    in "fp64"."""
     import torch
 
-    from hos_gb300 import cases
+    from hos_gb300 import cases, gate_train
     from hos_gb300.solver import FP32, FP64, Solver3D
 
+    gate, rep = gate_train.train3d(sizes=(32,), seeds=range(2), steps=20, train_steps=800, capacity=1 << 20)
     pb, con = cases.tgv3d(64)
-    for name, prec, k in (("fp32", FP32, 2), ("fp64", FP64, 1)):
+    for name, prec, k in (("fp32", FP32, 2), ("gated", FP32, 2), ("fp64", FP64, 1)):
         s = Solver3D(pb, prec)
         s.set_state(con)
+        if name == "gated":
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
         torch.cuda.nvtx.range_push(name)
         s.advance(k)
         s.sync()
         torch.cuda.nvtx.range_pop()
-        print(name, s.sync(), flush=True)
+        print(name, s.sync(), s.gate_stats() if name == "gated" else "", flush=True)
         s.close()
+    gate.close()
 
 
 def main():
