@@ -273,7 +273,10 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, con
             const size_t q = (size_t)gi * geo.ny + gj;
             float w[4];
             if (a.W32) {
-                w[0] = a.W32[q]; w[1] = a.W32[plane + q]; w[2] = a.W32[2 * plane + q]; w[3] = a.W32[3 * plane + q];
+                // the FP32 mirror's rows are padded to mirror_pitch(ny)
+                const size_t p32 = (size_t)mirror_pitch(geo.ny), pl32 = (size_t)geo.nx * p32;
+                const size_t qm = (size_t)gi * p32 + gj;
+                w[0] = a.W32[qm]; w[1] = a.W32[pl32 + qm]; w[2] = a.W32[2 * pl32 + qm]; w[3] = a.W32[3 * pl32 + qm];
             } else {
                 w[0] = float(a.W[q]); w[1] = float(a.W[plane + q]); w[2] = float(a.W[2 * plane + q]); w[3] = float(a.W[3 * plane + q]);
             }

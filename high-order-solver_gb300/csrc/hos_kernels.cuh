@@ -10,6 +10,9 @@
 //                      x-face (I, J), I in [0, nodex], J in [0, nodey): I*nodey + J
 //                      y-face (I, J), I in [0, nodex), J in [0, nodey]: I*(nodey+1) + J
 //   ctl                dt, t, CFL accumulator (bits of a positive double), status word
+//   W32[6][nx*P]       FP32 solvers: FP32 mirror of W0..W3, alpha_x, alpha_y, rows padded to
+//                      the pitch P = mirror_pitch(ny) (hos_tma.cuh); the FP32 face kernels
+//                      stage their tiles from it with TMA tile loads
 //
 // One stage = bc_fill -> face_kernel<x> -> face_kernel<y> -> update_kernel.  The face
 // kernel fuses, for a tile of faces, the normal line reconstruction (staged in shared
@@ -19,6 +22,7 @@
 #pragma once
 #include <cstdint>
 #include "hos_gks.cuh"
+#include "hos_tma.cuh"
 
 namespace hos {
 
@@ -26,7 +30,8 @@ struct StepCtl {
     double dt;           // time step of the current step
     double t;            // simulation time at the end of the current step
     unsigned long long cfl_bits;  // running min of CFL candidates (positive doubles as bits)
-    unsigned int status; // bit 0: negative density/pressure or NaN (reference would exit)
+    unsigned int status; // bit 0: negative density/pressure or NaN (reference would exit);
+                         // TMA_TIMEOUT_BIT: a tile load did not complete within its wait limit
     unsigned int active; // 0 once t >= tstop: the step's kernels return without work
     double tbeg;         // simulation time at the start of the current step (Block2d::t)
 };
@@ -107,8 +112,8 @@ struct UpdateArgs {
     const double* FAy;
     StepCtl* ctl;
     int stage;
-    float* W32;   // FP32 solvers: mirror of W and of alpha_x | alpha_y (may be null)
-    float* A32;
+    float* W32;   // FP32 solvers: mirror of W (planes 0-3) and of alpha_x | alpha_y (planes
+    float* A32;   // 4-5, A32 = W32 + 4 * nx * P), pitch P = mirror_pitch(ny); may be null
 };
 
 // step kernels defined in hos_solver.cu
@@ -136,8 +141,8 @@ struct FaceArgs {
     // every earlier stage [stage][4][nf]
     double* FS;
     double* DS;
-    // FP32 solvers: FP32 mirrors of the state and of the DF indicators, read by the FP32 tiles
-    // instead of converting the FP64 arrays (null: convert)
+    // FP32 solvers: FP32 mirrors of the state and of the DF indicators (pitch mirror_pitch(ny)),
+    // read by the FP32 tiles instead of converting the FP64 arrays (null: convert)
     const float* W32;
     const float* AN32;
     const float* AT32;
@@ -174,6 +179,23 @@ struct FaceSmem {
     static constexpr int GFLAGS = ((TILE_N + 1) * TL + (int)sizeof(T) - 1) / (int)sizeof(T);  // gate flag bytes
     static constexpr size_t bytes = sizeof(T) * (size_t)(UNION + GSTATES + ATILE);
     static constexpr size_t gated_bytes = bytes + sizeof(T) * (size_t)GFLAGS;
+};
+
+// TMA box of one FP32 face tile in the pitched mirror: x runs along j, y along i, z over the
+// six planes.  x faces: rows are the TN normal cells, x covers the TL tangential cells; y faces:
+// rows are the TL tangential cells, x covers the TN normal cells.  The x origin is rounded
+// down to 4 floats (a TMA box must start on a 16-byte boundary), so x takes up to 3 more
+// cells, rounded up to a multiple of 4.  The box is staged in the line-state region, which is
+// free until phase 1 writes it.
+template <int ORDER, int DIR, class TS = DefaultTile>
+struct TmaBox {
+    using S = FaceSmem<float, ORDER, TS>;
+    static constexpr int X = ((DIR == 0 ? S::TL : S::TN) + 3 + 3) / 4 * 4;
+    static constexpr int Y = DIR == 0 ? S::TN : S::TL;
+    static constexpr int Z = MIRROR_PLANES;
+    static constexpr unsigned bytes = 4u * X * Y * Z;
+    static_assert(X * Y * Z <= S::UNION, "the staged box must fit the line-state region");
+    static_assert(X <= 256 && Y <= 256, "TMA box extents are at most 256");
 };
 
 // Gauss weights of gausspoint 2 / 3 / 4 (SetGuassPoint, src/fluid_mesh.cpp:20-44)
@@ -219,9 +241,12 @@ __device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, 
 // One tile of faces: N0, T0 are the first face indices along the normal and the tangent.
 // GATED (FP32 only): cells the learned gate marks smooth reconstruct with the full-stencil
 // polynomial alone; see hos_gate.cuh.
-template <class T, int ORDER, int DIR, class TS, bool GATED = false, bool NS = false>
+// TMA (FP32 with the pitched mirror): phase 0 stages the tile from the mirror with one TMA
+// tile load (tmap: the mirror's tensor map with this tile shape's box).
+template <class T, int ORDER, int DIR, class TS, bool GATED = false, bool NS = false, bool TMA = false>
 __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo, const int N0, const int T0,
-                                          unsigned char* smem_raw) {
+                                          unsigned char* smem_raw, const CUtensorMap* tmap = nullptr) {
+    static_assert(!TMA || sizeof(T) == 4, "TMA staging reads the FP32 mirror");
     using S = FaceSmem<T, ORDER, TS>;
     constexpr int TILE_N = TS::N, TILE_T = TS::T;
     constexpr int r = S::r, N = ORDER, GP = S::GP, TL = S::TL;
@@ -252,8 +277,48 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     // ---------------- phase 0: stage the tile's cells once, converted to T ----------------
     // cells n in [g+N0-1-r, g+N0+TILE_N-1+r] (the normal stencils), t in [g+T0-r, g+T0+TILE_T+r);
     // y-face states are rotated into the x-face frame here (YchangetoX: (u, v) -> (v, -u)).
-    {
+    if constexpr (TMA) {
+        // one TMA tile load of W0..W3, alpha_x, alpha_y with the stencil halo into the line-state
+        // region, then the same rotation / split into the tile arrays from shared memory
+        using B = TmaBox<ORDER, DIR, TS>;
+        constexpr int PZ = B::X * B::Y;   // floats per staged plane
+        __shared__ __align__(8) uint64_t tma_bar;
+        float* stg = reinterpret_cast<float*>(smem_raw);
+        const int x0 = DIR == 0 ? g + T0 - r : g + N0 - 1 - r;   // j of the first staged cell
+        const int y0 = DIR == 0 ? g + N0 - 1 - r : g + T0 - r;   // i of the first staged row
+        const int xa = x0 & ~3, off = x0 - xa;                    // 16-byte aligned box origin
+        const bool aligned = (smem_u32(stg) & 127u) == 0;
+        if (tid == 0 && aligned) {
+            mbar_init(&tma_bar, 1);
+            mbar_expect_tx(&tma_bar, B::bytes);
+            tma_load_3d(stg, tmap, xa, y0, 0, &tma_bar);
+        }
+        __syncthreads();   // the barrier is initialised before any thread polls it
+        const bool ok = __syncthreads_and(aligned && mbar_wait(&tma_bar, 0));
+        if (!ok) {
+            // record the failure, let a load still in flight land, and leave the tile
+            if (tid == 0) atomicOr(const_cast<unsigned*>(&a.ctl->status), TMA_TIMEOUT_BIT);
+            if (aligned) mbar_wait(&tma_bar, 0);
+            return;
+        }
         const int nmax = DIR == 0 ? nx : ny, tmax = DIR == 0 ? ny : nx;
+        for (int c = tid; c < S::TN * TL; c += FACE_THREADS) {
+            const int nn = c / TL, tl = c % TL;
+            const int n = g + N0 - 1 - r + nn, t = g + T0 - r + tl;
+            if (n >= nmax || t >= tmax) continue;
+            const float* q = stg + (DIR == 0 ? nn * B::X + off + tl : tl * B::X + off + nn);
+            T* d = wtile + (nn * TL + tl) * 4;
+            if (DIR == 0) { d[0] = q[0]; d[1] = q[PZ]; d[2] = q[2 * PZ]; d[3] = q[3 * PZ]; }
+            else { d[0] = q[0]; d[1] = q[2 * PZ]; d[2] = -q[PZ]; d[3] = q[3 * PZ]; }
+            antile[nn * TL + tl] = q[(DIR == 0 ? 4 : 5) * PZ];
+            if (nn >= r && nn <= r + TILE_N) {
+                attile[(nn - r) * TL + tl] = q[(DIR == 0 ? 5 : 4) * PZ];
+                if constexpr (GATED) gfl[(nn - r) * TL + tl] = a.gate[cidx(n, t)];
+            }
+        }
+    } else {
+        const int nmax = DIR == 0 ? nx : ny, tmax = DIR == 0 ? ny : nx;
+        const size_t pitch = (size_t)mirror_pitch(ny), plane32 = (size_t)nx * pitch;
         for (int c = tid; c < S::TN * TL; c += FACE_THREADS) {
             // x faces: t (= j) runs fastest; y faces: n (= j) runs fastest -- coalesced rows
             const int nn = DIR == 0 ? c / TL : c % S::TN;
@@ -265,9 +330,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             bool mirrored = false;
             if constexpr (sizeof(T) == 4) {
                 if (a.W32) {
-                    w0 = a.W32[ci]; w1 = a.W32[plane + ci]; w2 = a.W32[2 * plane + ci]; w3 = a.W32[3 * plane + ci];
-                    an = a.AN32[ci];
-                    at = a.AT32[ci];
+                    const size_t cm = DIR == 0 ? (size_t)n * pitch + t : (size_t)t * pitch + n;
+                    w0 = a.W32[cm]; w1 = a.W32[plane32 + cm]; w2 = a.W32[2 * plane32 + cm]; w3 = a.W32[3 * plane32 + cm];
+                    an = a.AN32[cm];
+                    at = a.AT32[cm];
                     mirrored = true;
                 }
             }
@@ -692,6 +758,16 @@ template <class T, int ORDER, int DIR, bool GATED = false, bool NS = false>
 __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_kernel(FaceArgs a, Geometry geo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     face_tile<T, ORDER, DIR, DefaultTile, GATED, NS>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
+}
+
+// FP32 face kernel of the solvers with the pitched FP32 mirror: the tile is staged by one TMA
+// tile load (tmap: the mirror's tensor map, box TmaBox<ORDER, DIR>)
+template <int ORDER, int DIR, bool GATED = false, bool NS = false>
+__global__ void __launch_bounds__(FACE_THREADS, 2)
+    face_kernel_tma(FaceArgs a, Geometry geo, const __grid_constant__ CUtensorMap tmap) {
+    extern __shared__ __align__(128) unsigned char smem_tma[];
+    face_tile<float, ORDER, DIR, DefaultTile, GATED, NS, true>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T,
+                                                               smem_tma, &tmap);
 }
 
 }  // namespace hos

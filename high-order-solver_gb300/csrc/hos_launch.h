@@ -6,14 +6,16 @@
 
 namespace hos {
 // precision: 0 = FP64 compute, 1 = FP32 compute (state and accumulation stay FP64),
-// 2 = FP32 compute with the learned gate (FaceArgs::gate set)
+// 2 = FP32 compute with the learned gate (FaceArgs::gate set), 3 / 4 = FP64 / FP32 with the
+// Navier-Stokes collision time.  tm: the FP32 mirror's tensor maps (x- and y-face boxes); with
+// them the FP32 kernels stage their tiles by TMA tile loads from the mirror.
 cudaError_t configure_faces5(int precision);
 cudaError_t configure_faces7(int precision);
 cudaError_t configure_faces9(int precision);
 cudaError_t launch_faces5(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
-                           cudaEvent_t* ev = nullptr);
+                           cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr);
 cudaError_t launch_faces7(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
-                           cudaEvent_t* ev = nullptr);
+                           cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr);
 cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
-                           cudaEvent_t* ev = nullptr);
+                           cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr);
 }  // namespace hos

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/hos_gb300.h"
 #include "hos_gate.cuh"
 #include "hos_launch.h"
@@ -21,15 +23,18 @@ __global__ void bc_fill_kernel(double* __restrict__ W, Geometry geo, BcSpec bc, 
     bc_fill_one(W, geo, bc, ctl, blockIdx.x * (long long)blockDim.x + threadIdx.x, W32);
 }
 
-// FP32 mirrors of the whole state and of the DF indicators (after an upload)
+// FP32 mirrors of the whole state and of the DF indicators (after an upload), rows at the
+// mirror's pitch
 __global__ void mirror_state_kernel(const double* __restrict__ W, const double* __restrict__ AX,
                                     const double* __restrict__ AY, float* __restrict__ W32, float* __restrict__ A32,
-                                    size_t n) {
+                                    int nx, int ny) {
+    const size_t n = (size_t)nx * ny, pitch = (size_t)mirror_pitch(ny), n32 = (size_t)nx * pitch;
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t cm = (c / ny) * pitch + c % ny;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) W32[v * n + c] = (float)W[v * n + c];
-        A32[c] = (float)AX[c];
-        A32[n + c] = (float)AY[c];
+        for (int v = 0; v < 4; ++v) W32[v * n32 + cm] = (float)W[v * n + c];
+        A32[cm] = (float)AX[c];
+        A32[n32 + cm] = (float)AY[c];
     }
 }
 
@@ -141,6 +146,41 @@ static int cuda_fail(cudaError_t e, const char* where) {
     return fail(HOS_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// Tensor maps of the FP32 mirror (base: nx rows of ny cells at pitch mirror_pitch(ny), six
+// planes) with the x-face and the y-face tile boxes of the given WENO order.  The encoder is
+// the driver's cuTensorMapEncodeTiled, fetched through the runtime so that the library does not
+// link libcuda.  Cells past ny in a row read as zero (the out-of-bounds fill).
+static int encode_mirror_maps(CUtensorMap* maps, float* base, int nx, int ny, int order) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return fail(HOS_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    int bx[2], by[2];
+    switch (order) {
+        case 5: bx[0] = TmaBox<5, 0>::X; by[0] = TmaBox<5, 0>::Y; bx[1] = TmaBox<5, 1>::X; by[1] = TmaBox<5, 1>::Y; break;
+        case 7: bx[0] = TmaBox<7, 0>::X; by[0] = TmaBox<7, 0>::Y; bx[1] = TmaBox<7, 1>::X; by[1] = TmaBox<7, 1>::Y; break;
+        default: bx[0] = TmaBox<9, 0>::X; by[0] = TmaBox<9, 0>::Y; bx[1] = TmaBox<9, 1>::X; by[1] = TmaBox<9, 1>::Y; break;
+    }
+    const cuuint64_t pitch = (cuuint64_t)mirror_pitch(ny);
+    const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)MIRROR_PLANES};
+    const cuuint64_t strides[2] = {pitch * sizeof(float), pitch * (cuuint64_t)nx * sizeof(float)};
+    const cuuint32_t es[3] = {1, 1, 1};
+    for (int d = 0; d < 2; ++d) {
+        const cuuint32_t box[3] = {(cuuint32_t)bx[d], (cuuint32_t)by[d], (cuuint32_t)MIRROR_PLANES};
+        CUresult r = encode(&maps[d], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(HOS_E_CUDA, "cuTensorMapEncodeTiled failed on the FP32 mirror (code " +
+                                                       std::to_string((int)r) + ")");
+    }
+    return HOS_OK;
+}
+
 }  // namespace hos
 
 using namespace hos;
@@ -165,8 +205,9 @@ struct hos_solver2d {
     double* FPy = nullptr;
     double* FAy = nullptr;
     double* scratch = nullptr;  // 8 * ncell doubles: AoS staging + primitive planes
-    float* W32 = nullptr;       // FP32 solvers: mirror of W [4][nx*ny] ...
-    float* A32 = nullptr;       // ... and of alpha_x | alpha_y [2][nx*ny]
+    float* W32 = nullptr;       // FP32 solvers: mirror of W [4][nx*P] ...
+    float* A32 = nullptr;       // ... and of alpha_x | alpha_y [2][nx*P] (inside the W32 allocation)
+    CUtensorMap tmap[2];        // FP32 solvers: the mirror's tensor maps with the x- / y-face boxes
     double* stagex = nullptr;   // methods other than S2O4: per-stage F and D of x faces [2][4][4][nfx]
     double* stagey = nullptr;   // ... and of y faces
     StepCtl* ctl = nullptr;
@@ -224,7 +265,7 @@ void free_all(hos_solver2d* s) {
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->ctl) cudaFree(s->ctl);
-    void* gbufs[] = {s->gflags, s->gstats, s->gw, s->gb, s->W32, s->A32};
+    void* gbufs[] = {s->gflags, s->gstats, s->gw, s->gb, s->W32};
     for (void* b : gbufs)
         if (b) cudaFree(b);
     if (s->graph) cudaGraphExecDestroy(s->graph);
@@ -269,10 +310,12 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     mark(1);
     // x faces then y faces, back to back on the stream (events after each when profiling)
     const int prec = geo.tau_type == HOS_TAU_NS ? (s->precision == HOS_FP64 ? 3 : 4) : s->gated ? 2 : s->precision;
+    // FP32 solvers stage their tiles from the mirror with TMA tile loads
+    const CUtensorMap* tm = s->W32 ? s->tmap : nullptr;
     switch (s->p.order) {
-        case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
-        case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
-        default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr); break;
+        case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm); break;
+        case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm); break;
+        default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
     UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage, s->W32, s->A32};
@@ -300,7 +343,7 @@ int enqueue_step(hos_solver2d* s, double tstop) {
 cudaError_t refresh_mirror(hos_solver2d* s) {
     if (!s->W32) return cudaSuccess;
     mirror_state_kernel<<<(unsigned)std::min<size_t>((s->ncell + 255) / 256, 4096), 256, 0, s->stream>>>(
-        s->W, s->AX, s->AY, s->W32, s->A32, s->ncell);
+        s->W, s->AX, s->AY, s->W32, s->A32, s->geo.nx, s->geo.ny);
     return cudaGetLastError();
 }
 
@@ -405,13 +448,19 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
         return fail(HOS_E_NOMEM, "cudaMalloc ctl");
     }
     if (precision == HOS_FP32) {
-        if ((e = cudaMalloc(&s->W32, 4 * s->ncell * sizeof(float))) != cudaSuccess ||
-            (e = cudaMalloc(&s->A32, 2 * s->ncell * sizeof(float))) != cudaSuccess ||
-            (e = cudaMemset(s->W32, 0, 4 * s->ncell * sizeof(float))) != cudaSuccess ||
-            (e = cudaMemset(s->A32, 0, 2 * s->ncell * sizeof(float))) != cudaSuccess) {
+        const size_t n32 = (size_t)s->geo.nx * mirror_pitch(s->geo.ny);
+        if ((e = cudaMalloc(&s->W32, MIRROR_PLANES * n32 * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemset(s->W32, 0, MIRROR_PLANES * n32 * sizeof(float))) != cudaSuccess) {
             free_all(s);
             delete s;
             return fail(HOS_E_NOMEM, "cudaMalloc FP32 mirror");
+        }
+        s->A32 = s->W32 + 4 * n32;
+        const int st = encode_mirror_maps(s->tmap, s->W32, s->geo.nx, s->geo.ny, p.order);
+        if (st != HOS_OK) {
+            free_all(s);
+            delete s;
+            return st;
         }
     }
     cudaMemset(s->ctl, 0, sizeof(StepCtl));
@@ -716,6 +765,7 @@ int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
     if (t) *t = c.t;
     if (dt) *dt = c.dt;
     if (c.status & 1u) return fail(HOS_E_BLOWUP, "negative density/pressure or NaN in the state");
+    if (c.status & TMA_TIMEOUT_BIT) return fail(HOS_E_TIMEOUT, "a face kernel's TMA tile load did not complete");
     return HOS_OK;
 }
 

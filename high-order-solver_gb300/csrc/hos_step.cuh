@@ -25,10 +25,12 @@ __device__ __forceinline__ void bc_fill_one(double* __restrict__ W, const Geomet
         j = jl < g ? jl : ny - 2 * g + jl;
     }
     const size_t plane = (size_t)nx * ny;
-    // the FP32 mirror of the state (FP32 solvers) takes the same ghost values, rounded
+    // the FP32 mirror of the state (FP32 solvers, pitch mirror_pitch(ny)) takes the same ghost
+    // values, rounded
+    const size_t pitch = (size_t)mirror_pitch(ny), plane32 = (size_t)nx * pitch;
     auto put = [&](int v, double x) {
         W[v * plane + (size_t)i * ny + j] = x;
-        if (W32) W32[v * plane + (size_t)i * ny + j] = (float)x;
+        if (W32) W32[v * plane32 + (size_t)i * pitch + j] = (float)x;
     };
     double out[4];
     int si = i, sj = j;
@@ -118,6 +120,9 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         const int I = idx / nodey, J = idx % nodey;
         const size_t plane = (size_t)geo.nx * ny;
         const size_t c = (size_t)(I + g) * ny + (J + g);
+        // the cell in the FP32 mirror (FP32 solvers): pitch mirror_pitch(ny)
+        const size_t pitch = (size_t)mirror_pitch(ny), plane32 = (size_t)geo.nx * pitch;
+        const size_t cm = (size_t)(I + g) * pitch + (J + g);
         const size_t nfx = (size_t)(nodex + 1) * nodey, nfy = (size_t)nodex * (nodey + 1);
         const size_t fl = (size_t)I * nodey + J, fr = fl + nodey;
         const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
@@ -162,7 +167,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             else
                 w[v] = old + total * iarea;
             a.W[v * plane + c] = w[v];
-            if (a.W32) a.W32[v * plane + c] = (float)w[v];
+            if (a.W32) a.W32[v * plane32 + cm] = (float)w[v];
         }
         const int jend = nodex < nodey ? nodex : nodey;
         if (J < jend) {
@@ -170,8 +175,8 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             a.AX[c] = ax;
             a.AY[c] = ay;
             if (a.A32) {
-                a.A32[c] = (float)ax;
-                a.A32[plane + c] = (float)ay;
+                a.A32[cm] = (float)ax;
+                a.A32[plane32 + cm] = (float)ay;
             }
         }
         const double ir = 1.0 / w[0];
@@ -238,8 +243,9 @@ __device__ __forceinline__ void begin_step_one(StepCtl* ctl, double tstop, doubl
     double dt = __longlong_as_double((long long)ctl->cfl_bits);
     const double t = ctl->t;
     // the driver loop runs while t < tstop; steps queued past it do nothing.  A problem whose
-    // state went bad (status bit 0; the reference exits there) takes no further steps.
-    const bool go = t < tstop && !(ctl->status & 1u);
+    // state went bad (status bit 0; the reference exits there) or whose step lost a tile to a
+    // TMA load that never completed takes no further steps.
+    const bool go = t < tstop && !(ctl->status & (1u | TMA_TIMEOUT_BIT));
     ctl->active = go ? 1u : 0u;
     ctl->tbeg = t;
     if (!go) return;

@@ -35,6 +35,7 @@ extern "C" {
 #define HOS_E_CUDA 3        /* CUDA runtime error (no device, launch failure, ...)       */
 #define HOS_E_ARG 4         /* null pointer or bad argument                              */
 #define HOS_E_NOMEM 5       /* device allocation failed                                  */
+#define HOS_E_TIMEOUT 6     /* a device-side wait (TMA tile load) ran past its limit      */
 
 /* boundary kinds, per side (left, right, down, up) */
 #define HOS_BC_FREE 0       /* free_boundary_*  (zero-gradient outflow)  */
