@@ -77,13 +77,19 @@ __global__ void __launch_bounds__(gate::GATE_THREADS) gate_batch_kernel(const Pr
                                                                         const GateTile* __restrict__ tiles, int ntiles,
                                                                         gate::Net net, gate::Stats* stats, float threshold,
                                                                         unsigned audit_mask, unsigned seed) {
+    __shared__ gate::MlpTc mlp;   // the network on the tcgen05 tensor cores, set up once per block
+    if (blockIdx.x >= ntiles) return;
+    gate::mlp_tc_setup(mlp, net);
+    unsigned phase = 0;
+    bool broken = false;
     for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
         const GateTile t = tiles[k];
         const Prob* pr = probs + t.p;
         gate::GateArgs a{pr->W, pr->AX, pr->AY, pr->gflags, stats, threshold, audit_mask, seed,
                          nullptr, 0, 0xffffffffu, pr->ctl};
-        gate::gate_tile<ORDER>(a, net, pr->geo, t.i0, t.j0, (unsigned)k);
+        gate::gate_tile<ORDER>(a, pr->geo, t.i0, t.j0, (unsigned)k, mlp, phase, broken);
     }
+    gate::mlp_tc_teardown(mlp, phase, broken);
 }
 
 thread_local std::string g_errb;

@@ -30,7 +30,35 @@ struct TrainArgs {
     float* logits;               // forward-only: [n] outputs (may be null)
 };
 
-// Forward on the tensor cores (the inference routine), backward on the FP32 cores; each block
+// Logits of samples [first, first + n) through the inference network on the tcgen05 tensor
+// cores (the gate kernels' routine), 512 samples per block of 256 threads; status bit 0: a
+// wait ran past its limit.
+__global__ void __launch_bounds__(TC_THREADS) forward_tc_kernel(const float* samples, unsigned long long first,
+                                                                int n, Net net, float* logits, unsigned* status) {
+    __shared__ MlpTc mlp;
+    mlp_tc_setup(mlp, net);
+    unsigned phase = 0;
+    bool broken = false;
+    float f[2][NF], z[2];
+    long long b[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        b[h] = (long long)blockIdx.x * TC_ROWS + h * TC_THREADS + threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) f[h][k] = b[h] < n ? samples[(first + (unsigned long long)b[h]) * NS + k] : 0.0f;
+    }
+    mlp_tc_put(mlp, 0, f[0]);
+    mlp_tc_put(mlp, 1, f[1]);
+    mlp_tc_eval(mlp, z, phase, broken);
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (b[h] < n) logits[b[h]] = z[h];
+    if (broken && threadIdx.x == 0) atomicOr(status, 1u);
+    mlp_tc_teardown(mlp, phase, broken);
+}
+
+// Forward on the tensor cores (mma.sync, keeping the hidden activations for the backward
+// pass), backward on the FP32 cores; each block
 // adds its share of the weighted binary cross-entropy gradient to a.grad.
 __global__ void __launch_bounds__(TRAIN_ROWS * 2) train_grad_kernel(TrainArgs a, Net net, const float* params) {
     __shared__ __align__(16) __nv_bfloat16 xs[TRAIN_ROWS * NF];
@@ -340,16 +368,20 @@ int hos_gate_forward(hos_gate* g, unsigned long long first, int n, float* logits
     float* scratch = nullptr;
     if (e == cudaSuccess) e = cudaMalloc(&scratch, NPARAM * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(scratch, 0, NPARAM * sizeof(float));
-    TrainArgs a{g->samples, have, first, 1, n, 1.f, 1.f, scratch, nullptr, d};
+    unsigned* status = reinterpret_cast<unsigned*>(scratch);
     if (e == cudaSuccess) {
-        train_grad_kernel<<<(n + TRAIN_ROWS - 1) / TRAIN_ROWS, TRAIN_ROWS * 2, 0, g->stream>>>(a, g->net(), g->params);
+        forward_tc_kernel<<<(n + TC_ROWS - 1) / TC_ROWS, TC_THREADS, 0, g->stream>>>(g->samples, first, n, g->net(),
+                                                                                     d, status);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e == cudaSuccess) e = cudaMemcpy(logits, d, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    unsigned st = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&st, status, sizeof st, cudaMemcpyDeviceToHost);
     if (d) cudaFree(d);
     if (scratch) cudaFree(scratch);
-    return e == cudaSuccess ? HOS_OK : gcuda(e, "forward");
+    if (e != cudaSuccess) return gcuda(e, "forward");
+    return st ? gfail(HOS_E_TIMEOUT, "a tensor-core MMA did not complete within its wait limit") : HOS_OK;
 }
 
 // Adam on mini-batches drawn from the collected samples (a fresh coprime-stride permutation

@@ -16,6 +16,7 @@
 #include <cuda_bf16.h>
 
 #include "hos_kernels.cuh"
+#include "hos_umma.cuh"
 
 namespace hos {
 namespace gate {
@@ -219,6 +220,151 @@ __device__ __forceinline__ void mlp16(const Net& net, const __nv_bfloat16* x, fl
     }
 }
 
+// ---------------- the MLP on the 5th-generation tensor cores (tcgen05) ----------------
+// The gate kernels evaluate the network for 512 rows per CTA, two per thread (row t and row
+// 256 + t: a cell's x and y stencils): layer 1 is four 128 x 32 x 16 MMAs, layer 2 four
+// 128 x 32 x 32 MMAs (two K steps each), issued by one thread over BF16 operands in shared
+// memory with FP32 accumulators in 128 tensor-memory columns (columns 32 m .. 32 m + 31 hold
+// rows 128 m .. 128 m + 127).  Bias, ReLU and the BF16 rounding of the activations run on the
+// CUDA cores between the layers, as does the 32-wide output layer.  Rounding points are those
+// of mlp16 above (BF16 inputs, weights and activations, FP32 accumulation).
+constexpr int TC_THREADS = 256;
+constexpr int TC_ROWS = 2 * TC_THREADS;
+constexpr int TC_MTILES = TC_ROWS / 128;
+constexpr uint32_t TC_COLS = TC_MTILES * NH;
+
+struct MlpTc {
+    // features (K = 16, 16 KB) until the layer-1 MMAs have read them, then the layer-1
+    // activations (K = 32, 32 KB) over the same bytes
+    alignas(128) unsigned char act[TC_ROWS * NH * 2];
+    alignas(128) unsigned char b1[NH * NF * 2];        // W1 [out][in], K-major canonical layout
+    alignas(128) unsigned char b2[NH * NH * 2];        // W2 [out][in]
+    float bias1[NH], bias2[NH], w3[NH];
+    float b3;
+    uint64_t bar;        // tcgen05.commit arrives here once the issued MMAs complete
+    uint32_t tmem;       // base address of the CTA's tensor-memory columns
+};
+
+// Per-CTA set-up, by all TC_THREADS threads: weights into the operand layouts, the barrier,
+// the tensor memory.  An allocation that finds the SM's 512 columns taken waits for resident
+// CTAs to release theirs; they never wait on this one.
+__device__ __forceinline__ void mlp_tc_setup(MlpTc& s, const Net& net) {
+    const int tid = threadIdx.x;
+    for (int e = tid; e < NH * NF; e += blockDim.x)
+        *reinterpret_cast<__nv_bfloat16*>(s.b1 + umma::kmajor_offset<NF>(e / NF, e % NF)) = net.w1[e];
+    for (int e = tid; e < NH * NH; e += blockDim.x)
+        *reinterpret_cast<__nv_bfloat16*>(s.b2 + umma::kmajor_offset<NH>(e / NH, e % NH)) = net.w2[e];
+    if (tid < NH) {
+        s.bias1[tid] = net.b1[tid];
+        s.bias2[tid] = net.b2[tid];
+        s.w3[tid] = __bfloat162float(net.w3[tid]);
+    }
+    if (tid == 0) {
+        s.b3 = net.b3[0];
+        mbar_init(&s.bar, 1);
+    }
+    if (tid < 32) umma::tmem_alloc(&s.tmem, TC_COLS);
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+}
+
+// Per-CTA tear-down, by all threads: after a wait that ran past its limit, the MMAs still in
+// flight get one more bounded wait before their columns are released.
+__device__ __forceinline__ void mlp_tc_teardown(MlpTc& s, unsigned phase, bool broken) {
+    if (broken) mbar_wait(&s.bar, phase);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        umma::fence_after_sync();
+        umma::tmem_dealloc(s.tmem, TC_COLS);
+    }
+}
+
+// Row h * 256 + t of the network's input (x: its NF features), written by thread t.
+__device__ __forceinline__ void mlp_tc_put(MlpTc& s, int h, const float* x) {
+    const int row = h * TC_THREADS + threadIdx.x;
+    *reinterpret_cast<uint4*>(s.act + umma::kmajor_offset<NF>(row, 0)) =
+        make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
+    *reinterpret_cast<uint4*>(s.act + umma::kmajor_offset<NF>(row, 8)) =
+        make_uint4(pack_bf16(x[8], x[9]), pack_bf16(x[10], x[11]), pack_bf16(x[12], x[13]), pack_bf16(x[14], x[15]));
+}
+
+// Logits z[0], z[1] of this thread's rows t and 256 + t, whose features every thread has put
+// (mlp_tc_put); called by all 256 threads of the CTA.  phase: parity of the barrier's next
+// phase, the same in every thread.  A wait past its limit sets broken (uniformly): the network
+// is then not evaluated any more (-inf: not smooth) and the caller records the timeout.
+__device__ __forceinline__ void mlp_tc_eval(MlpTc& s, float* z, unsigned& phase, bool& broken) {
+    const int tid = threadIdx.x, warp = tid >> 5;
+    z[0] = z[1] = -INFINITY;
+    if (broken) return;
+    umma::fence_smem_to_async();
+    __syncthreads();
+    constexpr uint32_t ID = umma::idesc_bf16_f32<128, NH>();
+    constexpr uint32_t LBO = umma::KMAJOR_LBO, SBO1 = umma::kmajor_sbo<NF>(), SBO2 = umma::kmajor_sbo<NH>();
+    const uint32_t tm = s.tmem;
+    if (tid == 0) {
+        umma::fence_after_sync();
+#pragma unroll
+        for (int mt = 0; mt < TC_MTILES; ++mt)
+            umma::mma_bf16(tm + mt * NH, umma::smem_desc(s.act + mt * 128 * NF * 2, LBO, SBO1),
+                           umma::smem_desc(s.b1, LBO, SBO1), ID, 0);
+        umma::commit(&s.bar);
+    }
+    if (!__syncthreads_and(mbar_wait(&s.bar, phase))) {
+        broken = true;
+        return;
+    }
+    phase ^= 1u;
+    umma::fence_after_sync();
+    // row h * 256 + t sits in M tile 2 h + warp / 4, tensor-memory lane 32 (warp % 4) + lane
+    const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+    float d[NH];
+    // every layer-1 MMA has read the features: the activations overwrite them
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        umma::ld_32cols(tm + lanes + (uint32_t)(2 * h + (warp >> 2)) * NH, d);
+#pragma unroll
+        for (int q = 0; q < NH / 8; ++q) {
+            float a[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] = fmaxf(d[8 * q + k] + s.bias1[8 * q + k], 0.0f);
+            *reinterpret_cast<uint4*>(s.act + umma::kmajor_offset<NH>(h * TC_THREADS + tid, 8 * q)) =
+                make_uint4(pack_bf16(a[0], a[1]), pack_bf16(a[2], a[3]), pack_bf16(a[4], a[5]), pack_bf16(a[6], a[7]));
+        }
+    }
+    umma::fence_before_sync();
+    umma::fence_smem_to_async();
+    __syncthreads();
+    if (tid == 0) {
+        umma::fence_after_sync();
+#pragma unroll
+        for (int mt = 0; mt < TC_MTILES; ++mt)
+#pragma unroll
+            for (int ks = 0; ks < NH / 16; ++ks)
+                umma::mma_bf16(tm + mt * NH, umma::smem_desc(s.act + mt * 128 * NH * 2 + ks * 2 * LBO, LBO, SBO2),
+                               umma::smem_desc(s.b2 + ks * 2 * LBO, LBO, SBO2), ID, (uint32_t)ks);
+        umma::commit(&s.bar);
+    }
+    if (!__syncthreads_and(mbar_wait(&s.bar, phase))) {
+        broken = true;
+        return;
+    }
+    phase ^= 1u;
+    umma::fence_after_sync();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        umma::ld_32cols(tm + lanes + (uint32_t)(2 * h + (warp >> 2)) * NH, d);
+        float o = s.b3;
+#pragma unroll
+        for (int k = 0; k < NH; ++k)
+            o += __bfloat162float(__float2bfloat16_rn(fmaxf(d[k] + s.bias2[k], 0.0f))) * s.w3[k];
+        z[h] = o;
+    }
+    umma::fence_before_sync();
+}
+
 __device__ __forceinline__ unsigned mix_hash(unsigned x) {
     x ^= x >> 16;
     x *= 0x7feb352du;
@@ -250,14 +396,14 @@ constexpr int GATE_TILE = 16;   // 16 x 16 cells per block, one thread per cell
 // One block per 16 x 16 tile of cells, one thread per cell, both directions.  The tile and
 // its stencil halo are converted once to FP32 density and pressure in shared memory; the
 // features are read from there.  Stencils that leave the array get no flag (the face kernel
-// then reconstructs that cell with full WENO-AO).
+// then reconstructs that cell with full WENO-AO).  The network runs on the tcgen05 tensor
+// cores for the tile's 256 cells per direction (mlp: set up by the kernel, see mlp_tc_rows).
 // One 16 x 16 tile with first cell (i0, j0); tile_id numbers the tile for the audit draw.
+static_assert(GATE_TILE * GATE_TILE == TC_THREADS && GATE_THREADS == TC_THREADS, "two network rows per thread");
 template <int ORDER>
-__device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, const Geometry& geo, int i0, int j0,
-                                          unsigned tile_id) {
+__device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo, int i0, int j0, unsigned tile_id,
+                                          MlpTc& mlp, unsigned& phase, bool& broken) {
     constexpr int r = ORDER / 2, H = GATE_TILE + 2 * r;
-    __shared__ __align__(16) __nv_bfloat16 xs[GATE_THREADS / 32][32 * NF];
-    __shared__ float zs[GATE_THREADS / 32][32];
     __shared__ float srho[H][H + 1], sp[H][H + 1];
     __shared__ unsigned counts[4];           // cells x, cells y, smooth x, smooth y of the block
     if (a.ctl && !a.ctl->active) return;   // uniform over the block
@@ -294,12 +440,10 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, con
     const bool in = i < geo.nx && j < geo.ny;
     const size_t c = in ? (size_t)i * geo.ny + j : 0;
     unsigned char flag = 0;
-#pragma unroll
-    for (int dir = 0; dir < 2; ++dir) {
+    // features of this cell along dir (zero where the stencil leaves the array)
+    auto features = [&](int dir, float* f) {
         const int pos = dir == 0 ? i : j, n = dir == 0 ? geo.nx : geo.ny;
         const bool fits = in && pos >= r && pos < n - r;
-        const long long stride = dir == 0 ? geo.ny : 1;
-        float f[NF];
         if (fits) {
             float rs[ORDER], ps[ORDER];
 #pragma unroll
@@ -317,22 +461,31 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, con
 #pragma unroll
             for (int k = 0; k < NF; ++k) f[k] = 0.0f;
         }
-        __nv_bfloat16* row = xs[warp] + lane * NF;
+    };
+    // both directions' features into the network's input, then one pass over the tile's 512
+    // rows; sampled cells (collect mode) compute their features again afterwards
 #pragma unroll
-        for (int k = 0; k < NF; k += 2)
-            *reinterpret_cast<__nv_bfloat162*>(row + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
-        __syncwarp();
-        mlp16(net, xs[warp], nullptr, nullptr, zs[warp]);
-        mlp16(net, xs[warp] + 16 * NF, nullptr, nullptr, zs[warp] + 16);
-        __syncwarp();
-        const float z = zs[warp][lane];
-        const bool smooth = fits && z > a.threshold;
+    for (int dir = 0; dir < 2; ++dir) {
+        float f[NF];
+        features(dir, f);
+        mlp_tc_put(mlp, dir, f);
+    }
+    float zd[2];
+    mlp_tc_eval(mlp, zd, phase, broken);
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const int pos = dir == 0 ? i : j, n = dir == 0 ? geo.nx : geo.ny;
+        const bool fits = in && pos >= r && pos < n - r;
+        const long long stride = dir == 0 ? geo.ny : 1;
+        const bool smooth = fits && zd[dir] > a.threshold;
         const unsigned h = mix_hash((unsigned)c * 2u + (unsigned)dir + a.seed * 0x9e3779b9u);
         if (a.samples && fits && (h & a.sample_mask) == 0) {
             const float d = dir == 0 ? weight_distance<ORDER, 0>(a.W, plane, c, stride, gamma, geo.characteristic)
                                      : weight_distance<ORDER, 1>(a.W, plane, c, stride, gamma, geo.characteristic);
             const unsigned long long slot = atomicAdd(&a.stats->samples, 1ull);
             if (slot < a.capacity) {
+                float f[NF];
+                features(dir, f);
                 float* o = a.samples + slot * NS;
 #pragma unroll
                 for (int k = 0; k < NF; ++k) o[k] = f[k];
@@ -370,12 +523,24 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Net& net, con
         if (tid < 2) atomicAdd(&a.stats->cells[tid], (unsigned long long)counts[tid]);
         else if (tid < 4) atomicAdd(&a.stats->smooth[tid - 2], (unsigned long long)counts[tid]);
     }
+    // a tensor-core wait past its limit: the tile got no smooth flags (full WENO-AO, still
+    // correct); the problem's status records it and its next step does not start
+    if (broken && tid == 0 && a.ctl) atomicOr(const_cast<unsigned*>(&a.ctl->status), WAIT_TIMEOUT_BIT);
     __syncthreads();   // the shared arrays are reused by the block's next tile
 }
 
+// One block per 16 x 16 tile.  The kernel is latency bound (global loads, the two MMA round
+// trips): WENO5/7 tiles fit three blocks per SM in registers, WENO9 two.
 template <int ORDER>
-__global__ void __launch_bounds__(GATE_THREADS) gate_kernel(GateArgs a, Net net, Geometry geo) {
-    gate_tile<ORDER>(a, net, geo, blockIdx.y * GATE_TILE, blockIdx.x * GATE_TILE, blockIdx.y * gridDim.x + blockIdx.x);
+__global__ void __launch_bounds__(GATE_THREADS, ORDER == 9 ? 2 : 3) gate_kernel(GateArgs a, Net net, Geometry geo) {
+    __shared__ MlpTc mlp;
+    if (a.ctl && !a.ctl->active) return;   // uniform: nothing allocated yet
+    mlp_tc_setup(mlp, net);
+    unsigned phase = 0;
+    bool broken = false;
+    gate_tile<ORDER>(a, geo, blockIdx.y * GATE_TILE, blockIdx.x * GATE_TILE, blockIdx.y * gridDim.x + blockIdx.x, mlp,
+                     phase, broken);
+    mlp_tc_teardown(mlp, phase, broken);
 }
 
 }  // namespace gate

@@ -31,7 +31,8 @@ struct StepCtl {
     double t;            // simulation time at the end of the current step
     unsigned long long cfl_bits;  // running min of CFL candidates (positive doubles as bits)
     unsigned int status; // bit 0: negative density/pressure or NaN (reference would exit);
-                         // TMA_TIMEOUT_BIT: a tile load did not complete within its wait limit
+                         // WAIT_TIMEOUT_BIT: a TMA tile load or a tensor-core MMA did not
+                         // complete within its wait limit
     unsigned int active; // 0 once t >= tstop: the step's kernels return without work
     double tbeg;         // simulation time at the start of the current step (Block2d::t)
 };
@@ -297,7 +298,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         const bool ok = __syncthreads_and(aligned && mbar_wait(&tma_bar, 0));
         if (!ok) {
             // record the failure, let a load still in flight land, and leave the tile
-            if (tid == 0) atomicOr(const_cast<unsigned*>(&a.ctl->status), TMA_TIMEOUT_BIT);
+            if (tid == 0) atomicOr(const_cast<unsigned*>(&a.ctl->status), WAIT_TIMEOUT_BIT);
             if (aligned) mbar_wait(&tma_bar, 0);
             return;
         }

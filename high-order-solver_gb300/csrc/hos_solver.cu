@@ -765,7 +765,7 @@ int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
     if (t) *t = c.t;
     if (dt) *dt = c.dt;
     if (c.status & 1u) return fail(HOS_E_BLOWUP, "negative density/pressure or NaN in the state");
-    if (c.status & TMA_TIMEOUT_BIT) return fail(HOS_E_TIMEOUT, "a face kernel's TMA tile load did not complete");
+    if (c.status & WAIT_TIMEOUT_BIT) return fail(HOS_E_TIMEOUT, "a TMA tile load or tensor-core MMA did not complete within its wait limit");
     return HOS_OK;
 }
 

@@ -245,7 +245,7 @@ __device__ __forceinline__ void begin_step_one(StepCtl* ctl, double tstop, doubl
     // the driver loop runs while t < tstop; steps queued past it do nothing.  A problem whose
     // state went bad (status bit 0; the reference exits there) or whose step lost a tile to a
     // TMA load that never completed takes no further steps.
-    const bool go = t < tstop && !(ctl->status & (1u | TMA_TIMEOUT_BIT));
+    const bool go = t < tstop && !(ctl->status & (1u | WAIT_TIMEOUT_BIT));
     ctl->active = go ? 1u : 0u;
     ctl->tbeg = t;
     if (!go) return;

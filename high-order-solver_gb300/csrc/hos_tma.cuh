@@ -17,11 +17,12 @@ namespace hos {
 constexpr int MIRROR_PLANES = 6;
 __host__ __device__ __forceinline__ int mirror_pitch(int ny) { return (ny + 7) & ~7; }
 
-// waits on an mbarrier give up after this many polls (each poll may itself suspend the thread
-// for a short hardware-defined interval); a load that never completes then raises
-// TMA_TIMEOUT_BIT in the step's status word instead of hanging the kernel
-constexpr unsigned TMA_WAIT_POLLS = 1u << 22;
-constexpr unsigned TMA_TIMEOUT_BIT = 4u;
+// waits on an mbarrier give up after this many polls, each suspending the thread for at most
+// TMA_WAIT_HINT_NS (about a second in all); a TMA load or tensor-core MMA that never completes
+// then raises WAIT_TIMEOUT_BIT in the step's status word instead of hanging the kernel
+constexpr unsigned TMA_WAIT_POLLS = 1u << 20;
+constexpr unsigned TMA_WAIT_HINT_NS = 1000;
+constexpr unsigned WAIT_TIMEOUT_BIT = 4u;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -46,10 +47,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(TMA_WAIT_HINT_NS)
             : "memory");
         if (done) return true;
     }
