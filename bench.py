@@ -76,9 +76,10 @@ def parse():
     ap.add_argument("--n", type=int, default=N_CELLS, help=argparse.SUPPRESS)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched sweep")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D Taylor-Green leg")
-    ap.add_argument("--case", choices=["gated256", "tgv3d64"], default=None,
+    ap.add_argument("--case", choices=["gated256", "gated1024", "tgv3d64"], default=None,
                     help="small profiling case: gated256 = gate trained as in the bench, then 21 plain FP32 "
-                         "and 21 gated FP32 steps of the 256^2 WENO7 Riemann problem; tgv3d64 = 2 FP32 and "
+                         "and 21 gated FP32 steps of the 256^2 WENO7 Riemann problem; gated1024 = the same "
+                         "gate, then 2 gated FP32 steps of the 1024^2 problem; tgv3d64 = 2 FP32 and "
                          "1 FP64 steps of the 64^3 Taylor-Green vortex in NVTX ranges fp32 / fp64")
     return ap.parse_args()
 
@@ -468,7 +469,7 @@ def dgemm_tflops(torch, dev):
     return 3 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
 
 
-def profile_case():
+def profile_case(n=256, steps=21, plain=True):
     """The launches the ncu summaries under profiles/ capture (see --case): the steps run inside
     NVTX ranges "plain" and "gated" so that ncu --nvtx-include selects them."""
     import torch
@@ -478,14 +479,14 @@ def profile_case():
 
     gate, rep = gate_train.train(order=ORDER, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
                                  train_steps=3000, batch=4096)
-    pb, con, prim = cases.riemann2d(256, order=ORDER)
-    for gated in (False, True):
+    pb, con, prim = cases.riemann2d(n, order=ORDER)
+    for gated in ((False, True) if plain else (True,)):
         s = Solver2D(pb, FP32)
         s.set_state(con, prim)
         if gated:
             s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
         torch.cuda.nvtx.range_push("gated" if gated else "plain")
-        s.advance(21, 1e30, graph=False)
+        s.advance(steps, 1e30, graph=False)
         s.sync()
         torch.cuda.nvtx.range_pop()
         print("gated" if gated else "plain", s.gate_stats() if gated else "", flush=True)
@@ -525,6 +526,9 @@ def main():
         return
     if args.case == "gated256":
         profile_case()
+        return
+    if args.case == "gated1024":
+        profile_case(1024, 2, plain=False)
         return
     if args.case == "tgv3d64":
         profile_case_3d()

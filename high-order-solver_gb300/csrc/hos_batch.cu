@@ -278,8 +278,7 @@ int hos_batch2d_create(const hos_params2d* params, const double* tstop, int coun
         geo.nodey = p.nodey;
         geo.nx = p.nodex + 2 * p.ghost;
         geo.ny = p.nodey + 2 * p.ghost;
-        geo.dx = (p.right - p.left) / p.nodex;
-        geo.dy = (p.up - p.down) / p.nodey;
+        geo.set_spacing((p.right - p.left) / p.nodex, (p.up - p.down) / p.nodey);
         geo.cfl = p.cfl;
         geo.gamma = p.gamma;
         geo.K = p.K;

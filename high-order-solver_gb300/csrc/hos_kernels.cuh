@@ -50,6 +50,16 @@ struct Geometry {
     int tau_type = 0;
     double mu = -1.0, nu = -1.0, prandtl_coef = 0.0;
     int stages = 2;
+    // 1 / dx, 1 / dy, 1 / (dx dy), set on the host by set_spacing(): a double division costs the
+    // FP64 pipe about ten instructions per thread
+    double idx = 0.0, idy = 0.0, iarea = 0.0;
+    __host__ void set_spacing(double dx_, double dy_) {
+        dx = dx_;
+        dy = dy_;
+        idx = 1.0 / dx_;
+        idy = 1.0 / dy_;
+        iarea = 1.0 / (dx_ * dy_);
+    }
 };
 
 // Stages per step and Block2d::timecoefficient[s][k][f or derf] of each time-marching method
@@ -263,8 +273,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     const int nx = geo.nx, ny = geo.ny, g = geo.g;
     const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;  // faces along normal: nodeN + 1
     const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;  // faces along tangent: nodeT
-    const T hN = T(1.0 / (DIR == 0 ? geo.dx : geo.dy));   // inverse normal spacing
-    const T hT = T(1.0 / (DIR == 0 ? geo.dy : geo.dx));   // inverse face length
+    const T hN = T(DIR == 0 ? geo.idx : geo.idy);   // inverse normal spacing
+    const T hT = T(DIR == 0 ? geo.idy : geo.idx);   // inverse face length
     const T gamma = T(geo.gamma), K = T(geo.K);
     const size_t plane = (size_t)nx * ny;
     const int tid = threadIdx.x;
@@ -735,8 +745,15 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 }
             }
             // mean over Gauss points, zeroed below 2 (Calculate_alpha, :1497-1516)
-            const double as = double(asum);
-            double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
+            // FP64 divides as the reference does; the FP32 path takes the mean in FP32 (an
+            // indicator, not part of the FP64 stage combination) instead of a double division
+            double am;
+            if constexpr (sizeof(T) == 8) {
+                const double as = double(asum);
+                am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
+            } else {
+                am = double(GP == 2 ? T(0.5) * asum : GP == 3 ? asum * T(1.0 / 3.0) : T(0.25) * asum);
+            }
             a.FA[fi] = am < 2.0 ? 0.0 : am;
             if (s2o4 && a.stage == 1 && !geo.source) {
 #pragma unroll

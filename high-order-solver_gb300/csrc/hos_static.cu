@@ -109,8 +109,7 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
     geo.nodey = p.nodey;
     geo.nx = p.nodex + 2 * p.ghost;
     geo.ny = p.nodey + 2 * p.ghost;
-    geo.dx = (p.right - p.left) / p.nodex;
-    geo.dy = (p.up - p.down) / p.nodey;
+    geo.set_spacing((p.right - p.left) / p.nodex, (p.up - p.down) / p.nodey);
     geo.cfl = p.cfl;
     geo.gamma = p.gamma;
     geo.K = p.K;

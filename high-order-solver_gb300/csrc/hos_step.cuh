@@ -127,7 +127,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         const size_t fl = (size_t)I * nodey + J, fr = fl + nodey;
         const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
         // one reciprocal instead of four divisions: the FP64 pipe is the update's bound
-        const double iarea = 1.0 / (geo.dx * geo.dy);
+        const double iarea = geo.iarea;
         double w[4], w0[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
