@@ -15,14 +15,18 @@ struct FaceLaunch {
         using S = FaceSmem<T, ORDER>;
         const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;
         const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;
-        dim3 grid((nodeT + TILE_T - 1) / TILE_T, (nodeN + 1 + TILE_N - 1) / TILE_N);
-        const size_t smem = GATED ? S::gated_bytes : S::bytes;
         if constexpr (sizeof(T) == 4) {
             if (tm) {
-                face_kernel_tma<ORDER, DIR, GATED, NS><<<grid, FACE_THREADS, smem, s>>>(a, geo, tm[DIR]);
+                using TS = TmaTile<ORDER>;
+                using ST = FaceSmem<float, ORDER, TS>;
+                dim3 g((nodeT + TS::T - 1) / TS::T, (nodeN + 1 + TS::N - 1) / TS::N);
+                face_kernel_tma<ORDER, DIR, GATED, NS>
+                    <<<g, FACE_THREADS, GATED ? ST::gated_bytes : ST::bytes, s>>>(a, geo, tm[DIR]);
                 return cudaGetLastError();
             }
         }
+        dim3 grid((nodeT + TILE_T - 1) / TILE_T, (nodeN + 1 + TILE_N - 1) / TILE_N);
+        const size_t smem = GATED ? S::gated_bytes : S::bytes;
         face_kernel<T, ORDER, DIR, GATED, NS><<<grid, FACE_THREADS, smem, s>>>(a, geo);
         return cudaGetLastError();
     }
@@ -41,8 +45,11 @@ struct FaceLaunch {
         using S = FaceSmem<T, ORDER>;
         const size_t smem = GATED ? S::gated_bytes : S::bytes;
         cudaError_t e = attrs(face_kernel<T, ORDER, DIR, GATED, NS>, smem);
-        if constexpr (sizeof(T) == 4)
-            if (e == cudaSuccess) e = attrs(face_kernel_tma<ORDER, DIR, GATED, NS>, smem);
+        if constexpr (sizeof(T) == 4) {
+            using ST = FaceSmem<float, ORDER, TmaTile<ORDER>>;
+            if (e == cudaSuccess)
+                e = attrs(face_kernel_tma<ORDER, DIR, GATED, NS>, GATED ? ST::gated_bytes : ST::bytes);
+        }
         return e;
     }
     template <class T, bool GATED, bool NS = false>

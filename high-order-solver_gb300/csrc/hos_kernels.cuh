@@ -21,6 +21,7 @@
 // never travel to HBM.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include "hos_gks.cuh"
 #include "hos_tma.cuh"
 
@@ -159,12 +160,12 @@ struct FaceArgs {
     const float* AT32;
 };
 
-// A tile is TN faces along the normal by TT along the tangent, handled by one CTA of
-// 2 * TN * TT = 256 threads (one thread per face side in the tangential phase).
+// A tile is TN faces along the normal by TT along the tangent, handled by one CTA of 256
+// threads: 128 faces (one thread per face side in the tangential phase) or 256 faces (two).
 constexpr int FACE_THREADS = 256;
 template <int TN_, int TT_> struct TileShape {
     static constexpr int N = TN_, T = TT_;
-    static_assert(2 * TN_ * TT_ == FACE_THREADS, "a tile has 128 faces");
+    static_assert((2 * TN_ * TT_) % FACE_THREADS == 0, "a tile has 128 or 256 faces");
 };
 using DefaultTile = TileShape<8, 16>;
 constexpr int TILE_N = DefaultTile::N;    // default tile: 8 faces along the normal
@@ -479,10 +480,11 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     }
     __syncthreads();
 
-    // ---------------- phase 2: tangential reconstruction, one (face, side) per thread ----------------
-    {
-        const int side = tid & 1;
-        const int fidx = tid >> 1;                 // face within the tile
+    // ---------------- phase 2: tangential reconstruction, one (face, side) per thread and pass ----------------
+#pragma unroll 1
+    for (int item = tid; item < 2 * TILE_N * TILE_T; item += FACE_THREADS) {
+        const int side = item & 1;
+        const int fidx = item >> 1;                // face within the tile
         const int fn = fidx / TILE_T, ft = fidx % TILE_T;
         const int facen = N0 + fn, facet = T0 + ft;
         if (facen <= nodeN && facet < nodeT) {
@@ -689,8 +691,9 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     __syncthreads();
 
     // ---------------- phase 4: Gauss quadrature, S2O4 stage combination, face DF indicator ----------------
-    if (tid < TILE_N * TILE_T) {
-        const int fidx = tid, fn = fidx / TILE_T, ft = fidx % TILE_T;
+#pragma unroll 1
+    for (int fidx = tid; fidx < TILE_N * TILE_T; fidx += FACE_THREADS) {
+        const int fn = fidx / TILE_T, ft = fidx % TILE_T;
         const int facen = N0 + fn, facet = T0 + ft;
         if (facen <= nodeN && facet < nodeT) {
             const size_t nf = DIR == 0 ? (size_t)(geo.nodex + 1) * geo.nodey : (size_t)geo.nodex * (geo.nodey + 1);
@@ -778,14 +781,20 @@ __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_ker
     face_tile<T, ORDER, DIR, DefaultTile, GATED, NS>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
 }
 
+// Tile of the FP32 TMA face kernels: 16 x 16 faces for WENO5/7 (256 faces: every thread has
+// the same number of (face, Gauss point) flux items, 103 KB of shared memory at WENO7, two
+// CTAs per SM), 8 x 16 for WENO9 (its four Gauss points would need 137 KB at 16 x 16).
+template <int ORDER>
+using TmaTile = typename std::conditional<ORDER == 9, TileShape<8, 16>, TileShape<16, 16>>::type;
+
 // FP32 face kernel of the solvers with the pitched FP32 mirror: the tile is staged by one TMA
-// tile load (tmap: the mirror's tensor map, box TmaBox<ORDER, DIR>)
+// tile load (tmap: the mirror's tensor map, box TmaBox<ORDER, DIR, TmaTile<ORDER>>)
 template <int ORDER, int DIR, bool GATED = false, bool NS = false>
 __global__ void __launch_bounds__(FACE_THREADS, 2)
     face_kernel_tma(FaceArgs a, Geometry geo, const __grid_constant__ CUtensorMap tmap) {
+    using TS = TmaTile<ORDER>;
     extern __shared__ __align__(128) unsigned char smem_tma[];
-    face_tile<float, ORDER, DIR, DefaultTile, GATED, NS, true>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T,
-                                                               smem_tma, &tmap);
+    face_tile<float, ORDER, DIR, TS, GATED, NS, true>(a, geo, blockIdx.y * TS::N, blockIdx.x * TS::T, smem_tma, &tmap);
 }
 
 }  // namespace hos

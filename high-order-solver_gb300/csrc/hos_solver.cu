@@ -147,7 +147,7 @@ static int cuda_fail(cudaError_t e, const char* where) {
 }
 
 // Tensor maps of the FP32 mirror (base: nx rows of ny cells at pitch mirror_pitch(ny), six
-// planes) with the x-face and the y-face tile boxes of the given WENO order.  The encoder is
+// planes) with the x-face and the y-face tile boxes of the given WENO order's TMA face tile.  The encoder is
 // the driver's cuTensorMapEncodeTiled, fetched through the runtime so that the library does not
 // link libcuda.  Cells past ny in a row read as zero (the out-of-bounds fill).
 static int encode_mirror_maps(CUtensorMap* maps, float* base, int nx, int ny, int order) {
@@ -162,9 +162,12 @@ static int encode_mirror_maps(CUtensorMap* maps, float* base, int nx, int ny, in
     }
     int bx[2], by[2];
     switch (order) {
-        case 5: bx[0] = TmaBox<5, 0>::X; by[0] = TmaBox<5, 0>::Y; bx[1] = TmaBox<5, 1>::X; by[1] = TmaBox<5, 1>::Y; break;
-        case 7: bx[0] = TmaBox<7, 0>::X; by[0] = TmaBox<7, 0>::Y; bx[1] = TmaBox<7, 1>::X; by[1] = TmaBox<7, 1>::Y; break;
-        default: bx[0] = TmaBox<9, 0>::X; by[0] = TmaBox<9, 0>::Y; bx[1] = TmaBox<9, 1>::X; by[1] = TmaBox<9, 1>::Y; break;
+        case 5: bx[0] = TmaBox<5, 0, TmaTile<5>>::X; by[0] = TmaBox<5, 0, TmaTile<5>>::Y;
+                 bx[1] = TmaBox<5, 1, TmaTile<5>>::X; by[1] = TmaBox<5, 1, TmaTile<5>>::Y; break;
+        case 7: bx[0] = TmaBox<7, 0, TmaTile<7>>::X; by[0] = TmaBox<7, 0, TmaTile<7>>::Y;
+                 bx[1] = TmaBox<7, 1, TmaTile<7>>::X; by[1] = TmaBox<7, 1, TmaTile<7>>::Y; break;
+        default: bx[0] = TmaBox<9, 0, TmaTile<9>>::X; by[0] = TmaBox<9, 0, TmaTile<9>>::Y;
+                 bx[1] = TmaBox<9, 1, TmaTile<9>>::X; by[1] = TmaBox<9, 1, TmaTile<9>>::Y; break;
     }
     const cuuint64_t pitch = (cuuint64_t)mirror_pitch(ny);
     const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)MIRROR_PLANES};
