@@ -47,11 +47,12 @@ FLOP_PER_FACE = 24028.0
 BYTES_PER_FACE = 120.0
 # dram__bytes_read + write per face of one face-kernel launch (ncu, 256^2 case: 4.02 MB / 65,792)
 TRAFFIC_PER_FACE = 61.0
-# FP32 operations (2 x FFMA + FADD + FMUL) one gated FP32 face-kernel launch executes per face,
-# and its DRAM traffic per face (ncu, 256^2 Riemann WENO7 after 20 steps; the plain FP32
-# kernel executes 17,998 per face)
-FP32_FLOP_PER_FACE_GATED = 7586.0
-TRAFFIC_PER_FACE_FP32 = 86.4
+# FP32 operations (2 x FFMA + FADD + FMUL) one gated FP32 face-kernel launch (TMA staging,
+# 16 x 16-face tiles) executes per face, and its DRAM traffic per face averaged over the
+# stage-0 and stage-1 launches (ncu, --case gated1024: 1024^2 Riemann WENO7, 7.04e9 flop and
+# 46-71 MB per launch over 1,049,600 faces)
+FP32_FLOP_PER_FACE_GATED = 6716.0
+TRAFFIC_PER_FACE_FP32 = 55.7
 AUDIT_LOG2 = 10   # audit one warp in 1024 of predicted-smooth cells with full weights
 N_3D = 256        # cells per side of the 3D Taylor-Green leg
 # 3D point kernel (tangential point sweep + GKS3D at 4 Gauss points + FP64 stage combination):
@@ -687,7 +688,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(2 * host_in.numel() * 8),
                 "d2h_bytes_per_step": int(host_out.numel() * 8)},
         "gpu_launches": launches,
-        "roofline": {"kernel": "face_kernel<float,7,x|y,gated>", "bound": "fp32", "unit": "TFLOP/s",
+        "roofline": {"kernel": "face_kernel_tma<7,x|y,gated>", "bound": "fp32", "unit": "TFLOP/s",
                      "achieved": fl_g, "peak": fp32_peak, "frac": fl_g / fp32_peak,
                      "peak_source": "cuBLAS SGEMM 8192^3 (no TF32) measured in this run",
                      "flop_per_face": FP32_FLOP_PER_FACE_GATED, "launch_ms": face_g,

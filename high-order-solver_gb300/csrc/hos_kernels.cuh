@@ -51,15 +51,14 @@ struct Geometry {
     int tau_type = 0;
     double mu = -1.0, nu = -1.0, prandtl_coef = 0.0;
     int stages = 2;
-    // 1 / dx, 1 / dy, 1 / (dx dy), set on the host by set_spacing(): a double division costs the
-    // FP64 pipe about ten instructions per thread
-    double idx = 0.0, idy = 0.0, iarea = 0.0;
+    // 1 / dx, 1 / dy, set on the host by set_spacing(): a double division costs the FP64 pipe
+    // about ten instructions per thread
+    double idx = 0.0, idy = 0.0;
     __host__ void set_spacing(double dx_, double dy_) {
         dx = dx_;
         dy = dy_;
         idx = 1.0 / dx_;
         idy = 1.0 / dy_;
-        iarea = 1.0 / (dx_ * dy_);
     }
 };
 

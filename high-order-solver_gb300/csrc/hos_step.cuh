@@ -126,8 +126,9 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         const size_t nfx = (size_t)(nodex + 1) * nodey, nfy = (size_t)nodex * (nodey + 1);
         const size_t fl = (size_t)I * nodey + J, fr = fl + nodey;
         const size_t fd = (size_t)I * (nodey + 1) + J, fu = fd + 1;
-        // one reciprocal instead of four divisions: the FP64 pipe is the update's bound
-        const double iarea = geo.iarea;
+        // the FP64 pipe is the update's bound: the flux balance
+        // (dx (F_down - F_up) + dy (F_left - F_right)) / (dx dy) is taken as two differences
+        // scaled by 1 / dy and 1 / dx (precomputed), not as four products and a division
         double w[4], w0[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
@@ -143,11 +144,8 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 old = a.Wold[v * plane + c];
             }
             w0[v] = cur;
-            double total = 0.0;
-            total += geo.dx * a.FXy[v * nfy + fd];
-            total += -geo.dx * a.FXy[v * nfy + fu];
-            total += geo.dy * a.FXx[v * nfx + fl];
-            total += -geo.dy * a.FXx[v * nfx + fr];
+            const double rate = (a.FXy[v * nfy + fd] - a.FXy[v * nfy + fu]) * geo.idy +
+                                (a.FXx[v * nfx + fl] - a.FXx[v * nfx + fr]) * geo.idx;
             if (geo.source) {
                 // Update_with_source under S2O4 (src/time_advance.cpp:534-704): stage 0 takes
                 // W_old + dt (L + S), S = (0, 0, rho, rho v) of the stage's state; stage 1
@@ -156,16 +154,16 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                     // the stage's state: w0[0] and w0[2] hold rho and rho v read before this
                     // loop wrote the new values
                     const double S = v == 2 ? w0[0] : v == 3 ? w0[2] : 0.0;
-                    w[v] = old + (total * iarea + a.ctl->dt * S);
+                    w[v] = old + (rate + a.ctl->dt * S);
                 } else {
                     w[v] = cur;
                 }
             } else if (geo.integrator == 4 && a.stage == 1)        // RK3 (Update_with_gauss_RK3, :511-526)
-                w[v] = 0.75 * old + 0.25 * cur + total * iarea;
+                w[v] = 0.75 * old + 0.25 * cur + rate;
             else if (geo.integrator == 4 && a.stage == 2)
-                w[v] = 1.0 / 3.0 * old + 2.0 / 3.0 * cur + total * iarea;
+                w[v] = 1.0 / 3.0 * old + 2.0 / 3.0 * cur + rate;
             else
-                w[v] = old + total * iarea;
+                w[v] = old + rate;
             a.W[v * plane + c] = w[v];
             if (a.W32) a.W32[v * plane32 + cm] = (float)w[v];
         }
