@@ -62,7 +62,10 @@ __global__ void __launch_bounds__(256) bc3_kernel(double* __restrict__ W, Geo3 g
     }
 }
 
-__device__ __forceinline__ double cfl_candidate3(const double* w, const Geo3& g, unsigned& bad, bool is_prim) {
+// with_cfl false: the state check alone (stage 1 takes no candidates; the square roots and
+// divisions of the candidate are the FP64 pipe's largest cost in the update)
+__device__ __forceinline__ double cfl_candidate3(const double* w, const Geo3& g, unsigned& bad, bool is_prim,
+                                                 bool with_cfl = true) {
     double pr[5];
     if (is_prim) {
         for (int v = 0; v < 5; ++v) pr[v] = w[v];
@@ -75,6 +78,7 @@ __device__ __forceinline__ double cfl_candidate3(const double* w, const Geo3& g,
         pr[4] = (g.gamma - 1.0) * (w[4] - 0.5 * (w[1] * pr[1] + w[2] * pr[2] + w[3] * pr[3]));
     }
     bad = (pr[0] < 0 || pr[4] < 0 || isnan(pr[0]) || isnan(pr[4])) ? 1u : 0u;
+    if (!with_cfl) return 1e300;
     // Dtx_3d (src/time_advance.cpp:826-848)
     const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + sqrt(g.gamma * pr[4] / pr[0]);
     double q = g.cfl * g.rc / tmp;
@@ -127,7 +131,7 @@ __global__ void __launch_bounds__(256) update3_kernel(double* __restrict__ W, do
         load_flux3(FY, ly.n(), ly.idx(J + 1, Ib, K), yr);
         load_flux3(FZ, lz.n(), lz.idx(K, J, Ib), zl);
         load_flux3(FZ, lz.n(), lz.idx(K + 1, J, Ib), zr);
-        const double idx_ = 1.0 / g.dx, idy = 1.0 / g.dy, idz = 1.0 / g.dz;
+        const double idx_ = g.idx, idy = g.idy, idz = g.idz;
         // global-frame flux differences: y faces (u, v) = (-v', u'), z faces (u, w) = (-w', u')
         double tot[5];
         tot[0] = idz * (zl[0] - zr[0]) + idy * (yl[0] - yr[0]) + idx_ * (xl[0] - xr[0]);
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(256) update3_kernel(double* __restrict__ W, do
             w[v] = old + tot[v];
             W[v * plane + c] = w[v];
         }
-        const double q = cfl_candidate3(w, g, bad, false);
+        const double q = cfl_candidate3(w, g, bad, false, stage == 0);
         if (stage == 0) cand = q;
     }
     reduce3(cand, bad, ctl, stage == 0);
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(256) cfl3_init_kernel(const double* __restrict
 __global__ void begin3_kernel(Ctl3* ctl, double tstop, double seed, int first) {
     if (!first) ctl->step += ctl->active ? 1 : 0;
     const double t = ctl->t;
-    const bool go = t < tstop && !(ctl->status & 1u);
+    const bool go = t < tstop && !(ctl->status & (1u | WAIT_TIMEOUT_BIT));
     ctl->active = go ? 1u : 0u;
     ctl->tbeg = t;
     double dt = __longlong_as_double((long long)ctl->cfl_bits);
@@ -263,6 +267,9 @@ Dir3 make_dir(const Geo3& g, int dir) {
     if (dir == 0) { d.n0 = g.nodex; d.n1 = g.nodey; d.n2 = g.nodez; d.hn = g.dx; d.h1 = g.dy; d.h2 = g.dz; }
     else if (dir == 1) { d.n0 = g.nodey; d.n1 = g.nodex; d.n2 = g.nodez; d.hn = g.dy; d.h1 = g.dx; d.h2 = g.dz; }
     else { d.n0 = g.nodez; d.n1 = g.nodey; d.n2 = g.nodex; d.hn = g.dz; d.h1 = g.dy; d.h2 = g.dx; }
+    d.ihn = 1.0 / d.hn;
+    d.ih1 = 1.0 / d.h1;
+    d.ih2 = 1.0 / d.h2;
     const int af = dir == 2 ? 1 : 0;
     d.fv = Lay{d.n0 + 1, d.n1 + 4, d.n2 + 4, af};
     d.cel = Lay{d.n0 + 2, d.n1 + 4, d.n2 + 4, af};
@@ -382,6 +389,9 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
     g.dx = (p.right - p.left) / p.nodex;
     g.dy = (p.up - p.down) / p.nodey;
     g.dz = (p.front - p.back) / p.nodez;
+    g.idx = 1.0 / g.dx;
+    g.idy = 1.0 / g.dy;
+    g.idz = 1.0 / g.dz;
     g.rc = g.dx;
     if (g.dy < g.rc) g.rc = g.dy;
     if (g.dz < g.rc) g.rc = g.dz;
@@ -522,6 +532,8 @@ int hos3d_sync(hos_solver3d* s, double* t, double* dt) {
     if (t) *t = c.t;
     if (dt) *dt = c.dt;
     if (c.status & 1u) return fail3(HOS_E_BLOWUP, "negative density/pressure or NaN in the state");
+    if (c.status & WAIT_TIMEOUT_BIT)
+        return fail3(HOS_E_TIMEOUT, "a tensor-core MMA of the gate did not complete within its wait limit");
     return HOS_OK;
 }
 

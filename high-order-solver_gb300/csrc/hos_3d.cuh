@@ -28,7 +28,8 @@ namespace d3 {
 struct Ctl3 {
     double dt, t;
     unsigned long long cfl_bits;  // running min of CFL candidates (positive doubles as bits)
-    unsigned int status, active;  // status bit 0: negative density/pressure or NaN
+    unsigned int status, active;  // status bit 0: negative density/pressure or NaN; WAIT_TIMEOUT_BIT:
+                                  // a tensor-core MMA of the gate ran past its wait limit
     int step, pad;
     double tbeg;
 };
@@ -36,6 +37,7 @@ struct Ctl3 {
 struct Geo3 {
     int nx, ny, nz, g, nodex, nodey, nodez;
     double dx, dy, dz, rc, cfl, gamma, K, c1, c2, mu;
+    double idx, idy, idz;   // 1 / dx, 1 / dy, 1 / dz (host)
     int tau_type, characteristic;
     int bc[6];
 };
@@ -68,6 +70,7 @@ struct Dir3 {
     int dir;
     int n0, n1, n2;
     double hn, h1, h2;
+    double ihn, ih1, ih2;   // their inverses, computed on the host (no FP64 division per thread)
     Lay fv;   // face values: faces 0..n0, b in [-2, n1+2), c in [-2, n2+2)
     Lay cel;  // face3 thread space: cells -1..n0 of the normal, fv's b and c
     Lay lv;   // line values: faces 0..n0, b interior, c in [-2, n2+2)
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const double* __re
     d.cel.decode(t, a0, b0, c0);
     const int ac = a0 - 1, G = g.g;
     const size_t plane = (size_t)g.nx * g.ny * g.nz;
-    const T gamma = T(g.gamma), K = T(g.K), ih = T(1.0 / d.hn);
+    const T gamma = T(g.gamma), K = T(g.K), ih = T(d.ihn);
     T st[5][5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -728,7 +731,7 @@ __global__ void __launch_bounds__(LINE3_THREADS) line3_kernel(const T* __restric
     int a, b, c;
     d.lv.decode(t, a, b, c);
     const size_t nfv = d.fv.n(), nlv = d.lv.n();
-    const T ih = T(1.0 / d.h1), K = T(g.K);
+    const T ih = T(d.ih1), K = T(g.K);
     bool reduce = false;
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
@@ -812,7 +815,7 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
     int a = 0, b = 0, c = 0;
     if (valid) {
         d.fs.decode(face, a, b, c);
-        const T ih = T(1.0 / d.h2), K = T(g.K), dt = T(ctl->dt);
+        const T ih = T(d.ih2), K = T(g.K), dt = T(ctl->dt);
         // point states: [ip][side][value | normal | t1 | t2 slope][5]
         T pt[2][2][4][5];
         bool reduce = false;

@@ -93,31 +93,39 @@ __global__ void __launch_bounds__(256) density_pressure3(GateRun3 r) {
     r.rp[c] = make_float2(float(rho), float((r.g.gamma - 1.0) * (e - 0.5 * (mx * mx + my * my + mz * mz) / rho)));
 }
 
-__global__ void __launch_bounds__(GATE3_THREADS) gate3_kernel(GateRun3 r) {
+// One thread per cell, three rows of the network per cell (one per axis): the block's 768
+// rows go through the tcgen05 routine of the 2D gate in two 512-row passes (axes x and y,
+// then z with an empty second half).
+__global__ void __launch_bounds__(GATE3_THREADS, 3) gate3_kernel(GateRun3 r) {
     using namespace gate;
-    __shared__ __align__(16) __nv_bfloat16 xs[GATE3_THREADS / 32][32 * NF];
-    __shared__ float zs[GATE3_THREADS / 32][32];
+    static_assert(GATE3_THREADS == TC_THREADS, "two network rows per thread and pass");
+    __shared__ MlpTc mlp;
     __shared__ unsigned counts[6];   // cells x, y, z; smooth x, y, z of the block
     if (r.ctl && !r.ctl->active) return;   // uniform over the grid
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid < 6) counts[tid] = 0;
-    __syncthreads();
+    mlp_tc_setup(mlp, r.net);   // synchronises the block
+    unsigned phase = 0;
+    bool broken = false;
     const Geo3& g = r.g;
     const size_t plane = (size_t)g.nx * g.ny * g.nz;
     const size_t c = (size_t)blockIdx.x * GATE3_THREADS + tid;
     const bool in = c < plane;
     const int k = in ? (int)(c % g.nz) : 0, j = in ? (int)((c / g.nz) % g.ny) : 0;
     const int i = in ? (int)(c / ((size_t)g.nz * g.ny)) : 0;
-    unsigned char flag = 0;
-#pragma unroll 1
-    for (int ax = 0; ax < 3; ++ax) {
+    auto stride_of = [&](int ax) {
+        return ax == 0 ? (size_t)g.ny * g.nz : ax == 1 ? (size_t)g.nz : (size_t)1;
+    };
+    auto fits_of = [&](int ax) {
         const int pos = ax == 0 ? i : ax == 1 ? j : k, n = ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz;
-        const size_t stride = ax == 0 ? (size_t)g.ny * g.nz : ax == 1 ? (size_t)g.nz : 1;
-        const bool fits = in && pos >= 2 && pos < n - 2;
-        float f[NF];
+        return in && pos >= 2 && pos < n - 2;
+    };
+    // features of this cell along axis ax (zero where the stencil leaves the array)
+    auto features = [&](int ax, float* f) {
 #pragma unroll
         for (int q = 0; q < NF; ++q) f[q] = 0.0f;
-        if (fits) {
+        if (fits_of(ax)) {
+            const size_t stride = stride_of(ax);
             float rs[5], ps[5];
 #pragma unroll
             for (int m = 0; m < 5; ++m) {
@@ -128,21 +136,37 @@ __global__ void __launch_bounds__(GATE3_THREADS) gate3_kernel(GateRun3 r) {
             indicator5(rs, f);
             indicator5(ps, f + 7);
         }
-        __nv_bfloat16* row = xs[warp] + lane * NF;
+    };
+    float z[3];
+    {
+        float f[NF];
+        features(0, f);
+        mlp_tc_put(mlp, 0, f);
+        features(1, f);
+        mlp_tc_put(mlp, 1, f);
+        mlp_tc_eval(mlp, z, phase, broken);
+        features(2, f);
+        mlp_tc_put(mlp, 0, f);
 #pragma unroll
-        for (int q = 0; q < NF; q += 2)
-            *reinterpret_cast<__nv_bfloat162*>(row + q) = __floats2bfloat162_rn(f[q], f[q + 1]);
-        __syncwarp();
-        mlp16(r.net, xs[warp], nullptr, nullptr, zs[warp]);
-        mlp16(r.net, xs[warp] + 16 * NF, nullptr, nullptr, zs[warp] + 16);
-        __syncwarp();
-        const float z = zs[warp][lane];
-        const bool smooth = fits && z > r.threshold;
+        for (int q = 0; q < NF; ++q) f[q] = 0.0f;
+        mlp_tc_put(mlp, 1, f);
+        float zz[2];
+        mlp_tc_eval(mlp, zz, phase, broken);
+        z[2] = zz[0];
+    }
+    unsigned char flag = 0;
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        const size_t stride = stride_of(ax);
+        const bool fits = fits_of(ax);
+        const bool smooth = fits && z[ax] > r.threshold;
         const unsigned h = mix_hash((unsigned)c * 3u + (unsigned)ax + r.seed * 0x9e3779b9u);
         if (r.samples && fits && (h & r.sample_mask) == 0) {
             const float d = weight_distance3(r.W, g, c, stride, ax);
             const unsigned long long slot = atomicAdd(r.sample_count, 1ull);
             if (slot < r.capacity) {
+                float f[NF];
+                features(ax, f);
                 float* o = r.samples + slot * NS;
 #pragma unroll
                 for (int q = 0; q < NF; ++q) o[q] = f[q];
@@ -168,7 +192,6 @@ __global__ void __launch_bounds__(GATE3_THREADS) gate3_kernel(GateRun3 r) {
             }
         }
         flag |= smooth ? (unsigned char)(1u << ax) : (unsigned char)0;
-        __syncwarp();
     }
     if (r.flags) {
         if (in) r.flags[c] = flag;
@@ -176,6 +199,10 @@ __global__ void __launch_bounds__(GATE3_THREADS) gate3_kernel(GateRun3 r) {
         if (tid < 3) atomicAdd(&r.stats->cells[tid], (unsigned long long)counts[tid]);
         else if (tid < 6) atomicAdd(&r.stats->smooth[tid - 3], (unsigned long long)counts[tid]);
     }
+    // a tensor-core wait past its limit: the block's cells got no smooth flags (full WENO-AO,
+    // still correct); the solver's status records it and its next step does not start
+    if (broken && tid == 0 && r.ctl) atomicOr(const_cast<unsigned*>(&r.ctl->status), WAIT_TIMEOUT_BIT);
+    mlp_tc_teardown(mlp, phase, broken);
 }
 
 }  // namespace

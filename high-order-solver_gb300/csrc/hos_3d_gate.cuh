@@ -1,7 +1,7 @@
 // hos_3d_gate.cuh -- the learned smoothness gate on the 3D FP32-bulk path.
 //
 // The network, its training and its sample format are those of the 2D gate (hos_gate.cuh):
-// a 16 -> 32 -> 32 -> 1 BF16 MLP on the tensor cores.  Its inputs for one cell and one
+// a 16 -> 32 -> 32 -> 1 BF16 MLP, evaluated on the tcgen05 tensor cores by the 2D gate's routine.  Its inputs for one cell and one
 // global axis are the normalised smoothness indicators of the cell's WENO5-AO stencil along
 // that axis (the three small-stencil betas, the big-stencil beta padded to 6, and tau) for
 // density and for pressure; there is no discontinuity-feedback indicator in 3D (inputs 14
