@@ -283,6 +283,57 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
                 "aposteriori_rejections": gst["fallback"]}}
 
 
+def vortex_leg(sizes=(50, 100, 200, 400)):
+    """The isentropic vortex on the periodic [0, 10]^2 (unit freestream, strength 5, WENO5-AO-DF,
+    characteristic, CFL 0.5) run to t = 2 in FP64 and in FP32 bulk at each size: density L1 / L-inf
+    error against the exact solution (the initial vortex moved by (2, 2)), the FP32 path's
+    deviation from FP64, the L1 / L-inf convergence order between the sizes, and the throughput
+    of the whole run (graph-captured steps, wall time by CUDA-synchronised host clock)."""
+    from hos_gb300 import cases
+    from hos_gb300.solver import FP32, FP64, Solver2D
+
+    out = {"workload": "isentropic_vortex_periodic10_weno5ao_df_char_gp2_t2", "sizes": {}}
+    l1, linf = {}, {}
+    for n in sizes:
+        pb, con, prim = cases.isentropic_vortex(n, order=5)
+        _, exact, _ = cases.isentropic_vortex(n, order=5, center=(7.0, 7.0))
+        g = pb.ghost
+        ex = exact[g:-g, g:-g, 0]
+        row = {}
+        rho = {}
+        for name, prec in (("fp64", FP64), ("fp32_bulk", FP32)):
+            # the run to t = 2 one step per call counts the steps; a second run queues exactly
+            # that many steps behind one synchronisation for the throughput
+            s = Solver2D(pb, prec)
+            s.set_state(con, prim)
+            nsteps = s.run(2.0, graph=True, check_every=1)
+            r = s.get_state()["convar"][g:-g, g:-g, 0]
+            s.close()
+            s = Solver2D(pb, prec)
+            s.set_state(con, prim)
+            s.sync()
+            t0 = time.perf_counter()
+            s.advance(nsteps, 2.0, graph=True)
+            s.sync()
+            wall = time.perf_counter() - t0
+            s.close()
+            e = np.abs(r - ex)
+            rho[name] = r
+            row[name] = {"l1": float(e.mean()), "linf": float(e.max()), "steps": int(nsteps),
+                         "cell_updates_per_s": pb.nodex * pb.nodey * nsteps / wall}
+        d = np.abs(rho["fp32_bulk"] - rho["fp64"])
+        row["rho_rel_l1_fp32_vs_fp64"] = float(d.mean() / np.abs(rho["fp64"]).mean())
+        row["rho_rel_linf_fp32_vs_fp64"] = float(d.max() / np.abs(rho["fp64"]).max())
+        out["sizes"][f"{n}x{n}"] = row
+        l1[n], linf[n] = row["fp64"]["l1"], row["fp64"]["linf"]
+    # orders between consecutive sizes; from 200^2 on the error nears the floor of the initial
+    # data's non-periodic tail (a velocity jump of up to 2.4e-5 across the boundary)
+    out["order_fp64"] = {f"{a}-{b}": {"l1": float(np.log2(l1[a] / l1[b]) / np.log2(b / a)),
+                                      "linf": float(np.log2(linf[a] / linf[b]) / np.log2(b / a))}
+                         for a, b in zip(sizes, sizes[1:])}
+    return out
+
+
 def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n512=True):
     """3D Taylor-Green vortex, n^3 cells (WENO5-AO on 2 x 2 Gauss points per face, GKS3D with
     the Navier-Stokes collision time, S2O4): gated FP32 bulk (the learned gate trained on the
@@ -723,6 +774,7 @@ def main():
     }
     if ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
+    line["variants"]["vortex2d"] = vortex_leg()
     if not args.no_3d:
         line["variants"]["tgv3d"] = tgv3d_leg(torch, dev, flush, args.steps, args.warmup, fp32_peak, fp64_peak)
     if not args.no_batch:
