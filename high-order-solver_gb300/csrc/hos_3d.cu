@@ -107,6 +107,26 @@ __device__ __forceinline__ void load_flux3(const double* FS, size_t nf, size_t f
     for (int v = 0; v < 5; ++v) out[v] = FS[v * nf + f];
 }
 
+// FP32 solvers, once per stage after the ghost fill: the FP32 mirror of the whole state
+// (ghosts included) that the FP32 face kernels read, and -- with the gate on -- each cell's FP32
+// (density, pressure) pair for the gate's features.  GB300's FP64 pipe converts at 1/64 of the
+// FP32 rate: converting once per cell here replaces the 25 conversions per cell and direction
+// the face kernel would make.
+__global__ void __launch_bounds__(256) mirror3_kernel(const double* __restrict__ W, float* __restrict__ W32,
+                                                      float2* __restrict__ rp, size_t plane, float gamma,
+                                                      const Ctl3* ctl) {
+    if (!ctl->active) return;
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= plane) return;
+    float w[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        w[v] = (float)W[v * plane + c];
+        W32[v * plane + c] = w[v];
+    }
+    if (rp) rp[c] = make_float2(w[0], (gamma - 1.0f) * (w[4] - 0.5f * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]) / w[0]));
+}
+
 // W = W_old + sum over the six faces; y and z face fluxes turned back to the global frame
 // (src/time_advance.cpp:942-997).  Stage 0 takes the snapshot W_old and produces the next
 // step's CFL candidates from its new state; every stage flags a bad state.
@@ -230,6 +250,7 @@ struct hos_solver3d {
     Dir3 dirs[3];
     cudaStream_t stream = nullptr;
     double *W = nullptr, *Wold = nullptr, *stage_buf = nullptr;
+    float* W32 = nullptr;   // FP32 solvers: the FP32 mirror of W, refreshed once per stage
     double* FS[3] = {nullptr, nullptr, nullptr};
     void *FV = nullptr, *LV = nullptr;
     Ctl3* ctl = nullptr;
@@ -254,7 +275,7 @@ void free3(hos_solver3d* s) {
         if (x) cudaFree(x);
     if (s->FV) cudaFree(s->FV);
     if (s->LV) cudaFree(s->LV);
-    void* gbufs[] = {s->gflags, s->grp, s->gstats, s->gw, s->gb};
+    void* gbufs[] = {s->gflags, s->grp, s->gstats, s->gw, s->gb, s->W32};
     for (void* x : gbufs)
         if (x) cudaFree(x);
     if (s->ctl) cudaFree(s->ctl);
@@ -282,8 +303,8 @@ cudaError_t flux_dir(hos_solver3d* s, int dir, int stage, cudaEvent_t* ev) {
     const Dir3& d = s->dirs[dir];
     const Gate3 gt{s->gated ? s->gflags : nullptr, s->gated ? &s->gstats->fallback : nullptr};
     if (s->precision == HOS_FP32)
-        return launch_flux3<float>(s->W, (float*)s->FV, (float*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream, ev,
-                                   gt);
+        return launch_flux3<float>(s->W32, (float*)s->FV, (float*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream,
+                                   ev, gt);
     return launch_flux3<double>(s->W, (double*)s->FV, (double*)s->LV, s->FS[dir], s->geo, d, s->ctl, stage, s->stream, ev,
                                 gt);
 }
@@ -314,6 +335,11 @@ int enqueue_begin3(hos_solver3d* s, double tstop, cudaEvent_t ev) {
 int enqueue_stage3(hos_solver3d* s, int stage, cudaEvent_t* ev) {
     const Geo3& g = s->geo;
     bc3_kernel<<<blocks((size_t)g.nx * g.ny * g.nz, 256), 256, 0, s->stream>>>(s->W, g, s->ctl);
+    if (s->W32) {
+        const size_t plane = (size_t)g.nx * g.ny * g.nz;
+        mirror3_kernel<<<blocks(plane, 256), 256, 0, s->stream>>>(s->W, s->W32, s->gated ? s->grp : nullptr, plane,
+                                                                  (float)g.gamma, s->ctl);
+    }
     if (ev) cudaEventRecord(ev[0], s->stream);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && s->gated) {
@@ -324,7 +350,7 @@ int enqueue_stage3(hos_solver3d* s, int stage, cudaEvent_t* ev) {
         r.threshold = s->gthreshold;
         r.audit_mask = s->gaudit_mask;
         r.seed = s->gseed++;
-        e = launch_gate3(r, s->stream);
+        e = launch_gate3(r, s->stream, /*rp_ready=*/true);   // mirror3 wrote the (density, pressure) pairs
     }
     if (ev) cudaEventRecord(ev[1], s->stream);
     for (int dir = 0; dir < 3 && e == cudaSuccess; ++dir) {
@@ -426,8 +452,10 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
         {(void**)&s->FS[2], 10 * s->dirs[2].fs.n() * sizeof(double)},
         {&s->FV, 20 * nfv * tsz},
         {&s->LV, 60 * nlv * tsz},
-        {(void**)&s->ctl, sizeof(Ctl3)}};
+        {(void**)&s->ctl, sizeof(Ctl3)},
+        {(void**)&s->W32, precision == HOS_FP32 ? 5 * s->ncell * sizeof(float) : 0}};
     for (auto& a : al) {
+        if (a.bytes == 0) continue;
         if ((e = cudaMalloc(a.q, a.bytes)) != cudaSuccess) {
             free3(s);
             delete s;

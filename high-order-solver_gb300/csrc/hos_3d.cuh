@@ -106,8 +106,8 @@ __device__ __forceinline__ bool reduce5(const T* w, T K) {  // Check_Order_Reduc
     const T lam = lambda5(w, K);
     return !(lam > T(0));
 }
-template <class T>
-__device__ __forceinline__ void rotate_in(int dir, T* o, const double* wv) {
+template <class T, class S>
+__device__ __forceinline__ void rotate_in(int dir, T* o, const S* wv) {
     o[0] = (T)wv[0];
     o[4] = (T)wv[4];
     if (dir == 0) { o[1] = (T)wv[1]; o[2] = (T)wv[2]; o[3] = (T)wv[3]; }
@@ -564,8 +564,10 @@ constexpr int POINT3_THREADS = 128;
 // left-hand state of face a+1), WENO5_AO (src/reconstruction.cpp:3803-3925).  The two values
 // fall back to the cell average with zero slope when either has a non-positive lambda.
 // FV planes: q 0..4 left-hand value, 5..9 its normal slope, 10..14 right-hand value, 15..19.
+// W: the state in the compute type -- the FP64 state, or for T = float the FP32 mirror the
+// stage's mirror3 pass writes (converted once per cell instead of once per stencil use)
 template <class T, bool GATED = false>
-__global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const double* __restrict__ W, T* __restrict__ FV,
+__global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const T* __restrict__ W, T* __restrict__ FV,
                                                               Geo3 g, Dir3 d, const Ctl3* ctl, Gate3 gt) {
     if (!ctl->active) return;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -579,7 +581,7 @@ __global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const double* __re
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
         const size_t cc = cell_of(g, d.dir, ac - 2 + m + G, b0 - 2 + G, c0 - 2 + G);
-        double wv[5];
+        T wv[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) wv[v] = W[v * plane + cc];
         rotate_in<T>(d.dir, st[m], wv);

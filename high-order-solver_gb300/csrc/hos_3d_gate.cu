@@ -207,9 +207,9 @@ __global__ void __launch_bounds__(GATE3_THREADS, 3) gate3_kernel(GateRun3 r) {
 
 }  // namespace
 
-cudaError_t launch_gate3(const GateRun3& r, cudaStream_t s) {
+cudaError_t launch_gate3(const GateRun3& r, cudaStream_t s, bool rp_ready) {
     const size_t plane = (size_t)r.g.nx * r.g.ny * r.g.nz;
-    density_pressure3<<<(unsigned)((plane + 255) / 256), 256, 0, s>>>(r);
+    if (!rp_ready) density_pressure3<<<(unsigned)((plane + 255) / 256), 256, 0, s>>>(r);
     gate3_kernel<<<(unsigned)((plane + GATE3_THREADS - 1) / GATE3_THREADS), GATE3_THREADS, 0, s>>>(r);
     return cudaGetLastError();
 }

@@ -42,7 +42,9 @@ struct GateRun3 {
     const Ctl3* ctl;                  // inactive solver: no work (may be null)
 };
 
-cudaError_t launch_gate3(const GateRun3& r, cudaStream_t s);
+// rp_ready: r.rp already holds this stage's (density, pressure) pairs (the FP32 solver's
+// mirror pass writes them); otherwise they are computed first
+cudaError_t launch_gate3(const GateRun3& r, cudaStream_t s, bool rp_ready = false);
 
 }  // namespace d3
 }  // namespace hos

@@ -6,7 +6,7 @@ namespace d3 {
 
 namespace {
 template <bool GATED>
-cudaError_t flux3_f32(const double* W, float* FV, float* LV, double* FS, const Geo3& g, const Dir3& d, const Ctl3* ctl,
+cudaError_t flux3_f32(const float* W, float* FV, float* LV, double* FS, const Geo3& g, const Dir3& d, const Ctl3* ctl,
                       int stage, cudaStream_t s, cudaEvent_t* ev, Gate3 gt) {
     const size_t nc = d.cel.n(), nl = d.lv.n(), np = 2 * d.fs.n();
     face3_kernel<float, GATED><<<(unsigned)((nc + FACE3_THREADS - 1) / FACE3_THREADS), FACE3_THREADS, 0, s>>>(W, FV, g, d, ctl,
@@ -23,7 +23,7 @@ cudaError_t flux3_f32(const double* W, float* FV, float* LV, double* FS, const G
 }  // namespace
 
 template <>
-cudaError_t launch_flux3<float>(const double* W, float* FV, float* LV, double* FS, const Geo3& g, const Dir3& d,
+cudaError_t launch_flux3<float>(const float* W, float* FV, float* LV, double* FS, const Geo3& g, const Dir3& d,
                                 const Ctl3* ctl, int stage, cudaStream_t s, cudaEvent_t* ev, Gate3 gt) {
     return gt.flags ? flux3_f32<true>(W, FV, LV, FS, g, d, ctl, stage, s, ev, gt)
                     : flux3_f32<false>(W, FV, LV, FS, g, d, ctl, stage, s, ev, gt);
