@@ -25,6 +25,9 @@ __global__ void aos_to_soa_kernel(const double* __restrict__ aos, double* __rest
 __global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __restrict__ aos, size_t n);
 __global__ void __launch_bounds__(256) cfl_from_prim_kernel(const double* __restrict__ prim, Geometry geo, StepCtl* ctl);
 __global__ void prim_of_state_kernel(const double* __restrict__ W, double* __restrict__ P, size_t n, double gamma);
+__global__ void mirror_state_kernel(const double* __restrict__ W, const double* __restrict__ AX,
+                                    const double* __restrict__ AY, float* __restrict__ W32, float* __restrict__ A32,
+                                    int nx, int ny);
 void fill_wedge(BcSpec& bc, const hos_params2d& p, double dx);
 
 namespace batch {
@@ -35,14 +38,15 @@ __global__ void bc_batch_kernel(const Prob* __restrict__ probs) {
     const Geometry geo = pr->geo;
     const long long n = 2LL * geo.g * geo.ny + 2LL * geo.g * geo.nodex;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-        bc_fill_one(pr->W, geo, pr->bc, pr->ctl, e);
+        bc_fill_one(pr->W, geo, pr->bc, pr->ctl, e, pr->W32);
 }
 
 __global__ void __launch_bounds__(256) update_batch_kernel(const Prob* __restrict__ probs, int stage) {
     const Prob* pr = probs + blockIdx.y;
     if (!pr->ctl->active) return;
     const Geometry geo = pr->geo;
-    UpdateArgs a{pr->W, pr->Wold, pr->AX, pr->AY, pr->FXx, pr->FXy, pr->FAx, pr->FAy, pr->ctl, stage};
+    float* A32 = pr->W32 ? pr->W32 + 4 * (size_t)geo.nx * mirror_pitch(geo.ny) : nullptr;
+    UpdateArgs a{pr->W, pr->Wold, pr->AX, pr->AY, pr->FXx, pr->FXy, pr->FAx, pr->FAy, pr->ctl, stage, pr->W32, A32};
     const int n = geo.nodex * geo.nodey;
     double cmin = 1e300;
     unsigned int bad = 0;
@@ -86,7 +90,7 @@ __global__ void __launch_bounds__(gate::GATE_THREADS) gate_batch_kernel(const Pr
         const GateTile t = tiles[k];
         const Prob* pr = probs + t.p;
         gate::GateArgs a{pr->W, pr->AX, pr->AY, pr->gflags, stats, threshold, audit_mask, seed,
-                         nullptr, 0, 0xffffffffu, pr->ctl};
+                         nullptr, 0, 0xffffffffu, pr->ctl, pr->W32};
         gate::gate_tile<ORDER>(a, pr->geo, t.i0, t.j0, (unsigned)k, mlp, phase, broken);
     }
     gate::mlp_tc_teardown(mlp, phase, broken);
@@ -110,6 +114,7 @@ struct hos_batch2d {
     std::vector<Prob> host_probs;
     Prob* probs = nullptr;
     double* arena = nullptr;
+    float* arena32 = nullptr;   // FP32 batches: every problem's FP32 mirror
     StepCtl* ctls = nullptr;
     int* last_step = nullptr;
     int* counter = nullptr;
@@ -144,7 +149,7 @@ void freeb(hos_batch2d* b) {
     for (int d = 0; d < 2; ++d)
         for (int k = 0; k < kShapes; ++k)
             if (b->tiles_by_shape[d][k]) cudaFree(b->tiles_by_shape[d][k]);
-    void* ptrs[] = {b->probs, b->arena, b->ctls, b->last_step, b->counter, b->staging,
+    void* ptrs[] = {b->probs, b->arena, b->arena32, b->ctls, b->last_step, b->counter, b->staging,
                     b->gflags, b->gstats, b->gw, b->gb, b->gtiles};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -239,14 +244,16 @@ int hos_batch2d_create(const hos_params2d* params, const double* tstop, int coun
         return failb(HOS_E_CUDA, std::string("device: ") + cudaGetErrorString(e));
     }
     // one arena for every problem's buffers
-    size_t total = 0, maxcells = 0;
-    std::vector<size_t> off(count);
+    size_t total = 0, maxcells = 0, total32 = 0;
+    std::vector<size_t> off(count), off32(count);
     for (int k = 0; k < count; ++k) {
         const hos_params2d& p = params[k];
         const size_t nc = (size_t)(p.nodex + 2 * p.ghost) * (p.nodey + 2 * p.ghost);
         const size_t nfx = (size_t)(p.nodex + 1) * p.nodey, nfy = (size_t)p.nodex * (p.nodey + 1);
         off[k] = total;
         total += 10 * nc + 9 * nfx + 9 * nfy;
+        off32[k] = total32;
+        total32 += (size_t)MIRROR_PLANES * (p.nodex + 2 * p.ghost) * mirror_pitch(p.nodey + 2 * p.ghost);
         maxcells = std::max(maxcells, nc);
         b->cells += (long long)p.nodex * p.nodey;
     }
@@ -257,6 +264,7 @@ int hos_batch2d_create(const hos_params2d* params, const double* tstop, int coun
         if (e == cudaSuccess) e = cudaMemset(*q, 0, bytes);
     };
     alloc((void**)&b->arena, total * sizeof(double));
+    if (precision == HOS_FP32) alloc((void**)&b->arena32, total32 * sizeof(float));
     alloc((void**)&b->staging, 8 * maxcells * sizeof(double));
     alloc((void**)&b->ctls, count * sizeof(StepCtl));
     alloc((void**)&b->last_step, count * sizeof(int));
@@ -307,6 +315,7 @@ int hos_batch2d_create(const hos_params2d* params, const double* tstop, int coun
         pr.FXy = q; q += 4 * nfy;
         pr.FPy = q; q += 4 * nfy;
         pr.FAy = q;
+        pr.W32 = b->arena32 ? b->arena32 + off32[k] : nullptr;
         pr.ctl = b->ctls + k;
         pr.tstop = tstop[k];
         pr.last_step = b->last_step + k;
@@ -379,6 +388,12 @@ int hos_batch2d_set_state(hos_batch2d* b, int k, const double* convar, const dou
     if (e == cudaSuccess) e = cudaMemsetAsync(pr.AX, 0, n * sizeof(double), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(pr.AY, 0, n * sizeof(double), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(pr.last_step, 0xff, sizeof(int), b->stream);
+    if (e == cudaSuccess && pr.W32) {
+        const size_t n32 = (size_t)pr.geo.nx * mirror_pitch(pr.geo.ny);
+        mirror_state_kernel<<<std::min(blocks, 4096u), 256, 0, b->stream>>>(pr.W, pr.AX, pr.AY, pr.W32, pr.W32 + 4 * n32,
+                                                                             pr.geo.nx, pr.geo.ny);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return failb(HOS_E_CUDA, std::string("set_state: ") + cudaGetErrorString(e));
     StepCtl back;

@@ -17,17 +17,21 @@ struct Prob {
     double tstop;
     int* last_step;   // batch step index of this problem's last active step
     unsigned char* gflags;   // learned-gate flags of this problem's cells (gated batches)
+    // FP32 batches: FP32 mirror of W0..W3, alpha_x, alpha_y (pitch mirror_pitch(ny)), written by
+    // the boundary and update kernels and read by the FP32 face and gate tiles (null: FP64)
+    float* W32;
 };
 
 struct TileRef { int p, n0, t0, pad; };
 
-// candidate tile shapes (faces along normal x tangent); 128 faces each
+// candidate tile shapes (faces along normal x tangent): 128 faces, or 256 for 16 x 16 (every
+// thread then has the same number of flux items; WENO5 only)
 using Shape0 = TileShape<8, 16>;
-using Shape1 = TileShape<4, 32>;
+using Shape1 = TileShape<16, 16>;
 using Shape2 = TileShape<16, 8>;
 constexpr int kShapes = 3;
-const int kShapeN[kShapes] = {8, 4, 16};
-const int kShapeT[kShapes] = {16, 32, 8};
+const int kShapeN[kShapes] = {8, 16, 16};
+const int kShapeT[kShapes] = {16, 16, 8};
 
 // FP32 tiles fit two CTAs per SM in 128 registers; FP64 tiles need more registers than that
 template <class T, int ORDER, int DIR, class TS, bool GATED = false>
@@ -39,7 +43,7 @@ __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_bat
         const TileRef tr = tiles[k];
         const Prob* pr = probs + tr.p;
         const Geometry geo = pr->geo;
-        FaceArgs a{};   // members not set below (FP32 mirrors, per-stage buffers) stay null
+        FaceArgs a{};   // members not set below (per-stage buffers) stay null
         a.W = pr->W;
         a.AN = DIR == 0 ? pr->AX : pr->AY;
         a.AT = DIR == 0 ? pr->AY : pr->AX;
@@ -50,6 +54,12 @@ __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_bat
         a.stage = stage;
         a.gate = pr->gflags;
         a.fallback = fallback;
+        if (pr->W32) {
+            const size_t plane32 = (size_t)geo.nx * mirror_pitch(geo.ny);
+            a.W32 = pr->W32;
+            a.AN32 = pr->W32 + (DIR == 0 ? 4 : 5) * plane32;
+            a.AT32 = pr->W32 + (DIR == 0 ? 5 : 4) * plane32;
+        }
         face_tile<T, ORDER, DIR, TS, GATED>(a, geo, tr.n0, tr.t0, smem_raw);
         __syncthreads();  // the next tile reuses the shared memory
     }

@@ -1,4 +1,5 @@
-// hos_batch5.cu -- batched WENO5-AO-DF face kernels (3 tile shapes; FP64, FP32 and gated FP32).
+// hos_batch5.cu -- batched WENO5-AO-DF face kernels (3 tile shapes: 8 x 16, 16 x 16, 16 x 8; FP64, FP32
+// and gated FP32).
 #include "hos_batch.cuh"
 
 namespace hos {

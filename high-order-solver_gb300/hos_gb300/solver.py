@@ -458,7 +458,7 @@ def _checkb(code: int) -> None:
 class Batch2D:
     """Independent 2D problems advanced together (one launch per phase for the batch)."""
 
-    SHAPES = ((8, 16), (4, 32), (16, 8))   # face-tile shapes (normal x tangential)
+    SHAPES = ((8, 16), (16, 16), (16, 8))   # face-tile shapes (normal x tangential); 16 x 16: WENO5 only
 
     def __init__(self, problems, tstops, precision: int = FP64):
         self._lib = load()
