@@ -696,13 +696,13 @@ def main():
     pout = ctypes.cast(host_out.data_ptr(), dp)
     ke = max(3, args.steps)
     lib.hos2d_set_state(sg._h, pin, ppr)
-    sg.step(1e30)
+    sg.advance(1, 1e30, graph=True)
     lib.hos2d_get_state(sg._h, pout, None, None, None)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(ke):
         assert lib.hos2d_set_state(sg._h, pin, ppr) == 0
-        sg.step(1e30)
+        sg.advance(1, 1e30, graph=True)
         assert lib.hos2d_get_state(sg._h, pout, None, None, None) == 0
     te = time.perf_counter() - t0
     e2e_value = ws * cells * ke / te

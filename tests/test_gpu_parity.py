@@ -270,3 +270,35 @@ def test_gpu_time_marching_and_flux_vs_oracle(integrator, flux):
     ref = oracle_run(pb, con, prim, 4)
     assert rel_linf(got["convar"], ref["convar"], pb) <= TOL_FP64
     np.testing.assert_allclose(got["dts"], ref["dts"], rtol=1e-14, atol=0)
+
+
+def test_pinned_host_buffers_match_pageable():
+    """hos2d_set_state / hos2d_get_state on pinned host buffers (the fast host link path the
+    bench's end-to-end figure uses) and on pageable ones give the same state."""
+    import ctypes
+
+    import torch
+
+    pb, con, prim = cases.riemann2d(64, order=7)
+    outs = []
+    for pinned in (False, True):
+        s = Solver2D(pb, FP32)
+        lib, dp = s._lib, ctypes.POINTER(ctypes.c_double)
+        if pinned:
+            hin = torch.from_numpy(np.ascontiguousarray(con.reshape(-1))).pin_memory()
+            hpr = torch.from_numpy(np.ascontiguousarray(prim.reshape(-1))).pin_memory()
+            hout = torch.zeros_like(hin).pin_memory()
+            pin, ppr, pout = (ctypes.cast(t.data_ptr(), dp) for t in (hin, hpr, hout))
+            out = lambda: hout.numpy().reshape(pb.nx, pb.ny, 4).copy()   # noqa: E731
+        else:
+            hin, hpr = np.ascontiguousarray(con.reshape(-1)), np.ascontiguousarray(prim.reshape(-1))
+            hout = np.zeros_like(hin)
+            pin, ppr, pout = (a.ctypes.data_as(dp) for a in (hin, hpr, hout))
+            out = lambda: hout.reshape(pb.nx, pb.ny, 4).copy()   # noqa: E731
+        assert lib.hos2d_set_state(s._h, pin, ppr) == 0
+        s.advance(3, 1e30, graph=True)
+        assert lib.hos2d_get_state(s._h, pout, None, None, None) == 0
+        outs.append(out())
+        s.close()
+    assert np.array_equal(outs[0], outs[1])
+    assert np.abs(outs[1] - con).max() > 0   # the state moved
