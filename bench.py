@@ -86,10 +86,8 @@ def parse():
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from hos_gb300 import replicas
+    return replicas.env()
 
 
 def peaks():
@@ -588,7 +586,7 @@ def main():
     import torch
     import torch.distributed as dist
 
-    from hos_gb300 import cases, gate_train
+    from hos_gb300 import cases, gate_train, replicas
     from hos_gb300.solver import FP32, FP64, Solver2D
 
     ws, rank, local = dist_env()
@@ -641,16 +639,11 @@ def main():
         s.set_state(con, prim)
         if gated:
             s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
-        if ws > 1:
-            dist.barrier()
+        replicas.barrier(ws)
         torch.cuda.synchronize(dev)
         t = timed_steps(s, args.steps, args.warmup)
         torch.cuda.synchronize(dev)
-        if ws > 1:
-            tt = torch.tensor([t], device=dev, dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t = float(tt.item())
-        return s, t
+        return s, replicas.max_over_ranks(t, ws, dev)
 
     # ---- gated FP32 (the headline), plain FP64 and plain FP32 on the same initial data ----
     with ClockSampler(local) as clk:
@@ -726,7 +719,8 @@ def main():
     bytes_gbs = BYTES_PER_FACE * faces / (face_g / 1e3) / 1e9
     smooth = (gstats["smooth_x"] + gstats["smooth_y"]) / max(1, gstats["cells_x"] + gstats["cells_y"])
     line = {
-        "metric": METRIC, "value": ws * cells * args.steps / tg, "unit": "cell-updates/s", "n_gpus": ws,
+        "metric": METRIC, "value": replicas.aggregate_rate(ws, cells * args.steps, tg), "unit": "cell-updates/s",
+        "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tg / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 reconstruction/flux/gate (bf16 MLP on tensor cores); f64 state, stage combination, CFL",
