@@ -109,6 +109,61 @@ __global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __rest
     if (c >= n) return;
     for (int v = 0; v < 4; ++v) aos[4 * c + v] = soa[v * n + c];
 }
+// The host-facing upload in one pass over the cells (hos2d_set_state): the staged AoS conserved
+// state into the SoA planes, the DF indicators zeroed, the FP32 mirror (if any) written, and for
+// interior cells the CFL candidates of the primitives -- the staged AoS primvar if given, else
+// the state's own (Convar_to_primvar_2D) -- with the same arithmetic as cfl_from_prim_kernel.
+__global__ void __launch_bounds__(256) upload_state_kernel(const double* __restrict__ aos,
+                                                           const double* __restrict__ prim_aos, double* __restrict__ W,
+                                                           double* __restrict__ AX, double* __restrict__ AY,
+                                                           float* __restrict__ W32, Geometry geo, StepCtl* ctl) {
+    const size_t n = (size_t)geo.nx * geo.ny;
+    const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    double cand = 1e300;
+    unsigned int bad = 0;
+    if (c < n) {
+        double w[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            w[v] = aos[4 * c + v];
+            W[v * n + c] = w[v];
+        }
+        AX[c] = 0.0;
+        AY[c] = 0.0;
+        const int i = (int)(c / geo.ny), j = (int)(c % geo.ny);
+        if (W32) {
+            const size_t pitch = (size_t)mirror_pitch(geo.ny), plane32 = (size_t)geo.nx * pitch;
+            const size_t cm = (size_t)i * pitch + j;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) W32[v * plane32 + cm] = (float)w[v];
+            W32[4 * plane32 + cm] = 0.0f;
+            W32[5 * plane32 + cm] = 0.0f;
+        }
+        if (i >= geo.g && i < geo.g + geo.nodex && j >= geo.g && j < geo.g + geo.nodey) {
+            double p[4];
+            if (prim_aos) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) p[v] = prim_aos[4 * c + v];
+            } else {
+                to_prim<double>(p, w, geo.gamma);
+            }
+            const double rho = p[0], u = p[1], v = p[2], pr = p[3];
+            const double tmp = sqrt(u * u + v * v) + sqrt(geo.gamma * pr / rho);
+            const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
+            if (qx > 0) cand = qx;
+            if (qy > 0 && qy < cand) cand = qy;
+            if (geo.tau_type == 1 && geo.mu > 0) {   // viscous cap of Dtx
+                const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
+                const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
+                if (cx < cand) cand = cx;
+                if (cy < cand) cand = cy;
+            }
+            if (rho < 0 || pr < 0 || isnan(rho) || isnan(pr)) bad = 1;
+        }
+    }
+    reduce_block(cand, bad, ctl, true);
+}
+
 // primitive variables of a conserved state (Convar_to_primvar_2D, src/basic_function.cpp:811-817)
 __global__ void prim_of_state_kernel(const double* __restrict__ W, double* __restrict__ P, size_t n, double gamma) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -499,21 +554,29 @@ int hos2d_dims(const hos_solver2d* s, int* nx, int* ny) {
 int hos2d_set_state(hos_solver2d* s, const double* convar, const double* primvar) {
     if (!s || !convar) return fail(HOS_E_ARG, "null argument");
     const size_t n = s->ncell;
-    double* stage = s->scratch;          // AoS staging [n][4]
-    double* prim = s->scratch + 4 * n;   // SoA primitive planes
+    double* stage = s->scratch;               // AoS staging [n][4] of convar ...
+    double* stage_prim = s->scratch + 4 * n;  // ... and of primvar
+    // the copies back to back, then one pass (upload_state_kernel) for the transposition, the
+    // DF indicators, the FP32 mirror and the first CFL candidates
     cudaError_t e = cudaMemcpyAsync(stage, convar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "upload convar");
-    const unsigned blocks = (unsigned)((n + 255) / 256);
-    aos_to_soa_kernel<<<blocks, 256, 0, s->stream>>>(stage, s->W, n);
-    if (primvar) {
-        if ((e = cudaMemcpyAsync(stage, primvar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
-            return cuda_fail(e, "upload primvar");
-        aos_to_soa_kernel<<<blocks, 256, 0, s->stream>>>(stage, prim, n);
-    } else {
-        prim_of_state_kernel<<<blocks, 256, 0, s->stream>>>(s->W, prim, n, s->geo.gamma);
-    }
+    if (primvar &&
+        (e = cudaMemcpyAsync(stage_prim, primvar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "upload primvar");
+    StepCtl c{};
+    double seed = s->geo.dx;
+    std::memcpy(&c.cfl_bits, &seed, sizeof seed);
+    c.active = 1;
+    if ((e = cudaMemcpyAsync(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "ctl upload");
+    upload_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(stage, primvar ? stage_prim : nullptr, s->W,
+                                                                             s->AX, s->AY, s->W32, s->geo, s->ctl);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "set_state");
-    return reset_ctl_and_cfl(s, prim);
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "set_state");
+    StepCtl back;
+    if ((e = cudaMemcpy(&back, s->ctl, sizeof back, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "ctl read");
+    if (back.status & 1u) return fail(HOS_E_BLOWUP, "initial state has negative density/pressure or NaN");
+    return HOS_OK;
 }
 
 int hos2d_set_state_device(hos_solver2d* s, const double* d_convar_soa, const double* d_primvar_soa) {
