@@ -399,6 +399,7 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
     if (p.nodex < p.ghost || p.nodey < p.ghost || p.nodez < p.ghost) return fail3(HOS_E_CONFIG, "nodes must be >= ghost");
     if (int st = check_bc3(p.bc)) return st;
     if (p.tau_type != 0 && p.tau_type != 1) return fail3(HOS_E_CONFIG, "tau_type must be 0 (Euler) or 1 (NS)");
+    if (p.prandtl_fix && !(p.prandtl > 0)) return fail3(HOS_E_CONFIG, "the Prandtl fix needs prandtl > 0");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail3(HOS_E_CONFIG, "bad precision");
     hos_solver3d* s = new (std::nothrow) hos_solver3d();
     if (!s) return fail3(HOS_E_NOMEM, "host allocation");
@@ -415,6 +416,7 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
     g.dx = (p.right - p.left) / p.nodex;
     g.dy = (p.up - p.down) / p.nodey;
     g.dz = (p.front - p.back) / p.nodez;
+    g.prandtl_coef = p.prandtl_fix ? 1.0 / p.prandtl - 1.0 : 0.0;
     g.idx = 1.0 / g.dx;
     g.idy = 1.0 / g.dy;
     g.idz = 1.0 / g.dz;

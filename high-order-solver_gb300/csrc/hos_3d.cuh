@@ -38,6 +38,7 @@ struct Geo3 {
     int nx, ny, nz, g, nodex, nodey, nodez;
     double dx, dy, dz, rc, cfl, gamma, K, c1, c2, mu;
     double idx, idy, idz;   // 1 / dx, 1 / dy, 1 / dz (host)
+    double prandtl_coef;    // 1 / Pr - 1 with the Prandtl fix, else 0
     int tau_type, characteristic;
     int bc[6];
 };
@@ -473,6 +474,9 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
     micro3<T>(a0, d0[0], p0, K);
     gaddr<T, false, 2, 0, 0>(m0, a0, s4);
     gaddr<T, false, 1, 0, 0>(m0, a0, der);
+    T a0xuu[5];   // the x-slope part alone, for the Prandtl fix
+#pragma unroll
+    for (int v = 0; v < 5; ++v) a0xuu[v] = s4[v];
     micro3<T>(a0, d0[1], p0, K);
     gaddr<T, false, 1, 1, 0>(m0, a0, tmp);
     gaddr<T, false, 0, 1, 0>(m0, a0, tmp2);
@@ -492,6 +496,18 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
     for (int v = 0; v < 5; ++v) {
         Fa[v] += p0[0] * (ta[3] * g0u[v] + ta[4] * s4[v] + ta[5] * tmp[v]);
         Fb[v] += p0[0] * (tb[3] * g0u[v] + tb[4] * s4[v] + tb[5] * tmp[v]);
+    }
+    if (g.prandtl_coef != 0.0) {
+        // Prandtl-number correction of the heat flux: GKS2D's (src/flux_function.cpp:630-636,
+        // 678-684; the reference's GKS3D has none) with the third velocity component
+        const T prc = T(g.prandtl_coef);
+        const T qs = a0xuu[4] + tmp[4] - p0[1] * (a0xuu[1] + tmp[1]) - p0[2] * (a0xuu[2] + tmp[2]) -
+                     p0[3] * (a0xuu[3] + tmp[3]);
+        Fa[4] += prc * (qs * (-p0[0] * tau * dt));
+        Fb[4] += prc * (qs * (-p0[0] * tau * dt2));
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
         f[v] = T(4) * Fb[v] - Fa[v];
         df[v] = T(4) * (Fa[v] - T(2) * Fb[v]);
     }

@@ -297,17 +297,18 @@ def batch_sweep(count: int = 64, seed: int = 0, side_min: int = 128, side_max: i
 
 
 def tgv3d(n: int = 256, re: float = 1600.0, mach: float = 0.1, gamma: float = 1.4,
-          characteristic: bool = True) -> tuple:
+          characteristic: bool = True, prandtl: float | None = 0.71) -> tuple:
     """Taylor-Green vortex on the periodic box [0, 2 pi]^3 (no counterpart among the reference's
     drivers; its 3D path is CubicTube, src/3Dproblem.cpp:3-172): rho = 1,
     u = sin x cos y cos z, v = -cos x sin y cos z, w = 0,
     p = 1/(gamma Ma^2) + (cos 2x + cos 2y)(cos 2z + 2)/16 at the cell centres, Navier-Stokes
-    collision time with mu = 1/Re (rho_0 = V_0 = L = 1).  The BGK collision gives Prandtl
-    number 1 (the reference's GKS3D has no Prandtl correction).  Returns (problem, convar)."""
+    collision time with mu = 1/Re (rho_0 = V_0 = L = 1), Prandtl number Pr through the heat-flux
+    correction (prandtl None: the BGK collision's Pr = 1).  Returns (problem, convar)."""
     L = 2.0 * math.pi
     pb = Problem3D(nodex=n, nodey=n, nodez=n, ghost=3, characteristic=characteristic, K=2, gamma=gamma,
                    c1_euler=0.0, c2_euler=1.0, cfl=0.5, tau_type=TAU_NS, mu=1.0 / re,
-                   left=0.0, right=L, down=0.0, up=L, back=0.0, front=L, bc=("periodic",) * 6)
+                   left=0.0, right=L, down=0.0, up=L, back=0.0, front=L, bc=("periodic",) * 6,
+                   prandtl_fix=prandtl is not None, prandtl=1.0 if prandtl is None else prandtl)
     h = L / n
     xc = (np.arange(pb.shape[0]) - pb.ghost + 0.5) * h
     X, Y, Z = np.meshgrid(xc, xc, xc, indexing="ij", sparse=True)

@@ -196,7 +196,7 @@ class Params3D(ctypes.Structure):
         ("cfl", ctypes.c_double), ("tau_type", ctypes.c_int), ("mu", ctypes.c_double),
         ("left", ctypes.c_double), ("right", ctypes.c_double), ("down", ctypes.c_double),
         ("up", ctypes.c_double), ("back", ctypes.c_double), ("front", ctypes.c_double),
-        ("bc", ctypes.c_int * 6),
+        ("bc", ctypes.c_int * 6), ("prandtl_fix", ctypes.c_int), ("prandtl", ctypes.c_double),
     ]
 
 
@@ -226,6 +226,8 @@ class Problem3D:
     back: float = 0.0
     front: float = 1.0
     bc: tuple = ("free",) * 6
+    prandtl_fix: bool = False   # Prandtl-number correction of the heat flux ...
+    prandtl: float = 1.0        # ... with this Pr
 
     @property
     def shape(self) -> tuple:
@@ -256,4 +258,5 @@ class Problem3D:
         for s in range(6):
             b = self.bc[s]
             p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
+        p.prandtl_fix, p.prandtl = 1 if self.prandtl_fix else 0, float(self.prandtl)
         return p

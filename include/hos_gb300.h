@@ -303,6 +303,8 @@ typedef struct hos_params3d {
     double left, right, down, up, back, front;
     int bc[6];                        /* left, right, down, up, back, front: HOS_BC_FREE,
                                          HOS_BC_PERIODIC or HOS_BC_REFLECT                */
+    int prandtl_fix;                  /* 1: Prandtl-number correction of the heat flux    */
+    double prandtl;                   /* Pr (prandtl_fix = 1)                             */
 } hos_params3d;
 
 typedef struct hos_solver3d hos_solver3d;

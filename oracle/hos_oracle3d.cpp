@@ -467,6 +467,11 @@ void gks3(const Side& L, const Side& R, double dt, double* f, double* df) {
     for (int v = 0; v < 5; ++v) derA0[v] = -p0[0] * (a0xu[v] + a0yv[v] + a0zw[v]);
     micro3(A0, derA0, p0);
     gaddr(m0, 0, 1, 0, 0, 0, A0, A0u);
+    // Prandtl-number correction of the heat flux: GKS2D's (src/flux_function.cpp:630-636,
+    // 678-684; the reference's GKS3D has none) with the third velocity component
+    const double prc = P.prandtl_fix ? 1.0 / P.prandtl - 1.0 : 0.0;
+    double qs = a0xuu[4] + A0u[4] - p0[1] * (a0xuu[1] + A0u[1]) - p0[2] * (a0xuu[2] + A0u[2]) -
+                p0[3] * (a0xuu[3] + A0u[3]);
     double F0[5], F1[5];
     for (int v = 0; v < 5; ++v) {
         F0[v] = dl * t[0] * glu[v] + dr * t[0] * gru[v];
@@ -476,6 +481,7 @@ void gks3(const Side& L, const Side& R, double dt, double* f, double* df) {
         F0[v] = F0[v] + p0[0] * t[4] * (a0xuu[v] + a0yuv[v] + a0zuw[v]);
         F0[v] = F0[v] + p0[0] * t[5] * (A0u[v]);
     }
+    if (P.prandtl_fix) F0[4] += prc * (qs * (-p0[0] * tau * dt));
     const double dt2 = 0.5 * dt;
     time_coeffs(t, tau, tau_num(dl, dr, p0[0], pl[4], prr[4], p0[4], HALF_TAU_OF_DT ? dt : dt2), dt2);
     for (int v = 0; v < 5; ++v) {
@@ -486,6 +492,7 @@ void gks3(const Side& L, const Side& R, double dt, double* f, double* df) {
         F1[v] = F1[v] + p0[0] * t[4] * (a0xuu[v] + a0yuv[v] + a0zuw[v]);
         F1[v] = F1[v] + p0[0] * t[5] * (A0u[v]);
     }
+    if (P.prandtl_fix) F1[4] += prc * (qs * (-p0[0] * tau * 0.5 * dt));
     for (int v = 0; v < 5; ++v) {
         f[v] = (4.0 * F1[v] - F0[v]);
         df[v] = 4.0 * (F0[v] - 2.0 * F1[v]);

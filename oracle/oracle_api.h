@@ -130,6 +130,8 @@ typedef struct hos3d_params {
     double mu;
     double left, right, down, up, back, front;
     int bc[6];                        /* left, right, down, up, back, front: FREE / PERIODIC / REFLECT */
+    int prandtl_fix;                  /* 1: Prandtl-number correction of the heat flux      */
+    double prandtl;                   /* Pr */
 } hos3d_params;
 
 int    oracle3d_init(const hos3d_params* p);

@@ -76,8 +76,8 @@ def _compare(pb, W, steps, precision=FP64):
     return _interior(got), _interior(ref), np.array(dts)
 
 
-@pytest.mark.parametrize("case", ["periodic", "periodic_conservative", "periodic_ns", "cubic_sod_free",
-                                  "cubic_sod_reflect"])
+@pytest.mark.parametrize("case", ["periodic", "periodic_conservative", "periodic_ns", "periodic_ns_prandtl",
+                                  "cubic_sod_free", "cubic_sod_reflect"])
 def test_gpu3d_fp64_matches_oracle(case):
     if case == "periodic":
         pb, W = smooth_periodic()
@@ -85,6 +85,8 @@ def test_gpu3d_fp64_matches_oracle(case):
         pb, W = smooth_periodic(seed=1, characteristic=False)
     elif case == "periodic_ns":
         pb, W = smooth_periodic(seed=2, tau_type=TAU_NS, mu=0.01, c2_euler=1.0)
+    elif case == "periodic_ns_prandtl":
+        pb, W = smooth_periodic(seed=4, tau_type=TAU_NS, mu=0.01, c2_euler=1.0, prandtl_fix=True, prandtl=0.71)
     elif case == "cubic_sod_free":
         pb, W = cubic_sod()
     else:

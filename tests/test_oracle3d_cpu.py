@@ -12,6 +12,8 @@ the 3D restatement is pinned as follows:
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -165,3 +167,28 @@ def test_3d_mirror_symmetry_in_each_axis():
         m = np.flip(out, axis=ax).copy()
         m[..., 1 + ax] = -m[..., 1 + ax]
         assert np.abs(m - out).max() / np.abs(out).max() < 1e-12, ax
+
+
+def test_3d_prandtl_fix_corrects_the_energy_flux_only():
+    """The Prandtl-number correction adds (1/Pr - 1) q to the energy flux (q: the heat flux of
+    the equilibrium part's slopes, GKS2D's form with the third velocity component): mass and
+    momentum fluxes of a stage are unchanged, the energy flux moves, and Pr = 1 changes
+    nothing."""
+    from hos_gb300.params import TAU_NS
+    fl = {}
+    for name, fix, pr in (("off", False, 1.0), ("pr1", True, 1.0), ("pr071", True, 0.71)):
+        pb, W = _random_periodic(8, 5)
+        pb.tau_type, pb.mu, pb.c2_euler = TAU_NS, 0.01, 1.0
+        pb.prandtl_fix, pb.prandtl = fix, pr
+        o = CpuStep3D().init(pb)
+        o.set_state(W)
+        dt = o.lib.oracle3d_begin_step(ctypes.c_double(1e30), ctypes.c_double(0.0))
+        assert o.fn("stage")(0, ctypes.c_double(dt)) == 0
+        nf = (pb.nodex + 1) * pb.nodey * pb.nodez
+        out = np.zeros(nf * 2 * 10)
+        o.fn("get_flux")(0, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        fl[name] = out.reshape(nf, 2, 10)[:, 0, :]
+    assert np.array_equal(fl["off"], fl["pr1"])
+    a, b = fl["off"], fl["pr071"]
+    assert np.array_equal(a[:, [0, 1, 2, 3, 5, 6, 7, 8]], b[:, [0, 1, 2, 3, 5, 6, 7, 8]])
+    assert np.abs(a[:, 4] - b[:, 4]).max() > 1e-10 * np.abs(a[:, 4]).max()
