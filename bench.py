@@ -348,7 +348,7 @@ def tgv3d_leg(torch, dev, flush, steps, warmup, fp32_peak, fp64_peak, n=N_3D, n5
 
     pb, con = cases.tgv3d(n)
     cells = n ** 3
-    out = {"workload": f"tgv3d_{n}^3_re1600_ma0.1_weno5ao_char_4gp_gks3d_ns_s2o4", "cells": cells}
+    out = {"workload": f"tgv3d_{n}^3_re1600_ma0.1_pr0.71_weno5ao_char_4gp_gks3d_ns_s2o4", "cells": cells}
 
     def timed(prec, k, w, gated=False):
         s = Solver3D(pb, prec)
