@@ -173,8 +173,15 @@ __global__ void adam_kernel(float* params, float* m, float* v, float* grad, int 
 }
 
 
-cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s) {
+cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s,
+                        const CUtensorMap* tm) {
     const dim3 blocks((geo.ny + GATE_TILE - 1) / GATE_TILE, (geo.nx + GATE_TILE - 1) / GATE_TILE);
+    if (tm) {
+        if (order == 5) gate_kernel_tma<5><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo, *tm);
+        else if (order == 7) gate_kernel_tma<7><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo, *tm);
+        else gate_kernel_tma<9><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo, *tm);
+        return cudaGetLastError();
+    }
     if (order == 5) gate_kernel<5><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
     else if (order == 7) gate_kernel<7><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
     else gate_kernel<9><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);

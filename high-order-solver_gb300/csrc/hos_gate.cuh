@@ -400,17 +400,71 @@ constexpr int GATE_TILE = 16;   // 16 x 16 cells per block, one thread per cell
 // cores for the tile's 256 cells per direction (mlp: set up by the kernel, see mlp_tc_rows).
 // One 16 x 16 tile with first cell (i0, j0); tile_id numbers the tile for the audit draw.
 static_assert(GATE_TILE * GATE_TILE == TC_THREADS && GATE_THREADS == TC_THREADS, "two network rows per thread");
+
+// TMA box of a gate tile in the FP32 mirror (x along j, y along i, the six planes): the tile
+// and its stencil halo, the x origin rounded down to 16 bytes.  It is staged in the network's
+// operand region, which is free until the features are written.
 template <int ORDER>
+struct GateBox {
+    static constexpr int H = GATE_TILE + 2 * (ORDER / 2);
+    static constexpr int X = (H + 3 + 3) / 4 * 4, Y = H, Z = MIRROR_PLANES;
+    static constexpr unsigned bytes = 4u * X * Y * Z;
+    static_assert(bytes <= sizeof(MlpTc::act), "the staged box must fit the operand region");
+};
+
+// tmap (TMA): the mirror's tensor map with the GateBox<ORDER> box; the tile is then staged by
+// one TMA tile load instead of per-cell loads of the mirror
+template <int ORDER, bool TMA = false>
 __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo, int i0, int j0, unsigned tile_id,
-                                          MlpTc& mlp, unsigned& phase, bool& broken) {
+                                          MlpTc& mlp, unsigned& phase, bool& broken,
+                                          const CUtensorMap* tmap = nullptr) {
     constexpr int r = ORDER / 2, H = GATE_TILE + 2 * r;
     __shared__ float srho[H][H + 1], sp[H][H + 1];
+    __shared__ float salpha[2][GATE_TILE * GATE_TILE];   // TMA: the tile cells' alpha_x, alpha_y
     __shared__ unsigned counts[4];           // cells x, cells y, smooth x, smooth y of the block
     if (a.ctl && !a.ctl->active) return;   // uniform over the block
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid < 4) counts[tid] = 0;
     const size_t plane = (size_t)geo.nx * geo.ny;
     const float gamma = float(geo.gamma);
+    if constexpr (TMA) {
+        using B = GateBox<ORDER>;
+        constexpr int PZ = B::X * B::Y;
+        __shared__ __align__(8) uint64_t gbar;
+        float* stg = reinterpret_cast<float*>(mlp.act);
+        const int x0 = j0 - r, y0 = i0 - r, xa = x0 & ~3, off = x0 - xa;   // negative origins read zeros
+        if (tid == 0) {
+            mbar_init(&gbar, 1);
+            mbar_expect_tx(&gbar, B::bytes);
+            tma_load_3d(stg, tmap, xa, y0, 0, &gbar);
+        }
+        __syncthreads();
+        if (!__syncthreads_and(mbar_wait(&gbar, 0))) {
+            // the load did not complete: let a late one land, and flag no cell of the kernel
+            // smooth (the network is skipped; the caller records the timeout)
+            mbar_wait(&gbar, 0);
+            broken = true;
+        }
+        for (int e = tid; e < H * H; e += GATE_THREADS) {
+            const int hi = e / H, hj = e % H;
+            const int gi = i0 - r + hi, gj = j0 - r + hj;
+            float rho = 0.0f, pr = 0.0f;
+            if (gi >= 0 && gi < geo.nx && gj >= 0 && gj < geo.ny) {
+                const float* q = stg + hi * B::X + off + hj;
+                float w[4] = {q[0], q[PZ], q[2 * PZ], q[3 * PZ]}, pv[4];
+                to_prim(pv, w, gamma);
+                rho = pv[0];
+                pr = pv[3];
+            }
+            srho[hi][hj] = rho;
+            sp[hi][hj] = pr;
+            if (hi >= r && hi < r + GATE_TILE && hj >= r && hj < r + GATE_TILE) {
+                const int t = (hi - r) * GATE_TILE + (hj - r);
+                salpha[0][t] = stg[4 * PZ + hi * B::X + off + hj];
+                salpha[1][t] = stg[5 * PZ + hi * B::X + off + hj];
+            }
+        }
+    } else
     for (int e = tid; e < H * H; e += GATE_THREADS) {
         const int hi = e / H, hj = e % H;               // j fastest: coalesced rows
         const int gi = i0 - r + hi, gj = j0 - r + hj;
@@ -454,7 +508,9 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo
             }
             indicator_features<ORDER>(rs, f);
             indicator_features<ORDER>(ps, f + 7);
-            const float al = float(dir == 0 ? a.AX[c] : a.AY[c]);
+            float al;
+            if constexpr (TMA) al = salpha[dir][tid];   // the mirror's FP32 copy of alpha
+            else al = float(dir == 0 ? a.AX[c] : a.AY[c]);
             f[14] = al / (1.0f + al);
             f[15] = 0.0f;
         } else {
@@ -543,13 +599,30 @@ __global__ void __launch_bounds__(GATE_THREADS, ORDER == 9 ? 2 : 3) gate_kernel(
     mlp_tc_teardown(mlp, phase, broken);
 }
 
+// the FP32 solvers' gate: the tile staged from the FP32 mirror by one TMA tile load
+template <int ORDER>
+__global__ void __launch_bounds__(GATE_THREADS, ORDER == 9 ? 2 : 3)
+    gate_kernel_tma(GateArgs a, Net net, Geometry geo, const __grid_constant__ CUtensorMap tmap) {
+    __shared__ MlpTc mlp;
+    if (a.ctl && !a.ctl->active) return;   // uniform: nothing allocated yet
+    mlp_tc_setup(mlp, net);
+    unsigned phase = 0;
+    bool broken = false;
+    gate_tile<ORDER, true>(a, geo, blockIdx.y * GATE_TILE, blockIdx.x * GATE_TILE, blockIdx.y * gridDim.x + blockIdx.x,
+                           mlp, phase, broken, &tmap);
+    mlp_tc_teardown(mlp, phase, broken);
+}
+
 }  // namespace gate
 }  // namespace hos
 
 // ---------------- host side (hos_gate.cu) ----------------
 namespace hos {
 namespace gate {
-cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s);
+// tm (may be null): the FP32 mirror's tensor map with the GateBox<order> box; with it the
+// tiles are staged by TMA
+cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s,
+                        const CUtensorMap* tm = nullptr);
 }  // namespace gate
 }  // namespace hos
 

@@ -202,7 +202,8 @@ static int cuda_fail(cudaError_t e, const char* where) {
 }
 
 // Tensor maps of the FP32 mirror (base: nx rows of ny cells at pitch mirror_pitch(ny), six
-// planes) with the x-face and the y-face tile boxes of the given WENO order's TMA face tile.  The encoder is
+// planes) with the x-face and the y-face tile boxes of the given WENO order's TMA face tile and
+// the gate tile's box.  The encoder is
 // the driver's cuTensorMapEncodeTiled, fetched through the runtime so that the library does not
 // link libcuda.  Cells past ny in a row read as zero (the out-of-bounds fill).
 static int encode_mirror_maps(CUtensorMap* maps, float* base, int nx, int ny, int order) {
@@ -215,20 +216,23 @@ static int encode_mirror_maps(CUtensorMap* maps, float* base, int nx, int ny, in
             return fail(HOS_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    int bx[2], by[2];
+    int bx[3], by[3];
     switch (order) {
         case 5: bx[0] = TmaBox<5, 0, TmaTile<5>>::X; by[0] = TmaBox<5, 0, TmaTile<5>>::Y;
-                 bx[1] = TmaBox<5, 1, TmaTile<5>>::X; by[1] = TmaBox<5, 1, TmaTile<5>>::Y; break;
+                 bx[1] = TmaBox<5, 1, TmaTile<5>>::X; by[1] = TmaBox<5, 1, TmaTile<5>>::Y;
+                 bx[2] = gate::GateBox<5>::X; by[2] = gate::GateBox<5>::Y; break;
         case 7: bx[0] = TmaBox<7, 0, TmaTile<7>>::X; by[0] = TmaBox<7, 0, TmaTile<7>>::Y;
-                 bx[1] = TmaBox<7, 1, TmaTile<7>>::X; by[1] = TmaBox<7, 1, TmaTile<7>>::Y; break;
+                 bx[1] = TmaBox<7, 1, TmaTile<7>>::X; by[1] = TmaBox<7, 1, TmaTile<7>>::Y;
+                 bx[2] = gate::GateBox<7>::X; by[2] = gate::GateBox<7>::Y; break;
         default: bx[0] = TmaBox<9, 0, TmaTile<9>>::X; by[0] = TmaBox<9, 0, TmaTile<9>>::Y;
-                 bx[1] = TmaBox<9, 1, TmaTile<9>>::X; by[1] = TmaBox<9, 1, TmaTile<9>>::Y; break;
+                 bx[1] = TmaBox<9, 1, TmaTile<9>>::X; by[1] = TmaBox<9, 1, TmaTile<9>>::Y;
+                 bx[2] = gate::GateBox<9>::X; by[2] = gate::GateBox<9>::Y; break;
     }
     const cuuint64_t pitch = (cuuint64_t)mirror_pitch(ny);
     const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)MIRROR_PLANES};
     const cuuint64_t strides[2] = {pitch * sizeof(float), pitch * (cuuint64_t)nx * sizeof(float)};
     const cuuint32_t es[3] = {1, 1, 1};
-    for (int d = 0; d < 2; ++d) {
+    for (int d = 0; d < 3; ++d) {
         const cuuint32_t box[3] = {(cuuint32_t)bx[d], (cuuint32_t)by[d], (cuuint32_t)MIRROR_PLANES};
         CUresult r = encode(&maps[d], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -265,7 +269,8 @@ struct hos_solver2d {
     double* scratch = nullptr;  // 8 * ncell doubles: AoS staging + primitive planes
     float* W32 = nullptr;       // FP32 solvers: mirror of W [4][nx*P] ...
     float* A32 = nullptr;       // ... and of alpha_x | alpha_y [2][nx*P] (inside the W32 allocation)
-    CUtensorMap tmap[2];        // FP32 solvers: the mirror's tensor maps with the x- / y-face boxes
+    CUtensorMap tmap[3];        // FP32 solvers: the mirror's tensor maps with the x- / y-face boxes
+                                // and the gate tile's box
     double* stagex = nullptr;   // methods other than S2O4: per-stage F and D of x faces [2][4][4][nfx]
     double* stagey = nullptr;   // ... and of y faces
     StepCtl* ctl = nullptr;
@@ -361,7 +366,9 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
         // per-cell smoothness flags of this stage's state (ghosts filled) for both directions
         gate::GateArgs ga{s->W, s->AX, s->AY, s->gflags, s->gstats, s->gthreshold, s->gaudit_mask, s->gseed++,
                           nullptr, 0, 0xffffffffu, s->ctl, s->W32};
-        if ((e = gate::launch_gate(s->p.order, ga, s->gnet(), geo, s->stream)) != cudaSuccess) return cuda_fail(e, "gate");
+        if ((e = gate::launch_gate(s->p.order, ga, s->gnet(), geo, s->stream, s->W32 ? &s->tmap[2] : nullptr)) !=
+            cudaSuccess)
+            return cuda_fail(e, "gate");
         ax.gate = ay.gate = s->gflags;
         ax.fallback = ay.fallback = &s->gstats->fallback;
     }
