@@ -174,6 +174,16 @@ __global__ void prim_of_state_kernel(const double* __restrict__ W, double* __res
     for (int v = 0; v < 4; ++v) P[v * n + c] = p[v];
 }
 
+// one block waits on an mbarrier that expects one arrival and receives none: the bounded wait
+// must give up and report (hos_wait_limit_selftest)
+__global__ void wait_limit_selftest_kernel(unsigned* out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const bool done = mbar_wait(&bar, 0);
+    if (threadIdx.x == 0) *out = done ? 1u : 2u;
+}
+
 static thread_local std::string g_last_error;
 
 // conserved wedge states and geometry (Primvar_to_convar_2D on the primitive states)
@@ -440,6 +450,23 @@ int reset_ctl_and_cfl(hos_solver2d* s, const double* dprim_soa) {
 extern "C" {
 
 const char* hos_last_error(void) { return g_last_error.c_str(); }
+
+int hos_wait_limit_selftest(void) {
+    unsigned* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned));
+    if (e != cudaSuccess) return cuda_fail(e, "selftest alloc");
+    unsigned h = 0;
+    if ((e = cudaMemset(d, 0, sizeof(unsigned))) == cudaSuccess) {
+        wait_limit_selftest_kernel<<<1, 32>>>(d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "selftest");
+    if (h == 2u) return fail(HOS_E_TIMEOUT, "the wait gave up at its limit (expected)");
+    return h == 1u ? fail(HOS_OK, "the wait completed: the barrier was not expected to") : fail(HOS_E_CUDA, "no result");
+}
 
 int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) {
     if (!params || !out) return fail(HOS_E_ARG, "null argument");

@@ -182,6 +182,13 @@ void* hos2d_stream(hos_solver2d* s);
 /* Human-readable text of the last error on this thread. */
 const char* hos_last_error(void);
 
+/* Self-test of the device-side wait limit (no counterpart in the reference): one block waits
+ * on an mbarrier that nothing completes, with the bounded wait the TMA tile loads and the
+ * gate's tensor-core MMAs use.  Returns HOS_E_TIMEOUT when the wait gave up as designed (after
+ * about a second) and the context is still usable, HOS_OK if the wait had completed (a fault
+ * in the limit), HOS_E_CUDA on a launch error. */
+int hos_wait_limit_selftest(void);
+
 /* ---- learned gate (FP32-bulk path; no counterpart in the reference) ---------------------
  * A 16 -> 32 -> 32 -> 1 MLP (BF16 weights, FP32 accumulation on the tensor cores) predicts,
  * per cell and direction, from the normalised WENO-AO smoothness indicators of density and
