@@ -12,7 +12,7 @@ struct FaceLaunch {
     // Navier-Stokes collision time
     template <class T, int DIR, bool GATED, bool NS = false>
     static cudaError_t one(const FaceArgs& a, const Geometry& geo, cudaStream_t s, const CUtensorMap* tm) {
-        using S = FaceSmem<T, ORDER>;
+        using S = FaceSmem<T, ORDER, KernelTile<ORDER>>;
         const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;
         const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;
         if constexpr (sizeof(T) == 4) {
@@ -25,7 +25,8 @@ struct FaceLaunch {
                 return cudaGetLastError();
             }
         }
-        dim3 grid((nodeT + TILE_T - 1) / TILE_T, (nodeN + 1 + TILE_N - 1) / TILE_N);
+        using KT = KernelTile<ORDER>;
+        dim3 grid((nodeT + KT::T - 1) / KT::T, (nodeN + 1 + KT::N - 1) / KT::N);
         const size_t smem = GATED ? S::gated_bytes : S::bytes;
         face_kernel<T, ORDER, DIR, GATED, NS><<<grid, FACE_THREADS, smem, s>>>(a, geo);
         return cudaGetLastError();
@@ -42,7 +43,7 @@ struct FaceLaunch {
     }
     template <class T, int DIR, bool GATED, bool NS = false>
     static cudaError_t configure_one() {
-        using S = FaceSmem<T, ORDER>;
+        using S = FaceSmem<T, ORDER, KernelTile<ORDER>>;
         const size_t smem = GATED ? S::gated_bytes : S::bytes;
         cudaError_t e = attrs(face_kernel<T, ORDER, DIR, GATED, NS>, smem);
         if constexpr (sizeof(T) == 4) {

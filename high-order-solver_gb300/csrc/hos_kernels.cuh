@@ -774,17 +774,21 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     }
 }
 
+// Tile of the single-problem face kernels: 16 x 16 faces for WENO5/7 (256 faces: every thread
+// has the same number of (face, Gauss point) flux items; at WENO7 103 KB of shared memory in
+// FP32, two CTAs per SM, and 206 KB in FP64, one), 8 x 16 for WENO9 (its four Gauss points would
+// need 137 KB in FP32 at 16 x 16).
+template <int ORDER>
+using KernelTile = typename std::conditional<ORDER == 9, TileShape<8, 16>, TileShape<16, 16>>::type;
+template <int ORDER>
+using TmaTile = KernelTile<ORDER>;
+
 template <class T, int ORDER, int DIR, bool GATED = false, bool NS = false>
 __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_kernel(FaceArgs a, Geometry geo) {
+    using TS = KernelTile<ORDER>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    face_tile<T, ORDER, DIR, DefaultTile, GATED, NS>(a, geo, blockIdx.y * TILE_N, blockIdx.x * TILE_T, smem_raw);
+    face_tile<T, ORDER, DIR, TS, GATED, NS>(a, geo, blockIdx.y * TS::N, blockIdx.x * TS::T, smem_raw);
 }
-
-// Tile of the FP32 TMA face kernels: 16 x 16 faces for WENO5/7 (256 faces: every thread has
-// the same number of (face, Gauss point) flux items, 103 KB of shared memory at WENO7, two
-// CTAs per SM), 8 x 16 for WENO9 (its four Gauss points would need 137 KB at 16 x 16).
-template <int ORDER>
-using TmaTile = typename std::conditional<ORDER == 9, TileShape<8, 16>, TileShape<16, 16>>::type;
 
 // FP32 face kernel of the solvers with the pitched FP32 mirror: the tile is staged by one TMA
 // tile load (tmap: the mirror's tensor map, box TmaBox<ORDER, DIR, TmaTile<ORDER>>)
