@@ -127,7 +127,7 @@ void recon_cell(int i, bool df_variant, Pt& L, Pt& R) {
             double s[9];
             for (int k = 0; k < n; ++k) s[k] = ch[sd][k][v];
             if (df_variant) weno_normal(order, sd, s, df, h, var[v], der[v]);
-            else weno5_plain(sd, s, h, var[v], der[v]);
+            else weno5_plain(sd, s, h, var[v], der[v], P.wenotype);
         }
         Pt& Q = sd == 0 ? L : R;
         if (P.characteristic) {

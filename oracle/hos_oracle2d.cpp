@@ -12,6 +12,9 @@
 //   Convar_to_Primvar ...... src/basic_function.cpp:752-773 (blow-up -> status 1, no exit)
 //   normal recon (DF) ...... src/reconstruction.cpp:1701-1859 (WENO5), 1861-2028 (WENO7),
 //                            2030-2211 (WENO9); scalar kernels :480-657, :750-974, :1072-1364
+//   normal recon (non-DF) .. src/reconstruction.cpp:1562-1699 (WENO5_AO_normal, WENO5_AO),
+//                            scalar kernels :161-360 with the wenotype choice
+//   tangential (non-DF) .... src/reconstruction.cpp:2233-2551 (WENO5_AO_tangent, 2 pts)
 //   tangential recon (DF) .. src/reconstruction.cpp:2553-2838 (WENO5, 2 pts),
 //                            2840-3174 (WENO7, 3 pts), 3176-3609 (WENO9, 4 pts + Polynomial_9th)
 //   positivity fallback .... src/reconstruction.cpp:1439-1449
@@ -177,6 +180,10 @@ inline bool needs_order_reduction(const double* w) {
 
 // scalar tangential reconstruction at all Gauss points of one face side
 void weno_tangent(int order, const double* s, const double* df, double h, double* g, double* gx) {
+    if (!C.p.use_df) {   // non-DF WENO5-AO at the 2 Gauss points (WENO5_AO_tangential, :2244-2391)
+        weno5_2gauss(s, h, true, g, gx, C.p.wenotype);
+        return;
+    }
     double fw[6], p[6], px[6];
     int n = ao_weights(order, s, fw);
     for (int ig = 0; ig < C.gp; ++ig) {
@@ -226,7 +233,8 @@ void normal_cell(int order, const double (*st)[4], const double* al, double h, P
         }
         for (int v = 0; v < 4; ++v) {
             for (int k = 0; k < n; ++k) s[k] = ch[k][v];
-            weno_normal(order, side, s, df, h, var[v], der[v]);
+            if (C.p.use_df) weno_normal(order, side, s, df, h, var[v], der[v]);
+            else weno5_plain(side, s, h, var[v], der[v], C.p.wenotype);   // WENO5_AO, :1589-1699
         }
         Point& P = side == 0 ? Lp : Rp;
         if (C.p.characteristic) {
@@ -420,18 +428,11 @@ double tau_ns(double d0, double l0) {
 }
 
 // ----------------------------------------------------------------------------------------
-// GKS2D at one Gauss point (src/flux_function.cpp:345-698, gks2nd, Euler tau, S2O4 branch):
-// centre state by collision (also stored in re.center), the full second-order flux over
-// [0, dt] and [0, dt/2], combined into f = 4F(dt/2) - F(dt), derf = 4(F(dt) - 2F(dt/2)).
+// Centre (g0) state of a Gauss point by collision, with its x and y slopes from the left and
+// right micro-slopes (Center_all_collision_2d_multi, src/reconstruction.cpp:3652-3687; GKS2D
+// recomputes the same state, src/flux_function.cpp:369-401).  ml, mr: the sides' moments.
 // ----------------------------------------------------------------------------------------
-void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
-    double pl[4], pr[4], p0[4];
-    to_ulambda(pl, re.left.convar);
-    to_ulambda(pr, re.right.convar);
-    Moments ml, mr;
-    moments(ml, pl[1], pl[2], pl[3]);
-    moments(mr, pr[1], pr[2], pr[3]);
-    // collision (Collision, :561-569)
+void centre_state(Recon& re, const double* pl, const double* pr, const Moments& ml, const Moments& mr) {
     double* w0 = re.center.convar;
     w0[0] = pl[0] * ml.uplus[0] + pr[0] * mr.uminus[0];
     w0[1] = pl[0] * ml.uplus[1] + pr[0] * mr.uminus[1];
@@ -453,6 +454,21 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
             re.center.der1y[v] = pl[0] * al0y[v] + pr[0] * ar0y[v];
         }
     }
+}
+
+// ----------------------------------------------------------------------------------------
+// GKS2D at one Gauss point (src/flux_function.cpp:345-698, gks2nd, Euler tau, S2O4 branch):
+// centre state by collision (also stored in re.center), the full second-order flux over
+// [0, dt] and [0, dt/2], combined into f = 4F(dt/2) - F(dt), derf = 4(F(dt) - 2F(dt/2)).
+// ----------------------------------------------------------------------------------------
+void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
+    double pl[4], pr[4], p0[4];
+    to_ulambda(pl, re.left.convar);
+    to_ulambda(pr, re.right.convar);
+    Moments ml, mr;
+    moments(ml, pl[1], pl[2], pl[3]);
+    moments(mr, pr[1], pr[2], pr[3]);
+    centre_state(re, pl, pr, ml, mr);
     to_ulambda(p0, re.center.convar);
     const double tau = tau_ns(p0[0], p0[3]);
     double tn = tau_num(pl[0], pr[0], pl[3], pr[3], dt, p0[0], p0[3]);
@@ -555,8 +571,33 @@ void gks2d(Recon& re, double dt, double* fo, double* dfo, bool one_level) {
     }
 }
 
-// Lax-Friedrichs flux times dt at a Gauss point (LF2D, src/flux_function.cpp:700-735)
-void lf2d(const Recon& re, double dt, double* fo, double* dfo) {
+// LF2D's viscous term (NS_by_central_difference_prim_2D, src/flux_function.cpp:737-754), as
+// written: it reads the centre state's entries as (rho, u, v, T) and their slopes, while the
+// centre state holds conserved variables (rho, rho u, rho v, rho E) and their slopes; mu = Mu,
+// or Nu rho when Nu > 0; the heat-flux factor (K + 4) / (2 Pr).
+void ns_central(const Recon& re, double dt, double* fo) {
+    double mu = C.p.mu;
+    if (C.p.nu > 0) mu = C.p.nu * re.center.convar[0];
+    const double u = re.center.convar[1];
+    const double v = re.center.convar[2];
+    const double ux = re.center.der1x[1];
+    const double vx = re.center.der1x[2];
+    const double uy = re.center.der1y[1];
+    const double vy = re.center.der1y[2];
+    const double tau_xx = 2 * mu * ux - 2.0 / 3.0 * mu * (ux + vy);
+    const double tau_xy = mu * (uy + vx);
+    const double q = u * tau_xx + v * tau_xy + (C.K + 4) / (2 * C.p.prandtl) * mu * re.center.der1x[3];
+    fo[1] += tau_xx * dt;
+    fo[2] += tau_xy * dt;
+    fo[3] += q * dt;
+}
+
+// Lax-Friedrichs flux times dt at a Gauss point (LF2D, src/flux_function.cpp:700-735); with
+// the Navier-Stokes collision time its viscous term is added.  That term reads the centre
+// state, which the reference computes only for GKS2D (Center_all_collision_multi returns for
+// other fluxes, src/reconstruction.cpp:3642-3650, and leaves the Gauss points' centre states
+// as allocated, uninitialised); here it is the collision state GKS2D would use.
+void lf2d(Recon& re, double dt, double* fo, double* dfo) {
     double pl[4], pr[4];
     to_prim(pl, re.left.convar);
     to_prim(pr, re.right.convar);
@@ -577,6 +618,16 @@ void lf2d(const Recon& re, double dt, double* fo, double* dfo) {
         fo[m] = 0.5 * ((fl[m] + fr[m]) - beta * (re.right.convar[m] - re.left.convar[m]));
         fo[m] *= dt;
         dfo[m] = 0.0;
+    }
+    if (C.p.tau_type == 1) {
+        double ql[4], qr[4];
+        to_ulambda(ql, re.left.convar);
+        to_ulambda(qr, re.right.convar);
+        Moments ml, mr;
+        moments(ml, ql[1], ql[2], ql[3]);
+        moments(mr, qr[1], qr[2], qr[3]);
+        centre_state(re, ql, qr, ml, mr);
+        ns_central(re, dt, fo);
     }
 }
 
@@ -763,7 +814,11 @@ int oracle2d_init(const hos2d_params* p) {
     C = Config();
     C.p = *p;
     if (!(p->order == 5 || p->order == 7 || p->order == 9)) return 2;
-    if (!p->use_df) return 2;  // only the discontinuity-feedback variants are restated
+    // the non-DF scheme (WENO5_AO_normal / WENO5_AO_tangent, the drivers' default slots) exists
+    // for WENO5 only, and its tangential sweep writes the Gauss points only when gausspoint == 2
+    // (src/reconstruction.cpp:2264, :2279)
+    if (!p->use_df && p->order != 5) return 2;
+    if (p->wenotype < 0 || p->wenotype > 2) return 2;
     const int need_gp = p->order == 5 ? 2 : p->order == 7 ? 3 : 4;
     if (p->gausspoint != need_gp) return 2;
     if (p->ghost < p->order / 2 + 1) return 2;
@@ -1028,7 +1083,9 @@ int oracle2d_stage(int stage, double dt) {
             }
         }
     }
-    // DF factor update (Update_alpha, :1523-1534)
+    // DF factor update (Update_alpha, :1523-1534), which the drivers call only with
+    // is_using_df_factor set (src/2Dproblem.cpp:154)
+    if (!C.p.use_df) return 0;
     const int jend = g + std::min(C.p.nodex, C.p.nodey);
 #pragma omp parallel for
     for (int i = g; i < g + C.p.nodex; ++i)

@@ -55,6 +55,14 @@ const double TC[2][2][2] = {{{0.5, 1.0 / 8.0}, {0.0, 0.0}}, {{1.0, 1.0 / 6.0}, {
 // the 3D restatement follow the 1D convention so that one-dimensional data can be compared
 // with the reference-pinned 1D restatement with every GKS term active.
 int HALF_TAU_OF_DT = 0;
+// Checker-only switch: the reference's own 3D conventions, the two departures listed at the
+// top of this file (pressure in the lambda slot of GKS3D; order-reduction flags of lines and
+// points that stay set), so that the restatement can be compared bit for bit with the
+// reference's 3D functions run by oracle/ref_driver3d.cpp.
+int REF_CONVENTIONS = 0;
+// the reference's sticky flags: per direction, line flags over the line grid of
+// direction_fluxes (face a, b interior, c with halo 2), point flags per interior face and line
+std::vector<unsigned char> LINE_FLAG[3], POINT_FLAG[3];
 
 inline size_t cell(int i, int j, int k) { return ((size_t)i * NY + j) * NZ + k; }
 
@@ -251,7 +259,9 @@ void sweep_side(const Side* const* stencil, int nd, double h, Side* out) {
 // both sides of a face position, with the order reduction of the sweep (:4110-4142,
 // :4362-4397): any non-positive lambda among the two points' left/right values sends both
 // points back to the centre state with a zero slope along the sweep
-void sweep(const LR* const* stencil, int nd, double h, LR* out) {
+// sticky (reference conventions only): the position's order-reduction flag, read and set as
+// the reference's line[0].order_reduce / point[0].order_reduce are (:4124-4132, :4380-4384)
+void sweep(const LR* const* stencil, int nd, double h, LR* out, unsigned char* sticky = nullptr) {
     const Side* sl[5];
     const Side* sr[5];
     for (int m = 0; m < 5; ++m) { sl[m] = &stencil[m]->l; sr[m] = &stencil[m]->r; }
@@ -260,6 +270,10 @@ void sweep(const LR* const* stencil, int nd, double h, LR* out) {
     sweep_side(sr, nd, h, orr);
     bool reduce = false;
     for (int ig = 0; ig < 2; ++ig) reduce = reduce || needs_reduce(ol[ig].c) || needs_reduce(orr[ig].c);
+    if (sticky) {
+        reduce = reduce || *sticky;
+        if (reduce) *sticky = 1;
+    }
     for (int ig = 0; ig < 2; ++ig) {
         if (reduce) {
             out[ig] = *stencil[2];
@@ -395,8 +409,11 @@ void time_coeffs(double* t, double tau, double tn, double dt) {
 // f = 4 F(dt/2) - F(dt), derf = 4 (F(dt) - 2 F(dt/2)), in the face's frame
 void gks3(const Side& L, const Side& R, double dt, double* f, double* df) {
     double pl[5], prr[5], p0[5];
-    to_ulambda(pl, L.c);
-    to_ulambda(prr, R.c);
+    // the reference hands Convar_to_primvar_3D's pressure to every lambda slot
+    // (src/flux_function.cpp:831-836, 914); the restatement uses lambda
+    auto prim_of = REF_CONVENTIONS ? to_prim : to_ulambda;
+    prim_of(pl, L.c);
+    prim_of(prr, R.c);
     Mom3 ml, mr;
     mom3(ml, 0, pl[1], pl[2], pl[3], pl[4]);
     mom3(mr, 1, prr[1], prr[2], prr[3], prr[4]);
@@ -418,7 +435,7 @@ void gks3(const Side& L, const Side& R, double dt, double* f, double* df) {
         gaddr(mr, 2, 0, 0, 0, 0, ar[d], a0r);
         for (int v = 0; v < 5; ++v) d0[d][v] = dl * a0l[v] + dr * a0r[v];
     }
-    to_ulambda(p0, c0);
+    prim_of(p0, c0);
     const double tau = tau_ns(p0[0], p0[4]);
     double t[6];
     time_coeffs(t, tau, tau_num(dl, dr, p0[0], pl[4], prr[4], p0[4], dt), dt);
@@ -537,6 +554,7 @@ void bc3() {
 // per direction: face values on the local grid, lines, points, GKS at the four Gauss points;
 // stored per face as sum over the points of weight 1/4 x (f, derf) in the face frame
 std::vector<double> FXS[3];  // [dir][(face * 2 + stage) * 10 + q]: f[5], derf[5]
+std::vector<double> FXP[3];  // per Gauss point: [dir][((face * 2 + stage) * 4 + point) * 10 + q]
 
 struct FaceGrid {
     int na, nb, nc;  // local face grid: normal faces 0..n0-2G (interior faces), tangential interior
@@ -571,7 +589,8 @@ void direction_fluxes(int dir, int stage, double dt) {
                 const LR* st[5];
                 for (int m = 0; m < 5; ++m) st[m] = &fv(a, b - 2 + m, c);
                 LR out[2];
-                sweep(st, 1, gr.h1, out);
+                const size_t li = ((size_t)(a - g) * n1 + (b - g)) * ec + (c - g + 2);
+                sweep(st, 1, gr.h1, out, REF_CONVENTIONS ? &LINE_FLAG[dir][li] : nullptr);
                 lv(a, b, c, 0) = out[0];
                 lv(a, b, c, 1) = out[1];
             }
@@ -582,46 +601,48 @@ void direction_fluxes(int dir, int stage, double dt) {
         for (int b = g; b < gr.n1 - g; ++b)
             for (int c = g; c < gr.n2 - g; ++c) {
                 double acc[10] = {0};
+                const size_t face = ((size_t)(a - g) * n1 + (b - g)) * n2 + (c - g);
+                double* opt = &FXP[dir][(face * 2 + stage) * 4 * 10];
                 for (int ig = 0; ig < 2; ++ig) {
                     const LR* st[5];
                     for (int m = 0; m < 5; ++m) st[m] = &lv(a, b, c - 2 + m, ig);
                     LR pt[2];
-                    sweep(st, 2, gr.h2, pt);
+                    const size_t pi = ((((size_t)(a - g) * n1 + (b - g)) * n2 + (c - g)) * 2) + ig;
+                    sweep(st, 2, gr.h2, pt, REF_CONVENTIONS ? &POINT_FLAG[dir][pi] : nullptr);
                     for (int ip = 0; ip < 2; ++ip) {
                         double f[5], df[5];
                         gks3(pt[ip].l, pt[ip].r, dt, f, df);
+                        // the reference's Gauss point ig * 2 + ip (gauss[i * sqrt(gausspoint)], :4152-4160)
+                        for (int v = 0; v < 5; ++v) {
+                            opt[(ig * 2 + ip) * 10 + v] = f[v];
+                            opt[(ig * 2 + ip) * 10 + 5 + v] = df[v];
+                        }
                         for (int v = 0; v < 5; ++v) {
                             acc[v] += 0.25 * f[v];
                             acc[5 + v] += 0.25 * df[v];
                         }
                     }
                 }
-                const size_t face = ((size_t)(a - g) * n1 + (b - g)) * n2 + (c - g);
                 double* o = &FX[(face * 2 + stage) * 10];
                 for (int q = 0; q < 10; ++q) o[q] = acc[q];
             }
 }
 
-// stage-combined flux of local face (a, b, c) (interior-relative indices), global frame
-void combined(int dir, int stage, int a, int b, int c, double* out) {
+// stage-combined flux of Gauss point m of local face (a, b, c) (interior-relative indices),
+// in the face frame: sum over the stages so far of c_f f + c_d derf (Update_gauss,
+// src/time_advance.cpp:866-939)
+void combined(int dir, int stage, int a, int b, int c, int m, double* loc) {
     const Grid gr = grid(dir);
     const int n1 = gr.n1 - 2 * G, n2 = gr.n2 - 2 * G;
     const size_t face = ((size_t)a * n1 + b) * n2 + c;
-    double loc[5];
     for (int v = 0; v < 5; ++v) {
         double s = 0.0;
         for (int k = 0; k <= stage; ++k) {
-            const double* q = &FXS[dir][(face * 2 + k) * 10];
+            const double* q = &FXP[dir][((face * 2 + k) * 4 + m) * 10];
             s = s + (TC[stage][k][0] * q[v] + TC[stage][k][1] * q[5 + v]);
         }
         loc[v] = s;
     }
-    // back to the global frame (Update_gauss, src/time_advance.cpp:958-972)
-    out[0] = loc[0];
-    out[4] = loc[4];
-    if (dir == 0) { out[1] = loc[1]; out[2] = loc[2]; out[3] = loc[3]; }
-    else if (dir == 1) { out[1] = -loc[2]; out[2] = loc[1]; out[3] = loc[3]; }
-    else { out[1] = -loc[3]; out[2] = loc[2]; out[3] = loc[1]; }
 }
 
 int stage3(int stage, double dt) {
@@ -642,20 +663,33 @@ int stage3(int stage, double dt) {
     for (int I = 0; I < nx; ++I)
         for (int J = 0; J < ny; ++J)
             for (int K = 0; K < nz; ++K) {
-                // local indices of the six faces: x (I, J, K); y (J, nx-1-I, K); z (K, J, nx-1-I)
-                double xl[5], xr[5], yl[5], yr[5], zl[5], zr[5];
-                combined(0, stage, I, J, K, xl);
-                combined(0, stage, I + 1, J, K, xr);
-                combined(1, stage, J, nx - 1 - I, K, yl);
-                combined(1, stage, J + 1, nx - 1 - I, K, yr);
-                combined(2, stage, K, J, nx - 1 - I, zl);
-                combined(2, stage, K + 1, J, nx - 1 - I, zr);
+                // local indices of the six faces: x (I, J, K); y (J, nx-1-I, K); z (K, J, nx-1-I).
+                // Per Gauss point the z, y and x face differences are accumulated in that order
+                // with weight 1/4, the y and z faces' momentum components rotated back to the
+                // global frame as the reference writes them (Update_gauss, :941-996).
+                const double odx = 1 / DX, ody = 1 / DY, odz = 1 / DZ, w = 0.25;
                 double tot[5];
                 for (int v = 0; v < 5; ++v) tot[v] = 0.0;
-                // the four Gauss points' weights were applied when the fluxes were summed
-                for (int v = 0; v < 5; ++v) tot[v] += 1.0 / DZ * (zl[v] - zr[v]);
-                for (int v = 0; v < 5; ++v) tot[v] += 1.0 / DY * (yl[v] - yr[v]);
-                for (int v = 0; v < 5; ++v) tot[v] += 1.0 / DX * (xl[v] - xr[v]);
+                for (int m = 0; m < 4; ++m) {
+                    double xl[5], xr[5], yl[5], yr[5], zl[5], zr[5];
+                    combined(0, stage, I, J, K, m, xl);
+                    combined(0, stage, I + 1, J, K, m, xr);
+                    combined(1, stage, J, nx - 1 - I, K, m, yl);
+                    combined(1, stage, J + 1, nx - 1 - I, K, m, yr);
+                    combined(2, stage, K, J, nx - 1 - I, m, zl);
+                    combined(2, stage, K + 1, J, nx - 1 - I, m, zr);
+                    tot[0] += w * odz * (zl[0] - zr[0]);
+                    tot[1] += w * odz * (-zl[3] + zr[3]);
+                    tot[2] += w * odz * (zl[2] - zr[2]);
+                    tot[3] += w * odz * (zl[1] - zr[1]);
+                    tot[4] += w * odz * (zl[4] - zr[4]);
+                    tot[0] += w * ody * (yl[0] - yr[0]);
+                    tot[1] += w * ody * (-yl[2] + yr[2]);
+                    tot[2] += w * ody * (yl[1] - yr[1]);
+                    tot[3] += w * ody * (yl[3] - yr[3]);
+                    tot[4] += w * ody * (yl[4] - yr[4]);
+                    for (int v = 0; v < 5; ++v) tot[v] += w * odx * (xl[v] - xr[v]);
+                }
                 const size_t cc = cell(I + G, J + G, K + G);
                 for (int v = 0; v < 5; ++v) W[5 * cc + v] = Wold[5 * cc + v] + tot[v];
             }
@@ -688,6 +722,7 @@ int oracle3d_init(const hos3d_params* p) {
     for (int d = 0; d < 3; ++d) {
         const Grid gr = grid(d);
         FXS[d].assign((size_t)(gr.n0 - 2 * G + 1) * (gr.n1 - 2 * G) * (gr.n2 - 2 * G) * 2 * 10, 0.0);
+        FXP[d].assign(FXS[d].size() * 4, 0.0);
     }
     return 0;
 }
@@ -695,10 +730,18 @@ int oracle3d_init(const hos3d_params* p) {
 void oracle3d_free(void) {
     W.clear(); Wold.clear(); PR.clear();
     for (auto& f : FXS) f.clear();
+    for (auto& f : FXP) f.clear();
 }
 
 void oracle3d_set_state(const double* convar, const double* primvar) {
     const size_t n = (size_t)NX * NY * NZ * 5;
+    // a new run: the reference's sticky order-reduction flags start cleared
+    for (int d = 0; d < 3; ++d) {
+        const Grid gr = grid(d);
+        const size_t nn = gr.n0 - 2 * G + 1, n1 = gr.n1 - 2 * G, n2 = gr.n2 - 2 * G;
+        LINE_FLAG[d].assign(nn * n1 * (n2 + 4), 0);
+        POINT_FLAG[d].assign(nn * n1 * n2 * 2, 0);
+    }
     std::memcpy(W.data(), convar, n * sizeof(double));
     if (primvar) std::memcpy(PR.data(), primvar, n * sizeof(double));
     else
@@ -735,6 +778,17 @@ double oracle3d_begin_step(double tstop, double t) {
 int oracle3d_stage(int stage, double dt) { return stage3(stage, dt); }
 
 void oracle3d_set_half_tau_of_dt(int on) { HALF_TAU_OF_DT = on; }
+
+void oracle3d_set_reference_conventions(int on) { REF_CONVENTIONS = on; }
+
+long long oracle3d_reduced_count(void) {
+    long long n = 0;
+    for (int d = 0; d < 3; ++d) {
+        for (unsigned char f : LINE_FLAG[d]) n += f ? 2 : 0;     // both lines of the face
+        for (unsigned char f : POINT_FLAG[d]) n += f ? 2 : 0;    // both points of the line
+    }
+    return n;
+}
 
 int oracle3d_step(double tstop, double t, double* dt_out) {
     double dt = oracle3d_begin_step(tstop, t);

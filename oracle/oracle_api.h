@@ -32,7 +32,7 @@ typedef struct hos2d_params {
     int order;            /* WENO-AO order: 5, 7 or 9                        */
     int gausspoint;       /* Gauss points per face: 2 (5th), 3 (7th), 4 (9th)*/
     int characteristic;   /* 1: characteristic variables, 0: conservative    */
-    int use_df;           /* 1: discontinuity-feedback variants (always 1 here) */
+    int use_df;           /* 1: discontinuity-feedback variants; 0: non-DF WENO5-AO (order 5) */
     int K;                /* internal degrees of freedom (2D: K = 3 for gamma 1.4) */
     double gamma;
     double c1_euler, c2_euler;  /* numerical collision time coefficients     */
@@ -51,6 +51,9 @@ typedef struct hos2d_params {
     double mu, nu;
     int prandtl_fix;
     double prandtl;
+    /* weights of the non-DF WENO5-AO scheme (use_df = 0; the reference's wenotype):
+     * 0 Z-type (wenoz), 1 Jiang-Shu (wenojs), 2 linear */
+    int wenotype;
 } hos2d_params;
 
 /* ---- restatement (liboracle.so) ---- */
@@ -104,6 +107,7 @@ typedef struct hos1d_params {
     double cfl;
     double left, right;
     int bc[2];            /* left, right: HOS_BC_FREE / PERIODIC / REFLECT              */
+    int wenotype;         /* non-DF steps: 0 Z-type, 1 Jiang-Shu, 2 linear weights      */
 } hos1d_params;
 
 int    oracle1d_init(const hos1d_params* p);
@@ -132,6 +136,8 @@ typedef struct hos3d_params {
     int bc[6];                        /* left, right, down, up, back, front: FREE / PERIODIC / REFLECT */
     int prandtl_fix;                  /* 1: Prandtl-number correction of the heat flux      */
     double prandtl;                   /* Pr */
+    int gks3d_pressure_slot;          /* GPU switch of the same layout; the restatement takes
+                                         oracle3d_set_reference_conventions instead          */
 } hos3d_params;
 
 int    oracle3d_init(const hos3d_params* p);
@@ -144,6 +150,23 @@ int    oracle3d_step(double tstop, double t, double* dt_out);
 /* 1: keep the collision time of dt at the dt/2 level (the 1D GKS convention), for comparing
  * one-dimensional 3D data with the 1D restatement; 0 (default): recompute it (GKS3D) */
 void   oracle3d_set_half_tau_of_dt(int on);
+/* 1: the reference's own 3D conventions (pressure in GKS3D's lambda slots, order-reduction flags
+ * of lines and Gauss points that stay set once set), for comparing with the reference's 3D
+ * functions run by ref_driver3d.cpp; 0 (default): lambda, each reconstruction decides afresh */
+void   oracle3d_set_reference_conventions(int on);
+/* number of line / Gauss-point reconstructions whose order-reduction flag is set (reference
+ * conventions only) */
+long long oracle3d_reduced_count(void);
+
+/* ---- compiled reference, 3D (_ref/libhosref.so, ref_driver3d.cpp): free sides only ---- */
+int    ref3d_init(const hos3d_params* p);
+void   ref3d_set_threads(int n);
+void   ref3d_set_state(const double* convar, const double* primvar);
+void   ref3d_get_state(double* convar, double* primvar);
+double ref3d_begin_step(double tstop, double t);
+int    ref3d_stage(int stage, double dt);
+int    ref3d_step(double tstop, double t, double* dt_out);
+long long ref3d_reduced_count(void);
 /* per interior face of direction dir, stage fluxes summed over the 4 Gauss points with
  * weight 1/4, in the face frame: [face][stage][f 5, derf 5]; faces ordered (normal, t1, t2)
  * with x faces (i, j, k), y faces (j, nx-1-i, k), z faces (k, j, nx-1-i) over interior cells */

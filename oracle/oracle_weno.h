@@ -356,8 +356,30 @@ inline double beta5_big(double wn2, double wn1, double w0, double wp1, double wp
                              8209.0 * wn2 * wp2 - 51001.0 * wp1 * wp2 + 6908.0 * wp2 * wp2);
 }
 
-// non-DF WENO5-AO (wenoz, epsilon 1e-10, full 5th-order indicator), :161-360
-inline void weno5_plain(int side, const double* s, double h, double& var, double& der) {
+// Nonlinear weights of the non-DF WENO5-AO kernels for each wenotype (the reference's
+// WENOtype global, src/reconstruction.cpp:7): WENO_Z alpha_k = d_k (1 + (tau / (beta_k + eps))^2),
+// WENO_JS alpha_k = d_k / (eps + beta_k)^2, WENO_LINEAR the linear weights (:176-216).
+enum { WENO_Z = 0, WENO_JS = 1, WENO_LINEAR = 2 };
+inline void weno5_nonlinear(int wtype, const double* d, const double* beta, double tau, double eps, double* ww) {
+    if (wtype == WENO_LINEAR) {
+        for (int k = 0; k < 4; ++k) ww[k] = d[k];
+        return;
+    }
+    double alpha[4], sum = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        if (wtype == WENO_JS) {
+            alpha[k] = d[k] / ((eps + beta[k]) * (eps + beta[k]));
+        } else {
+            double gd = tau / (beta[k] + eps);
+            alpha[k] = d[k] * (1 + gd * gd);
+        }
+        sum += alpha[k];
+    }
+    for (int k = 0; k < 4; ++k) ww[k] = alpha[k] / sum;
+}
+
+// non-DF WENO5-AO (epsilon 1e-10, full 5th-order indicator), :161-360
+inline void weno5_plain(int side, const double* s, double h, double& var, double& der, int wtype = WENO_Z) {
     const double dhi = 0.85, dlo = 0.85, eps = 1e-10;
     const double wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
     double d[4] = {(1.0 - dhi) * (1.0 - dlo) / 2.0, (1.0 - dhi) * dlo, (1.0 - dhi) * (1.0 - dlo) / 2.0, dhi};
@@ -365,13 +387,8 @@ inline void weno5_plain(int side, const double* s, double h, double& var, double
     beta3(s, 2, beta);
     beta[3] = beta5_big(wn2, wn1, w0, wp1, wp2);
     double tau = 1.0 / 3.0 * (std::abs(beta[3] - beta[0]) + std::abs(beta[3] - beta[1]) + std::abs(beta[3] - beta[2]));
-    double alpha[4], sum = 0.0, ww[4], fw[4], p[4], px[4];
-    for (int k = 0; k < 4; ++k) {
-        double gd = tau / (beta[k] + eps);
-        alpha[k] = d[k] * (1 + gd * gd);
-        sum += alpha[k];
-    }
-    for (int k = 0; k < 4; ++k) ww[k] = alpha[k] / sum;
+    double ww[4], fw[4], p[4], px[4];
+    weno5_nonlinear(wtype, d, beta, tau, eps, ww);
     if (side == 0) {
         p[0] = -1.0 / 6.0 * wn2 + 5.0 / 6.0 * wn1 + 1.0 / 3.0 * w0;
         p[1] = 1.0 / 3.0 * wn1 + 5.0 / 6.0 * w0 - 1.0 / 6.0 * wp1;
@@ -403,8 +420,10 @@ inline void weno5_plain(int side, const double* s, double h, double& var, double
 
 // Non-DF WENO5-AO at the two Gauss-Legendre points -h/(2 sqrt 3) (g[0]) and +h/(2 sqrt 3)
 // (g[1]) of the centre cell, with first derivatives when want_der (weno_5th_ao_2gauss,
-// src/reconstruction.cpp:2393-2551: epsilon 1e-6, wenoz weights).
-inline void weno5_2gauss(const double* s, double h, bool want_der, double* g, double* gx) {
+// src/reconstruction.cpp:2393-2551: epsilon 1e-6; Z-type or Jiang-Shu weights).  Under
+// wenotype = linear the reference leaves alpha and sum_alpha unset (:2446-2468 have no linear
+// branch), so its result is undefined; this restatement takes the linear weights there.
+inline void weno5_2gauss(const double* s, double h, bool want_der, double* g, double* gx, int wtype = WENO_Z) {
     const double dhi = 0.85, dlo = 0.85, eps = 1e-6;
     const double wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
     double d[4] = {(1 - dhi) * (1 - dlo) * 0.5, (1 - dhi) * dlo, (1 - dhi) * (1 - dlo) * 0.5, dhi};
@@ -412,13 +431,8 @@ inline void weno5_2gauss(const double* s, double h, bool want_der, double* g, do
     beta3(s, 2, beta);
     beta[3] = beta5_big(wn2, wn1, w0, wp1, wp2);
     double tau = 1.0 / 3.0 * (std::abs(beta[3] - beta[0]) + std::abs(beta[3] - beta[1]) + std::abs(beta[3] - beta[2]));
-    double alpha[4], sum = 0.0, ww[4], fw[4], p[4], px[4];
-    for (int k = 0; k < 4; ++k) {
-        double gd = tau / (beta[k] + eps);
-        alpha[k] = d[k] * (1 + gd * gd);
-        sum += alpha[k];
-    }
-    for (int k = 0; k < 4; ++k) ww[k] = alpha[k] / sum;
+    double ww[4], fw[4], p[4], px[4];
+    weno5_nonlinear(wtype, d, beta, tau, eps, ww);
     fw[3] = ww[3] / d[3];
     for (int k = 0; k < 3; ++k) fw[k] = ww[k] - ww[3] / d[3] * d[k];
     const double sqrt3 = 1.732050807568877294;

@@ -91,7 +91,7 @@ int ref2d_init(const hos2d_params* p) {
     gausspoint = p->gausspoint;
     SetGuassPoint();
     reconstruction_variable = p->characteristic ? characteristic : conservative;
-    wenotype = wenoz;
+    wenotype = p->wenotype == 1 ? wenojs : p->wenotype == 2 ? linear : wenoz;
     is_using_df_factor = p->use_df != 0;
     if (p->order == 5) {
         cellreconstruction_2D_normal = p->use_df ? WENO5_AO_with_df_normal : WENO5_AO_normal;
@@ -209,6 +209,22 @@ int ref2d_stage(int stage, double dt) {
     Convar_to_Primvar(g_fluids, g_block);
     Reconstruction_within_cell(g_xif, g_yif, g_fluids, g_block);
     Reconstruction_forg0(g_xif, g_yif, g_fluids, g_block);
+    if (flux_function_2d == LF2D && tau_type == NS) {
+        // LF2D's viscous term (NS_by_central_difference_prim_2D) reads each Gauss point's
+        // centre state, which Center_all_collision_multi fills only when the flux is GKS2D
+        // (src/reconstruction.cpp:3642-3650); the reference leaves it as allocated
+        // (uninitialised).  The harness fills it with the reference's own
+        // Center_all_collision_2d_multi on every face Calculate_flux evaluates.
+        const Block2d b = g_block;
+#pragma omp parallel for
+        for (int i = b.ghost; i < b.nodex + b.ghost + 1; i++)
+            for (int j = b.ghost; j < b.nodey + b.ghost; j++)
+                for (int m = 0; m < gausspoint; m++) Center_all_collision_2d_multi(g_xif[i * (b.ny + 1) + j].gauss[m]);
+#pragma omp parallel for
+        for (int i = b.ghost; i < b.nodex + b.ghost; i++)
+            for (int j = b.ghost; j < b.nodey + b.ghost + 1; j++)
+                for (int m = 0; m < gausspoint; m++) Center_all_collision_2d_multi(g_yif[i * (b.ny + 1) + j].gauss[m]);
+    }
     Calculate_flux(g_xfl, g_yfl, g_xif, g_yif, g_block, stage);
     if (g_source) Update_with_source(g_fluids, g_xfl, g_yfl, g_block, stage);
     else Update(g_fluids, g_xfl, g_yfl, g_block, stage);
@@ -286,7 +302,7 @@ int ref1d_init(const hos1d_params* p) {
     tau_type = Euler;
     c1_euler = p->c1_euler;
     c2_euler = p->c2_euler;
-    wenotype = wenoz;
+    wenotype = p->wenotype == 1 ? wenojs : p->wenotype == 2 ? linear : wenoz;
     reconstruction_variable = p->characteristic ? characteristic : conservative;
     g0reconstruction = Center_collision;
     flux_function = GKS;

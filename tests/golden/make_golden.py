@@ -9,7 +9,8 @@ alpha_x, alpha_y) after 1 and after 3 S2O4 steps, and the three time steps ("fo_
 step 0 with First_order_normal / First_order_tangent, as the drivers do when
 is_using_df_factor is set; "ns_" cases use the Navier-Stokes collision time, no-slip walls
 and the Prandtl fix, also with a first-order step 0; "rt_" is the RT_instability loop with
-Update_with_source).
+Update_with_source; "nodf_" cases run the drivers' default non-DF WENO5-AO slots with
+is_using_df_factor = false and the Z-type or Jiang-Shu weights).
 
 tests/golden/refapi/ holds runs of the reference-API drivers (tests/refapi/driver2d.cpp,
 driver1d.cpp) linked against the reference's own objects (oracle/Makefile, refdrivers): the
@@ -48,7 +49,9 @@ def step_cases():
                  "tmarch_rk3_lf_w5_24", "tmarch_rk4_gks_w9_24", "tmarch_s2o4_lf_w7_24"):
         yield name, _problem(name)
     for name in ("fo_w5_free_24", "fo_w7_periodic_24", "fo_w9_reflect_24",
-                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w7_cap_24", "ns_w9_nu_24", "rt_w5_12"):
+                 "ns_w5_noslip_24", "ns_w7_wall_24", "ns_w7_cap_24", "ns_w9_nu_24", "rt_w5_12",
+                 "nodf_w5_z_free_24", "nodf_w5_js_reflect_24", "nodf_w5_z_cons_20",
+                 "lfns_w5_mu_24", "lfns_w7_nu_24", "lfns_w9_walls_24"):
         yield name, _problem(name)
 
 
@@ -119,9 +122,31 @@ def refapi():
     print("refapi_sod1d_1000", r["steps"], r["t"])
 
 
+def three_d():
+    """The reference's own 3D functions run by oracle/ref_driver3d.cpp (which allocates the
+    Gauss-point arrays the reference leaves unallocated): initial state, every step's state
+    and dt of the cases of test_oracle3d_cpu.ref3d_problem."""
+    from oracle_lib import CpuStep3D
+    from test_oracle3d_cpu import REF3D_CASES, ref3d_problem
+    for name in REF3D_CASES:
+        pb, W, steps = ref3d_problem(name)
+        r = CpuStep3D("ref").init(pb)
+        r.set_state(W)
+        out = {"convar0": W}
+        dts = []
+        for k in range(steps):
+            dts.append(r.step())
+            out[f"convar{k + 1}"] = r.state()["convar"]
+        np.savez_compressed(OUT / f"{name}.npz", dts=np.array(dts), **out)
+        print(name, dts)
+
+
 def main(only=None):
     if only == "refapi":
         refapi()
+        return
+    if only == "ref3d":
+        three_d()
         return
     for name, (pb, con, prim) in step_cases():
         if only and not name.startswith(only):
@@ -150,6 +175,7 @@ def main(only=None):
     print(errs)
     one_d()
     refapi()
+    three_d()
 
 
 if __name__ == "__main__":

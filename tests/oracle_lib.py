@@ -12,7 +12,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent.parent
 ORACLE_DIR = ROOT / "oracle"
-REFERENCE = Path("/root/reference")
+REFERENCE = Path(os.environ.get("HOS_REFERENCE", "/root/reference"))
 _DP = ctypes.POINTER(ctypes.c_double)
 
 
@@ -164,20 +164,24 @@ def gate_cells(pb, convar, alpha_x=None, alpha_y=None):
 
 
 class CpuStep3D:
-    """The 3D restatement (oracle3d_*)."""
+    """The 3D restatement (oracle3d_*) or, with kind="ref", the compiled reference's own 3D
+    functions driven by oracle/ref_driver3d.cpp (ref3d_*)."""
 
-    def __init__(self):
-        self.lib = CpuStep("oracle").lib
-        self.lib.oracle3d_begin_step.restype = ctypes.c_double
+    def __init__(self, kind: str = "oracle"):
+        self.lib = CpuStep(kind).lib
+        self.pre = "oracle3d_" if kind == "oracle" else "ref3d_"
+        self.fn("begin_step").restype = ctypes.c_double
 
     def fn(self, name):
-        return getattr(self.lib, "oracle3d_" + name)
+        return getattr(self.lib, self.pre + name)
 
-    def init(self, pb):
+    def init(self, pb, threads: int | None = None):
         self.pb = pb
         self.params = pb.to_c()
         if self.fn("init")(ctypes.byref(self.params)) != 0:
             raise RuntimeError("init failed")
+        if threads and self.pre == "ref3d_":
+            self.fn("set_threads")(threads)
         self.t, self.nstep = 0.0, 0
         return self
 

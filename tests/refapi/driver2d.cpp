@@ -12,7 +12,9 @@
 // reference's drivers do at step 0 when is_using_df_factor is set, src/2Dproblem.cpp:733-745;
 // tau_type (1: NS), mu, nu, prandtl_fix, pr: the collision-time globals; bc names may be
 // noslip, whose wall velocity comes from the side's bcprim entry; source 1: the RT_instability
-// loop, RT_boundary and Update_with_source, src/2Dproblem.cpp:746-763).
+// loop, RT_boundary and Update_with_source, src/2Dproblem.cpp:746-763; df 0: the drivers'
+// default with is_using_df_factor = false, the slots WENO5_AO_normal / WENO5_AO_tangent and
+// the weights "wenotype z|js|linear", src/2Dproblem.cpp:35-38, 132-136).
 // state_in.bin: convar then primvar, [nx*ny][4] doubles each.  state_out.bin: convar, primvar,
 // alpha_x, alpha_y, then t, the step count and every step's dt.
 #include <cstdio>
@@ -87,7 +89,8 @@ int main(int argc, char** argv) {
     gausspoint = order == 5 ? 2 : order == 7 ? 3 : 4;
     SetGuassPoint();
     reconstruction_variable = num("characteristic") != 0 ? characteristic : conservative;
-    wenotype = wenoz;
+    const std::string wt = cfg.count("wenotype") ? cfg.at("wenotype").at(0) : "z";
+    wenotype = wt == "js" ? wenojs : wt == "linear" ? linear : wenoz;
     Reconstruction_within_Cell_2D_normal normal_df =
         order == 5 ? WENO5_AO_with_df_normal : order == 7 ? WENO7_AO_with_df_normal : WENO9_AO_with_df_normal;
     Reconstruction_within_Cell_2D_tangent tangent_df =
@@ -97,7 +100,11 @@ int main(int argc, char** argv) {
     g0reconstruction_2D_normal = Center_do_nothing_normal;
     g0reconstruction_2D_tangent = Center_all_collision_multi;
     is_reduce_order_warning = false;
-    is_using_df_factor = true;
+    is_using_df_factor = !(cfg.count("df") && num("df") == 0);
+    if (!is_using_df_factor) {
+        cellreconstruction_2D_normal = WENO5_AO_normal;
+        cellreconstruction_2D_tangent = WENO5_AO_tangent;
+    }
     gks2dsolver = gks2nd_2d;
     tau_type = cfg.count("tau_type") && num("tau_type") == 1 ? NS : Euler;
     if (cfg.count("mu")) Mu = num("mu");

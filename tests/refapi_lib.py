@@ -39,6 +39,8 @@ def config2d(pb, steps: int, tstop: float = 1e30, precision: int = 0, mirror: in
              f"c1 {pb.c1_euler!r}", f"c2 {pb.c2_euler!r}", f"cfl {pb.cfl!r}", f"left {pb.left!r}",
              f"right {pb.right!r}", f"down {pb.down!r}", f"up {pb.up!r}", "bc " + " ".join(bc),
              f"steps {steps}", f"tstop {tstop!r}", f"precision {precision}", f"mirror {mirror}"]
+    if not getattr(pb, "use_df", True):
+        lines += ["df 0", "wenotype " + {"wenoz": "z", "wenojs": "js", "linear": "linear"}[pb.wenotype]]
     if getattr(pb, "first_order_steps", 0):
         lines.append(f"first_order_steps {pb.first_order_steps}")
     if getattr(pb, "source", False):
@@ -122,9 +124,17 @@ def refapi_cases_2d():
     # the RT_instability loop (src/2Dproblem.cpp:699-763): RT_boundary, Update_with_source
     rt = cases.rt2d(12)
     rt[0].source, rt[0].first_order_steps = True, 1
+    # PlanarShock with the reference's default is_using_df_factor = false: the slots stay
+    # WENO5_AO_normal / WENO5_AO_tangent (non-DF WENO5-AO, Z-type weights), no Update_alpha
+    nodf = cases.riemann2d(20, order=5)
+    nodf[0].use_df = False
+    nodf_js = cases.random_riemann2d(20, seed=21, order=5)
+    nodf_js[0].use_df, nodf_js[0].wenotype, nodf_js[0].bc = False, "wenojs", ("periodic",) * 4
     return [("refapi_riemann_w7_24", cases.riemann2d(24, order=7), 5),
             ("refapi_rt_w5_12", rt, 4),
             ("refapi_fo_w9_reflect_20", fo, 4),
             ("refapi_ns_noslip_w5_20", ns, 4),
             ("refapi_inflow_reflect_w5_20", inflow, 5),
-            ("refapi_vortex_w9_20", cases.isentropic_vortex(20, order=9), 3)]
+            ("refapi_vortex_w9_20", cases.isentropic_vortex(20, order=9), 3),
+            ("refapi_nodf_riemann_w5_20", nodf, 5),
+            ("refapi_nodf_js_periodic_w5_20", nodf_js, 4)]

@@ -68,3 +68,20 @@ def test_oracle1d_matches_reference_bitwise(order, charac, bc):
     g = pb.ghost
     assert np.array_equal(a.state()["convar"][g:-g], b.state()["convar"][g:-g])
     assert np.array_equal(a.state()["alpha"], b.state()["alpha"])
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference checkout not present")
+@pytest.mark.parametrize("wenotype", ["wenojs", "linear"])
+def test_oracle1d_wenotype_matches_reference_bitwise(wenotype):
+    """The Sod driver's non-DF WENO5-AO steps under the other wenotype weights
+    (weno_5th_ao_left / _right, src/reconstruction.cpp:161-360, honour all three)."""
+    pb, con = cases.sod1d(120, order=5)
+    pb.df_mode, pb.wenotype = 0, wenotype
+    a = CpuStep1D("ref").init(pb)
+    b = CpuStep1D("oracle").init(pb)
+    a.set_state(con)
+    b.set_state(con)
+    for _ in range(20):
+        assert a.step(0.2) == b.step(0.2)
+    g = pb.ghost
+    assert np.array_equal(a.state()["convar"][g:-g], b.state()["convar"][g:-g])

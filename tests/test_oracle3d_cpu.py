@@ -1,7 +1,12 @@
 """The 3D restatement (oracle/hos_oracle3d.cpp), checked on the CPU.
 
-The reference's own 3D path does not run (its Gauss-point arrays are never allocated), so
-the 3D restatement is pinned as follows:
+The reference's own 3D path does not run as shipped: its Gauss-point arrays are never
+allocated.  oracle/ref_driver3d.cpp allocates them and runs the reference's own 3D
+functions unmodified (CubicTube's loop).  The restatement is pinned as follows:
+  * with the reference's own conventions switched on (pressure in GKS3D's lambda slots,
+    order-reduction flags of lines and points that stay set), it equals the reference's 3D
+    code bit for bit (golden vectors tests/golden/ref3d_*.npz, and the compiled reference
+    where the checkout exists); switching them off is the only difference to the default;
   * one-dimensional data along x, y or z gives the 1D restatement's result, which is itself
     bit-exact with the compiled reference (test_oracle1d_cpu.py), to rounding: this covers
     the normal reconstruction, every GKS3D term, the update, the CFL and the frame rotations;
@@ -17,11 +22,105 @@ import ctypes
 import numpy as np
 import pytest
 
-from oracle_lib import CpuStep1D, CpuStep3D
+from oracle_lib import CpuStep1D, CpuStep3D, ref_available
 
 from hos_gb300.params import DF_NEVER, Problem1D, Problem3D
 
 G = 3
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+REF3D_CASES = ["ref3d_smooth_free_12", "ref3d_cubicsod_free_12", "ref3d_smooth_cons_ns_10"]
+
+
+def _grid3(pb):
+    xc = pb.left + (np.arange(pb.shape[0]) - G + 0.5) * pb.dx
+    yc = pb.down + (np.arange(pb.shape[1]) - G + 0.5) * pb.dy
+    zc = pb.back + (np.arange(pb.shape[2]) - G + 0.5) * pb.dz
+    return np.meshgrid(xc, yc, zc, indexing="ij")
+
+
+def _state3(rho, u, v, w, p, gamma=1.4):
+    return np.stack([rho, rho * u, rho * v, rho * w, p / (gamma - 1) + 0.5 * rho * (u * u + v * v + w * w)], -1)
+
+
+def ref3d_problem(name):
+    """The 3D cases the reference's own code is run on (free sides: the reference's only 3D
+    boundary), as (problem, convar, steps).
+      smooth_free   : a smooth seeded field, characteristic variables, Euler, 3 steps
+      cubicsod_free : CubicTube's box (src/3Dproblem.cpp:174-219), 1 step (with the pressure
+                      in the lambda slots the reference blows up in its second step)
+      smooth_cons_ns: the smooth field in conservative variables, NS collision time with
+                      Mu = 2e-3, 3 steps"""
+    n = int(name.rsplit("_", 1)[1])
+    kw = dict(nodex=n, nodey=n, nodez=n, ghost=G, bc=("free",) * 6, c1_euler=0.05, c2_euler=1.0)
+    if "cubicsod" in name:
+        pb = Problem3D(**kw)
+        X, Y, Z = _grid3(pb)
+        inside = (np.abs(X - 0.5) < 0.2) & (np.abs(Y - 0.5) < 0.2) & (np.abs(Z - 0.5) < 0.2)
+        zero = np.zeros(pb.shape)
+        return pb, _state3(np.where(inside, 1.0, 0.125), zero, zero, zero, np.where(inside, 1.0, 0.1)), 1
+    if "cons_ns" in name:
+        kw.update(characteristic=False, tau_type=1, mu=2e-3)
+    pb = Problem3D(**kw)
+    X, Y, Z = _grid3(pb)
+    k = 2 * np.pi
+    a = np.random.default_rng(n).uniform(-0.4, 0.4, 12)
+    rho = 1.0 + 0.2 * np.sin(k * X + a[0]) * np.cos(k * Y + a[1]) + 0.1 * np.sin(k * Z + a[2])
+    u = 0.3 * np.sin(k * Y + a[3])
+    v = 0.3 * np.sin(k * Z + a[5])
+    w = 0.3 * np.sin(k * X + a[7])
+    p = 1.0 + 0.2 * np.cos(k * (X + Y) + a[9])
+    return pb, _state3(rho, u, v, w, p), 3
+
+
+def _run_conventions(kind, pb, W, steps):
+    c = CpuStep3D(kind).init(pb)
+    if kind == "oracle":
+        c.fn("set_reference_conventions")(1)
+    c.set_state(W)
+    dts, states = [], []
+    for _ in range(steps):
+        dts.append(c.step())
+        states.append(c.state()["convar"])
+    return c, np.array(dts), states
+
+
+@pytest.mark.parametrize("name", REF3D_CASES)
+def test_3d_restatement_matches_reference_golden_bitwise(name):
+    """With the reference's conventions the restatement reproduces the reference's own 3D
+    functions' outputs (tests/golden/ref3d_*.npz, made by tests/golden/make_golden.py) bit for
+    bit: every time step and every interior state."""
+    pb, W, steps = ref3d_problem(name)
+    gold = np.load(GOLDEN / f"{name}.npz")
+    assert np.array_equal(W[G:-G, G:-G, G:-G], gold["convar0"][G:-G, G:-G, G:-G])
+    c, dts, states = _run_conventions("oracle", pb, gold["convar0"], steps)
+    assert np.array_equal(dts, gold["dts"])
+    for k, st in enumerate(states):
+        assert np.array_equal(st[G:-G, G:-G, G:-G], gold[f"convar{k + 1}"][G:-G, G:-G, G:-G]), k
+    c.fn("reduced_count").restype = ctypes.c_longlong
+    assert c.fn("reduced_count")() == 0   # no order reduction on the faces the fluxes use
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference checkout not present")
+def test_3d_restatement_matches_compiled_reference_bitwise():
+    pb, W, _ = ref3d_problem("ref3d_smooth_free_12")
+    _, da, sa = _run_conventions("ref", pb, W, 6)
+    _, db, sb = _run_conventions("oracle", pb, W, 6)
+    assert np.array_equal(da, db)
+    for a, b in zip(sa, sb):
+        assert np.array_equal(a[G:-G, G:-G, G:-G], b[G:-G, G:-G, G:-G])
+
+
+def test_3d_reference_conventions_differ_from_the_default():
+    """The two conventions are the only switch between the pinned and the default restatement;
+    with the pressure in the lambda slots the step is a different (wrong) one."""
+    pb, W, _ = ref3d_problem("ref3d_smooth_free_12")
+    _, _, sa = _run_conventions("oracle", pb, W, 1)
+    d = CpuStep3D("oracle").init(pb)
+    d.fn("set_reference_conventions")(0)
+    d.set_state(W)
+    d.step()
+    b = d.state()["convar"]
+    assert np.abs(sa[0] - b)[G:-G, G:-G, G:-G].max() > 1e-6
 
 
 def _sod_1d(n, c1, c2):

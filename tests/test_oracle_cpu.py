@@ -9,7 +9,8 @@ from hos_gb300 import cases
 from oracle_lib import CpuStep, interior, ref_available, rel_linf
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem)
+STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem
+              and not p.stem.startswith("ref3d"))
 
 
 def first_order_steps(name):
@@ -31,7 +32,7 @@ def _problem(name):
         seed = int(name.split("_")[2][1:])
         return cases.random_riemann2d(n, seed=seed, order=7)
     if name.startswith("vortex"):
-        return cases.isentropic_vortex(n, order=5)
+        return cases.isentropic_vortex(n, order=5, images=False)   # the fixture's initial data
     if name.startswith("sinwave"):
         return cases.sinwave2d(n, order=9)
     if name.startswith("fo_"):
@@ -40,6 +41,35 @@ def _problem(name):
         _, w, bc, _ = name.split("_")
         pb, con, prim = cases.random_riemann2d(n, seed=int(w[1]), order=int(w[1]))
         pb.bc = (bc,) * 4
+        return pb, con, prim
+    if name.startswith("nodf_"):
+        # nodf_w5_<wenotype>_<bc>_<n>: seeded random quadrants with the drivers' default slots
+        # WENO5_AO_normal / WENO5_AO_tangent (is_using_df_factor = false): non-DF WENO5-AO with
+        # Z-type ("z") or Jiang-Shu ("js") weights; "cons" runs conservative variables, periodic
+        _, _, wt, bc, _ = name.split("_")
+        pb, con, prim = cases.random_riemann2d(n, seed=50 + len(wt) + len(bc), order=5)
+        pb.use_df, pb.wenotype = False, {"z": "wenoz", "js": "wenojs"}[wt]
+        if bc == "cons":
+            pb.characteristic, bc = False, "periodic"
+        pb.bc = (bc,) * 4
+        return pb, con, prim
+    if name.startswith("lfns_"):
+        # lfns_w<order>_<variant>_<n>: LF2D with the Navier-Stokes collision time, i.e. with its
+        # viscous term NS_by_central_difference_prim_2D (src/flux_function.cpp:720-754)
+        #   mu    : Mu = 2e-3, Pr = 0.72, free sides
+        #   nu    : Nu = 1e-3 (Mu unset), Pr = 1, periodic
+        #   walls : Mu = 1e-2, no-slip walls moving at the bcprim velocities (the dt cap decides)
+        _, w, variant, _ = name.split("_")
+        order = int(w[1])
+        pb, con, prim = cases.random_riemann2d(n, seed=30 + order, order=order)
+        pb.flux, pb.tau_type = "LF", 1
+        if variant == "mu":
+            pb.mu, pb.prandtl = 2e-3, 0.72
+        elif variant == "nu":
+            pb.mu, pb.nu, pb.bc = -1.0, 1e-3, ("periodic",) * 4
+        else:
+            pb.mu, pb.bc = 1e-2, ("noslip",) * 4
+            pb.bc_prim = ((0.0, 0.0, 0.2, 0.0), (0.0, 0.0, -0.1, 0.0), (0.0, 0.3, 0.0, 0.0), (0.0, -0.25, 0.0, 0.0))
         return pb, con, prim
     if name.startswith("rt_"):
         # rt_w5_<nodex>: the RT_instability set-up, first-order step 0, gravity source
@@ -104,13 +134,19 @@ def test_oracle_matches_golden_bitwise(name):
 
 
 @pytest.mark.skipif(not ref_available(), reason="reference checkout not present")
-@pytest.mark.parametrize("order,charac,bc", [
-    (5, True, "free"), (7, True, "free"), (9, True, "free"), (9, False, "free"),
-    (7, True, "reflect"), (5, False, "periodic"), (7, True, "inflow"),
+@pytest.mark.parametrize("order,charac,bc,wenotype", [
+    (5, True, "free", None), (7, True, "free", None), (9, True, "free", None), (9, False, "free", None),
+    (7, True, "reflect", None), (5, False, "periodic", None), (7, True, "inflow", None),
+    (5, True, "free", "wenoz"), (5, True, "reflect", "wenojs"), (5, False, "periodic", "wenoz"),
+    (5, False, "free", "wenojs"),
 ])
-def test_oracle_matches_reference_bitwise(order, charac, bc):
+def test_oracle_matches_reference_bitwise(order, charac, bc, wenotype):
+    """The restatement equals the compiled reference bit for bit; a wenotype selects the
+    reference's default non-DF WENO5-AO slots (is_using_df_factor = false)."""
     pb, con, prim = cases.random_riemann2d(18, seed=order * 10 + len(bc), order=order)
     pb.characteristic = charac
+    if wenotype:
+        pb.use_df, pb.wenotype = False, wenotype
     if bc == "inflow":
         pb.bc = ("inflow", "free", "reflect", "free")
         pb.bc_prim = ((1.2, 0.8, 0.1, 1.1), (0,) * 4, (0,) * 4, (0,) * 4)
@@ -131,6 +167,38 @@ def test_oracle_matches_reference_bitwise(order, charac, bc):
         g = pb.ghost
         sl = (slice(g, g + pb.nodex), slice(g, g + pb.nodey))
         assert np.array_equal(ga[sl], gb[sl])
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference checkout not present")
+@pytest.mark.parametrize("name", ["lfns_w5_mu_18", "lfns_w7_nu_18", "lfns_w9_walls_18"])
+def test_oracle_lf_viscous_term_matches_reference_bitwise(name):
+    """LF2D + NS_by_central_difference_prim_2D against the reference run by the harness, which
+    fills the centre states the reference computes only for GKS2D."""
+    pb, con, prim = _problem(name)
+    a = CpuStep("ref").init(pb)
+    b = CpuStep("oracle").init(pb)
+    a.set_state(con, prim)
+    b.set_state(con, prim)
+    for _ in range(4):
+        assert a.step() == b.step()
+    sa, sb = a.state(), b.state()
+    assert np.array_equal(interior(pb, sa["convar"]), interior(pb, sb["convar"]))
+    assert np.array_equal(sa["alpha_x"], sb["alpha_x"])
+
+
+def test_oracle_lf_viscous_term_acts():
+    """The viscous term changes the LF2D step of a smooth flow (it is not silently dropped)."""
+    pb, con, prim = cases.isentropic_vortex(24, order=5)
+    pb.flux, pb.mu = "LF", 1e-2
+    out = []
+    for tau in (0, 1):
+        pb.tau_type = tau
+        o = CpuStep("oracle").init(pb)
+        o.set_state(con, prim)
+        for _ in range(3):
+            o.step()
+        out.append(o.state()["convar"])
+    assert rel_linf(out[1], out[0], pb) > 1e-5
 
 
 def _sinwave_errors(n):

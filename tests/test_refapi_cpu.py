@@ -89,7 +89,8 @@ def test_driver_reports_a_missing_gpu_as_the_reference_api_error(tmp_path):
 
 
 @pytest.mark.parametrize("name", ["refapi_riemann_w7_24", "refapi_rt_w5_12", "refapi_fo_w9_reflect_20",
-                                  "refapi_ns_noslip_w5_20", "refapi_inflow_reflect_w5_20", "refapi_vortex_w9_20"])
+                                  "refapi_ns_noslip_w5_20", "refapi_inflow_reflect_w5_20", "refapi_vortex_w9_20",
+                                  "refapi_nodf_riemann_w5_20", "refapi_nodf_js_periodic_w5_20"])
 def test_refapi_fixture_equals_the_oracle(name):
     """The reference run of the same driver loop equals the oracle bit for bit."""
     from oracle_lib import CpuStep
