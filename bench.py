@@ -65,7 +65,6 @@ TRAFFIC_PER_FACE_POINT3 = 289.0
 # flop per face and DRAM bytes per face
 GATED_FLOP_PER_FACE_POINT3 = 17440.0
 GATED_TRAFFIC_PER_FACE_POINT3 = 290.0
-ACC_STEPS = 200   # steps of the 512^2 runs whose density deviation the line states
 
 
 def parse():
@@ -77,6 +76,11 @@ def parse():
     ap.add_argument("--n", type=int, default=N_CELLS, help=argparse.SUPPRESS)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched sweep")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D Taylor-Green leg")
+    ap.add_argument("--no-endtime", action="store_true", help="skip the 1024^2 end-time accuracy leg")
+    ap.add_argument("--endtime", action="store_true",
+                    help="accuracy studies at the end times instead of the bench line: 1024^2 Riemann to "
+                         "t = 0.25 and 64^3 Taylor-Green to t = 10 (FP64, FP32 bulk, gated FP32)")
+    ap.add_argument("--endtime-256", action="store_true", help="with --endtime: also gated FP32 256^3 to t = 10")
     ap.add_argument("--case", choices=["gated256", "gated1024", "tgv3d64"], default=None,
                     help="small profiling case: gated256 = gate trained as in the bench, then 21 plain FP32 "
                          "and 21 gated FP32 steps of the 256^2 WENO7 Riemann problem; gated1024 = the same "
@@ -245,6 +249,13 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
     e0 = torch.cuda.Event(enable_timing=True)
     e0.record(ext)
     evs = []
+    # the drivers' first-order step 0 (e.g. src/2Dproblem.cpp:940-945), then WENO5-AO-DF
+    b.set_reconstruction(True)
+    b.advance(1, graph=True)
+    ev = torch.cuda.Event(enable_timing=True)
+    ev.record(ext)
+    evs.append(ev)
+    b.set_reconstruction(False)
     while len(evs) < max_steps:
         for _ in range(25):
             b.advance(1, graph=True)
@@ -262,8 +273,11 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
     tts = np.array([e0.elapsed_time(evs[int(n) - 1]) / 1e3 for n in nsteps])
     done = ~failed
     total = e0.elapsed_time(evs[int(nsteps.max()) - 1]) / 1e3
+    # the aggregate counts the steps of the problems that reached their end time only
     return {"problems": count, "seed": seed, "cells": int(cells.sum()),
-            "value": float((cells * nsteps).sum() / total), "unit": "cell-updates/s",
+            "value": float((cells * nsteps)[done].sum() / total), "unit": "cell-updates/s",
+            "value_over": "cell updates of the problems that reached their end time / wall time of the batch",
+            "first_order_step0": True,
             "wall_s": total, "batch_steps": int(nsteps.max()), "unfinished": int(act),
             "blown_up": int(failed.sum()),
             "blown_up_problems": [sweep[k][4] for k in np.flatnonzero(failed)],
@@ -279,6 +293,157 @@ def batch_leg(dev, precision, count=64, seed=0, max_steps=4000, gate=None, thres
                 "linear_path_fraction": (gst["smooth_x"] + gst["smooth_y"]) / max(1, gst["cells_x"] + gst["cells_y"]),
                 "audited": gst["audited"], "audit_false_negative_rate": gst["false_neg"] / max(1, gst["audited"]),
                 "aposteriori_rejections": gst["fallback"]}}
+
+
+def endtime2d_leg(gate, rep, n=N_CELLS, tstop=0.25):
+    """The four-quadrant Riemann problem at n^2 (WENO7-AO-DF, characteristic, 3 Gauss points) run
+    to its end time t = 0.25 in plain FP64, plain FP32 bulk and gated FP32 from the same initial
+    data: density deviation of each FP32 form from FP64 at t = 0.25 (relative L1 and L-inf over
+    the interior cells), steps taken, and the gate's activity over the whole gated run (linear-path
+    fraction, audits, false negatives among the audited, a-posteriori rejections).  Steps are
+    graph replays; the time step is the solver's own CFL, clipped to the end time."""
+    from hos_gb300 import cases
+    from hos_gb300.solver import FP32, FP64, Solver2D
+
+    pb, con, prim = cases.riemann2d(n, order=ORDER)
+    g = pb.ghost
+    rho, runs = {}, {}
+    for name, prec, gated in (("fp64", FP64, False), ("fp32", FP32, False), ("gated", FP32, True)):
+        s = Solver2D(pb, prec)
+        s.set_state(con, prim)
+        if gated:
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+            s.gate_stats(reset=True)
+        t0 = time.perf_counter()
+        steps = 0
+        t, _ = s.sync()
+        while t < tstop:
+            s.advance(1, tstop, graph=True)
+            steps += 1
+            if steps % 16 == 0 or steps > 1000:
+                t, _ = s.sync()
+        t, _ = s.sync()
+        wall = time.perf_counter() - t0
+        rho[name] = s.get_state()["convar"][g:-g, g:-g, 0]
+        runs[name] = {"steps": steps, "t": t, "wall_s": wall}
+        if gated:
+            st = s.gate_stats()
+            cells = max(1, st["cells_x"] + st["cells_y"])
+            runs[name]["gate"] = {"linear_path_fraction": (st["smooth_x"] + st["smooth_y"]) / cells,
+                                  "audited": st["audited"], "audit_false_negatives": st["false_neg"],
+                                  "audit_false_negative_rate": st["false_neg"] / max(1, st["audited"]),
+                                  "aposteriori_rejections": st["fallback"]}
+        s.close()
+
+    def rel(a, b, norm):
+        d = np.abs(a - b)
+        return float(d.mean() / np.abs(b).mean()) if norm == 1 else float(d.max() / np.abs(b).max())
+
+    return {"grid": f"{n}x{n}", "t_end": tstop, "runs": runs,
+            "rho_rel_l1_gated_vs_fp64": rel(rho["gated"], rho["fp64"], 1),
+            "rho_rel_linf_gated_vs_fp64": rel(rho["gated"], rho["fp64"], 0),
+            "rho_rel_l1_fp32_vs_fp64": rel(rho["fp32"], rho["fp64"], 1),
+            "rho_rel_linf_fp32_vs_fp64": rel(rho["fp32"], rho["fp64"], 0),
+            "rho_rel_l1_gated_vs_fp32": rel(rho["gated"], rho["fp32"], 1),
+            "cells_off_by_1e-2_gated": float((np.abs(rho["gated"] - rho["fp64"]) > 1e-2 * np.abs(rho["fp64"])).mean()),
+            "target": "rho_rel_l1_gated_vs_fp64 <= 1e-3"}
+
+
+def endtime3d_leg(gate, rep, n=64, tstop=10.0, every=0.25, forms=("fp64", "fp32", "gated")):
+    """The Taylor-Green vortex at n^3 (Re 1600, Mach 0.1, Pr 0.71; WENO5-AO, GKS3D with the
+    Navier-Stokes collision time, S2O4) run to t = 10 in each form from the same initial data,
+    stopping at the same checkpoints every ``every`` time units (the last step before each
+    checkpoint is clipped to it, as the end time is): kinetic energy <rho |u|^2 / 2> at every
+    checkpoint, the dissipation rate -dKE/dt from central differences of those, their largest
+    deviation from FP64 (KE relative to the initial KE, the rate relative to FP64's peak rate),
+    density deviation at t = 10, and the gate's activity per checkpoint interval."""
+    from hos_gb300 import cases
+    from hos_gb300.solver import FP32, FP64, Solver3D
+
+    pb, con = cases.tgv3d(n)
+    g = pb.ghost
+    marks = np.round(np.arange(every, tstop + 0.5 * every, every), 10)
+    ke, rho, runs = {}, {}, {}
+    for name in forms:
+        prec = FP64 if name == "fp64" else FP32
+        s = Solver3D(pb, prec)
+        s.set_state(con)
+        if name == "gated":
+            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+            s.gate_stats(reset=True)
+        kk, acts = [], []
+        t0 = time.perf_counter()
+        steps = 0
+
+        def energy():
+            st = s.get_state()["convar"][g:-g, g:-g, g:-g]
+            return 0.5 * float(((st[..., 1] ** 2 + st[..., 2] ** 2 + st[..., 3] ** 2) / st[..., 0]).mean()), st
+
+        kk.append(energy()[0])
+        for tm in marks:
+            steps += s.run(float(tm), check_every=20)
+            e, st = energy()
+            kk.append(e)
+            if name == "gated":
+                gs = s.gate_stats(reset=True)
+                cells = max(1, gs["cells_x"] + gs["cells_y"] + gs["cells_z"])
+                acts.append({"t": float(tm),
+                             "linear_fraction": (gs["smooth_x"] + gs["smooth_y"] + gs["smooth_z"]) / cells,
+                             "audited": gs["audited"], "false_neg": gs["false_neg"], "fallback": gs["fallback"]})
+        runs[name] = {"steps_upper_bound": steps, "wall_s": time.perf_counter() - t0, "t": s.sync()[0]}
+        if acts:
+            runs[name]["gate_by_interval"] = acts
+        rho[name] = st[..., 0].copy()
+        ke[name] = np.array(kk)
+        s.close()
+    tt = np.concatenate([[0.0], marks])
+    out = {"grid": f"{n}^3", "t_end": tstop, "checkpoint_every": every, "runs": runs,
+           "t": tt.tolist(), "kinetic_energy": {k: v.tolist() for k, v in ke.items()}}
+    eps = {k: (-(v[2:] - v[:-2]) / (tt[2:] - tt[:-2])) for k, v in ke.items()}
+    out["dissipation_rate"] = {k: v.tolist() for k, v in eps.items()}
+    out["dissipation_rate_t"] = tt[1:-1].tolist()
+    if "fp64" in ke:
+        for k in ke:
+            if k == "fp64":
+                continue
+            out[f"kinetic_energy_rel_dev_max_{k}"] = float(np.abs(ke[k] - ke["fp64"]).max() / ke["fp64"][0])
+            out[f"dissipation_rate_rel_dev_max_{k}"] = float(np.abs(eps[k] - eps["fp64"]).max()
+                                                             / np.abs(eps["fp64"]).max())
+            out[f"rho_rel_l1_{k}_vs_fp64"] = float(np.abs(rho[k] - rho["fp64"]).mean() / np.abs(rho["fp64"]).mean())
+        out["dissipation_peak_fp64"] = {"t": float(out["dissipation_rate_t"][int(np.argmax(eps["fp64"]))]),
+                                        "rate": float(eps["fp64"].max())}
+    return out
+
+
+def endtime_main(args):
+    """--endtime: the accuracy studies at the configurations' end times, one JSON line: the 2D
+    Riemann problem at 1024^2 to t = 0.25 and the Taylor-Green vortex at 64^3 to t = 10 (FP64,
+    FP32 bulk, gated FP32), then gated FP32 alone at 256^3 to t = 10 for its throughput and
+    kinetic-energy curve."""
+    import torch
+
+    from hos_gb300 import gate_train
+
+    torch.cuda.set_device(0)
+    out = {"mode": "endtime"}
+    t0 = time.perf_counter()
+    gate, rep = gate_train.train(order=ORDER, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
+                                 train_steps=3000, batch=4096)
+    out["gate2d"] = {"train_s": time.perf_counter() - t0, "threshold": rep.threshold, "heldout": rep.heldout}
+    out["riemann2d"] = endtime2d_leg(gate, rep)
+    print(json.dumps({"riemann2d": out["riemann2d"]}), flush=True)
+    gate.close()
+    t0 = time.perf_counter()
+    gate3, rep3 = gate_train.train3d()
+    out["gate3d"] = {"train_s": time.perf_counter() - t0, "threshold": rep3.threshold, "heldout": rep3.heldout}
+    out["tgv3d_64"] = endtime3d_leg(gate3, rep3, n=64)
+    print(json.dumps({"tgv3d_64": out["tgv3d_64"]}), flush=True)
+    if args.endtime_256:
+        out["tgv3d_256_gated"] = endtime3d_leg(gate3, rep3, n=256, every=0.5, forms=("gated",))
+        r = out["tgv3d_256_gated"]["runs"]["gated"]
+        r["cell_updates_per_s_upper_bound"] = 256 ** 3 * r["steps_upper_bound"] / r["wall_s"]
+    gate3.close()
+    print(json.dumps(out), flush=True)
 
 
 def vortex_leg(sizes=(50, 100, 200, 400)):
@@ -574,6 +739,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.endtime:
+        endtime_main(args)
+        return
     if args.case == "gated256":
         profile_case()
         return
@@ -660,17 +828,8 @@ def main():
     s64.close()
     s32.close()
 
-    # deviation once the solution has structure: 512^2, 200 steps of each form from the same data
-    pa, ca, pra = cases.riemann2d(512, order=ORDER)
-    long_rho = {}
-    for name, prec, gated in (("fp64", FP64, False), ("fp32", FP32, False), ("gated", FP32, True)):
-        s = Solver2D(pa, prec)
-        s.set_state(ca, pra)
-        if gated:
-            s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
-        s.advance(ACC_STEPS, 1e30, graph=True)
-        long_rho[name] = s.get_state()["convar"][g:-g, g:-g, 0]
-        s.close()
+    # deviation at the configuration's end time: every form run to t = 0.25 from the same data
+    end_time = endtime2d_leg(gate, rep, n=n) if not args.no_endtime else None
 
     def dev_l1(a, b):
         return float(np.abs(a - b).mean() / np.abs(b).mean())
@@ -752,10 +911,7 @@ def main():
                      "rho_rel_linf_gated_vs_fp64": dev_linf(rho_g, rho_64),
                      "rho_rel_l1_fp32_vs_fp64": dev_l1(rho_32, rho_64),
                      "rho_rel_l1_gated_vs_fp32": dev_l1(rho_g, rho_32),
-                     "developed": {"grid": "512x512", "steps": ACC_STEPS,
-                                   "rho_rel_l1_gated_vs_fp64": dev_l1(long_rho["gated"], long_rho["fp64"]),
-                                   "rho_rel_linf_gated_vs_fp64": dev_linf(long_rho["gated"], long_rho["fp64"]),
-                                   "rho_rel_l1_fp32_vs_fp64": dev_l1(long_rho["fp32"], long_rho["fp64"])}},
+                     "end_time": end_time},
         "gate": {"train_s": train_s, "samples": rep.samples, "smooth_label_fraction": rep.smooth_fraction,
                  "threshold": rep.threshold, "heldout": rep.heldout,
                  "linear_path_fraction": smooth, "audited": gstats["audited"],

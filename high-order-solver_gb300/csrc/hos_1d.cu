@@ -33,6 +33,7 @@ struct Ctl {
 
 struct Geo {
     int nx, g, nodex, order, characteristic, df_mode, update_alpha;
+    int wenotype;   // weights of the non-DF WENO5-AO steps (HOS_WENO_*)
     double dx, cfl, gamma, K, c1, c2;
     int bc[2];
 };
@@ -83,33 +84,7 @@ template <class T> struct Char1 {
     }
 };
 
-// non-DF WENO5-AO weights: Z-type, epsilon 1e-10, full 5th-order smoothness indicator
-template <class T>
-__device__ __forceinline__ void weights5_plain(const T* s, T* fw) {
-    constexpr double dhi = 0.85, dlo = 0.85;
-    const double dd[4] = {(1.0 - dhi) * (1.0 - dlo) / 2.0, (1.0 - dhi) * dlo, (1.0 - dhi) * (1.0 - dlo) / 2.0, dhi};
-    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
-    T beta[4];
-    beta3<T>(s, beta);
-    beta[3] = T(1.0 / 5040.0) * (T(231153.0) * w0 * w0 + T(104963.0) * wn1 * wn1 + T(6908.0) * wn2 * wn2 -
-                                 T(38947.0) * wn2 * wp1 + T(104963.0) * wp1 * wp1 +
-                                 wn1 * (T(-51001.0) * wn2 + T(179098.0) * wp1 - T(38947.0) * wp2) -
-                                 T(3.0) * w0 * (T(99692.0) * wn1 - T(22641.0) * wn2 + T(99692.0) * wp1 - T(22641.0) * wp2) +
-                                 T(8209.0) * wn2 * wp2 - T(51001.0) * wp1 * wp2 + T(6908.0) * wp2 * wp2);
-    const T tau = T(1.0 / 3.0) * (fabsT(beta[3] - beta[0]) + fabsT(beta[3] - beta[1]) + fabsT(beta[3] - beta[2]));
-    T alpha[4], sum = T(0);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const T gd = tau / (beta[k] + T(1e-10));
-        alpha[k] = T(dd[k]) * (T(1) + gd * gd);
-        sum += alpha[k];
-    }
-    const T inv = T(1.0) / sum;
-    const T wt = alpha[3] * inv * T(1.0 / dd[3]);
-    fw[3] = wt;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) fw[k] = alpha[k] * inv - wt * T(dd[k]);
-}
+// non-DF WENO5-AO weights: weights5 (hos_weno.cuh), epsilon 1e-10, the wenotype weights
 
 // 1D Maxwellian moments (MMDF1d); entries (i, k) = moment_i * xi_k, i <= 6, k <= 2
 template <class T> struct Mom1 {
@@ -353,7 +328,7 @@ __global__ void __launch_bounds__(TILE) face1d_kernel(FaceArgs1 a, Geo geo) {
                 T s[N], fw[NW], p[NW], px[NW];
 #pragma unroll
                 for (int q = 0; q < N; ++q) s[q] = ch[sd][q][v];
-                if (ORDER == 5 && !df) weights5_plain<T>(s, fw);
+                if (ORDER == 5 && !df) weights5<T>(s, T(1e-10), fw, geo.wenotype);
                 else ao_weights<T, ORDER>(s, fw);
                 if (sd == 0) normal_face<T, ORDER, 0>(s, dfa, ih, p, px);
                 else normal_face<T, ORDER, 1>(s, dfa, ih, p, px);
@@ -591,6 +566,7 @@ int hos1d_create(const hos_params1d* params, int precision, hos_solver1d** out) 
     if (!(p.order == 5 || p.order == 7 || p.order == 9)) return fail1(HOS_E_CONFIG, "order must be 5, 7 or 9");
     if (p.df_mode != 1 && p.order != 5) return fail1(HOS_E_CONFIG, "the non-DF variant exists for WENO5 only");
     if (p.df_mode < 0 || p.df_mode > 2) return fail1(HOS_E_CONFIG, "bad df_mode");
+    if (p.wenotype < HOS_WENO_Z || p.wenotype > HOS_WENO_LINEAR) return fail1(HOS_E_CONFIG, "bad wenotype");
     if (p.ghost < p.order / 2 + 1 || p.nodex < p.ghost) return fail1(HOS_E_CONFIG, "ghost/nodex too small");
     if (p.ghost > 16) return fail1(HOS_E_CONFIG, "ghost must be <= 16");  // one warp fills both ends
     if (int st = check_bc1(p.bc)) return st;
@@ -607,6 +583,7 @@ int hos1d_create(const hos_params1d* params, int precision, hos_solver1d** out) 
     geo.characteristic = p.characteristic ? 1 : 0;
     geo.df_mode = p.df_mode;
     geo.update_alpha = p.update_alpha ? 1 : 0;
+    geo.wenotype = p.wenotype;
     geo.dx = (p.right - p.left) / p.nodex;
     geo.cfl = p.cfl;
     geo.gamma = p.gamma;

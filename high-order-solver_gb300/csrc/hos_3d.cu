@@ -401,6 +401,8 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
     if (p.tau_type != 0 && p.tau_type != 1) return fail3(HOS_E_CONFIG, "tau_type must be 0 (Euler) or 1 (NS)");
     if (p.prandtl_fix && !(p.prandtl > 0)) return fail3(HOS_E_CONFIG, "the Prandtl fix needs prandtl > 0");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail3(HOS_E_CONFIG, "bad precision");
+    if (p.gks3d_pressure_slot && (precision != HOS_FP64 || p.prandtl_fix))
+        return fail3(HOS_E_CONFIG, "the reference's GKS3D pressure convention runs in FP64 without the Prandtl fix");
     hos_solver3d* s = new (std::nothrow) hos_solver3d();
     if (!s) return fail3(HOS_E_NOMEM, "host allocation");
     s->p = p;
@@ -417,6 +419,7 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
     g.dy = (p.up - p.down) / p.nodey;
     g.dz = (p.front - p.back) / p.nodez;
     g.prandtl_coef = p.prandtl_fix ? 1.0 / p.prandtl - 1.0 : 0.0;
+    g.p_slot = p.gks3d_pressure_slot ? 1 : 0;
     g.idx = 1.0 / g.dx;
     g.idy = 1.0 / g.dy;
     g.idz = 1.0 / g.dz;

@@ -41,6 +41,7 @@ struct Geo3 {
     double prandtl_coef;    // 1 / Pr - 1 with the Prandtl fix, else 0
     int tau_type, characteristic;
     int bc[6];
+    int p_slot;   // FP64: the reference's GKS3D convention, pressure where lambda belongs
 };
 
 // index space of one per-direction array: extents (NA, NB, NC), k-aligned axis fastest
@@ -155,108 +156,7 @@ struct Char5 {
     }
 };
 
-// ---- WENO5-AO, non-DF (src/reconstruction.cpp:161-360, 2393-2551) -------------------------
-template <class T>
-__device__ __forceinline__ T beta5_big(T wn2, T wn1, T w0, T wp1, T wp2) {
-    return T(1.0 / 5040.0) * (T(231153) * w0 * w0 + T(104963) * wn1 * wn1 + T(6908) * wn2 * wn2 -
-                              T(38947) * wn2 * wp1 + T(104963) * wp1 * wp1 +
-                              wn1 * (T(-51001) * wn2 + T(179098) * wp1 - T(38947) * wp2) -
-                              T(3) * w0 * (T(99692) * wn1 - T(22641) * wn2 + T(99692) * wp1 - T(22641) * wp2) +
-                              T(8209) * wn2 * wp2 - T(51001) * wp1 * wp2 + T(6908) * wp2 * wp2);
-}
-// final AO weights (linear weights d = {0.01125, 0.1275, 0.01125, 0.85} from dhi = dlo = 0.85)
-template <class T>
-__device__ __forceinline__ void weights5(const T* s, T eps, T* fw) {
-    const T d0 = T(0.5) * T(0.15) * T(0.15), d1 = T(0.15) * T(0.85), d3 = T(0.85);
-    T b[4];
-    beta3<T>(s, b);
-    if constexpr (sizeof(T) == 4) {
-        // the big-stencil indicator expands into terms ~1e5 w^2 that cancel; it depends on
-        // differences only, so FP32 evaluates it about the centre value
-        b[3] = beta5_big(s[0] - s[2], s[1] - s[2], T(0), s[3] - s[2], s[4] - s[2]);
-    } else {
-        b[3] = beta5_big(s[0], s[1], s[2], s[3], s[4]);
-    }
-    const T tau = T(1.0 / 3.0) * (fabsT(b[3] - b[0]) + fabsT(b[3] - b[1]) + fabsT(b[3] - b[2]));
-    T al[4];
-    const T dd[4] = {d0, d1, d0, d3};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const T q = tau / (b[k] + eps);
-        al[k] = dd[k] * (T(1) + q * q);
-    }
-    const T isum = T(1) / (al[0] + al[1] + al[2] + al[3]);
-    const T w3 = al[3] * isum;
-    fw[3] = w3 / d3;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) fw[k] = al[k] * isum - fw[3] * dd[k];
-}
-// value and slope at the left (side 0) or right (side 1) face of the centre cell, epsilon 1e-10
-template <class T>
-__device__ __forceinline__ void weno5_face(int side, const T* s, T ih, T& var, T& der) {
-    T fw[4];
-    weights5<T>(s, T(1e-10), fw);
-    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
-    T p[4], px[4];
-    if (side == 0) {
-        p[0] = T(-1.0 / 6.0) * wn2 + T(5.0 / 6.0) * wn1 + T(1.0 / 3.0) * w0;
-        p[1] = T(1.0 / 3.0) * wn1 + T(5.0 / 6.0) * w0 - T(1.0 / 6.0) * wp1;
-        p[2] = T(11.0 / 6.0) * w0 - T(7.0 / 6.0) * wp1 + T(1.0 / 3.0) * wp2;
-        p[3] = T(1.0 / 60.0) * (T(47) * w0 + T(27) * wn1 - T(3) * wn2 - T(13) * wp1 + T(2) * wp2);
-        px[0] = (w0 - wn1) * ih;
-        px[1] = px[0];
-        px[2] = -(T(2) * w0 - T(3) * wp1 + wp2) * ih;
-        px[3] = (T(15) * w0 - T(15) * wn1 + wn2 - wp1) * (T(1.0 / 12.0) * ih);
-    } else {
-        p[0] = T(1.0 / 3.0) * wn2 - T(7.0 / 6.0) * wn1 + T(11.0 / 6.0) * w0;
-        p[1] = T(-1.0 / 6.0) * wn1 + T(5.0 / 6.0) * w0 + T(1.0 / 3.0) * wp1;
-        p[2] = T(1.0 / 3.0) * w0 + T(5.0 / 6.0) * wp1 - T(1.0 / 6.0) * wp2;
-        p[3] = T(1.0 / 60.0) * (T(47) * w0 - T(13) * wn1 + T(2) * wn2 + T(27) * wp1 - T(3) * wp2);
-        px[0] = (T(2) * w0 - T(3) * wn1 + wn2) * ih;
-        px[1] = (wp1 - w0) * ih;
-        px[2] = px[1];
-        px[3] = (T(-15) * w0 + wn1 + T(15) * wp1 - wp2) * (T(1.0 / 12.0) * ih);
-    }
-    var = fw[0] * p[0] + fw[1] * p[1] + fw[2] * p[2] + fw[3] * p[3];
-    der = fw[0] * px[0] + fw[1] * px[1] + fw[2] * px[2] + fw[3] * px[3];
-}
-// values (and slopes when DER) at the Gauss points -h/(2 sqrt 3) (g0) and +h/(2 sqrt 3) (g1)
-// of the centre cell, epsilon 1e-6 (weno_5th_ao_2gauss)
-template <class T, bool DER>
-__device__ __forceinline__ void weno5_2g(const T* s, T ih, T* g, T* gx) {
-    T fw[4];
-    weights5<T>(s, T(1e-6), fw);
-    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
-    const T r3 = T(1.732050807568877294), i4r3 = T(1) / (T(4) * r3);
-    // candidate polynomials at g0; g1 is their mirror image
-    T p0 = w0 - r3 * w0 * T(0.25) + (T(4) * wn1 - wn2) * i4r3;
-    T p1 = w0 + (wn1 - wp1) * i4r3;
-    T p2 = T(1.0 / 12.0) * (T(3) * (T(4) + r3) * w0 + r3 * (T(-4) * wp1 + wp2));
-    T p3 = (T(4314) * w0 + (T(4) + T(500) * r3) * wn1 - wn2 - T(70) * r3 * wn2 + T(4) * wp1 - T(500) * r3 * wp1 - wp2
-            + T(70) * r3 * wp2) * T(1.0 / 4320.0);
-    g[0] = fw[0] * p0 + fw[1] * p1 + fw[2] * p2 + fw[3] * p3;
-    p0 = T(1.0 / 12.0) * (T(3) * (T(4) + r3) * w0 + r3 * (T(-4) * wn1 + wn2));
-    p1 = w0 + (wp1 - wn1) * i4r3;
-    p2 = w0 - r3 * w0 * T(0.25) + (T(4) * wp1 - wp2) * i4r3;
-    p3 = (T(4314) * w0 + (T(4) - T(500) * r3) * wn1 - wn2 + T(70) * r3 * wn2 + T(4) * wp1 + T(500) * r3 * wp1 - wp2
-          - T(70) * r3 * wp2) * T(1.0 / 4320.0);
-    g[1] = fw[0] * p0 + fw[1] * p1 + fw[2] * p2 + fw[3] * p3;
-    if (DER) {
-        const T i6h = ih * T(1.0 / 6.0), i108h = ih * T(1.0 / 108.0);
-        T q0 = -((r3 - T(9)) * w0 - T(2) * (r3 - T(6)) * wn1 + (r3 - T(3)) * wn2) * i6h;
-        T q1 = -(T(-2) * r3 * w0 + (T(3) + r3) * wn1 + (r3 - T(3)) * wp1) * i6h;
-        T q2 = -((T(9) + r3) * w0 - T(2) * (T(6) + r3) * wp1 + (T(3) + r3) * wp2) * i6h;
-        T q3 = (T(48) * r3 * w0 - T(72) * wn1 - T(26) * r3 * wn1 + T(9) * wn2 + T(2) * r3 * wn2 + T(72) * wp1
-                - T(26) * r3 * wp1 - T(9) * wp2 + T(2) * r3 * wp2) * i108h;
-        gx[0] = fw[0] * q0 + fw[1] * q1 + fw[2] * q2 + fw[3] * q3;
-        q0 = ((T(9) + r3) * w0 - T(2) * (T(6) + r3) * wn1 + (T(3) + r3) * wn2) * i6h;
-        q1 = (T(-2) * r3 * w0 + (r3 - T(3)) * wn1 + (T(3) + r3) * wp1) * i6h;
-        q2 = ((r3 - T(9)) * w0 - T(2) * (r3 - T(6)) * wp1 + (r3 - T(3)) * wp2) * i6h;
-        q3 = -(T(48) * r3 * w0 + T(72) * wn1 - T(26) * r3 * wn1 - T(9) * wn2 + T(2) * r3 * wn2 - T(72) * wp1
-               - T(26) * r3 * wp1 + T(9) * wp2 + T(2) * r3 * wp2) * i108h;
-        gx[1] = fw[0] * q0 + fw[1] * q1 + fw[2] * q2 + fw[3] * q3;
-    }
-}
+// non-DF WENO5-AO (weights5, weno5_face, weno5_2g): hos_weno.cuh
 
 // ---- GKS3D (src/flux_function.cpp:813-1103) ------------------------------------------------
 // Moments of one Maxwellian: whole-space <u^i> (u), one half-space (h: u>0 for the left
@@ -430,8 +330,16 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
                      T* df) {
     const T K = T(g.K);
     T pl[5], pr[5];
-    ulambda5<T>(pl, Lc, K);
-    ulambda5<T>(pr, Rc, K);
+    // the reference's GKS3D hands Convar_to_primvar_3D's pressure to every lambda slot
+    // (src/flux_function.cpp:831-836, 914); only the FP64 kernels carry that convention
+    const bool p_slot = sizeof(T) == 8 && g.p_slot;
+    if (p_slot) {
+        prim5<T>(pl, Lc, T(g.gamma));
+        prim5<T>(pr, Rc, T(g.gamma));
+    } else {
+        ulambda5<T>(pl, Lc, K);
+        ulambda5<T>(pr, Rc, K);
+    }
     Mom3<T> ml, mr;
     mom_whole<T>(ml, pl[1], pl[2], pl[3], pl[4], K);
     mom_half<T>(ml, pl[1], pl[4], T(1));
@@ -457,7 +365,8 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
         for (int v = 0; v < 5; ++v) d0[d][v] = pl[0] * a0l[v] + pr[0] * a0r[v];
     }
     T p0[5];
-    ulambda5<T>(p0, c0, K);
+    if (p_slot) prim5<T>(p0, c0, T(g.gamma));
+    else ulambda5<T>(p0, c0, K);
     const T tau = (g.tau_type != 0 && g.mu > 0) ? T(2) * T(g.mu) * p0[4] / p0[0] : T(0);
     T ta[6], tb[6];
     const T dt2 = T(0.5) * dt;

@@ -521,6 +521,19 @@ int hos_batch2d_status(hos_batch2d* b, int* active, double* t, int* last_step, i
     return failed ? HOS_OK : failb(HOS_E_BLOWUP, std::to_string(bad) + " problem(s) of the batch blew up");
 }
 
+int hos_batch2d_set_reconstruction(hos_batch2d* b, int mode) {
+    if (!b) return failb(HOS_E_ARG, "null batch");
+    if (mode != HOS_RECON_WENO && mode != HOS_RECON_FIRST_ORDER) return failb(HOS_E_ARG, "bad reconstruction mode");
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return failb(HOS_E_CUDA, "set_reconstruction");
+    for (auto& pr : b->host_probs) pr.geo.first_order = mode;
+    // the face tiles read each problem's geometry from the table when they run, so a captured
+    // step picks the change up without being captured again
+    e = cudaMemcpy(b->probs, b->host_probs.data(), b->count * sizeof(Prob), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return failb(HOS_E_CUDA, "problem table");
+    return HOS_OK;
+}
+
 int hos_batch2d_set_gate(hos_batch2d* b, const hos_gate* g, float threshold, int audit_log2) {
     using namespace gate;
     if (!b) return failb(HOS_E_ARG, "null batch");

@@ -6,7 +6,8 @@
 
 namespace hos {
 
-template <int ORDER>
+// PLAIN: the non-DF WENO5-AO kernels (ORDER 5; no gated form)
+template <int ORDER, bool PLAIN = false>
 struct FaceLaunch {
     // precision: 0 FP64, 1 FP32, 2 FP32 with the learned gate, 3 FP64 and 4 FP32 with the
     // Navier-Stokes collision time
@@ -20,7 +21,7 @@ struct FaceLaunch {
                 using TS = TmaTile<ORDER>;
                 using ST = FaceSmem<float, ORDER, TS>;
                 dim3 g((nodeT + TS::T - 1) / TS::T, (nodeN + 1 + TS::N - 1) / TS::N);
-                face_kernel_tma<ORDER, DIR, GATED, NS>
+                face_kernel_tma<ORDER, DIR, GATED, NS, PLAIN>
                     <<<g, FACE_THREADS, GATED ? ST::gated_bytes : ST::bytes, s>>>(a, geo, tm[DIR]);
                 return cudaGetLastError();
             }
@@ -28,7 +29,7 @@ struct FaceLaunch {
         using KT = KernelTile<ORDER>;
         dim3 grid((nodeT + KT::T - 1) / KT::T, (nodeN + 1 + KT::N - 1) / KT::N);
         const size_t smem = GATED ? S::gated_bytes : S::bytes;
-        face_kernel<T, ORDER, DIR, GATED, NS><<<grid, FACE_THREADS, smem, s>>>(a, geo);
+        face_kernel<T, ORDER, DIR, GATED, NS, PLAIN><<<grid, FACE_THREADS, smem, s>>>(a, geo);
         return cudaGetLastError();
     }
 
@@ -45,11 +46,11 @@ struct FaceLaunch {
     static cudaError_t configure_one() {
         using S = FaceSmem<T, ORDER, KernelTile<ORDER>>;
         const size_t smem = GATED ? S::gated_bytes : S::bytes;
-        cudaError_t e = attrs(face_kernel<T, ORDER, DIR, GATED, NS>, smem);
+        cudaError_t e = attrs(face_kernel<T, ORDER, DIR, GATED, NS, PLAIN>, smem);
         if constexpr (sizeof(T) == 4) {
             using ST = FaceSmem<float, ORDER, TmaTile<ORDER>>;
             if (e == cudaSuccess)
-                e = attrs(face_kernel_tma<ORDER, DIR, GATED, NS>, GATED ? ST::gated_bytes : ST::bytes);
+                e = attrs(face_kernel_tma<ORDER, DIR, GATED, NS, PLAIN>, GATED ? ST::gated_bytes : ST::bytes);
         }
         return e;
     }
@@ -64,7 +65,9 @@ struct FaceLaunch {
             case 1: return configure_pair<float, false>();
             case 3: return configure_pair<double, false, true>();
             case 4: return configure_pair<float, false, true>();
-            default: return configure_pair<float, true>();
+            default:
+                if constexpr (PLAIN) return cudaErrorInvalidValue;
+                else return configure_pair<float, true>();
         }
     }
 
@@ -85,7 +88,9 @@ struct FaceLaunch {
             case 1: return pair<float, false>(ax, ay, geo, s, ev, tm);
             case 3: return pair<double, false, true>(ax, ay, geo, s, ev, nullptr);
             case 4: return pair<float, false, true>(ax, ay, geo, s, ev, tm);
-            default: return pair<float, true>(ax, ay, geo, s, ev, tm);
+            default:
+                if constexpr (PLAIN) return cudaErrorInvalidValue;
+                else return pair<float, true>(ax, ay, geo, s, ev, tm);
         }
     }
 };

@@ -425,4 +425,60 @@ __device__ __forceinline__ void lf_point(const T* wl, const T* wr, T dt, T gamma
     for (int m = 0; m < 4; ++m) f[m] = dt * (T(0.5) * ((fl[m] + fr[m]) - beta * (wr[m] - wl[m])));
 }
 
+
+// Centre (g0) state of a Gauss point and its x / y slopes (Center_all_collision_2d_multi,
+// src/reconstruction.cpp:3652-3687): the collision of the left and right Maxwellians' half
+// spaces and the half-space moments of their micro-slopes, in conserved variables.
+template <class T>
+__device__ __forceinline__ void centre_state(const GState<T>& L, const GState<T>& R, T K, T* w0, T* c0x, T* c0y) {
+    const GasK<T> gk(K);
+    T pl[4], pr[4];
+    to_ulambda(pl, L.w, K);
+    to_ulambda(pr, R.w, K);
+    Mom<T> ml, mr;
+    ml.init_half(pl[1], pl[2], pl[3], K);
+    mr.init_half(pr[1], pr[2], pr[3], K);
+    w0[0] = pl[0] * ml.up[0] + pr[0] * mr.un[0];
+    w0[1] = pl[0] * ml.up[1] + pr[0] * mr.un[1];
+    w0[2] = pl[0] * ml.vw[1] * ml.up[0] + pr[0] * mr.vw[1] * mr.un[0];
+    w0[3] = T(0.5) * pl[0] * (ml.up[2] + ml.up[0] * ml.vw[2] + ml.up[0] * ml.xi2) +
+            T(0.5) * pr[0] * (mr.un[2] + mr.un[0] * mr.vw[2] + mr.un[0] * mr.xi2);
+    T alx[4], arx[4], aly[4], ary[4], q0[4], q1[4], q2[4], q3[4];
+    microslope(alx, L.dx, pl, gk);
+    microslope(arx, R.dx, pr, gk);
+    microslope(aly, L.dy, pl, gk);
+    microslope(ary, R.dy, pr, gk);
+    contract<T, 0, 0, 0>(ml, alx, q0);
+    contract<T, 1, 0, 0>(mr, arx, q1);
+    contract<T, 0, 0, 0>(ml, aly, q2);
+    contract<T, 1, 0, 0>(mr, ary, q3);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        c0x[v] = pl[0] * q0[v] + pr[0] * q1[v];
+        c0y[v] = pl[0] * q2[v] + pr[0] * q3[v];
+    }
+}
+
+// LF2D's viscous term with the Navier-Stokes collision time (NS_by_central_difference_prim_2D,
+// src/flux_function.cpp:737-754) added to the Lax-Friedrichs flux f, as the reference writes
+// it: the centre state's entries are read as (rho, u, v, T) and their slopes as slopes of
+// those, although the centre state holds conserved variables (rho, rho u, rho v, rho E);
+// mu = Mu, or Nu rho when Nu > 0; heat-flux factor (K + 4) / (2 Pr).
+template <class T>
+__device__ __forceinline__ void lf_viscous(const GState<T>& L, const GState<T>& R, T dt, T K, T mu_c, T nu_c, T pr,
+                                           T* f) {
+    T w0[4], cx[4], cy[4];
+    centre_state<T>(L, R, K, w0, cx, cy);
+    T mu = mu_c;
+    if (nu_c > T(0)) mu = nu_c * w0[0];
+    const T u = w0[1], v = w0[2];
+    const T ux = cx[1], vx = cx[2], uy = cy[1], vy = cy[2];
+    const T tau_xx = T(2) * mu * ux - T(2.0 / 3.0) * mu * (ux + vy);
+    const T tau_xy = mu * (uy + vx);
+    const T q = u * tau_xx + v * tau_xy + (K + T(4)) / (T(2) * pr) * mu * cx[3];
+    f[1] += tau_xx * dt;
+    f[2] += tau_xy * dt;
+    f[3] += q * dt;
+}
+
 }  // namespace hos

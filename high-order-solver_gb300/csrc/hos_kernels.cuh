@@ -46,10 +46,18 @@ struct Geometry {
     int integrator = 0;   // HOS_INT_*: S2O4, S1O1, S1O2, RK2, RK3, RK4
     int flux = 0;         // HOS_FLUX_*: GKS2D, LF2D
     int first_order = 0;  // 1: first-order reconstruction (First_order_normal / _tangent)
+    // 1: the non-DF WENO5-AO scheme (WENO5_AO_normal / WENO5_AO_tangent, is_using_df_factor
+    // false): the DF indicators are neither read nor updated; wenotype picks its weights
+    int plain = 0;
+    int wenotype = 0;
     int source = 0;       // 1: Update_with_source (gravity along +y; S2O4 stage 0 alone updates)
     // Navier-Stokes collision time (tau_type 1): Mu, Nu; Prandtl fix factor 1/Pr - 1 (0: off)
     int tau_type = 0;
     double mu = -1.0, nu = -1.0, prandtl_coef = 0.0;
+    double prandtl = 1.0;   // Pr of LF2D's viscous term (NS_by_central_difference_prim_2D)
+    // learned gate: the a-posteriori check widens the three central cells' range by this
+    // fraction of it (density and total energy of a linear reconstruction)
+    float gate_slack = 0.1f;
     int stages = 2;
     // 1 / dx, 1 / dy, set on the host by set_spacing(): a double division costs the FP64 pipe
     // about ten instructions per thread
@@ -235,15 +243,15 @@ __device__ __forceinline__ T alpha_k(const T* wl, const T* wr, T gamma) {
 }
 
 // A-posteriori check of a linear (gated) reconstruction: density and total energy of each
-// reconstructed state stay within the range of the three central stencil entries widened by a
-// tenth of that range, and the state keeps a positive temperature.
+// reconstructed state stay within the range of the three central stencil entries widened by
+// slack times that range (a tenth unless set), and the state keeps a positive temperature.
 template <class T>
-__device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, const T* wp, T K) {
+__device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, const T* wp, T K, T slack = T(0.1)) {
     if (needs_order_reduction(q, K)) return false;
 #pragma unroll
     for (int v = 0; v < 4; v += 3) {
         const T lo = fminT(fminT(wm[v], w0[v]), wp[v]), hi = fmaxT(fmaxT(wm[v], w0[v]), wp[v]);
-        const T m = T(0.1) * (hi - lo) + T(1e-6) * fabsT(w0[v]);
+        const T m = slack * (hi - lo) + T(1e-6) * fabsT(w0[v]);
         if (!(q[v] >= lo - m && q[v] <= hi + m)) return false;
     }
     return true;
@@ -252,12 +260,17 @@ __device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, 
 // One tile of faces: N0, T0 are the first face indices along the normal and the tangent.
 // GATED (FP32 only): cells the learned gate marks smooth reconstruct with the full-stencil
 // polynomial alone; see hos_gate.cuh.
+// PLAIN (ORDER 5 only): the non-DF WENO5-AO of the drivers' default slots (WENO5_AO,
+// src/reconstruction.cpp:1589-1699, and WENO5_AO_tangential, :2244-2391) in place of the DF
+// variant, with the wenotype weights of geo.wenotype.
 // TMA (FP32 with the pitched mirror): phase 0 stages the tile from the mirror with one TMA
 // tile load (tmap: the mirror's tensor map with this tile shape's box).
-template <class T, int ORDER, int DIR, class TS, bool GATED = false, bool NS = false, bool TMA = false>
+template <class T, int ORDER, int DIR, class TS, bool GATED = false, bool NS = false, bool TMA = false,
+          bool PLAIN = false>
 __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo, const int N0, const int T0,
                                           unsigned char* smem_raw, const CUtensorMap* tmap = nullptr) {
     static_assert(!TMA || sizeof(T) == 4, "TMA staging reads the FP32 mirror");
+    static_assert(!PLAIN || (ORDER == 5 && !GATED), "the non-DF scheme is WENO5-AO, without the gate");
     using S = FaceSmem<T, ORDER, TS>;
     constexpr int TILE_N = TS::N, TILE_T = TS::T;
     constexpr int r = S::r, N = ORDER, GP = S::GP, TL = S::TL;
@@ -382,7 +395,12 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             al[k] = antile[(nl + k) * TL + tl];
         }
         T df[NW];
-        df_factors<T, ORDER>(al, df);
+        if constexpr (PLAIN) {
+#pragma unroll
+            for (int k = 0; k < NW; ++k) df[k] = T(1.0);
+        } else {
+            df_factors<T, ORDER>(al, df);
+        }
         T pn1[4], p0[4], pp1[4];
         to_prim(pn1, st[r - 1], gamma);
         to_prim(p0, st[r], gamma);
@@ -413,8 +431,9 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                     outv[side][v] = p[NW - 1];
                     outv[side][4 + v] = px[NW - 1];
                 }
-            lin = linear_ok<T>(outv[0], st[r - 1], st[r], st[r + 1], K) &&
-                  linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K);
+            const T slack = T(geo.gate_slack);
+            lin = linear_ok<T>(outv[0], st[r - 1], st[r], st[r + 1], K, slack) &&
+                  linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K, slack);
             if (!lin) atomicAdd(&rejected, 1u);
         }
 #pragma unroll
@@ -437,17 +456,23 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             T var[4], der[4];
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
-                T s[N], fw[NW], p[NW], px[NW];
+                T s[N];
 #pragma unroll
                 for (int k = 0; k < N; ++k) s[k] = ch[k][v];
-                ao_weights<T, ORDER>(s, fw);
-                if (side == 0) normal_face<T, ORDER, 0>(s, df, hN, p, px);
-                else normal_face<T, ORDER, 1>(s, df, hN, p, px);
-                T x = T(0.0), y = T(0.0);
+                if constexpr (PLAIN) {
+                    // weno_5th_ao_left / _right (:161-360): epsilon 1e-10, full 5th-order indicator
+                    weno5_face<T>(side, s, hN, var[v], der[v], geo.wenotype);
+                } else {
+                    T fw[NW], p[NW], px[NW];
+                    ao_weights<T, ORDER>(s, fw);
+                    if (side == 0) normal_face<T, ORDER, 0>(s, df, hN, p, px);
+                    else normal_face<T, ORDER, 1>(s, df, hN, p, px);
+                    T x = T(0.0), y = T(0.0);
 #pragma unroll
-                for (int k = 0; k < NW; ++k) { x += fw[k] * p[k]; y += fw[k] * px[k]; }
-                var[v] = x;
-                der[v] = y;
+                    for (int k = 0; k < NW; ++k) { x += fw[k] * p[k]; y += fw[k] * px[k]; }
+                    var[v] = x;
+                    der[v] = y;
+                }
             }
             if (geo.characteristic) {
                 cb.from_char(outv[side], var);
@@ -493,7 +518,12 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
 #pragma unroll
             for (int k = 0; k < N; ++k) al[k] = attile[(fn + side) * TL + tc + sgn * (k - r)];
             T df[NW];
-            df_factors<T, ORDER>(al, df);
+            if constexpr (PLAIN) {
+#pragma unroll
+                for (int k = 0; k < NW; ++k) df[k] = T(1.0);
+            } else {
+                df_factors<T, ORDER>(al, df);
+            }
             auto line = [&](int k, int sd) -> const T* {
                 return lines + ((fn * TL + (tc + sgn * (k - r))) * 2 + sd) * 8;
             };
@@ -531,7 +561,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 }
                 lin = true;
 #pragma unroll
-                for (int ig = 0; ig < GP; ++ig) lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K);
+                for (int ig = 0; ig < GP; ++ig)
+                    lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K, T(geo.gate_slack));
                 if (!lin) atomicAdd(&rejected, 1u);
             }
             T base[4], w0c[4];
@@ -574,6 +605,14 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                     T s[N], fw[NW];
 #pragma unroll
                     for (int k = 0; k < N; ++k) s[k] = ch[k][v];
+                    if constexpr (PLAIN) {
+                        // weno_5th_ao_2gauss (:2393-2551): epsilon 1e-6, full 5th-order indicator
+                        T g2[2], gx2[2];
+                        weno5_2g<T, true>(s, hT, g2, gx2, geo.wenotype);
+#pragma unroll
+                        for (int ig = 0; ig < GP; ++ig) { gv[ig][v] = g2[ig]; gd[ig][v] = gx2[ig]; }
+                        continue;
+                    }
                     ao_weights<T, ORDER>(s, fw);
 #pragma unroll
                     for (int ig = 0; ig < GP; ++ig) {
@@ -597,6 +636,13 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                     T s[N], fw[NW];
 #pragma unroll
                     for (int k = 0; k < N; ++k) s[k] = line(k, side)[v];
+                    if constexpr (PLAIN) {
+                        T g2[2], gx2[2];
+                        weno5_2g<T, true>(s, hT, g2, gx2, geo.wenotype);
+#pragma unroll
+                        for (int ig = 0; ig < GP; ++ig) { res[ig][v] = g2[ig]; res[ig][8 + v] = gx2[ig]; }
+                        continue;
+                    }
                     ao_weights<T, ORDER>(s, fw);
 #pragma unroll
                     for (int ig = 0; ig < GP; ++ig) {
@@ -616,6 +662,13 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 T s[N], fw[NW];
 #pragma unroll
                 for (int k = 0; k < N; ++k) s[k] = line(k, side)[4 + v];
+                if constexpr (PLAIN) {
+                    T g2[2], gx2[2];
+                    weno5_2g<T, false>(s, hT, g2, gx2, geo.wenotype);
+#pragma unroll
+                    for (int ig = 0; ig < GP; ++ig) res[ig][4 + v] = g2[ig];
+                    continue;
+                }
                 ao_weights<T, ORDER>(s, fw);
 #pragma unroll
                 for (int ig = 0; ig < GP; ++ig) {
@@ -665,6 +718,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         T f[4], d[4];
         if (geo.flux == 1) {
             lf_point<T>(L.w, R.w, dt, gamma, f);
+            // the Navier-Stokes instantiation adds LF2D's viscous term
+            if constexpr (NS) lf_viscous<T>(L, R, dt, K, T(geo.mu), T(geo.nu), T(geo.prandtl), f);
 #pragma unroll
             for (int v = 0; v < 4; ++v) d[v] = T(0.0);
         } else {
@@ -783,21 +838,22 @@ using KernelTile = typename std::conditional<ORDER == 9, TileShape<8, 16>, TileS
 template <int ORDER>
 using TmaTile = KernelTile<ORDER>;
 
-template <class T, int ORDER, int DIR, bool GATED = false, bool NS = false>
+template <class T, int ORDER, int DIR, bool GATED = false, bool NS = false, bool PLAIN = false>
 __global__ void __launch_bounds__(FACE_THREADS, sizeof(T) == 4 ? 2 : 1) face_kernel(FaceArgs a, Geometry geo) {
     using TS = KernelTile<ORDER>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    face_tile<T, ORDER, DIR, TS, GATED, NS>(a, geo, blockIdx.y * TS::N, blockIdx.x * TS::T, smem_raw);
+    face_tile<T, ORDER, DIR, TS, GATED, NS, false, PLAIN>(a, geo, blockIdx.y * TS::N, blockIdx.x * TS::T, smem_raw);
 }
 
 // FP32 face kernel of the solvers with the pitched FP32 mirror: the tile is staged by one TMA
 // tile load (tmap: the mirror's tensor map, box TmaBox<ORDER, DIR, TmaTile<ORDER>>)
-template <int ORDER, int DIR, bool GATED = false, bool NS = false>
+template <int ORDER, int DIR, bool GATED = false, bool NS = false, bool PLAIN = false>
 __global__ void __launch_bounds__(FACE_THREADS, 2)
     face_kernel_tma(FaceArgs a, Geometry geo, const __grid_constant__ CUtensorMap tmap) {
     using TS = TmaTile<ORDER>;
     extern __shared__ __align__(128) unsigned char smem_tma[];
-    face_tile<float, ORDER, DIR, TS, GATED, NS, true>(a, geo, blockIdx.y * TS::N, blockIdx.x * TS::T, smem_tma, &tmap);
+    face_tile<float, ORDER, DIR, TS, GATED, NS, true, PLAIN>(a, geo, blockIdx.y * TS::N, blockIdx.x * TS::T, smem_tma,
+                                                            &tmap);
 }
 
 }  // namespace hos

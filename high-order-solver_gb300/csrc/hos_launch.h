@@ -18,4 +18,20 @@ cudaError_t launch_faces7(int precision, const FaceArgs& ax, const FaceArgs& ay,
                            cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr);
 cudaError_t launch_faces9(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
                            cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr);
+// the non-DF WENO5-AO kernels (Geometry::plain; precisions 0, 1, 3, 4)
+cudaError_t configure_faces5p(int precision);
+cudaError_t launch_faces5p(int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo, cudaStream_t s,
+                            cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr);
+// the face kernels of geo's order and scheme
+inline cudaError_t configure_faces(const Geometry& geo, int order, int precision) {
+    if (geo.plain) return configure_faces5p(precision);
+    return order == 5 ? configure_faces5(precision) : order == 7 ? configure_faces7(precision) : configure_faces9(precision);
+}
+inline cudaError_t launch_faces(int order, int precision, const FaceArgs& ax, const FaceArgs& ay, const Geometry& geo,
+                                cudaStream_t s, cudaEvent_t* ev = nullptr, const CUtensorMap* tm = nullptr) {
+    if (geo.plain) return launch_faces5p(precision, ax, ay, geo, s, ev, tm);
+    return order == 5 ? launch_faces5(precision, ax, ay, geo, s, ev, tm)
+         : order == 7 ? launch_faces7(precision, ax, ay, geo, s, ev, tm)
+                      : launch_faces9(precision, ax, ay, geo, s, ev, tm);
+}
 }  // namespace hos

@@ -387,11 +387,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     const int prec = geo.tau_type == HOS_TAU_NS ? (s->precision == HOS_FP64 ? 3 : 4) : s->gated ? 2 : s->precision;
     // FP32 solvers stage their tiles from the mirror with TMA tile loads
     const CUtensorMap* tm = s->W32 ? s->tmap : nullptr;
-    switch (s->p.order) {
-        case 5: e = launch_faces5(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm); break;
-        case 7: e = launch_faces7(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm); break;
-        default: e = launch_faces9(prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm); break;
-    }
+    e = launch_faces(s->p.order, prec, ax, ay, geo, s->stream, ev ? ev + 2 : nullptr, tm);
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
     UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage, s->W32, s->A32};
     const int n = geo.nodex * geo.nodey;
@@ -474,7 +470,12 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     if (!(p.order == 5 || p.order == 7 || p.order == 9)) return fail(HOS_E_CONFIG, "order must be 5, 7 or 9");
     const int need_gp = p.order == 5 ? 2 : p.order == 7 ? 3 : 4;
     if (p.gausspoint != need_gp) return fail(HOS_E_CONFIG, "gausspoint must be 2/3/4 for order 5/7/9");
-    if (!p.use_df) return fail(HOS_E_CONFIG, "only the discontinuity-feedback variants are provided (use_df = 1)");
+    // use_df = 0: the drivers' default WENO5_AO_normal / WENO5_AO_tangent, which exist for
+    // WENO5 only (and write the Gauss points only with gausspoint = 2, :2264, :2279)
+    if (!p.use_df && p.order != 5)
+        return fail(HOS_E_CONFIG, "without the DF factor (use_df = 0) the reconstruction is WENO5-AO: order must be 5");
+    if (!p.use_df && (p.wenotype < HOS_WENO_Z || p.wenotype > HOS_WENO_LINEAR))
+        return fail(HOS_E_CONFIG, "wenotype must be HOS_WENO_Z, HOS_WENO_JS or HOS_WENO_LINEAR");
     if (p.ghost < p.order / 2 + 1) return fail(HOS_E_CONFIG, "ghost must be >= order/2 + 1");
     if (p.nodex < p.ghost || p.nodey < p.ghost) return fail(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail(HOS_E_CONFIG, "precision must be HOS_FP64 or HOS_FP32");
@@ -482,9 +483,9 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     if (p.integrator < HOS_INT_S2O4 || p.integrator > HOS_INT_RK4) return fail(HOS_E_CONFIG, "bad time-marching method");
     if (p.flux != HOS_FLUX_GKS && p.flux != HOS_FLUX_LF) return fail(HOS_E_CONFIG, "bad flux");
     if (p.tau_type != HOS_TAU_EULER && p.tau_type != HOS_TAU_NS) return fail(HOS_E_CONFIG, "bad tau_type");
-    if (p.tau_type == HOS_TAU_NS && p.flux != HOS_FLUX_GKS)
-        return fail(HOS_E_CONFIG, "the Navier-Stokes collision time goes with the GKS2D flux");
     if (p.prandtl_fix && !(p.prandtl > 0)) return fail(HOS_E_CONFIG, "the Prandtl fix needs prandtl > 0");
+    if (p.tau_type == HOS_TAU_NS && p.flux == HOS_FLUX_LF && !(p.prandtl > 0))
+        return fail(HOS_E_CONFIG, "LF2D's viscous term divides by the Prandtl number: prandtl must be > 0");
     hos_solver2d* s = new (std::nothrow) hos_solver2d();
     if (!s) return fail(HOS_E_NOMEM, "host allocation");
     s->p = p;
@@ -504,6 +505,8 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     geo.c1 = p.c1_euler;
     geo.c2 = p.c2_euler;
     geo.characteristic = p.characteristic ? 1 : 0;
+    geo.plain = p.use_df ? 0 : 1;
+    geo.wenotype = p.use_df ? 0 : p.wenotype;
     geo.integrator = p.integrator;
     geo.flux = p.flux;
     geo.stages = integrator_stages(p.integrator);
@@ -511,6 +514,7 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     geo.mu = p.mu;
     geo.nu = p.nu;
     geo.prandtl_coef = p.tau_type == HOS_TAU_NS && p.prandtl_fix ? 1.0 / p.prandtl - 1.0 : 0.0;
+    geo.prandtl = p.prandtl;
     fill_boundaries(s->bc, p, geo.dx);
     s->ncell = (size_t)geo.nx * geo.ny;
     s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;
@@ -556,11 +560,7 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     }
     cudaMemset(s->ctl, 0, sizeof(StepCtl));
     const int variant = p.tau_type == HOS_TAU_NS ? (precision == HOS_FP64 ? 3 : 4) : precision;
-    switch (p.order) {
-        case 5: e = configure_faces5(variant); break;
-        case 7: e = configure_faces7(variant); break;
-        default: e = configure_faces9(variant); break;
-    }
+    e = configure_faces(s->geo, p.order, variant);
     if (e != cudaSuccess) {
         free_all(s);
         delete s;
@@ -725,6 +725,20 @@ int hos2d_set_time(hos_solver2d* s, double t) {
     return e == cudaSuccess ? HOS_OK : cuda_fail(e, "set_time");
 }
 
+int hos2d_set_gate_check(hos_solver2d* s, double slack) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    if (!(slack >= 0.0 && slack <= 10.0)) return fail(HOS_E_ARG, "slack must be in [0, 10]");
+    if (s->geo.gate_slack == (float)slack) return HOS_OK;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "set_gate_check");
+    s->geo.gate_slack = (float)slack;
+    if (s->graph) {  // the captured step holds the old geometry
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    return HOS_OK;
+}
+
 int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audit_log2) {
     using namespace gate;
     if (!s) return fail(HOS_E_ARG, "null solver");
@@ -740,6 +754,7 @@ int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audi
     }
     if (s->precision != HOS_FP32) return fail(HOS_E_CONFIG, "the learned gate runs on the FP32-bulk path");
     if (s->geo.tau_type == HOS_TAU_NS) return fail(HOS_E_CONFIG, "the learned gate runs with the Euler collision time");
+    if (s->geo.plain) return fail(HOS_E_CONFIG, "the learned gate runs with the DF variants (use_df = 1)");
     if (audit_log2 < 0 || audit_log2 > 31) return fail(HOS_E_ARG, "audit_log2 must be 0..31");
     if (!s->gflags) {
         if ((e = cudaMalloc(&s->gflags, s->ncell)) == cudaSuccess && (e = cudaMalloc(&s->gstats, sizeof(Stats))) == cudaSuccess &&

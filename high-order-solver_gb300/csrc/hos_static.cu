@@ -11,7 +11,11 @@
 // until the process exits.
 //
 // Limits: nodex, nodey <= HOS_STATIC_MAX_NODE (256) and ghost <= HOS_STATIC_MAX_GHOST (5),
-// i.e. about 11.7 MB of scratch.  Larger problems are rejected with HOS_E_CONFIG.
+// i.e. about 11.7 MB of scratch.  Larger problems are rejected with HOS_E_CONFIG, and so are
+// settings the step does not run: time marching other than S2O4, the LF flux, the non-DF
+// scheme, and the wedge and no-slip boundaries.  Both collision times (Euler, Navier-Stokes
+// with the Prandtl fix) are run as hos2d_create runs them.  Each call waits for its stream
+// to finish before returning (it reads the step's status word back).
 // The first call on a device looks up the array's device address (cudaGetSymbolAddress)
 // and enables the face kernels' shared-memory size for that device; make that first call
 // before any stream capture.  Every call shares the one array and it keeps the last call's
@@ -36,8 +40,11 @@ constexpr size_t kScratchDoubles = 4 * kMaxCells + 2 * 9 * kMaxFaces + kCtlDoubl
 static __device__ __align__(256) double g_step_scratch[kScratchDoubles];
 
 constexpr int kMaxDevices = 64;
+// Per-device set-up state.  These host globals are written without a lock: two host threads
+// making a device's first call at the same time both look up the same address and set the
+// same bits, so the race is benign; calls themselves must be serialised per device anyway.
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
-unsigned g_configured[kMaxDevices] = {0};   // bit (order/2 - 2) * 2 + precision
+unsigned g_configured[kMaxDevices] = {0};   // bit (order/2 - 2) * 5 + face-kernel variant
 
 thread_local std::string g_err;
 
@@ -71,6 +78,9 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
     if (!p.use_df) return fail_static(HOS_E_CONFIG, "use_df must be 1");
     if (p.integrator != HOS_INT_S2O4 || p.flux != HOS_FLUX_GKS)
         return fail_static(HOS_E_CONFIG, "the allocation-free step runs S2O4 with the GKS flux");
+    if (p.tau_type != HOS_TAU_EULER && p.tau_type != HOS_TAU_NS) return fail_static(HOS_E_CONFIG, "bad tau_type");
+    if (p.tau_type == HOS_TAU_NS && p.prandtl_fix && !(p.prandtl > 0))
+        return fail_static(HOS_E_CONFIG, "the Prandtl fix needs prandtl > 0");
     if (p.ghost < p.order / 2 + 1) return fail_static(HOS_E_CONFIG, "ghost must be >= order/2 + 1");
     if (p.nodex < p.ghost || p.nodey < p.ghost) return fail_static(HOS_E_CONFIG, "nodex and nodey must be >= ghost");
     if (p.nodex > kMaxNode || p.nodey > kMaxNode || p.ghost > kMaxGhost)
@@ -79,7 +89,9 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
                                              "); use hos2d_create for larger problems");
     if (precision != HOS_FP64 && precision != HOS_FP32) return fail_static(HOS_E_CONFIG, "bad precision");
     for (int k = 0; k < 4; ++k)
-        if (p.bc[k] < 0 || p.bc[k] > 3) return fail_static(HOS_E_CONFIG, "bad boundary kind");
+        if (p.bc[k] < 0 || p.bc[k] > 3)
+            return fail_static(HOS_E_CONFIG, "the allocation-free step takes free, periodic, reflective and inflow "
+                                             "boundaries (HOS_BC_FREE .. HOS_BC_INFLOW)");
     if ((p.bc[0] == HOS_BC_PERIODIC) != (p.bc[1] == HOS_BC_PERIODIC) ||
         (p.bc[2] == HOS_BC_PERIODIC) != (p.bc[3] == HOS_BC_PERIODIC))
         return fail_static(HOS_E_CONFIG, "periodic boundaries must be paired");
@@ -96,9 +108,12 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
         if (e != cudaSuccess) return fail_static(HOS_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         g_scratch_ptr[dev] = static_cast<double*>(ptr);
     }
-    const unsigned bit = 1u << ((p.order / 2 - 2) * 2 + precision);
+    // face-kernel variant: 0 / 1 FP64 / FP32 with the Euler collision time, 3 / 4 with the
+    // Navier-Stokes one
+    const int variant = p.tau_type == HOS_TAU_NS ? (precision == HOS_FP64 ? 3 : 4) : precision;
+    const unsigned bit = 1u << ((p.order / 2 - 2) * 5 + variant);
     if (!(g_configured[dev] & bit)) {
-        e = p.order == 5 ? configure_faces5(precision) : p.order == 7 ? configure_faces7(precision) : configure_faces9(precision);
+        e = p.order == 5 ? configure_faces5(variant) : p.order == 7 ? configure_faces7(variant) : configure_faces9(variant);
         if (e != cudaSuccess) return fail_static(HOS_E_CUDA, std::string("configure face kernels: ") + cudaGetErrorString(e));
         g_configured[dev] |= bit;
     }
@@ -116,6 +131,10 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
     geo.c1 = p.c1_euler;
     geo.c2 = p.c2_euler;
     geo.characteristic = p.characteristic ? 1 : 0;
+    geo.tau_type = p.tau_type;
+    geo.mu = p.mu;
+    geo.nu = p.nu;
+    geo.prandtl_coef = p.tau_type == HOS_TAU_NS && p.prandtl_fix ? 1.0 / p.prandtl - 1.0 : 0.0;
     BcSpec bc;
     for (int k = 0; k < 4; ++k) {
         bc.kind[k] = p.bc[k];
@@ -146,9 +165,9 @@ extern "C" int hos2d_step_static(const hos_params2d* params, int precision, doub
         bc_fill_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(d_W, geo, bc, ctl, 1);
         FaceArgs ax{d_W, d_alpha_x, d_alpha_y, FXx, FPx, FAx, ctl, stage};
         FaceArgs ay{d_W, d_alpha_y, d_alpha_x, FXy, FPy, FAy, ctl, stage};
-        e = p.order == 5 ? launch_faces5(precision, ax, ay, geo, s)
-          : p.order == 7 ? launch_faces7(precision, ax, ay, geo, s)
-                         : launch_faces9(precision, ax, ay, geo, s);
+        e = p.order == 5 ? launch_faces5(variant, ax, ay, geo, s)
+          : p.order == 7 ? launch_faces7(variant, ax, ay, geo, s)
+                         : launch_faces9(variant, ax, ay, geo, s);
         if (e != cudaSuccess) return fail_static(HOS_E_CUDA, std::string("face kernels: ") + cudaGetErrorString(e));
         UpdateArgs ua{d_W, Wold, d_alpha_x, d_alpha_y, FXx, FXy, FAx, FAy, ctl, stage};
         const int n = geo.nodex * geo.nodey;

@@ -168,7 +168,8 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             if (a.W32) a.W32[v * plane32 + cm] = (float)w[v];
         }
         const int jend = nodex < nodey ? nodex : nodey;
-        if (J < jend) {
+        // Update_alpha runs only under is_using_df_factor (src/2Dproblem.cpp:154)
+        if (J < jend && !geo.plain) {
             const double ax = a.FAx[fl] + a.FAx[fr], ay = a.FAy[fd] + a.FAy[fu];
             a.AX[c] = ax;
             a.AY[c] = ay;

@@ -416,4 +416,123 @@ __device__ __forceinline__ void tangent_point(int ig, const T* s, const T* df, T
     }
 }
 
+// ---- non-DF WENO5-AO (src/reconstruction.cpp:161-360, 2393-2551): the 3D scheme and the 2D
+// drivers' default slots WENO5_AO_normal / WENO5_AO_tangent (is_using_df_factor = false) ----
+// nonlinear weights: the reference's WENOtype (HOS_WENO_* of the C ABI)
+enum { WENO_Z = 0, WENO_JS = 1, WENO_LINEAR = 2 };
+template <class T>
+__device__ __forceinline__ T beta5_big(T wn2, T wn1, T w0, T wp1, T wp2) {
+    return T(1.0 / 5040.0) * (T(231153) * w0 * w0 + T(104963) * wn1 * wn1 + T(6908) * wn2 * wn2 -
+                              T(38947) * wn2 * wp1 + T(104963) * wp1 * wp1 +
+                              wn1 * (T(-51001) * wn2 + T(179098) * wp1 - T(38947) * wp2) -
+                              T(3) * w0 * (T(99692) * wn1 - T(22641) * wn2 + T(99692) * wp1 - T(22641) * wp2) +
+                              T(8209) * wn2 * wp2 - T(51001) * wp1 * wp2 + T(6908) * wp2 * wp2);
+}
+// final AO weights (linear weights d = {0.01125, 0.1275, 0.01125, 0.85} from dhi = dlo = 0.85);
+// wtype: WENO_Z, WENO_JS or WENO_LINEAR (the reference's wenotype, :176-216)
+template <class T>
+__device__ __forceinline__ void weights5(const T* s, T eps, T* fw, int wtype = WENO_Z) {
+    const T d0 = T(0.5) * T(0.15) * T(0.15), d1 = T(0.15) * T(0.85), d3 = T(0.85);
+    if (wtype == WENO_LINEAR) {
+        // the linear weights select the big-stencil polynomial alone
+        fw[0] = T(0); fw[1] = T(0); fw[2] = T(0); fw[3] = T(1);
+        return;
+    }
+    T b[4];
+    beta3<T>(s, b);
+    if constexpr (sizeof(T) == 4) {
+        // the big-stencil indicator expands into terms ~1e5 w^2 that cancel; it depends on
+        // differences only, so FP32 evaluates it about the centre value
+        b[3] = beta5_big(s[0] - s[2], s[1] - s[2], T(0), s[3] - s[2], s[4] - s[2]);
+    } else {
+        b[3] = beta5_big(s[0], s[1], s[2], s[3], s[4]);
+    }
+    const T tau = T(1.0 / 3.0) * (fabsT(b[3] - b[0]) + fabsT(b[3] - b[1]) + fabsT(b[3] - b[2]));
+    T al[4];
+    const T dd[4] = {d0, d1, d0, d3};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (wtype == WENO_JS) {
+            const T e = eps + b[k];
+            al[k] = dd[k] / (e * e);
+        } else {
+            const T q = tau / (b[k] + eps);
+            al[k] = dd[k] * (T(1) + q * q);
+        }
+    }
+    const T isum = T(1) / (al[0] + al[1] + al[2] + al[3]);
+    const T w3 = al[3] * isum;
+    fw[3] = w3 / d3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) fw[k] = al[k] * isum - fw[3] * dd[k];
+}
+// value and slope at the left (side 0) or right (side 1) face of the centre cell, epsilon 1e-10
+template <class T>
+__device__ __forceinline__ void weno5_face(int side, const T* s, T ih, T& var, T& der, int wtype = WENO_Z) {
+    T fw[4];
+    weights5<T>(s, T(1e-10), fw, wtype);
+    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+    T p[4], px[4];
+    if (side == 0) {
+        p[0] = T(-1.0 / 6.0) * wn2 + T(5.0 / 6.0) * wn1 + T(1.0 / 3.0) * w0;
+        p[1] = T(1.0 / 3.0) * wn1 + T(5.0 / 6.0) * w0 - T(1.0 / 6.0) * wp1;
+        p[2] = T(11.0 / 6.0) * w0 - T(7.0 / 6.0) * wp1 + T(1.0 / 3.0) * wp2;
+        p[3] = T(1.0 / 60.0) * (T(47) * w0 + T(27) * wn1 - T(3) * wn2 - T(13) * wp1 + T(2) * wp2);
+        px[0] = (w0 - wn1) * ih;
+        px[1] = px[0];
+        px[2] = -(T(2) * w0 - T(3) * wp1 + wp2) * ih;
+        px[3] = (T(15) * w0 - T(15) * wn1 + wn2 - wp1) * (T(1.0 / 12.0) * ih);
+    } else {
+        p[0] = T(1.0 / 3.0) * wn2 - T(7.0 / 6.0) * wn1 + T(11.0 / 6.0) * w0;
+        p[1] = T(-1.0 / 6.0) * wn1 + T(5.0 / 6.0) * w0 + T(1.0 / 3.0) * wp1;
+        p[2] = T(1.0 / 3.0) * w0 + T(5.0 / 6.0) * wp1 - T(1.0 / 6.0) * wp2;
+        p[3] = T(1.0 / 60.0) * (T(47) * w0 - T(13) * wn1 + T(2) * wn2 + T(27) * wp1 - T(3) * wp2);
+        px[0] = (T(2) * w0 - T(3) * wn1 + wn2) * ih;
+        px[1] = (wp1 - w0) * ih;
+        px[2] = px[1];
+        px[3] = (T(-15) * w0 + wn1 + T(15) * wp1 - wp2) * (T(1.0 / 12.0) * ih);
+    }
+    var = fw[0] * p[0] + fw[1] * p[1] + fw[2] * p[2] + fw[3] * p[3];
+    der = fw[0] * px[0] + fw[1] * px[1] + fw[2] * px[2] + fw[3] * px[3];
+}
+// values (and slopes when DER) at the Gauss points -h/(2 sqrt 3) (g0) and +h/(2 sqrt 3) (g1)
+// of the centre cell, epsilon 1e-6 (weno_5th_ao_2gauss).  Under wenotype = linear the
+// reference leaves its weights unset (:2446-2468 have no linear branch); the linear weights
+// are taken here.
+template <class T, bool DER>
+__device__ __forceinline__ void weno5_2g(const T* s, T ih, T* g, T* gx, int wtype = WENO_Z) {
+    T fw[4];
+    weights5<T>(s, T(1e-6), fw, wtype);
+    const T wn2 = s[0], wn1 = s[1], w0 = s[2], wp1 = s[3], wp2 = s[4];
+    const T r3 = T(1.732050807568877294), i4r3 = T(1) / (T(4) * r3);
+    // candidate polynomials at g0; g1 is their mirror image
+    T p0 = w0 - r3 * w0 * T(0.25) + (T(4) * wn1 - wn2) * i4r3;
+    T p1 = w0 + (wn1 - wp1) * i4r3;
+    T p2 = T(1.0 / 12.0) * (T(3) * (T(4) + r3) * w0 + r3 * (T(-4) * wp1 + wp2));
+    T p3 = (T(4314) * w0 + (T(4) + T(500) * r3) * wn1 - wn2 - T(70) * r3 * wn2 + T(4) * wp1 - T(500) * r3 * wp1 - wp2
+            + T(70) * r3 * wp2) * T(1.0 / 4320.0);
+    g[0] = fw[0] * p0 + fw[1] * p1 + fw[2] * p2 + fw[3] * p3;
+    p0 = T(1.0 / 12.0) * (T(3) * (T(4) + r3) * w0 + r3 * (T(-4) * wn1 + wn2));
+    p1 = w0 + (wp1 - wn1) * i4r3;
+    p2 = w0 - r3 * w0 * T(0.25) + (T(4) * wp1 - wp2) * i4r3;
+    p3 = (T(4314) * w0 + (T(4) - T(500) * r3) * wn1 - wn2 + T(70) * r3 * wn2 + T(4) * wp1 + T(500) * r3 * wp1 - wp2
+          - T(70) * r3 * wp2) * T(1.0 / 4320.0);
+    g[1] = fw[0] * p0 + fw[1] * p1 + fw[2] * p2 + fw[3] * p3;
+    if (DER) {
+        const T i6h = ih * T(1.0 / 6.0), i108h = ih * T(1.0 / 108.0);
+        T q0 = -((r3 - T(9)) * w0 - T(2) * (r3 - T(6)) * wn1 + (r3 - T(3)) * wn2) * i6h;
+        T q1 = -(T(-2) * r3 * w0 + (T(3) + r3) * wn1 + (r3 - T(3)) * wp1) * i6h;
+        T q2 = -((T(9) + r3) * w0 - T(2) * (T(6) + r3) * wp1 + (T(3) + r3) * wp2) * i6h;
+        T q3 = (T(48) * r3 * w0 - T(72) * wn1 - T(26) * r3 * wn1 + T(9) * wn2 + T(2) * r3 * wn2 + T(72) * wp1
+                - T(26) * r3 * wp1 - T(9) * wp2 + T(2) * r3 * wp2) * i108h;
+        gx[0] = fw[0] * q0 + fw[1] * q1 + fw[2] * q2 + fw[3] * q3;
+        q0 = ((T(9) + r3) * w0 - T(2) * (T(6) + r3) * wn1 + (T(3) + r3) * wn2) * i6h;
+        q1 = (T(-2) * r3 * w0 + (r3 - T(3)) * wn1 + (T(3) + r3) * wp1) * i6h;
+        q2 = ((r3 - T(9)) * w0 - T(2) * (r3 - T(6)) * wp1 + (r3 - T(3)) * wp2) * i6h;
+        q3 = -(T(48) * r3 * w0 + T(72) * wn1 - T(26) * r3 * wn1 - T(9) * wn2 + T(2) * r3 * wn2 - T(72) * wp1
+               - T(26) * r3 * wp1 + T(9) * wp2 + T(2) * r3 * wp2) * i108h;
+        gx[1] = fw[0] * q0 + fw[1] * q1 + fw[2] * q2 + fw[3] * q3;
+    }
+}
+
 }  // namespace hos

@@ -75,11 +75,17 @@ def random_riemann2d(n: int, seed: int, order: int = 7) -> tuple:
 
 def isentropic_vortex(n: int = 200, order: int = 5, strength: float = 5.0,
                       center=(5.0, 5.0), length: float = 10.0,
-                      characteristic: bool = True) -> tuple:
+                      characteristic: bool = True, images: bool = True) -> tuple:
     """Isentropic vortex on the periodic square [0, L]^2 over a unit freestream
     (rho, u, v, p) = (1, 1, 1, 1); cell averages by 4x4 Gauss-Legendre quadrature.
     The flow is smooth, so the numerical collision time is zero (c1 = c2 = 0) as in the
-    reference's smooth accuracy drivers (src/2Dproblem.cpp:1376-1377)."""
+    reference's smooth accuracy drivers (src/2Dproblem.cpp:1376-1377).
+
+    images: the vortex's perturbations (velocity and the temperature factor e^2) are summed
+    over its periodic images at offsets -L, 0, +L in x and y, so the data are periodic to
+    round-off (the nearest omitted image lies 15 or more away: e^(-112)).  A single vortex on
+    [0, 10]^2 is not periodic: its velocity tail jumps by up to 2.4e-5 across the boundary,
+    which bounds the error of any scheme near 4e-7 in L1."""
     pb = Problem2D(nodex=n, nodey=n, order=order, characteristic=characteristic,
                    c1_euler=0.0, c2_euler=0.0, cfl=0.5, left=0.0, right=length,
                    down=0.0, up=length, bc=("periodic",) * 4)
@@ -93,13 +99,17 @@ def isentropic_vortex(n: int = 200, order: int = 5, strength: float = 5.0,
         for b, wb in zip(xg, wg):
             x = xc[:, None] + 0.5 * pb.dx * a
             y = yc[None, :] + 0.5 * pb.dy * b
-            dxv = x - center[0]
-            dyv = y - center[1]
-            r2 = dxv * dxv + dyv * dyv
-            e = np.exp(0.5 * (1.0 - r2))
-            du = -strength / (2 * math.pi) * e * dyv
-            dv = strength / (2 * math.pi) * e * dxv
-            t = 1.0 - (gamma - 1.0) * strength ** 2 / (8 * gamma * math.pi ** 2) * e * e
+            du, dv, dt = 0.0, 0.0, 0.0
+            for ox in ((-length, 0.0, length) if images else (0.0,)):
+                for oy in ((-length, 0.0, length) if images else (0.0,)):
+                    dxv = x - (center[0] + ox)
+                    dyv = y - (center[1] + oy)
+                    r2 = dxv * dxv + dyv * dyv
+                    e = np.exp(0.5 * (1.0 - r2))
+                    du = du - strength / (2 * math.pi) * e * dyv
+                    dv = dv + strength / (2 * math.pi) * e * dxv
+                    dt = dt + (gamma - 1.0) * strength ** 2 / (8 * gamma * math.pi ** 2) * e * e
+            t = 1.0 - dt
             rho = t ** (1.0 / (gamma - 1.0))
             prim = np.stack([rho, 1.0 + du, 1.0 + dv, rho * t], axis=-1)
             cons += 0.25 * wa * wb * prim_to_con(prim, gamma)
@@ -226,11 +236,13 @@ def wedge2d(nodex: int = 240, nodey: int = 60, mach: float = 10.0, order: int = 
 
 
 def shock_vortex2d(n: int = 128, mach: float = 1.5, strength: float = 0.3, order: int = 5,
-                   characteristic: bool = True) -> tuple:
+                   characteristic: bool = True, c1_euler: float = 0.05) -> tuple:
     """Shock-vortex interaction on [0, 2] x [0, 1] (2n x n cells): a stationary normal shock at
     x = 0.5 with upstream Mach ``mach``, upstream state (1, M sqrt(gamma), 0, 1), and an
     isentropic vortex of strength ``strength`` (core radius 0.05, decay 0.204) centred at
-    (0.25, 0.5) in the upstream flow; inflow left, outflow right, reflective top and bottom."""
+    (0.25, 0.5) in the upstream flow; inflow left, outflow right, reflective top and bottom.
+    c1_euler: the numerical collision-time coefficient (the reference's drivers take 0.05 for
+    the quadrant problems and 0.2 for the Mach-10 double Mach reflection)."""
     gamma = 1.4
     u1 = mach * math.sqrt(gamma)
     m2 = mach * mach
@@ -239,7 +251,7 @@ def shock_vortex2d(n: int = 128, mach: float = 1.5, strength: float = 0.3, order
     up = (1.0, u1, 0.0, 1.0)
     down = (rho2, u1 / rho2, 0.0, p2)
     pb = Problem2D(nodex=2 * n, nodey=n, order=order, characteristic=characteristic,
-                   c1_euler=0.05, c2_euler=1.0, cfl=0.5, left=0.0, right=2.0, down=0.0, up=1.0,
+                   c1_euler=c1_euler, c2_euler=1.0, cfl=0.5, left=0.0, right=2.0, down=0.0, up=1.0,
                    bc=("inflow", "free", "reflect", "reflect"),
                    bc_prim=(up, (0.0,) * 4, (0.0,) * 4, (0.0,) * 4))
     g = pb.ghost
@@ -275,7 +287,10 @@ def batch_sweep(count: int = 64, seed: int = 0, side_min: int = 128, side_max: i
     [0,4]x[0,1] (square cells in both).  Shock Mach numbers are uniform in [mach_min, mach_max]
     and vortex strengths uniform in [0, strength_max].  End times are set so that the vortex
     crosses 0.3 of the domain height through the shock (0.3 / u_upstream) and the wedge shock
-    trace moves the same distance whatever its Mach number (0.5 / M).
+    trace moves the same distance whatever its Mach number (0.5 / M).  Shocks of Mach 3 and
+    above take the reference's strong-shock collision coefficient c1 = 0.2
+    (src/2Dproblem.cpp:839-840, the Mach-10 driver), weaker ones the quadrant problems' 0.05;
+    the drivers' first-order step 0 is the caller's (Batch2D.set_reconstruction).
 
     Returns a list of (problem, convar, primvar, tstop, label)."""
     rng = np.random.default_rng(seed)
@@ -285,7 +300,8 @@ def batch_sweep(count: int = 64, seed: int = 0, side_min: int = 128, side_max: i
         mach = float(rng.uniform(mach_min, mach_max))
         if k % 2 == 0:
             strength = float(rng.uniform(0.0, strength_max))
-            pb, con, prim = shock_vortex2d(s // 2, mach=mach, strength=strength, order=order)
+            pb, con, prim = shock_vortex2d(s // 2, mach=mach, strength=strength, order=order,
+                                           c1_euler=0.2 if mach >= 3.0 else 0.05)
             tstop = 0.3 / (mach * math.sqrt(pb.gamma))
             label = f"shock_vortex {pb.nodex}x{pb.nodey} M={mach:.2f} eps={strength:.2f}"
         else:

@@ -38,8 +38,12 @@ class Params2D(ctypes.Structure):
         ("integrator", ctypes.c_int), ("flux", ctypes.c_int),
         ("tau_type", ctypes.c_int), ("mu", ctypes.c_double), ("nu", ctypes.c_double),
         ("prandtl_fix", ctypes.c_int), ("prandtl", ctypes.c_double),
+        ("wenotype", ctypes.c_int),
     ]
 
+
+# weights of the non-DF WENO5-AO scheme (HOS_WENO_* in include/hos_gb300.h)
+WENOTYPES = {"wenoz": 0, "wenojs": 1, "linear": 2}
 
 # time-marching methods and fluxes (HOS_INT_*, HOS_FLUX_* in include/hos_gb300.h)
 INTEGRATORS = {"S2O4": 0, "S1O1": 1, "S1O2": 2, "RK2": 3, "RK3": 4, "RK4": 5}
@@ -82,6 +86,10 @@ class Problem2D:
     nu: float = -1.0
     prandtl_fix: bool = False
     prandtl: float = 1.0
+    # is_using_df_factor: True the DF variants; False the non-DF WENO5-AO with the wenotype
+    # weights ("wenoz", "wenojs" or "linear")
+    use_df: bool = True
+    wenotype: str = "wenoz"
 
     @property
     def nx(self) -> int:
@@ -105,7 +113,8 @@ class Problem2D:
         p.order = self.order
         p.gausspoint = GAUSS_POINTS[self.order]
         p.characteristic = 1 if self.characteristic else 0
-        p.use_df = 1
+        p.use_df = 1 if self.use_df else 0
+        p.wenotype = WENOTYPES[self.wenotype]
         p.K = self.K
         p.gamma, p.c1_euler, p.c2_euler, p.cfl = self.gamma, self.c1_euler, self.c2_euler, self.cfl
         p.left, p.right, p.down, p.up = self.left, self.right, self.down, self.up
@@ -134,7 +143,7 @@ class Params1D(ctypes.Structure):
         ("characteristic", ctypes.c_int), ("df_mode", ctypes.c_int), ("update_alpha", ctypes.c_int),
         ("K", ctypes.c_int), ("gamma", ctypes.c_double), ("c1_euler", ctypes.c_double),
         ("c2_euler", ctypes.c_double), ("cfl", ctypes.c_double), ("left", ctypes.c_double),
-        ("right", ctypes.c_double), ("bc", ctypes.c_int * 2),
+        ("right", ctypes.c_double), ("bc", ctypes.c_int * 2), ("wenotype", ctypes.c_int),
     ]
 
 
@@ -160,6 +169,8 @@ class Problem1D:
     left: float = 0.0
     right: float = 1.0
     bc: tuple = ("free", "free")
+    # weights of the non-DF WENO5-AO steps ("wenoz", "wenojs" or "linear")
+    wenotype: str = "wenoz"
 
     @property
     def nx(self) -> int:
@@ -175,6 +186,7 @@ class Problem1D:
         p.characteristic = 1 if self.characteristic else 0
         p.df_mode = int(self.df_mode)
         p.update_alpha = 1 if self.update_alpha else 0
+        p.wenotype = WENOTYPES[self.wenotype]
         p.K = self.K
         p.gamma, p.c1_euler, p.c2_euler, p.cfl = self.gamma, self.c1_euler, self.c2_euler, self.cfl
         p.left, p.right = self.left, self.right
@@ -197,6 +209,7 @@ class Params3D(ctypes.Structure):
         ("left", ctypes.c_double), ("right", ctypes.c_double), ("down", ctypes.c_double),
         ("up", ctypes.c_double), ("back", ctypes.c_double), ("front", ctypes.c_double),
         ("bc", ctypes.c_int * 6), ("prandtl_fix", ctypes.c_int), ("prandtl", ctypes.c_double),
+        ("gks3d_pressure_slot", ctypes.c_int),
     ]
 
 
@@ -228,6 +241,8 @@ class Problem3D:
     bc: tuple = ("free",) * 6
     prandtl_fix: bool = False   # Prandtl-number correction of the heat flux ...
     prandtl: float = 1.0        # ... with this Pr
+    # the reference's own GKS3D convention (pressure where lambda belongs), FP64 only
+    gks3d_pressure_slot: bool = False
 
     @property
     def shape(self) -> tuple:
@@ -259,4 +274,5 @@ class Problem3D:
             b = self.bc[s]
             p.bc[s] = _BC_NAMES[b] if isinstance(b, str) else int(b)
         p.prandtl_fix, p.prandtl = 1 if self.prandtl_fix else 0, float(self.prandtl)
+        p.gks3d_pressure_slot = 1 if self.gks3d_pressure_slot else 0
         return p

@@ -110,7 +110,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                    ctypes.c_uint, _DP]
     lib.hos_gate_last_error.restype = ctypes.c_char_p
     lib.hos2d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
+    lib.hos2d_set_gate_check.argtypes = [vp, ctypes.c_double]
     lib.hos_batch2d_set_gate.argtypes = [vp, vp, ctypes.c_float, ctypes.c_int]
+    lib.hos_batch2d_set_reconstruction.argtypes = [vp, ctypes.c_int]
     lib.hos_batch2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     lib.hos2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     lib.hos3d_create.argtypes = [ctypes.POINTER(Params3D), ctypes.c_int, ctypes.POINTER(vp)]
@@ -259,6 +261,10 @@ class Solver2D:
     def set_gate(self, gate: "Gate | None", threshold: float = 0.0, audit_log2: int = 6) -> None:
         """Attach a copy of a learned gate (FP32 solvers); None detaches it."""
         _check(self._lib.hos2d_set_gate(self._h, gate._h if gate is not None else None, threshold, audit_log2))
+
+    def set_gate_check(self, slack: float) -> None:
+        """Widening of the linear path's a-posteriori range check (fraction of the range)."""
+        _check(self._lib.hos2d_set_gate_check(self._h, slack))
 
     def gate_stats(self, reset: bool = False) -> dict:
         v = (ctypes.c_ulonglong * 8)()
@@ -516,6 +522,11 @@ class Batch2D:
         if failed:
             return act.value, t, np.array(last[:]), np.array(bad[:], dtype=bool)
         return act.value, t, np.array(last[:])
+
+    def set_reconstruction(self, first_order: bool) -> None:
+        """First-order reconstruction for the following steps of every problem (the drivers'
+        step 0) or the WENO-AO scheme."""
+        _checkb(self._lib.hos_batch2d_set_reconstruction(self._h, 1 if first_order else 0))
 
     def set_gate(self, gate, threshold: float = 0.0, audit_log2: int = 10) -> None:
         """Attach a copy of a learned gate (FP32 batches); None detaches it."""

@@ -92,6 +92,7 @@ bool same(const Side& a, const Side& b) {
 struct Ctx2 {
     hos_solver2d* h = nullptr;
     int nx = 0, ny = 0, order = 0;
+    int use_df = 1;         // the solver's scheme: DF variants (1) or the non-DF WENO5-AO (0)
     double cfl = 0, tstop = 0;
     Side cur[4], pend[4];
     unsigned pend_mask = 0;
@@ -121,7 +122,10 @@ int tangent_order_of(Reconstruction_within_Cell_2D_tangent f) {
 // the problem parameters the globals and the Block2d describe (src/2Dproblem.cpp:7-81).
 // First_order_normal / _tangent (the drivers' step 0 when is_using_df_factor is set,
 // src/2Dproblem.cpp:733-745) run on the solver of the order whose Gauss points gausspoint
-// names, which the drivers then pair with their WENO-AO-DF scheme.
+// names, which the drivers then pair with their WENO-AO-DF scheme.  Without
+// is_using_df_factor the drivers keep their first slots, WENO5_AO_normal / WENO5_AO_tangent
+// (the non-DF WENO5-AO with the wenotype weights), and never call Update_alpha
+// (src/2Dproblem.cpp:37-38, 132-136, 154-157): the solver runs that scheme (use_df = 0).
 hos_params2d params2(const Block2d& b, int* order_out, int* first_order_out = nullptr) {
     const bool fo = cellreconstruction_2D_normal == First_order_normal;
     int order;
@@ -137,15 +141,22 @@ hos_params2d params2(const Block2d& b, int* order_out, int* first_order_out = nu
             stop(HOS_E_CONFIG, "cellreconstruction_2D_tangent must be the WENO-AO variant of the normal reconstruction's order");
     }
     if (first_order_out) *first_order_out = fo ? 1 : 0;
-    if (!is_using_df_factor)
-        stop(HOS_E_CONFIG, "the GPU path provides the discontinuity-feedback WENO-AO variants: set is_using_df_factor = true");
+    if (!is_using_df_factor) {
+        // the reference leaves the DF indicators at zero then; the GPU path runs the slots that
+        // do not read them
+        if (fo || cellreconstruction_2D_normal != WENO5_AO_normal || cellreconstruction_2D_tangent != WENO5_AO_tangent)
+            stop(HOS_E_CONFIG, "with is_using_df_factor = false the GPU path runs WENO5_AO_normal / WENO5_AO_tangent "
+                               "(the DF variants and first order update the DF indicators: set is_using_df_factor = true)");
+        if (gausspoint != 2)
+            stop(HOS_E_CONFIG, "WENO5_AO_tangent writes its Gauss points only with gausspoint = 2");
+    }
     if (g0reconstruction_2D_normal != Center_do_nothing_normal || g0reconstruction_2D_tangent != Center_all_collision_multi)
         stop(HOS_E_CONFIG, "the GPU path builds the GKS centre state by Center_all_collision_multi");
     if (flux_function_2d != GKS2D && flux_function_2d != LF2D)
         stop(HOS_E_CONFIG, "the GPU path provides the GKS2D and LF2D fluxes");
     if (tau_type != Euler && tau_type != NS) stop(HOS_E_CONFIG, "the GPU path provides the Euler and NS collision times");
-    if (tau_type == NS && flux_function_2d != GKS2D)
-        stop(HOS_E_CONFIG, "the GPU path provides the NS collision time with GKS2D (LF2D's viscous term is not provided)");
+    if (tau_type == NS && flux_function_2d == LF2D && !(Pr > 0))
+        stop(HOS_E_CONFIG, "LF2D's viscous term divides by Pr: set Pr > 0");
     int integrator = -1, stages = 0;
     const TimeMarchingCoefficient_2d methods[6] = {S2O4_2D, S1O1_2D, S1O2_2D, RK2_2D, RK3_2D, RK4_2D};
     const int method_stages[6] = {2, 1, 1, 2, 3, 4};
@@ -166,7 +177,8 @@ hos_params2d params2(const Block2d& b, int* order_out, int* first_order_out = nu
     p.order = order;
     p.gausspoint = gausspoint;
     p.characteristic = reconstruction_variable == characteristic ? 1 : 0;
-    p.use_df = 1;
+    p.use_df = is_using_df_factor ? 1 : 0;
+    p.wenotype = wenotype == wenojs ? HOS_WENO_JS : wenotype == linear ? HOS_WENO_LINEAR : HOS_WENO_Z;
     p.K = K;
     p.gamma = Gamma;
     p.c1_euler = c1_euler;
@@ -255,6 +267,7 @@ void create2(Ctx2& c, const Block2d& b, const Fluid2d* f) {
     c.nx = b.nx;
     c.ny = b.ny;
     c.order = order;
+    c.use_df = p.use_df;
     c.cfl = b.CFL;
     c.stepped = false;
     upload2(c, f, b.t);
@@ -377,6 +390,7 @@ void create1(Ctx1& c, const Block1d& b, const Fluid1d* f) {
     // (src/1Dproblem.cpp:103-106)
     p.df_mode = df ? 1 : (is_using_df_factor && b.step == 0 ? 2 : 0);
     p.update_alpha = is_using_df_factor ? 1 : 0;
+    p.wenotype = wenotype == wenojs ? HOS_WENO_JS : wenotype == linear ? HOS_WENO_LINEAR : HOS_WENO_Z;
     p.K = K;
     p.gamma = Gamma;
     p.c1_euler = c1_euler;
@@ -491,10 +505,13 @@ namespace {
 void update2(Fluid2d* fluids, Block2d block, int stage, bool source) {
     Ctx2& c = live2(fluids, "Update");
     if (stage != c.next) stop(HOS_E_CONFIG, "wrong middle stage,pls check the time marching setting");
+    if (is_using_df_factor && cellreconstruction_2D_normal == WENO5_AO_normal)
+        stop(HOS_E_CONFIG, "WENO5_AO_normal with is_using_df_factor = true: the GPU path runs the DF variants while "
+                           "the driver updates the DF indicators (assign WENO5_AO_with_df_normal / _tangent)");
     if (stage == 0) {
         int order = 0;
-        params2(block, &order);
-        if (order != c.order) {
+        const hos_params2d q = params2(block, &order);
+        if (order != c.order || q.use_df != c.use_df) {
             // a driver may pick its reconstruction after Get_CFL (src/2Dproblem.cpp:133-137);
             // before the first stage the solver is rebuilt for it with the same dt
             if (c.stepped) stop(HOS_E_CONFIG, "the reconstruction order changed under a running solver");
@@ -510,8 +527,9 @@ void update2(Fluid2d* fluids, Block2d block, int stage, bool source) {
     {
         // the slots may switch between first order and WENO-AO from one step to the next
         int order = 0, fo = 0;
-        params2(block, &order, &fo);
-        if (order != c.order) stop(HOS_E_CONFIG, "the reconstruction order changed under a running solver");
+        const hos_params2d q = params2(block, &order, &fo);
+        if (order != c.order || q.use_df != c.use_df)
+            stop(HOS_E_CONFIG, "the reconstruction order changed under a running solver");
         check2(hos2d_set_reconstruction(c.h, fo ? HOS_RECON_FIRST_ORDER : HOS_RECON_WENO), "Update");
         check2(hos2d_set_source(c.h, source ? 1 : 0), "Update_with_source");
     }

@@ -75,7 +75,9 @@ typedef struct hos_params2d {
     int order;              /* WENO-AO order: 5, 7 or 9                         */
     int gausspoint;         /* Gauss points per face                           */
     int characteristic;     /* reconstruction_variable: 1 characteristic, 0 conservative */
-    int use_df;             /* is_using_df_factor; must be 1                   */
+    int use_df;             /* is_using_df_factor: 1 the DF variants (WENO5/7/9), 0 the
+                               non-DF WENO5-AO the drivers install first (order 5, 2 Gauss
+                               points; WENO5_AO_normal / WENO5_AO_tangent) */
     int K;                  /* internal degrees of freedom                      */
     double gamma;           /* Gamma                                            */
     double c1_euler, c2_euler; /* numerical collision time tau_num = c1 dt + c2 dt |dp|/|p| */
@@ -101,7 +103,16 @@ typedef struct hos_params2d {
     double mu, nu;
     int prandtl_fix;
     double prandtl;
+    /* nonlinear weights of the non-DF WENO5-AO scheme (use_df = 0; the reference's wenotype
+     * global, src/reconstruction.cpp:7): HOS_WENO_Z, HOS_WENO_JS or HOS_WENO_LINEAR */
+    int wenotype;
 } hos_params2d;
+
+/* wenotype values (WENOtype, include/reconstruction.h in the reference: linear, wenojs,
+ * wenoz); zero is the Z-type weights every reference 2D driver selects */
+#define HOS_WENO_Z 0
+#define HOS_WENO_JS 1
+#define HOS_WENO_LINEAR 2
 
 #define HOS_TAU_EULER 0
 #define HOS_TAU_NS 1
@@ -225,6 +236,11 @@ const char* hos_gate_last_error(void);
  * threshold take the linear path; predicted-smooth cells whose hash has audit_log2 low zero
  * bits are re-checked with full weights */
 int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audit_log2);
+/* a-posteriori check of the linear path: a linear reconstruction is kept when its density and
+ * total energy lie within the three central cells' range widened by slack times that range
+ * (default 0.1; 0 accepts only values inside the range) and its temperature is positive;
+ * otherwise the full WENO-AO reconstruction replaces it.  No counterpart in the reference. */
+int hos2d_set_gate_check(hos_solver2d* s, double slack);
 /* counters since the last reset: cells gated x, y; predicted smooth x, y; audited; audited but
  * not smooth (false negatives of the gate); linear results rejected; (unused) */
 int hos2d_gate_stats(hos_solver2d* s, unsigned long long* stats, int reset);
@@ -253,6 +269,7 @@ typedef struct hos_params1d {
     double cfl;
     double left, right;
     int bc[2];            /* HOS_BC_FREE, HOS_BC_PERIODIC or HOS_BC_REFLECT, left and right */
+    int wenotype;         /* weights of the non-DF WENO5-AO steps: HOS_WENO_Z, _JS or _LINEAR */
 } hos_params1d;
 
 typedef struct hos_solver1d hos_solver1d;
@@ -312,6 +329,11 @@ typedef struct hos_params3d {
                                          HOS_BC_PERIODIC or HOS_BC_REFLECT                */
     int prandtl_fix;                  /* 1: Prandtl-number correction of the heat flux    */
     double prandtl;                   /* Pr (prandtl_fix = 1)                             */
+    /* 1 (FP64 only, no Prandtl fix): the reference's own GKS3D convention, which hands
+     * Convar_to_primvar_3D's pressure to every slot where lambda belongs (the Maxwellian
+     * moments, micro-slopes and collision times, src/flux_function.cpp:831-836, 914), to
+     * compare with outputs of the reference's 3D code; 0 (default): lambda, as 1D and 2D do */
+    int gks3d_pressure_slot;
 } hos_params3d;
 
 typedef struct hos_solver3d hos_solver3d;
@@ -373,6 +395,10 @@ int hos_batch2d_advance(hos_batch2d* b, int nsteps, int use_graph);
  * bad (negative density/pressure or NaN: the reference's exit) stops stepping; the others go
  * on.  With failed == NULL such a failure is reported as HOS_E_BLOWUP. */
 int hos_batch2d_status(hos_batch2d* b, int* active, double* t, int* last_step, int* failed);
+/* reconstruction of the following steps of every problem: HOS_RECON_WENO or
+ * HOS_RECON_FIRST_ORDER (the drivers' first-order step 0, as hos2d_set_reconstruction);
+ * waits for queued work */
+int hos_batch2d_set_reconstruction(hos_batch2d* b, int mode);
 /* attach a copy of a learned gate to an FP32 batch (NULL detaches); counters as hos2d_gate_stats */
 int hos_batch2d_set_gate(hos_batch2d* b, const hos_gate* g, float threshold, int audit_log2);
 int hos_batch2d_gate_stats(hos_batch2d* b, unsigned long long* stats, int reset);
@@ -389,12 +415,17 @@ const char* hos_batch2d_last_error(void);
  *   d_W        conserved state, SoA planes [4][nx*ny], ghosts included (in/out)
  *   d_alpha_x, d_alpha_y   DF indicators [nx*ny] (in/out; zero before the first step)
  *   dt         the step's time step (the caller's CFL choice)
- *   stream     cudaStream_t as void* (NULL: default stream); the call synchronises it
- * Problems with nodex or nodey above HOS_STATIC_MAX_NODE or ghost above
- * HOS_STATIC_MAX_GHOST are rejected with HOS_E_CONFIG.  The first call on a device sets up
- * that device (looks up the array's address); make it before any stream capture.  All
- * calls share the one array, so calls that overlap on the GPU race.  Errors are described
- * by hos_static_last_error(). */
+ *   stream     cudaStream_t as void* (NULL: default stream); each call waits for this stream
+ *              to finish before it returns (it reads the step's status word back)
+ * What it runs: S2O4 with the GKS2D flux, the DF variants (use_df = 1) of WENO5/7/9, Euler or
+ * Navier-Stokes collision time (with the Prandtl fix), boundary kinds HOS_BC_FREE,
+ * HOS_BC_PERIODIC, HOS_BC_REFLECT and HOS_BC_INFLOW.  Other settings (other time marching, LF,
+ * use_df = 0, wedge and no-slip sides), problems with nodex or nodey above
+ * HOS_STATIC_MAX_NODE and ghost above HOS_STATIC_MAX_GHOST are rejected with HOS_E_CONFIG.
+ * The first call on a device sets up that device (looks up the array's address); make it
+ * before any stream capture.  All calls share the one array and it keeps the last call's
+ * contents, so calls that overlap on the GPU (other streams, other host threads) race:
+ * serialise them per device.  Errors are described by hos_static_last_error(). */
 #define HOS_STATIC_MAX_NODE 256
 #define HOS_STATIC_MAX_GHOST 5
 int hos2d_step_static(const hos_params2d* params, int precision, double* d_W, double* d_alpha_x,

@@ -102,7 +102,11 @@ def test_bad_config_rejected_before_touching_cuda(lib):
     assert lib.hos2d_create(ctypes.byref(p), 0, ctypes.byref(h)) == hs.HOS_E_CONFIG
     p.gausspoint = 2
     p.use_df = 0
+    p.wenotype = 3  # HOS_WENO_Z, HOS_WENO_JS, HOS_WENO_LINEAR only
     assert lib.hos2d_create(ctypes.byref(p), 0, ctypes.byref(h)) == hs.HOS_E_CONFIG
+    # the non-DF scheme (the drivers' default slots) exists for WENO5 only
+    p7 = Problem2D(nodex=16, nodey=16, order=7, use_df=False).to_c()
+    assert lib.hos2d_create(ctypes.byref(p7), 0, ctypes.byref(h)) == hs.HOS_E_CONFIG
 
 
 def test_batch_sweep_is_seeded_and_in_range():

@@ -89,3 +89,21 @@ def test_gpu1d_fp32_close_to_fp64():
     a.close()
     b.close()
     assert np.abs(ra - rb).mean() / np.abs(ra).mean() <= 1e-4
+
+
+@pytest.mark.parametrize("wenotype", ["wenoz", "wenojs", "linear"])
+def test_gpu1d_nodf_wenotype_vs_oracle(wenotype):
+    """Non-DF WENO5-AO every step with each wenotype weight choice against the oracle."""
+    pb, con = cases.sod1d(200, order=5)
+    pb.df_mode, pb.wenotype = 0, wenotype
+    o = CpuStep1D("oracle").init(pb)
+    o.set_state(con)
+    s = Solver1D(pb, FP64)
+    s.set_state(con)
+    for _ in range(3):
+        o.step(0.2)
+        s.step(0.2)
+    s.sync()
+    got = s.get_state()["convar"]
+    s.close()
+    assert _rel(got, o.state()["convar"], pb.ghost) <= 1e-12

@@ -96,6 +96,40 @@ def test_gpu3d_fp64_matches_oracle(case):
     assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-11
 
 
+@pytest.mark.parametrize("name", ["ref3d_smooth_free_12", "ref3d_cubicsod_free_12", "ref3d_smooth_cons_ns_10"])
+def test_gpu3d_reference_convention_matches_reference_golden(name):
+    """The GPU with the reference's own GKS3D convention (gks3d_pressure_slot: pressure where
+    lambda belongs) against the outputs of the reference's 3D functions (tests/golden/ref3d_*,
+    run by oracle/ref_driver3d.cpp): 1e-12 relative L-inf after the first step, 1e-11 after
+    three, every dt to 1e-13.  No order reduction occurs on the faces the fluxes use there,
+    so the reference's never-cleared reduction flags do not enter."""
+    from pathlib import Path
+
+    from test_oracle3d_cpu import ref3d_problem
+
+    pb, _, steps = ref3d_problem(name)
+    pb.gks3d_pressure_slot = True
+    gold = np.load(Path(__file__).resolve().parent / "golden" / f"{name}.npz")
+    s = Solver3D(pb, FP64)
+    s.set_state(gold["convar0"])
+    for k in range(steps):
+        s.step()
+        dt = s.sync()[1]
+        np.testing.assert_allclose(dt, gold["dts"][k], rtol=1e-13)
+        got, ref = _interior(s.get_state()["convar"]), _interior(gold[f"convar{k + 1}"])
+        assert np.abs(got - ref).max() / np.abs(ref).max() <= (1e-12 if k == 0 else 1e-11), k
+    s.close()
+
+
+def test_gpu3d_reference_convention_needs_fp64():
+    from test_oracle3d_cpu import ref3d_problem
+
+    pb, _, _ = ref3d_problem("ref3d_smooth_free_12")
+    pb.gks3d_pressure_slot = True
+    with pytest.raises(HosError):
+        Solver3D(pb, FP32)
+
+
 @pytest.mark.parametrize("axis", [0, 1, 2])
 def test_gpu3d_sod_along_each_axis_matches_oracle(axis):
     dims = [4, 4, 4]

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from hos_gb300 import cases, gate_train
-from hos_gb300.solver import FP32, FP64, Gate, HosError, Solver2D
+from hos_gb300.solver import FP32, FP64, Gate, HosBlowUp, HosError, Solver2D
 from oracle_lib import gate_cells
 
 sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
@@ -26,7 +26,15 @@ def built():
 @pytest.fixture(scope="module")
 def trained():
     g, rep = gate_train.train(order=7, sizes=(64, 128), seeds=range(3), steps=60, sample_log2=2,
-                              train_steps=1500, batch=2048, capacity=1 << 21)
+                              train_steps=1500, batch=2048, capacity=1 << 21, fn_target=0.01)
+    yield g, rep
+    g.close()
+
+
+@pytest.fixture(scope="module")
+def trained5():
+    g, rep = gate_train.train(order=5, sizes=(128, 256), seeds=range(3), steps=80, sample_log2=3,
+                              train_steps=2000, batch=4096, capacity=1 << 21)
     yield g, rep
     g.close()
 
@@ -132,3 +140,59 @@ def test_gate_needs_the_fp32_path():
         s.set_gate(g)
     s.close()
     g.close()
+
+
+def _run(pb, con, prim, precision, steps, gate=None, threshold=0.0, slack=None):
+    s = Solver2D(pb, precision)
+    s.set_state(con, prim)
+    if gate is not None:
+        s.set_gate(gate, threshold, audit_log2=10)
+        if slack is not None:
+            s.set_gate_check(slack)
+    try:
+        s.advance(steps, 1e30, graph=True)
+        s.sync()
+        rho = s.get_state()["convar"][pb.ghost:-pb.ghost, pb.ghost:-pb.ghost, 0]
+    except HosBlowUp:
+        rho = None
+    s.close()
+    return rho
+
+
+def _ms_per_step(pb, con, prim, gate=None, threshold=0.0, steps=40):
+    import time
+    s = Solver2D(pb, FP32)
+    s.set_state(con, prim)
+    if gate is not None:
+        s.set_gate(gate, threshold, audit_log2=10)
+    s.advance(5, 1e30, graph=True)
+    s.sync()
+    t0 = time.perf_counter()
+    s.advance(steps, 1e30, graph=True)
+    s.sync()
+    ms = 1e3 * (time.perf_counter() - t0) / steps
+    s.close()
+    return ms
+
+
+def test_gate_gains_over_the_method_without_it(trained5):
+    """What the trained network gains over the method without it, on the 512^2 quadrant problem
+    (WENO5-AO-DF, characteristic, 80 steps):
+      speed    -- the gated FP32 step is faster than the plain FP32 step, which runs the full
+                  WENO-AO weights everywhere;
+      accuracy -- its density deviation from FP64 is far below that of linear weights
+                  everywhere, both as the reference's own wenotype = linear (non-DF WENO5-AO)
+                  and as a gate that sends every cell down the linear path."""
+    g, rep = trained5
+    pb, con, prim = cases.riemann2d(512, order=5)
+    ref = _run(pb, con, prim, FP64, 80)
+    dev = lambda r: np.inf if r is None else float(np.abs(r - ref).mean() / np.abs(ref).mean())
+    gated = dev(_run(pb, con, prim, FP32, 80, g, rep.threshold))
+    always = dev(_run(pb, con, prim, FP32, 80, g, -1e30, slack=10.0))
+    pb_lin, _, _ = cases.riemann2d(512, order=5)
+    pb_lin.use_df, pb_lin.wenotype = False, "linear"
+    linear = dev(_run(pb_lin, con, prim, FP32, 80))
+    assert gated <= 1e-3 and gated < 0.2 * linear and gated < 0.2 * always, (gated, linear, always)
+    t_plain = _ms_per_step(pb, con, prim)
+    t_gated = _ms_per_step(pb, con, prim, g, rep.threshold)
+    assert t_gated < t_plain, (t_gated, t_plain)

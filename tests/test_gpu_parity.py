@@ -1,7 +1,9 @@
 """GPU parity of the CUDA step against the oracle and the reference's golden vectors.
 
 Tolerances: the plain FP64 path must agree with the reference CPU solver to 1e-12 relative
-L-inf per step (max |W_gpu - W_ref| / max |W_ref| over interior cells, all 4 variables).
+L-inf per step (max |W_gpu - W_ref| / max |W_ref| over interior cells, all 4 variables), or to
+ten times the reference algorithm's own response to a 1e-15 perturbation of the initial state
+where the algorithm amplifies rounding beyond that (the viscous-cap case, the non-DF scheme).
 The FP32-bulk path is bounded separately (relative L1 of density vs the FP64 run)."""
 from pathlib import Path
 
@@ -15,6 +17,9 @@ from oracle_lib import CpuStep, interior, rel_linf
 pytestmark = pytest.mark.gpu
 GOLDEN = Path(__file__).resolve().parent / "golden"
 TOL_FP64 = 1e-12
+# DF indicators: the same 1e-12, relative to max(1, max |alpha|) (an indicator below 2 is zeroed,
+# so the values that survive are O(1) and carry the reconstruction's rounding)
+TOL_ALPHA = 1e-12
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -55,13 +60,32 @@ def oracle_run(pb, con, prim, nsteps, tstop=1e30):
     return st
 
 
-# The viscous-cap case: the reference algorithm itself carries a 1e-15 relative perturbation
-# of the initial state to ~4e-12 after three steps there (tau_num >> dt in the GKS time
-# coefficients; test_oracle_cpu.test_viscous_cap_case_amplifies_rounding), so after three steps
-# it is held to the rounding it amplifies; after one step to 1e-12 like every case.
-TOL_AFTER_3 = {"ns_w7_cap_24": 1e-10}
 
-GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem)
+def sensitivity(pb, con, prim, steps, first_order_steps=0, source=False):
+    """Relative L-inf change of the oracle's own state after ``steps`` steps when the initial
+    conserved state is perturbed by 1e-15 (relative, sin-pattern): how far the reference
+    algorithm itself carries rounding on this case.  It is ~2e-15 for the DF schemes and
+    reaches 1e-12 - 1e-10 for the viscous-cap case (tau_num >> dt in the GKS time
+    coefficients) and the non-DF WENO5-AO (test_oracle_cpu.test_*_amplifies_rounding)."""
+    out = []
+    for eps in (0.0, 1e-15):
+        o = CpuStep("oracle").init(pb, threads=8)
+        o.set_state(con * (1 + eps * np.sin(np.arange(con.size).reshape(con.shape))), prim)
+        o.fn("set_source")(1 if source else 0)
+        for k in range(steps):
+            o.fn("set_first_order")(1 if k < first_order_steps else 0)
+            o.step()
+        out.append(o.state()["convar"])
+    return rel_linf(out[1], out[0], pb)
+
+
+def tol_for(sens):
+    """The parity bound: 1e-12 relative L-inf, or ten times the reference algorithm's own
+    sensitivity to a 1e-15 perturbation where that is larger."""
+    return max(TOL_FP64, 10.0 * sens)
+
+GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if "accuracy" not in p.stem and "1d" not in p.stem
+              and not p.stem.startswith("ref3d"))
 
 
 def _golden_problem(name):
@@ -76,13 +100,15 @@ def test_gpu_matches_reference_golden(name):
     gold = np.load(GOLDEN / f"{name}.npz")
     fo, src = first_order_steps(name), with_source(name)
     s1 = gpu_run(pb, gold["convar0"], gold["primvar0"], 1, first_order_steps=fo, source=src)
-    assert rel_linf(s1["convar"], gold["convar1"], pb) <= TOL_FP64
+    t1 = tol_for(sensitivity(pb, gold["convar0"], gold["primvar0"], 1, fo, src))
+    assert rel_linf(s1["convar"], gold["convar1"], pb) <= t1
     s3 = gpu_run(pb, gold["convar0"], gold["primvar0"], 3, first_order_steps=fo, source=src)
-    assert rel_linf(s3["convar"], gold["convar3"], pb) <= TOL_AFTER_3.get(name, TOL_FP64)
+    t3 = tol_for(sensitivity(pb, gold["convar0"], gold["primvar0"], 3, fo, src))
+    assert rel_linf(s3["convar"], gold["convar3"], pb) <= t3
     np.testing.assert_allclose(s3["dts"], gold["dts"], rtol=1e-14, atol=0)
     for k in ("alpha_x3", "alpha_y3"):
         a, b = s3[k[:-1]], gold[k]
-        assert np.abs(a - b).max() <= 1e-9 * max(1.0, np.abs(b).max())
+        assert np.abs(a - b).max() <= max(TOL_ALPHA, t3) * max(1.0, np.abs(b).max()), (k, np.abs(a - b).max())
 
 
 @pytest.mark.parametrize("order", [5, 7, 9])
@@ -116,7 +142,7 @@ def test_gpu_single_step_from_midrun_state():
     got = s.get_state()
     s.close()
     assert rel_linf(got["convar"], nxt["convar"], pb) <= TOL_FP64
-    assert np.abs(got["alpha_x"] - nxt["alpha_x"]).max() <= 1e-9 * max(1.0, np.abs(nxt["alpha_x"]).max())
+    assert np.abs(got["alpha_x"] - nxt["alpha_x"]).max() <= TOL_ALPHA * max(1.0, np.abs(nxt["alpha_x"]).max())
 
 
 def test_gpu_inflow_reflect_boundaries():
@@ -302,3 +328,44 @@ def test_pinned_host_buffers_match_pageable():
         s.close()
     assert np.array_equal(outs[0], outs[1])
     assert np.abs(outs[1] - con).max() > 0   # the state moved
+
+
+@pytest.mark.parametrize("wenotype", ["wenoz", "wenojs", "linear"])
+@pytest.mark.parametrize("charac,bc", [(True, "free"), (False, "periodic"), (True, "reflect")])
+def test_gpu_nodf_parity_vs_oracle(wenotype, charac, bc):
+    """The reference drivers' default slots (is_using_df_factor = false): non-DF WENO5-AO
+    (WENO5_AO_normal / WENO5_AO_tangent) with each wenotype against the oracle, which is
+    bit-exact with the compiled reference for wenoz and wenojs.  The DF indicators stay zero
+    (Update_alpha is not called)."""
+    pb, con, prim = cases.random_riemann2d(40, seed=7 + len(bc), order=5)
+    pb.use_df, pb.wenotype, pb.characteristic, pb.bc = False, wenotype, charac, (bc,) * 4
+    ref = oracle_run(pb, con, prim, 3)
+    got = gpu_run(pb, con, prim, 3)
+    # the non-DF scheme carries a 1e-15 perturbation to 3e-12 - 7e-11 in three steps on these
+    # data (epsilon 1e-10 and the raw big-stencil indicator), so the bound follows it
+    assert rel_linf(got["convar"], ref["convar"], pb) <= tol_for(sensitivity(pb, con, prim, 3))
+    np.testing.assert_allclose(got["dts"], ref["dts"], rtol=1e-14)
+    assert not got["alpha_x"].any() and not got["alpha_y"].any()
+
+
+def test_gpu_nodf_differs_from_df():
+    """The non-DF scheme is a different scheme, not the DF one under another name."""
+    pb, con, prim = cases.random_riemann2d(40, seed=3, order=5)
+    a = gpu_run(pb, con, prim, 3)
+    pb.use_df = False
+    b = gpu_run(pb, con, prim, 3)
+    assert rel_linf(b["convar"], a["convar"], pb) > 1e-6
+
+
+@pytest.mark.parametrize("wenotype", ["wenoz", "wenojs"])
+def test_gpu_nodf_fp32_bulk_close_to_fp64(wenotype):
+    """FP32 bulk of the non-DF scheme stays within 1e-5 relative L1 (density) of FP64 after 20
+    steps of the isentropic vortex (the indicator of the big stencil is evaluated about the
+    centre value in FP32)."""
+    pb, con, prim = cases.isentropic_vortex(64, order=5)
+    pb.use_df, pb.wenotype = False, wenotype
+    a = gpu_run(pb, con, prim, 20)
+    b = gpu_run(pb, con, prim, 20, precision=FP32)
+    ra, rb = interior(pb, a["convar"][..., 0]), interior(pb, b["convar"][..., 0])
+    l1 = float(np.abs(rb - ra).mean() / np.abs(ra).mean())
+    assert l1 <= 1e-5, l1

@@ -35,9 +35,12 @@ def test_reference_api_2d_driver_matches_reference(drivers, name, mirror):
     np.testing.assert_allclose(r["dts"], gold["dts"], rtol=1e-12, atol=0)
     assert abs(r["t"] - float(gold["t"])) <= 1e-12 * abs(float(gold["t"]))
     g = pb.ghost
-    assert _rel(r["convar"][g:-g, g:-g], gold["convar"][g:-g, g:-g]) <= 1e-12
+    # the non-DF scheme carries rounding far more than the DF ones (3e-12 - 7e-11 after three
+    # steps for a 1e-15 perturbation): its runs are held to 1e-10
+    tol = 1e-10 if "nodf" in name else 1e-12
+    assert _rel(r["convar"][g:-g, g:-g], gold["convar"][g:-g, g:-g]) <= tol
     if mirror:  # copied back every step: primvar as the reference leaves it (last stage's start)
-        assert _rel(r["primvar"][g:-g, g:-g], gold["primvar"][g:-g, g:-g]) <= 1e-12
+        assert _rel(r["primvar"][g:-g, g:-g], gold["primvar"][g:-g, g:-g]) <= tol
     for key in ("alpha_x", "alpha_y"):
         assert np.abs(r[key] - gold[key]).max() <= 1e-9 * max(1.0, np.abs(gold[key]).max()), key
 

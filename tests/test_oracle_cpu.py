@@ -258,6 +258,27 @@ def test_oblique_shock_states_reduce_to_reference_constants():
     assert abs(p1 * (2 * g * m2 - (g - 1)) / (g + 1) - 116.5) < 1e-12
 
 
+@pytest.mark.parametrize("name", ["nodf_w5_z_free_24", "nodf_w5_z_cons_20"])
+def test_nodf_scheme_amplifies_rounding(name):
+    """The non-DF WENO5-AO (epsilon 1e-10 in the weights, the big-stencil indicator as a raw
+    quadratic form with coefficients ~1e5) carries a 1e-15 relative perturbation of the initial
+    state past 1e-13 within three steps, where the DF variant of the same data stays near 1e-15:
+    that bounds how closely any other arithmetic can follow the reference there."""
+    pb, con, prim = _problem(name)
+    dev = {}
+    for df in (False, True):
+        pb.use_df = df
+        runs = []
+        for eps in (0.0, 1e-15):
+            o = CpuStep("oracle").init(pb, threads=4)
+            o.set_state(con * (1 + eps * np.sin(np.arange(con.size).reshape(con.shape))), prim)
+            for _ in range(3):
+                o.step()
+            runs.append(o.state()["convar"])
+        dev[df] = rel_linf(runs[1], runs[0], pb)
+    assert dev[False] > 1e-13 and dev[True] < 1e-14, dev
+
+
 def test_viscous_cap_case_amplifies_rounding():
     """In the viscous-cap case the algorithm amplifies rounding: a 1e-15 relative perturbation
     of the initial state grows past 1e-13 within three steps (the GKS time coefficients
