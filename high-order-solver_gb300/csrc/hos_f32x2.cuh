@@ -1,0 +1,104 @@
+// hos_f32x2.cuh -- two FP32 lanes in one register pair, computed with Blackwell's paired FP32
+// instructions (fma / add / mul / sub .f32x2): one issue slot performs the operation on both
+// lanes.  The FP32 face kernels are issue bound, so the hot arithmetic (the GKS flux of two
+// Gauss points, the linear reconstruction of two variables) runs on F2 values.
+//
+// Every lane rounds as the scalar FP32 operation of that lane.  A product is kept unevaluated
+// (P2) until it meets an addition, so a * b + c becomes one fused multiply-add as in the
+// contracted scalar code; a product used on its own is rounded by a paired multiply.  The paired
+// instructions take no negated operands (a negated pair costs two scalar instructions), so a
+// difference with a product is a paired multiply and a paired subtraction, and -x is 0 - x.
+// Transcendental functions, square roots and divisions run per lane with the scalar FP32
+// routines.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace hos {
+
+struct F2 {
+    float2 v;
+    F2() = default;
+    __device__ __forceinline__ F2(float2 a) : v(a) {}
+    __device__ __forceinline__ F2(float a, float b) : v(make_float2(a, b)) {}
+    // broadcasts: T(c) of the templated math gives the same constant in both lanes
+    __device__ __forceinline__ explicit F2(double a) : v(make_float2((float)a, (float)a)) {}
+    __device__ __forceinline__ explicit F2(float a) : v(make_float2(a, a)) {}
+    __device__ __forceinline__ explicit F2(int a) : v(make_float2((float)a, (float)a)) {}
+};
+
+namespace f2op {
+__device__ __forceinline__ F2 fma(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
+__device__ __forceinline__ F2 add(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 mul(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 sub(F2 a, F2 b) {
+    unsigned long long d;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<const unsigned long long*>(&a.v)), "l"(*reinterpret_cast<const unsigned long long*>(&b.v)));
+    return F2(*reinterpret_cast<const float2*>(&d));
+}
+}  // namespace f2op
+
+// an unevaluated product a * b
+struct P2 {
+    F2 a, b;
+    __device__ __forceinline__ operator F2() const { return f2op::mul(a, b); }
+};
+
+__device__ __forceinline__ F2 operator-(F2 a) { return f2op::sub(F2(0.0f), a); }
+__device__ __forceinline__ F2 operator-(P2 p) { return -F2(p); }
+
+__device__ __forceinline__ P2 operator*(F2 a, F2 b) { return P2{a, b}; }
+__device__ __forceinline__ P2 operator*(P2 p, F2 b) { return P2{F2(p), b}; }
+__device__ __forceinline__ P2 operator*(F2 a, P2 q) { return P2{a, F2(q)}; }
+__device__ __forceinline__ P2 operator*(P2 p, P2 q) { return P2{F2(p), F2(q)}; }
+
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return f2op::add(a, b); }
+__device__ __forceinline__ F2 operator+(P2 p, F2 c) { return f2op::fma(p.a, p.b, c); }
+__device__ __forceinline__ F2 operator+(F2 c, P2 p) { return f2op::fma(p.a, p.b, c); }
+__device__ __forceinline__ F2 operator+(P2 p, P2 q) { return f2op::fma(p.a, p.b, F2(q)); }
+
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return f2op::sub(a, b); }
+__device__ __forceinline__ F2 operator-(P2 p, F2 c) { return f2op::sub(F2(p), c); }
+__device__ __forceinline__ F2 operator-(F2 c, P2 p) { return f2op::sub(c, F2(p)); }
+__device__ __forceinline__ F2 operator-(P2 p, P2 q) { return f2op::sub(F2(p), F2(q)); }
+
+__device__ __forceinline__ F2 operator/(F2 a, F2 b) { return F2(a.v.x / b.v.x, a.v.y / b.v.y); }
+__device__ __forceinline__ F2 operator/(P2 p, F2 b) { return F2(p) / b; }
+__device__ __forceinline__ F2 operator/(F2 a, P2 q) { return a / F2(q); }
+__device__ __forceinline__ F2 operator/(P2 p, P2 q) { return F2(p) / F2(q); }
+
+__device__ __forceinline__ F2& operator+=(F2& a, F2 b) { return a = a + b; }
+__device__ __forceinline__ F2& operator+=(F2& a, P2 p) { return a = a + p; }
+__device__ __forceinline__ F2& operator-=(F2& a, F2 b) { return a = a - b; }
+__device__ __forceinline__ F2& operator*=(F2& a, F2 b) { return a = F2(a * b); }
+
+// per-lane functions (the global FP32 / FP64 overloads stay visible beside them)
+using ::sqrt;
+using ::exp;
+using ::erfc;
+__device__ __forceinline__ F2 sqrt(F2 a) { return F2(sqrtf(a.v.x), sqrtf(a.v.y)); }
+__device__ __forceinline__ F2 exp(F2 a) { return F2(expf(a.v.x), expf(a.v.y)); }
+__device__ __forceinline__ F2 erfc(F2 a) { return F2(erfcf(a.v.x), erfcf(a.v.y)); }
+__device__ __forceinline__ F2 fabsT(F2 a) { return F2(fabsf(a.v.x), fabsf(a.v.y)); }
+__device__ __forceinline__ F2 fminT(F2 a, F2 b) { return F2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y)); }
+__device__ __forceinline__ F2 fmaxT(F2 a, F2 b) { return F2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y)); }
+
+// FP32 -> FP64 conversion on the integer pipes, for the FP32 kernels' FP64 stage combination
+// (there the FP64 pipe, which also runs the conversion instruction, is the bound): exact for
+// every normal FP32 value and zero; FP32 subnormals read as signed zero (the FP32 kernels flush
+// them); infinities and NaNs keep their class and payload.
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const unsigned u = __float_as_uint(x), m = u & 0x7fffffffu;
+    unsigned hi = (m >> 3) + 0x38000000u;                  // exponent bias 127 -> 1023
+    if (m >= 0x7f800000u) hi = (m >> 3) | 0x7ff00000u;     // infinity, NaN
+    unsigned lo = u << 29;
+    if (m < 0x00800000u) hi = lo = 0u;                     // zero, subnormal
+    return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
+}
+
+// the scalar type of a compute type: the uniform parameters of the templated math
+template <class T> struct ScalarOf { using type = T; };
+template <> struct ScalarOf<F2> { using type = float; };
+
+}  // namespace hos

@@ -2,6 +2,7 @@
 // GPU (forward on the tensor cores, backward and Adam on the FP32 cores) and the per-stage
 // gate launch.  The solver couples it to a problem in hos_solver.cu (hos2d_set_gate,
 // hos_gate_collect).  The reference has no counterpart.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -175,16 +176,22 @@ __global__ void adam_kernel(float* params, float* m, float* v, float* grad, int 
 
 cudaError_t launch_gate(int order, const GateArgs& a, const Net& net, const Geometry& geo, cudaStream_t s,
                         const CUtensorMap* tm) {
-    const dim3 blocks((geo.ny + GATE_TILE - 1) / GATE_TILE, (geo.nx + GATE_TILE - 1) / GATE_TILE);
+    // the resident blocks of the current device (blocks per SM: the kernels' launch bounds)
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int ntx = (geo.ny + GATE_TILE - 1) / GATE_TILE, ntiles = ntx * ((geo.nx + GATE_TILE - 1) / GATE_TILE);
+    const int grid = std::min(ntiles, sms * (order == 9 ? 2 : 3));
     if (tm) {
-        if (order == 5) gate_kernel_tma<5><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo, *tm);
-        else if (order == 7) gate_kernel_tma<7><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo, *tm);
-        else gate_kernel_tma<9><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo, *tm);
+        if (order == 5) gate_kernel_tma<5><<<grid, GATE_THREADS, 0, s>>>(a, net, geo, ntx, ntiles, *tm);
+        else if (order == 7) gate_kernel_tma<7><<<grid, GATE_THREADS, 0, s>>>(a, net, geo, ntx, ntiles, *tm);
+        else gate_kernel_tma<9><<<grid, GATE_THREADS, 0, s>>>(a, net, geo, ntx, ntiles, *tm);
         return cudaGetLastError();
     }
-    if (order == 5) gate_kernel<5><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
-    else if (order == 7) gate_kernel<7><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
-    else gate_kernel<9><<<blocks, GATE_THREADS, 0, s>>>(a, net, geo);
+    if (order == 5) gate_kernel<5><<<grid, GATE_THREADS, 0, s>>>(a, net, geo, ntx, ntiles);
+    else if (order == 7) gate_kernel<7><<<grid, GATE_THREADS, 0, s>>>(a, net, geo, ntx, ntiles);
+    else gate_kernel<9><<<grid, GATE_THREADS, 0, s>>>(a, net, geo, ntx, ntiles);
     return cudaGetLastError();
 }
 

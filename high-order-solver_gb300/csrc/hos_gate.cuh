@@ -414,10 +414,12 @@ struct GateBox {
 
 // tmap (TMA): the mirror's tensor map with the GateBox<ORDER> box; the tile is then staged by
 // one TMA tile load instead of per-cell loads of the mirror
+// iter: tiles this block handled before (TMA: the load barrier is initialised on the first and
+// its phase parity follows the count).
 template <int ORDER, bool TMA = false>
 __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo, int i0, int j0, unsigned tile_id,
                                           MlpTc& mlp, unsigned& phase, bool& broken,
-                                          const CUtensorMap* tmap = nullptr) {
+                                          const CUtensorMap* tmap = nullptr, int iter = 0) {
     constexpr int r = ORDER / 2, H = GATE_TILE + 2 * r;
     __shared__ float srho[H][H + 1], sp[H][H + 1];
     __shared__ float salpha[2][GATE_TILE * GATE_TILE];   // TMA: the tile cells' alpha_x, alpha_y
@@ -433,17 +435,22 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo
         __shared__ __align__(8) uint64_t gbar;
         float* stg = reinterpret_cast<float*>(mlp.act);
         const int x0 = j0 - r, y0 = i0 - r, xa = x0 & ~3, off = x0 - xa;   // negative origins read zeros
-        if (tid == 0) {
-            mbar_init(&gbar, 1);
-            mbar_expect_tx(&gbar, B::bytes);
-            tma_load_3d(stg, tmap, xa, y0, 0, &gbar);
-        }
-        __syncthreads();
-        if (!__syncthreads_and(mbar_wait(&gbar, 0))) {
-            // the load did not complete: let a late one land, and flag no cell of the kernel
-            // smooth (the network is skipped; the caller records the timeout)
-            mbar_wait(&gbar, 0);
-            broken = true;
+        const unsigned par = (unsigned)iter & 1u;
+        // after a load that did not complete (broken, uniform over the block) the barrier's phase
+        // is unknown: no further loads are issued, and the network is skipped for the rest
+        if (!broken) {
+            if (tid == 0) {
+                if (iter == 0) mbar_init(&gbar, 1);
+                mbar_expect_tx(&gbar, B::bytes);
+                tma_load_3d(stg, tmap, xa, y0, 0, &gbar);
+            }
+            __syncthreads();
+            if (!__syncthreads_and(mbar_wait(&gbar, par))) {
+                // the load did not complete: let a late one land, and flag no cell of the kernel
+                // smooth (the network is skipped; the caller records the timeout)
+                mbar_wait(&gbar, par);
+                broken = true;
+            }
         }
         for (int e = tid; e < H * H; e += GATE_THREADS) {
             const int hi = e / H, hj = e % H;
@@ -585,31 +592,35 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo
     __syncthreads();   // the shared arrays are reused by the block's next tile
 }
 
-// One block per 16 x 16 tile.  The kernel is latency bound (global loads, the two MMA round
-// trips): WENO5/7 tiles fit three blocks per SM in registers, WENO9 two.
+// Persistent blocks (a grid of resident blocks) walk the 16 x 16 tiles, so the network's
+// set-up (weights into the operand layouts, tensor memory, barrier) happens once per block.  The
+// kernel is latency bound (the tile loads, the two MMA round trips): WENO5/7 tiles fit three
+// blocks per SM in registers, WENO9 two.  ntx: tiles along j; ntiles: all tiles.
 template <int ORDER>
-__global__ void __launch_bounds__(GATE_THREADS, ORDER == 9 ? 2 : 3) gate_kernel(GateArgs a, Net net, Geometry geo) {
+__global__ void __launch_bounds__(GATE_THREADS, ORDER == 9 ? 2 : 3)
+    gate_kernel(GateArgs a, Net net, Geometry geo, int ntx, int ntiles) {
     __shared__ MlpTc mlp;
     if (a.ctl && !a.ctl->active) return;   // uniform: nothing allocated yet
     mlp_tc_setup(mlp, net);
     unsigned phase = 0;
     bool broken = false;
-    gate_tile<ORDER>(a, geo, blockIdx.y * GATE_TILE, blockIdx.x * GATE_TILE, blockIdx.y * gridDim.x + blockIdx.x, mlp,
-                     phase, broken);
+    for (int k = blockIdx.x; k < ntiles; k += gridDim.x)
+        gate_tile<ORDER>(a, geo, (k / ntx) * GATE_TILE, (k % ntx) * GATE_TILE, (unsigned)k, mlp, phase, broken);
     mlp_tc_teardown(mlp, phase, broken);
 }
 
-// the FP32 solvers' gate: the tile staged from the FP32 mirror by one TMA tile load
+// the FP32 solvers' gate: each tile staged from the FP32 mirror by one TMA tile load
 template <int ORDER>
 __global__ void __launch_bounds__(GATE_THREADS, ORDER == 9 ? 2 : 3)
-    gate_kernel_tma(GateArgs a, Net net, Geometry geo, const __grid_constant__ CUtensorMap tmap) {
+    gate_kernel_tma(GateArgs a, Net net, Geometry geo, int ntx, int ntiles, const __grid_constant__ CUtensorMap tmap) {
     __shared__ MlpTc mlp;
     if (a.ctl && !a.ctl->active) return;   // uniform: nothing allocated yet
     mlp_tc_setup(mlp, net);
     unsigned phase = 0;
     bool broken = false;
-    gate_tile<ORDER, true>(a, geo, blockIdx.y * GATE_TILE, blockIdx.x * GATE_TILE, blockIdx.y * gridDim.x + blockIdx.x,
-                           mlp, phase, broken, &tmap);
+    for (int k = blockIdx.x, it = 0; k < ntiles; k += gridDim.x, ++it)
+        gate_tile<ORDER, true>(a, geo, (k / ntx) * GATE_TILE, (k % ntx) * GATE_TILE, (unsigned)k, mlp, phase, broken,
+                               &tmap, it);
     mlp_tc_teardown(mlp, phase, broken);
 }
 

@@ -11,6 +11,7 @@
 // 7x7x3 tables: the entry (i, j, k) is uplus[i] * vwhole[j] * xi_k exactly as the table
 // constructor computes it, so only the entries the contractions touch are ever evaluated.
 #pragma once
+#include <type_traits>
 #include "hos_weno.cuh"
 
 namespace hos {
@@ -52,12 +53,26 @@ template <class T> struct Mom {
 // table selectors: 0 = u > 0 half space, 1 = u < 0 half space, 2 = whole space.  The
 // reference's whole-space table is uplus*v + uminus*v, equal to uwhole*v to within one
 // rounding; the whole-space recurrence is used directly.
+//
+// For the paired FP32 type the unit factors vw[0] = uw[0] = 1 are left out (x * 1 == x, but a
+// paired multiply is not folded away); the scalar types keep the products as written.
 template <class T, int TAB>
 __device__ __forceinline__ T M(const Mom<T>& m, int i, int j, int k) {
-    const T xk = k == 0 ? T(1) : k == 1 ? m.xi2 : m.xi4;
-    if (TAB == 0) return k == 0 ? m.up[i] * m.vw[j] : m.up[i] * m.vw[j] * xk;
-    if (TAB == 1) return k == 0 ? m.un[i] * m.vw[j] : m.un[i] * m.vw[j] * xk;
-    return k == 0 ? m.uw[i] * m.vw[j] : m.uw[i] * m.vw[j] * xk;
+    if constexpr (std::is_same<T, F2>::value) {
+        const T xk = k == 1 ? m.xi2 : m.xi4;
+        const T& ui = TAB == 0 ? m.up[i] : TAB == 1 ? m.un[i] : m.uw[i];
+        if (TAB == 2 && i == 0) {
+            if (j == 0) return k == 0 ? T(1) : xk;
+            return k == 0 ? m.vw[j] : T(m.vw[j] * xk);
+        }
+        if (j == 0) return k == 0 ? ui : T(ui * xk);
+        return k == 0 ? T(ui * m.vw[j]) : T(ui * m.vw[j] * xk);
+    } else {
+        const T xk = k == 0 ? T(1) : k == 1 ? m.xi2 : m.xi4;
+        if (TAB == 0) return k == 0 ? m.up[i] * m.vw[j] : m.up[i] * m.vw[j] * xk;
+        if (TAB == 1) return k == 0 ? m.un[i] * m.vw[j] : m.un[i] * m.vw[j] * xk;
+        return k == 0 ? m.uw[i] * m.vw[j] : m.uw[i] * m.vw[j] * xk;
+    }
 }
 
 // moment contraction <a psi u^NU v^NV> (GL_address / GR_address / G_address, :603-636)
@@ -124,20 +139,106 @@ __device__ __forceinline__ T tau_ratio(T dl, T dr, T ll, T lr, T c2) {
     const T a = dl / ll, b = dr / lr;
     return c2 * fabsT(a - b) / fabsT(a + b);
 }
-template <class T>
-__device__ __forceinline__ T tau_num(T Cc, T dt, T c1, T c2) {
-    if (c1 <= T(0) && c2 <= T(0)) return T(0.0);
-    return c1 * dt + dt * Cc;
+template <class T, class S>
+__device__ __forceinline__ T tau_num(T Cc, T dt, S c1, S c2) {
+    if (c1 <= S(0) && c2 <= S(0)) return T(0.0);
+    return T(c1) * dt + dt * Cc;
 }
 
 // Gauss-point state: convar[4], der1x[4], der1y[4] of one side
 template <class T> struct GState { T w[4], dx[4], dy[4]; };
 
+// The centre (g0) part and the time integration of GKS2D's Euler form at one Gauss point
+// (src/flux_function.cpp:410-690 with tau = 0): from the collision state w0 and its slopes c0x,
+// c0y, the sides' <u psi> moments gl, gr (SUMMED: gl already holds rl gl + rr gr; gr unused),
+// the <a u^2 + a u v> terms t1s, and the sides' densities rl, rr and lambdas ll, lr.
+template <class T, bool SUMMED = false>
+__device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y, const T* gl, const T* gr,
+                                         const T* t1s, T rl, T rr, T ll, T lr, T dt, T K,
+                                         typename ScalarOf<T>::type c1, typename ScalarOf<T>::type c2, T* fo,
+                                         T* dfo) {
+    const GasK<T> gk(K);
+    T p0[4];
+    to_ulambda(p0, w0, K);
+    T g0u[4], t4s[4], A0u[4];
+    {
+        Mom<T> m0;
+        m0.init_whole(p0[1], p0[2], p0[3], K);
+        contract_unit<T, 2, 1, 0>(m0, g0u);
+        T a0x[4], a0y[4], a0xu[4], a0xuu[4], a0yv[4], a0yuv[4];
+        microslope(a0x, c0x, p0, gk);
+        contract<T, 2, 1, 0>(m0, a0x, a0xu);
+        contract<T, 2, 2, 0>(m0, a0x, a0xuu);
+        microslope(a0y, c0y, p0, gk);
+        contract<T, 2, 0, 1>(m0, a0y, a0yv);
+        contract<T, 2, 1, 1>(m0, a0y, a0yuv);
+        T dA0[4], A0[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            t4s[v] = a0xuu[v] + a0yuv[v];
+            dA0[v] = -p0[0] * (a0xu[v] + a0yv[v]);
+        }
+        microslope(A0, dA0, p0, gk);
+        contract<T, 2, 1, 0>(m0, A0, A0u);
+    }
+    // time-integration coefficients for tau = 0 (Euler) at dt and dt/2
+    T F0[4], F1[4];
+    const T Cc = tau_ratio(rl, rr, ll, lr, T(c2));
+    {
+        const T tn = tau_num(Cc, dt, c1, c2);
+        const T eta = exp(-dt / tn);
+        const T t0 = tn * (T(1) - eta);
+        const T t1 = tn * (eta * (dt + tn) - tn);
+        const T t3 = tn * eta + dt - tn;
+        const T t4 = tn * (tn - eta * (dt + tn));
+        const T t5 = T(0.5) * dt * dt;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            T f;
+            if constexpr (SUMMED) f = t0 * gl[v];
+            else f = rl * t0 * gl[v] + rr * t0 * gr[v];
+            f = f + p0[0] * t3 * g0u[v];
+            f = f + t1 * t1s[v];
+            f = f + p0[0] * t4 * t4s[v];
+            f = f + p0[0] * t5 * A0u[v];
+            F0[v] = f;
+        }
+    }
+    {
+        const T dt2 = T(0.5) * dt;
+        const T tn = tau_num(Cc, dt2, c1, c2);
+        const T eta = exp(-dt2 / tn);
+        const T t0 = tn * (T(1) - eta);
+        const T t1 = tn * (eta * (dt2 + tn) - tn);
+        const T t3 = tn * eta + dt2 - tn;
+        const T t4 = tn * (tn - eta * (dt2 + tn));
+        const T t5 = T(0.5) * dt2 * dt2;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            T f;
+            if constexpr (SUMMED) f = t0 * gl[v];
+            else f = t0 * (rl * gl[v] + rr * gr[v]);
+            f = f + t1 * t1s[v];
+            f = f + p0[0] * t3 * g0u[v];
+            f = f + p0[0] * t4 * t4s[v];
+            f = f + p0[0] * t5 * A0u[v];
+            F1[v] = f;
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        fo[v] = (T(4.0) * F1[v] - F0[v]);
+        dfo[v] = T(4.0) * (F0[v] - T(2.0) * F1[v]);
+    }
+}
+
 // Time-integrated GKS flux at one Gauss point: fo = 4 F(dt/2) - F(dt),
-// dfo = 4 (F(dt) - 2 F(dt/2)) (src/flux_function.cpp:686-690).
+// dfo = 4 (F(dt) - 2 F(dt/2)) (src/flux_function.cpp:686-690).  T = F2 computes two Gauss
+// points at once (c1, c2 stay scalars: the launch's collision coefficients).
 template <class T>
-__device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R, T dt, T K, T c1, T c2,
-                                          T* fo, T* dfo) {
+__device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R, T dt, T K,
+                                          typename ScalarOf<T>::type c1, typename ScalarOf<T>::type c2, T* fo,
+                                          T* dfo) {
     const GasK<T> gk(K);
     T pl[4], pr[4], p0[4];
     to_ulambda(pl, L.w, K);
@@ -180,73 +281,63 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
 #pragma unroll
         for (int v = 0; v < 4; ++v) t1s[v] = pl[0] * (q0[v] + q2[v]) + pr[0] * (q1[v] + q3[v]);
     }
-    to_ulambda(p0, w0, K);
-    T g0u[4], t4s[4], A0u[4];
-    {
-        Mom<T> m0;
-        m0.init_whole(p0[1], p0[2], p0[3], K);
-        contract_unit<T, 2, 1, 0>(m0, g0u);
-        T a0x[4], a0y[4], a0xu[4], a0xuu[4], a0yv[4], a0yuv[4];
-        microslope(a0x, c0x, p0, gk);
-        contract<T, 2, 1, 0>(m0, a0x, a0xu);
-        contract<T, 2, 2, 0>(m0, a0x, a0xuu);
-        microslope(a0y, c0y, p0, gk);
-        contract<T, 2, 0, 1>(m0, a0y, a0yv);
-        contract<T, 2, 1, 1>(m0, a0y, a0yuv);
-        T dA0[4], A0[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            t4s[v] = a0xuu[v] + a0yuv[v];
-            dA0[v] = -p0[0] * (a0xu[v] + a0yv[v]);
-        }
-        microslope(A0, dA0, p0, gk);
-        contract<T, 2, 1, 0>(m0, A0, A0u);
-    }
-    // time-integration coefficients for tau = 0 (Euler) at dt and dt/2
-    T F0[4], F1[4];
-    const T Cc = tau_ratio(pl[0], pr[0], pl[3], pr[3], c2);
-    {
-        const T tn = tau_num(Cc, dt, c1, c2);
-        const T eta = exp(-dt / tn);
-        const T t0 = tn * (T(1) - eta);
-        const T t1 = tn * (eta * (dt + tn) - tn);
-        const T t3 = tn * eta + dt - tn;
-        const T t4 = tn * (tn - eta * (dt + tn));
-        const T t5 = T(0.5) * dt * dt;
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            T f = pl[0] * t0 * glu[v] + pr[0] * t0 * gru[v];
-            f = f + p0[0] * t3 * g0u[v];
-            f = f + t1 * t1s[v];
-            f = f + p0[0] * t4 * t4s[v];
-            f = f + p0[0] * t5 * A0u[v];
-            F0[v] = f;
-        }
-    }
-    {
-        const T dt2 = T(0.5) * dt;
-        const T tn = tau_num(Cc, dt2, c1, c2);
-        const T eta = exp(-dt2 / tn);
-        const T t0 = tn * (T(1) - eta);
-        const T t1 = tn * (eta * (dt2 + tn) - tn);
-        const T t3 = tn * eta + dt2 - tn;
-        const T t4 = tn * (tn - eta * (dt2 + tn));
-        const T t5 = T(0.5) * dt2 * dt2;
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            T f = t0 * (pl[0] * glu[v] + pr[0] * gru[v]);
-            f = f + t1 * t1s[v];
-            f = f + p0[0] * t3 * g0u[v];
-            f = f + p0[0] * t4 * t4s[v];
-            f = f + p0[0] * t5 * A0u[v];
-            F1[v] = f;
-        }
-    }
+    gks_tail<T>(w0, c0x, c0y, glu, gru, t1s, pl[0], pr[0], pl[3], pr[3], dt, K, c1, c2, fo, dfo);
+}
+
+// FP32 GKS2D (Euler form) at one Gauss point with the two sides in the two lanes of the paired
+// FP32 type: lane x carries the left state and the u > 0 half space of its Maxwellian, lane y
+// the right state and the u < 0 half space of its own.  The side terms of the collision, its
+// slopes and the <u psi> and <a u^2 + a u v> moments are formed on both lanes at once and
+// summed across them; the centre part (one state) is scalar.  The u < 0 half-space moments
+// follow the same recurrence as the u > 0 ones (0.5 erfc(+sqrt(lambda) u) and the opposite sign
+// of the boundary term), not 1 - up and uw - up.
+__device__ __forceinline__ void gks_point_lr(const GState<float>& L, const GState<float>& R, float dt, float K,
+                                             float c1, float c2, float* fo, float* dfo) {
+    const F2 Kp(K);
+    const GasK<F2> gk(Kp);
+    F2 w[4], sx[4], sy[4], ps[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        fo[v] = (T(4.0) * F1[v] - F0[v]);
-        dfo[v] = T(4.0) * (F0[v] - T(2.0) * F1[v]);
+        w[v] = F2(L.w[v], R.w[v]);
+        sx[v] = F2(L.dx[v], R.dx[v]);
+        sy[v] = F2(L.dy[v], R.dy[v]);
     }
+    to_ulambda(ps, w, Kp);
+    const F2 r = ps[0];
+    auto hs = [](F2 a) { return a.v.x + a.v.y; };
+    float w0[4], c0x[4], c0y[4], gs[4], t1s[4];
+    {
+        constexpr double pi = 3.14159265358979323846;
+        Mom<F2> m;   // up[] holds the lanes' half-space moments
+        const F2 u = ps[1], lam = ps[3], ol = F2(1.0f) / lam;
+        m.whole(u, ps[2], ol, Kp);
+        m.up[0] = F2(0.5f) * erfc(F2(-1.0f, 1.0f) * sqrt(lam) * u);
+        m.up[1] = u * m.up[0] + F2(0.5f, -0.5f) * (exp(-(lam * u * u)) / sqrt(F2(pi) * lam));
+#pragma unroll
+        for (int i = 2; i <= 6; ++i) m.up[i] = u * m.up[i - 1] + F2(0.5 * (i - 1)) * ol * m.up[i - 2];
+        w0[0] = hs(r * m.up[0]);
+        w0[1] = hs(r * m.up[1]);
+        w0[2] = hs(r * m.vw[1] * m.up[0]);
+        w0[3] = hs(F2(0.5f) * r * (m.up[2] + m.up[0] * m.vw[2] + m.up[0] * m.xi2));
+        F2 ax[4], ay[4], q[4], q2[4];
+        microslope(ax, sx, ps, gk);
+        microslope(ay, sy, ps, gk);
+        contract<F2, 0, 0, 0>(m, ax, q);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c0x[v] = hs(r * q[v]);
+        contract<F2, 0, 0, 0>(m, ay, q);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c0y[v] = hs(r * q[v]);
+        contract_unit<F2, 0, 1, 0>(m, q);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) gs[v] = hs(r * q[v]);
+        contract<F2, 0, 2, 0>(m, ax, q);    // <a_x u^2>
+        contract<F2, 0, 1, 1>(m, ay, q2);   // <a_y u v>
+#pragma unroll
+        for (int v = 0; v < 4; ++v) t1s[v] = hs(r * (q[v] + q2[v]));
+    }
+    gks_tail<float, true>(w0, c0x, c0y, gs, nullptr, t1s, r.v.x, r.v.y, ps[3].v.x, ps[3].v.y, dt, K, c1, c2, fo,
+                          dfo);
 }
 
 // Navier-Stokes collision times (tau_type NS): Get_Tau_NS and Get_Tau

@@ -317,6 +317,20 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             mbar_expect_tx(&tma_bar, B::bytes);
             tma_load_3d(stg, tmap, xa, y0, 0, &tma_bar);
         }
+        const int nmax = DIR == 0 ? nx : ny, tmax = DIR == 0 ? ny : nx;
+        // GATED: the face cells' gate flags, loaded before the wait so that their latency overlaps
+        // the tile load's; consecutive threads take consecutive cells of a row (coalesced)
+        constexpr int NGF = (TILE_N + 1) * TL, GFL_PER = (NGF + FACE_THREADS - 1) / FACE_THREADS;
+        unsigned char gpre[GATED ? GFL_PER : 1];
+        if constexpr (GATED) {
+#pragma unroll
+            for (int k = 0; k < GFL_PER; ++k) {
+                const int c = tid + k * FACE_THREADS;
+                const int fnn = DIR == 0 ? c / TL : c % (TILE_N + 1), tl = DIR == 0 ? c % TL : c / (TILE_N + 1);
+                const int n = g + N0 - 1 + fnn, t = g + T0 - r + tl;
+                gpre[k] = c < NGF && n < nmax && t < tmax ? a.gate[cidx(n, t)] : (unsigned char)0;
+            }
+        }
         __syncthreads();   // the barrier is initialised before any thread polls it
         const bool ok = __syncthreads_and(aligned && mbar_wait(&tma_bar, 0));
         if (!ok) {
@@ -325,7 +339,14 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             if (aligned) mbar_wait(&tma_bar, 0);
             return;
         }
-        const int nmax = DIR == 0 ? nx : ny, tmax = DIR == 0 ? ny : nx;
+        if constexpr (GATED) {
+#pragma unroll
+            for (int k = 0; k < GFL_PER; ++k) {
+                const int c = tid + k * FACE_THREADS;
+                const int fnn = DIR == 0 ? c / TL : c % (TILE_N + 1), tl = DIR == 0 ? c % TL : c / (TILE_N + 1);
+                if (c < NGF) gfl[fnn * TL + tl] = gpre[k];
+            }
+        }
         for (int c = tid; c < S::TN * TL; c += FACE_THREADS) {
             const int nn = c / TL, tl = c % TL;
             const int n = g + N0 - 1 - r + nn, t = g + T0 - r + tl;
@@ -335,10 +356,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             if (DIR == 0) { d[0] = q[0]; d[1] = q[PZ]; d[2] = q[2 * PZ]; d[3] = q[3 * PZ]; }
             else { d[0] = q[0]; d[1] = q[2 * PZ]; d[2] = -q[PZ]; d[3] = q[3 * PZ]; }
             antile[nn * TL + tl] = q[(DIR == 0 ? 4 : 5) * PZ];
-            if (nn >= r && nn <= r + TILE_N) {
-                attile[(nn - r) * TL + tl] = q[(DIR == 0 ? 5 : 4) * PZ];
-                if constexpr (GATED) gfl[(nn - r) * TL + tl] = a.gate[cidx(n, t)];
-            }
+            if (nn >= r && nn <= r + TILE_N) attile[(nn - r) * TL + tl] = q[(DIR == 0 ? 5 : 4) * PZ];
         }
     } else {
         const int nmax = DIR == 0 ? nx : ny, tmax = DIR == 0 ? ny : nx;
@@ -418,19 +436,25 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         }
         if constexpr (GATED) if (!lin && ((gfl[nl * TL + tl] >> DIR) & 1)) {
             // predicted smooth: the linear weights select the full-stencil polynomial, and a
-            // linear reconstruction commutes with the characteristic projection
+            // linear reconstruction commutes with the characteristic projection; two variables
+            // per paired FP32 operation
+            using C = lin::Normal<ORDER>;
+            const F2 dft(df[NW - 1]), dfi(df[NW - 1] * hN);
 #pragma unroll
-            for (int side = 0; side < 2; ++side)
+            for (int vp = 0; vp < 2; ++vp) {
+                F2 s2[N];
 #pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    T s[N], p[NW], px[NW];
+                for (int k = 0; k < N; ++k) s2[k] = F2(st[k][2 * vp], st[k][2 * vp + 1]);
 #pragma unroll
-                    for (int k = 0; k < N; ++k) s[k] = st[k][v];
-                    if (side == 0) normal_face<T, ORDER, 0>(s, df, hN, p, px);
-                    else normal_face<T, ORDER, 1>(s, df, hN, p, px);
-                    outv[side][v] = p[NW - 1];
-                    outv[side][4 + v] = px[NW - 1];
+                for (int side = 0; side < 2; ++side) {
+                    const F2 val = lin_value<F2, N, C>(side, s2, dft);
+                    const F2 der = lin_slope<F2, N, C>(side, s2, dfi);
+                    outv[side][2 * vp] = val.v.x;
+                    outv[side][2 * vp + 1] = val.v.y;
+                    outv[side][4 + 2 * vp] = der.v.x;
+                    outv[side][5 + 2 * vp] = der.v.y;
                 }
+            }
             const T slack = T(geo.gate_slack);
             lin = linear_ok<T>(outv[0], st[r - 1], st[r], st[r + 1], K, slack) &&
                   linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K, slack);
@@ -545,18 +569,25 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             }
             if constexpr (GATED) if (!lin && ((gfl[(fn + side) * TL + tc] >> (1 - DIR)) & 1)) {
                 // the side cell is smooth along the tangent: full-stencil polynomial at the
-                // Gauss points, in conservative variables
+                // Gauss points, in conservative variables; two line entries per paired FP32
+                // operation (values and normal slopes; tangential slopes of the values)
+                using C = lin::Tangent<ORDER>;
+                const F2 dft(df[NW - 1]), dfi(df[NW - 1] * hT);
 #pragma unroll
-                for (int v = 0; v < 8; ++v) {
-                    T s[N];
+                for (int vp = 0; vp < 4; ++vp) {
+                    F2 s2[N];
 #pragma unroll
-                    for (int k = 0; k < N; ++k) s[k] = line(k, side)[v];
+                    for (int k = 0; k < N; ++k) s2[k] = F2(*reinterpret_cast<const float2*>(line(k, side) + 2 * vp));
 #pragma unroll
                     for (int ig = 0; ig < GP; ++ig) {
-                        T p[NW], px[NW];
-                        tangent_point<T, ORDER>(ig, s, df, hT, p, px);
-                        res[ig][v] = p[NW - 1];
-                        if (v < 4) res[ig][8 + v] = px[NW - 1];
+                        const F2 val = lin_value<F2, N, C>(ig, s2, dft);
+                        res[ig][2 * vp] = val.v.x;
+                        res[ig][2 * vp + 1] = val.v.y;
+                        if (vp < 2) {
+                            const F2 der = lin_slope<F2, N, C>(ig, s2, dfi);
+                            res[ig][8 + 2 * vp] = der.v.x;
+                            res[ig][9 + 2 * vp] = der.v.y;
+                        }
                     }
                 }
                 lin = true;
@@ -727,6 +758,9 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             // of its code
             if constexpr (NS)
                 gks_point_ns<T>(L, R, dt, K, NsParam<T>{T(geo.c2), T(geo.mu), T(geo.nu), T(geo.prandtl_coef)}, f, d);
+            else if constexpr (std::is_same<T, float>::value)
+                // FP32: the left and right states share the paired FP32 lanes
+                gks_point_lr(L, R, dt, K, float(geo.c1), float(geo.c2), f, d);
             else
                 gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
             if (geo.integrator == 1) {   // S1O1 takes the dt integral F0 = f + d / 2 alone
@@ -770,8 +804,24 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             }
             double X[4], P[4];
             const bool s2o4 = geo.integrator == 0;
+            // FP32 kernels, plain S2O4: the FP64 pipe bounds this phase, so the conversions run on
+            // the integer pipes (f32_to_f64, exact) and each result takes one FP64 operation:
+            // X0 = 0.5 F + D / 8 (D / 8 exact in FP32), P0 = F + D / 6, X1 = P0 + D / 3
+            const bool fast64 = sizeof(T) == 4 && s2o4 && !geo.source;
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
+            for (int v = 0; v < 4 && fast64; ++v) {
+                const float fq = float(Fq[v]), dq = float(Dq[v]);
+                if (a.stage == 0) {
+                    const double F = f32_to_f64(fq);
+                    X[v] = fma(0.5, F, f32_to_f64(0.125f * dq));
+                    P[v] = fma(1.0 / 6.0, f32_to_f64(dq), F);
+                } else {
+                    X[v] = fma(1.0 / 3.0, f32_to_f64(dq), a.FP[v * nf + fi]);
+                    P[v] = 0.0;
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < 4 && !fast64; ++v) {
                 const double F = double(Fq[v]), D = double(Dq[v]);
                 if (s2o4) {
                     if (geo.source) {
@@ -804,15 +854,15 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             // mean over Gauss points, zeroed below 2 (Calculate_alpha, :1497-1516)
             // FP64 divides as the reference does; the FP32 path takes the mean in FP32 (an
             // indicator, not part of the FP64 stage combination) instead of a double division
-            double am;
             if constexpr (sizeof(T) == 8) {
                 const double as = double(asum);
-                am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
+                const double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
+                a.FA[fi] = am < 2.0 ? 0.0 : am;
             } else {
-                am = double(GP == 2 ? T(0.5) * asum : GP == 3 ? asum * T(1.0 / 3.0) : T(0.25) * asum);
+                const float am = float(GP == 2 ? T(0.5) * asum : GP == 3 ? asum * T(1.0 / 3.0) : T(0.25) * asum);
+                a.FA[fi] = am < 2.0f ? 0.0 : f32_to_f64(am);
             }
-            a.FA[fi] = am < 2.0 ? 0.0 : am;
-            if (s2o4 && a.stage == 1 && !geo.source) {
+            if (s2o4 && a.stage == 1 && !geo.source && !fast64) {
 #pragma unroll
                 for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
             }

@@ -184,6 +184,12 @@ __global__ void wait_limit_selftest_kernel(unsigned* out) {
     if (threadIdx.x == 0) *out = done ? 1u : 2u;
 }
 
+// f32_to_f64 over an array (hos_convert_selftest)
+__global__ void convert_selftest_kernel(const float* __restrict__ x, double* __restrict__ y, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = f32_to_f64(x[i]);
+}
+
 static thread_local std::string g_last_error;
 
 // conserved wedge states and geometry (Primvar_to_convar_2D on the primitive states)
@@ -462,6 +468,24 @@ int hos_wait_limit_selftest(void) {
     if (e != cudaSuccess) return cuda_fail(e, "selftest");
     if (h == 2u) return fail(HOS_E_TIMEOUT, "the wait gave up at its limit (expected)");
     return h == 1u ? fail(HOS_OK, "the wait completed: the barrier was not expected to") : fail(HOS_E_CUDA, "no result");
+}
+
+int hos_convert_selftest(const float* x, double* y, size_t n) {
+    if ((!x || !y) && n) return fail(HOS_E_ARG, "null argument");
+    if (n == 0) return HOS_OK;
+    float* dx = nullptr;
+    double* dy = nullptr;
+    cudaError_t e = cudaMalloc(&dx, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dy, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        convert_selftest_kernel<<<(unsigned)((n + 255) / 256), 256>>>(dx, dy, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    return e == cudaSuccess ? HOS_OK : cuda_fail(e, "convert selftest");
 }
 
 int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) {

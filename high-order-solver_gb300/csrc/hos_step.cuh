@@ -178,6 +178,14 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 a.A32[plane32 + cm] = (float)ay;
             }
         }
+        if (a.W32 && a.stage != cfl_stage(geo)) {
+            // FP32 solvers, a stage without CFL candidates: Convar_to_Primvar's sign tests without
+            // its division (the FP64 pipe bounds this kernel): rho > 0 and
+            // 2 rho (rho E) - |rho u|^2 >= 0, which a NaN fails
+            const double e = 2.0 * w[0] * w[3] - (w[1] * w[1] + w[2] * w[2]);
+            if (!(w[0] > 0.0) || !(e >= 0.0)) bad = 1;
+            return;
+        }
         const double ir = 1.0 / w[0];
         double pr[4];
         pr[0] = w[0];

@@ -9,6 +9,8 @@
 // divisions 13/3 == 4 and 781/20 == 39 of its 7th-order indicator are kept.
 #pragma once
 #include <cuda_runtime.h>
+#include "hos_f32x2.cuh"
+#include "hos_linear_coef.cuh"
 
 namespace hos {
 
@@ -414,6 +416,35 @@ __device__ __forceinline__ void tangent_point(int ig, const T* s, const T* df, T
         p[5] = w0 + df[5] * (a9 + b9 * x + c9 * x2 + d9 * x3 + e9 * x4 + f9 * x5 + g9 * x6 + h9 * x7 + i9 * x8 - w0);
         px[5] = df[5] * (b9 + T(2.0) * c9 * x + T(3.0) * d9 * x2 + T(4.0) * e9 * x3 + T(5.0) * f9 * x4 + T(6.0) * g9 * x5 + T(7.0) * h9 * x6 + T(8.0) * i9 * x7) * ih;
     }
+}
+
+// ---- the full-stencil (linear-weight) reconstruction of the learned gate's linear path ----
+// sum_k c(p, k) s[k] over the nonzero coefficients of row p of a table of hos_linear_coef.cuh
+// (C::V: values, C::D: slopes)
+template <class T, int N, class C, bool DER>
+__device__ __forceinline__ T lin_dot(int p, const T* s) {
+    T acc = T(0.0);
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const double c = DER ? C::D(p, k) : C::V(p, k);
+        if (c == 0.0) continue;
+        if (first) acc = T(c) * s[k];
+        else acc = T(c) * s[k] + acc;
+        first = false;
+    }
+    return acc;
+}
+// value and slope of the top candidate polynomial with its DF factor at point p of the centre
+// cell: w0 + df (P - w0) and df ih P' (dfi = df * ih).  The same polynomial as normal_face /
+// tangent_point's last candidate, with the coefficients collected per stencil cell.
+template <class T, int N, class C>
+__device__ __forceinline__ T lin_value(int p, const T* s, T df) {
+    return s[N / 2] + df * (lin_dot<T, N, C, false>(p, s) - s[N / 2]);
+}
+template <class T, int N, class C>
+__device__ __forceinline__ T lin_slope(int p, const T* s, T dfi) {
+    return lin_dot<T, N, C, true>(p, s) * dfi;
 }
 
 // ---- non-DF WENO5-AO (src/reconstruction.cpp:161-360, 2393-2551): the 3D scheme and the 2D

@@ -200,6 +200,11 @@ const char* hos_last_error(void);
  * in the limit), HOS_E_CUDA on a launch error. */
 int hos_wait_limit_selftest(void);
 
+/* Self-test of the FP32 -> FP64 conversion the FP32 face kernels' stage combination runs on the
+ * integer pipes (no counterpart in the reference): y[i] = x[i] widened on the device, n host
+ * values.  Exact for normal values and zero; FP32 subnormals give signed zero. */
+int hos_convert_selftest(const float* x, double* y, size_t n);
+
 /* ---- learned gate (FP32-bulk path; no counterpart in the reference) ---------------------
  * A 16 -> 32 -> 32 -> 1 MLP (BF16 weights, FP32 accumulation on the tensor cores) predicts,
  * per cell and direction, from the normalised WENO-AO smoothness indicators of density and
