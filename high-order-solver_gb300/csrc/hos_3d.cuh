@@ -167,8 +167,9 @@ struct Mom3 {
 };
 template <class T>
 __device__ __forceinline__ T erfcT(T x) { return erfc(x); }
+// FP32: the fitted form of ferfc (hos_f32x2.cuh), without the library's conversion instructions
 template <>
-__device__ __forceinline__ float erfcT<float>(float x) { return erfcf(x); }
+__device__ __forceinline__ float erfcT<float>(float x) { return ferfc(x); }
 template <class T>
 __device__ __forceinline__ T expT(T x) { return exp(x); }
 template <>

@@ -75,11 +75,44 @@ __device__ __forceinline__ F2& operator*=(F2& a, F2 b) { return a = F2(a * b); }
 
 // per-lane functions (the global FP32 / FP64 overloads stay visible beside them)
 using ::sqrt;
-using ::exp;
-using ::erfc;
 __device__ __forceinline__ F2 sqrt(F2 a) { return F2(sqrtf(a.v.x), sqrtf(a.v.y)); }
-__device__ __forceinline__ F2 exp(F2 a) { return F2(expf(a.v.x), expf(a.v.y)); }
-__device__ __forceinline__ F2 erfc(F2 a) { return F2(erfcf(a.v.x), erfcf(a.v.y)); }
+
+// exp and erfc of the GKS flux.  FP64 keeps the library functions.  The FP32 forms avoid the
+// conversion instructions of the library's expf / erfcf, which GB300 executes on its narrow FP64
+// pipe: exp is the hardware base-2 exponential (__expf; error 2 + 1.2 |x| ulp, where the flux
+// takes exp of arguments of a few tens at most, giving absolute errors far below the FP32
+// rounding of the terms they multiply), and erfc is the Chebyshev-fitted form of Press et al.,
+// Numerical Recipes in C, 2nd ed., section 6.2 (erfcc, fractional error below 1.2e-7):
+//   erfc(z) = t exp(-z^2 + P(t)),  t = 1 / (1 + z / 2),  z >= 0,  erfc(-z) = 2 - erfc(z).
+__device__ __forceinline__ double fexp(double x) { return exp(x); }
+__device__ __forceinline__ float fexp(float x) { return __expf(x); }
+__device__ __forceinline__ F2 fexp(F2 a) { return F2(__expf(a.v.x), __expf(a.v.y)); }
+// P(t) of the fitted form, Horner from the highest coefficient
+template <class T>
+__device__ __forceinline__ T erfc_poly(T t) {
+    T p = T(0.17087277) * t + T(-0.82215223);
+    p = p * t + T(1.48851587);
+    p = p * t + T(-1.13520398);
+    p = p * t + T(0.27886807);
+    p = p * t + T(-0.18628806);
+    p = p * t + T(0.09678418);
+    p = p * t + T(0.37409196);
+    p = p * t + T(1.00002368);
+    return p * t + T(-1.26551223);
+}
+__device__ __forceinline__ double ferfc(double x) { return erfc(x); }
+__device__ __forceinline__ float ferfc(float x) {
+    const float z = fabsf(x), t = 1.0f / (1.0f + 0.5f * z);
+    const float r = t * __expf(erfc_poly(t) - z * z);
+    return x >= 0.0f ? r : 2.0f - r;
+}
+__device__ __forceinline__ F2 ferfc(F2 a) {
+    const F2 z(fabsf(a.v.x), fabsf(a.v.y));
+    const F2 t(1.0f / (1.0f + 0.5f * z.v.x), 1.0f / (1.0f + 0.5f * z.v.y));
+    const F2 q = erfc_poly(t) - z * z;
+    const F2 r = t * F2(__expf(q.v.x), __expf(q.v.y));
+    return F2(a.v.x >= 0.0f ? r.v.x : 2.0f - r.v.x, a.v.y >= 0.0f ? r.v.y : 2.0f - r.v.y);
+}
 __device__ __forceinline__ F2 fabsT(F2 a) { return F2(fabsf(a.v.x), fabsf(a.v.y)); }
 __device__ __forceinline__ F2 fminT(F2 a, F2 b) { return F2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y)); }
 __device__ __forceinline__ F2 fmaxT(F2 a, F2 b) { return F2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y)); }

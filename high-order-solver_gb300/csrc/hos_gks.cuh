@@ -38,9 +38,9 @@ template <class T> struct Mom {
         constexpr double pi = 3.14159265358979323846;
         const T ol = T(1.0) / lambda;
         whole(u, v, ol, K);
-        up[0] = T(0.5) * erfc(sqrt(lambda) * -u);
+        up[0] = T(0.5) * ferfc(T(sqrt(lambda) * -u));
         un[0] = T(1.0) - up[0];
-        up[1] = u * up[0] + T(0.5) * (exp(-lambda * u * u) / sqrt(T(pi) * lambda));
+        up[1] = u * up[0] + T(0.5) * (fexp(T(-lambda * u * u)) / sqrt(T(pi) * lambda));
         un[1] = u - up[1];
 #pragma unroll
         for (int i = 2; i <= 6; ++i) {
@@ -186,7 +186,7 @@ __device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y
     const T Cc = tau_ratio(rl, rr, ll, lr, T(c2));
     {
         const T tn = tau_num(Cc, dt, c1, c2);
-        const T eta = exp(-dt / tn);
+        const T eta = fexp(T(-dt / tn));
         const T t0 = tn * (T(1) - eta);
         const T t1 = tn * (eta * (dt + tn) - tn);
         const T t3 = tn * eta + dt - tn;
@@ -207,7 +207,7 @@ __device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y
     {
         const T dt2 = T(0.5) * dt;
         const T tn = tau_num(Cc, dt2, c1, c2);
-        const T eta = exp(-dt2 / tn);
+        const T eta = fexp(T(-dt2 / tn));
         const T t0 = tn * (T(1) - eta);
         const T t1 = tn * (eta * (dt2 + tn) - tn);
         const T t3 = tn * eta + dt2 - tn;
@@ -311,8 +311,8 @@ __device__ __forceinline__ void gks_point_lr(const GState<float>& L, const GStat
         Mom<F2> m;   // up[] holds the lanes' half-space moments
         const F2 u = ps[1], lam = ps[3], ol = F2(1.0f) / lam;
         m.whole(u, ps[2], ol, Kp);
-        m.up[0] = F2(0.5f) * erfc(F2(-1.0f, 1.0f) * sqrt(lam) * u);
-        m.up[1] = u * m.up[0] + F2(0.5f, -0.5f) * (exp(-(lam * u * u)) / sqrt(F2(pi) * lam));
+        m.up[0] = F2(0.5f) * ferfc(F2(F2(-1.0f, 1.0f) * sqrt(lam) * u));
+        m.up[1] = u * m.up[0] + F2(0.5f, -0.5f) * (fexp(-F2(lam * u * u)) / sqrt(F2(pi) * lam));
 #pragma unroll
         for (int i = 2; i <= 6; ++i) m.up[i] = u * m.up[i - 1] + F2(0.5 * (i - 1)) * ol * m.up[i - 2];
         w0[0] = hs(r * m.up[0]);
@@ -455,7 +455,7 @@ __device__ __forceinline__ void gks_point_ns(const GState<T>& L, const GState<T>
     for (int lev = 0; lev < 2; ++lev) {
         const T h = lev == 0 ? dt : T(0.5) * dt;
         const T tn = tau_num_ns(q, ratio, h, p0[0], p0[3]);
-        const T eta = exp(-h / tn);
+        const T eta = fexp(T(-h / tn));
         const T t0 = tn * (T(1) - eta);
         const T t1 = tn * (eta * (h + tn) - tn) + tau * tn * (eta - T(1));
         const T t2 = tau * tn * (eta - T(1));

@@ -186,7 +186,10 @@ struct FaceSmem {
     static constexpr int r = ORDER / 2;
     static constexpr int GP = GaussCount<ORDER>::GP;
     static constexpr int TL = TILE_T + 2 * r;                      // line states along t
-    static constexpr int LINES = TILE_N * TL * 2 * 8;              // [fn][tl][side][8]
+    // line states: for face row fn, entry pair qp (values 0-3, normal slopes 4-7, two per pair),
+    // tangential cell tl and side: [fn][qp][tl][side][2], so that the tangential pass, whose
+    // consecutive threads take consecutive (tl, side), reads consecutive pairs
+    static constexpr int LINES = TILE_N * TL * 2 * 8;
     static constexpr int GSTATES = TILE_N * TILE_T * 2 * GP * 12;  // [face][side][gp][12]
     static constexpr int FLUX = TILE_N * TILE_T * GP * 9;          // [face][gp][f4 d4 alpha]
     static constexpr int UNION = LINES > FLUX ? LINES : FLUX;
@@ -245,8 +248,8 @@ __device__ __forceinline__ T alpha_k(const T* wl, const T* wr, T gamma) {
 // A-posteriori check of a linear (gated) reconstruction: density and total energy of each
 // reconstructed state stay within the range of the three central stencil entries widened by
 // slack times that range (a tenth unless set), and the state keeps a positive temperature.
-template <class T>
-__device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, const T* wp, T K, T slack = T(0.1)) {
+template <class T, class A, class B, class C>
+__device__ __forceinline__ bool linear_ok(const T* q, const A& wm, const B& w0, const C& wp, T K, T slack = T(0.1)) {
     if (needs_order_reduction(q, K)) return false;
 #pragma unroll
     for (int v = 0; v < 4; v += 3) {
@@ -256,6 +259,16 @@ __device__ __forceinline__ bool linear_ok(const T* q, const T* wm, const T* w0, 
     }
     return true;
 }
+
+// One entry (line cell, side) of the line states: element q (0-3 values, 4-7 normal slopes) at
+// base[(q / 2) * stride + q % 2]
+template <class T>
+struct LineRef {
+    const T* base;
+    int stride;
+    __device__ __forceinline__ T operator[](int q) const { return base[(q >> 1) * stride + (q & 1)]; }
+    __device__ __forceinline__ const T* pair(int qp) const { return base + qp * stride; }
+};
 
 // One tile of faces: N0, T0 are the first face indices along the normal and the tangent.
 // GATED (FP32 only): cells the learned gate marks smooth reconstruct with the full-stencil
@@ -286,14 +299,25 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     const int nx = geo.nx, ny = geo.ny, g = geo.g;
     const int nodeN = DIR == 0 ? geo.nodex : geo.nodey;  // faces along normal: nodeN + 1
     const int nodeT = DIR == 0 ? geo.nodey : geo.nodex;  // faces along tangent: nodeT
-    const T hN = T(DIR == 0 ? geo.idx : geo.idy);   // inverse normal spacing
-    const T hT = T(DIR == 0 ? geo.idy : geo.idx);   // inverse face length
-    const T gamma = T(geo.gamma), K = T(geo.K);
     const size_t plane = (size_t)nx * ny;
     const int tid = threadIdx.x;
     if (!a.ctl->active) return;
     __shared__ unsigned rejected;   // GATED: linear results the check rejected in this tile
     if constexpr (GATED) if (tid == 0) rejected = 0;
+    // FP32: the launch's FP64 parameters narrowed once per tile (a conversion from FP64 runs on
+    // GB300's narrow FP64 pipe; per thread they would cost as much as the stage combination)
+    __shared__ float fpar[7];
+    if constexpr (sizeof(T) == 4) {
+        if (tid == 0) {
+            fpar[0] = float(DIR == 0 ? geo.idx : geo.idy);
+            fpar[1] = float(DIR == 0 ? geo.idy : geo.idx);
+            fpar[2] = float(geo.gamma);
+            fpar[3] = float(geo.K);
+            fpar[4] = float(a.ctl->dt);
+            fpar[5] = float(geo.c1);
+            fpar[6] = float(geo.c2);
+        }
+    }
     auto cidx = [&](int n, int t) -> size_t {
         return DIR == 0 ? (size_t)n * ny + t : (size_t)t * ny + n;
     };
@@ -394,7 +418,11 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             }
         }
     }
-    __syncthreads();
+    __syncthreads();   // also publishes fpar
+    const T hN = sizeof(T) == 4 ? T(fpar[0]) : T(DIR == 0 ? geo.idx : geo.idy);   // inverse normal spacing
+    const T hT = sizeof(T) == 4 ? T(fpar[1]) : T(DIR == 0 ? geo.idy : geo.idx);   // inverse face length
+    const T gamma = sizeof(T) == 4 ? T(fpar[2]) : T(geo.gamma);
+    const T K = sizeof(T) == 4 ? T(fpar[3]) : T(geo.K);
 
     // ---------------- phase 1: normal reconstruction of the tile's cells ----------------
     // cells n in [g+N0-1, g+N0+TILE_N), t in [g+T0-r, g+T0+TILE_T+r)
@@ -516,14 +544,14 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         // left-face value -> right side of face n; right-face value -> left side of face n+1
         const int fl = n - (g + N0);
         if (fl >= 0 && fl < TILE_N) {
-            T* d = lines + ((fl * TL + tl) * 2 + 1) * 8;
+            T* d = lines + ((fl * 4 * TL + tl) * 2 + 1) * 2;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) d[q] = outv[0][q];
+            for (int q = 0; q < 8; ++q) d[(q >> 1) * 4 * TL + (q & 1)] = outv[0][q];
         }
         if (fl + 1 >= 0 && fl + 1 < TILE_N) {
-            T* d = lines + (((fl + 1) * TL + tl) * 2 + 0) * 8;
+            T* d = lines + (((fl + 1) * 4 * TL + tl) * 2 + 0) * 2;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) d[q] = outv[1][q];
+            for (int q = 0; q < 8; ++q) d[(q >> 1) * 4 * TL + (q & 1)] = outv[1][q];
         }
     }
     __syncthreads();
@@ -548,10 +576,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             } else {
                 df_factors<T, ORDER>(al, df);
             }
-            auto line = [&](int k, int sd) -> const T* {
-                return lines + ((fn * TL + (tc + sgn * (k - r))) * 2 + sd) * 8;
+            auto line = [&](int k, int sd) -> LineRef<T> {
+                return LineRef<T>{lines + ((fn * 4 * TL + (tc + sgn * (k - r))) * 2 + sd) * 2, 4 * TL};
             };
-            const T* w0 = line(r, side);
+            const LineRef<T> w0 = line(r, side);
             T res[GP][12];
             bool lin = false;
             if (geo.first_order) {
@@ -577,7 +605,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 for (int vp = 0; vp < 4; ++vp) {
                     F2 s2[N];
 #pragma unroll
-                    for (int k = 0; k < N; ++k) s2[k] = F2(*reinterpret_cast<const float2*>(line(k, side) + 2 * vp));
+                    for (int k = 0; k < N; ++k) s2[k] = F2(*reinterpret_cast<const float2*>(line(k, side).pair(vp)));
 #pragma unroll
                     for (int ig = 0; ig < GP; ++ig) {
                         const F2 val = lin_value<F2, N, C>(ig, s2, dft);
@@ -615,7 +643,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 if (ORDER == 9 && side == 1) {
                     // the reference's right side keeps the left side's projection of the two
                     // outermost entries (src/reconstruction.cpp:3318-3327)
-                    const T* l0 = line(r, 0);
+                    const LineRef<T> l0 = line(r, 0);
                     T b0[4], lw[4];
 #pragma unroll
                     for (int v = 0; v < 4; ++v) lw[v] = l0[v];
@@ -733,7 +761,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     if constexpr (GATED) if (tid == 0 && rejected) atomicAdd(a.fallback, (unsigned long long)rejected);
 
     // ---------------- phase 3: GKS flux, one (face, Gauss point) per thread ----------------
-    const T dt = T(a.ctl->dt);
+    const T dt = sizeof(T) == 4 ? T(fpar[4]) : T(a.ctl->dt);
     for (int item = tid; item < TILE_N * TILE_T * GP; item += FACE_THREADS) {
         const int fidx = item / GP, ig = item % GP;
         const int fn = fidx / TILE_T, ft = fidx % TILE_T;
@@ -760,7 +788,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 gks_point_ns<T>(L, R, dt, K, NsParam<T>{T(geo.c2), T(geo.mu), T(geo.nu), T(geo.prandtl_coef)}, f, d);
             else if constexpr (std::is_same<T, float>::value)
                 // FP32: the left and right states share the paired FP32 lanes
-                gks_point_lr(L, R, dt, K, float(geo.c1), float(geo.c2), f, d);
+                gks_point_lr(L, R, dt, K, fpar[5], fpar[6], f, d);
             else
                 gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
             if (geo.integrator == 1) {   // S1O1 takes the dt integral F0 = f + d / 2 alone
