@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched sweep")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D Taylor-Green leg")
     ap.add_argument("--no-endtime", action="store_true", help="skip the 1024^2 end-time accuracy leg")
+    ap.add_argument("--batch-failures", action="store_true",
+                    help="run every problem the gated FP32 batch loses to a blow-up alone: plain FP64 on the GPU "
+                         "and the FP64 restatement on the host cores, with the step where each stops")
     ap.add_argument("--endtime", action="store_true",
                     help="accuracy studies at the end times instead of the bench line: 1024^2 Riemann to "
                          "t = 0.25 and 64^3 Taylor-Green to t = 10 (FP64, FP32 bulk, gated FP32)")
@@ -415,6 +418,80 @@ def endtime3d_leg(gate, rep, n=64, tstop=10.0, every=0.25, forms=("fp64", "fp32"
     return out
 
 
+def _steps_until_blowup(step, tstop, blowup, max_steps=20000, budget_s=None):
+    """Steps of a driver loop (first-order step 0, then the scheme) until t >= tstop or a blow-up
+    (an exception of type ``blowup``).  step(k) runs step k and returns the time after it.
+    Returns (steps taken, blew_up, t after the last good step, seconds); blew_up is None when the
+    time budget ran out first."""
+    t0 = time.perf_counter()
+    k, t = 0, 0.0
+    while t < tstop and k < max_steps:
+        try:
+            t = step(k)
+        except blowup:
+            return k + 1, True, t, time.perf_counter() - t0
+        k += 1
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            return k, None, t, time.perf_counter() - t0
+    return k, False, t, time.perf_counter() - t0
+
+
+def batch_failures_main(args):
+    """The problems of the 64-problem sweep that the gated FP32 batch loses to a blow-up, each run
+    alone from the same initial data with the drivers' first-order step 0: the plain FP64 GPU
+    solver, the gated FP32 solver, and the FP64 restatement of the reference's algorithm on the
+    host cores (at most ~120 s per problem).  Prints one JSON line with the step at which each
+    stops (negative density / pressure) or its end."""
+    import torch
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    from hos_gb300 import cases, gate_train
+    from hos_gb300.solver import FP32, FP64, HosBlowUp, Solver2D
+    from oracle_lib import CpuStep
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    gate5, rep5 = gate_train.train(order=5, sizes=(256, 512), seeds=range(4), steps=120, sample_log2=5,
+                                   train_steps=3000, batch=4096)
+    res = batch_leg(dev, FP32, gate=gate5, threshold=rep5.threshold)
+    sweep = {x[4]: x for x in cases.batch_sweep(count=64, seed=0)}
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    out = []
+    for label in res["blown_up_problems"]:
+        pb, con, prim, tstop, _ = sweep[label]
+        row = {"problem": label, "t_end": tstop}
+        for name, prec, gated in (("gpu_fp64", FP64, False), ("gpu_fp32_gated", FP32, True)):
+            s = Solver2D(pb, prec)
+            s.set_state(con, prim)
+            if gated:
+                s.set_gate(gate5, rep5.threshold, audit_log2=AUDIT_LOG2)
+
+            def step(k, s=s):
+                s.set_reconstruction(k == 0)
+                s.step(tstop)
+                return s.sync()[0]
+
+            n, bad, t, sec = _steps_until_blowup(step, tstop, HosBlowUp)
+            row[name] = {"steps": n, "blew_up": bad, "t": t}
+            s.close()
+        o = CpuStep("oracle").init(pb, threads=cores)
+        o.set_state(con, prim)
+
+        def ostep(k):
+            o.fn("set_first_order")(1 if k == 0 else 0)
+            o.step(tstop)
+            return o.t
+
+        # the restatement reports its blow-up status as a RuntimeError
+        n, bad, t, sec = _steps_until_blowup(ostep, tstop, RuntimeError, budget_s=120.0)
+        row["cpu_fp64_restatement"] = {"steps": n, "blew_up": bad, "t": t, "seconds": sec, "threads": cores}
+        out.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    gate5.close()
+    print(json.dumps({"mode": "batch_failures", "batch": {k: res[k] for k in ("blown_up", "value", "wall_s")},
+                      "problems": out}), flush=True)
+
+
 def endtime_main(args):
     """--endtime: the accuracy studies at the configurations' end times, one JSON line: the 2D
     Riemann problem at 1024^2 to t = 0.25 and the Taylor-Green vortex at 64^3 to t = 10 (FP64,
@@ -741,6 +818,9 @@ def main():
         return
     if args.endtime:
         endtime_main(args)
+        return
+    if args.batch_failures:
+        batch_failures_main(args)
         return
     if args.case == "gated256":
         profile_case()

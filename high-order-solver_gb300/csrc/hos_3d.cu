@@ -291,6 +291,9 @@ Dir3 make_dir(const Geo3& g, int dir) {
     d.ihn = 1.0 / d.hn;
     d.ih1 = 1.0 / d.h1;
     d.ih2 = 1.0 / d.h2;
+    d.fihn = (float)d.ihn;
+    d.fih1 = (float)d.ih1;
+    d.fih2 = (float)d.ih2;
     const int af = dir == 2 ? 1 : 0;
     d.fv = Lay{d.n0 + 1, d.n1 + 4, d.n2 + 4, af};
     d.cel = Lay{d.n0 + 2, d.n1 + 4, d.n2 + 4, af};
@@ -435,6 +438,7 @@ int hos3d_create(const hos_params3d* params, int precision, hos_solver3d** out) 
     g.tau_type = p.tau_type;
     g.characteristic = p.characteristic ? 1 : 0;
     for (int k = 0; k < 6; ++k) g.bc[k] = p.bc[k];
+    narrow_params3(g);
     for (int d = 0; d < 3; ++d) s->dirs[d] = make_dir(g, d);
     s->ncell = (size_t)g.nx * g.ny * g.nz;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);

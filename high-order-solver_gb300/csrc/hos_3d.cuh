@@ -42,6 +42,8 @@ struct Geo3 {
     int tau_type, characteristic;
     int bc[6];
     int p_slot;   // FP64: the reference's GKS3D convention, pressure where lambda belongs
+    // FP32 copies of gamma, K, c1, c2, mu, prandtl_coef, narrowed on the host (narrow_params3)
+    float fgamma, fK, fc1, fc2, fmu, fprc;
 };
 
 // index space of one per-direction array: extents (NA, NB, NC), k-aligned axis fastest
@@ -73,11 +75,28 @@ struct Dir3 {
     int n0, n1, n2;
     double hn, h1, h2;
     double ihn, ih1, ih2;   // their inverses, computed on the host (no FP64 division per thread)
+    float fihn, fih1, fih2; // and their FP32 copies
     Lay fv;   // face values: faces 0..n0, b in [-2, n1+2), c in [-2, n2+2)
     Lay cel;  // face3 thread space: cells -1..n0 of the normal, fv's b and c
     Lay lv;   // line values: faces 0..n0, b interior, c in [-2, n2+2)
     Lay fs;   // fluxes: faces 0..n0, b and c interior
 };
+
+// a launch parameter in the compute type: the FP32 kernels take the copy narrowed on the host (a
+// conversion from FP64 runs on GB300's narrow FP64 pipe, once per thread and use otherwise)
+template <class T>
+__device__ __forceinline__ T par(double d, float f) {
+    if constexpr (sizeof(T) == 4) return f;
+    else return d;
+}
+inline void narrow_params3(Geo3& g) {
+    g.fgamma = (float)g.gamma;
+    g.fK = (float)g.K;
+    g.fc1 = (float)g.c1;
+    g.fc2 = (float)g.c2;
+    g.fmu = (float)g.mu;
+    g.fprc = (float)g.prandtl_coef;
+}
 
 // global cell of local absolute (A, B, C) (ghosts included)
 __device__ __forceinline__ size_t cell_of(const Geo3& g, int dir, int A, int B, int C) {
@@ -281,14 +300,14 @@ __device__ __forceinline__ void tcoef(T* t, T tau, T tn, T dt) {
 }
 template <class T>
 __device__ __forceinline__ T tau_num3(const Geo3& g, T dl, T dr, T ll, T lr, T d0, T l0, T dt) {
-    const T C = T(g.c2) * fabsT(dl / ll - dr / lr) / fabsT(dl / ll + dr / lr);
+    const T C = par<T>(g.c2, g.fc2) * fabsT(dl / ll - dr / lr) / fabsT(dl / ll + dr / lr);
     if (g.tau_type == 0) {
         if (g.c1 <= 0 && g.c2 <= 0) return T(0);
-        return T(g.c1) * dt + dt * C;
+        return par<T>(g.c1, g.fc1) * dt + dt * C;
     }
     T tn = C * dt;
     if (tn != tn) tn = T(0);
-    return g.mu > 0 ? tn + T(2) * T(g.mu) * l0 / d0 : T(0);
+    return g.mu > 0 ? tn + T(2) * par<T>(g.mu, g.fmu) * l0 / d0 : T(0);
 }
 
 // one side's contribution to the flux: rho t0 <u g> + rho t1 <u a.psi (u, v, w)> +
@@ -329,7 +348,7 @@ __device__ __forceinline__ void side_flux(const Mom3<T>& m, const T* pr, const T
 template <class T>
 __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5], T dt, const Geo3& g, T* f,
                      T* df) {
-    const T K = T(g.K);
+    const T K = par<T>(g.K, g.fK);
     T pl[5], pr[5];
     // the reference's GKS3D hands Convar_to_primvar_3D's pressure to every lambda slot
     // (src/flux_function.cpp:831-836, 914); only the FP64 kernels carry that convention
@@ -368,7 +387,7 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
     T p0[5];
     if (p_slot) prim5<T>(p0, c0, T(g.gamma));
     else ulambda5<T>(p0, c0, K);
-    const T tau = (g.tau_type != 0 && g.mu > 0) ? T(2) * T(g.mu) * p0[4] / p0[0] : T(0);
+    const T tau = (g.tau_type != 0 && g.mu > 0) ? T(2) * par<T>(g.mu, g.fmu) * p0[4] / p0[0] : T(0);
     T ta[6], tb[6];
     const T dt2 = T(0.5) * dt;
     tcoef<T>(ta, tau, tau_num3<T>(g, pl[0], pr[0], pl[4], pr[4], p0[0], p0[4], dt), dt);
@@ -410,7 +429,7 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
     if (g.prandtl_coef != 0.0) {
         // Prandtl-number correction of the heat flux: GKS2D's (src/flux_function.cpp:630-636,
         // 678-684; the reference's GKS3D has none) with the third velocity component
-        const T prc = T(g.prandtl_coef);
+        const T prc = par<T>(g.prandtl_coef, g.fprc);
         const T qs = a0xuu[4] + tmp[4] - p0[1] * (a0xuu[1] + tmp[1]) - p0[2] * (a0xuu[2] + tmp[2]) -
                      p0[3] * (a0xuu[3] + tmp[3]);
         Fa[4] += prc * (qs * (-p0[0] * tau * dt));
@@ -502,7 +521,7 @@ __global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const T* __restric
     d.cel.decode(t, a0, b0, c0);
     const int ac = a0 - 1, G = g.g;
     const size_t plane = (size_t)g.nx * g.ny * g.nz;
-    const T gamma = T(g.gamma), K = T(g.K), ih = T(d.ihn);
+    const T gamma = par<T>(g.gamma, g.fgamma), K = par<T>(g.K, g.fK), ih = par<T>(d.ihn, d.fihn);
     T st[5][5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -597,7 +616,7 @@ __global__ void __launch_bounds__(FACE3_THREADS) face3_kernel(const T* __restric
 // :3963-4108; WENO5_AO_for_point_value, :4165-4360).
 template <class T, int NQ>
 __device__ __forceinline__ void sweep_side(const T (*st)[NQ][5], T ih, const Geo3& g, T (*out)[NQ + 1][5]) {
-    const T gamma = T(g.gamma);
+    const T gamma = par<T>(g.gamma, g.fgamma);
     Char5<T> ch;
     if (g.characteristic) {
         T base[5];
@@ -659,7 +678,7 @@ __global__ void __launch_bounds__(LINE3_THREADS) line3_kernel(const T* __restric
     int a, b, c;
     d.lv.decode(t, a, b, c);
     const size_t nfv = d.fv.n(), nlv = d.lv.n();
-    const T ih = T(d.ih1), K = T(g.K);
+    const T ih = par<T>(d.ih1, d.fih1), K = par<T>(g.K, g.fK);
     bool reduce = false;
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
@@ -743,7 +762,7 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
     int a = 0, b = 0, c = 0;
     if (valid) {
         d.fs.decode(face, a, b, c);
-        const T ih = T(d.ih2), K = T(g.K), dt = T(ctl->dt);
+        const T ih = par<T>(d.ih2, d.fih2), K = par<T>(g.K, g.fK), dt = T(ctl->dt);
         // point states: [ip][side][value | normal | t1 | t2 slope][5]
         T pt[2][2][4][5];
         bool reduce = false;

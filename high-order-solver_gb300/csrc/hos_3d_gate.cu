@@ -28,7 +28,7 @@ __device__ __forceinline__ void indicator5(const float* s, float* f) {
 // regularisation epsilon 1e-6 of the 2D gate's label
 __device__ float weight_distance3(const double* __restrict__ W, const Geo3& g, size_t c, size_t stride, int ax) {
     const size_t plane = (size_t)g.nx * g.ny * g.nz;
-    const float gamma = float(g.gamma);
+    const float gamma = g.fgamma;
     float st[5][5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {

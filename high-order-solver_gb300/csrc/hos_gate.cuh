@@ -61,18 +61,21 @@ struct Stats {
 // Normalised indicators of one stencil: betas / (sum beta + tau + 1e-10 c^2), padded to 6, then
 // tau.  The floor keeps variations below 1e-5 of the value (FP32 rounding of the primitives
 // included) from looking like structure.
-template <int ORDER>
-__device__ __forceinline__ void indicator_features(const float* s, float* f) {
+// T = float, or F2 for two stencils at once (the gate kernels: a cell's x and y stencils).
+template <int ORDER, class T = float>
+__device__ __forceinline__ void indicator_features(const T* s, T* f) {
     constexpr int NW = AO<ORDER>::N;
-    float beta[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const float tau = ao_betas<float, ORDER>(s, beta);
-    float sum = tau;
+    T beta[6];
 #pragma unroll
-    for (int k = 0; k < NW; ++k) sum += beta[k];
-    const float c = s[ORDER / 2];
-    const float inv = 1.0f / (sum + 1e-10f * c * c + 1e-30f);
+    for (int k = 0; k < 6; ++k) beta[k] = T(0.0f);
+    const T tau = ao_betas<T, ORDER>(s, beta);
+    T sum = tau;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) f[k] = k < NW ? beta[k] * inv : 0.0f;
+    for (int k = 0; k < NW; ++k) sum = sum + beta[k];
+    const T c = s[ORDER / 2];
+    const T inv = T(1.0f) / (sum + T(1e-10f) * c * c + T(1e-30f));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[k] = k < NW ? T(beta[k] * inv) : T(0.0f);
     f[6] = tau * inv;
 }
 
@@ -526,12 +529,36 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo
         }
     };
     // both directions' features into the network's input, then one pass over the tile's 512
-    // rows; sampled cells (collect mode) compute their features again afterwards
+    // rows; the x and y stencils of the cell run in the two lanes of the paired FP32 type.
+    // Sampled cells (collect mode) compute their features again afterwards, one direction at a
+    // time.
+    {
+        const bool fx = in && i >= r && i < geo.nx - r, fy = in && j >= r && j < geo.ny - r;
+        F2 rs[ORDER], ps[ORDER], f2[NF];
 #pragma unroll
-    for (int dir = 0; dir < 2; ++dir) {
+        for (int k = 0; k < ORDER; ++k) {
+            rs[k] = F2(srho[ti + k][tj + r], srho[ti + r][tj + k]);
+            ps[k] = F2(sp[ti + k][tj + r], sp[ti + r][tj + k]);
+        }
+        indicator_features<ORDER, F2>(rs, f2);
+        indicator_features<ORDER, F2>(ps, f2 + 7);
+        float ax, ay;
+        if constexpr (TMA) {
+            ax = salpha[0][tid];   // the mirror's FP32 copy of alpha
+            ay = salpha[1][tid];
+        } else {
+            ax = in ? float(a.AX[c]) : 0.0f;
+            ay = in ? float(a.AY[c]) : 0.0f;
+        }
+        f2[14] = F2(ax / (1.0f + ax), ay / (1.0f + ay));
+        f2[15] = F2(0.0f);
         float f[NF];
-        features(dir, f);
-        mlp_tc_put(mlp, dir, f);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) f[k] = fx ? f2[k].v.x : 0.0f;
+        mlp_tc_put(mlp, 0, f);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) f[k] = fy ? f2[k].v.y : 0.0f;
+        mlp_tc_put(mlp, 1, f);
     }
     float zd[2];
     mlp_tc_eval(mlp, zd, phase, broken);
