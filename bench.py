@@ -311,11 +311,13 @@ def endtime2d_leg(gate, rep, n=N_CELLS, tstop=0.25):
     pb, con, prim = cases.riemann2d(n, order=ORDER)
     g = pb.ghost
     rho, runs = {}, {}
-    for name, prec, gated in (("fp64", FP64, False), ("fp32", FP32, False), ("gated", FP32, True)):
+    for name, prec, gated in (("fp64", FP64, False), ("fp32", FP32, False), ("gated", FP32, True),
+                              ("gated_every_stage", FP32, True)):
         s = Solver2D(pb, prec)
         s.set_state(con, prim)
         if gated:
             s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+            s.set_gate_reuse(name == "gated")
             s.gate_stats(reset=True)
         t0 = time.perf_counter()
         steps = 0
@@ -349,6 +351,9 @@ def endtime2d_leg(gate, rep, n=N_CELLS, tstop=0.25):
             "rho_rel_linf_fp32_vs_fp64": rel(rho["fp32"], rho["fp64"], 0),
             "rho_rel_l1_gated_vs_fp32": rel(rho["gated"], rho["fp32"], 1),
             "cells_off_by_1e-2_gated": float((np.abs(rho["gated"] - rho["fp64"]) > 1e-2 * np.abs(rho["fp64"])).mean()),
+            "gated": "network at stage 0, its flags dilated by one cell at stage 1 (hos2d_set_gate_reuse)",
+            "rho_rel_l1_gated_every_stage_vs_fp64": rel(rho["gated_every_stage"], rho["fp64"], 1),
+            "rho_rel_linf_gated_every_stage_vs_fp64": rel(rho["gated_every_stage"], rho["fp64"], 0),
             "target": "rho_rel_l1_gated_vs_fp64 <= 1e-3"}
 
 
@@ -777,6 +782,7 @@ def profile_case(n=256, steps=21, plain=True):
         s.set_state(con, prim)
         if gated:
             s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+            s.set_gate_reuse(True)
         torch.cuda.nvtx.range_push("gated" if gated else "plain")
         s.advance(steps, 1e30, graph=False)
         s.sync()
@@ -887,6 +893,7 @@ def main():
         s.set_state(con, prim)
         if gated:
             s.set_gate(gate, rep.threshold, audit_log2=AUDIT_LOG2)
+            s.set_gate_reuse(True)   # the network at stage 0; stage 1 takes its flags dilated
         replicas.barrier(ws)
         torch.cuda.synchronize(dev)
         t = timed_steps(s, args.steps, args.warmup)
@@ -968,7 +975,8 @@ def main():
                    "characteristic": True, "form": "gated FP32 (learned gate) vs plain FP64",
                    "parallelism": "replicas" if ws > 1 else "single",
                    "l2": "flushed between timed steps (256 MB write)",
-                   "gate_training": "seeded random-quadrant runs at 256^2 and 512^2 (4 seeds each, 120 steps)"},
+                   "gate_training": "seeded random-quadrant runs at 256^2 and 512^2 (4 seeds each, 120 steps)",
+                   "gate_stages": "network at stage 0, its flags dilated by one cell at stage 1"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(host_in.numel() * 8),
                 "d2h_bytes_per_step": int(host_out.numel() * 8)},
         "gpu_launches": launches,

@@ -189,10 +189,14 @@ __device__ __forceinline__ T erfcT(T x) { return erfc(x); }
 // FP32: the fitted form of ferfc (hos_f32x2.cuh), without the library's conversion instructions
 template <>
 __device__ __forceinline__ float erfcT<float>(float x) { return ferfc(x); }
+template <>
+__device__ __forceinline__ F2 erfcT<F2>(F2 x) { return ferfc(x); }
 template <class T>
 __device__ __forceinline__ T expT(T x) { return exp(x); }
 template <>
 __device__ __forceinline__ float expT<float>(float x) { return __expf(x); }
+template <>
+__device__ __forceinline__ F2 expT<F2>(F2 x) { return fexp(x); }
 
 template <class T>
 __device__ __forceinline__ void mom_whole(Mom3<T>& m, T u, T v, T w, T lambda, T K) {
@@ -225,10 +229,25 @@ __device__ __forceinline__ void mom_half(Mom3<T>& m, T u, T lambda, T sgn) {
     for (int i = 2; i <= 6; ++i) m.h[i] = u * m.h[i - 1] + T(i - 1) * hl * m.h[i - 2];
 }
 // <u^i v^j w^k xi^2q> over the whole space (H = false) or the stored half space (H = true)
+// (the paired FP32 type leaves out the unit factors u[0] = v[0] = w[0] = 1: a paired multiply is
+// not folded away; the scalar types keep the products as written)
 template <class T, bool H>
 __device__ __forceinline__ T M(const Mom3<T>& m, int i, int j, int k, int q) {
-    const T r = (H ? m.h[i] : m.u[i]) * m.v[j] * m.w[k];
-    return q == 0 ? r : q == 1 ? r * m.x1 : r * m.x2;
+    if constexpr (std::is_same<T, F2>::value) {
+        const bool unit_u = !H && i == 0;
+        const T& ui = H ? m.h[i] : m.u[i];
+        T r;
+        if (j == 0 && k == 0) r = unit_u ? T(1.0f) : ui;
+        else if (j == 0) r = unit_u ? m.w[k] : T(ui * m.w[k]);
+        else if (k == 0) r = unit_u ? m.v[j] : T(ui * m.v[j]);
+        else r = unit_u ? T(m.v[j] * m.w[k]) : T(ui * m.v[j] * m.w[k]);
+        if (q == 0) return r;
+        const T& x = q == 1 ? m.x1 : m.x2;
+        return unit_u && j == 0 && k == 0 ? x : T(r * x);
+    } else {
+        const T r = (H ? m.h[i] : m.u[i]) * m.v[j] * m.w[k];
+        return q == 0 ? r : q == 1 ? r * m.x1 : r * m.x2;
+    }
 }
 // <a psi u^NU v^NV w^NW> (GL_/GR_/G_address, include/basic_function.h:222-358)
 template <class T, bool H, int NU, int NV, int NW>
@@ -312,10 +331,10 @@ __device__ __forceinline__ T tau_num3(const Geo3& g, T dl, T dr, T ll, T lr, T d
 
 // one side's contribution to the flux: rho t0 <u g> + rho t1 <u a.psi (u, v, w)> +
 // rho t2 <u A psi>, for the two time levels (coefficients ta, tb)
+// The three moment sets of one side: g = <u psi>, s1 = <u a.psi (u, v, w)>, s2 = <u A psi>.
 template <class T>
-__device__ __forceinline__ void side_flux(const Mom3<T>& m, const T* pr, const T (*al)[5], T K, const T* ta,
-                                          const T* tb, T* Fa, T* Fb) {
-    T g[5], s1[5], s2[5], tmp[5];
+__device__ __forceinline__ void side_terms(const Mom3<T>& m, const T* pr, const T (*al)[5], T K, T* g, T* s1, T* s2) {
+    T tmp[5];
     gunit<T, true, 1>(m, g);
     gaddr<T, true, 2, 0, 0>(m, al[0], s1);
     gaddr<T, true, 1, 1, 0>(m, al[1], tmp);
@@ -336,6 +355,12 @@ __device__ __forceinline__ void side_flux(const Mom3<T>& m, const T* pr, const T
     T A[5];
     micro3<T>(A, der, pr, K);
     gaddr<T, true, 1, 0, 0>(m, A, s2);
+}
+template <class T>
+__device__ __forceinline__ void side_flux(const Mom3<T>& m, const T* pr, const T (*al)[5], T K, const T* ta,
+                                          const T* tb, T* Fa, T* Fb) {
+    T g[5], s1[5], s2[5];
+    side_terms<T>(m, pr, al, K, g, s1, s2);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
         Fa[v] += pr[0] * (ta[0] * g[v] + ta[1] * s1[v] + ta[2] * s2[v]);
@@ -343,59 +368,26 @@ __device__ __forceinline__ void side_flux(const Mom3<T>& m, const T* pr, const T
     }
 }
 
-// GKS3D at one Gauss point, face frame: S2O4 pair f = 4 F(dt/2) - F(dt), derf = 4 (F(dt) - 2 F(dt/2)).
-// L/R: value (c) and slopes along normal, t1, t2 (d[3]) of the left and right states.
+// Collision-state primitives p0 and the time-integration coefficients of both time levels (ta:
+// dt, tb: dt / 2) from the sides' densities and lambdas; returns the physical collision time.
 template <class T>
-__device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5], T dt, const Geo3& g, T* f,
-                     T* df) {
-    const T K = par<T>(g.K, g.fK);
-    T pl[5], pr[5];
-    // the reference's GKS3D hands Convar_to_primvar_3D's pressure to every lambda slot
-    // (src/flux_function.cpp:831-836, 914); only the FP64 kernels carry that convention
-    const bool p_slot = sizeof(T) == 8 && g.p_slot;
-    if (p_slot) {
-        prim5<T>(pl, Lc, T(g.gamma));
-        prim5<T>(pr, Rc, T(g.gamma));
-    } else {
-        ulambda5<T>(pl, Lc, K);
-        ulambda5<T>(pr, Rc, K);
-    }
-    Mom3<T> ml, mr;
-    mom_whole<T>(ml, pl[1], pl[2], pl[3], pl[4], K);
-    mom_half<T>(ml, pl[1], pl[4], T(1));
-    mom_whole<T>(mr, pr[1], pr[2], pr[3], pr[4], K);
-    mom_half<T>(mr, pr[1], pr[4], T(-1));
-    // all-collision centre state and its slopes
-    T c0[5];
-    c0[0] = pl[0] * ml.h[0] + pr[0] * mr.h[0];
-    c0[1] = pl[0] * ml.h[1] + pr[0] * mr.h[1];
-    c0[2] = pl[0] * ml.v[1] * ml.h[0] + pr[0] * mr.v[1] * mr.h[0];
-    c0[3] = pl[0] * ml.w[1] * ml.h[0] + pr[0] * mr.w[1] * mr.h[0];
-    c0[4] = T(0.5) * pl[0] * (ml.h[2] + ml.h[0] * (ml.v[2] + ml.w[2] + ml.x1))
-            + T(0.5) * pr[0] * (mr.h[2] + mr.h[0] * (mr.v[2] + mr.w[2] + mr.x1));
-    T al[3][5], ar[3][5], d0[3][5];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        micro3<T>(al[d], Ld[d], pl, K);
-        micro3<T>(ar[d], Rd[d], pr, K);
-        T a0l[5], a0r[5];
-        gaddr<T, true, 0, 0, 0>(ml, al[d], a0l);
-        gaddr<T, true, 0, 0, 0>(mr, ar[d], a0r);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) d0[d][v] = pl[0] * a0l[v] + pr[0] * a0r[v];
-    }
-    T p0[5];
+__device__ __forceinline__ T gks3_coef(const T* c0, T pl0, T pr0, T pl4, T pr4, T dt, const Geo3& g, T K, bool p_slot,
+                                       T* p0, T* ta, T* tb) {
     if (p_slot) prim5<T>(p0, c0, T(g.gamma));
     else ulambda5<T>(p0, c0, K);
     const T tau = (g.tau_type != 0 && g.mu > 0) ? T(2) * par<T>(g.mu, g.fmu) * p0[4] / p0[0] : T(0);
-    T ta[6], tb[6];
     const T dt2 = T(0.5) * dt;
-    tcoef<T>(ta, tau, tau_num3<T>(g, pl[0], pr[0], pl[4], pr[4], p0[0], p0[4], dt), dt);
-    tcoef<T>(tb, tau, tau_num3<T>(g, pl[0], pr[0], pl[4], pr[4], p0[0], p0[4], dt2), dt2);
-    T Fa[5] = {T(0), T(0), T(0), T(0), T(0)}, Fb[5] = {T(0), T(0), T(0), T(0), T(0)};
-    side_flux<T>(ml, pl, al, K, ta, tb, Fa, Fb);
-    side_flux<T>(mr, pr, ar, K, ta, tb, Fa, Fb);
-    // equilibrium part about the centre state
+    tcoef<T>(ta, tau, tau_num3<T>(g, pl0, pr0, pl4, pr4, p0[0], p0[4], dt), dt);
+    tcoef<T>(tb, tau, tau_num3<T>(g, pl0, pr0, pl4, pr4, p0[0], p0[4], dt2), dt2);
+    return tau;
+}
+
+// The equilibrium part about the centre state p0 (slopes d0 of the collision state) added to the
+// sides' time-integrated fluxes Fa (dt) and Fb (dt / 2); f, df: the S2O4 pair.
+template <class T>
+__device__ __forceinline__ void gks3_centre(const T* p0, const T (*d0)[5], T tau, const T* ta, const T* tb, T dt,
+                                            const Geo3& g, T K, T* Fa, T* Fb, T* f, T* df) {
+    const T dt2 = T(0.5) * dt;
     Mom3<T> m0;
     mom_whole<T>(m0, p0[1], p0[2], p0[3], p0[4], K);
     T g0u[5], a0[5], s4[5], der[5], tmp[5], tmp2[5];
@@ -441,6 +433,107 @@ __device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5
         df[v] = T(4) * (Fa[v] - T(2) * Fb[v]);
     }
 }
+
+// GKS3D at one Gauss point, face frame: S2O4 pair f = 4 F(dt/2) - F(dt), derf = 4 (F(dt) - 2 F(dt/2)).
+// L/R: value (c) and slopes along normal, t1, t2 (d[3]) of the left and right states.
+template <class T>
+__device__ void gks3(const T* Lc, const T (*Ld)[5], const T* Rc, const T (*Rd)[5], T dt, const Geo3& g, T* f,
+                     T* df) {
+    const T K = par<T>(g.K, g.fK);
+    T pl[5], pr[5];
+    // the reference's GKS3D hands Convar_to_primvar_3D's pressure to every lambda slot
+    // (src/flux_function.cpp:831-836, 914); only the FP64 kernels carry that convention
+    const bool p_slot = sizeof(T) == 8 && g.p_slot;
+    if (p_slot) {
+        prim5<T>(pl, Lc, T(g.gamma));
+        prim5<T>(pr, Rc, T(g.gamma));
+    } else {
+        ulambda5<T>(pl, Lc, K);
+        ulambda5<T>(pr, Rc, K);
+    }
+    Mom3<T> ml, mr;
+    mom_whole<T>(ml, pl[1], pl[2], pl[3], pl[4], K);
+    mom_half<T>(ml, pl[1], pl[4], T(1));
+    mom_whole<T>(mr, pr[1], pr[2], pr[3], pr[4], K);
+    mom_half<T>(mr, pr[1], pr[4], T(-1));
+    // all-collision centre state and its slopes
+    T c0[5];
+    c0[0] = pl[0] * ml.h[0] + pr[0] * mr.h[0];
+    c0[1] = pl[0] * ml.h[1] + pr[0] * mr.h[1];
+    c0[2] = pl[0] * ml.v[1] * ml.h[0] + pr[0] * mr.v[1] * mr.h[0];
+    c0[3] = pl[0] * ml.w[1] * ml.h[0] + pr[0] * mr.w[1] * mr.h[0];
+    c0[4] = T(0.5) * pl[0] * (ml.h[2] + ml.h[0] * (ml.v[2] + ml.w[2] + ml.x1))
+            + T(0.5) * pr[0] * (mr.h[2] + mr.h[0] * (mr.v[2] + mr.w[2] + mr.x1));
+    T al[3][5], ar[3][5], d0[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        micro3<T>(al[d], Ld[d], pl, K);
+        micro3<T>(ar[d], Rd[d], pr, K);
+        T a0l[5], a0r[5];
+        gaddr<T, true, 0, 0, 0>(ml, al[d], a0l);
+        gaddr<T, true, 0, 0, 0>(mr, ar[d], a0r);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) d0[d][v] = pl[0] * a0l[v] + pr[0] * a0r[v];
+    }
+    T p0[5], ta[6], tb[6];
+    const T tau = gks3_coef<T>(c0, pl[0], pr[0], pl[4], pr[4], dt, g, K, p_slot, p0, ta, tb);
+    T Fa[5] = {T(0), T(0), T(0), T(0), T(0)}, Fb[5] = {T(0), T(0), T(0), T(0), T(0)};
+    side_flux<T>(ml, pl, al, K, ta, tb, Fa, Fb);
+    side_flux<T>(mr, pr, ar, K, ta, tb, Fa, Fb);
+    gks3_centre<T>(p0, d0, tau, ta, tb, dt, g, K, Fa, Fb, f, df);
+}
+
+// FP32 GKS3D with the two sides in the two lanes of the paired FP32 type (lane x the left state
+// and the u > 0 half space of its Maxwellian, lane y the right state and its u < 0 half space):
+// the side moments, micro-slopes, the collision state and its slopes and the sides' flux
+// contributions are formed on both lanes at once and summed across them; the time coefficients
+// and the centre part are scalar (gks3_coef, gks3_centre).  Euler or Navier-Stokes collision
+// time, the lambda convention (the reference's pressure slot is FP64 only).
+__device__ __forceinline__ void gks3_lr(const float* Lc, const float (*Ld)[5], const float* Rc, const float (*Rd)[5],
+                                        float dt, const Geo3& g, float* f, float* df) {
+    const float K = g.fK;
+    const F2 Kp(K);
+    F2 w[5], ps[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) w[v] = F2(Lc[v], Rc[v]);
+    ulambda5<F2>(ps, w, Kp);
+    Mom3<F2> m;
+    mom_whole<F2>(m, ps[1], ps[2], ps[3], ps[4], Kp);
+    mom_half<F2>(m, ps[1], ps[4], F2(1.0f, -1.0f));
+    const F2 r = ps[0];
+    float c0[5];
+    c0[0] = hsum(r * m.h[0]);
+    c0[1] = hsum(r * m.h[1]);
+    c0[2] = hsum(r * m.v[1] * m.h[0]);
+    c0[3] = hsum(r * m.w[1] * m.h[0]);
+    c0[4] = hsum(F2(0.5f) * r * (m.h[2] + m.h[0] * (m.v[2] + m.w[2] + m.x1)));
+    F2 a[3][5];
+    float d0[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        F2 sl[5], a0[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sl[v] = F2(Ld[d][v], Rd[d][v]);
+        micro3<F2>(a[d], sl, ps, Kp);
+        gaddr<F2, true, 0, 0, 0>(m, a[d], a0);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) d0[d][v] = hsum(r * a0[v]);
+    }
+    // the sides' moment sets before the time coefficients: the moments and micro-slopes need not
+    // stay live across the scalar part
+    F2 gs[5], s1[5], s2[5];
+    side_terms<F2>(m, ps, a, Kp, gs, s1, s2);
+    float p0[5], ta[6], tb[6];
+    const float tau = gks3_coef<float>(c0, r.v.x, r.v.y, ps[4].v.x, ps[4].v.y, dt, g, K, false, p0, ta, tb);
+    float Fa[5], Fb[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        Fa[v] = hsum(r * (F2(ta[0]) * gs[v] + F2(ta[1]) * s1[v] + F2(ta[2]) * s2[v]));
+        Fb[v] = hsum(r * (F2(tb[0]) * gs[v] + F2(tb[1]) * s1[v] + F2(tb[2]) * s2[v]));
+    }
+    gks3_centre<float>(p0, d0, tau, ta, tb, dt, g, K, Fa, Fb, f, df);
+}
+
 
 // ---- learned gate (FP32 path): linear reconstructions and their check --------------------
 // Per cell one flag byte, bit a set when the gate predicts the WENO5-AO weights of the cell's
@@ -826,7 +919,10 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
 #pragma unroll 1
         for (int ip = 0; ip < 2; ++ip) {
             T f[5], df[5];
-            gks3<T>(pt[ip][0][0], &pt[ip][0][1], pt[ip][1][0], &pt[ip][1][1], dt, g, f, df);
+            if constexpr (sizeof(T) == 4)
+                gks3_lr(pt[ip][0][0], &pt[ip][0][1], pt[ip][1][0], &pt[ip][1][1], dt, g, f, df);
+            else
+                gks3<T>(pt[ip][0][0], &pt[ip][0][1], pt[ip][1][0], &pt[ip][1][1], dt, g, f, df);
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 acc[v] += T(0.25) * f[v];
@@ -840,12 +936,26 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
         const size_t f = d.fs.idx(a, b, c);
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-            const double fv = (double)acc[v], dv = (double)acc[5 + v];
-            if (stage == 0) {
-                FS[v * nfs + f] = 0.0 + (0.5 * fv + (1.0 / 8.0) * dv);
-                FS[(5 + v) * nfs + f] = 0.0 + (1.0 * fv + (1.0 / 6.0) * dv);
+            if constexpr (sizeof(T) == 4) {
+                // FP32: widened on the integer pipes, one FP64 operation per result (the FP64
+                // pipe also runs conversions): X0 = 0.5 F + D / 8 (D / 8 exact), P0 = F + D / 6,
+                // X1 = P0 + D / 3
+                const float fq = float(acc[v]), dq = float(acc[5 + v]);
+                if (stage == 0) {
+                    const double fv = f32_to_f64(fq);
+                    FS[v * nfs + f] = fma(0.5, fv, f32_to_f64(0.125f * dq));
+                    FS[(5 + v) * nfs + f] = fma(1.0 / 6.0, f32_to_f64(dq), fv);
+                } else {
+                    FS[v * nfs + f] = fma(1.0 / 3.0, f32_to_f64(dq), FS[(5 + v) * nfs + f]);
+                }
             } else {
-                FS[v * nfs + f] = FS[(5 + v) * nfs + f] + (0.0 * fv + (1.0 / 3.0) * dv);
+                const double fv = (double)acc[v], dv = (double)acc[5 + v];
+                if (stage == 0) {
+                    FS[v * nfs + f] = 0.0 + (0.5 * fv + (1.0 / 8.0) * dv);
+                    FS[(5 + v) * nfs + f] = 0.0 + (1.0 * fv + (1.0 / 6.0) * dv);
+                } else {
+                    FS[v * nfs + f] = FS[(5 + v) * nfs + f] + (0.0 * fv + (1.0 / 3.0) * dv);
+                }
             }
         }
     }

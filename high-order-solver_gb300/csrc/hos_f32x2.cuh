@@ -130,6 +130,9 @@ __device__ __forceinline__ double f32_to_f64(float x) {
     return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
 }
 
+// the sum of the two lanes
+__device__ __forceinline__ float hsum(F2 a) { return a.v.x + a.v.y; }
+
 // the scalar type of a compute type: the uniform parameters of the templated math
 template <class T> struct ScalarOf { using type = T; };
 template <> struct ScalarOf<F2> { using type = float; };

@@ -1,5 +1,6 @@
 // hos_solver.cu -- step kernels other than the face kernels, the C++ host solver and the
 // C ABI declared in include/hos_gb300.h.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -174,6 +175,24 @@ __global__ void prim_of_state_kernel(const double* __restrict__ W, double* __res
     for (int v = 0; v < 4; ++v) P[v * n + c] = p[v];
 }
 
+// The gate's flags of the step's first stage for a later stage: a cell keeps its x (y) bit only
+// when its neighbours along x (y) have it too.  Within a stage a front moves by at most a
+// quarter cell (CFL 0.5, half a step), so it cannot enter a stencil that a flagged neighbour's
+// stencil, one cell further out, did not already see.
+__global__ void __launch_bounds__(256) dilate_flags_kernel(const unsigned char* __restrict__ f0,
+                                                           unsigned char* __restrict__ f1, int nx, int ny,
+                                                           const StepCtl* ctl) {
+    if (!ctl->active) return;
+    const size_t n = (size_t)nx * ny;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c / ny), j = (int)(c % ny);
+        unsigned x = f0[c] & 1u, y = f0[c] & 2u;
+        if (x) x = i > 0 && i + 1 < nx ? f0[c - ny] & f0[c + ny] & 1u : 0u;
+        if (y) y = j > 0 && j + 1 < ny ? f0[c - 1] & f0[c + 1] & 2u : 0u;
+        f1[c] = (unsigned char)(x | y);
+    }
+}
+
 // one block waits on an mbarrier that expects one arrival and receives none: the bounded wait
 // must give up and report (hos_wait_limit_selftest)
 __global__ void wait_limit_selftest_kernel(unsigned* out) {
@@ -296,6 +315,10 @@ struct hos_solver2d {
     // learned gate (FP32 path): per-cell flags, counters, the network's inference copy
     int gated = 0;
     unsigned char* gflags = nullptr;
+    // the network runs at stage 0 only; later stages take its flags dilated by one cell along
+    // each flag's axis (gflags2)
+    int greuse = 0;
+    unsigned char* gflags2 = nullptr;
     gate::Stats* gstats = nullptr;
     __nv_bfloat16* gw = nullptr;
     float* gb = nullptr;
@@ -344,7 +367,7 @@ void free_all(hos_solver2d* s) {
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->ctl) cudaFree(s->ctl);
-    void* gbufs[] = {s->gflags, s->gstats, s->gw, s->gb, s->W32};
+    void* gbufs[] = {s->gflags, s->gflags2, s->gstats, s->gw, s->gb, s->W32};
     for (void* b : gbufs)
         if (b) cudaFree(b);
     if (s->graph) cudaGraphExecDestroy(s->graph);
@@ -378,7 +401,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
         ay.FS = s->stagey;
         ay.DS = s->stagey + 16 * s->nfy;
     }
-    if (s->gated) {
+    if (s->gated && (stage == 0 || !s->greuse)) {
         // per-cell smoothness flags of this stage's state (ghosts filled) for both directions
         gate::GateArgs ga{s->W, s->AX, s->AY, s->gflags, s->gstats, s->gthreshold, s->gaudit_mask, s->gseed++,
                           nullptr, 0, 0xffffffffu, s->ctl, s->W32};
@@ -386,6 +409,13 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
             cudaSuccess)
             return cuda_fail(e, "gate");
         ax.gate = ay.gate = s->gflags;
+        ax.fallback = ay.fallback = &s->gstats->fallback;
+    } else if (s->gated) {
+        const size_t n = s->ncell;
+        dilate_flags_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s->stream>>>(
+            s->gflags, s->gflags2, geo.nx, geo.ny, s->ctl);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "dilate_flags");
+        ax.gate = ay.gate = s->gflags2;
         ax.fallback = ay.fallback = &s->gstats->fallback;
     }
     mark(1);
@@ -801,6 +831,20 @@ int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audi
     s->gthreshold = threshold;
     s->gaudit_mask = audit_log2 == 31 ? 0xffffffffu : (1u << audit_log2) - 1u;
     s->gated = 1;
+    return HOS_OK;
+}
+
+int hos2d_set_gate_reuse(hos_solver2d* s, int reuse) {
+    if (!s) return fail(HOS_E_ARG, "null solver");
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "set_gate_reuse");
+    if (reuse && !s->gflags2 && (e = cudaMalloc(&s->gflags2, s->ncell)) != cudaSuccess)
+        return fail(HOS_E_NOMEM, std::string("gate flags: ") + cudaGetErrorString(e));
+    if (s->graph && (reuse != 0) != (s->greuse != 0)) {  // the captured step has the old launch sequence
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    s->greuse = reuse ? 1 : 0;
     return HOS_OK;
 }
 

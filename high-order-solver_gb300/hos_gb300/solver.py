@@ -262,6 +262,11 @@ class Solver2D:
         """Attach a copy of a learned gate (FP32 solvers); None detaches it."""
         _check(self._lib.hos2d_set_gate(self._h, gate._h if gate is not None else None, threshold, audit_log2))
 
+    def set_gate_reuse(self, reuse: bool) -> None:
+        """Run the gate's network at the first stage of each step only and give the later stages
+        its flags dilated by one cell along each flag's axis (hos2d_set_gate_reuse)."""
+        _check(self._lib.hos2d_set_gate_reuse(self._h, 1 if reuse else 0))
+
     def set_gate_check(self, slack: float) -> None:
         """Widening of the linear path's a-posteriori range check (fraction of the range)."""
         _check(self._lib.hos2d_set_gate_check(self._h, slack))

@@ -246,6 +246,11 @@ int hos2d_set_gate(hos_solver2d* s, const hos_gate* g, float threshold, int audi
  * (default 0.1; 0 accepts only values inside the range) and its temperature is positive;
  * otherwise the full WENO-AO reconstruction replaces it.  No counterpart in the reference. */
 int hos2d_set_gate_check(hos_solver2d* s, double slack);
+/* reuse != 0: the network runs at the first stage of each step only; the later stages take its
+ * flags dilated by one cell along each flag's axis (a cell keeps its x / y flag when both its
+ * x / y neighbours have it), which covers the at most quarter-cell motion of a front within a
+ * stage.  0 (the default): the network runs at every stage.  No counterpart in the reference. */
+int hos2d_set_gate_reuse(hos_solver2d* s, int reuse);
 /* counters since the last reset: cells gated x, y; predicted smooth x, y; audited; audited but
  * not smooth (false negatives of the gate); linear results rejected; (unused) */
 int hos2d_gate_stats(hos_solver2d* s, unsigned long long* stats, int reset);

@@ -132,6 +132,35 @@ def test_gated_solver_deviation_and_coverage(trained):
     assert st["audited"] > 100 and st["false_neg"] / st["audited"] <= 0.05, st
 
 
+def test_gate_flags_reused_at_the_second_stage(trained):
+    """hos2d_set_gate_reuse: the network runs at stage 0 only and stage 1 takes its flags dilated
+    by one cell.  The step is the same number of launches; the gated run with reused flags stays as
+    close to plain FP32 as the gate run at every stage, and predicts no more cells smooth at
+    stage 1 than the network did at stage 0 (the dilation only clears flags)."""
+    g, rep = trained
+    pb, con, prim = cases.riemann2d(128, order=7)
+    runs = {}
+    for name, gated, reuse in (("fp32", False, False), ("every", True, False), ("reuse", True, True)):
+        s = Solver2D(pb, FP32)
+        s.set_state(con, prim)
+        if gated:
+            s.set_gate(g, rep.threshold, audit_log2=2)
+            s.set_gate_reuse(reuse)
+        n = s.launches_per_step
+        s.advance(40, 1e30)
+        s.sync()
+        runs[name] = (s.get_state()["convar"][..., 0], s.gate_stats() if gated else None, n)
+        s.close()
+    gh = pb.ghost
+    ref = runs["fp32"][0][gh:-gh, gh:-gh]
+    dev = {k: np.abs(runs[k][0][gh:-gh, gh:-gh] - ref).mean() / np.abs(ref).mean() for k in ("every", "reuse")}
+    assert dev["reuse"] <= 1e-3 and dev["reuse"] <= 2.0 * dev["every"] + 1e-7, dev
+    assert runs["reuse"][2] == runs["every"][2]
+    st = runs["reuse"][1]
+    # the network ran at stage 0 only: half the cells of the every-stage run were classified
+    assert st["cells_x"] * 2 == runs["every"][1]["cells_x"], (st, runs["every"][1])
+
+
 def test_gate_needs_the_fp32_path():
     pb, con, prim = cases.riemann2d(16, order=5)
     s = Solver2D(pb, FP64)
