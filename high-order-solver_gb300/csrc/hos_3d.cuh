@@ -844,6 +844,14 @@ template <class T, bool GATED = false>
 __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3_kernel(const T* __restrict__ LV, double* __restrict__ FS,
                                                                 Geo3 g, Dir3 d, const Ctl3* ctl, int stage, Gate3 gt) {
     if (!ctl->active) return;
+    // point states [ip][side][value | normal | t1 | t2 slope][5]: FP64 in registers, FP32 in
+    // shared memory (one column per thread), which leaves the paired GKS its registers
+    __shared__ float pt_sm[sizeof(T) == 4 ? 80 : 1][POINT3_THREADS];
+    T pt_reg[sizeof(T) == 4 ? 1 : 2][2][4][5];
+    auto PT = [&](int ip, int side, int q, int v) -> T& {
+        if constexpr (sizeof(T) == 4) return pt_sm[((ip * 2 + side) * 4 + q) * 5 + v][threadIdx.x];
+        else return pt_reg[ip][side][q][v];
+    };
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t nfs = d.fs.n(), nlv = d.lv.n();
     const bool valid = t < 2 * nfs;
@@ -856,8 +864,6 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
     if (valid) {
         d.fs.decode(face, a, b, c);
         const T ih = par<T>(d.ih2, d.fih2), K = par<T>(g.K, g.fK), dt = T(ctl->dt);
-        // point states: [ip][side][value | normal | t1 | t2 slope][5]
-        T pt[2][2][4][5];
         bool reduce = false;
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
@@ -904,7 +910,7 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
 #pragma unroll
-                    for (int v = 0; v < 5; ++v) pt[ip][side][q][v] = out[ip][q][v];
+                    for (int v = 0; v < 5; ++v) PT(ip, side, q, v) = out[ip][q][v];
             }
         }
         if (reduce) {  // rare: both points take the line values with zero slope along c
@@ -912,17 +918,26 @@ __global__ void __launch_bounds__(POINT3_THREADS, sizeof(T) == 4 ? 3 : 1) point3
             for (int side = 0; side < 2; ++side)
                 for (int ip = 0; ip < 2; ++ip) {
                     for (int q = 0; q < 3; ++q)
-                        for (int v = 0; v < 5; ++v) pt[ip][side][q][v] = LV[(((ig * 2 + side) * 3 + q) * 5 + v) * nlv + l];
-                    for (int v = 0; v < 5; ++v) pt[ip][side][3][v] = T(0);
+                        for (int v = 0; v < 5; ++v) PT(ip, side, q, v) = LV[(((ig * 2 + side) * 3 + q) * 5 + v) * nlv + l];
+                    for (int v = 0; v < 5; ++v) PT(ip, side, 3, v) = T(0);
                 }
         }
 #pragma unroll 1
         for (int ip = 0; ip < 2; ++ip) {
             T f[5], df[5];
-            if constexpr (sizeof(T) == 4)
-                gks3_lr(pt[ip][0][0], &pt[ip][0][1], pt[ip][1][0], &pt[ip][1][1], dt, g, f, df);
-            else
-                gks3<T>(pt[ip][0][0], &pt[ip][0][1], pt[ip][1][0], &pt[ip][1][1], dt, g, f, df);
+            if constexpr (sizeof(T) == 4) {
+                float Lp[4][5], Rp[4][5];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        Lp[q][v] = PT(ip, 0, q, v);
+                        Rp[q][v] = PT(ip, 1, q, v);
+                    }
+                gks3_lr(Lp[0], &Lp[1], Rp[0], &Rp[1], dt, g, f, df);
+            } else {
+                gks3<T>(pt_reg[ip][0][0], &pt_reg[ip][0][1], pt_reg[ip][1][0], &pt_reg[ip][1][1], dt, g, f, df);
+            }
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 acc[v] += T(0.25) * f[v];
