@@ -150,7 +150,8 @@ template <class T> struct GState { T w[4], dx[4], dy[4]; };
 
 // The centre (g0) part and the time integration of GKS2D's Euler form at one Gauss point
 // (src/flux_function.cpp:410-690 with tau = 0): from the collision state w0 and its slopes c0x,
-// c0y, the sides' <u psi> moments gl, gr (SUMMED: gl already holds rl gl + rr gr; gr unused),
+// c0y, the sides' <u psi> moments gl, gr (SUMMED, the FP32 form: gl already holds rl gl + rr gr,
+// gr is unused, and the time levels are folded as described below),
 // the <a u^2 + a u v> terms t1s, and the sides' densities rl, rr and lambdas ll, lr.
 template <class T, bool SUMMED = false>
 __device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y, const T* gl, const T* gr,
@@ -181,9 +182,30 @@ __device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y
         microslope(A0, dA0, p0, gk);
         contract<T, 2, 1, 0>(m0, A0, A0u);
     }
+    const T Cc = tau_ratio(rl, rr, ll, lr, T(c2));
+    if constexpr (SUMMED) {
+        // FP32 form.  The Euler collision time is proportional to the time level,
+        // tau_num(h) = (c1 + C) h, so exp(-h / tau_num) is the same at h = dt and dt/2 and every
+        // time coefficient below scales exactly as h (t0, t3) or h^2 (t1, t4, t5).  In
+        // 4 F(dt/2) - F(dt) the h^2 terms cancel and the h terms stay once; in
+        // 4 (F(dt) - 2 F(dt/2)) the h terms cancel and the h^2 terms stay twice.  The two
+        // results are formed that way, from the dt level alone, without the cancellation.
+        const T tn = tau_num(Cc, dt, c1, c2);
+        const T eta = fexp(T(-dt / tn));
+        const T t0 = tn * (T(1) - eta);
+        const T t1 = tn * (eta * (dt + tn) - tn);
+        const T t3 = tn * eta + dt - tn;
+        const T t4 = tn * (tn - eta * (dt + tn));
+        const T r3 = p0[0] * t3, d1 = T(2) * t1, d4 = T(2) * p0[0] * t4, d5 = p0[0] * dt * dt;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            fo[v] = t0 * gl[v] + r3 * g0u[v];
+            dfo[v] = d1 * t1s[v] + d4 * t4s[v] + d5 * A0u[v];
+        }
+        return;
+    }
     // time-integration coefficients for tau = 0 (Euler) at dt and dt/2
     T F0[4], F1[4];
-    const T Cc = tau_ratio(rl, rr, ll, lr, T(c2));
     {
         const T tn = tau_num(Cc, dt, c1, c2);
         const T eta = fexp(T(-dt / tn));
@@ -194,9 +216,7 @@ __device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y
         const T t5 = T(0.5) * dt * dt;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            T f;
-            if constexpr (SUMMED) f = t0 * gl[v];
-            else f = rl * t0 * gl[v] + rr * t0 * gr[v];
+            T f = rl * t0 * gl[v] + rr * t0 * gr[v];
             f = f + p0[0] * t3 * g0u[v];
             f = f + t1 * t1s[v];
             f = f + p0[0] * t4 * t4s[v];
@@ -215,9 +235,7 @@ __device__ __forceinline__ void gks_tail(const T* w0, const T* c0x, const T* c0y
         const T t5 = T(0.5) * dt2 * dt2;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            T f;
-            if constexpr (SUMMED) f = t0 * gl[v];
-            else f = t0 * (rl * gl[v] + rr * gr[v]);
+            T f = t0 * (rl * gl[v] + rr * gr[v]);
             f = f + t1 * t1s[v];
             f = f + p0[0] * t3 * g0u[v];
             f = f + p0[0] * t4 * t4s[v];
