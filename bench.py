@@ -945,6 +945,22 @@ def main():
         assert lib.hos2d_get_state(sg._h, pout, None, None, None) == 0
     te = time.perf_counter() - t0
     e2e_value = ws * cells * ke / te
+    # where the end-to-end step goes (outside the timed loop: a synchronize after the step
+    # separates it from the download)
+    split = {"set_state": [], "step": [], "get_state": []}
+    for _ in range(ke):
+        ta = time.perf_counter()
+        assert lib.hos2d_set_state(sg._h, pin, None) == 0
+        tb = time.perf_counter()
+        sg.advance(1, 1e30, graph=True)
+        torch.cuda.synchronize(dev)
+        tc = time.perf_counter()
+        assert lib.hos2d_get_state(sg._h, pout, None, None, None) == 0
+        td = time.perf_counter()
+        split["set_state"].append(tb - ta)
+        split["step"].append(tc - tb)
+        split["get_state"].append(td - tc)
+    e2e_split = {k + "_ms": round(1e3 * float(np.median(v)), 4) for k, v in split.items()}
     launches = args.steps * sg.launches_per_step
     sg.close()
 
@@ -978,7 +994,7 @@ def main():
                    "gate_training": "seeded random-quadrant runs at 256^2 and 512^2 (4 seeds each, 120 steps)",
                    "gate_stages": "network at stage 0, its flags dilated by one cell at stage 1"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(host_in.numel() * 8),
-                "d2h_bytes_per_step": int(host_out.numel() * 8)},
+                "d2h_bytes_per_step": int(host_out.numel() * 8), "split": e2e_split},
         "gpu_launches": launches,
         "roofline": {"kernel": "face_kernel_tma<7,x|y,gated>", "bound": "fp32", "unit": "TFLOP/s",
                      "achieved": fl_g, "peak": fp32_peak, "frac": fl_g / fp32_peak,

@@ -48,16 +48,16 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const Prob* __restric
     float* A32 = pr->W32 ? pr->W32 + 4 * (size_t)geo.nx * mirror_pitch(geo.ny) : nullptr;
     UpdateArgs a{pr->W, pr->Wold, pr->AX, pr->AY, pr->FXx, pr->FXy, pr->FAx, pr->FAy, pr->ctl, stage, pr->W32, A32};
     const int n = geo.nodex * geo.nodey;
-    double cmin = 1e300;
+    double smax = -1.0;
     unsigned int bad = 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         double c;
         unsigned int b;
         update_one(a, geo, base + threadIdx.x, c, b);
-        cmin = fmin(cmin, c);
+        smax = fmax(smax, c);
         bad |= b;
     }
-    reduce_block(cmin, bad, pr->ctl, stage == cfl_stage(geo));
+    reduce_block_speed(smax, bad, pr->ctl, stage == cfl_stage(geo), geo);
 }
 
 // step prologue for every problem (one block); *counter is the batch step index

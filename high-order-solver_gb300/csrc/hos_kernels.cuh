@@ -447,10 +447,6 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         } else {
             df_factors<T, ORDER>(al, df);
         }
-        T pn1[4], p0[4], pp1[4];
-        to_prim(pn1, st[r - 1], gamma);
-        to_prim(p0, st[r], gamma);
-        to_prim(pp1, st[r + 1], gamma);
         T outv[2][8];
         bool lin = false;
         if (geo.first_order) {
@@ -488,14 +484,21 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                   linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K, slack);
             if (!lin) atomicAdd(&rejected, 1u);
         }
+        // the characteristic bases' primitives, only for cells that take the WENO-AO path
+        T pn1[4], p0[4], pp1[4];
+        if (!lin && geo.characteristic) {
+            to_prim(pn1, st[r - 1], gamma);
+            to_prim(p0, st[r], gamma);
+            to_prim(pp1, st[r + 1], gamma);
+        }
 #pragma unroll
         for (int side = 0; side < 2 && !lin; ++side) {
-            T base[4];
-#pragma unroll
-            for (int v = 0; v < 4; ++v) base[v] = T(0.5) * ((side == 0 ? pn1[v] : pp1[v]) + p0[v]);
             CharBase<T> cb;
             T ch[N][4];
             if (geo.characteristic) {
+                T base[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) base[v] = T(0.5) * ((side == 0 ? pn1[v] : pp1[v]) + p0[v]);
                 cb.init(base, gamma);
 #pragma unroll
                 for (int k = 0; k < N; ++k) cb.to_char(ch[k], st[k]);
@@ -624,12 +627,12 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                     lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K, T(geo.gate_slack));
                 if (!lin) atomicAdd(&rejected, 1u);
             }
-            T base[4], w0c[4];
-#pragma unroll
-            for (int v = 0; v < 4; ++v) w0c[v] = w0[v];
-            to_prim(base, w0c, gamma);
             if (lin) {
             } else if (geo.characteristic) {
+                T base[4], w0c[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) w0c[v] = w0[v];
+                to_prim(base, w0c, gamma);
                 CharBase<T> cb;
                 cb.init(base, gamma);
                 T ch[N][4];
@@ -807,102 +810,137 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     __syncthreads();
 
     // ---------------- phase 4: Gauss quadrature, S2O4 stage combination, face DF indicator ----------------
+    // the FP64 stage combination and the face's global reads and writes, from its Gauss-quadrature
+    // sums of f and f_t (in the compute type) and of the DF contributions
+    auto finish = [&](int fn, int ft, const T* Fq, const T* Dq, T asum) {
+        const int facen = N0 + fn, facet = T0 + ft;
+        const size_t nf = DIR == 0 ? (size_t)(geo.nodex + 1) * geo.nodey : (size_t)geo.nodex * (geo.nodey + 1);
+        const size_t fi = DIR == 0 ? (size_t)facen * geo.nodey + facet : (size_t)facet * (geo.nodey + 1) + facen;
+        double X[4], P[4];
+        const bool s2o4 = geo.integrator == 0;
+        // FP32 kernels, plain S2O4: the FP64 pipe bounds this phase, so the conversions run on
+        // the integer pipes (f32_to_f64, exact) and each result takes one FP64 operation:
+        // X0 = 0.5 F + D / 8 (D / 8 exact in FP32), P0 = F + D / 6, X1 = P0 + D / 3
+        const bool fast64 = sizeof(T) == 4 && s2o4 && !geo.source;
+#pragma unroll
+        for (int v = 0; v < 4 && fast64; ++v) {
+            const float fq = float(Fq[v]), dq = float(Dq[v]);
+            if (a.stage == 0) {
+                const double F = f32_to_f64(fq);
+                X[v] = fma(0.5, F, f32_to_f64(0.125f * dq));
+                P[v] = fma(1.0 / 6.0, f32_to_f64(dq), F);
+            } else {
+                X[v] = fma(1.0 / 3.0, f32_to_f64(dq), a.FP[v * nf + fi]);
+                P[v] = 0.0;
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < 4 && !fast64; ++v) {
+            const double F = double(Fq[v]), D = double(Dq[v]);
+            if (s2o4) {
+                if (geo.source) {
+                    // Update_with_source: the Gauss-weighted f of the stage itself
+                    X[v] = F;
+                    P[v] = 0.0;
+                } else if (a.stage == 0) {
+                    X[v] = 0.5 * F + (1.0 / 8.0) * D;
+                    P[v] = 1.0 * F + (1.0 / 6.0) * D;
+                } else {
+                    X[v] = (1.0 / 3.0) * D;
+                    P[v] = 0.0;
+                }
+            } else {
+                // X_s = sum over stages k <= s of c[s][k] (F_k, D_k) (Update, :378-428)
+                const int sg = a.stage;
+                double x = time_coefficient(geo.integrator, sg, sg, 0) * F +
+                           time_coefficient(geo.integrator, sg, sg, 1) * D;
+                for (int k = 0; k < sg; ++k)
+                    x += time_coefficient(geo.integrator, sg, k, 0) * a.FS[((size_t)k * 4 + v) * nf + fi] +
+                         time_coefficient(geo.integrator, sg, k, 1) * a.DS[((size_t)k * 4 + v) * nf + fi];
+                X[v] = x;
+                if (sg + 1 < geo.stages) {
+                    a.FS[((size_t)sg * 4 + v) * nf + fi] = F;
+                    a.DS[((size_t)sg * 4 + v) * nf + fi] = D;
+                }
+                P[v] = 0.0;
+            }
+        }
+        // mean over Gauss points, zeroed below 2 (Calculate_alpha, :1497-1516)
+        // FP64 divides as the reference does; the FP32 path takes the mean in FP32 (an
+        // indicator, not part of the FP64 stage combination) instead of a double division
+        if constexpr (sizeof(T) == 8) {
+            const double as = double(asum);
+            const double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
+            a.FA[fi] = am < 2.0 ? 0.0 : am;
+        } else {
+            const float am = float(GP == 2 ? T(0.5) * asum : GP == 3 ? asum * T(1.0 / 3.0) : T(0.25) * asum);
+            a.FA[fi] = am < 2.0f ? 0.0 : f32_to_f64(am);
+        }
+        if (s2o4 && a.stage == 1 && !geo.source && !fast64) {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
+        }
+        // y-face local (normal, tangential) momentum -> global (Local_to_Global, :1226-1233)
+        double Xg[4] = {X[0], X[1], X[2], X[3]};
+        if (DIR == 1) { Xg[1] = -X[2]; Xg[2] = X[1]; }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) a.FX[v * nf + fi] = Xg[v];
+        if (s2o4 && a.stage == 0) {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) a.FP[v * nf + fi] = P[v];
+        }
+    };
+    // y faces lie along n in memory (fi = t (nodey + 1) + n) while the tile's threads run along t:
+    // their sums are staged in the Gauss-state region (free after phase 3), [9][TILE_T][TILE_N + 1]
+    // (the padding keeps both passes free of bank conflicts), and the combination runs with
+    // consecutive threads on consecutive faces of memory, so its global accesses coalesce
+    constexpr int SP = TILE_N + 1;
+    T* qst = gst;
 #pragma unroll 1
     for (int fidx = tid; fidx < TILE_N * TILE_T; fidx += FACE_THREADS) {
         const int fn = fidx / TILE_T, ft = fidx % TILE_T;
-        const int facen = N0 + fn, facet = T0 + ft;
-        if (facen <= nodeN && facet < nodeT) {
-            const size_t nf = DIR == 0 ? (size_t)(geo.nodex + 1) * geo.nodey : (size_t)geo.nodex * (geo.nodey + 1);
-            const size_t fi = DIR == 0 ? (size_t)facen * geo.nodey + facet : (size_t)facet * (geo.nodey + 1) + facen;
-            // Gauss quadrature of f and f_t over the face in the compute type; the S2O4
-            // stage combination of the two time-integral moments below is FP64
-            T Fq[4], Dq[4], asum = T(0.0);
+        if (N0 + fn > nodeN || T0 + ft >= nodeT) continue;
+        // Gauss quadrature of f and f_t over the face in the compute type; the S2O4 stage
+        // combination of the two time-integral moments is FP64
+        T Fq[4], Dq[4], asum = T(0.0);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) { Fq[v] = T(0.0); Dq[v] = T(0.0); }
+        for (int v = 0; v < 4; ++v) { Fq[v] = T(0.0); Dq[v] = T(0.0); }
 #pragma unroll
-            for (int ig = 0; ig < GP; ++ig) {
-                const T* o = flux + (fidx * GP + ig) * 9;
-                const T gw = T(gauss_weight<GP>(ig));
+        for (int ig = 0; ig < GP; ++ig) {
+            const T* o = flux + (fidx * GP + ig) * 9;
+            const T gw = T(gauss_weight<GP>(ig));
 #pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    Fq[v] += gw * o[v];
-                    Dq[v] += gw * o[4 + v];
-                }
-                asum += o[8];
+            for (int v = 0; v < 4; ++v) {
+                Fq[v] += gw * o[v];
+                Dq[v] += gw * o[4 + v];
             }
-            double X[4], P[4];
-            const bool s2o4 = geo.integrator == 0;
-            // FP32 kernels, plain S2O4: the FP64 pipe bounds this phase, so the conversions run on
-            // the integer pipes (f32_to_f64, exact) and each result takes one FP64 operation:
-            // X0 = 0.5 F + D / 8 (D / 8 exact in FP32), P0 = F + D / 6, X1 = P0 + D / 3
-            const bool fast64 = sizeof(T) == 4 && s2o4 && !geo.source;
+            asum += o[8];
+        }
+        if constexpr (DIR == 0) {
+            finish(fn, ft, Fq, Dq, asum);
+        } else {
 #pragma unroll
-            for (int v = 0; v < 4 && fast64; ++v) {
-                const float fq = float(Fq[v]), dq = float(Dq[v]);
-                if (a.stage == 0) {
-                    const double F = f32_to_f64(fq);
-                    X[v] = fma(0.5, F, f32_to_f64(0.125f * dq));
-                    P[v] = fma(1.0 / 6.0, f32_to_f64(dq), F);
-                } else {
-                    X[v] = fma(1.0 / 3.0, f32_to_f64(dq), a.FP[v * nf + fi]);
-                    P[v] = 0.0;
-                }
+            for (int v = 0; v < 4; ++v) {
+                qst[(v * TILE_T + ft) * SP + fn] = Fq[v];
+                qst[((4 + v) * TILE_T + ft) * SP + fn] = Dq[v];
             }
+            qst[(8 * TILE_T + ft) * SP + fn] = asum;
+        }
+    }
+    if constexpr (DIR == 1) {
+        static_assert(9 * TILE_T * (TILE_N + 1) <= S::GSTATES, "the staged sums must fit the Gauss-state region");
+        __syncthreads();
+#pragma unroll 1
+        for (int fc = tid; fc < TILE_N * TILE_T; fc += FACE_THREADS) {
+            const int fn = fc % TILE_N, ft = fc / TILE_N;
+            if (N0 + fn > nodeN || T0 + ft >= nodeT) continue;
+            T Fq[4], Dq[4];
 #pragma unroll
-            for (int v = 0; v < 4 && !fast64; ++v) {
-                const double F = double(Fq[v]), D = double(Dq[v]);
-                if (s2o4) {
-                    if (geo.source) {
-                        // Update_with_source: the Gauss-weighted f of the stage itself
-                        X[v] = F;
-                        P[v] = 0.0;
-                    } else if (a.stage == 0) {
-                        X[v] = 0.5 * F + (1.0 / 8.0) * D;
-                        P[v] = 1.0 * F + (1.0 / 6.0) * D;
-                    } else {
-                        X[v] = (1.0 / 3.0) * D;
-                        P[v] = 0.0;
-                    }
-                } else {
-                    // X_s = sum over stages k <= s of c[s][k] (F_k, D_k) (Update, :378-428)
-                    const int sg = a.stage;
-                    double x = time_coefficient(geo.integrator, sg, sg, 0) * F +
-                               time_coefficient(geo.integrator, sg, sg, 1) * D;
-                    for (int k = 0; k < sg; ++k)
-                        x += time_coefficient(geo.integrator, sg, k, 0) * a.FS[((size_t)k * 4 + v) * nf + fi] +
-                             time_coefficient(geo.integrator, sg, k, 1) * a.DS[((size_t)k * 4 + v) * nf + fi];
-                    X[v] = x;
-                    if (sg + 1 < geo.stages) {
-                        a.FS[((size_t)sg * 4 + v) * nf + fi] = F;
-                        a.DS[((size_t)sg * 4 + v) * nf + fi] = D;
-                    }
-                    P[v] = 0.0;
-                }
+            for (int v = 0; v < 4; ++v) {
+                Fq[v] = qst[(v * TILE_T + ft) * SP + fn];
+                Dq[v] = qst[((4 + v) * TILE_T + ft) * SP + fn];
             }
-            // mean over Gauss points, zeroed below 2 (Calculate_alpha, :1497-1516)
-            // FP64 divides as the reference does; the FP32 path takes the mean in FP32 (an
-            // indicator, not part of the FP64 stage combination) instead of a double division
-            if constexpr (sizeof(T) == 8) {
-                const double as = double(asum);
-                const double am = GP == 2 ? 0.5 * as : GP == 3 ? as / 3.0 : 0.25 * as;
-                a.FA[fi] = am < 2.0 ? 0.0 : am;
-            } else {
-                const float am = float(GP == 2 ? T(0.5) * asum : GP == 3 ? asum * T(1.0 / 3.0) : T(0.25) * asum);
-                a.FA[fi] = am < 2.0f ? 0.0 : f32_to_f64(am);
-            }
-            if (s2o4 && a.stage == 1 && !geo.source && !fast64) {
-#pragma unroll
-                for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
-            }
-            // y-face local (normal, tangential) momentum -> global (Local_to_Global, :1226-1233)
-            double Xg[4] = {X[0], X[1], X[2], X[3]};
-            if (DIR == 1) { Xg[1] = -X[2]; Xg[2] = X[1]; }
-#pragma unroll
-            for (int v = 0; v < 4; ++v) a.FX[v * nf + fi] = Xg[v];
-            if (s2o4 && a.stage == 0) {
-#pragma unroll
-                for (int v = 0; v < 4; ++v) a.FP[v * nf + fi] = P[v];
-            }
+            finish(fn, ft, Fq, Dq, qst[(8 * TILE_T + ft) * SP + fn]);
         }
     }
 }

@@ -50,51 +50,26 @@ __global__ void mirror_state_kernel(const double* __restrict__ W, const double* 
 
 __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo) {
     if (!a.ctl->active) return;
-    double cand;
+    double spd;
     unsigned int bad;
-    update_one(a, geo, blockIdx.x * blockDim.x + threadIdx.x, cand, bad);
-    reduce_block(cand, bad, a.ctl, a.stage == cfl_stage(geo));
+    update_one(a, geo, blockIdx.x * blockDim.x + threadIdx.x, spd, bad);
+    reduce_block_speed(spd, bad, a.ctl, a.stage == cfl_stage(geo), geo);
 }
 
 // CFL candidates from a primitive state (the initial data's primvar at step 0)
 __global__ void __launch_bounds__(256) cfl_from_prim_kernel(const double* __restrict__ prim, Geometry geo, StepCtl* ctl) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    double cand = 1e300;
+    double spd = -1.0;
     unsigned int bad = 0;
     if (idx < geo.nodex * geo.nodey) {
         const int I = idx / geo.nodey, J = idx % geo.nodey;
         const size_t plane = (size_t)geo.nx * geo.ny;
         const size_t c = (size_t)(I + geo.g) * geo.ny + (J + geo.g);
         const double rho = prim[c], u = prim[plane + c], v = prim[2 * plane + c], p = prim[3 * plane + c];
-        const double tmp = sqrt(u * u + v * v) + sqrt(geo.gamma * p / rho);
-        const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
-        if (qx > 0) cand = qx;
-        if (qy > 0 && qy < cand) cand = qy;
-        if (geo.tau_type == 1 && geo.mu > 0) {   // viscous cap of Dtx
-            const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
-            const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
-            if (cx < cand) cand = cx;
-            if (cy < cand) cand = cy;
-        }
+        spd = signal_speed(sqrt(u * u + v * v) + sqrt(geo.gamma * p / rho));
         if (rho < 0 || p < 0 || isnan(rho) || isnan(p)) bad = 1;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        cand = fmin(cand, __shfl_xor_sync(0xffffffffu, cand, o));
-        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
-    }
-    __shared__ double sc[8];
-    __shared__ unsigned int sb[8];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { sc[wid] = cand; sb[wid] = bad; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = sc[0];
-        unsigned int b = sb[0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmin(m, sc[k]); b |= sb[k]; }
-        if (m < 1e300) atomic_min_pos(&ctl->cfl_bits, m);
-        if (b) atomicOr(&ctl->status, 1u);
-    }
+    reduce_block_speed<true>(spd, bad, ctl, true, geo);
 }
 
 __global__ void begin_step_kernel(StepCtl* ctl, double tstop, double seed) { begin_step_one(ctl, tstop, seed); }
@@ -105,10 +80,19 @@ __global__ void aos_to_soa_kernel(const double* __restrict__ aos, double* __rest
     if (c >= n) return;
     for (int v = 0; v < 4; ++v) soa[v * n + c] = aos[4 * c + v];
 }
-__global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __restrict__ aos, size_t n) {
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    for (int v = 0; v < 4; ++v) aos[4 * c + v] = soa[v * n + c];
+// SoA -> AoS staged through shared memory, so that each warp writes 256 contiguous bytes: the
+// destination may be pinned host memory written over the host link, where a warp's strided
+// 8-byte stores would each move a partial line.  blockDim.x == 256.
+__global__ void __launch_bounds__(256) soa_to_aos_kernel(const double* __restrict__ soa, double* __restrict__ aos,
+                                                         size_t n) {
+    __shared__ double t[4][256];
+    const size_t c0 = (size_t)blockIdx.x * 256;
+    const int tid = threadIdx.x;
+    if (c0 + tid < n)
+        for (int v = 0; v < 4; ++v) t[v][tid] = soa[v * n + c0 + tid];
+    __syncthreads();
+    const int m = (int)(n - c0 < 256 ? n - c0 : 256) * 4;
+    for (int k = tid; k < m; k += 256) aos[4 * c0 + k] = t[k & 3][k >> 2];
 }
 // The host-facing upload in one pass over the cells (hos2d_set_state): the staged AoS conserved
 // state into the SoA planes, the DF indicators zeroed, the FP32 mirror (if any) written, and for
@@ -120,7 +104,7 @@ __global__ void __launch_bounds__(256) upload_state_kernel(const double* __restr
                                                            float* __restrict__ W32, Geometry geo, StepCtl* ctl) {
     const size_t n = (size_t)geo.nx * geo.ny;
     const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    double cand = 1e300;
+    double spd = -1.0;
     unsigned int bad = 0;
     if (c < n) {
         double w[4];
@@ -149,20 +133,11 @@ __global__ void __launch_bounds__(256) upload_state_kernel(const double* __restr
                 to_prim<double>(p, w, geo.gamma);
             }
             const double rho = p[0], u = p[1], v = p[2], pr = p[3];
-            const double tmp = sqrt(u * u + v * v) + sqrt(geo.gamma * pr / rho);
-            const double qx = geo.cfl * geo.dx / tmp, qy = geo.cfl * geo.dy / tmp;
-            if (qx > 0) cand = qx;
-            if (qy > 0 && qy < cand) cand = qy;
-            if (geo.tau_type == 1 && geo.mu > 0) {   // viscous cap of Dtx
-                const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
-                const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
-                if (cx < cand) cand = cx;
-                if (cy < cand) cand = cy;
-            }
+            spd = signal_speed(sqrt(u * u + v * v) + sqrt(geo.gamma * pr / rho));
             if (rho < 0 || pr < 0 || isnan(rho) || isnan(pr)) bad = 1;
         }
     }
-    reduce_block(cand, bad, ctl, true);
+    reduce_block_speed<true>(spd, bad, ctl, true, geo);
 }
 
 // primitive variables of a conserved state (Convar_to_primvar_2D, src/basic_function.cpp:811-817)
@@ -232,6 +207,19 @@ static int fail(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
+// The device address of a pinned host buffer (cudaHostAlloc, cudaMallocHost, cudaHostRegister:
+// under unified addressing every pinned allocation is mapped), else nullptr.  The host-facing
+// transfers read and write such buffers from their kernels over the host link, which moves the
+// data at the copy engine's rate and leaves out the staging pass on the device.
+static const void* mapped_host(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 static int cuda_fail(cudaError_t e, const char* where) {
     return fail(HOS_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
@@ -309,6 +297,7 @@ struct hos_solver2d {
     double* stagex = nullptr;   // methods other than S2O4: per-stage F and D of x faces [2][4][4][nfx]
     double* stagey = nullptr;   // ... and of y faces
     StepCtl* ctl = nullptr;
+    StepCtl* hctl = nullptr;    // pinned host copy: control-word uploads and read-backs on the stream
     // captured step
     cudaGraphExec_t graph = nullptr;
     double graph_tstop = 0.0;
@@ -367,6 +356,7 @@ void free_all(hos_solver2d* s) {
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->ctl) cudaFree(s->ctl);
+    if (s->hctl) cudaFreeHost(s->hctl);
     void* gbufs[] = {s->gflags, s->gflags2, s->gstats, s->gw, s->gb, s->W32};
     for (void* b : gbufs)
         if (b) cudaFree(b);
@@ -591,10 +581,11 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
         }
         cudaMemset(*a.p, 0, a.n * sizeof(double));
     }
-    if ((e = cudaMalloc(&s->ctl, sizeof(StepCtl))) != cudaSuccess) {
+    if ((e = cudaMalloc(&s->ctl, sizeof(StepCtl))) != cudaSuccess ||
+        (e = cudaMallocHost(&s->hctl, sizeof(StepCtl))) != cudaSuccess) {
         free_all(s);
         delete s;
-        return fail(HOS_E_NOMEM, "cudaMalloc ctl");
+        return fail(HOS_E_NOMEM, "ctl allocation");
     }
     if (precision == HOS_FP32) {
         const size_t n32 = (size_t)s->geo.nx * mirror_pitch(s->geo.ny);
@@ -642,28 +633,41 @@ int hos2d_dims(const hos_solver2d* s, int* nx, int* ny) {
 int hos2d_set_state(hos_solver2d* s, const double* convar, const double* primvar) {
     if (!s || !convar) return fail(HOS_E_ARG, "null argument");
     const size_t n = s->ncell;
-    double* stage = s->scratch;               // AoS staging [n][4] of convar ...
-    double* stage_prim = s->scratch + 4 * n;  // ... and of primvar
-    // the copies back to back, then one pass (upload_state_kernel) for the transposition, the
-    // DF indicators, the FP32 mirror and the first CFL candidates
-    cudaError_t e = cudaMemcpyAsync(stage, convar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "upload convar");
-    if (primvar &&
-        (e = cudaMemcpyAsync(stage_prim, primvar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
-        return cuda_fail(e, "upload primvar");
+    // one pass (upload_state_kernel) for the transposition, the DF indicators, the FP32 mirror
+    // and the first CFL candidates; it reads pinned host buffers over the host link, other
+    // buffers from a device staging copy (AoS [n][4] of convar, then of primvar)
+    const double* src = static_cast<const double*>(mapped_host(convar));
+    const double* src_prim = primvar ? static_cast<const double*>(mapped_host(primvar)) : nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!src) {
+        double* stage = s->scratch;
+        if ((e = cudaMemcpyAsync(stage, convar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+            return cuda_fail(e, "upload convar");
+        src = stage;
+    }
+    if (primvar && !src_prim) {
+        double* stage_prim = s->scratch + 4 * n;
+        if ((e = cudaMemcpyAsync(stage_prim, primvar, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream)) !=
+            cudaSuccess)
+            return cuda_fail(e, "upload primvar");
+        src_prim = stage_prim;
+    }
+    // the control word reset from the pinned host copy, read back into it after the pass: one
+    // synchronisation
     StepCtl c{};
     double seed = s->geo.dx;
     std::memcpy(&c.cfl_bits, &seed, sizeof seed);
     c.active = 1;
-    if ((e = cudaMemcpyAsync(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+    *s->hctl = c;
+    if ((e = cudaMemcpyAsync(s->ctl, s->hctl, sizeof c, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
         return cuda_fail(e, "ctl upload");
-    upload_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(stage, primvar ? stage_prim : nullptr, s->W,
-                                                                             s->AX, s->AY, s->W32, s->geo, s->ctl);
+    upload_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(src, src_prim, s->W, s->AX, s->AY, s->W32,
+                                                                             s->geo, s->ctl);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "set_state");
+    if ((e = cudaMemcpyAsync(s->hctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "ctl read");
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "set_state");
-    StepCtl back;
-    if ((e = cudaMemcpy(&back, s->ctl, sizeof back, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "ctl read");
-    if (back.status & 1u) return fail(HOS_E_BLOWUP, "initial state has negative density/pressure or NaN");
+    if (s->hctl->status & 1u) return fail(HOS_E_BLOWUP, "initial state has negative density/pressure or NaN");
     return HOS_OK;
 }
 
@@ -699,16 +703,22 @@ int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* al
     double* prim = s->scratch + 4 * n;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     cudaError_t e;
+    // pinned host buffers are written by the transposition itself over the host link; other
+    // buffers through a device staging copy
     if (convar) {
-        soa_to_aos_kernel<<<blocks, 256, 0, s->stream>>>(s->W, stage, n);
-        if ((e = cudaMemcpyAsync(convar, stage, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+        double* dst = static_cast<double*>(const_cast<void*>(mapped_host(convar)));
+        soa_to_aos_kernel<<<blocks, 256, 0, s->stream>>>(s->W, dst ? dst : stage, n);
+        if (!dst && (e = cudaMemcpyAsync(convar, stage, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) !=
+                        cudaSuccess)
             return cuda_fail(e, "download convar");
         if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "download convar");
     }
     if (primvar) {
+        double* dst = static_cast<double*>(const_cast<void*>(mapped_host(primvar)));
         prim_of_state_kernel<<<blocks, 256, 0, s->stream>>>(s->W, prim, n, s->geo.gamma);
-        soa_to_aos_kernel<<<blocks, 256, 0, s->stream>>>(prim, stage, n);
-        if ((e = cudaMemcpyAsync(primvar, stage, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+        soa_to_aos_kernel<<<blocks, 256, 0, s->stream>>>(prim, dst ? dst : stage, n);
+        if (!dst && (e = cudaMemcpyAsync(primvar, stage, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) !=
+                        cudaSuccess)
             return cuda_fail(e, "download primvar");
         if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "download primvar");
     }
@@ -940,10 +950,10 @@ int hos2d_advance(hos_solver2d* s, int nsteps, double tstop, int use_graph) {
 
 int hos2d_sync(hos_solver2d* s, double* t, double* dt) {
     if (!s) return fail(HOS_E_ARG, "null solver");
-    cudaError_t e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "sync");
-    StepCtl c;
-    if ((e = cudaMemcpy(&c, s->ctl, sizeof c, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "ctl read");
+    cudaError_t e = cudaMemcpyAsync(s->hctl, s->ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "ctl read");
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "sync");
+    const StepCtl c = *s->hctl;
     if (t) *t = c.t;
     if (dt) *dt = c.dt;
     if (c.status & 1u) return fail(HOS_E_BLOWUP, "negative density/pressure or NaN in the state");

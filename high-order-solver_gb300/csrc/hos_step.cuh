@@ -110,11 +110,18 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* addr, double 
 // the stage whose update produces the next step's CFL candidates
 __device__ __forceinline__ int cfl_stage(const Geometry& geo) { return geo.stages >= 2 ? geo.stages - 2 : 0; }
 
-// update of interior cell idx; returns its CFL candidate (at cfl_stage) and blow-up bit
-__device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& geo, int idx, double& cand,
+// a cell's signal speed |u| + c for the CFL reduction; one that is not finite gives no candidate
+// in Dtx (its dt is not > 0), as 0 does in cfl_of_speed (dt = inf)
+__device__ __forceinline__ double signal_speed(double tmp) { return tmp <= 1.7976931348623157e308 ? tmp : 0.0; }
+
+// update of interior cell idx; returns its signal speed |u| + c for the CFL (at cfl_stage; 0 when
+// it is not finite, -1 for no candidate) and its blow-up bit.  Dtx's candidate CFL dx / (|u| + c)
+// falls monotonically with the speed, so the block converts its largest speed once
+// (cfl_of_speed) and gets the same minimum.
+__device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& geo, int idx, double& spd,
                                            unsigned int& bad) {
     const int nodex = geo.nodex, nodey = geo.nodey, g = geo.g, ny = geo.ny;
-    cand = 1e300;
+    spd = -1.0;
     bad = 0;
     if (idx < nodex * nodey) {
         const int I = idx / nodey, J = idx % nodey;
@@ -205,40 +212,62 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 pr[2] = w0[2] * ir2;
                 pr[3] = (geo.gamma - 1.0) * (w0[3] - 0.5 * (w0[1] * pr[1] + w0[2] * pr[2]));
             }
-            // Dtx (src/time_advance.cpp:264-305) with one reciprocal for both directions
+            // Dtx's speed (src/time_advance.cpp:295)
             const double tmp = sqrt(pr[1] * pr[1] + pr[2] * pr[2]) + sqrt(geo.gamma * pr[3] * ir2);
-            const double it = geo.cfl / tmp;
-            const double qx = geo.dx * it, qy = geo.dy * it;
-            if (qx > 0) cand = qx;
-            if (qy > 0 && qy < cand) cand = qy;
-            if (geo.tau_type == 1 && geo.mu > 0) {
-                // viscous cap of Dtx (src/time_advance.cpp:300-303), the same for every cell
-                const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
-                const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
-                if (cx < cand) cand = cx;
-                if (cy < cand) cand = cy;
-            }
+            spd = signal_speed(tmp);
         }
     }
 }
 
-// block reduction of the CFL candidates and status bits into one problem's control word
-__device__ __forceinline__ void reduce_block(double cand, unsigned int bad, StepCtl* ctl, bool do_cfl) {
+// Dtx (src/time_advance.cpp:264-305) for the largest signal speed of a set of cells: the update
+// takes one reciprocal for both directions, the upload of a state the reference's CFL dx / tmp
+// (REF); the viscous cap (:300-303) is the same for every cell.  A negative speed: no cell of the
+// set produced a candidate.
+template <bool REF = false>
+__device__ __forceinline__ double cfl_of_speed(const Geometry& geo, double smax) {
+    double cand = 1e300;
+    if (!(smax >= 0.0)) return cand;
+    double qx, qy;
+    if constexpr (REF) {
+        qx = geo.cfl * geo.dx / smax;
+        qy = geo.cfl * geo.dy / smax;
+    } else {
+        const double it = geo.cfl / smax;
+        qx = geo.dx * it;
+        qy = geo.dy * it;
+    }
+    if (qx > 0) cand = qx;
+    if (qy > 0 && qy < cand) cand = qy;
+    if (geo.tau_type == 1 && geo.mu > 0) {
+        const double cx = 0.25 * geo.cfl * geo.dx * geo.dx / geo.mu;
+        const double cy = 0.25 * geo.cfl * geo.dy * geo.dy / geo.mu;
+        if (cx < cand) cand = cx;
+        if (cy < cand) cand = cy;
+    }
+    return cand;
+}
+
+// block reduction of the cells' signal speeds (update_one) and status bits into one problem's
+// control word: the largest speed, converted to the block's CFL candidate by one thread
+template <bool REF = false>
+__device__ __forceinline__ void reduce_block_speed(double spd, unsigned int bad, StepCtl* ctl, bool do_cfl,
+                                                   const Geometry& geo) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        cand = fmin(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+        spd = fmax(spd, __shfl_xor_sync(0xffffffffu, spd, o));
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     __shared__ double sc[8];
     __shared__ unsigned int sb[8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { sc[wid] = cand; sb[wid] = bad; }
+    if (lane == 0) { sc[wid] = spd; sb[wid] = bad; }
     __syncthreads();
     if (threadIdx.x == 0) {
         double m = sc[0];
         unsigned int b = sb[0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmin(m, sc[k]); b |= sb[k]; }
-        if (do_cfl && m < 1e300) atomic_min_pos(&ctl->cfl_bits, m);
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmax(m, sc[k]); b |= sb[k]; }
+        const double cand = cfl_of_speed<REF>(geo, m);
+        if (do_cfl && cand < 1e300) atomic_min_pos(&ctl->cfl_bits, cand);
         if (b) atomicOr(&ctl->status, 1u);
     }
 }

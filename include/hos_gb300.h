@@ -129,7 +129,9 @@ int hos2d_dims(const hos_solver2d* s, int* nx, int* ny);
 
 /* Upload the conserved state (host, [nx*ny][4]) and optionally the primitive state the
  * first step's CFL reads (host, [nx*ny][4], may be NULL: then derived from convar).
- * Resets time to 0 and the DF indicators to 0.  Synchronous. */
+ * Resets time to 0 and the DF indicators to 0.  Synchronous.  Pinned host buffers
+ * (cudaHostAlloc, cudaMallocHost, cudaHostRegister) are read by the upload kernel over the host
+ * link; other host memory goes through a device staging copy first. */
 int hos2d_set_state(hos_solver2d* s, const double* convar, const double* primvar);
 /* Same from device memory already resident in HBM (SoA planes [4][nx*ny]). */
 int hos2d_set_state_device(hos_solver2d* s, const double* d_convar_soa, const double* d_primvar_soa);
@@ -139,7 +141,8 @@ int hos2d_set_state_device(hos_solver2d* s, const double* d_convar_soa, const do
 int hos2d_set_alpha(hos_solver2d* s, const double* alpha_x, const double* alpha_y);
 
 /* Download the conserved state, its primitive variables, alpha_x, alpha_y (host arrays;
- * any pointer may be NULL).  Synchronous. */
+ * any pointer may be NULL).  Synchronous.  Pinned convar / primvar buffers are written by the
+ * transposition kernel over the host link; other host memory through a device staging copy. */
 int hos2d_get_state(hos_solver2d* s, double* convar, double* primvar, double* alpha_x, double* alpha_y);
 
 /* Replace the four boundary kinds (HOS_BC_*, left, right, down, up) and, when bc_prim is not
