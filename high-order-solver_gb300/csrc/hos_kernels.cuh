@@ -59,6 +59,10 @@ struct Geometry {
     // fraction of it (density and total energy of a linear reconstruction)
     float gate_slack = 0.1f;
     int stages = 2;
+    // 1 (the single-problem FP32 solvers): under plain S2O4 the face kernels store the stage-
+    // combined fluxes per unit cell width -- the FP32 quadrature sums times the inverse normal
+    // spacing, in FP32 -- and the update (update_kernel_scaled) sums them without FP64 products
+    int scaled_flux = 0;
     // 1 / dx, 1 / dy, set on the host by set_spacing(): a double division costs the FP64 pipe
     // about ten instructions per thread
     double idx = 0.0, idy = 0.0;
@@ -440,13 +444,6 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             for (int v = 0; v < 4; ++v) st[k][v] = q[v];
             al[k] = antile[(nl + k) * TL + tl];
         }
-        T df[NW];
-        if constexpr (PLAIN) {
-#pragma unroll
-            for (int k = 0; k < NW; ++k) df[k] = T(1.0);
-        } else {
-            df_factors<T, ORDER>(al, df);
-        }
         T outv[2][8];
         bool lin = false;
         if (geo.first_order) {
@@ -463,7 +460,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             // linear reconstruction commutes with the characteristic projection; two variables
             // per paired FP32 operation
             using C = lin::Normal<ORDER>;
-            const F2 dft(df[NW - 1]), dfi(df[NW - 1] * hN);
+            const T dfl = df_full<T, ORDER>(al);
+            const F2 dft(dfl), dfi(dfl * hN);
 #pragma unroll
             for (int vp = 0; vp < 2; ++vp) {
                 F2 s2[N];
@@ -484,7 +482,17 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                   linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K, slack);
             if (!lin) atomicAdd(&rejected, 1u);
         }
-        // the characteristic bases' primitives, only for cells that take the WENO-AO path
+        // the DF factors and the characteristic bases' primitives, only for cells that take the
+        // WENO-AO path
+        T df[NW];
+        if (!lin) {
+            if constexpr (PLAIN) {
+#pragma unroll
+                for (int k = 0; k < NW; ++k) df[k] = T(1.0);
+            } else {
+                df_factors<T, ORDER>(al, df);
+            }
+        }
         T pn1[4], p0[4], pp1[4];
         if (!lin && geo.characteristic) {
             to_prim(pn1, st[r - 1], gamma);
@@ -572,13 +580,6 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             T al[N];
 #pragma unroll
             for (int k = 0; k < N; ++k) al[k] = attile[(fn + side) * TL + tc + sgn * (k - r)];
-            T df[NW];
-            if constexpr (PLAIN) {
-#pragma unroll
-                for (int k = 0; k < NW; ++k) df[k] = T(1.0);
-            } else {
-                df_factors<T, ORDER>(al, df);
-            }
             auto line = [&](int k, int sd) -> LineRef<T> {
                 return LineRef<T>{lines + ((fn * 4 * TL + (tc + sgn * (k - r))) * 2 + sd) * 2, 4 * TL};
             };
@@ -603,7 +604,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 // Gauss points, in conservative variables; two line entries per paired FP32
                 // operation (values and normal slopes; tangential slopes of the values)
                 using C = lin::Tangent<ORDER>;
-                const F2 dft(df[NW - 1]), dfi(df[NW - 1] * hT);
+                const T dfl = df_full<T, ORDER>(al);
+                const F2 dft(dfl), dfi(dfl * hT);
 #pragma unroll
                 for (int vp = 0; vp < 4; ++vp) {
                     F2 s2[N];
@@ -626,6 +628,16 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 for (int ig = 0; ig < GP; ++ig)
                     lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K, T(geo.gate_slack));
                 if (!lin) atomicAdd(&rejected, 1u);
+            }
+            // the DF factors, only for faces that take the WENO-AO path
+            T df[NW];
+            if (!lin) {
+                if constexpr (PLAIN) {
+#pragma unroll
+                    for (int k = 0; k < NW; ++k) df[k] = T(1.0);
+                } else {
+                    df_factors<T, ORDER>(al, df);
+                }
             }
             if (lin) {
             } else if (geo.characteristic) {
@@ -822,9 +834,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         // the integer pipes (f32_to_f64, exact) and each result takes one FP64 operation:
         // X0 = 0.5 F + D / 8 (D / 8 exact in FP32), P0 = F + D / 6, X1 = P0 + D / 3
         const bool fast64 = sizeof(T) == 4 && s2o4 && !geo.source;
+        const float sc = geo.scaled_flux ? float(hN) : 1.0f;
 #pragma unroll
         for (int v = 0; v < 4 && fast64; ++v) {
-            const float fq = float(Fq[v]), dq = float(Dq[v]);
+            const float fq = float(Fq[v]) * sc, dq = float(Dq[v]) * sc;
             if (a.stage == 0) {
                 const double F = f32_to_f64(fq);
                 X[v] = fma(0.5, F, f32_to_f64(0.125f * dq));

@@ -55,6 +55,14 @@ __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo)
     update_one(a, geo, blockIdx.x * blockDim.x + threadIdx.x, spd, bad);
     reduce_block_speed(spd, bad, a.ctl, a.stage == cfl_stage(geo), geo);
 }
+// the same for fluxes stored per unit cell width (Geometry::scaled_flux, plain S2O4)
+__global__ void __launch_bounds__(256) update_kernel_scaled(UpdateArgs a, Geometry geo) {
+    if (!a.ctl->active) return;
+    double spd;
+    unsigned int bad;
+    update_one<true>(a, geo, blockIdx.x * blockDim.x + threadIdx.x, spd, bad);
+    reduce_block_speed(spd, bad, a.ctl, a.stage == cfl_stage(geo), geo);
+}
 
 // CFL candidates from a primitive state (the initial data's primvar at step 0)
 __global__ void __launch_bounds__(256) cfl_from_prim_kernel(const double* __restrict__ prim, Geometry geo, StepCtl* ctl) {
@@ -417,7 +425,10 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
     UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage, s->W32, s->A32};
     const int n = geo.nodex * geo.nodey;
-    update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
+    if (geo.scaled_flux && geo.integrator == HOS_INT_S2O4 && !geo.source)
+        update_kernel_scaled<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
+    else
+        update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "update");
     mark(4);
     return HOS_OK;
@@ -559,6 +570,7 @@ int hos2d_create(const hos_params2d* params, int precision, hos_solver2d** out) 
     geo.nu = p.nu;
     geo.prandtl_coef = p.tau_type == HOS_TAU_NS && p.prandtl_fix ? 1.0 / p.prandtl - 1.0 : 0.0;
     geo.prandtl = p.prandtl;
+    geo.scaled_flux = precision == HOS_FP32 ? 1 : 0;
     fill_boundaries(s->bc, p, geo.dx);
     s->ncell = (size_t)geo.nx * geo.ny;
     s->nfx = (size_t)(geo.nodex + 1) * geo.nodey;

@@ -118,6 +118,8 @@ __device__ __forceinline__ double signal_speed(double tmp) { return tmp <= 1.797
 // it is not finite, -1 for no candidate) and its blow-up bit.  Dtx's candidate CFL dx / (|u| + c)
 // falls monotonically with the speed, so the block converts its largest speed once
 // (cfl_of_speed) and gets the same minimum.
+// SCALED: the fluxes are stored per unit cell width (Geometry::scaled_flux; plain S2O4 only).
+template <bool SCALED = false>
 __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& geo, int idx, double& spd,
                                            unsigned int& bad) {
     const int nodex = geo.nodex, nodey = geo.nodey, g = geo.g, ny = geo.ny;
@@ -151,8 +153,12 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 old = a.Wold[v * plane + c];
             }
             w0[v] = cur;
-            const double rate = (a.FXy[v * nfy + fd] - a.FXy[v * nfy + fu]) * geo.idy +
-                                (a.FXx[v * nfx + fl] - a.FXx[v * nfx + fr]) * geo.idx;
+            double rate;
+            if constexpr (SCALED)
+                rate = (a.FXy[v * nfy + fd] - a.FXy[v * nfy + fu]) + (a.FXx[v * nfx + fl] - a.FXx[v * nfx + fr]);
+            else
+                rate = (a.FXy[v * nfy + fd] - a.FXy[v * nfy + fu]) * geo.idy +
+                       (a.FXx[v * nfx + fl] - a.FXx[v * nfx + fr]) * geo.idx;
             if (geo.source) {
                 // Update_with_source under S2O4 (src/time_advance.cpp:534-704): stage 0 takes
                 // W_old + dt (L + S), S = (0, 0, rho, rho v) of the stage's state; stage 1

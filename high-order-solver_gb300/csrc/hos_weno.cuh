@@ -258,6 +258,17 @@ __device__ __forceinline__ void df_factors(const T* a, T* df) {
     for (int k = 0; k < AO<ORDER>::N; ++k) df[k] = s[k] < T(2.0) ? T(1.0) : T(2.0) / s[k];
 }
 
+// the full stencil's factor alone (df_factors' last entry, the same arithmetic): the gate's
+// linear path needs no other
+template <class T, int ORDER>
+__device__ __forceinline__ T df_full(const T* a) {
+    T s;
+    if (ORDER == 5) s = a[0] + a[2] + a[4];
+    else if (ORDER == 7) s = a[0] + a[2] + a[4] + a[6];
+    else s = a[0] + a[2] + a[4] + a[6] + a[8];
+    return s < T(2.0) ? T(1.0) : T(2.0) / s;
+}
+
 // ---- candidate polynomials at the left (SIDE 0) or right (SIDE 1) face of the centre cell ----
 template <class T, int ORDER, int SIDE>
 __device__ __forceinline__ void normal_face(const T* s, const T* df, T ih, T* p, T* px) {
