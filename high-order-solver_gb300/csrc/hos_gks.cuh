@@ -309,8 +309,15 @@ __device__ __forceinline__ void gks_point(const GState<T>& L, const GState<T>& R
 // summed across them; the centre part (one state) is scalar.  The u < 0 half-space moments
 // follow the same recurrence as the u > 0 ones (0.5 erfc(+sqrt(lambda) u) and the opposite sign
 // of the boundary term), not 1 - up and uw - up.
+// alpha (not null): the DF indicator contribution of the point (Calculate_alpha_k,
+// src/reconstruction.cpp:1463-1476) from the lanes' (rho, u, v, lambda): the pressure is
+// beta rho / lambda and the squared sound speed gamma beta / lambda, beta = (gamma - 1)(K + 2) / 4,
+// so |pl - pr| / pl + |pl - pr| / pr = |ql - qr| (1 / ql + 1 / qr) with q = rho / lambda, and
+// 1 / c = sqrt(lambda / (gamma beta)); the squared Mach differences add normal first (dir 0) or
+// tangential first (dir 1), as the reference's y faces do after the rotation back.
 __device__ __forceinline__ void gks_point_lr(const GState<float>& L, const GState<float>& R, float dt, float K,
-                                             float c1, float c2, float* fo, float* dfo) {
+                                             float c1, float c2, float* fo, float* dfo, float gamma = 0.0f,
+                                             int dir = 0, float* alpha = nullptr) {
     const F2 Kp(K);
     const GasK<F2> gk(Kp);
     F2 w[4], sx[4], sy[4], ps[4];
@@ -328,6 +335,15 @@ __device__ __forceinline__ void gks_point_lr(const GState<float>& L, const GStat
         constexpr double pi = 3.14159265358979323846;
         Mom<F2> m;   // up[] holds the lanes' half-space moments
         const F2 u = ps[1], lam = ps[3], ol = F2(1.0f) / lam;
+        if (alpha) {
+            const F2 q = r * ol, iq = F2(1.0f) / q;
+            const float igb = 4.0f / (gamma * (gamma - 1.0f) * (K + 2.0f));
+            const F2 ic = sqrt(F2(lam * F2(igb)));
+            const F2 mn = u * ic, mt = ps[2] * ic;
+            const float dn = mn.v.x - mn.v.y, dtg = mt.v.x - mt.v.y;
+            const float a = fabsf(q.v.x - q.v.y) * (iq.v.x + iq.v.y);
+            *alpha = dir == 0 ? a + dn * dn + dtg * dtg : a + dtg * dtg + dn * dn;
+        }
         m.whole(u, ps[2], ol, Kp);
         m.up[0] = F2(0.5f) * ferfc(F2(F2(-1.0f, 1.0f) * sqrt(lam) * u));
         m.up[1] = u * m.up[0] + F2(0.5f, -0.5f) * (fexp(-F2(lam * u * u)) / sqrt(F2(pi) * lam));

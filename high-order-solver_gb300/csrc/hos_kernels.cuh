@@ -545,8 +545,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 for (int v = 0; v < 4; ++v) { outv[side][v] = var[v]; outv[side][4 + v] = der[v]; }
             }
         }
-        // positivity fallback couples the two faces of the cell (src/reconstruction.cpp:1843-1858)
-        if (needs_order_reduction(outv[1], K) || needs_order_reduction(outv[0], K)) {
+        // positivity fallback couples the two faces of the cell (src/reconstruction.cpp:1843-1858);
+        // a linear reconstruction the check accepted has passed it, and a first-order one is the
+        // fallback's own result
+        if (!lin && (needs_order_reduction(outv[1], K) || needs_order_reduction(outv[0], K))) {
 #pragma unroll
             for (int side = 0; side < 2; ++side)
 #pragma unroll
@@ -754,10 +756,11 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                     res[ig][4 + v] = x;
                 }
             }
-            // positivity fallback per Gauss point (src/reconstruction.cpp:2764-2791)
+            // positivity fallback per Gauss point (src/reconstruction.cpp:2764-2791); not for a
+            // linear or first-order result (checked, or the fallback's own values)
 #pragma unroll
             for (int ig = 0; ig < GP; ++ig) {
-                if (needs_order_reduction(res[ig], K)) {
+                if (!lin && needs_order_reduction(res[ig], K)) {
 #pragma unroll
                     for (int v = 0; v < 4; ++v) {
                         res[ig][v] = w0[v];
@@ -790,6 +793,8 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             R.w[v] = sr[v]; R.dx[v] = sr[4 + v]; R.dy[v] = sr[8 + v];
         }
         T f[4], d[4];
+        float alk = 0.0f;   // FP32 GKS: the DF indicator contribution from its lanes
+        bool alk_set = false;
         if (geo.flux == 1) {
             lf_point<T>(L.w, R.w, dt, gamma, f);
             // the Navier-Stokes instantiation adds LF2D's viscous term
@@ -801,11 +806,14 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             // of its code
             if constexpr (NS)
                 gks_point_ns<T>(L, R, dt, K, NsParam<T>{T(geo.c2), T(geo.mu), T(geo.nu), T(geo.prandtl_coef)}, f, d);
-            else if constexpr (std::is_same<T, float>::value)
-                // FP32: the left and right states share the paired FP32 lanes
-                gks_point_lr(L, R, dt, K, fpar[5], fpar[6], f, d);
-            else
+            else if constexpr (std::is_same<T, float>::value) {
+                // FP32: the left and right states share the paired FP32 lanes, and the DF
+                // indicator's contribution comes from the same lanes
+                gks_point_lr(L, R, dt, K, fpar[5], fpar[6], f, d, gamma, DIR, &alk);
+                alk_set = true;
+            } else {
                 gks_point<T>(L, R, dt, K, T(geo.c1), T(geo.c2), f, d);
+            }
             if (geo.integrator == 1) {   // S1O1 takes the dt integral F0 = f + d / 2 alone
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
@@ -817,7 +825,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         T* o = flux + (fidx * GP + ig) * 9;
 #pragma unroll
         for (int v = 0; v < 4; ++v) { o[v] = f[v]; o[4 + v] = d[v]; }
-        o[8] = alpha_k<T, DIR>(L.w, R.w, gamma);
+        o[8] = alk_set ? alk : alpha_k<T, DIR>(L.w, R.w, gamma);
     }
     __syncthreads();
 
