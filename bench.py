@@ -334,10 +334,15 @@ def endtime2d_leg(gate, rep, n=N_CELLS, tstop=0.25):
         if gated:
             st = s.gate_stats()
             cells = max(1, st["cells_x"] + st["cells_y"])
+            fc = s.gate_audit_check()
             runs[name]["gate"] = {"linear_path_fraction": (st["smooth_x"] + st["smooth_y"]) / cells,
                                   "audited": st["audited"], "audit_false_negatives": st["false_neg"],
                                   "audit_false_negative_rate": st["false_neg"] / max(1, st["audited"]),
-                                  "aposteriori_rejections": st["fallback"]}
+                                  "aposteriori_rejections": st["fallback"],
+                                  # what the check did with the audited false negatives' linear
+                                  # reconstructions: accepted (wrongly) or sent back to WENO-AO
+                                  "false_negative_linear_reconstructions": fc["fn_linear"],
+                                  "false_negative_accepted_by_check": fc["fn_linear_accepted"]}
         s.close()
 
     def rel(a, b, norm):

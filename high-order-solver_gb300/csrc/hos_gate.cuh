@@ -54,6 +54,9 @@ struct Stats {
     unsigned long long false_neg;     // of those, weights farther than GATE_EPS from linear
     unsigned long long samples;       // training samples written
     unsigned long long fallback;      // linear results rejected by the a-posteriori check
+    // linear reconstructions in cell-directions an audit found not smooth (flag bits 2 + d):
+    // tried, and accepted by the a-posteriori check
+    unsigned long long fn_linear, fn_linear_accepted;
 };
 
 // ---------------- features ----------------
@@ -594,7 +597,10 @@ __device__ __forceinline__ void gate_tile(const GateArgs& a, const Geometry& geo
                 const float d = dir == 0 ? weight_distance<ORDER, 0>(a.W, plane, c, stride, gamma, geo.characteristic)
                                          : weight_distance<ORDER, 1>(a.W, plane, c, stride, gamma, geo.characteristic);
                 atomicAdd(&a.stats->audited, 1ull);
-                if (d > GATE_EPS) atomicAdd(&a.stats->false_neg, 1ull);
+                if (d > GATE_EPS) {
+                    atomicAdd(&a.stats->false_neg, 1ull);
+                    flag |= (unsigned char)(4u << dir);   // the face kernels count what the check does with it
+                }
             }
             const unsigned fits_mask = __ballot_sync(0xffffffffu, fits);
             const unsigned smooth_mask = __ballot_sync(0xffffffffu, smooth);

@@ -156,8 +156,9 @@ struct FaceArgs {
     double* FA;         // face DF indicator [nf]
     const StepCtl* ctl;
     int stage;
-    // learned gate (FP32 path only): per-cell flags, bit 0 x-smooth, bit 1 y-smooth; counter
-    // of linear results the a-posteriori check rejected
+    // learned gate (FP32 path only): per-cell flags, bit 0 x-smooth, bit 1 y-smooth, bits 2 / 3
+    // x / y audited and found not smooth; counter of linear results the a-posteriori check
+    // rejected
     const unsigned char* gate;
     unsigned long long* fallback;
     // time-marching methods other than S2O4: Gauss-integrated flux and its time derivative of
@@ -169,6 +170,9 @@ struct FaceArgs {
     const float* W32;
     const float* AN32;
     const float* AT32;
+    // gated: counters of the linear reconstructions in audited not-smooth cell-directions, tried
+    // and accepted by the a-posteriori check (null: not counted)
+    unsigned long long* fn_check = nullptr;
 };
 
 // A tile is TN faces along the normal by TT along the tangent, handled by one CTA of 256
@@ -307,7 +311,14 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     const int tid = threadIdx.x;
     if (!a.ctl->active) return;
     __shared__ unsigned rejected;   // GATED: linear results the check rejected in this tile
-    if constexpr (GATED) if (tid == 0) rejected = 0;
+    // GATED: linear reconstructions in cell-directions the gate's audit found not smooth, tried
+    // and accepted by the check
+    __shared__ unsigned fn_seen[2];
+    if constexpr (GATED)
+        if (tid == 0) {
+            rejected = 0;
+            fn_seen[0] = fn_seen[1] = 0;
+        }
     // FP32: the launch's FP64 parameters narrowed once per tile (a conversion from FP64 runs on
     // GB300's narrow FP64 pipe; per thread they would cost as much as the stage combination)
     __shared__ float fpar[7];
@@ -481,6 +492,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             lin = linear_ok<T>(outv[0], st[r - 1], st[r], st[r + 1], K, slack) &&
                   linear_ok<T>(outv[1], st[r - 1], st[r], st[r + 1], K, slack);
             if (!lin) atomicAdd(&rejected, 1u);
+            if ((gfl[nl * TL + tl] >> (2 + DIR)) & 1) {
+                atomicAdd(&fn_seen[0], 1u);
+                if (lin) atomicAdd(&fn_seen[1], 1u);
+            }
         }
         // the DF factors and the characteristic bases' primitives, only for cells that take the
         // WENO-AO path
@@ -630,6 +645,10 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                 for (int ig = 0; ig < GP; ++ig)
                     lin = lin && linear_ok<T>(res[ig], line(r - 1, side), w0, line(r + 1, side), K, T(geo.gate_slack));
                 if (!lin) atomicAdd(&rejected, 1u);
+                if ((gfl[(fn + side) * TL + tc] >> (3 - DIR)) & 1) {
+                    atomicAdd(&fn_seen[0], 1u);
+                    if (lin) atomicAdd(&fn_seen[1], 1u);
+                }
             }
             // the DF factors, only for faces that take the WENO-AO path
             T df[NW];
@@ -776,7 +795,14 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
     }
     __syncthreads();
 
-    if constexpr (GATED) if (tid == 0 && rejected) atomicAdd(a.fallback, (unsigned long long)rejected);
+    if constexpr (GATED)
+        if (tid == 0) {
+            if (rejected) atomicAdd(a.fallback, (unsigned long long)rejected);
+            if (fn_seen[0] && a.fn_check) {
+                atomicAdd(a.fn_check, (unsigned long long)fn_seen[0]);
+                atomicAdd(a.fn_check + 1, (unsigned long long)fn_seen[1]);
+            }
+        }
 
     // ---------------- phase 3: GKS flux, one (face, Gauss point) per thread ----------------
     const T dt = sizeof(T) == 4 ? T(fpar[4]) : T(a.ctl->dt);

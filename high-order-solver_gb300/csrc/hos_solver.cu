@@ -408,6 +408,7 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
             return cuda_fail(e, "gate");
         ax.gate = ay.gate = s->gflags;
         ax.fallback = ay.fallback = &s->gstats->fallback;
+        ax.fn_check = ay.fn_check = &s->gstats->fn_linear;
     } else if (s->gated) {
         const size_t n = s->ncell;
         dilate_flags_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s->stream>>>(
@@ -884,6 +885,19 @@ int hos2d_gate_stats(hos_solver2d* s, unsigned long long* stats, int reset) {
     const unsigned long long v[8] = {st.cells[0], st.cells[1], st.smooth[0], st.smooth[1], st.audited, st.false_neg,
                                      st.fallback, st.samples};
     std::memcpy(stats, v, sizeof v);
+    return HOS_OK;
+}
+
+int hos2d_gate_audit_check(hos_solver2d* s, unsigned long long* out) {
+    if (!s || !out) return fail(HOS_E_ARG, "null argument");
+    out[0] = out[1] = 0;
+    if (!s->gstats) return HOS_OK;
+    gate::Stats st;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, s->gstats, sizeof st, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "gate_audit_check");
+    out[0] = st.fn_linear;
+    out[1] = st.fn_linear_accepted;
     return HOS_OK;
 }
 

@@ -115,6 +115,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     lib.hos_batch2d_set_reconstruction.argtypes = [vp, ctypes.c_int]
     lib.hos_batch2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
     lib.hos2d_gate_stats.argtypes = [vp, _ULL, ctypes.c_int]
+    lib.hos2d_gate_audit_check.argtypes = [vp, _ULL]
     lib.hos3d_create.argtypes = [ctypes.POINTER(Params3D), ctypes.c_int, ctypes.POINTER(vp)]
     lib.hos3d_destroy.argtypes = [vp]
     lib.hos3d_set_state.argtypes = [vp, _DP, _DP]
@@ -276,6 +277,13 @@ class Solver2D:
         _check(self._lib.hos2d_gate_stats(self._h, v, 1 if reset else 0))
         keys = ("cells_x", "cells_y", "smooth_x", "smooth_y", "audited", "false_neg", "fallback", "unused")
         return dict(zip(keys, (int(x) for x in v)))
+
+    def gate_audit_check(self) -> dict:
+        """Linear reconstructions in cell-directions an audit found not smooth, and how many of
+        them the a-posteriori check accepted (hos2d_gate_audit_check)."""
+        v = (ctypes.c_ulonglong * 2)()
+        _check(self._lib.hos2d_gate_audit_check(self._h, v))
+        return {"fn_linear": int(v[0]), "fn_linear_accepted": int(v[1])}
 
     def run(self, tstop: float, max_steps: int = 10**9, graph: bool = True, check_every: int = 50) -> int:
         """Advance until t >= tstop (the driver's while loop); returns steps taken."""

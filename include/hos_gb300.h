@@ -257,6 +257,12 @@ int hos2d_set_gate_reuse(hos_solver2d* s, int reuse);
 /* counters since the last reset: cells gated x, y; predicted smooth x, y; audited; audited but
  * not smooth (false negatives of the gate); linear results rejected; (unused) */
 int hos2d_gate_stats(hos_solver2d* s, unsigned long long* stats, int reset);
+/* what the a-posteriori check did with the gate's errors: out[0] linear reconstructions in
+ * cell-directions an audit found not smooth (predicted smooth, full weights farther than the
+ * label's tolerance from the linear ones), out[1] how many of them the check accepted (the rest
+ * fell back to WENO-AO); counted at the stages where the network runs, reset with
+ * hos2d_gate_stats.  No counterpart in the reference. */
+int hos2d_gate_audit_check(hos_solver2d* s, unsigned long long* out);
 
 /* ---- 1D path --------------------------------------------------------------------------
  * The reference's 1D drivers (SodTubeProblem, accuracy_sinwave_1d, src/1Dproblem.cpp:3-149,
