@@ -441,11 +441,11 @@ const char* hos_batch2d_last_error(void);
  * HOS_BC_PERIODIC, HOS_BC_REFLECT and HOS_BC_INFLOW.  Other settings (other time marching, LF,
  * use_df = 0, wedge and no-slip sides), problems with nodex or nodey above
  * HOS_STATIC_MAX_NODE and ghost above HOS_STATIC_MAX_GHOST are rejected with HOS_E_CONFIG.
- * Each call synchronises with its stream, so no call can be captured into a CUDA graph; the
- * first call on a device also sets up that device (looks up the array's address).  All calls
- * share the one array and it keeps the last call's
- * contents, so calls that overlap on the GPU (other streams, other host threads) race:
- * serialise them per device.  Errors are described by hos_static_last_error(). */
+ * Each call waits for its stream to finish before it returns.  The first call on a device
+ * also sets up that device (looks up the array's address): make it before any stream
+ * capture.  All calls share the one array and it keeps the last call's contents, so calls
+ * that overlap on the GPU (other streams, other host threads) race: serialise them per
+ * device.  Errors are described by hos_static_last_error(). */
 #define HOS_STATIC_MAX_NODE 256
 #define HOS_STATIC_MAX_GHOST 5
 int hos2d_step_static(const hos_params2d* params, int precision, double* d_W, double* d_alpha_x,
