@@ -130,6 +130,31 @@ __device__ __forceinline__ double f32_to_f64(float x) {
     return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
 }
 
+// FP64 -> FP32 rounding to nearest, ties to even, on the integer pipes (the bit pattern's high
+// and low words in, the FP32 bit pattern out), for kernels whose bound is the FP64 pipe, which
+// also runs the conversion instruction: IEEE rounding with FP32 subnormal results flushed to
+// signed zero, as the -ftz build's float(x) gives for every result in FP32's normal range and
+// for zero and infinity; NaNs give the canonical NaN.  The double's exponent field sits in bits
+// 30..20 of hi: rebiased from 1023 to 127 (896 << 20 = 0x38000000) and shifted left by 3
+// together with the top 3 bits of lo, it lands in the float's place beside 20 + 3 significand
+// bits; the 29 dropped bits round, and a carry out of the significand moves into the exponent
+// (up to infinity) by itself.
+__host__ __device__ __forceinline__ unsigned f64_bits_to_f32_bits(unsigned hi, unsigned lo) {
+    const unsigned s = hi & 0x80000000u, a = hi & 0x7fffffffu;
+    if (a - 0x38100000u < 0x0fe00000u) {   // exponent field 897..1150: a normal FP32 before rounding
+        const unsigned f = ((a - 0x38000000u) << 3) | (lo >> 29);
+        const unsigned up = (lo & 0x1fffffffu) + ((lo >> 29) & 1u) > 0x10000000u;
+        return s | (f + up);
+    }
+    // below 2^-126: zero, unless it rounds up to 2^-126 (from 2^-126 - 2^-150 on, ties to even)
+    if (a < 0x38100000u) return a == 0x380fffffu && lo >= 0xe0000000u ? s | 0x00800000u : s;
+    if (a > 0x7ff00000u || (a == 0x7ff00000u && lo != 0u)) return 0x7fffffffu;   // NaN
+    return s | 0x7f800000u;                                                  // 2^128 and above
+}
+__device__ __forceinline__ float f64_to_f32(double x) {
+    return __uint_as_float(f64_bits_to_f32_bits((unsigned)__double2hiint(x), (unsigned)__double2loint(x)));
+}
+
 // the sum of the two lanes
 __device__ __forceinline__ float hsum(F2 a) { return a.v.x + a.v.y; }
 

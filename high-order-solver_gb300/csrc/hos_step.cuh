@@ -178,7 +178,8 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             else
                 w[v] = old + rate;
             a.W[v * plane + c] = w[v];
-            if (a.W32) a.W32[v * plane32 + cm] = (float)w[v];
+            // the mirror's rounding on the integer pipes (f64_to_f32: the same values as float())
+            if (a.W32) a.W32[v * plane32 + cm] = f64_to_f32(w[v]);
         }
         const int jend = nodex < nodey ? nodex : nodey;
         // Update_alpha runs only under is_using_df_factor (src/2Dproblem.cpp:154)
@@ -187,8 +188,8 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             a.AX[c] = ax;
             a.AY[c] = ay;
             if (a.A32) {
-                a.A32[cm] = (float)ax;
-                a.A32[plane32 + cm] = (float)ay;
+                a.A32[cm] = f64_to_f32(ax);
+                a.A32[plane32 + cm] = f64_to_f32(ay);
             }
         }
         if (a.W32 && a.stage != cfl_stage(geo)) {
@@ -205,7 +206,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         pr[1] = w[1] * ir;
         pr[2] = w[2] * ir;
         pr[3] = (geo.gamma - 1.0) * (w[3] - 0.5 * (w[1] * pr[1] + w[2] * pr[2]));
-        if (pr[0] < 0 || pr[3] < 0 || isnan(pr[0]) || isnan(pr[3])) bad = 1;
+        if (!(pr[0] >= 0.0) || !(pr[3] >= 0.0)) bad = 1;   // negative or NaN
         if (a.stage == cfl_stage(geo)) {
             // the reference's Get_CFL reads the primitives converted at the start of the last
             // stage: the new state of stage stages - 2, or the step's starting state for
@@ -254,24 +255,30 @@ __device__ __forceinline__ double cfl_of_speed(const Geometry& geo, double smax)
 }
 
 // block reduction of the cells' signal speeds (update_one) and status bits into one problem's
-// control word: the largest speed, converted to the block's CFL candidate by one thread
+// control word: the largest speed, converted to the block's CFL candidate by one thread.  A
+// speed is -1 (no candidate), +0 or a positive finite double, and over these values the bit
+// patterns read as signed 64-bit integers order as the doubles do, so the maximum is taken on
+// the integer pipes (the update's bound is the FP64 pipe).
 template <bool REF = false>
 __device__ __forceinline__ void reduce_block_speed(double spd, unsigned int bad, StepCtl* ctl, bool do_cfl,
                                                    const Geometry& geo) {
+    long long sk = __double_as_longlong(spd);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        spd = fmax(spd, __shfl_xor_sync(0xffffffffu, spd, o));
+        const long long other = __shfl_xor_sync(0xffffffffu, sk, o);
+        sk = other > sk ? other : sk;
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
-    __shared__ double sc[8];
+    __shared__ long long sc[8];
     __shared__ unsigned int sb[8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { sc[wid] = spd; sb[wid] = bad; }
+    if (lane == 0) { sc[wid] = sk; sb[wid] = bad; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double m = sc[0];
+        long long mk = sc[0];
         unsigned int b = sb[0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m = fmax(m, sc[k]); b |= sb[k]; }
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { mk = sc[k] > mk ? sc[k] : mk; b |= sb[k]; }
+        const double m = __longlong_as_double(mk);
         const double cand = cfl_of_speed<REF>(geo, m);
         if (do_cfl && cand < 1e300) atomic_min_pos(&ctl->cfl_bits, cand);
         if (b) atomicOr(&ctl->status, 1u);
