@@ -41,6 +41,10 @@ __global__ void bc_batch_kernel(const Prob* __restrict__ probs) {
         bc_fill_one(pr->W, geo, pr->bc, pr->ctl, e, pr->W32);
 }
 
+// every problem of a batch runs plain S2O4 (hos_batch2d_create): one instantiation per stage kind
+// (update_one's KIND: 1 at stage 0, which gives the CFL candidates; 0 at stage 1 of an FP32
+// batch, whose problems all have the FP32 mirror; -1, the generic form, at stage 1 of an FP64 batch)
+template <int KIND>
 __global__ void __launch_bounds__(256) update_batch_kernel(const Prob* __restrict__ probs, int stage) {
     const Prob* pr = probs + blockIdx.y;
     if (!pr->ctl->active) return;
@@ -48,16 +52,18 @@ __global__ void __launch_bounds__(256) update_batch_kernel(const Prob* __restric
     float* A32 = pr->W32 ? pr->W32 + 4 * (size_t)geo.nx * mirror_pitch(geo.ny) : nullptr;
     UpdateArgs a{pr->W, pr->Wold, pr->AX, pr->AY, pr->FXx, pr->FXy, pr->FAx, pr->FAy, pr->ctl, stage, pr->W32, A32};
     const int n = geo.nodex * geo.nodey;
-    double smax = -1.0;
+    // the largest speed on the bit patterns (-1, +0 and positive speeds order as signed integers)
+    long long smax = __double_as_longlong(-1.0);
     unsigned int bad = 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         double c;
         unsigned int b;
-        update_one(a, geo, base + threadIdx.x, c, b);
-        smax = fmax(smax, c);
+        update_one<false, KIND, (KIND >= 0)>(a, geo, base + threadIdx.x, c, b);
+        const long long ck = __double_as_longlong(c);
+        smax = ck > smax ? ck : smax;
         bad |= b;
     }
-    reduce_block_speed(smax, bad, pr->ctl, stage == cfl_stage(geo), geo);
+    reduce_block_speed(__longlong_as_double(smax), bad, pr->ctl, stage == cfl_stage(geo), geo);
 }
 
 // step prologue for every problem (one block); *counter is the batch step index
@@ -195,7 +201,13 @@ int enqueue_batch_step(hos_batch2d* b) {
         }
         if ((e = launch_faces(b, 0, stage)) != cudaSuccess) return failb(HOS_E_CUDA, std::string("face x: ") + cudaGetErrorString(e));
         if ((e = launch_faces(b, 1, stage)) != cudaSuccess) return failb(HOS_E_CUDA, std::string("face y: ") + cudaGetErrorString(e));
-        update_batch_kernel<<<dim3(std::min(maxc, 256), b->count), 256, 0, b->stream>>>(b->probs, stage);
+        const dim3 ugrid(std::min(maxc, 256), b->count);
+        if (stage == 0)
+            update_batch_kernel<1><<<ugrid, 256, 0, b->stream>>>(b->probs, stage);
+        else if (b->arena32)
+            update_batch_kernel<0><<<ugrid, 256, 0, b->stream>>>(b->probs, stage);
+        else
+            update_batch_kernel<-1><<<ugrid, 256, 0, b->stream>>>(b->probs, stage);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return failb(HOS_E_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     return HOS_OK;

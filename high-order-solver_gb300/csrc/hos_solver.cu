@@ -55,13 +55,16 @@ __global__ void __launch_bounds__(256) update_kernel(UpdateArgs a, Geometry geo)
     update_one(a, geo, blockIdx.x * blockDim.x + threadIdx.x, spd, bad);
     reduce_block_speed(spd, bad, a.ctl, a.stage == cfl_stage(geo), geo);
 }
-// the same for fluxes stored per unit cell width (Geometry::scaled_flux, plain S2O4)
+// the same for fluxes stored per unit cell width (Geometry::scaled_flux, plain S2O4, the FP32
+// mirror present), one instantiation per stage kind (update_one's KIND: 1 at stage 0, which
+// gives the CFL candidates, 0 at stage 1)
+template <int KIND>
 __global__ void __launch_bounds__(256) update_kernel_scaled(UpdateArgs a, Geometry geo) {
     if (!a.ctl->active) return;
     double spd;
     unsigned int bad;
-    update_one<true>(a, geo, blockIdx.x * blockDim.x + threadIdx.x, spd, bad);
-    reduce_block_speed(spd, bad, a.ctl, a.stage == cfl_stage(geo), geo);
+    update_one<true, KIND>(a, geo, blockIdx.x * blockDim.x + threadIdx.x, spd, bad);
+    reduce_block_speed(spd, bad, a.ctl, KIND == 1, geo);
 }
 
 // CFL candidates from a primitive state (the initial data's primvar at step 0)
@@ -426,9 +429,12 @@ int enqueue_stage(hos_solver2d* s, int stage, cudaEvent_t* ev = nullptr) {
     if (e != cudaSuccess) return cuda_fail(e, "face_kernel");
     UpdateArgs ua{s->W, s->Wold, s->AX, s->AY, s->FXx, s->FXy, s->FAx, s->FAy, s->ctl, stage, s->W32, s->A32};
     const int n = geo.nodex * geo.nodey;
-    if (geo.scaled_flux && geo.integrator == HOS_INT_S2O4 && !geo.source)
-        update_kernel_scaled<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
-    else
+    if (geo.scaled_flux && geo.integrator == HOS_INT_S2O4 && !geo.source) {   // FP32 solvers: W32 set
+        if (stage == cfl_stage(geo))
+            update_kernel_scaled<1><<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
+        else
+            update_kernel_scaled<0><<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
+    } else
         update_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(ua, geo);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "update");
     mark(4);

@@ -108,7 +108,7 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* addr, double 
 }
 
 // the stage whose update produces the next step's CFL candidates
-__device__ __forceinline__ int cfl_stage(const Geometry& geo) { return geo.stages >= 2 ? geo.stages - 2 : 0; }
+__host__ __device__ __forceinline__ int cfl_stage(const Geometry& geo) { return geo.stages >= 2 ? geo.stages - 2 : 0; }
 
 // a cell's signal speed |u| + c for the CFL reduction; one that is not finite gives no candidate
 // in Dtx (its dt is not > 0), as 0 does in cfl_of_speed (dt = inf)
@@ -119,7 +119,14 @@ __device__ __forceinline__ double signal_speed(double tmp) { return tmp <= 1.797
 // falls monotonically with the speed, so the block converts its largest speed once
 // (cfl_of_speed) and gets the same minimum.
 // SCALED: the fluxes are stored per unit cell width (Geometry::scaled_flux; plain S2O4 only).
-template <bool SCALED = false>
+// PLAIN: plain S2O4 without the source term (the scaled update, the batches), so the RK3 and
+// source forms are not compiled in.  KIND: the tail the update runs, when the launch
+// knows it -- 1 the stage that gives the CFL candidates (primitives, blow-up test, signal speed),
+// 0 a stage without candidates of a solver with the FP32 mirror (the division-free positivity
+// test), -1 decided per launch from a.stage.  The compiler if-converts short uniform branches, and
+// predicated-off FP64 instructions still take the FP64 pipe that bounds this kernel, so the
+// forms a launch does not run are left out at compile time.
+template <bool SCALED = false, int KIND = -1, bool PLAIN = SCALED>
 __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& geo, int idx, double& spd,
                                            unsigned int& bad) {
     const int nodex = geo.nodex, nodey = geo.nodey, g = geo.g, ny = geo.ny;
@@ -138,12 +145,13 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         // the FP64 pipe is the update's bound: the flux balance
         // (dx (F_down - F_up) + dy (F_left - F_right)) / (dx dy) is taken as two differences
         // scaled by 1 / dy and 1 / dx (precomputed), not as four products and a division
+        const bool src = !PLAIN && geo.source, rk3 = !PLAIN && geo.integrator == 4;
         double w[4], w0[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             // the state the stage started from: needed at stage 0 (snapshot, and the CFL of
             // one-stage methods) and by RK3's state combination
-            const bool need_cur = a.stage == 0 || geo.integrator == 4 || geo.source;
+            const bool need_cur = a.stage == 0 || rk3 || src;
             const double cur = need_cur ? a.W[v * plane + c] : 0.0;
             double old;
             if (a.stage == 0) {
@@ -159,7 +167,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
             else
                 rate = (a.FXy[v * nfy + fd] - a.FXy[v * nfy + fu]) * geo.idy +
                        (a.FXx[v * nfx + fl] - a.FXx[v * nfx + fr]) * geo.idx;
-            if (geo.source) {
+            if (src) {
                 // Update_with_source under S2O4 (src/time_advance.cpp:534-704): stage 0 takes
                 // W_old + dt (L + S), S = (0, 0, rho, rho v) of the stage's state; stage 1
                 // leaves the state
@@ -171,9 +179,9 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 } else {
                     w[v] = cur;
                 }
-            } else if (geo.integrator == 4 && a.stage == 1)        // RK3 (Update_with_gauss_RK3, :511-526)
+            } else if (rk3 && a.stage == 1)        // RK3 (Update_with_gauss_RK3, :511-526)
                 w[v] = 0.75 * old + 0.25 * cur + rate;
-            else if (geo.integrator == 4 && a.stage == 2)
+            else if (rk3 && a.stage == 2)
                 w[v] = 1.0 / 3.0 * old + 2.0 / 3.0 * cur + rate;
             else
                 w[v] = old + rate;
@@ -192,7 +200,7 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
                 a.A32[plane32 + cm] = f64_to_f32(ay);
             }
         }
-        if (a.W32 && a.stage != cfl_stage(geo)) {
+        if (KIND == 0 || (KIND < 0 && a.W32 && a.stage != cfl_stage(geo))) {
             // FP32 solvers, a stage without CFL candidates: Convar_to_Primvar's sign tests without
             // its division (the FP64 pipe bounds this kernel): rho > 0 and
             // 2 rho (rho E) - |rho u|^2 >= 0, which a NaN fails
@@ -207,12 +215,12 @@ __device__ __forceinline__ void update_one(const UpdateArgs& a, const Geometry& 
         pr[2] = w[2] * ir;
         pr[3] = (geo.gamma - 1.0) * (w[3] - 0.5 * (w[1] * pr[1] + w[2] * pr[2]));
         if (!(pr[0] >= 0.0) || !(pr[3] >= 0.0)) bad = 1;   // negative or NaN
-        if (a.stage == cfl_stage(geo)) {
+        if (KIND == 1 || (KIND < 0 && a.stage == cfl_stage(geo))) {
             // the reference's Get_CFL reads the primitives converted at the start of the last
             // stage: the new state of stage stages - 2, or the step's starting state for
             // one-stage methods
             double ir2 = ir;
-            if (geo.stages == 1) {
+            if (!PLAIN && geo.stages == 1) {
                 ir2 = 1.0 / w0[0];
                 pr[0] = w0[0];
                 pr[1] = w0[1] * ir2;
