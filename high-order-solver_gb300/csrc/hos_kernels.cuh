@@ -857,22 +857,28 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
 
     // ---------------- phase 4: Gauss quadrature, S2O4 stage combination, face DF indicator ----------------
     // the FP64 stage combination and the face's global reads and writes, from its Gauss-quadrature
-    // sums of f and f_t (in the compute type) and of the DF contributions
-    auto finish = [&](int fn, int ft, const T* Fq, const T* Dq, T asum) {
+    // sums of f and f_t (in the compute type) and of the DF contributions.  stg: the S2O4 stage
+    // as a compile-time constant (std::integral_constant) where the FP32 kernels run plain S2O4,
+    // -1 where the stage and the time marching are read at run time.  With the stage fixed, the
+    // other stage's FP64 operations are not compiled in: the compiler if-converts short uniform
+    // branches, and an FP64 operation predicated off in every lane still takes its FP64-pipe slot.
+    auto finish = [&](auto stg, int fn, int ft, const T* Fq, const T* Dq, T asum) {
+        constexpr int SG = decltype(stg)::value;
         const int facen = N0 + fn, facet = T0 + ft;
         const size_t nf = DIR == 0 ? (size_t)(geo.nodex + 1) * geo.nodey : (size_t)geo.nodex * (geo.nodey + 1);
         const size_t fi = DIR == 0 ? (size_t)facen * geo.nodey + facet : (size_t)facet * (geo.nodey + 1) + facen;
         double X[4], P[4];
-        const bool s2o4 = geo.integrator == 0;
+        const bool s2o4 = SG >= 0 || geo.integrator == 0;
+        const bool st0 = SG >= 0 ? SG == 0 : a.stage == 0;
         // FP32 kernels, plain S2O4: the FP64 pipe bounds this phase, so the conversions run on
         // the integer pipes (f32_to_f64, exact) and each result takes one FP64 operation:
         // X0 = 0.5 F + D / 8 (D / 8 exact in FP32), P0 = F + D / 6, X1 = P0 + D / 3
-        const bool fast64 = sizeof(T) == 4 && s2o4 && !geo.source;
+        const bool fast64 = SG >= 0 || (sizeof(T) == 4 && s2o4 && !geo.source);
         const float sc = geo.scaled_flux ? float(hN) : 1.0f;
 #pragma unroll
         for (int v = 0; v < 4 && fast64; ++v) {
             const float fq = float(Fq[v]) * sc, dq = float(Dq[v]) * sc;
-            if (a.stage == 0) {
+            if (st0) {
                 const double F = f32_to_f64(fq);
                 X[v] = fma(0.5, F, f32_to_f64(0.125f * dq));
                 P[v] = fma(1.0 / 6.0, f32_to_f64(dq), F);
@@ -889,7 +895,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
                     // Update_with_source: the Gauss-weighted f of the stage itself
                     X[v] = F;
                     P[v] = 0.0;
-                } else if (a.stage == 0) {
+                } else if (st0) {
                     X[v] = 0.5 * F + (1.0 / 8.0) * D;
                     P[v] = 1.0 * F + (1.0 / 6.0) * D;
                 } else {
@@ -923,7 +929,7 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
             const float am = float(GP == 2 ? T(0.5) * asum : GP == 3 ? asum * T(1.0 / 3.0) : T(0.25) * asum);
             a.FA[fi] = am < 2.0f ? 0.0 : f32_to_f64(am);
         }
-        if (s2o4 && a.stage == 1 && !geo.source && !fast64) {
+        if (s2o4 && !st0 && !geo.source && !fast64) {
 #pragma unroll
             for (int v = 0; v < 4; ++v) X[v] = a.FP[v * nf + fi] + X[v];
         }
@@ -932,64 +938,77 @@ __device__ __forceinline__ void face_tile(const FaceArgs& a, const Geometry& geo
         if (DIR == 1) { Xg[1] = -X[2]; Xg[2] = X[1]; }
 #pragma unroll
         for (int v = 0; v < 4; ++v) a.FX[v * nf + fi] = Xg[v];
-        if (s2o4 && a.stage == 0) {
+        if (s2o4 && st0) {
 #pragma unroll
             for (int v = 0; v < 4; ++v) a.FP[v * nf + fi] = P[v];
         }
     };
-    // y faces lie along n in memory (fi = t (nodey + 1) + n) while the tile's threads run along t:
-    // their sums are staged in the Gauss-state region (free after phase 3), [9][TILE_T][TILE_N + 1]
-    // (the padding keeps both passes free of bank conflicts), and the combination runs with
-    // consecutive threads on consecutive faces of memory, so its global accesses coalesce
-    constexpr int SP = TILE_N + 1;
-    T* qst = gst;
+    auto phase4 = [&](auto stg) {
+        // y faces lie along n in memory (fi = t (nodey + 1) + n) while the tile's threads run along t:
+        // their sums are staged in the Gauss-state region (free after phase 3), [9][TILE_T][TILE_N + 1]
+        // (the padding keeps both passes free of bank conflicts), and the combination runs with
+        // consecutive threads on consecutive faces of memory, so its global accesses coalesce
+        constexpr int SP = TILE_N + 1;
+        T* qst = gst;
 #pragma unroll 1
-    for (int fidx = tid; fidx < TILE_N * TILE_T; fidx += FACE_THREADS) {
-        const int fn = fidx / TILE_T, ft = fidx % TILE_T;
-        if (N0 + fn > nodeN || T0 + ft >= nodeT) continue;
-        // Gauss quadrature of f and f_t over the face in the compute type; the S2O4 stage
-        // combination of the two time-integral moments is FP64
-        T Fq[4], Dq[4], asum = T(0.0);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) { Fq[v] = T(0.0); Dq[v] = T(0.0); }
-#pragma unroll
-        for (int ig = 0; ig < GP; ++ig) {
-            const T* o = flux + (fidx * GP + ig) * 9;
-            const T gw = T(gauss_weight<GP>(ig));
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                Fq[v] += gw * o[v];
-                Dq[v] += gw * o[4 + v];
-            }
-            asum += o[8];
-        }
-        if constexpr (DIR == 0) {
-            finish(fn, ft, Fq, Dq, asum);
-        } else {
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                qst[(v * TILE_T + ft) * SP + fn] = Fq[v];
-                qst[((4 + v) * TILE_T + ft) * SP + fn] = Dq[v];
-            }
-            qst[(8 * TILE_T + ft) * SP + fn] = asum;
-        }
-    }
-    if constexpr (DIR == 1) {
-        static_assert(9 * TILE_T * (TILE_N + 1) <= S::GSTATES, "the staged sums must fit the Gauss-state region");
-        __syncthreads();
-#pragma unroll 1
-        for (int fc = tid; fc < TILE_N * TILE_T; fc += FACE_THREADS) {
-            const int fn = fc % TILE_N, ft = fc / TILE_N;
+        for (int fidx = tid; fidx < TILE_N * TILE_T; fidx += FACE_THREADS) {
+            const int fn = fidx / TILE_T, ft = fidx % TILE_T;
             if (N0 + fn > nodeN || T0 + ft >= nodeT) continue;
-            T Fq[4], Dq[4];
+            // Gauss quadrature of f and f_t over the face in the compute type; the S2O4 stage
+            // combination of the two time-integral moments is FP64
+            T Fq[4], Dq[4], asum = T(0.0);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                Fq[v] = qst[(v * TILE_T + ft) * SP + fn];
-                Dq[v] = qst[((4 + v) * TILE_T + ft) * SP + fn];
+            for (int v = 0; v < 4; ++v) { Fq[v] = T(0.0); Dq[v] = T(0.0); }
+#pragma unroll
+            for (int ig = 0; ig < GP; ++ig) {
+                const T* o = flux + (fidx * GP + ig) * 9;
+                const T gw = T(gauss_weight<GP>(ig));
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    Fq[v] += gw * o[v];
+                    Dq[v] += gw * o[4 + v];
+                }
+                asum += o[8];
             }
-            finish(fn, ft, Fq, Dq, qst[(8 * TILE_T + ft) * SP + fn]);
+            if constexpr (DIR == 0) {
+                finish(stg, fn, ft, Fq, Dq, asum);
+            } else {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    qst[(v * TILE_T + ft) * SP + fn] = Fq[v];
+                    qst[((4 + v) * TILE_T + ft) * SP + fn] = Dq[v];
+                }
+                qst[(8 * TILE_T + ft) * SP + fn] = asum;
+            }
+        }
+        if constexpr (DIR == 1) {
+            static_assert(9 * TILE_T * (TILE_N + 1) <= S::GSTATES, "the staged sums must fit the Gauss-state region");
+            __syncthreads();
+#pragma unroll 1
+            for (int fc = tid; fc < TILE_N * TILE_T; fc += FACE_THREADS) {
+                const int fn = fc % TILE_N, ft = fc / TILE_N;
+                if (N0 + fn > nodeN || T0 + ft >= nodeT) continue;
+                T Fq[4], Dq[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    Fq[v] = qst[(v * TILE_T + ft) * SP + fn];
+                    Dq[v] = qst[((4 + v) * TILE_T + ft) * SP + fn];
+                }
+                finish(stg, fn, ft, Fq, Dq, qst[(8 * TILE_T + ft) * SP + fn]);
+            }
+        }
+    };
+    // FP32 kernels, plain S2O4: phase 4 compiled once per stage (finish's stg)
+    if constexpr (sizeof(T) == 4) {
+        if (geo.integrator == 0 && !geo.source) {
+            if (a.stage == 0)
+                phase4(std::integral_constant<int, 0>{});
+            else
+                phase4(std::integral_constant<int, 1>{});
+            return;
         }
     }
+    phase4(std::integral_constant<int, -1>{});
 }
 
 // Tile of the single-problem face kernels: 16 x 16 faces for WENO5/7 (256 faces: every thread
