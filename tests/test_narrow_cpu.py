@@ -83,3 +83,24 @@ def test_integer_pipe_narrowing_equals_ieee_rounding(tmp_path):
     assert r.returncode == 0, r.stdout
     n, bad = map(int, r.stdout.split()[-2:])
     assert bad == 0 and n > 10_000_000
+
+
+def test_speed_bit_patterns_order_as_doubles():
+    """The update kernels take the block's largest CFL signal speed on the speeds' bit patterns
+    read as signed 64-bit integers (reduce_block_speed in hos_step.cuh): a speed is -1 (a cell with
+    no candidate), +0 (a speed that was not finite) or a positive finite double, and over those
+    values the integer order must be the double order."""
+    import numpy as np
+
+    rng = np.random.default_rng(7)
+    pos = np.concatenate([rng.uniform(0.0, 10.0, 20000), 10.0 ** rng.uniform(-300, 300, 20000),
+                          [np.finfo(np.float64).tiny, 5e-324, np.finfo(np.float64).max, 1.0]])
+    vals = np.concatenate([[-1.0, 0.0], pos[pos > 0]])
+    bits = vals.view(np.int64)
+    order_d = np.argsort(vals, kind="stable")
+    order_i = np.argsort(bits, kind="stable")
+    assert np.array_equal(vals[order_d], vals[order_i])
+    # and the maximum of any subset agrees
+    for _ in range(200):
+        sub = rng.choice(vals.size, 256)
+        assert vals[sub].max() == vals[sub][np.argmax(bits[sub])]
